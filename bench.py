@@ -1,0 +1,300 @@
+"""Benchmark of the closure hot path on one GB300 (or N independent replicas).
+
+Headline workload (``--workload lookup``, the default): vector tabulated EOS
+lookup, 2^24 queries on a 256 x 256 NQT-log (rho, T) table sampled from the
+StiffGas model (a SpinerEOSDependsRhoT layout); per query T(rho, sie) by
+regula falsi on the table, then P and the bulk modulus (FillEos with
+T|P|bmod outputs). Inputs are seeded synthetic data (no public dataset).
+
+Secondary workloads, measured in the same run and reported under "pte":
+plain FP64 PTE closure of 65,536 two-material cells (IdealGas + StiffGas) and
+of 2^22 uneven cells with 2-5 materials from an 8-EOS pool.
+
+Timing: CUDA events on the launching stream around exactly --steps steps,
+after --warmup untimed steps, with a device synchronize on both sides. The
+lookup inputs (256 MB) are larger than L2 (129 MB). ``e2e`` is the same
+metric through the C ABI with the inputs copied from pinned host memory and
+the outputs read back inside the timed region.
+
+``--impl reference`` times the CPU implementation of the same path on the
+host cores (the oracle restatement, oracle/_build/libsgport.so, all threads).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "singularity-eos_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+N_LOOKUP = 1 << 24
+N_PTE2 = 65536
+N_PTE_BATCH = 1 << 22
+LOOKUP_BYTES_PER_QUERY = 16 + 24  # rho, sie in; T, P, bmod out (float64)
+Q_OUT = 8 | 4 | 32                # temperature | pressure | bulk modulus
+METRIC = "PTE mixed cells/s & EOS lookups/s, 1 GB300, batched+FP32-refined vs plain FP64"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.samples, self.proc, self.index = [], None, index
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 6:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4)
+                          if s[2 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": float(self.samples[0][1]) if self.samples else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def time_steps(fn, steps, warmup, stream):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(steps):
+        fn()
+    stop.record(stream)
+    torch.cuda.synchronize()
+    return start.elapsed_time(stop) / 1e3
+
+
+def lookup_inputs(table_dir):
+    from sgx import sp5lite
+    path = os.path.join(table_dir, "stiffgas.sp5")
+    sp5lite.stiffgas_table(path)
+    rho, sie = sp5lite.stiffgas_queries(N_LOOKUP, seed=2024)
+    return path, rho, sie
+
+
+def run_ours(args):
+    import torch
+    from sgx import lib, workloads as W
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    hbm, hbm_kind = peaks()
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        path, rho_h, sie_h = lookup_inputs(td)
+        tab = lib.spiner_eos(path, 1)
+        rho = torch.as_tensor(rho_h, device="cuda")
+        sie = torch.as_tensor(sie_h, device="cuda")
+        T, P, B = (torch.empty_like(rho) for _ in range(3))
+
+        def step():
+            lib.fill_eos(tab, rho, T, sie, P, None, B, Q_OUT, stream=stream)
+
+        barrier(world)
+        with ClockSampler(local) as clk:
+            dt = time_steps(step, args.steps, args.warmup, stream)
+        barrier(world)
+        dt = max_over_ranks(dt, world)
+        per_launch = dt / args.steps
+        value = world * N_LOOKUP * args.steps / dt
+        achieved = LOOKUP_BYTES_PER_QUERY * N_LOOKUP / per_launch / 1e9
+        out["clocks"] = clk.summary()
+        out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                           "frac": achieved / hbm, "traffic": None,
+                           "peak_kind": hbm_kind + " (burst copy)",
+                           "kernel": "fill_kernel (sgx_fp64.cu)"}
+        # e2e: host buffers in pinned memory, copies inside the timed region
+        rho_p = torch.as_tensor(rho_h).pin_memory()
+        sie_p = torch.as_tensor(sie_h).pin_memory()
+        outs_p = [torch.empty(N_LOOKUP, dtype=torch.float64).pin_memory() for _ in range(3)]
+
+        def e2e_step():
+            rho.copy_(rho_p, non_blocking=True)
+            sie.copy_(sie_p, non_blocking=True)
+            lib.fill_eos(tab, rho, T, sie, P, None, B, Q_OUT, stream=stream)
+            for h, d in zip(outs_p, (T, P, B)):
+                h.copy_(d, non_blocking=True)
+
+        e2e_steps = max(1, min(args.steps, 5))
+        barrier(world)
+        dte = max_over_ranks(time_steps(e2e_step, e2e_steps, 1, stream), world)
+        out["e2e"] = {"value": world * N_LOOKUP * e2e_steps / dte, "unit": "lookups/s",
+                      "h2d_bytes_per_step": 16 * N_LOOKUP, "d2h_bytes_per_step": 24 * N_LOOKUP}
+        lib.load().sgx_eos_finalize(__import__("ctypes").byref(tab))
+        out["value"], out["ms_per_step"] = value, per_launch * 1e3
+
+    # PTE secondary workloads (plain FP64)
+    pte = {}
+    for name, wl_fn, n in (("pte_2mat_65536", W.pte_two_material, N_PTE2),
+                           ("pte_batched_2^22", W.pte_batched, N_PTE_BATCH)):
+        wl = wl_fn(n, seed=77)
+        eos_list = [lib.make_eos(k, p) for k, p in wl["materials"]]
+        base = {k: torch.as_tensor(wl[k], device="cuda") for k in
+                ("rho", "vfrac", "sie", "temp", "press")}
+        work = {k: v.clone() for k, v in base.items()}
+        idx = torch.as_tensor(wl["eos_idx"], device="cuda") if wl["eos_idx"] is not None else None
+        vt = torch.as_tensor(wl["vfrac_tot"], device="cuda")
+        st = torch.as_tensor(wl["sie_tot"], device="cuda")
+        status = torch.empty(n * 16, dtype=torch.uint8, device="cuda")
+
+        def pstep():
+            for k in work:
+                work[k].copy_(base[k])
+            lib.pte_solve(lib.PTE_RHOT, eos_list, idx, vt, st, work["rho"], work["vfrac"],
+                          work["sie"], work["temp"], work["press"], status=status,
+                          stream=stream)
+
+        ps = max(1, min(args.steps, 5))
+        dt = max_over_ranks(time_steps(pstep, ps, 2, stream), world)
+        conv = lib.status_view(status)["converged"].mean()
+        pte[name] = {"cells_per_s": world * n * ps / dt, "ms_per_step": dt / ps * 1e3,
+                     "converged_frac": float(conv), "precision": "fp64"}
+    out["pte"] = pte
+    out["gpu_launches"] = args.steps
+    return out, world, rank
+
+
+def cpu_baseline(sample=1 << 21, min_seconds=3.0):
+    """The oracle restatement timed on the host cores over a bounded sample
+    of the lookup workload."""
+    import refbind as rb
+    port = rb.port()
+    with tempfile.TemporaryDirectory() as td:
+        from sgx import sp5lite
+        path = os.path.join(td, "stiffgas.sp5")
+        sp5lite.stiffgas_table(path)
+        rho, sie = sp5lite.stiffgas_queries(sample, seed=2024)
+        d = rb.eos_desc(rb.SPINER_RHOT, [], path=path, matid=1)
+        T, P, cv, B = (np.zeros(sample) for _ in range(4))
+        port.fill_eos(d, rho[:1024].copy(), T[:1024], sie[:1024].copy(), P[:1024], cv[:1024],
+                      B[:1024], Q_OUT)  # load the table once
+        t0 = time.perf_counter()
+        reps = 0
+        while True:
+            port.fill_eos(d, rho, T, sie, P, cv, B, Q_OUT)
+            reps += 1
+            el = time.perf_counter() - t0
+            if el >= min_seconds:
+                break
+    return {"value": reps * sample / el, "unit": "lookups/s", "cores": os.cpu_count(),
+            "kind": "port",
+            "sample": f"{reps} x {sample} queries of the 2^24-query workload, OpenMP over all "
+                      f"host threads, oracle/port/sgport.cpp FillEos(T|P|bmod)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    config = {"workload": "vector tabulated EOS lookup (FillEos T|P|bmod), 2^24 queries, "
+                          "256x256 NQT-log StiffGas-sampled rho-T table",
+              "queries": N_LOOKUP, "table": "256x256", "l2": "inputs (256 MB) larger than L2"}
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        steps = args.steps
+        cb = cpu_baseline(min_seconds=2.0)
+        line = {"metric": METRIC, "value": cb["value"], "unit": "lookups/s", "n_gpus": args.gpus,
+                "steps": steps, "warmup": args.warmup, "ms_per_step": N_LOOKUP / cb["value"] * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic", "config": config, "impl": "reference",
+                "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": "lookups/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    out, world, rank = run_ours(args)
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": out["value"], "unit": "lookups/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded; StiffGas-sampled table)", "config": config,
+            "e2e": out["e2e"], "roofline": out["roofline"], "clocks": out["clocks"],
+            "gpu_launches": out["gpu_launches"], "pte": out["pte"]}
+    if not args.no_cpu_baseline and world == 1:
+        line["cpu_baseline"] = cpu_baseline()
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,215 @@
+/*
+ * sgx.h -- C ABI of the GB300 closure library (libsgx.so).
+ *
+ * A drop-in for singularity-eos's data-parallel closure path: the vector EOS
+ * lookups and the per-cell pressure-temperature-equilibrium (PTE) solve.
+ * Every entry point takes plain pointers and sizes. Arrays passed to the
+ * sgx_* compute calls live in device memory unless the name says _host; the
+ * call is stream-ordered on the given CUDA stream (NULL = legacy default
+ * stream) and returns an sgx_status code. Nothing here aborts the process.
+ *
+ * Reference interfaces replaced (paths inside lanl/singularity-eos):
+ *   sgx_eos_*            constructors of IdealGas/StiffGas/NobleAbel/
+ *                        Gruneisen/SpinerEOSDependsRhoT/Helmholtz
+ *                        (eos/eos_ideal.hpp:41, eos_stiff.hpp:40,
+ *                        eos_noble_abel.hpp:40, eos_gruneisen.hpp:62,
+ *                        eos_spiner_rho_temp.hpp:85, eos_helmholtz.hpp:446)
+ *                        plus GetOnDevice()/Finalize() (eos_variant.hpp:183-186,
+ *                        865-867)
+ *   sgx_eos_eval         the vector overloads generated by SG_EOS_VEC_2IN_1OUT
+ *                        (eos/eos_base.hpp:169-230) and forwarded by Variant
+ *                        (eos/eos_variant.hpp:56-143), including
+ *                        MinInternalEnergyFromDensity (eos_base.hpp:428-494)
+ *   sgx_eos_fill         vector FillEos (eos/eos_base.hpp:503-531)
+ *   sgx_pte_solve        a per-cell loop of PTESolverRhoT / PTESolverPT driven
+ *                        by PTESolver() (closure/mixed_cell_models.hpp:884-1193,
+ *                        1207-1446, 2188-2291), as get_sg_eos_rho_e.cpp:30-88
+ *                        runs it
+ *   sgx_mix_params_default  MixParams defaults (mixed_cell_models.hpp:43-78)
+ *   sgx_pte_rhot_required_scratch  PTESolverRhoTRequiredScratch (:873-881)
+ *   sgx_pte_pt_required_scratch    PTESolverPTRequiredScratch (:1198-1206)
+ */
+#ifndef SGX_H_
+#define SGX_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* cudaStream_t without including the CUDA runtime headers. */
+typedef struct CUstream_st *sgx_stream_t;
+
+typedef enum sgx_status {
+  SGX_OK = 0,
+  SGX_ERR_INVALID = 1,   /* bad argument (null pointer, bad size, bad type) */
+  SGX_ERR_CUDA = 2,      /* a CUDA runtime call failed; see sgx_last_error() */
+  SGX_ERR_NO_DEVICE = 3, /* no CUDA device visible */
+  SGX_ERR_IO = 4,        /* a table file could not be read */
+  SGX_ERR_UNSUPPORTED = 5, /* combination not implemented (e.g. nmat > 8) */
+  SGX_ERR_TIMEOUT = 6    /* a bounded device wait ran out */
+} sgx_status;
+
+/* EOS model codes. */
+enum {
+  SGX_IDEAL_GAS = 1,
+  SGX_STIFF_GAS = 2,
+  SGX_NOBLE_ABEL = 3,
+  SGX_GRUNEISEN = 4,
+  SGX_SPINER_RHOT = 5,
+  SGX_HELMHOLTZ = 6
+};
+
+/* thermalqs bits (singularity-eos/base/constants.hpp:22-34). */
+enum {
+  SGX_Q_DENSITY = 1,
+  SGX_Q_SIE = 2,
+  SGX_Q_PRESSURE = 4,
+  SGX_Q_TEMPERATURE = 8,
+  SGX_Q_SPECIFIC_HEAT = 16,
+  SGX_Q_BULK_MODULUS = 32
+};
+
+/* Vector lookup selectors for sgx_eos_eval (the EosBase vector members). */
+enum {
+  SGX_FN_T_FROM_RHO_SIE = 0,  /* TemperatureFromDensityInternalEnergy */
+  SGX_FN_SIE_FROM_RHO_T = 1,  /* InternalEnergyFromDensityTemperature */
+  SGX_FN_P_FROM_RHO_T = 2,    /* PressureFromDensityTemperature */
+  SGX_FN_P_FROM_RHO_SIE = 3,  /* PressureFromDensityInternalEnergy */
+  SGX_FN_CV_FROM_RHO_T = 4,   /* SpecificHeatFromDensityTemperature */
+  SGX_FN_CV_FROM_RHO_SIE = 5, /* SpecificHeatFromDensityInternalEnergy */
+  SGX_FN_B_FROM_RHO_T = 6,    /* BulkModulusFromDensityTemperature */
+  SGX_FN_B_FROM_RHO_SIE = 7,  /* BulkModulusFromDensityInternalEnergy */
+  SGX_FN_G_FROM_RHO_T = 8,    /* GruneisenParamFromDensityTemperature */
+  SGX_FN_G_FROM_RHO_SIE = 9,  /* GruneisenParamFromDensityInternalEnergy */
+  SGX_FN_MIN_SIE_FROM_RHO = 10 /* MinInternalEnergyFromDensity (in2 unused) */
+};
+
+/* One EOS instance: a 128-byte trivially copyable value (the analogue of the
+ * reference's GetOnDevice() copy). Analytic models keep their parameters in
+ * p[]; tabulated models also hold a device table owned by the library, freed
+ * by sgx_eos_finalize. */
+typedef struct sgx_eos {
+  int32_t type;  /* SGX_* model code */
+  int32_t flags; /* model options (Spiner: bit0 reproducibility mode;
+                    Helmholtz: bits 0-4 rad, gas, coul, ion, ele) */
+  uint64_t table; /* device address of the table image, 0 if analytic */
+  double p[14];  /* parameters, per model:
+                    IdealGas:  gm1, Cv
+                    StiffGas:  gm1, Cv, Pinf, qq
+                    NobleAbel: gm1, Cv, bb, qq
+                    Gruneisen: C0, s1, s2, s3, G0, b, rho0, T0, P0, Cv, rho_max */
+} sgx_eos;
+
+/* Field-for-field singularity::MixParams (mixed_cell_models.hpp:43-78). */
+typedef struct sgx_mix_params {
+  int32_t verbose;
+  int32_t iterate_t_guess;
+  double derivative_eps;
+  double pte_rel_tolerance_p, pte_rel_tolerance_t, pte_rel_tolerance_e;
+  double pte_rel_tolerance_v, pte_abs_tolerance_p, pte_abs_tolerance_t;
+  double pte_slow_convergence_thresh;
+  double pte_rel_tolerance_p_sufficient, pte_rel_tolerance_t_sufficient;
+  double pte_rel_tolerance_e_sufficient, pte_rel_tolerance_v_sufficient;
+  double pte_abs_tolerance_p_sufficient, pte_abs_tolerance_t_sufficient;
+  int64_t pte_max_iter_per_mat;
+  double line_search_alpha;
+  int64_t line_search_max_iter;
+  double line_search_fac;
+  double vfrac_safety_fac;
+  double temperature_limit;
+  double default_tguess;
+  double min_dtde;
+  int64_t pte_small_step_tries;
+  double pte_small_step_thresh;
+  double pte_max_dpdv;
+  int64_t pte_reduced_system_exclude_idx;
+} sgx_mix_params;
+
+/* Per-cell result of a PTE solve (the reference's SolverStatus,
+ * mixed_cell_models.hpp:80-87, plus the iteration count). */
+typedef struct sgx_pte_status {
+  double residual;
+  int32_t niter;
+  uint8_t converged;
+  uint8_t slow_convergence_detected;
+  uint8_t max_line_niter;
+  uint8_t small_step_iters;
+} sgx_pte_status;
+
+enum { SGX_PTE_RHOT = 0, SGX_PTE_PT = 1 };
+
+/* Precision of the PTE / lookup arithmetic.
+ * SGX_PREC_FP64: the plain path; follows the reference's iteration exactly.
+ * SGX_PREC_MIXED: FP32 iterations followed by FP64 refinement. */
+enum { SGX_PREC_FP64 = 0, SGX_PREC_MIXED = 1 };
+
+const char *sgx_version(void);
+/* Message of the last failing call on this host thread. */
+const char *sgx_last_error(void);
+
+/* ---- EOS construction ---- */
+int sgx_eos_ideal_gas(sgx_eos *out, double gm1, double Cv);
+int sgx_eos_stiff_gas(sgx_eos *out, double gm1, double Cv, double Pinf, double qq);
+int sgx_eos_noble_abel(sgx_eos *out, double gm1, double Cv, double bb, double qq);
+/* rho_max <= 0 computes it from the Us-up polynomial
+ * (Gruneisen::ComputeRhoMax, eos_gruneisen.hpp:231-329). */
+int sgx_eos_gruneisen(sgx_eos *out, double C0, double s1, double s2, double s3,
+                      double G0, double b, double rho0, double T0, double P0, double Cv,
+                      double rho_max);
+/* Loads a tabulated rho-T EOS from an sp5-lite image, derives the load-time
+ * tables (SpinerEOSDependsRhoT::loadDataboxes_, eos_spiner_rho_temp.hpp:545-687)
+ * and makes the table resident on the current device. */
+int sgx_eos_spiner_rhot(sgx_eos *out, const char *path, int matid, int reproducible);
+/* Releases a tabulated EOS's device table (no-op for analytic models). */
+int sgx_eos_finalize(sgx_eos *eos);
+/* Size in bytes of the device table behind a tabulated EOS (0 if analytic). */
+size_t sgx_eos_table_bytes(const sgx_eos *eos);
+/* Copies out a tabulated EOS's derived tables in the reference's DBLIST order
+ * (for parity checks). Returns the double count, or -1. */
+long sgx_eos_spiner_dump(const sgx_eos *eos, double *out, long cap);
+
+/* ---- Vector lookups (device arrays) ---- */
+/* out[i] = F(in1[i], in2[i], lambda row i). lambda may be NULL; otherwise
+ * row i starts at lambda + i*lambda_stride. */
+int sgx_eos_eval(const sgx_eos *eos, int fn, int64_t n, const double *in1,
+                 const double *in2, double *out, double *lambda, int lambda_stride,
+                 sgx_stream_t stream);
+/* Vector FillEos: output is a bit set of SGX_Q_*; arrays not in output are
+ * inputs. Any array that is neither read nor written may be NULL. */
+int sgx_eos_fill(const sgx_eos *eos, int64_t n, double *rho, double *temp, double *sie,
+                 double *press, double *cv, double *bmod, uint32_t output, double *lambda,
+                 int lambda_stride, sgx_stream_t stream);
+
+/* ---- PTE ---- */
+int sgx_mix_params_default(sgx_mix_params *p);
+int sgx_pte_rhot_required_scratch(int nmat);
+int sgx_pte_pt_required_scratch(int nmat);
+
+/* Solves PTE in every cell.
+ *  solver     SGX_PTE_RHOT or SGX_PTE_PT
+ *  nmat       materials per cell slot (1..8); per-material arrays are
+ *             [nmat][ncell], cell index fastest
+ *  eos_list   host array of neos EOS values (neos <= 16)
+ *  eos_idx    device [nmat][ncell] index into eos_list, -1 = material absent;
+ *             NULL = material m uses eos_list[m] in every cell
+ *  vfrac_tot, sie_tot   device [ncell]
+ *  rho, vfrac, sie, temp, press   device [nmat][ncell], in/out (the reference's
+ *             initial guesses in, equilibrium state out)
+ *  lambda     device [nmat][3][ncell] per-material cache, or NULL
+ *  params     NULL = defaults
+ *  status     device [ncell] or NULL
+ *  precision  SGX_PREC_FP64 or SGX_PREC_MIXED */
+int sgx_pte_solve(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list, int neos,
+                  const int32_t *eos_idx, const double *vfrac_tot, const double *sie_tot,
+                  double *rho, double *vfrac, double *sie, double *temp, double *press,
+                  double *lambda, const sgx_mix_params *params, sgx_pte_status *status,
+                  int precision, sgx_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SGX_H_ */

@@ -1,0 +1,221 @@
+"""ctypes binding to the oracle libraries.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, tests/golden/make_golden.py,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg, never by the
+product.
+
+Two libraries share one C surface (``sg*_pte``, ``sg*_eos_vec``,
+``sg*_fill_eos``, ...):
+
+* ``oracle/_ref/libsgref.so`` -- the reference's own headers compiled against
+  the shims in ``oracle/shims`` (built only where the reference sources are
+  present, by ``oracle/build_ref.sh``);
+* ``oracle/_build/libsgport.so`` -- ``oracle/port/sgport.cpp``, this
+  project's restatement of the same algorithms, built everywhere by
+  ``oracle/build_port.sh`` and pinned against the first library's output
+  through the committed golden fixtures.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_SO = os.path.join(HERE, "_ref", "libsgref.so")
+PORT_SO = os.path.join(HERE, "_build", "libsgport.so")
+
+# EOS type codes shared by the oracle and the product (include/sgx.h).
+IDEAL, STIFF, NOBLE_ABEL, GRUNEISEN, SPINER_RHOT, HELMHOLTZ = 1, 2, 3, 4, 5, 6
+
+# thermalqs bits (singularity-eos/base/constants.hpp:22-34)
+Q_DENSITY, Q_SIE, Q_PRESSURE, Q_TEMPERATURE = 1, 2, 4, 8
+Q_SPECIFIC_HEAT, Q_BULK_MODULUS = 16, 32
+
+
+class EosDesc(C.Structure):
+    _fields_ = [
+        ("type", C.c_int32),
+        ("flags", C.c_int32),
+        ("matid", C.c_int32),
+        ("pad", C.c_int32),
+        ("p", C.c_double * 16),
+        ("path", C.c_char_p),
+    ]
+
+
+class MixParams(C.Structure):
+    """Field-for-field copy of singularity::MixParams
+    (mixed_cell_models.hpp:43-78)."""
+
+    _fields_ = [
+        ("verbose", C.c_int32),
+        ("iterate_t_guess", C.c_int32),
+        ("derivative_eps", C.c_double),
+        ("pte_rel_tolerance_p", C.c_double),
+        ("pte_rel_tolerance_t", C.c_double),
+        ("pte_rel_tolerance_e", C.c_double),
+        ("pte_rel_tolerance_v", C.c_double),
+        ("pte_abs_tolerance_p", C.c_double),
+        ("pte_abs_tolerance_t", C.c_double),
+        ("pte_slow_convergence_thresh", C.c_double),
+        ("pte_rel_tolerance_p_sufficient", C.c_double),
+        ("pte_rel_tolerance_t_sufficient", C.c_double),
+        ("pte_rel_tolerance_e_sufficient", C.c_double),
+        ("pte_rel_tolerance_v_sufficient", C.c_double),
+        ("pte_abs_tolerance_p_sufficient", C.c_double),
+        ("pte_abs_tolerance_t_sufficient", C.c_double),
+        ("pte_max_iter_per_mat", C.c_int64),
+        ("line_search_alpha", C.c_double),
+        ("line_search_max_iter", C.c_int64),
+        ("line_search_fac", C.c_double),
+        ("vfrac_safety_fac", C.c_double),
+        ("temperature_limit", C.c_double),
+        ("default_tguess", C.c_double),
+        ("min_dtde", C.c_double),
+        ("pte_small_step_tries", C.c_int64),
+        ("pte_small_step_thresh", C.c_double),
+        ("pte_max_dpdv", C.c_double),
+        ("pte_reduced_system_exclude_idx", C.c_int64),
+    ]
+
+
+def eos_desc(type_, params=(), path=None, matid=0, flags=0):
+    d = EosDesc()
+    d.type = type_
+    d.flags = flags
+    d.matid = matid
+    for i, v in enumerate(params):
+        d.p[i] = float(v)
+    d.path = path.encode() if path else None
+    return d
+
+
+_D = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_I = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+class Oracle:
+    """One oracle library (prefix ``sgref`` or ``sgport``)."""
+
+    def __init__(self, path, prefix):
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = C.CDLL(path)
+        self.prefix = prefix
+        f = self._fn
+        f("mix_params_default").argtypes = [C.POINTER(MixParams)]
+        f("pte").restype = C.c_int
+        f("eos_vec").restype = C.c_int
+        f("fill_eos").restype = C.c_int
+        f("rho_sie_from_pt").restype = C.c_int
+        f("eos_bounds").restype = C.c_int
+        f("spiner_dump").restype = C.c_long
+        f("nqt").restype = None
+
+    def _fn(self, name):
+        return getattr(self.lib, f"{self.prefix}_{name}")
+
+    def mix_params(self, **kw):
+        m = MixParams()
+        self._fn("mix_params_default")(C.byref(m))
+        for k, v in kw.items():
+            setattr(m, k, v)
+        return m
+
+    def pte(self, solver, descs, eos_idx, vfrac_tot, sie_tot, rho, vfrac, sie, temp,
+            press, params=None, lam=None, nthreads=1):
+        """Runs PTESolverRhoT (solver=0) or PTESolverPT (solver=1) per cell.
+        Per-material arrays are [nmat_max, ncell] float64 and are updated in
+        place. Returns (converged, niter, residual)."""
+        nmat, ncell = rho.shape
+        arr = (EosDesc * len(descs))(*descs)
+        conv = np.zeros(ncell, np.int32)
+        nit = np.zeros(ncell, np.int32)
+        res = np.zeros(ncell, np.float64)
+        rc = self._fn("pte")(
+            C.c_int(solver), C.c_int(nmat), C.c_int(ncell), arr, C.c_int(len(descs)),
+            _ip(eos_idx), _dp(vfrac_tot), _dp(sie_tot), _dp(rho), _dp(vfrac), _dp(sie),
+            _dp(temp), _dp(press), _dp(lam),
+            C.byref(params) if params is not None else None, _ip(conv), _ip(nit),
+            _dp(res), C.c_int(nthreads))
+        if rc != 0:
+            raise RuntimeError(f"{self.prefix}_pte failed")
+        return conv, nit, res
+
+    def eos_vec(self, desc, fn, in1, in2=None, lam=None, lam_stride=0):
+        n = in1.shape[0]
+        out = np.zeros(n, np.float64)
+        if in2 is None:
+            in2 = np.zeros(n, np.float64)
+        rc = self._fn("eos_vec")(C.byref(desc), C.c_int(fn), C.c_int(n), _dp(in1),
+                                 _dp(in2), _dp(out), _dp(lam), C.c_int(lam_stride))
+        if rc != 0:
+            raise RuntimeError(f"{self.prefix}_eos_vec failed")
+        return out
+
+    def fill_eos(self, desc, rho, temp, sie, press, cv, bmod, output, lam=None,
+                 lam_stride=0):
+        n = rho.shape[0]
+        rc = self._fn("fill_eos")(C.byref(desc), C.c_int(n), _dp(rho), _dp(temp),
+                                  _dp(sie), _dp(press), _dp(cv), _dp(bmod),
+                                  C.c_ulong(output), _dp(lam), C.c_int(lam_stride))
+        if rc != 0:
+            raise RuntimeError(f"{self.prefix}_fill_eos failed")
+
+    def rho_sie_from_pt(self, desc, P, T, rho_guess=None):
+        n = P.shape[0]
+        rho = np.array(rho_guess, np.float64) if rho_guess is not None else np.zeros(n)
+        sie = np.zeros(n)
+        rc = self._fn("rho_sie_from_pt")(C.byref(desc), C.c_int(n), _dp(P), _dp(T),
+                                         _dp(rho), _dp(sie))
+        if rc != 0:
+            raise RuntimeError(f"{self.prefix}_rho_sie_from_pt failed")
+        return rho, sie
+
+    def eos_bounds(self, desc, what, x):
+        x = np.ascontiguousarray(x, np.float64)
+        out = np.zeros_like(x)
+        rc = self._fn("eos_bounds")(C.byref(desc), C.c_int(what), C.c_int(x.shape[0]),
+                                    _dp(x), _dp(out))
+        if rc != 0:
+            raise RuntimeError(f"{self.prefix}_eos_bounds failed")
+        return out
+
+    def spiner_dump(self, path, matid):
+        scal = np.zeros(8)
+        n = self._fn("spiner_dump")(path.encode(), C.c_int(matid), None, C.c_long(0),
+                                    _dp(scal))
+        if n < 0:
+            raise RuntimeError("spiner_dump failed")
+        out = np.zeros(n)
+        self._fn("spiner_dump")(path.encode(), C.c_int(matid), _dp(out), C.c_long(n),
+                                _dp(scal))
+        return out, scal
+
+    def nqt(self, which, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros_like(x)
+        self._fn("nqt")(C.c_int(which), C.c_int(x.shape[0]), _dp(x), _dp(y))
+        return y
+
+
+def reference():
+    """The compiled reference (only where oracle/_ref was built)."""
+    return Oracle(REF_SO, "sgref")
+
+
+def port():
+    """This project's C++ restatement."""
+    return Oracle(PORT_SO, "sgport")
+
+
+def have_reference():
+    return os.path.exists(REF_SO)

@@ -1,0 +1,455 @@
+// sgref: a C entry layer over the UNMODIFIED singularity-eos hot-path
+// headers, compiled against this folder's shims (ports-of-call-lite,
+// spiner-lite, hdf5-lite, Eigen-lite) into oracle/_ref/libsgref.so.
+//
+// TEST INFRASTRUCTURE ONLY: the oracle. Only tests/ (to make and check the
+// golden fixtures) and bench.py's CPU baseline may load it; the product
+// never does. It is built in the development container only, where the
+// reference sources are present (oracle/build_ref.sh).
+//
+// Each entry point calls the reference's own API the way its callers do:
+//   - PTE: PTESolverRhoT / PTESolverPT + PTESolver(), as
+//     get_sg_eos_rho_e.cpp:30-88 and test_pte.cpp:200-245 drive them;
+//   - vector lookups: the Variant vector overloads (eos_base.hpp:169-230,
+//     eos_variant.hpp:56-143) with a 2-D lambda indexer shaped like
+//     lambdaIndexer2D (singularity_eos.cpp:39-49);
+//   - FillEos vector (eos_base.hpp:503-531).
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include <singularity-eos/closure/mixed_cell_models.hpp>
+#include <singularity-eos/eos/eos.hpp>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+using namespace singularity;
+
+extern "C" {
+
+// EOS description passed across the oracle's C boundary.
+struct sgref_eos {
+  int32_t type; // 1 IdealGas, 2 StiffGas, 3 NobleAbel, 4 Gruneisen,
+                // 5 SpinerEOSDependsRhoT, 6 Helmholtz
+  int32_t flags;
+  int32_t matid;
+  int32_t pad;
+  double p[16];
+  const char *path;
+};
+
+// Field-for-field copy of singularity::MixParams (mixed_cell_models.hpp:43-78).
+struct sgref_mix_params {
+  int32_t verbose;
+  int32_t iterate_t_guess;
+  double derivative_eps;
+  double pte_rel_tolerance_p, pte_rel_tolerance_t, pte_rel_tolerance_e;
+  double pte_rel_tolerance_v, pte_abs_tolerance_p, pte_abs_tolerance_t;
+  double pte_slow_convergence_thresh;
+  double pte_rel_tolerance_p_sufficient, pte_rel_tolerance_t_sufficient;
+  double pte_rel_tolerance_e_sufficient, pte_rel_tolerance_v_sufficient;
+  double pte_abs_tolerance_p_sufficient, pte_abs_tolerance_t_sufficient;
+  int64_t pte_max_iter_per_mat;
+  double line_search_alpha;
+  int64_t line_search_max_iter;
+  double line_search_fac;
+  double vfrac_safety_fac;
+  double temperature_limit;
+  double default_tguess;
+  double min_dtde;
+  int64_t pte_small_step_tries;
+  double pte_small_step_thresh;
+  double pte_max_dpdv;
+  int64_t pte_reduced_system_exclude_idx;
+};
+
+} // extern "C"
+
+namespace {
+
+EOS make_eos(const sgref_eos &d) {
+  switch (d.type) {
+  case 1:
+    return IdealGas(d.p[0], d.p[1]);
+  case 2:
+    return StiffGas(d.p[0], d.p[1], d.p[2], d.p[3]);
+  case 3:
+    return NobleAbel(d.p[0], d.p[1], d.p[2], d.p[3]);
+  case 4:
+    return Gruneisen(d.p[0], d.p[1], d.p[2], d.p[3], d.p[4], d.p[5], d.p[6], d.p[7],
+                     d.p[8], d.p[9]);
+  case 5:
+    return SpinerEOSDependsRhoT(std::string(d.path), d.matid, (d.flags & 1) != 0);
+  case 6:
+    return Helmholtz(std::string(d.path), (d.flags & 1) != 0, (d.flags & 2) != 0,
+                     (d.flags & 4) != 0, (d.flags & 8) != 0, (d.flags & 16) != 0, false,
+                     (d.flags & 32) == 0);
+  }
+  PORTABLE_ALWAYS_THROW_OR_ABORT("sgref: unknown EOS type");
+  return IdealGas(0.4, 1.0);
+}
+
+MixParams to_mix(const sgref_mix_params *q) {
+  MixParams m;
+  if (q == nullptr) return m;
+  m.verbose = q->verbose != 0;
+  m.iterate_t_guess = q->iterate_t_guess != 0;
+  m.derivative_eps = q->derivative_eps;
+  m.pte_rel_tolerance_p = q->pte_rel_tolerance_p;
+  m.pte_rel_tolerance_t = q->pte_rel_tolerance_t;
+  m.pte_rel_tolerance_e = q->pte_rel_tolerance_e;
+  m.pte_rel_tolerance_v = q->pte_rel_tolerance_v;
+  m.pte_abs_tolerance_p = q->pte_abs_tolerance_p;
+  m.pte_abs_tolerance_t = q->pte_abs_tolerance_t;
+  m.pte_slow_convergence_thresh = q->pte_slow_convergence_thresh;
+  m.pte_rel_tolerance_p_sufficient = q->pte_rel_tolerance_p_sufficient;
+  m.pte_rel_tolerance_t_sufficient = q->pte_rel_tolerance_t_sufficient;
+  m.pte_rel_tolerance_e_sufficient = q->pte_rel_tolerance_e_sufficient;
+  m.pte_rel_tolerance_v_sufficient = q->pte_rel_tolerance_v_sufficient;
+  m.pte_abs_tolerance_p_sufficient = q->pte_abs_tolerance_p_sufficient;
+  m.pte_abs_tolerance_t_sufficient = q->pte_abs_tolerance_t_sufficient;
+  m.pte_max_iter_per_mat = static_cast<std::size_t>(q->pte_max_iter_per_mat);
+  m.line_search_alpha = q->line_search_alpha;
+  m.line_search_max_iter = static_cast<std::size_t>(q->line_search_max_iter);
+  m.line_search_fac = q->line_search_fac;
+  m.vfrac_safety_fac = q->vfrac_safety_fac;
+  m.temperature_limit = q->temperature_limit;
+  m.default_tguess = q->default_tguess;
+  m.min_dtde = q->min_dtde;
+  m.pte_small_step_tries = static_cast<std::size_t>(q->pte_small_step_tries);
+  m.pte_small_step_thresh = q->pte_small_step_thresh;
+  m.pte_max_dpdv = q->pte_max_dpdv;
+  m.pte_reduced_system_exclude_idx = q->pte_reduced_system_exclude_idx;
+  return m;
+}
+
+// Indexes the per-cell list of EOS objects (as EOSAccessor_ does in
+// get_sg_eos_functors.hpp, via an index array).
+struct CellEOS {
+  const EOS *all;
+  const int *idx;
+  const EOS &operator[](const int m) const { return all[idx[m]]; }
+};
+
+// lambdaIndexer2D shape (singularity_eos.cpp:39-49).
+struct Lambda2D {
+  int n;
+  double *data;
+  double *operator[](int i) const { return data + static_cast<std::size_t>(n) * i; }
+};
+
+std::vector<EOS> make_all(const sgref_eos *descs, int neos) {
+  std::vector<EOS> v;
+  v.reserve(neos);
+  for (int k = 0; k < neos; ++k)
+    v.push_back(make_eos(descs[k]));
+  return v;
+}
+
+template <template <class, class, class> class Solver>
+void pte_run(int nmat_max, int ncell, const sgref_eos *descs, int neos,
+             const int32_t *eos_idx, const double *vfrac_tot, const double *sie_tot,
+             double *rho, double *vfrac, double *sie, double *temp, double *press,
+             double *lambda, const sgref_mix_params *params, int32_t *converged,
+             int32_t *niter, double *residual, int nthreads) {
+  const MixParams mp = to_mix(params);
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel num_threads(nthreads)
+#endif
+  {
+    // One copy of the EOS objects per thread (Spiner's root counters are
+    // mutable members, eos_spiner_rho_temp.hpp:260).
+    std::vector<EOS> eos = make_all(descs, neos);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 64)
+#endif
+    for (int i = 0; i < ncell; ++i) {
+      int idx[16];
+      double r[16], v[16], e[16], t[16], p[16];
+      double cache[16 * MAX_NUM_LAMBDAS];
+      int n = 0;
+      for (int m = 0; m < nmat_max; ++m) {
+        const std::size_t k = static_cast<std::size_t>(m) * ncell + i;
+        const int ie = eos_idx ? eos_idx[k] : m;
+        if (ie < 0) continue;
+        idx[n] = ie;
+        r[n] = rho[k];
+        v[n] = vfrac[k];
+        e[n] = sie[k];
+        t[n] = temp[k];
+        p[n] = press[k];
+        for (std::size_t l = 0; l < MAX_NUM_LAMBDAS; ++l)
+          cache[n * MAX_NUM_LAMBDAS + l] =
+              lambda ? lambda[(static_cast<std::size_t>(m) * MAX_NUM_LAMBDAS + l) * ncell + i]
+                     : 0.0;
+        ++n;
+      }
+      CellEOS ceos{eos.data(), idx};
+      std::vector<double> scratch(Solver<CellEOS, double *, mix_impl::CacheAccessor>::
+                                      RequiredScratch(n) +
+                                  8);
+      mix_impl::CacheAccessor cacc(cache);
+      double *pr = r, *pv = v, *pe = e, *pt = t, *pp = p;
+      Solver<CellEOS, double *, mix_impl::CacheAccessor> method(
+          n, ceos, vfrac_tot[i], sie_tot[i], pr, pv, pe, pt, pp, cacc, scratch.data(), 0.0,
+          mp);
+      SolverStatus st = PTESolver(method);
+      int q = 0;
+      for (int m = 0; m < nmat_max; ++m) {
+        const std::size_t k = static_cast<std::size_t>(m) * ncell + i;
+        const int ie = eos_idx ? eos_idx[k] : m;
+        if (ie < 0) continue;
+        rho[k] = r[q];
+        vfrac[k] = v[q];
+        sie[k] = e[q];
+        temp[k] = t[q];
+        press[k] = p[q];
+        if (lambda)
+          for (std::size_t l = 0; l < MAX_NUM_LAMBDAS; ++l)
+            lambda[(static_cast<std::size_t>(m) * MAX_NUM_LAMBDAS + l) * ncell + i] =
+                cache[q * MAX_NUM_LAMBDAS + l];
+        ++q;
+      }
+      converged[i] = st.converged ? 1 : 0;
+      niter[i] = static_cast<int32_t>(method.Niter());
+      residual[i] = st.residual;
+    }
+  }
+}
+
+} // namespace
+
+extern "C" {
+
+void sgref_mix_params_default(sgref_mix_params *q) {
+  const MixParams m;
+  q->verbose = m.verbose;
+  q->iterate_t_guess = m.iterate_t_guess;
+  q->derivative_eps = m.derivative_eps;
+  q->pte_rel_tolerance_p = m.pte_rel_tolerance_p;
+  q->pte_rel_tolerance_t = m.pte_rel_tolerance_t;
+  q->pte_rel_tolerance_e = m.pte_rel_tolerance_e;
+  q->pte_rel_tolerance_v = m.pte_rel_tolerance_v;
+  q->pte_abs_tolerance_p = m.pte_abs_tolerance_p;
+  q->pte_abs_tolerance_t = m.pte_abs_tolerance_t;
+  q->pte_slow_convergence_thresh = m.pte_slow_convergence_thresh;
+  q->pte_rel_tolerance_p_sufficient = m.pte_rel_tolerance_p_sufficient;
+  q->pte_rel_tolerance_t_sufficient = m.pte_rel_tolerance_t_sufficient;
+  q->pte_rel_tolerance_e_sufficient = m.pte_rel_tolerance_e_sufficient;
+  q->pte_rel_tolerance_v_sufficient = m.pte_rel_tolerance_v_sufficient;
+  q->pte_abs_tolerance_p_sufficient = m.pte_abs_tolerance_p_sufficient;
+  q->pte_abs_tolerance_t_sufficient = m.pte_abs_tolerance_t_sufficient;
+  q->pte_max_iter_per_mat = static_cast<int64_t>(m.pte_max_iter_per_mat);
+  q->line_search_alpha = m.line_search_alpha;
+  q->line_search_max_iter = static_cast<int64_t>(m.line_search_max_iter);
+  q->line_search_fac = m.line_search_fac;
+  q->vfrac_safety_fac = m.vfrac_safety_fac;
+  q->temperature_limit = m.temperature_limit;
+  q->default_tguess = m.default_tguess;
+  q->min_dtde = m.min_dtde;
+  q->pte_small_step_tries = static_cast<int64_t>(m.pte_small_step_tries);
+  q->pte_small_step_thresh = m.pte_small_step_thresh;
+  q->pte_max_dpdv = m.pte_max_dpdv;
+  q->pte_reduced_system_exclude_idx = m.pte_reduced_system_exclude_idx;
+}
+
+// solver: 0 = PTESolverRhoT, 1 = PTESolverPT. Arrays are [nmat_max][ncell]
+// (cell index fastest, the LayoutLeft of get_sg_eos.hpp:30-31); eos_idx of -1
+// marks an absent material. lambda (nullable) is [nmat_max][3][ncell].
+int sgref_pte(int solver, int nmat_max, int ncell, const sgref_eos *descs, int neos,
+              const int32_t *eos_idx, const double *vfrac_tot, const double *sie_tot,
+              double *rho, double *vfrac, double *sie, double *temp, double *press,
+              double *lambda, const sgref_mix_params *params, int32_t *converged,
+              int32_t *niter, double *residual, int nthreads) {
+  try {
+    if (solver == 0)
+      pte_run<PTESolverRhoT>(nmat_max, ncell, descs, neos, eos_idx, vfrac_tot, sie_tot,
+                             rho, vfrac, sie, temp, press, lambda, params, converged,
+                             niter, residual, nthreads);
+    else
+      pte_run<PTESolverPT>(nmat_max, ncell, descs, neos, eos_idx, vfrac_tot, sie_tot, rho,
+                           vfrac, sie, temp, press, lambda, params, converged, niter,
+                           residual, nthreads);
+  } catch (const std::exception &ex) {
+    std::fprintf(stderr, "sgref_pte: %s\n", ex.what());
+    return 1;
+  }
+  return 0;
+}
+
+// Vector lookup through the Variant's vector overloads.
+// fn: 0 T(rho,e) 1 e(rho,T) 2 P(rho,T) 3 P(rho,e) 4 Cv(rho,T) 5 Cv(rho,e)
+//     6 B(rho,T) 7 B(rho,e) 8 G(rho,T) 9 G(rho,e) 10 emin(rho)
+// lambda (nullable) is row-per-element with lambda_stride doubles.
+int sgref_eos_vec(const sgref_eos *desc, int fn, int n, const double *in1,
+                  const double *in2, double *out, double *lambda, int lambda_stride) {
+  try {
+    EOS eos = make_eos(*desc);
+    auto run = [&](auto &&lam) {
+      switch (fn) {
+      case 0:
+        eos.TemperatureFromDensityInternalEnergy(in1, in2, out, n, lam);
+        break;
+      case 1:
+        eos.InternalEnergyFromDensityTemperature(in1, in2, out, n, lam);
+        break;
+      case 2:
+        eos.PressureFromDensityTemperature(in1, in2, out, n, lam);
+        break;
+      case 3:
+        eos.PressureFromDensityInternalEnergy(in1, in2, out, n, lam);
+        break;
+      case 4:
+        eos.SpecificHeatFromDensityTemperature(in1, in2, out, n, lam);
+        break;
+      case 5:
+        eos.SpecificHeatFromDensityInternalEnergy(in1, in2, out, n, lam);
+        break;
+      case 6:
+        eos.BulkModulusFromDensityTemperature(in1, in2, out, n, lam);
+        break;
+      case 7:
+        eos.BulkModulusFromDensityInternalEnergy(in1, in2, out, n, lam);
+        break;
+      case 8:
+        eos.GruneisenParamFromDensityTemperature(in1, in2, out, n, lam);
+        break;
+      case 9:
+        eos.GruneisenParamFromDensityInternalEnergy(in1, in2, out, n, lam);
+        break;
+      case 10:
+        eos.MinInternalEnergyFromDensity(in1, out, n, lam);
+        break;
+      default:
+        PORTABLE_ALWAYS_THROW_OR_ABORT("sgref_eos_vec: unknown function");
+      }
+    };
+    if (lambda)
+      run(Lambda2D{lambda_stride, lambda});
+    else
+      run(NullIndexer());
+    eos.Finalize();
+  } catch (const std::exception &ex) {
+    std::fprintf(stderr, "sgref_eos_vec: %s\n", ex.what());
+    return 1;
+  }
+  return 0;
+}
+
+// Vector FillEos (eos_base.hpp:503-531); output is a thermalqs bit set.
+int sgref_fill_eos(const sgref_eos *desc, int n, double *rho, double *temp, double *sie,
+                   double *press, double *cv, double *bmod, unsigned long output,
+                   double *lambda, int lambda_stride) {
+  try {
+    EOS eos = make_eos(*desc);
+    if (lambda)
+      eos.FillEos(rho, temp, sie, press, cv, bmod, n, output,
+                  Lambda2D{lambda_stride, lambda});
+    else
+      eos.FillEos(rho, temp, sie, press, cv, bmod, n, output, NullIndexer());
+    eos.Finalize();
+  } catch (const std::exception &ex) {
+    std::fprintf(stderr, "sgref_fill_eos: %s\n", ex.what());
+    return 1;
+  }
+  return 0;
+}
+
+// Scalar DensityEnergyFromPressureTemperature over an array (PT-space
+// inversion used by PTESolverPT).
+int sgref_rho_sie_from_pt(const sgref_eos *desc, int n, const double *P, const double *T,
+                          double *rho, double *sie) {
+  try {
+    EOS eos = make_eos(*desc);
+    for (int i = 0; i < n; ++i) {
+      Real r = rho[i], e = sie[i];
+      eos.DensityEnergyFromPressureTemperature(P[i], T[i], static_cast<Real *>(nullptr), r,
+                                               e);
+      rho[i] = r;
+      sie[i] = e;
+    }
+    eos.Finalize();
+  } catch (const std::exception &ex) {
+    std::fprintf(stderr, "sgref_rho_sie_from_pt: %s\n", ex.what());
+    return 1;
+  }
+  return 0;
+}
+
+// Bounds introspection used by the PTE solvers.
+// what: 0 MinimumDensity 1 MinimumTemperature 2 MaximumDensity
+//       3 MinimumPressure 4 MaximumPressureAtTemperature(x) 5 RhoPmin(x)
+int sgref_eos_bounds(const sgref_eos *desc, int what, int n, const double *x, double *out) {
+  try {
+    EOS eos = make_eos(*desc);
+    for (int i = 0; i < n; ++i) {
+      switch (what) {
+      case 0:
+        out[i] = eos.MinimumDensity();
+        break;
+      case 1:
+        out[i] = eos.MinimumTemperature();
+        break;
+      case 2:
+        out[i] = eos.MaximumDensity();
+        break;
+      case 3:
+        out[i] = eos.MinimumPressure();
+        break;
+      case 4:
+        out[i] = eos.MaximumPressureAtTemperature(x[i]);
+        break;
+      case 5:
+        out[i] = eos.RhoPmin(x[i]);
+        break;
+      }
+    }
+    eos.Finalize();
+  } catch (const std::exception &ex) {
+    std::fprintf(stderr, "sgref_eos_bounds: %s\n", ex.what());
+    return 1;
+  }
+  return 0;
+}
+
+// Copies out every DataBox of a loaded SpinerEOSDependsRhoT through its
+// public DumpDynamicMemory (eos_spiner_rho_temp.hpp:513-526): the boxes in
+// DBLIST order (P_, sie_, bMod_, dPdRho_, dPdE_, dTdRho_, dTdE_, dEdRho_,
+// dEdT_, mF_, PMax_, sielTMax_, dEdTMax_, gm1Max_, lTColdCrit_, PCold_,
+// sieCold_, bModCold_, dPdRhoCold_, dPdECold_, dTdRhoCold_, dTdECold_,
+// dEdTCold_, rho_at_pmin_), concatenated. scal receives rhoMin, rhoMax, TMin,
+// TMax, MinimumPressure, lRhoOffset, lTOffset. Returns the double count.
+long sgref_spiner_dump(const char *path, int matid, double *out, long cap, double *scal) {
+  try {
+    SpinerEOSDependsRhoT eos(std::string(path), matid);
+    const long n = static_cast<long>(eos.DynamicMemorySizeInBytes() / sizeof(double));
+    if (out && cap >= n) eos.DumpDynamicMemory(reinterpret_cast<char *>(out));
+    if (scal) {
+      scal[0] = eos.rhoMin();
+      scal[1] = eos.rhoMax();
+      scal[2] = eos.TMin();
+      scal[3] = eos.TMax();
+      scal[4] = eos.MinimumPressure();
+      scal[5] = eos.lRhoOffset();
+      scal[6] = eos.lTOffset();
+    }
+    eos.Finalize();
+    return n;
+  } catch (const std::exception &ex) {
+    std::fprintf(stderr, "sgref_spiner_dump: %s\n", ex.what());
+    return -1;
+  }
+}
+
+// FastMath NQT transforms (logs.hpp:188-214, 282-292), element-wise.
+void sgref_nqt(int which, int n, const double *x, double *y) {
+  for (int i = 0; i < n; ++i)
+    y[i] = which == 0 ? FastMath::log10(x[i]) : FastMath::pow10(x[i]);
+}
+
+} // extern "C"

@@ -1,0 +1,271 @@
+// The C ABI (include/sgx.h): argument checks, error reporting, EOS
+// construction, table residency, and the launches of the kernels in
+// sgx_fp64.cu / sgx_mixed.cu.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "sgx_internal.h"
+#include "sgx_table.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg) {
+  g_last_error = msg;
+  return code;
+}
+int cuda_fail(cudaError_t e, const char *what) {
+  return fail(SGX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+bool valid_type(int t) { return t >= SGX_IDEAL_GAS && t <= SGX_SPINER_RHOT; }
+
+} // namespace
+
+extern "C" {
+
+const char *sgx_version(void) { return "sgx 0.1 (sm_103a)"; }
+const char *sgx_last_error(void) { return g_last_error.c_str(); }
+
+int sgx_mix_params_default(sgx_mix_params *p) {
+  if (!p) return fail(SGX_ERR_INVALID, "sgx_mix_params_default: null");
+  // MixParams defaults (closure/mixed_cell_models.hpp:43-78)
+  std::memset(p, 0, sizeof(*p));
+  p->verbose = 0;
+  p->iterate_t_guess = 1;
+  p->derivative_eps = 3.0e-6;
+  p->pte_rel_tolerance_p = 1.0e-6;
+  p->pte_rel_tolerance_t = 1.0e-4;
+  p->pte_rel_tolerance_e = 1.0e-6;
+  p->pte_rel_tolerance_v = 1.0e-6;
+  p->pte_abs_tolerance_p = 1.0e-6;
+  p->pte_abs_tolerance_t = 1.0e-4;
+  p->pte_slow_convergence_thresh = 0.99;
+  p->pte_rel_tolerance_p_sufficient = 1.e2 * p->pte_rel_tolerance_p;
+  p->pte_rel_tolerance_t_sufficient = 10 * p->pte_rel_tolerance_t;
+  p->pte_rel_tolerance_e_sufficient = 1.e2 * p->pte_rel_tolerance_e;
+  p->pte_rel_tolerance_v_sufficient = 1.e2 * p->pte_rel_tolerance_v;
+  p->pte_abs_tolerance_p_sufficient = 1.e2 * p->pte_abs_tolerance_p;
+  p->pte_abs_tolerance_t_sufficient = 10 * p->pte_abs_tolerance_t;
+  p->pte_max_iter_per_mat = 128;
+  p->line_search_alpha = 1.e-2;
+  p->line_search_max_iter = 6;
+  p->line_search_fac = 0.5;
+  p->vfrac_safety_fac = 0.95;
+  p->temperature_limit = 1.0e15;
+  p->default_tguess = 300.;
+  p->min_dtde = 1.0e-16;
+  p->pte_small_step_tries = 2;
+  p->pte_small_step_thresh = 1e-16;
+  p->pte_max_dpdv = -1e-8;
+  p->pte_reduced_system_exclude_idx = -1;
+  return SGX_OK;
+}
+
+// PTESolverRhoTRequiredScratch / PTESolverPTRequiredScratch
+// (mixed_cell_models.hpp:873-881, 1198-1206). The GPU solver keeps this
+// state in registers; the numbers are reported for API compatibility.
+int sgx_pte_rhot_required_scratch(int nmat) { return nmat * nmat + 4 * nmat + 6 * nmat; }
+int sgx_pte_pt_required_scratch(int nmat) { return 2 * 2 + 4 * 2 + 2 * nmat; }
+
+int sgx_eos_ideal_gas(sgx_eos *out, double gm1, double Cv) {
+  if (!out) return fail(SGX_ERR_INVALID, "sgx_eos_ideal_gas: null");
+  // IdealGas::CheckParams (eos_ideal.hpp:65-76)
+  if (!(Cv >= 0) || !(gm1 >= 0)) return fail(SGX_ERR_INVALID, "IdealGas: Cv and gm1 must be >= 0");
+  std::memset(out, 0, sizeof(*out));
+  out->type = SGX_IDEAL_GAS;
+  out->p[0] = gm1;
+  out->p[1] = Cv;
+  return SGX_OK;
+}
+
+int sgx_eos_stiff_gas(sgx_eos *out, double gm1, double Cv, double Pinf, double qq) {
+  if (!out) return fail(SGX_ERR_INVALID, "sgx_eos_stiff_gas: null");
+  if (!(Cv >= 0) || !(gm1 >= 0)) return fail(SGX_ERR_INVALID, "StiffGas: Cv and gm1 must be >= 0");
+  std::memset(out, 0, sizeof(*out));
+  out->type = SGX_STIFF_GAS;
+  out->p[0] = gm1;
+  out->p[1] = Cv;
+  out->p[2] = Pinf;
+  out->p[3] = qq;
+  return SGX_OK;
+}
+
+int sgx_eos_noble_abel(sgx_eos *out, double gm1, double Cv, double bb, double qq) {
+  if (!out) return fail(SGX_ERR_INVALID, "sgx_eos_noble_abel: null");
+  if (!(Cv > 0) || !(gm1 >= 0) || !(bb >= 0))
+    return fail(SGX_ERR_INVALID, "NobleAbel: Cv > 0, gm1 >= 0 and b >= 0 required");
+  std::memset(out, 0, sizeof(*out));
+  out->type = SGX_NOBLE_ABEL;
+  out->p[0] = gm1;
+  out->p[1] = Cv;
+  out->p[2] = bb;
+  out->p[3] = qq;
+  return SGX_OK;
+}
+
+int sgx_eos_gruneisen(sgx_eos *out, double C0, double s1, double s2, double s3, double G0,
+                      double b, double rho0, double T0, double P0, double Cv, double rho_max) {
+  if (!out) return fail(SGX_ERR_INVALID, "sgx_eos_gruneisen: null");
+  if (!(rho_max > 0)) {
+    int err = 0;
+    rho_max = 0.99 * sgx::gruneisen_compute_rho_max(s1, s2, s3, rho0, &err);
+    if (err) return fail(SGX_ERR_INVALID, "Gruneisen: cubic root find for rho_max failed");
+  }
+  std::memset(out, 0, sizeof(*out));
+  out->type = SGX_GRUNEISEN;
+  const double v[11] = {C0, s1, s2, s3, G0, b, rho0, T0, P0, Cv, rho_max};
+  for (int k = 0; k < 11; ++k)
+    out->p[k] = v[k];
+  return SGX_OK;
+}
+
+int sgx_eos_spiner_rhot(sgx_eos *out, const char *path, int matid, int reproducible) {
+  if (!out || !path) return fail(SGX_ERR_INVALID, "sgx_eos_spiner_rhot: null");
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+    return fail(SGX_ERR_NO_DEVICE, "sgx_eos_spiner_rhot: no CUDA device");
+  std::string msg;
+  uint64_t handle = 0;
+  const int rc = sgx::table_load_spiner(path, matid, reproducible != 0, &handle, msg);
+  if (rc != SGX_OK) return fail(rc, msg);
+  std::memset(out, 0, sizeof(*out));
+  out->type = SGX_SPINER_RHOT;
+  out->flags = reproducible ? 1 : 0;
+  out->table = handle;
+  return SGX_OK;
+}
+
+int sgx_eos_finalize(sgx_eos *eos) {
+  if (!eos) return fail(SGX_ERR_INVALID, "sgx_eos_finalize: null");
+  if (eos->table) {
+    std::string msg;
+    const int rc = sgx::table_free(eos->table, msg);
+    eos->table = 0;
+    if (rc != SGX_OK) return fail(rc, msg);
+  }
+  return SGX_OK;
+}
+
+size_t sgx_eos_table_bytes(const sgx_eos *eos) {
+  return (eos && eos->table) ? sgx::table_bytes(eos->table) : 0;
+}
+
+long sgx_eos_spiner_dump(const sgx_eos *eos, double *out, long cap) {
+  if (!eos || eos->type != SGX_SPINER_RHOT || !eos->table) {
+    fail(SGX_ERR_INVALID, "sgx_eos_spiner_dump: not a tabulated EOS");
+    return -1;
+  }
+  return sgx::table_dump(eos->table, out, cap);
+}
+
+int sgx_eos_eval(const sgx_eos *eos, int fn, int64_t n, const double *in1, const double *in2,
+                 double *out, double *lambda, int lambda_stride, sgx_stream_t stream) {
+  if (!eos || !valid_type(eos->type)) return fail(SGX_ERR_INVALID, "sgx_eos_eval: bad eos");
+  if (fn < SGX_FN_T_FROM_RHO_SIE || fn > SGX_FN_MIN_SIE_FROM_RHO)
+    return fail(SGX_ERR_INVALID, "sgx_eos_eval: bad fn");
+  if (n < 0) return fail(SGX_ERR_INVALID, "sgx_eos_eval: n < 0");
+  if (n == 0) return SGX_OK;
+  if (!in1 || !out || (!in2 && fn != SGX_FN_MIN_SIE_FROM_RHO))
+    return fail(SGX_ERR_INVALID, "sgx_eos_eval: null array");
+  if (lambda && lambda_stride < 2) return fail(SGX_ERR_INVALID, "sgx_eos_eval: lambda_stride < 2");
+  sgx::EvalArgs a;
+  a.eos = *eos;
+  a.fn = fn;
+  a.n = n;
+  a.in1 = in1;
+  a.in2 = in2;
+  a.out = out;
+  a.lambda = lambda;
+  a.lambda_stride = lambda_stride;
+  const cudaError_t e = sgx::launch_eval_fp64(a, reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "sgx_eos_eval");
+  return SGX_OK;
+}
+
+int sgx_eos_fill(const sgx_eos *eos, int64_t n, double *rho, double *temp, double *sie,
+                 double *press, double *cv, double *bmod, uint32_t output, double *lambda,
+                 int lambda_stride, sgx_stream_t stream) {
+  if (!eos || !valid_type(eos->type)) return fail(SGX_ERR_INVALID, "sgx_eos_fill: bad eos");
+  if (n < 0) return fail(SGX_ERR_INVALID, "sgx_eos_fill: n < 0");
+  if (n == 0) return SGX_OK;
+  if (!rho) return fail(SGX_ERR_INVALID, "sgx_eos_fill: rho is required");
+  if (lambda && lambda_stride < 2) return fail(SGX_ERR_INVALID, "sgx_eos_fill: lambda_stride < 2");
+  sgx::FillArgs a;
+  a.eos = *eos;
+  a.n = n;
+  a.rho = rho;
+  a.temp = temp;
+  a.sie = sie;
+  a.press = press;
+  a.cv = cv;
+  a.bmod = bmod;
+  a.lambda = lambda;
+  a.lambda_stride = lambda_stride;
+  a.output = output;
+  a.err = nullptr;
+  const cudaError_t e = sgx::launch_fill_fp64(a, reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "sgx_eos_fill");
+  return SGX_OK;
+}
+
+int sgx_pte_solve(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list, int neos,
+                  const int32_t *eos_idx, const double *vfrac_tot, const double *sie_tot,
+                  double *rho, double *vfrac, double *sie, double *temp, double *press,
+                  double *lambda, const sgx_mix_params *params, sgx_pte_status *status,
+                  int precision, sgx_stream_t stream) {
+  if (solver != SGX_PTE_RHOT && solver != SGX_PTE_PT)
+    return fail(SGX_ERR_INVALID, "sgx_pte_solve: bad solver");
+  if (nmat < 1 || nmat > sgx::MAX_NMAT)
+    return fail(SGX_ERR_UNSUPPORTED, "sgx_pte_solve: nmat must be in 1..8");
+  if (neos < 1 || neos > sgx::MAX_EOS || !eos_list)
+    return fail(SGX_ERR_INVALID, "sgx_pte_solve: neos must be in 1..16");
+  if (!eos_idx && neos < nmat)
+    return fail(SGX_ERR_INVALID, "sgx_pte_solve: eos_idx NULL needs neos >= nmat");
+  if (ncell < 0) return fail(SGX_ERR_INVALID, "sgx_pte_solve: ncell < 0");
+  if (ncell == 0) return SGX_OK;
+  if (!vfrac_tot || !sie_tot || !rho || !vfrac || !sie || !temp || !press)
+    return fail(SGX_ERR_INVALID, "sgx_pte_solve: null array");
+  for (int k = 0; k < neos; ++k)
+    if (!valid_type(eos_list[k].type)) return fail(SGX_ERR_INVALID, "sgx_pte_solve: bad eos");
+  sgx::PteArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.solver = solver;
+  a.nmat = nmat;
+  a.ncell = ncell;
+  a.neos = neos;
+  for (int k = 0; k < neos; ++k)
+    a.eos[k] = eos_list[k];
+  a.eos_idx = eos_idx;
+  a.vfrac_tot = vfrac_tot;
+  a.sie_tot = sie_tot;
+  a.rho = rho;
+  a.vfrac = vfrac;
+  a.sie = sie;
+  a.temp = temp;
+  a.press = press;
+  a.lambda = lambda;
+  a.status = status;
+  if (params)
+    a.params = *params;
+  else
+    sgx_mix_params_default(&a.params);
+  cudaError_t e;
+  if (precision == SGX_PREC_MIXED)
+    e = sgx::launch_pte_mixed(a, reinterpret_cast<cudaStream_t>(stream));
+  else
+    e = sgx::launch_pte_fp64(a, reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "sgx_pte_solve");
+  return SGX_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,97 @@
+// FP64 kernels of the plain path: the vector EOS lookups and the dispatch of
+// the per-cell PTE kernels (one instantiation per material count, built from
+// sgx_pte_fp64_n.cu). Compiled with --fmad=false so that every expression
+// rounds exactly as the reference does when built without FP contraction.
+//
+//   eval_kernel   the EosBase vector overloads (eos/eos_base.hpp:169-230)
+//   fill_kernel   vector FillEos (eos/eos_base.hpp:503-531)
+#include <cuda_runtime.h>
+
+#include "sgx_internal.h"
+#include "sgx_dispatch.cuh"
+
+namespace sgx {
+
+template <int N> cudaError_t launch_pte_fp64_n(const PteArgs &a, cudaStream_t stream);
+
+namespace {
+
+__global__ void eval_kernel(const EvalArgs a) {
+  const sgx_eos e = a.eos;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < a.n;
+       i += stride) {
+    double *lam = a.lambda ? a.lambda + i * a.lambda_stride : nullptr;
+    const double b = a.in2 ? a.in2[i] : 0.0;
+    a.out[i] = ev_eval(e, a.fn, a.in1[i], b, lam);
+  }
+}
+
+__global__ void fill_kernel(const FillArgs a) {
+  const sgx_eos e = a.eos;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  int bad = 0;
+  for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < a.n;
+       i += stride) {
+    double rho = a.rho ? a.rho[i] : 0.0;
+    double temp = a.temp ? a.temp[i] : 0.0;
+    double sie = a.sie ? a.sie[i] : 0.0;
+    double press = a.press ? a.press[i] : 0.0;
+    double cv = 0.0, bmod = 0.0;
+    double *lam = a.lambda ? a.lambda + i * a.lambda_stride : nullptr;
+    int err = 0;
+    ev_fill(e, rho, temp, sie, press, cv, bmod, a.output, lam, &err);
+    bad |= err;
+    if ((a.output & Q_DENSITY) && a.rho) a.rho[i] = rho;
+    if ((a.output & Q_TEMPERATURE) && a.temp) a.temp[i] = temp;
+    if ((a.output & Q_SIE) && a.sie) a.sie[i] = sie;
+    if ((a.output & Q_PRESSURE) && a.press) a.press[i] = press;
+    if ((a.output & Q_CV) && a.cv) a.cv[i] = cv;
+    if ((a.output & Q_BMOD) && a.bmod) a.bmod[i] = bmod;
+  }
+  if (bad && a.err) atomicOr(a.err, 1);
+}
+
+int grid_for(long long n, int block) {
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long want = (n + block - 1) / block;
+  const long long cap = static_cast<long long>(sms) * 16;
+  return static_cast<int>(want < cap ? (want > 0 ? want : 1) : cap);
+}
+
+} // namespace
+
+cudaError_t launch_pte_fp64(const PteArgs &a, cudaStream_t stream) {
+  if (a.ncell <= 0) return cudaSuccess;
+  // Without an index map every cell holds exactly nmat materials.
+  const int lo = a.eos_idx ? 1 : a.nmat;
+  const int hi = a.nmat < PTE_MAX_N ? a.nmat : PTE_MAX_N;
+  cudaError_t e = cudaSuccess;
+  for (int n = lo; n <= hi && e == cudaSuccess; ++n) {
+    switch (n) {
+    case 1: e = launch_pte_fp64_n<1>(a, stream); break;
+    case 2: e = launch_pte_fp64_n<2>(a, stream); break;
+    case 3: e = launch_pte_fp64_n<3>(a, stream); break;
+    case 4: e = launch_pte_fp64_n<4>(a, stream); break;
+    case 5: e = launch_pte_fp64_n<5>(a, stream); break;
+    case 6: e = launch_pte_fp64_n<6>(a, stream); break;
+    }
+  }
+  return e;
+}
+
+cudaError_t launch_eval_fp64(const EvalArgs &a, cudaStream_t stream) {
+  if (a.n <= 0) return cudaSuccess;
+  eval_kernel<<<grid_for(a.n, 256), 256, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_fp64(const FillArgs &a, cudaStream_t stream) {
+  if (a.n <= 0) return cudaSuccess;
+  fill_kernel<<<grid_for(a.n, 256), 256, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+} // namespace sgx

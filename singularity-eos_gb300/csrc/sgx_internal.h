@@ -1,0 +1,56 @@
+// Internal interfaces between the C-ABI layer (sgx_capi.cu) and the kernel
+// translation units (sgx_fp64.cu, sgx_mixed.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "../../include/sgx.h"
+
+namespace sgx {
+
+constexpr int MAX_EOS = 16;
+constexpr int MAX_NMAT = 8;  // material slots per cell
+constexpr int PTE_MAX_N = 6; // materials present per cell (Jacobian up to 6x6)
+
+// Launch arguments of the per-cell PTE kernels (passed by value: about 2.4 KB
+// of kernel parameter space).
+struct PteArgs {
+  int solver;
+  int nmat;
+  long long ncell;
+  int neos;
+  int pad;
+  sgx_eos eos[MAX_EOS];
+  const int32_t *eos_idx;
+  const double *vfrac_tot, *sie_tot;
+  double *rho, *vfrac, *sie, *temp, *press, *lambda;
+  sgx_pte_status *status;
+  sgx_mix_params params;
+};
+
+// Per-cell PTE, FP64, following the reference iteration exactly.
+cudaError_t launch_pte_fp64(const PteArgs &a, cudaStream_t stream);
+// Per-cell PTE, FP32 iterations then FP64 refinement.
+cudaError_t launch_pte_mixed(const PteArgs &a, cudaStream_t stream);
+
+struct EvalArgs {
+  sgx_eos eos;
+  int fn;
+  long long n;
+  const double *in1, *in2;
+  double *out, *lambda;
+  int lambda_stride;
+};
+cudaError_t launch_eval_fp64(const EvalArgs &a, cudaStream_t stream);
+
+struct FillArgs {
+  sgx_eos eos;
+  long long n;
+  double *rho, *temp, *sie, *press, *cv, *bmod, *lambda;
+  unsigned output;
+  int lambda_stride;
+  int *err; // device flag: set to 1 on an undefined input/output combination
+};
+cudaError_t launch_fill_fp64(const FillArgs &a, cudaStream_t stream);
+
+} // namespace sgx

@@ -1,0 +1,786 @@
+// Per-cell pressure-temperature-equilibrium solvers, one GPU thread per cell,
+// state in registers/local memory.
+//
+// Restates, step for step and in the same floating-point operation order,
+// singularity-eos's closure/mixed_cell_models.hpp:
+//   PTESolverBase        :329-786  (InitBase, GetTguess, SetVfracFromT, ...)
+//   PTESolverRhoT        :873-1193 (reduced system in T and n-1 volume fractions)
+//   PTESolverPT          :1198-1446 (2x2 system in T and P)
+//   solve_Ax_b_wscr      :176-278  (Jacobi scaling, Cramer for 2x2, QR beyond)
+//   PTESolver            :2188-2291 (damped Newton with backtracking)
+// The compile-time material count N lets every per-material array live in
+// registers; ms (the excluded material) stays a runtime value.
+//
+// The arithmetic type T is double for the plain path (bit-identical to the
+// reference built without FP contraction) and float for the iteration phase
+// of the mixed-precision path, which is then refined in double.
+#pragma once
+
+#include "sgx_dispatch.cuh"
+
+namespace sgx {
+
+struct PteStatusLocal {
+  double residual = 0;
+  int niter = 0;
+  bool converged = false;
+  bool slow = false;
+  int max_line_niter = 0;
+  int small_step_iters = 0;
+};
+
+// Column-pivoted Householder QR solve of the n x n row-major system
+// A x = b (A, b overwritten; x written). Same loops and order as the oracle's
+// Eigen-lite (Businger-Golub; Golub & Van Loan Alg. 5.4.1, Eigen's
+// Householder convention); a zero pivot gives a zero component.
+template <typename T, int N>
+SGX_HD void colpiv_qr_solve(T (&R)[N * N], T (&b)[N], T (&x)[N]) {
+  constexpr int n = N;
+  int perm[N];
+#pragma unroll
+  for (int j = 0; j < n; ++j)
+    perm[j] = j;
+#pragma unroll
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    T cmax = T(-1.0);
+#pragma unroll
+    for (int j = k; j < n; ++j) {
+      T c = T(0.0);
+#pragma unroll
+      for (int i = k; i < n; ++i)
+        c += R[i * n + j] * R[i * n + j];
+      if (c > cmax) {
+        cmax = c;
+        p = j;
+      }
+    }
+    if (p != k) {
+#pragma unroll
+      for (int j = k + 1; j < n; ++j) {
+        if (j == p) {
+#pragma unroll
+          for (int i = 0; i < n; ++i) {
+            const T t = R[i * n + k];
+            R[i * n + k] = R[i * n + j];
+            R[i * n + j] = t;
+          }
+          const int t = perm[k];
+          perm[k] = perm[j];
+          perm[j] = t;
+        }
+      }
+    }
+    T sigma = T(0.0);
+#pragma unroll
+    for (int i = k + 1; i < n; ++i)
+      sigma += R[i * n + k] * R[i * n + k];
+    if (sigma == T(0.0)) continue;
+    const T x0 = R[k * n + k];
+#if defined(__CUDA_ARCH__)
+    const T mu = sqrt(x0 * x0 + sigma);
+#else
+    const T mu = __builtin_sqrt(x0 * x0 + sigma);
+#endif
+    const T beta = (x0 >= T(0.0)) ? -mu : mu;
+    const T v0 = x0 - beta;
+    const T tau = (beta - x0) / beta;
+#pragma unroll
+    for (int i = k + 1; i < n; ++i)
+      R[i * n + k] = R[i * n + k] / v0;
+    R[k * n + k] = beta;
+#pragma unroll
+    for (int j = k + 1; j < n; ++j) {
+      T s = R[k * n + j];
+#pragma unroll
+      for (int i = k + 1; i < n; ++i)
+        s += R[i * n + k] * R[i * n + j];
+      s = s * tau;
+      R[k * n + j] -= s;
+#pragma unroll
+      for (int i = k + 1; i < n; ++i)
+        R[i * n + j] -= s * R[i * n + k];
+    }
+    T s = b[k];
+#pragma unroll
+    for (int i = k + 1; i < n; ++i)
+      s += R[i * n + k] * b[i];
+    s = s * tau;
+    b[k] -= s;
+#pragma unroll
+    for (int i = k + 1; i < n; ++i)
+      b[i] -= s * R[i * n + k];
+  }
+  T z[N];
+#pragma unroll
+  for (int i = n - 1; i >= 0; --i) {
+    T s = b[i];
+#pragma unroll
+    for (int j = i + 1; j < n; ++j)
+      s -= R[i * n + j] * z[j];
+    z[i] = (R[i * n + i] == T(0.0)) ? T(0.0) : s / R[i * n + i];
+  }
+#pragma unroll
+  for (int i = 0; i < n; ++i) {
+#pragma unroll
+    for (int j = 0; j < n; ++j)
+      if (perm[i] == j) x[j] = z[i];
+  }
+}
+
+// mix_impl::isfinite (mixed_cell_models.hpp:155-157)
+template <typename T> SGX_HD bool mix_isfinite(const T a) {
+  return (a == a) && ((a == T(0)) || (a != 2 * a));
+}
+
+// solve_Ax_b_wscr (mixed_cell_models.hpp:176-278); b holds x on return.
+template <typename T, int N> SGX_HD bool solve_Ax_b(T (&a)[N * N], T (&b)[N]) {
+  constexpr int n = N;
+#pragma unroll
+  for (int row = 0; row < n; ++row) {
+    T maxabs = T(0);
+#pragma unroll
+    for (int column = 0; column < n; ++column)
+      maxabs = smax(sabs(a[row * n + column]), maxabs);
+    if (maxabs == T(0)) return false;
+#pragma unroll
+    for (int column = 0; column < n; ++column)
+      a[row * n + column] /= maxabs;
+    b[row] /= maxabs;
+  }
+  if constexpr (N == 1) {
+    b[0] = ratio(b[0], a[0]);
+  } else if constexpr (N == 2) {
+    const T det = a[0] * a[3] - a[1] * a[2];
+    const T x0 = ratio(a[3] * b[0] - a[1] * b[1], det);
+    const T x1 = ratio(a[0] * b[1] - a[2] * b[0], det);
+    b[0] = x0;
+    b[1] = x1;
+  } else {
+    T x[N];
+    colpiv_qr_solve<T, N>(a, b, x);
+#pragma unroll
+    for (int i = 0; i < n; ++i)
+      b[i] = x[i];
+  }
+  bool ok = true;
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+    if (!mix_isfinite(b[i])) ok = false;
+  return ok;
+}
+
+// Parameters used inside the iteration, converted to the arithmetic type.
+template <typename T> struct MixP {
+  bool iterate_t_guess;
+  T derivative_eps, tol_p, tol_e, tol_v, abs_p, slow_thresh;
+  T tol_p_suff, tol_e_suff, tol_v_suff, abs_p_suff;
+  int max_iter_per_mat;
+  T ls_alpha;
+  int ls_max_iter;
+  T ls_fac, vfrac_safety_fac, temperature_limit, default_tguess;
+  int small_step_tries;
+  T small_step_thresh, max_dpdv;
+  int exclude_idx;
+  SGX_HD MixP() {}
+  SGX_HD explicit MixP(const sgx_mix_params &q) {
+    iterate_t_guess = q.iterate_t_guess != 0;
+    derivative_eps = T(q.derivative_eps);
+    tol_p = T(q.pte_rel_tolerance_p);
+    tol_e = T(q.pte_rel_tolerance_e);
+    tol_v = T(q.pte_rel_tolerance_v);
+    abs_p = T(q.pte_abs_tolerance_p);
+    slow_thresh = T(q.pte_slow_convergence_thresh);
+    tol_p_suff = T(q.pte_rel_tolerance_p_sufficient);
+    tol_e_suff = T(q.pte_rel_tolerance_e_sufficient);
+    tol_v_suff = T(q.pte_rel_tolerance_v_sufficient);
+    abs_p_suff = T(q.pte_abs_tolerance_p_sufficient);
+    max_iter_per_mat = int(q.pte_max_iter_per_mat);
+    ls_alpha = T(q.line_search_alpha);
+    ls_max_iter = int(q.line_search_max_iter);
+    ls_fac = T(q.line_search_fac);
+    vfrac_safety_fac = T(q.vfrac_safety_fac);
+    temperature_limit = T(q.temperature_limit);
+    default_tguess = T(q.default_tguess);
+    small_step_tries = int(q.pte_small_step_tries);
+    small_step_thresh = T(q.pte_small_step_thresh);
+    max_dpdv = T(q.pte_max_dpdv);
+    exclude_idx = int(q.pte_reduced_system_exclude_idx);
+  }
+};
+
+// ===========================================================================
+// Shared base: PTESolverBase (mixed_cell_models.hpp:329-786)
+// ===========================================================================
+template <typename T, int N, int NEQ> struct PteBase {
+  static constexpr int n = N;
+  const sgx_eos *eos[N];
+  double *lam[N]; // per-material lambda cache (3 doubles) or nullptr
+  const MixP<T> *P;
+  T rho[N], vfrac[N], sie[N], temp[N], press[N];
+  T u[N], rhobar[N];
+  T jac[NEQ * NEQ], dx[NEQ], residual[NEQ];
+  T vfrac_total, sie_total, rho_total, uscale, utotal_scale, Tnorm;
+  int niter;
+  int err_flags; // non-zero when a reference abort path was taken
+
+  SGX_HD T e_of(int m, T r, T t) const { return ev_sie_from_rho_T<T>(*eos[m], r, t, lam[m]); }
+  // GetPressureFromPreferred with do_e_lookup = false (:583-597)
+  SGX_HD T p_pref(int m, T r, T t, T e) const {
+    if (preferred_input(*eos[m]) & Q_SIE) return ev_P_from_rho_sie<T>(*eos[m], r, e, lam[m]);
+    return ev_P_from_rho_T<T>(*eos[m], r, t, lam[m]);
+  }
+
+  SGX_HD void init_rhobar() {
+#pragma unroll
+    for (int m = 0; m < n; ++m)
+      rhobar[m] = rho[m] * vfrac[m];
+    rho_total = sum_neumaier(rhobar, n);
+  }
+  SGX_HD void normalize_vfrac() {
+    const T vfrac_sum = sum_neumaier(vfrac, n);
+#pragma unroll
+    for (int m = 0; m < n; ++m)
+      vfrac[m] *= ratio(vfrac_total, vfrac_sum);
+  }
+  SGX_HD T vfrac_max(int m, T Tk) const {
+    const T rho_min = T(ev_rho_pmin(*eos[m], double(Tk)));
+    return smin(T(0.9) * ratio(rhobar[m], rho_min), T(1.0));
+  }
+  // SetVfracFromT (:423-498); true = FAIL
+  SGX_HD bool set_vfrac_from_T(const T Tk) {
+    const T min_dv = T(1e-12);
+    T vfrac_max_sum = 0;
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      const T vmax = vfrac_max(m, Tk);
+      if (vfrac[m] <= T(0)) vfrac[m] = vmax;
+      vfrac_max_sum += vmax;
+    }
+    if (vfrac_max_sum < vfrac_total) return true;
+    normalize_vfrac();
+    for (int it = 0; it < n; ++it) {
+      T remaining = 0;
+      unsigned n_uncapped = n;
+#pragma unroll
+      for (int m = 0; m < n; ++m) {
+        const T vnew = smin(vfrac_max(m, Tk), vfrac[m]);
+        const T dv = vfrac[m] - vnew;
+        vfrac[m] -= dv;
+        remaining += dv;
+        n_uncapped -= (dv > min_dv);
+      }
+      if (sabs(remaining) < min_dv) break;
+#pragma unroll
+      for (int m = 0; m < n; ++m) {
+        const bool uncapped = ((vfrac_max(m, Tk) - vfrac[m]) > min_dv);
+        if (uncapped) vfrac[m] += remaining / T(n_uncapped);
+      }
+    }
+    normalize_vfrac();
+    return false;
+  }
+  // GetSieCvFromTAndPreferred (:599-620)
+  SGX_HD void sie_cv_pref(int m, T r, const T Pin, const T Tk, T &s, T &cv) const {
+    const sgx_eos &e = *eos[m];
+    if (preferred_input(e) & Q_PRESSURE) {
+      int err = 0;
+      const T Pmin = T(ev_min_pressure(e));
+      const T Pmax = T(ev_max_pressure_at_T(e, double(Tk), &err));
+      T Pguess;
+      if (bad_value(double(Pin)))
+        Pguess = T(0.5) * (Pmin + Pmax);
+      else
+        Pguess = smax(Pmin, smin(Pmax, Pin));
+      double rr = double(r), ss = 0;
+      ev_rho_sie_from_PT(e, double(Pguess), double(Tk), rr, ss, lam[m], &err);
+      r = T(rr);
+      s = T(ss);
+      cv = ev_cv_from_rho_sie<T>(e, r, s, lam[m]);
+    } else {
+      s = ev_sie_from_rho_T<T>(e, r, Tk, lam[m]);
+      cv = ev_cv_from_rho_T<T>(e, r, Tk, lam[m]);
+    }
+  }
+  // GetTguess (:500-581)
+  SGX_HD T get_tguess() {
+    T Tguess;
+    if (Tnorm > T(0.0)) {
+      Tguess = Tnorm;
+    } else {
+      Tguess = P->default_tguess;
+#pragma unroll
+      for (int m = 0; m < n; ++m)
+        Tguess = smax(Tguess, temp[m]);
+    }
+    auto newton_step = [&](T Tk) {
+      T dudt = 0, usum = 0;
+#pragma unroll
+      for (int m = 0; m < n; ++m) {
+        const T rho_max = T(ev_max_density(*eos[m]));
+        T s, cv;
+        sie_cv_pref(m, smin(rho[m], rho_max), press[m], Tk, s, cv);
+        usum += rhobar[m] * s;
+        dudt += rhobar[m] * cv;
+      }
+      return Tk - ratio((usum - utotal_scale * uscale), dudt);
+    };
+    const T Tfactor = T(10.0);
+    bool bad = false;
+    for (int i = 0; i < 3; i++) {
+      if (P->iterate_t_guess)
+        Tguess = smin(P->temperature_limit, smax(Tguess, newton_step(Tguess)));
+#pragma unroll
+      for (int m = 0; m < n; ++m)
+        Tguess = smax(T(ev_min_temperature(*eos[m])), Tguess);
+      bad = set_vfrac_from_T(Tguess);
+      if (bad) {
+        Tguess *= Tfactor;
+        continue;
+      }
+#pragma unroll
+      for (int m = 0; m < n; ++m)
+        rho[m] = ratio(rhobar[m], vfrac[m]);
+      bad = false;
+      for (int m = 0; m < n; ++m) {
+        const T rho_min = T(ev_rho_pmin(*eos[m], double(Tguess)));
+        if (rho[m] < rho_min) {
+          bad = true;
+          Tguess *= Tfactor;
+          break;
+        }
+      }
+      if (!bad) break;
+    }
+    return Tguess;
+  }
+  // InitBase (:627-662)
+  SGX_HD void init_base() {
+    init_rhobar();
+    const T utotal = rho_total * sie_total;
+    uscale = smax(sabs(utotal), T(1.0e-14));
+    utotal_scale = ratio(utotal, uscale);
+    const T Tguess = get_tguess();
+    Tnorm = Tguess;
+#pragma unroll
+    for (int m = 0; m < n; m++) {
+      temp[m] = T(1.0);
+      sie[m] = e_of(m, rho[m], Tguess);
+      if ((preferred_input(*eos[m]) & Q_PRESSURE) && !bad_value(double(press[m])))
+        press[m] = ratio(press[m], uscale);
+      else
+        press[m] = ratio(p_pref(m, rho[m], Tguess, sie[m]), uscale);
+    }
+#pragma unroll
+    for (int m = 0; m < n; ++m)
+      u[m] = sie[m] * ratio(rhobar[m], uscale);
+  }
+  SGX_HD T residual_norm() const { return T(0.5) * sum_neumaier_sq(residual, NEQ); }
+  SGX_HD bool solve() {
+#pragma unroll
+    for (int m = 0; m < NEQ; m++)
+      dx[m] = residual[m];
+    return solve_Ax_b<T, NEQ>(jac, dx);
+  }
+};
+
+// ===========================================================================
+// PTESolverRhoT (:884-1193)
+// ===========================================================================
+template <typename T, int N> struct PteRhoT : PteBase<T, N, N> {
+  using B = PteBase<T, N, N>;
+  using B::dx;
+  using B::eos;
+  using B::jac;
+  using B::P;
+  using B::press;
+  using B::residual;
+  using B::rho;
+  using B::rhobar;
+  using B::sie;
+  using B::temp;
+  using B::Tnorm;
+  using B::u;
+  using B::uscale;
+  using B::utotal_scale;
+  using B::vfrac;
+  static constexpr int n = N;
+  T dpdv[N], dedv[N], dpdT[N], vtemp[N];
+  T Tequil, Ttemp;
+  int ms;
+
+  SGX_HD void residual_eval() {
+    const T esum = sum_neumaier(u, n);
+    residual[0] = utotal_scale - esum;
+    int ires = 1;
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      if (m == ms) continue;
+      residual[ires++] = press[ms] - press[m];
+    }
+  }
+  SGX_HD T init() {
+    B::init_base();
+    if (P->exclude_idx >= 0) {
+      ms = P->exclude_idx;
+    } else {
+      ms = 0;
+      T xmax = 0;
+#pragma unroll
+      for (int m = 0; m < n; ++m) {
+        const T x = ratio(rhobar[m], B::rho_total);
+        if (x > xmax) {
+          xmax = x;
+          ms = m;
+        }
+      }
+    }
+    residual_eval();
+    Tequil = temp[0];
+    return B::residual_norm();
+  }
+  SGX_HD void fixup() {
+    if (P->exclude_idx < 0) {
+      T alphamax = 0;
+      ms = 0;
+#pragma unroll
+      for (int m = 0; m < n; ++m) {
+        if (vfrac[m] > alphamax) {
+          alphamax = vfrac[m];
+          ms = m;
+        }
+      }
+      residual_eval();
+    }
+  }
+  // CheckPTE (:1021-1040): {converged, acceptable}
+  SGX_HD void check(bool &conv, bool &acceptable) const {
+    T mean_p = 0;
+#pragma unroll
+    for (int m = 0; m < n; ++m)
+      mean_p += vfrac[m] * press[m];
+#if defined(__CUDA_ARCH__)
+    const T error_p = sqrt(sum_neumaier_sq(residual, n - 1, 1));
+#else
+    const T error_p = __builtin_sqrt(sum_neumaier_sq(residual, n - 1, 1));
+#endif
+    const T error_u = sabs(residual[0]);
+    const bool converged_p = (error_p < P->tol_p * sabs(mean_p) || error_p < P->abs_p);
+    const bool converged_u = (error_u < P->tol_e);
+    const bool acceptable_p =
+        (error_p < P->tol_p_suff * sabs(mean_p) || error_p < P->abs_p_suff);
+    const bool acceptable_u = (error_u < P->tol_e_suff);
+    conv = converged_p && converged_u;
+    acceptable = acceptable_p && acceptable_u;
+  }
+  SGX_HD void jacobian() {
+    T dedT_sum = 0.0;
+#pragma unroll
+    for (int m = 0; m < n; m++) {
+      const T dv = (vfrac[m] < T(0.5) ? T(1.0) : T(-1.0)) * vfrac[m] * P->derivative_eps;
+      const T vf_pert = vfrac[m] + dv;
+      const T rho_pert = ratio(rhobar[m], vf_pert);
+      T e_pert = B::e_of(m, rho_pert, Tnorm * Tequil);
+      T p_pert = ratio(B::p_pref(m, rho_pert, Tnorm * Tequil, e_pert), uscale);
+      dpdv[m] = smin(ratio((p_pert - press[m]), dv), -sabs(P->max_dpdv));
+      dedv[m] = ratio(rhobar[m] * ratio(e_pert, uscale) - u[m], dv);
+      const T dT = Tequil * P->derivative_eps;
+      e_pert = B::e_of(m, rho[m], Tnorm * (Tequil + dT));
+      p_pert = ratio(B::p_pref(m, rho[m], Tnorm * (Tequil + dT), e_pert), uscale);
+      dpdT[m] = ratio((p_pert - press[m]), dT);
+      dedT_sum += ratio(rhobar[m] * ratio(e_pert, uscale) - u[m], dT);
+    }
+#pragma unroll
+    for (int i = 0; i < n * n; ++i)
+      jac[i] = 0.0;
+    jac[0] = dedT_sum;
+    int col = 1;
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      if (m == ms) continue;
+      jac[col++] = dedv[m] - dedv[ms];
+    }
+    int row = 1;
+#pragma unroll
+    for (int m = 0; m < n; m++) {
+      if (m == ms) continue;
+      jac[row * n + 0] = dpdT[m] - dpdT[ms];
+      int c = 1;
+#pragma unroll
+      for (int mm = 0; mm < n; ++mm) {
+        if (mm == ms) continue;
+        jac[row * n + c] = (mm == m) ? dpdv[m] + dpdv[ms] : dpdv[ms];
+        c++;
+      }
+      row++;
+    }
+  }
+  SGX_HD T scale_dx() {
+    T scale = 1.0;
+    const T dalphaskip = -sum_neumaier(dx, n - 1, 1);
+    int idx = 1;
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      const T mydx = (m == ms) ? dalphaskip : dx[idx++];
+      if (scale * mydx < -P->vfrac_safety_fac * vfrac[m])
+        scale = smin(scale, sabs(P->vfrac_safety_fac * ratio(vfrac[m], mydx)));
+    }
+    const T Tnew = Tequil + scale * dx[0];
+    idx = 1;
+#pragma unroll
+    for (int m = 0; m < n; m++) {
+      const T rho_min = T(smax(ev_rho_pmin(*eos[m], double(Tnorm * Tequil)),
+                               ev_rho_pmin(*eos[m], double(Tnorm * Tnew))));
+      const T alpha_max = smin(T(1.0), ratio(rhobar[m], rho_min));
+      if (alpha_max < vfrac[m]) continue;
+      const T mydx = (m == ms) ? dalphaskip : dx[idx++];
+      if (scale * mydx > T(0.5) * (alpha_max - vfrac[m]))
+        scale = smin(ratio(T(0.5) * (alpha_max - vfrac[m]), mydx), scale);
+    }
+    if (scale * dx[0] < T(-0.95) * Tequil) scale = smin(scale, ratio(T(-0.95) * Tequil, dx[0]));
+#pragma unroll
+    for (int i = 0; i < n; ++i)
+      dx[i] *= scale;
+    return scale;
+  }
+  SGX_HD T test_update(const T scale, const bool cache_state = false) {
+    if (cache_state) {
+      Ttemp = Tequil;
+#pragma unroll
+      for (int m = 0; m < n; ++m)
+        vtemp[m] = vfrac[m];
+    }
+    Tequil = Ttemp + scale * dx[0];
+    int idx = 1;
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      if (ms == m) continue;
+      vfrac[m] = vtemp[m] + scale * dx[idx++];
+    }
+    vfrac[ms] = sum_neumaier(vfrac, n, 0, ms);
+    vfrac[ms] = 1 - vfrac[ms];
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      rho[m] = ratio(rhobar[m], vfrac[m]);
+      u[m] = rhobar[m] * B::e_of(m, rho[m], Tnorm * Tequil);
+      sie[m] = ratio(u[m], rhobar[m]);
+      u[m] = ratio(u[m], uscale);
+      temp[m] = Tequil;
+      press[m] = ratio(B::p_pref(m, rho[m], Tnorm * Tequil, sie[m]), uscale);
+    }
+    residual_eval();
+    return B::residual_norm();
+  }
+  // PTESolverBase::Finalize (:351-357)
+  SGX_HD void finalize() {
+#pragma unroll
+    for (int m = 0; m < n; m++) {
+      temp[m] *= Tnorm;
+      u[m] *= uscale;
+      press[m] *= uscale;
+    }
+  }
+};
+
+// ===========================================================================
+// PTESolverPT (:1207-1446)
+// ===========================================================================
+template <typename T, int N> struct PtePT : PteBase<T, N, 2> {
+  using B = PteBase<T, N, 2>;
+  using B::dx;
+  using B::eos;
+  using B::jac;
+  using B::lam;
+  using B::P;
+  using B::press;
+  using B::residual;
+  using B::rho;
+  using B::rhobar;
+  using B::sie;
+  using B::temp;
+  using B::Tnorm;
+  using B::u;
+  using B::uscale;
+  using B::utotal_scale;
+  using B::vfrac;
+  using B::vfrac_total;
+  static constexpr int n = N;
+  T Pequil, Tequil, Ptemp, Ttemp;
+  int ms = 0;
+
+  SGX_HD void rho_sie_PT(int m, T Pk, T Tk, T &r, T &s) {
+    double rr = double(r), ss = double(s);
+    ev_rho_sie_from_PT(*eos[m], double(Pk), double(Tk), rr, ss, lam[m], &this->err_flags);
+    r = T(rr);
+    s = T(ss);
+  }
+  SGX_HD void residual_eval() {
+    const T vsum = sum_neumaier(vfrac, n);
+    const T esum = sum_neumaier(u, n);
+    residual[0] = vfrac_total - vsum;
+    residual[1] = utotal_scale - esum;
+  }
+  SGX_HD T init() {
+    B::init_base();
+    residual_eval();
+    Pequil = 0;
+#pragma unroll
+    for (int m = 0; m < n; ++m)
+      Pequil += sabs(press[m]) * vfrac[m];
+    const T vsum = sum_neumaier(vfrac, n);
+    Pequil /= vsum;
+    Tequil = 1;
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      rho_sie_PT(m, Pequil * uscale, Tequil * Tnorm, rho[m], sie[m]);
+      vfrac[m] = ratio(rhobar[m], rho[m]);
+      u[m] = ratio(sie[m] * rhobar[m], uscale);
+      temp[m] = Tequil;
+    }
+    residual_eval();
+    return B::residual_norm();
+  }
+  SGX_HD void fixup() {}
+  SGX_HD void finalize() {
+#pragma unroll
+    for (int m = 0; m < n; m++) {
+      press[m] = Pequil * uscale;
+      temp[m] = Tequil * Tnorm;
+      u[m] *= uscale;
+    }
+  }
+  SGX_HD void check(bool &conv, bool &acceptable) const {
+    const T error_v = sabs(residual[0]);
+    const T error_u = sabs(residual[1]);
+    const bool converged_u = error_u < P->tol_e;
+    const bool converged_v = error_v < P->tol_v;
+    const bool acceptable_u = error_u < P->tol_e_suff;
+    const bool acceptable_v = error_v < P->tol_v_suff;
+    conv = converged_v && converged_u;
+    acceptable = acceptable_u && acceptable_v;
+  }
+  SGX_HD void jacobian() {
+    T dudT_P_sum = 0.0, dudP_T_sum = 0.0, rbor2_dr_dT_P_sum = 0.0, rbor2_dr_dP_T_sum = 0.0;
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      T r_pert = rho[m];
+      T e_pert = sie[m];
+      const T dp = -Pequil * P->derivative_eps;
+      rho_sie_PT(m, uscale * (Pequil + dp), Tnorm * Tequil, r_pert, e_pert);
+      const T drdp = ratio(r_pert - rho[m], dp);
+      const T dudp = ratio(ratio(rhobar[m] * e_pert, uscale) - u[m], dp);
+      rbor2_dr_dP_T_sum += ratio(rhobar[m], rho[m] * rho[m]) * drdp;
+      dudP_T_sum += dudp;
+      const T dT = Tequil * P->derivative_eps;
+      rho_sie_PT(m, uscale * Pequil, Tnorm * (Tequil + dT), r_pert, e_pert);
+      const T drdT = ratio(r_pert - rho[m], dT);
+      const T dudT = ratio(ratio(rhobar[m] * e_pert, uscale) - u[m], dT);
+      rbor2_dr_dT_P_sum += ratio(rhobar[m], rho[m] * rho[m]) * drdT;
+      dudT_P_sum += dudT;
+    }
+    jac[0] = -rbor2_dr_dT_P_sum;
+    jac[1] = -rbor2_dr_dP_T_sum;
+    jac[2] = dudT_P_sum;
+    jac[3] = dudP_T_sum;
+  }
+  SGX_HD T scale_dx() {
+    T scale = 1.0;
+    if (scale * dx[0] < T(-0.95) * Tequil) scale = ratio(T(-0.95) * Tequil, dx[0]);
+    auto bounded = [&](T Pbound, T delta) { return ratio(ratio(Pbound, uscale) - Pequil, delta); };
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      const T Pmin = T(ev_min_pressure(*eos[m]));
+      scale = smin(sabs(scale), sabs(T(0.95) * bounded(Pmin, dx[1])));
+    }
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      const T Ttest = (Tequil + scale * dx[0]) * Tnorm;
+      const T Pmax = T(ev_max_pressure_at_T(*eos[m], double(Ttest), &this->err_flags));
+      scale = smin(sabs(scale), sabs(T(0.95) * bounded(Pmax, dx[0])));
+    }
+    dx[0] *= scale;
+    dx[1] *= scale;
+    return scale;
+  }
+  SGX_HD T test_update(const T scale, const bool cache_state = false) {
+    if (cache_state) {
+      Ttemp = Tequil;
+      Ptemp = Pequil;
+    }
+    Tequil = Ttemp + scale * dx[0];
+    Pequil = Ptemp + scale * dx[1];
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      rho_sie_PT(m, Pequil * uscale, Tequil * Tnorm, rho[m], sie[m]);
+      vfrac[m] = ratio(rhobar[m], rho[m]);
+      u[m] = ratio(sie[m] * rhobar[m], uscale);
+      temp[m] = Tequil;
+      press[m] = Pequil;
+    }
+    residual_eval();
+    return B::residual_norm();
+  }
+};
+
+// ===========================================================================
+// PTESolver driver (:2188-2291)
+// ===========================================================================
+template <typename S, typename T> SGX_HD PteStatusLocal pte_solve(S &s) {
+  PteStatusLocal st;
+  T err = s.init();
+  const MixP<T> &params = *s.P;
+  bool converged = false, close_enough = false;
+  const int pte_max_iter = S::n * params.max_iter_per_mat;
+  int niter;
+  int max_line_niter = 0, small_step_iters = 0;
+  for (niter = 0; niter < pte_max_iter; ++niter) {
+    bool c, ce;
+    s.check(c, ce);
+    converged = c;
+    close_enough = ce;
+    if (converged) break;
+    s.jacobian();
+    if (!s.solve()) {
+      converged = false;
+      break;
+    }
+    T scale = smin(T(1.0), s.scale_dx());
+    if (sabs(scale) < params.small_step_thresh) small_step_iters++;
+    if (small_step_iters >= params.small_step_tries) {
+      converged = false;
+      break;
+    }
+    const T gradfdx = T(-2.0) * scale * err;
+    scale = 1.0;
+    const T err_old = err;
+    err = s.test_update(scale, true);
+    if (err > err_old + params.ls_alpha * gradfdx) {
+      scale = 0.5;
+      const T err_mid = s.test_update(scale);
+      if (err_mid < err && err_mid < err_old)
+        scale = T(0.75) + T(0.5) * ratio(err_mid - err, err - T(2.0) * err_mid + err_old);
+      for (int line_iter = 0; line_iter < params.ls_max_iter; line_iter++) {
+        err = s.test_update(scale);
+        if (err < err_old + params.ls_alpha * scale * gradfdx) break;
+        scale *= params.ls_fac;
+        max_line_niter = max_line_niter > line_iter ? max_line_niter : line_iter;
+      }
+    }
+    s.fixup();
+    if (((err > params.slow_thresh * err_old) || niter == pte_max_iter - 1) && close_enough) {
+      converged = true;
+      st.slow = true;
+      break;
+    }
+  }
+  s.fixup();
+  s.finalize();
+  st.residual = double(err);
+  st.niter = niter;
+  st.converged = converged;
+  st.max_line_niter = max_line_niter;
+  st.small_step_iters = small_step_iters;
+  return st;
+}
+
+} // namespace sgx

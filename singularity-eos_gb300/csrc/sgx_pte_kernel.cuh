@@ -1,0 +1,99 @@
+// The per-cell PTE kernel of the plain FP64 path, templated on the number of
+// materials N present in a cell. One launch per N covers the cells that hold
+// exactly N materials (the others return at once), so a warp never mixes
+// system sizes and each instantiation is compiled in its own translation unit.
+//
+// One thread per cell: gather the cell's materials, run PTESolverRhoT or
+// PTESolverPT + PTESolver() (closure/mixed_cell_models.hpp:884-1446,
+// 2188-2291), scatter the equilibrium state. get_sg_eos_rho_e.cpp:30-88 is
+// the reference's per-cell loop.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sgx_internal.h"
+#include "sgx_pte.cuh"
+
+namespace sgx {
+
+constexpr int PTE_BLOCK = 128;
+
+// Collects the present materials of cell i; returns their count.
+__device__ __forceinline__ int pte_gather(const PteArgs &a, long long i, int (&slot)[MAX_NMAT],
+                                          int (&eidx)[MAX_NMAT]) {
+  int n = 0;
+  for (int m = 0; m < a.nmat; ++m) {
+    const int ie = a.eos_idx ? a.eos_idx[static_cast<long long>(m) * a.ncell + i] : m;
+    if (ie < 0 || ie >= a.neos) continue;
+    slot[n] = m;
+    eidx[n] = ie;
+    ++n;
+  }
+  return n;
+}
+
+template <template <typename, int> class Solver, int N>
+__global__ void __launch_bounds__(PTE_BLOCK) pte_cell_kernel(const PteArgs a) {
+  __shared__ sgx_eos s_eos[MAX_EOS];
+  for (int k = threadIdx.x; k < a.neos; k += blockDim.x)
+    s_eos[k] = a.eos[k];
+  __syncthreads();
+  const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= a.ncell) return;
+  int slot[MAX_NMAT], eidx[MAX_NMAT];
+  if (pte_gather(a, i, slot, eidx) != N) return;
+  const MixP<double> mp(a.params);
+  const long long nc = a.ncell;
+  Solver<double, N> s;
+  double cache[N][3];
+  s.P = &mp;
+  s.vfrac_total = a.vfrac_tot[i];
+  s.sie_total = a.sie_tot[i];
+  s.Tnorm = 0.0;
+  s.err_flags = 0;
+  for (int q = 0; q < N; ++q) {
+    const long long k = static_cast<long long>(slot[q]) * nc + i;
+    s.eos[q] = &s_eos[eidx[q]];
+    s.rho[q] = a.rho[k];
+    s.vfrac[q] = a.vfrac[k];
+    s.sie[q] = a.sie[k];
+    s.temp[q] = a.temp[k];
+    s.press[q] = a.press[k];
+    for (int l = 0; l < 3; ++l)
+      cache[q][l] = a.lambda ? a.lambda[(static_cast<long long>(slot[q]) * 3 + l) * nc + i] : 0.0;
+    s.lam[q] = cache[q];
+  }
+  const PteStatusLocal st = pte_solve<Solver<double, N>, double>(s);
+  for (int q = 0; q < N; ++q) {
+    const long long k = static_cast<long long>(slot[q]) * nc + i;
+    a.rho[k] = s.rho[q];
+    a.vfrac[k] = s.vfrac[q];
+    a.sie[k] = s.sie[q];
+    a.temp[k] = s.temp[q];
+    a.press[k] = s.press[q];
+    if (a.lambda)
+      for (int l = 0; l < 3; ++l)
+        a.lambda[(static_cast<long long>(slot[q]) * 3 + l) * nc + i] = cache[q][l];
+  }
+  if (a.status) {
+    sgx_pte_status o;
+    o.residual = st.residual;
+    o.niter = st.niter;
+    o.converged = st.converged ? 1 : 0;
+    o.slow_convergence_detected = st.slow ? 1 : 0;
+    o.max_line_niter = static_cast<uint8_t>(st.max_line_niter);
+    o.small_step_iters = static_cast<uint8_t>(st.small_step_iters | (s.err_flags ? 0x80 : 0));
+    a.status[i] = o;
+  }
+}
+
+template <int N> cudaError_t launch_pte_fp64_n(const PteArgs &a, cudaStream_t stream) {
+  const long long blocks = (a.ncell + PTE_BLOCK - 1) / PTE_BLOCK;
+  if (a.solver == SGX_PTE_PT)
+    pte_cell_kernel<PtePT, N><<<static_cast<unsigned>(blocks), PTE_BLOCK, 0, stream>>>(a);
+  else
+    pte_cell_kernel<PteRhoT, N><<<static_cast<unsigned>(blocks), PTE_BLOCK, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+} // namespace sgx

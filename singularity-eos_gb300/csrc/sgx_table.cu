@@ -1,0 +1,508 @@
+// Host side of table residency.
+//
+// sp5-lite is this project's flat binary stand-in for the reference's SP5
+// HDF5 files (HDF5 is not a dependency here). Layout, little endian:
+//   char magic[8] = "SGXSP5L\0"; u32 version = 1; u32 nrecords;
+//   record: u32 kind (1 attr f64, 2 attr i32, 3 dataset f64, 4 attr string);
+//           u32 len, char path[len]; u32 len, char name[len];
+//           kind 1: f64; kind 2: i32; kind 4: u32 len, bytes;
+//           kind 3: u32 rank, per dim (fastest first) i32 n, f64 min, f64 max,
+//                   then f64 data[prod n] in C order (fastest index last).
+// Group and field names are the reference's SP5 keys
+// (base/sp5/singularity_eos_sp5.hpp:20-75).
+//
+// The derivation restates SpinerEOSDependsRhoT::loadDataboxes_
+// (eos/eos_spiner_rho_temp.hpp:545-687): fixBulkModulus_ (:689-714),
+// setlTColdCrit_ (:716-775), SetRhoPMin (eos_spiner_common.hpp:59-109) and the
+// cold-curve / maximum-temperature 1-D tables, using the same interpolation
+// functions the kernels use (sgx_spiner.cuh). Host code here is compiled
+// without floating-point contraction, so the derived tables equal the
+// reference's bit for bit.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/sgx.h"
+#include "sgx_spiner.cuh"
+#include "sgx_table.h"
+
+namespace sgx {
+
+namespace {
+
+struct Dataset {
+  std::vector<int> n;
+  std::vector<double> mn, mx;
+  std::vector<double> data;
+};
+struct Sp5 {
+  std::map<std::string, double> f64;
+  std::map<std::string, int> i32;
+  std::map<std::string, Dataset> ds;
+};
+
+bool read_sp5(const char *path, Sp5 &s, std::string &msg) {
+  FILE *f = std::fopen(path, "rb");
+  if (!f) {
+    msg = std::string("cannot open ") + path;
+    return false;
+  }
+  auto rd = [&](void *p, size_t n) { return std::fread(p, 1, n, f) == n; };
+  auto rdstr = [&](std::string &str) {
+    uint32_t len;
+    if (!rd(&len, 4) || len > (1u << 20)) return false;
+    str.resize(len);
+    return len == 0 || rd(&str[0], len);
+  };
+  char magic[8];
+  uint32_t version = 0, nrec = 0;
+  bool ok = rd(magic, 8) && std::memcmp(magic, "SGXSP5L", 8) == 0 && rd(&version, 4) &&
+            version == 1 && rd(&nrec, 4);
+  for (uint32_t k = 0; ok && k < nrec; ++k) {
+    uint32_t kind;
+    std::string p, name;
+    ok = rd(&kind, 4) && rdstr(p) && rdstr(name);
+    if (!ok) break;
+    const std::string key = p + "@" + name;
+    if (kind == 1) {
+      double v;
+      ok = rd(&v, 8);
+      s.f64[key] = v;
+    } else if (kind == 2) {
+      int32_t v;
+      ok = rd(&v, 4);
+      s.i32[key] = v;
+    } else if (kind == 4) {
+      std::string v;
+      ok = rdstr(v);
+    } else if (kind == 3) {
+      uint32_t rank;
+      ok = rd(&rank, 4) && rank >= 1 && rank <= 3;
+      Dataset d;
+      size_t total = 1;
+      for (uint32_t r = 0; ok && r < rank; ++r) {
+        int32_t n;
+        double a, b;
+        ok = rd(&n, 4) && rd(&a, 8) && rd(&b, 8) && n >= 2 && n <= (1 << 20);
+        d.n.push_back(n);
+        d.mn.push_back(a);
+        d.mx.push_back(b);
+        total *= static_cast<size_t>(n);
+      }
+      if (ok && total > (size_t(1) << 31)) ok = false;
+      if (ok) {
+        d.data.resize(total);
+        ok = rd(d.data.data(), total * 8);
+      }
+      s.ds[p] = std::move(d);
+    } else {
+      ok = false;
+    }
+  }
+  std::fclose(f);
+  if (!ok) msg = std::string("malformed sp5-lite image ") + path;
+  return ok;
+}
+
+Grid1D make_grid(double mn, double mx, int n) {
+  Grid1D g;
+  g.min = mn;
+  g.max = mx;
+  g.dx = (mx - mn) / static_cast<double>(n - 1);
+  g.inv_dx = 1 / g.dx;
+  g.n = n;
+  g.pad = 0;
+  return g;
+}
+
+// Host copy of a loaded table: owning storage plus a SpinerTable whose
+// pointers refer to it (used to run the shared interpolation code on host).
+struct HostTable {
+  int nRho = 0, nT = 0;
+  std::vector<double> f2[NF2D];
+  std::vector<double> f1[NF1D];
+  SpinerTable t{};
+  void bind() {
+    for (int k = 0; k < NF2D; ++k)
+      t.f2[k] = f2[k].data();
+    for (int k = 0; k < NF1D; ++k)
+      t.f1[k] = f1[k].data();
+  }
+};
+
+struct Resident {
+  void *dev = nullptr;
+  size_t bytes = 0;
+  int device = 0;
+  HostTable host;
+};
+std::mutex g_mu;
+std::map<uint64_t, Resident> g_tables;
+
+constexpr double VAPOR_DPDR_THRESH = 1e-8;
+
+// setlTColdCrit_ (eos_spiner_rho_temp.hpp:716-775) for one density node.
+double cold_crit(const HostTable &h, int j, const Grid1D &gCold) {
+  const SpinerTable &t = h.t;
+  const double lRho = gCold.x(j);
+  const double sieCold = interp1(gCold, t.f1[F_SIECOLD], lRho);
+  std::vector<int> crossings;
+  int last_pos_crossing = -1;
+  for (int i = 0; i < h.nT - 1; i++) {
+    const double sign_curr = h.f2[F_SIE][j * h.nT + i] - sieCold;
+    const double sign_next = h.f2[F_SIE][j * h.nT + i + 1] - sieCold;
+    if (sign_curr < 0 && sign_next > 0) {
+      crossings.push_back(i);
+      last_pos_crossing = static_cast<int>(crossings.size()) - 1;
+    } else if (sign_curr > 0 && sign_next < 0) {
+      crossings.push_back(i);
+    }
+  }
+  double lTc;
+  if (last_pos_crossing <= 0) {
+    lTc = t.lTMin;
+  } else {
+    const int ilast = crossings[last_pos_crossing];
+    const double lTlower = t.gT.x(ilast) - 1.0e-14;
+    const double lTupper = t.gT.x(ilast + 1) + 1.0e-14;
+    const double lTGuess = 0.5 * (lTlower + lTupper);
+    auto sieFunc = [&](const double x) { return interp2(t, t.f2[F_SIE], lRho, x); };
+    double lT = lTGuess;
+    if (regula_falsi(sieFunc, sieCold, lTGuess, lTlower, lTupper, SP_ROOT_THRESH, SP_ROOT_THRESH,
+                     lT) != RootStatus::SUCCESS)
+      lT = lTGuess;
+    lTc = lT;
+  }
+  return smax(t.lTMin, lTc);
+}
+
+} // namespace
+
+double gruneisen_compute_rho_max(double s1, double s2, double s3, double rho0, int *err) {
+  const double EPS = lim<double>::eps;
+  auto poly = [=](double eta) { return 1 - s1 * eta - s2 * (eta * eta) - s3 * (eta * (eta * eta)); };
+  auto near0 = [](double v, double tol) { return std::fabs(v) < tol; };
+  double root = -1.;
+  if (near0(s2, EPS) && near0(s3, EPS) && s1 > 1.) {
+    root = 1. / s1;
+  } else if (near0(s3, EPS) && !near0(s2, EPS)) {
+    const double disc = (s1 * s1) + 4. * s2;
+    if (disc < 0.) {
+      root = -1.;
+    } else {
+      const double r1 = (s1 + std::sqrt(disc)) / (-2. * s2);
+      const double r2 = (s1 - std::sqrt(disc)) / (-2. * s2);
+      const double lo = std::min(r1, r2), hi = std::max(r1, r2);
+      root = (lo > 0. && lo < 1.) ? lo : ((hi > 0. && hi < 1.) ? hi : -INFINITY);
+    }
+  } else if (!near0(s3, EPS)) {
+    const double ms2 = -s2;
+    const double disc = -18. * s3 * s2 * s1 - 4. * (ms2 * (ms2 * ms2)) + (s2 * s2) * (s1 * s1) -
+                        4. * s3 * (s1 * (s1 * s1)) - 27. * (s3 * s3);
+    double minbound = 0., maxbound = 1.;
+    if (disc >= 0) {
+      const double e1 = (s2 + std::sqrt((s2 * s2) - 3. * s3 * s1)) / (-3. * s3);
+      const double e2 = (s2 - std::sqrt((s2 * s2) - 3. * s3 * s1)) / (-3. * s3);
+      const double mn = std::min(e1, e2), mx = std::max(e1, e2);
+      if (s3 < 0.) {
+        minbound = std::max(mn, minbound);
+        maxbound = std::min(std::max(mx, minbound), maxbound);
+      } else if (mn > 0) {
+        maxbound = std::min(mn, maxbound);
+      }
+    }
+    if (poly(minbound) * poly(maxbound) < 0.) {
+      const double xtol = 100 * EPS, ytol = 100. / 10 * EPS;
+      if (regula_falsi(poly, 0., 0.001, minbound, maxbound, xtol, ytol, root) !=
+          RootStatus::SUCCESS) {
+        if (err) *err = 1;
+      }
+    } else if (near0(poly(minbound), EPS)) {
+      root = minbound;
+    } else if (near0(poly(maxbound), EPS)) {
+      root = maxbound;
+    } else {
+      root = -1.;
+    }
+  }
+  if (root > 0. && root < 1.) return rho0 / ((1 - root) + EPS);
+  return INFINITY;
+}
+
+int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *handle,
+                      std::string &msg) {
+  Sp5 s;
+  if (!read_sp5(path, s, msg)) return SGX_ERR_IO;
+  const int lt = s.i32.count("/@log_type") ? s.i32["/@log_type"] : 1;
+  if (lt != 2) {
+    msg = "sp5-lite image was written with a log type other than NQT order 2";
+    return SGX_ERR_IO;
+  }
+  const std::string mat = "/" + std::to_string(matid);
+  const std::string lTg = mat + "/dependsLogRhoLogT/";
+  const std::string cg = mat + "/coldCurve/";
+  const char *names2[NF2D] = {"pressure", "specific internal energy", "bulk modulus",
+                              "dPdRho",   "dPdE",                     "dTdRho",
+                              "dTdE",     "dEdRho",                   "dEdT"};
+  HostTable h;
+  SpinerTable &t = h.t;
+  std::memset(&t, 0, sizeof(t));
+  for (int k = 0; k < NF2D; ++k) {
+    auto it = s.ds.find(lTg + names2[k]);
+    if (it == s.ds.end() || it->second.n.size() != 2) {
+      msg = "missing 2-D field " + lTg + names2[k];
+      return SGX_ERR_IO;
+    }
+    if (k == 0) {
+      h.nT = it->second.n[0];
+      h.nRho = it->second.n[1];
+      t.gT = make_grid(it->second.mn[0], it->second.mx[0], h.nT);
+      t.gRho = make_grid(it->second.mn[1], it->second.mx[1], h.nRho);
+    } else if (it->second.n[0] != h.nT || it->second.n[1] != h.nRho) {
+      msg = "inconsistent 2-D field shapes";
+      return SGX_ERR_IO;
+    }
+    h.f2[k] = it->second.data;
+  }
+  const char *namesc[4] = {"pressure", "specific internal energy", "bulk modulus", "dPdRho"};
+  const int slotc[4] = {F_PCOLD, F_SIECOLD, F_BMODCOLD, F_DPDRHOCOLD};
+  for (int k = 0; k < 4; ++k) {
+    auto it = s.ds.find(cg + namesc[k]);
+    if (it == s.ds.end() || it->second.n.size() != 1 || it->second.n[0] != h.nRho) {
+      msg = "missing or misshapen cold-curve field " + cg + namesc[k];
+      return SGX_ERR_IO;
+    }
+    if (k == 0) t.gCold = make_grid(it->second.mn[0], it->second.mx[0], it->second.n[0]);
+    h.f1[slotc[k]] = it->second.data;
+  }
+  auto attr = [&](const char *name, double &v) {
+    auto it = s.f64.find(mat + "@" + name);
+    if (it == s.f64.end()) return false;
+    v = it->second;
+    return true;
+  };
+  double rOff = 0, tOff = 0;
+  if (!attr("rhoOffset", rOff) || !attr("TOffset", tOff)) {
+    msg = "missing offsets on " + mat;
+    return SGX_ERR_IO;
+  }
+  t.nRho = h.nRho;
+  t.nT = h.nT;
+  t.lRhoOffset = std::fabs(rOff);
+  t.lTOffset = std::fabs(tOff);
+  t.reproducible = reproducible ? 1 : 0;
+  for (int k = 0; k < NF1D; ++k)
+    if (h.f1[k].empty()) h.f1[k].assign(k == F_RHO_AT_PMIN ? h.nT : h.nRho, 0.0);
+  h.bind();
+  // set bounds (:601-608)
+  t.lRhoMin = t.gRho.min;
+  t.lRhoMax = t.gRho.max;
+  t.rhoMax = from_log(t.lRhoMax, t.lRhoOffset);
+  t.lTMin = t.gT.min;
+  t.lTMax = t.gT.max;
+  t.TMax = from_log(t.lTMax, t.lTOffset);
+  const int nR = h.nRho, nT = h.nT;
+  // fixBulkModulus_ (:689-714)
+  for (int j = 0; j < nR; j++) {
+    const double lRho = t.gRho.x(j);
+    const double rho = sp_rho(t, lRho);
+    for (int i = 0; i < nT; i++) {
+      const double lT = t.gT.x(i);
+      const double press = interp2(t, t.f2[F_P], lRho, lT);
+      const double DPDR_E = interp2(t, t.f2[F_DPDRHO], lRho, lT);
+      const double DPDE_R = interp2(t, t.f2[F_DPDE], lRho, lT);
+      const double DEDR_T = interp2(t, t.f2[F_DEDRHO], lRho, lT);
+      const double DPDR_T = DPDR_E + DPDE_R * DEDR_T;
+      double bMod;
+      if (DPDE_R > 0.0 && rho > 0.0)
+        bMod = rho * DPDR_E + DPDE_R * (press / rho);
+      else if (rho > 0.0)
+        bMod = smax(rho * DPDR_T, 0.0);
+      else
+        bMod = 0.0;
+      h.f2[F_BMOD][j * nT + i] = smax(bMod, std::fabs(lim<double>::eps));
+    }
+  }
+  // setlTColdCrit_ (:716-775)
+  for (int j = 0; j < nR; j++)
+    h.f1[F_LTCOLDCRIT][j] = cold_crit(h, j, t.gCold);
+  // SetRhoPMin without vapor-dome exclusion (eos_spiner_common.hpp:59-109)
+  double PMin = DBL_MAX;
+  for (int i = 0; i < nT; ++i) {
+    double PMin_at_T = DBL_MAX;
+    int jmax = 0;
+    for (int j = 0; j < nR; ++j) {
+      if (h.f2[F_P][j * nT + i] < PMin_at_T) {
+        PMin_at_T = h.f2[F_P][j * nT + i];
+        jmax = j;
+      }
+    }
+    if (PMin_at_T > 0) {
+      h.f1[F_RHO_AT_PMIN][i] = 0;
+      PMin_at_T = 0;
+    } else {
+      h.f1[F_RHO_AT_PMIN][i] = from_log(t.gRho.x(jmax), t.lRhoOffset);
+    }
+    PMin = smin(PMin_at_T, PMin);
+  }
+  (void)VAPOR_DPDR_THRESH;
+  t.PMin = PMin;
+  // cold-curve derived tables (:629-643)
+  for (int j = 0; j < nR; j++) {
+    const double lRho = t.gCold.x(j);
+    const double lT = h.f1[F_LTCOLDCRIT][j];
+    h.f1[F_BMODCOLD][j] = interp2(t, t.f2[F_BMOD], lRho, lT);
+    h.f1[F_DPDECOLD][j] = interp2(t, t.f2[F_DPDE], lRho, lT);
+    h.f1[F_DTDRHOCOLD][j] = interp2(t, t.f2[F_DTDRHO], lRho, lT);
+    h.f1[F_DTDECOLD][j] = interp2(t, t.f2[F_DTDE], lRho, lT);
+    h.f1[F_DEDTCOLD][j] = interp2(t, t.f2[F_DEDT], lRho, lT);
+  }
+  // maximum-temperature 1-D tables (:645-656)
+  for (int j = 0; j < nR; j++) {
+    const double lRho = t.gRho.x(j);
+    const double rho = sp_rho(t, lRho);
+    h.f1[F_PMAX][j] = h.f2[F_P][j * nT + nT - 1];
+    h.f1[F_DEDTMAX][j] = h.f2[F_DEDT][j * nT + nT - 1];
+    h.f1[F_GM1MAX][j] = ratio(h.f2[F_DPDE][j * nT + nT - 1], rho);
+    h.f1[F_SIELTMAX][j] = h.f2[F_SIE][j * nT + nT - 1];
+  }
+
+  // ---- device image ----
+  auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+  const size_t ncell = static_cast<size_t>(nR - 1) * (nT - 1);
+  size_t off = align(sizeof(SpinerTable));
+  size_t off2[NF2D], off1[NF1D], offq[3], offf;
+  for (int k = 0; k < NF2D; ++k) {
+    off2[k] = off;
+    off = align(off + h.f2[k].size() * 8);
+  }
+  for (int k = 0; k < NF1D; ++k) {
+    off1[k] = off;
+    off = align(off + h.f1[k].size() * 8);
+  }
+  for (int k = 0; k < 3; ++k) {
+    offq[k] = off;
+    off = align(off + ncell * sizeof(dq4));
+  }
+  offf = off;
+  off = align(off + ncell * sizeof(fq4));
+  const size_t bytes = off;
+  std::vector<unsigned char> img(bytes, 0);
+  for (int k = 0; k < NF2D; ++k)
+    std::memcpy(img.data() + off2[k], h.f2[k].data(), h.f2[k].size() * 8);
+  for (int k = 0; k < NF1D; ++k)
+    std::memcpy(img.data() + off1[k], h.f1[k].data(), h.f1[k].size() * 8);
+  const int qsrc[3] = {F_SIE, F_P, F_BMOD};
+  for (int k = 0; k < 3; ++k) {
+    unsigned char *q = img.data() + offq[k];
+    const std::vector<double> &f = h.f2[qsrc[k]];
+    for (int j = 0; j < nR - 1; ++j)
+      for (int i = 0; i < nT - 1; ++i) {
+        const double c[4] = {f[j * nT + i], f[j * nT + i + 1], f[(j + 1) * nT + i],
+                             f[(j + 1) * nT + i + 1]};
+        std::memcpy(q + (static_cast<size_t>(j) * (nT - 1) + i) * sizeof(dq4), c, sizeof(c));
+      }
+  }
+  {
+    unsigned char *q = img.data() + offf;
+    const std::vector<double> &f = h.f2[F_SIE];
+    for (int j = 0; j < nR - 1; ++j)
+      for (int i = 0; i < nT - 1; ++i) {
+        const float c[4] = {static_cast<float>(f[j * nT + i]), static_cast<float>(f[j * nT + i + 1]),
+                            static_cast<float>(f[(j + 1) * nT + i]),
+                            static_cast<float>(f[(j + 1) * nT + i + 1])};
+        std::memcpy(q + (static_cast<size_t>(j) * (nT - 1) + i) * sizeof(fq4), c, sizeof(c));
+      }
+  }
+  void *dev = nullptr;
+  cudaError_t e = cudaMalloc(&dev, bytes);
+  if (e != cudaSuccess) {
+    msg = std::string("cudaMalloc of table: ") + cudaGetErrorString(e);
+    return SGX_ERR_CUDA;
+  }
+  unsigned char *d = static_cast<unsigned char *>(dev);
+  SpinerTable td = t;
+  for (int k = 0; k < NF2D; ++k)
+    td.f2[k] = reinterpret_cast<const double *>(d + off2[k]);
+  for (int k = 0; k < NF1D; ++k)
+    td.f1[k] = reinterpret_cast<const double *>(d + off1[k]);
+  td.sie4 = reinterpret_cast<const dq4 *>(d + offq[0]);
+  td.P4 = reinterpret_cast<const dq4 *>(d + offq[1]);
+  td.bmod4 = reinterpret_cast<const dq4 *>(d + offq[2]);
+  td.sie4f = reinterpret_cast<const fq4 *>(d + offf);
+  std::memcpy(img.data(), &td, sizeof(td));
+  e = cudaMemcpy(dev, img.data(), bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(dev);
+    msg = std::string("cudaMemcpy of table: ") + cudaGetErrorString(e);
+    return SGX_ERR_CUDA;
+  }
+  Resident r;
+  r.dev = dev;
+  r.bytes = bytes;
+  cudaGetDevice(&r.device);
+  r.host = std::move(h);
+  r.host.bind();
+  const uint64_t key = reinterpret_cast<uint64_t>(dev);
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_tables[key] = std::move(r);
+    g_tables[key].host.bind();
+  }
+  *handle = key;
+  return SGX_OK;
+}
+
+int table_free(uint64_t handle, std::string &msg) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_tables.find(handle);
+  if (it == g_tables.end()) {
+    msg = "sgx_eos_finalize: unknown table (already finalized?)";
+    return SGX_ERR_INVALID;
+  }
+  cudaFree(it->second.dev);
+  g_tables.erase(it);
+  return SGX_OK;
+}
+
+size_t table_bytes(uint64_t handle) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_tables.find(handle);
+  return it == g_tables.end() ? 0 : it->second.bytes;
+}
+
+long table_dump(uint64_t handle, double *out, long cap) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_tables.find(handle);
+  if (it == g_tables.end()) return -1;
+  const HostTable &h = it->second.host;
+  // DBLIST order (eos_spiner_rho_temp.hpp:253-257); mF_ is empty.
+  std::vector<const std::vector<double> *> order;
+  for (int k = 0; k < NF2D; ++k)
+    order.push_back(&h.f2[k]);
+  const int o1[] = {F_PMAX,     F_SIELTMAX,   F_DEDTMAX,   F_GM1MAX,    F_LTCOLDCRIT,
+                    F_PCOLD,    F_SIECOLD,    F_BMODCOLD,  F_DPDRHOCOLD, F_DPDECOLD,
+                    F_DTDRHOCOLD, F_DTDECOLD, F_DEDTCOLD,  F_RHO_AT_PMIN};
+  for (int k : o1)
+    order.push_back(&h.f1[k]);
+  long total = 0;
+  for (auto *v : order)
+    total += static_cast<long>(v->size());
+  if (out && cap >= total) {
+    long o = 0;
+    for (auto *v : order) {
+      std::memcpy(out + o, v->data(), v->size() * 8);
+      o += static_cast<long>(v->size());
+    }
+  }
+  return total;
+}
+
+} // namespace sgx

@@ -1,0 +1,24 @@
+// Table residency: the sp5-lite reader, the load-time table derivation of
+// SpinerEOSDependsRhoT, and the registry of device table images.
+#pragma once
+
+#include <cstdint>
+#include <string>
+
+namespace sgx {
+
+// Loads /<matid>/dependsLogRhoLogT and /<matid>/coldCurve from an sp5-lite
+// image, derives the load-time tables and uploads the image to the current
+// device. *handle receives the device address of the table header.
+int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *handle,
+                      std::string &msg);
+int table_free(uint64_t handle, std::string &msg);
+size_t table_bytes(uint64_t handle);
+// Derived tables in the reference's DBLIST order; returns the count or -1.
+long table_dump(uint64_t handle, double *out, long cap);
+
+// Gruneisen::ComputeRhoMax (eos_gruneisen.hpp:231-329), without the 0.99
+// safety factor.
+double gruneisen_compute_rho_max(double s1, double s2, double s3, double rho0, int *err);
+
+} // namespace sgx

@@ -1,0 +1,181 @@
+"""ctypes binding of libsgx.so (include/sgx.h).
+
+Device arrays are passed as torch CUDA tensors (torch is used for device
+memory and streams only); every call goes through the C ABI. Loading fails
+loudly when the library has not been built -- there is no fallback.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(HERE), "lib", "libsgx.so")
+
+IDEAL_GAS, STIFF_GAS, NOBLE_ABEL, GRUNEISEN, SPINER_RHOT, HELMHOLTZ = 1, 2, 3, 4, 5, 6
+Q_DENSITY, Q_SIE, Q_PRESSURE, Q_TEMPERATURE, Q_SPECIFIC_HEAT, Q_BULK_MODULUS = 1, 2, 4, 8, 16, 32
+(FN_T_FROM_RHO_SIE, FN_SIE_FROM_RHO_T, FN_P_FROM_RHO_T, FN_P_FROM_RHO_SIE, FN_CV_FROM_RHO_T,
+ FN_CV_FROM_RHO_SIE, FN_B_FROM_RHO_T, FN_B_FROM_RHO_SIE, FN_G_FROM_RHO_T, FN_G_FROM_RHO_SIE,
+ FN_MIN_SIE_FROM_RHO) = range(11)
+PTE_RHOT, PTE_PT = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+
+EXPORTED = [
+    "sgx_version", "sgx_last_error", "sgx_eos_ideal_gas", "sgx_eos_stiff_gas",
+    "sgx_eos_noble_abel", "sgx_eos_gruneisen", "sgx_eos_spiner_rhot", "sgx_eos_finalize",
+    "sgx_eos_table_bytes", "sgx_eos_spiner_dump", "sgx_eos_eval", "sgx_eos_fill",
+    "sgx_mix_params_default", "sgx_pte_rhot_required_scratch", "sgx_pte_pt_required_scratch",
+    "sgx_pte_solve",
+]
+
+
+class SgxEos(C.Structure):
+    _fields_ = [("type", C.c_int32), ("flags", C.c_int32), ("table", C.c_uint64),
+                ("p", C.c_double * 14)]
+
+
+class MixParams(C.Structure):
+    _fields_ = [
+        ("verbose", C.c_int32), ("iterate_t_guess", C.c_int32),
+        ("derivative_eps", C.c_double), ("pte_rel_tolerance_p", C.c_double),
+        ("pte_rel_tolerance_t", C.c_double), ("pte_rel_tolerance_e", C.c_double),
+        ("pte_rel_tolerance_v", C.c_double), ("pte_abs_tolerance_p", C.c_double),
+        ("pte_abs_tolerance_t", C.c_double), ("pte_slow_convergence_thresh", C.c_double),
+        ("pte_rel_tolerance_p_sufficient", C.c_double),
+        ("pte_rel_tolerance_t_sufficient", C.c_double),
+        ("pte_rel_tolerance_e_sufficient", C.c_double),
+        ("pte_rel_tolerance_v_sufficient", C.c_double),
+        ("pte_abs_tolerance_p_sufficient", C.c_double),
+        ("pte_abs_tolerance_t_sufficient", C.c_double),
+        ("pte_max_iter_per_mat", C.c_int64), ("line_search_alpha", C.c_double),
+        ("line_search_max_iter", C.c_int64), ("line_search_fac", C.c_double),
+        ("vfrac_safety_fac", C.c_double), ("temperature_limit", C.c_double),
+        ("default_tguess", C.c_double), ("min_dtde", C.c_double),
+        ("pte_small_step_tries", C.c_int64), ("pte_small_step_thresh", C.c_double),
+        ("pte_max_dpdv", C.c_double), ("pte_reduced_system_exclude_idx", C.c_int64),
+    ]
+
+
+class PteStatus(C.Structure):
+    _fields_ = [("residual", C.c_double), ("niter", C.c_int32), ("converged", C.c_uint8),
+                ("slow_convergence_detected", C.c_uint8), ("max_line_niter", C.c_uint8),
+                ("small_step_iters", C.c_uint8)]
+
+
+_lib = None
+
+
+def load():
+    """Loads libsgx.so (built by singularity-eos_gb300/build.py)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"libsgx.so not built ({LIB_PATH}); run __graft_entry__.build()")
+    lib = C.CDLL(LIB_PATH)
+    P, I, D, V, U64 = C.c_void_p, C.c_int, C.c_double, C.c_void_p, C.c_uint64
+    lib.sgx_version.restype = C.c_char_p
+    lib.sgx_last_error.restype = C.c_char_p
+    lib.sgx_eos_ideal_gas.argtypes = [C.POINTER(SgxEos), D, D]
+    lib.sgx_eos_stiff_gas.argtypes = [C.POINTER(SgxEos), D, D, D, D]
+    lib.sgx_eos_noble_abel.argtypes = [C.POINTER(SgxEos), D, D, D, D]
+    lib.sgx_eos_gruneisen.argtypes = [C.POINTER(SgxEos)] + [D] * 11
+    lib.sgx_eos_spiner_rhot.argtypes = [C.POINTER(SgxEos), C.c_char_p, I, I]
+    lib.sgx_eos_finalize.argtypes = [C.POINTER(SgxEos)]
+    lib.sgx_eos_table_bytes.argtypes = [C.POINTER(SgxEos)]
+    lib.sgx_eos_table_bytes.restype = C.c_size_t
+    lib.sgx_eos_spiner_dump.argtypes = [C.POINTER(SgxEos), P, C.c_long]
+    lib.sgx_eos_spiner_dump.restype = C.c_long
+    lib.sgx_eos_eval.argtypes = [C.POINTER(SgxEos), I, C.c_int64, P, P, P, P, I, P]
+    lib.sgx_eos_fill.argtypes = [C.POINTER(SgxEos), C.c_int64, P, P, P, P, P, P, C.c_uint32,
+                                 P, I, P]
+    lib.sgx_mix_params_default.argtypes = [C.POINTER(MixParams)]
+    lib.sgx_pte_solve.argtypes = [I, I, C.c_int64, P, I, P, P, P, P, P, P, P, P, P,
+                                  C.POINTER(MixParams), P, I, P]
+    _lib = lib
+    return lib
+
+
+def check(rc):
+    if rc != 0:
+        raise RuntimeError(f"sgx error {rc}: {load().sgx_last_error().decode()}")
+
+
+def ptr(t):
+    """Device address of a torch tensor (or None)."""
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def stream_ptr(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def make_eos(kind, params):
+    """An sgx_eos value from (model code, parameters) as in sgx.workloads."""
+    lib = load()
+    e = SgxEos()
+    p = list(params)
+    if kind == IDEAL_GAS:
+        check(lib.sgx_eos_ideal_gas(C.byref(e), *p[:2]))
+    elif kind == STIFF_GAS:
+        check(lib.sgx_eos_stiff_gas(C.byref(e), *p[:4]))
+    elif kind == NOBLE_ABEL:
+        check(lib.sgx_eos_noble_abel(C.byref(e), *p[:4]))
+    elif kind == GRUNEISEN:
+        rho_max = p[10] if len(p) > 10 else 0.0
+        check(lib.sgx_eos_gruneisen(C.byref(e), *p[:10], rho_max))
+    else:
+        raise ValueError(f"use spiner_eos() for model {kind}")
+    return e
+
+
+def spiner_eos(path, matid, reproducible=False):
+    lib = load()
+    e = SgxEos()
+    check(lib.sgx_eos_spiner_rhot(C.byref(e), path.encode(), int(matid), int(reproducible)))
+    return e
+
+
+def mix_params(**kw):
+    m = MixParams()
+    check(load().sgx_mix_params_default(C.byref(m)))
+    for k, v in kw.items():
+        setattr(m, k, v)
+    return m
+
+
+def eval_eos(eos, fn, in1, in2, out, lam=None, lam_stride=0, stream=None):
+    n = in1.numel()
+    check(load().sgx_eos_eval(C.byref(eos), fn, n, ptr(in1), ptr(in2), ptr(out), ptr(lam),
+                              lam_stride, stream_ptr(stream)))
+
+
+def fill_eos(eos, rho, temp, sie, press, cv, bmod, output, lam=None, lam_stride=0, stream=None):
+    n = rho.numel()
+    check(load().sgx_eos_fill(C.byref(eos), n, ptr(rho), ptr(temp), ptr(sie), ptr(press),
+                              ptr(cv), ptr(bmod), output, ptr(lam), lam_stride,
+                              stream_ptr(stream)))
+
+
+def pte_solve(solver, eos_list, eos_idx, vfrac_tot, sie_tot, rho, vfrac, sie, temp, press,
+              lam=None, params=None, status=None, precision=PREC_FP64, stream=None):
+    """Per-cell PTE on device tensors; per-material tensors are [nmat, ncell]
+    float64 (updated in place); status is a uint8 tensor of ncell*16 bytes."""
+    nmat, ncell = rho.shape
+    arr = (SgxEos * len(eos_list))(*eos_list)
+    check(load().sgx_pte_solve(
+        solver, nmat, ncell, C.cast(arr, C.c_void_p), len(eos_list), ptr(eos_idx),
+        ptr(vfrac_tot), ptr(sie_tot), ptr(rho), ptr(vfrac), ptr(sie), ptr(temp), ptr(press),
+        ptr(lam), C.byref(params) if params is not None else None, ptr(status), precision,
+        stream_ptr(stream)))
+
+
+def status_view(status_u8):
+    """Splits a [ncell*16] uint8 status tensor (on host) into numpy fields."""
+    import numpy as np
+    raw = status_u8.cpu().numpy().view(np.uint8).reshape(-1, 16)
+    residual = raw[:, 0:8].copy().view(np.float64).ravel()
+    niter = raw[:, 8:12].copy().view(np.int32).ravel()
+    return dict(residual=residual, niter=niter, converged=raw[:, 12].astype(bool),
+                slow=raw[:, 13].astype(bool), max_line_niter=raw[:, 14],
+                small_step_iters=raw[:, 15] & 0x7F, error=(raw[:, 15] & 0x80) != 0)

@@ -1,0 +1,145 @@
+"""Generates the golden fixtures in this folder from the compiled reference.
+
+TEST INFRASTRUCTURE. Runs the reference's own hot-path code
+(oracle/_ref/libsgref.so, built by oracle/build_ref.sh from the reference
+sources with the shims in oracle/shims) on small seeded inputs and stores
+inputs and outputs as .npz. The GPU parity tests compare the CUDA library
+against these files on machines where the reference sources are absent.
+
+Usage: python tests/golden/make_golden.py
+"""
+import hashlib
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "singularity-eos_gb300"))
+
+import refbind as rb  # noqa: E402
+from sgx import sp5lite, workloads as W  # noqa: E402
+
+ALL_FN = list(range(11))
+Q_TPB = rb.Q_TEMPERATURE | rb.Q_PRESSURE | rb.Q_BULK_MODULUS | rb.Q_SPECIFIC_HEAT
+
+
+def desc(mat):
+    kind, params = mat
+    return rb.eos_desc(kind, params)
+
+
+def mats_array(materials):
+    """[n, 16] parameter rows with the model code in column 15."""
+    out = np.zeros((len(materials), 16))
+    for k, (kind, params) in enumerate(materials):
+        out[k, : len(params)] = params
+        out[k, 15] = kind
+    return out
+
+
+def pte_fixture(ref, wl, solver, params=None):
+    r = {k: wl[k].copy() for k in ("rho", "vfrac", "sie", "temp", "press")}
+    mp = ref.mix_params(**(params or {}))
+    conv, nit, res = ref.pte(solver, [desc(m) for m in wl["materials"]], wl["eos_idx"],
+                             wl["vfrac_tot"], wl["sie_tot"], r["rho"], r["vfrac"], r["sie"],
+                             r["temp"], r["press"], params=mp)
+    out = dict(materials=mats_array(wl["materials"]), vfrac_tot=wl["vfrac_tot"],
+               sie_tot=wl["sie_tot"], converged=conv, niter=nit, residual=res,
+               solver=np.int32(solver))
+    if wl["eos_idx"] is not None:
+        out["eos_idx"] = wl["eos_idx"]
+    for k in ("rho", "vfrac", "sie", "temp", "press"):
+        out["in_" + k] = wl[k]
+        out["out_" + k] = r[k]
+    for k, v in (params or {}).items():
+        out["param_" + k] = np.float64(v)
+    return out
+
+
+def vector_fixture(ref, materials, n=512, seed=11):
+    rng = np.random.default_rng(seed)
+    out = dict(materials=mats_array(materials))
+    for k, mat in enumerate(materials):
+        rho = np.exp(rng.uniform(np.log(1e-3), np.log(20.0), n))
+        sie = rng.uniform(1e8, 1e11, n)
+        T = np.exp(rng.uniform(np.log(50.0), np.log(1e5), n))
+        out[f"m{k}_rho"], out[f"m{k}_sie"], out[f"m{k}_T"] = rho, sie, T
+        d = desc(mat)
+        for fn in ALL_FN:
+            second = T if fn in (1, 2, 4, 6, 8) else sie
+            out[f"m{k}_fn{fn}"] = ref.eos_vec(d, fn, rho, second)
+    return out
+
+
+def spiner_fixture(ref, path, nq=4096, seed=5):
+    rho, sie = sp5lite.stiffgas_queries(nq, seed=seed)
+    d = rb.eos_desc(rb.SPINER_RHOT, [], path=path, matid=1)
+    out = dict(rho=rho, sie=sie)
+    T, P, cv, bm = (np.zeros(nq) for _ in range(4))
+    lam = np.full(2 * nq, np.nan)
+    ref.fill_eos(d, rho.copy(), T, sie.copy(), P, cv, bm, Q_TPB, lam=lam, lam_stride=2)
+    out.update(fill_T=T, fill_P=P, fill_cv=cv, fill_bmod=bm, fill_lambda=lam)
+    Tq = np.exp(np.random.default_rng(seed + 1).uniform(np.log(50.0), np.log(3e6), nq))
+    out["Tq"] = Tq
+    for fn in ALL_FN:
+        second = Tq if fn in (1, 2, 4, 6, 8) else sie
+        out[f"fn{fn}"] = ref.eos_vec(d, fn, rho, second)
+    dump, scal = ref.spiner_dump(path, 1)
+    # the full derived-table image is 4.7 MB: keep its hash and a strided sample
+    out["dump_sha256"] = np.array(hashlib.sha256(dump.tobytes()).hexdigest())
+    out["dump_len"] = np.int64(dump.size)
+    out["dump_sample"] = dump[::97].copy()
+    out["scal"] = scal
+    return out
+
+
+def main():
+    if not rb.have_reference():
+        sys.exit("oracle/_ref/libsgref.so not built; run oracle/build_ref.sh")
+    ref = rb.reference()
+    fx = {}
+    fx["pte_rhot_2mat"] = pte_fixture(ref, W.pte_two_material(2048, seed=101), 0)
+    fx["pte_rhot_2mat_tight"] = pte_fixture(
+        ref, W.pte_two_material(512, seed=102), 0,
+        dict(pte_rel_tolerance_p=1e-12, pte_rel_tolerance_e=1e-12,
+             pte_abs_tolerance_p=0.0, pte_rel_tolerance_p_sufficient=1e-10,
+             pte_rel_tolerance_e_sufficient=1e-10, pte_abs_tolerance_p_sufficient=0.0))
+    fx["pte_rhot_batched"] = pte_fixture(ref, W.pte_batched(2048, seed=103), 0)
+    fx["pte_pt_2mat"] = pte_fixture(ref, W.pte_two_material(1024, seed=104), 1)
+    wl = W.pte_batched(1024, seed=105)
+    wl["materials"] = wl["materials"][:7]  # ideal, stiff and Noble-Abel only
+    wl["eos_idx"] = np.where(wl["eos_idx"] == 7, 6, wl["eos_idx"]).astype(np.int32)
+    fx["pte_pt_batched"] = pte_fixture(ref, wl, 1)
+    fx["eos_vector"] = vector_fixture(
+        ref, [W.IDEAL_AIR, W.STIFF_WATER, W.NOBLE_ABEL_GAS, W.GRUNEISEN_CU])
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "stiffgas.sp5")
+        sp5lite.stiffgas_table(path)
+        sha = hashlib.sha256(open(path, "rb").read()).hexdigest()
+        fx["spiner_lookup"] = spiner_fixture(ref, path)
+        fx["spiner_lookup"]["table_sha256"] = np.array(sha)
+        # PTE with the tabulated material next to an ideal gas
+        wl = W.pte_two_material(512, seed=106)
+        wl["materials"] = [W.IDEAL_AIR, (rb.SPINER_RHOT, ())]
+        descs = [desc(W.IDEAL_AIR), rb.eos_desc(rb.SPINER_RHOT, [], path=path, matid=1)]
+        r = {k: wl[k].copy() for k in ("rho", "vfrac", "sie", "temp", "press")}
+        conv, nit, res = ref.pte(0, descs, None, wl["vfrac_tot"], wl["sie_tot"], r["rho"],
+                                 r["vfrac"], r["sie"], r["temp"], r["press"],
+                                 params=ref.mix_params())
+        o = dict(vfrac_tot=wl["vfrac_tot"], sie_tot=wl["sie_tot"], converged=conv, niter=nit,
+                 residual=res, table_sha256=np.array(sha))
+        for k in ("rho", "vfrac", "sie", "temp", "press"):
+            o["in_" + k] = wl[k]
+            o["out_" + k] = r[k]
+        fx["pte_rhot_spiner"] = o
+    for name, d in fx.items():
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+        print(name, {k: getattr(v, "shape", None) for k, v in list(d.items())[:4]})
+
+
+if __name__ == "__main__":
+    main()

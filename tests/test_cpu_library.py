@@ -1,0 +1,86 @@
+"""CPU-side checks: the C-ABI library builds, loads and exports every symbol
+include/sgx.h declares; host-side argument validation returns error codes
+without touching a GPU; the table writer and NQT transforms are bit-exact."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from sgx import lib as L
+from sgx import sp5lite
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    txt = open(os.path.join(ROOT, "include", "sgx.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(sgx_[a-z0-9_]+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(L.LIB_PATH):
+        pytest.skip("libsgx.so not built")
+    try:
+        return L.load()
+    except OSError as e:  # e.g. no libcudart on a CPU-only machine
+        pytest.skip(f"cannot load libsgx.so here: {e}")
+
+
+def test_header_declares_the_binding_list():
+    assert set(L.EXPORTED) <= set(declared_symbols())
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_symbols():
+        assert hasattr(lib, name), name
+
+
+def test_constructors_and_validation_need_no_gpu(lib):
+    e = L.SgxEos()
+    assert lib.sgx_eos_ideal_gas(C.byref(e), 0.4, 0.718e7) == 0
+    assert e.type == L.IDEAL_GAS and e.p[0] == 0.4
+    assert lib.sgx_eos_ideal_gas(C.byref(e), -1.0, 1.0) == 1  # CheckParams
+    assert lib.sgx_eos_gruneisen(C.byref(e), 3.94e5, 1.489, 0, 0, 2.02, 0.47, 8.93, 298.0,
+                                 0.0, 3.9e6, 0.0) == 0
+    # rho_max = 0.99 * rho0 / ((1 - 1/s1) + eps)  (eos_gruneisen.hpp:235-236, 321-322)
+    assert e.p[10] == 0.99 * (8.93 / ((1 - 1 / 1.489) + 10 * np.finfo(float).eps))
+    # bad solver / sizes fail before any device work
+    arr = (L.SgxEos * 1)(e)
+    rc = lib.sgx_pte_solve(7, 1, 10, C.cast(arr, C.c_void_p), 1, *([None] * 10), None, 0, None)
+    assert rc == 1
+    rc = lib.sgx_pte_solve(0, 9, 10, C.cast(arr, C.c_void_p), 1, *([None] * 10), None, 0, None)
+    assert rc == 5
+    assert lib.sgx_pte_solve(0, 1, 0, C.cast(arr, C.c_void_p), 1, *([None] * 10), None, 0,
+                             None) == 0  # empty batch
+    assert lib.sgx_eos_eval(C.byref(e), 99, 4, None, None, None, None, 0, None) == 1
+    assert b"bad fn" in lib.sgx_last_error()
+    m = L.MixParams()
+    assert lib.sgx_mix_params_default(C.byref(m)) == 0
+    assert m.pte_max_iter_per_mat == 128 and m.line_search_max_iter == 6
+    assert lib.sgx_pte_rhot_required_scratch(5) == 25 + 20 + 30
+    assert lib.sgx_pte_pt_required_scratch(3) == 4 + 8 + 6
+
+
+def test_missing_table_reports_io_error(lib, tmp_path):
+    e = L.SgxEos()
+    rc = lib.sgx_eos_spiner_rhot(C.byref(e), str(tmp_path / "nope.sp5").encode(), 1, 0)
+    assert rc in (3, 4)  # no device here, or unreadable file
+
+
+def test_nqt_transforms_are_near_inverses():
+    x = np.exp(np.random.default_rng(0).uniform(-30, 30, 10000))
+    # pow10(log10(x)) returns x up to the rounding of the log2/log10 factors
+    # (logs.hpp:188-214, 282-292)
+    y = sp5lite.pow10_nqt(sp5lite.log10_nqt(x))
+    assert np.max(np.abs(y - x) / x) < 1e-13
+
+
+def test_table_image_is_deterministic(tmp_path):
+    a, b = tmp_path / "a.sp5", tmp_path / "b.sp5"
+    sp5lite.stiffgas_table(str(a))
+    sp5lite.stiffgas_table(str(b))
+    assert a.read_bytes() == b.read_bytes()
