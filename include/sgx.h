@@ -190,7 +190,7 @@ int sgx_pte_pt_required_scratch(int nmat);
 
 /* Solves PTE in every cell.
  *  solver     SGX_PTE_RHOT or SGX_PTE_PT
- *  nmat       materials per cell slot (1..8); per-material arrays are
+ *  nmat       material slots per cell (1..6, the Jacobian is at most 6x6);
  *             [nmat][ncell], cell index fastest
  *  eos_list   host array of neos EOS values (neos <= 16)
  *  eos_idx    device [nmat][ncell] index into eos_list, -1 = material absent;

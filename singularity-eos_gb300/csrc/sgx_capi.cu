@@ -225,8 +225,8 @@ int sgx_pte_solve(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list, 
                   int precision, sgx_stream_t stream) {
   if (solver != SGX_PTE_RHOT && solver != SGX_PTE_PT)
     return fail(SGX_ERR_INVALID, "sgx_pte_solve: bad solver");
-  if (nmat < 1 || nmat > sgx::MAX_NMAT)
-    return fail(SGX_ERR_UNSUPPORTED, "sgx_pte_solve: nmat must be in 1..8");
+  if (nmat < 1 || nmat > sgx::PTE_MAX_N)
+    return fail(SGX_ERR_UNSUPPORTED, "sgx_pte_solve: nmat must be in 1..6");
   if (neos < 1 || neos > sgx::MAX_EOS || !eos_list)
     return fail(SGX_ERR_INVALID, "sgx_pte_solve: neos must be in 1..16");
   if (!eos_idx && neos < nmat)

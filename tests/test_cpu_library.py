@@ -52,7 +52,7 @@ def test_constructors_and_validation_need_no_gpu(lib):
     arr = (L.SgxEos * 1)(e)
     rc = lib.sgx_pte_solve(7, 1, 10, C.cast(arr, C.c_void_p), 1, *([None] * 10), None, 0, None)
     assert rc == 1
-    rc = lib.sgx_pte_solve(0, 9, 10, C.cast(arr, C.c_void_p), 1, *([None] * 10), None, 0, None)
+    rc = lib.sgx_pte_solve(0, 7, 10, C.cast(arr, C.c_void_p), 1, *([None] * 10), None, 0, None)
     assert rc == 5
     assert lib.sgx_pte_solve(0, 1, 0, C.cast(arr, C.c_void_p), 1, *([None] * 10), None, 0,
                              None) == 0  # empty batch
