@@ -3,8 +3,11 @@
 Headline workload (``--workload lookup``, the default): vector tabulated EOS
 lookup, 2^24 queries on a 256 x 256 NQT-log (rho, T) table sampled from the
 StiffGas model (a SpinerEOSDependsRhoT layout); per query T(rho, sie) by
-regula falsi on the table, then P and the bulk modulus (FillEos with
-T|P|bmod outputs). Inputs are seeded synthetic data (no public dataset).
+regula falsi on the table, then P, the bulk modulus and the sound speed
+(FillEos with T|P|bmod outputs plus cs = sqrt(bmod/rho)). The headline value
+is the mixed-precision path (FP32 bracket search, FP64 root and outputs); the
+plain FP64 path, which follows the reference's iteration bit for bit, is
+reported beside it. Inputs are seeded synthetic data (no public dataset).
 
 Secondary workloads, measured in the same run and reported under "pte":
 plain FP64 PTE closure of 65,536 two-material cells (IdealGas + StiffGas) and
@@ -38,7 +41,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 N_LOOKUP = 1 << 24
 N_PTE2 = 65536
 N_PTE_BATCH = 1 << 22
-LOOKUP_BYTES_PER_QUERY = 16 + 24  # rho, sie in; T, P, bmod out (float64)
+LOOKUP_BYTES_PER_QUERY = 16 + 32  # rho, sie in; T, P, bmod, cs out (float64)
 Q_OUT = 8 | 4 | 32                # temperature | pressure | bulk modulus
 METRIC = "PTE mixed cells/s & EOS lookups/s, 1 GB300, batched+FP32-refined vs plain FP64"
 
@@ -158,43 +161,58 @@ def run_ours(args):
         tab = lib.spiner_eos(path, 1)
         rho = torch.as_tensor(rho_h, device="cuda")
         sie = torch.as_tensor(sie_h, device="cuda")
-        T, P, B = (torch.empty_like(rho) for _ in range(3))
+        T, P, B, CS = (torch.empty_like(rho) for _ in range(4))
 
-        def step():
-            lib.fill_eos(tab, rho, T, sie, P, None, B, Q_OUT, stream=stream)
+        def make_step(prec):
+            def step():
+                lib.fill_eos(tab, rho, T, sie, P, None, B, Q_OUT, cs=CS, precision=prec,
+                             stream=stream)
+            return step
 
-        barrier(world)
-        with ClockSampler(local) as clk:
-            dt = time_steps(step, args.steps, args.warmup, stream)
-        barrier(world)
-        dt = max_over_ranks(dt, world)
-        per_launch = dt / args.steps
-        value = world * N_LOOKUP * args.steps / dt
-        achieved = LOOKUP_BYTES_PER_QUERY * N_LOOKUP / per_launch / 1e9
-        out["clocks"] = clk.summary()
-        out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                           "frac": achieved / hbm, "traffic": None,
+        results = {}
+        for prec, name in ((lib.PREC_FP64, "fp64"), (lib.PREC_MIXED, "mixed")):
+            steps = args.steps if prec == lib.PREC_MIXED else max(1, min(args.steps, 5))
+            barrier(world)
+            with ClockSampler(local) as clk:
+                dt = time_steps(make_step(prec), steps, args.warmup, stream)
+            barrier(world)
+            dt = max_over_ranks(dt, world)
+            per_launch = dt / steps
+            results[name] = dict(value=world * N_LOOKUP * steps / dt, ms=per_launch * 1e3,
+                                 gbs=LOOKUP_BYTES_PER_QUERY * N_LOOKUP / per_launch / 1e9,
+                                 clocks=clk.summary(), steps=steps)
+        m = results["mixed"]
+        out["clocks"] = m["clocks"]
+        out["roofline"] = {"bound": "hbm", "achieved": m["gbs"], "peak": hbm, "unit": "GB/s",
+                           "frac": m["gbs"] / hbm, "traffic": None,
                            "peak_kind": hbm_kind + " (burst copy)",
-                           "kernel": "fill_kernel (sgx_fp64.cu)"}
+                           "kernel": "spiner_fill_mixed (sgx_lookup_mixed.cu)",
+                           "bytes_per_query": LOOKUP_BYTES_PER_QUERY}
+        f = results["fp64"]
+        out["plain_fp64"] = {"value": f["value"], "unit": "lookups/s", "ms_per_step": f["ms"],
+                             "hbm_frac": f["gbs"] / hbm, "clocks": f["clocks"],
+                             "kernel": "fill_kernel (sgx_fp64.cu)"}
         # e2e: host buffers in pinned memory, copies inside the timed region
         rho_p = torch.as_tensor(rho_h).pin_memory()
         sie_p = torch.as_tensor(sie_h).pin_memory()
-        outs_p = [torch.empty(N_LOOKUP, dtype=torch.float64).pin_memory() for _ in range(3)]
+        outs_p = [torch.empty(N_LOOKUP, dtype=torch.float64).pin_memory() for _ in range(4)]
 
         def e2e_step():
             rho.copy_(rho_p, non_blocking=True)
             sie.copy_(sie_p, non_blocking=True)
-            lib.fill_eos(tab, rho, T, sie, P, None, B, Q_OUT, stream=stream)
-            for h, d in zip(outs_p, (T, P, B)):
+            lib.fill_eos(tab, rho, T, sie, P, None, B, Q_OUT, cs=CS, precision=lib.PREC_MIXED,
+                         stream=stream)
+            for h, d in zip(outs_p, (T, P, B, CS)):
                 h.copy_(d, non_blocking=True)
 
         e2e_steps = max(1, min(args.steps, 5))
         barrier(world)
         dte = max_over_ranks(time_steps(e2e_step, e2e_steps, 1, stream), world)
         out["e2e"] = {"value": world * N_LOOKUP * e2e_steps / dte, "unit": "lookups/s",
-                      "h2d_bytes_per_step": 16 * N_LOOKUP, "d2h_bytes_per_step": 24 * N_LOOKUP}
+                      "h2d_bytes_per_step": 16 * N_LOOKUP, "d2h_bytes_per_step": 32 * N_LOOKUP}
         lib.load().sgx_eos_finalize(__import__("ctypes").byref(tab))
-        out["value"], out["ms_per_step"] = value, per_launch * 1e3
+        out["value"], out["ms_per_step"] = m["value"], m["ms"]
+        out["gpu_launches"] = m["steps"]
 
     # PTE secondary workloads (plain FP64)
     pte = {}
@@ -223,7 +241,6 @@ def run_ours(args):
         pte[name] = {"cells_per_s": world * n * ps / dt, "ms_per_step": dt / ps * 1e3,
                      "converged_frac": float(conv), "precision": "fp64"}
     out["pte"] = pte
-    out["gpu_launches"] = args.steps
     return out, world, rank
 
 
@@ -265,8 +282,8 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    config = {"workload": "vector tabulated EOS lookup (FillEos T|P|bmod), 2^24 queries, "
-                          "256x256 NQT-log StiffGas-sampled rho-T table",
+    config = {"workload": "vector tabulated EOS lookup (FillEos T|P|bmod + sound speed), "
+                          "2^24 queries, 256x256 NQT-log StiffGas-sampled rho-T table",
               "queries": N_LOOKUP, "table": "256x256", "l2": "inputs (256 MB) larger than L2"}
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:
@@ -287,10 +304,12 @@ def main():
         return
     line = {"metric": METRIC, "value": out["value"], "unit": "lookups/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["ms_per_step"],
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 (f32 bracket search)",
             "data": "synthetic (seeded; StiffGas-sampled table)", "config": config,
             "e2e": out["e2e"], "roofline": out["roofline"], "clocks": out["clocks"],
-            "gpu_launches": out["gpu_launches"], "pte": out["pte"]}
+            "gpu_launches": out["gpu_launches"], "plain_fp64": out["plain_fp64"],
+            "pte": out["pte"]}
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline()
     print(json.dumps(line))

@@ -182,6 +182,16 @@ int sgx_eos_eval(const sgx_eos *eos, int fn, int64_t n, const double *in1,
 int sgx_eos_fill(const sgx_eos *eos, int64_t n, double *rho, double *temp, double *sie,
                  double *press, double *cv, double *bmod, uint32_t output, double *lambda,
                  int lambda_stride, sgx_stream_t stream);
+/* FillEos with two extensions: cs (nullable) receives the sound speed
+ * sqrt(bmod / rho), and precision selects the arithmetic. SGX_PREC_MIXED is
+ * available for a tabulated rho-T EOS with (rho, sie) inputs and T among the
+ * outputs: the bracketing table cell is found in FP32 and the root and every
+ * output are computed in FP64 (results agree with SGX_PREC_FP64 to the
+ * reference's root tolerance, 1e-14 in log10 T). No reference counterpart
+ * beyond FillEos (eos/eos_base.hpp:503-531). */
+int sgx_eos_fill_ex(const sgx_eos *eos, int64_t n, double *rho, double *temp, double *sie,
+                    double *press, double *cv, double *bmod, double *cs, uint32_t output,
+                    double *lambda, int lambda_stride, int precision, sgx_stream_t stream);
 
 /* ---- PTE ---- */
 int sgx_mix_params_default(sgx_mix_params *p);

@@ -25,6 +25,7 @@ COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
 UNITS = [
     ("sgx_fp64", "sgx_fp64.cu", ["--fmad=false"]),
     ("sgx_mixed", "sgx_mixed.cu", ["--fmad=true"]),
+    ("sgx_lookup_mixed", "sgx_lookup_mixed.cu", ["--fmad=true"]),
     ("sgx_capi", "sgx_capi.cu", ["--fmad=false"]),
     ("sgx_table", "sgx_table.cu", ["--fmad=false"]),
 ] + [(f"sgx_pte_fp64_n{n}", "sgx_pte_fp64_n.cu", ["--fmad=false", f"-DSGX_PTE_N={n}"])

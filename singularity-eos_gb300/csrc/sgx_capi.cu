@@ -192,14 +192,16 @@ int sgx_eos_eval(const sgx_eos *eos, int fn, int64_t n, const double *in1, const
   return SGX_OK;
 }
 
-int sgx_eos_fill(const sgx_eos *eos, int64_t n, double *rho, double *temp, double *sie,
-                 double *press, double *cv, double *bmod, uint32_t output, double *lambda,
-                 int lambda_stride, sgx_stream_t stream) {
+int sgx_eos_fill_ex(const sgx_eos *eos, int64_t n, double *rho, double *temp, double *sie,
+                    double *press, double *cv, double *bmod, double *cs, uint32_t output,
+                    double *lambda, int lambda_stride, int precision, sgx_stream_t stream) {
   if (!eos || !valid_type(eos->type)) return fail(SGX_ERR_INVALID, "sgx_eos_fill: bad eos");
   if (n < 0) return fail(SGX_ERR_INVALID, "sgx_eos_fill: n < 0");
   if (n == 0) return SGX_OK;
   if (!rho) return fail(SGX_ERR_INVALID, "sgx_eos_fill: rho is required");
   if (lambda && lambda_stride < 2) return fail(SGX_ERR_INVALID, "sgx_eos_fill: lambda_stride < 2");
+  if (precision != SGX_PREC_FP64 && precision != SGX_PREC_MIXED)
+    return fail(SGX_ERR_INVALID, "sgx_eos_fill: bad precision");
   sgx::FillArgs a;
   a.eos = *eos;
   a.n = n;
@@ -209,13 +211,35 @@ int sgx_eos_fill(const sgx_eos *eos, int64_t n, double *rho, double *temp, doubl
   a.press = press;
   a.cv = cv;
   a.bmod = bmod;
+  a.cs = cs;
   a.lambda = lambda;
   a.lambda_stride = lambda_stride;
   a.output = output;
   a.err = nullptr;
-  const cudaError_t e = sgx::launch_fill_fp64(a, reinterpret_cast<cudaStream_t>(stream));
+  cudaError_t e;
+  if (precision == SGX_PREC_MIXED) {
+    // The mixed path covers the hot call: a tabulated rho-T model with
+    // (rho, sie) in and any of T, P, cv, bmod out.
+    const uint32_t allowed = SGX_Q_TEMPERATURE | SGX_Q_PRESSURE | SGX_Q_SPECIFIC_HEAT |
+                             SGX_Q_BULK_MODULUS;
+    if (eos->type != SGX_SPINER_RHOT || (output & ~allowed) || !(output & SGX_Q_TEMPERATURE) ||
+        !sie)
+      return fail(SGX_ERR_UNSUPPORTED,
+                  "sgx_eos_fill: mixed precision needs a tabulated rho-T EOS, (rho, sie) "
+                  "inputs and T among the outputs");
+    e = sgx::launch_fill_mixed(a, reinterpret_cast<cudaStream_t>(stream));
+  } else {
+    e = sgx::launch_fill_fp64(a, reinterpret_cast<cudaStream_t>(stream));
+  }
   if (e != cudaSuccess) return cuda_fail(e, "sgx_eos_fill");
   return SGX_OK;
+}
+
+int sgx_eos_fill(const sgx_eos *eos, int64_t n, double *rho, double *temp, double *sie,
+                 double *press, double *cv, double *bmod, uint32_t output, double *lambda,
+                 int lambda_stride, sgx_stream_t stream) {
+  return sgx_eos_fill_ex(eos, n, rho, temp, sie, press, cv, bmod, nullptr, output, lambda,
+                         lambda_stride, SGX_PREC_FP64, stream);
 }
 
 int sgx_pte_solve(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list, int neos,

@@ -40,8 +40,9 @@ __global__ void fill_kernel(const FillArgs a) {
     double cv = 0.0, bmod = 0.0;
     double *lam = a.lambda ? a.lambda + i * a.lambda_stride : nullptr;
     int err = 0;
-    ev_fill(e, rho, temp, sie, press, cv, bmod, a.output, lam, &err);
+    ev_fill(e, rho, temp, sie, press, cv, bmod, a.output | (a.cs ? Q_BMOD : 0u), lam, &err);
     bad |= err;
+    if (a.cs) a.cs[i] = sqrt(bmod / rho);
     if ((a.output & Q_DENSITY) && a.rho) a.rho[i] = rho;
     if ((a.output & Q_TEMPERATURE) && a.temp) a.temp[i] = temp;
     if ((a.output & Q_SIE) && a.sie) a.sie[i] = sie;

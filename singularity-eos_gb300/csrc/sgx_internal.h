@@ -47,10 +47,13 @@ struct FillArgs {
   sgx_eos eos;
   long long n;
   double *rho, *temp, *sie, *press, *cv, *bmod, *lambda;
+  double *cs; // optional sound speed sqrt(bmod / rho)
   unsigned output;
   int lambda_stride;
   int *err; // device flag: set to 1 on an undefined input/output combination
 };
 cudaError_t launch_fill_fp64(const FillArgs &a, cudaStream_t stream);
+// Tabulated rho-T FillEos from (rho, sie): FP32 bracket search + FP64 solve.
+cudaError_t launch_fill_mixed(const FillArgs &a, cudaStream_t stream);
 
 } // namespace sgx

@@ -63,7 +63,9 @@ struct SpinerTable {
   double lRhoMin, lRhoMax, rhoMax, lTMin, lTMax, TMax, PMin, lRhoOffset, lTOffset;
   int nRho, nT;
   int reproducible;
-  int pad;
+  // 1 when sie increases strictly along T in every density row, which makes
+  // T(rho, sie) a unique root that a bracketing search can locate directly.
+  int sie_monotone_T;
   const double *f2[NF2D];
   const double *f1[NF1D];
   const dq4 *sie4, *P4, *bmod4; // corner-packed [nRho-1][nT-1]

@@ -298,6 +298,13 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
   t.lRhoOffset = std::fabs(rOff);
   t.lTOffset = std::fabs(tOff);
   t.reproducible = reproducible ? 1 : 0;
+  t.sie_monotone_T = 1;
+  for (int j = 0; j < h.nRho && t.sie_monotone_T; ++j)
+    for (int i = 0; i + 1 < h.nT; ++i)
+      if (!(h.f2[F_SIE][j * h.nT + i + 1] > h.f2[F_SIE][j * h.nT + i])) {
+        t.sie_monotone_T = 0;
+        break;
+      }
   for (int k = 0; k < NF1D; ++k)
     if (h.f1[k].empty()) h.f1[k].assign(k == F_RHO_AT_PMIN ? h.nT : h.nRho, 0.0);
   h.bind();

@@ -22,6 +22,7 @@ EXPORTED = [
     "sgx_version", "sgx_last_error", "sgx_eos_ideal_gas", "sgx_eos_stiff_gas",
     "sgx_eos_noble_abel", "sgx_eos_gruneisen", "sgx_eos_spiner_rhot", "sgx_eos_finalize",
     "sgx_eos_table_bytes", "sgx_eos_spiner_dump", "sgx_eos_eval", "sgx_eos_fill",
+    "sgx_eos_fill_ex",
     "sgx_mix_params_default", "sgx_pte_rhot_required_scratch", "sgx_pte_pt_required_scratch",
     "sgx_pte_solve",
 ]
@@ -87,6 +88,8 @@ def load():
     lib.sgx_eos_eval.argtypes = [C.POINTER(SgxEos), I, C.c_int64, P, P, P, P, I, P]
     lib.sgx_eos_fill.argtypes = [C.POINTER(SgxEos), C.c_int64, P, P, P, P, P, P, C.c_uint32,
                                  P, I, P]
+    lib.sgx_eos_fill_ex.argtypes = [C.POINTER(SgxEos), C.c_int64, P, P, P, P, P, P, P,
+                                    C.c_uint32, P, I, I, P]
     lib.sgx_mix_params_default.argtypes = [C.POINTER(MixParams)]
     lib.sgx_pte_solve.argtypes = [I, I, C.c_int64, P, I, P, P, P, P, P, P, P, P, P,
                                   C.POINTER(MixParams), P, I, P]
@@ -150,11 +153,17 @@ def eval_eos(eos, fn, in1, in2, out, lam=None, lam_stride=0, stream=None):
                               lam_stride, stream_ptr(stream)))
 
 
-def fill_eos(eos, rho, temp, sie, press, cv, bmod, output, lam=None, lam_stride=0, stream=None):
+def fill_eos(eos, rho, temp, sie, press, cv, bmod, output, lam=None, lam_stride=0, stream=None,
+             cs=None, precision=PREC_FP64):
     n = rho.numel()
-    check(load().sgx_eos_fill(C.byref(eos), n, ptr(rho), ptr(temp), ptr(sie), ptr(press),
-                              ptr(cv), ptr(bmod), output, ptr(lam), lam_stride,
-                              stream_ptr(stream)))
+    if cs is None and precision == PREC_FP64:
+        check(load().sgx_eos_fill(C.byref(eos), n, ptr(rho), ptr(temp), ptr(sie), ptr(press),
+                                  ptr(cv), ptr(bmod), output, ptr(lam), lam_stride,
+                                  stream_ptr(stream)))
+    else:
+        check(load().sgx_eos_fill_ex(C.byref(eos), n, ptr(rho), ptr(temp), ptr(sie),
+                                     ptr(press), ptr(cv), ptr(bmod), ptr(cs), output, ptr(lam),
+                                     lam_stride, precision, stream_ptr(stream)))
 
 
 def pte_solve(solver, eos_list, eos_idx, vfrac_tot, sie_tot, rho, vfrac, sie, temp, press,

@@ -1,0 +1,89 @@
+"""The mixed-precision lookup path (FP32 bracket search + FP64 root and
+outputs) against the reference fixtures and against the plain FP64 path.
+
+Error bar: T within 1e-12 relative (the reference's own root tolerance is
+1e-14 in log10 T, i.e. ~2.3e-14 relative in T). P, bmod and cv are
+interpolated at that T, so their difference is bounded by their slope in
+log10 T times 1e-14; the tests bound it by 1e-11 relative to the larger of
+the value and 1e-6 of the batch's largest magnitude (P crosses zero inside
+the table, where a pure relative bound is meaningless)."""
+import numpy as np
+import pytest
+
+from common import golden, rel_err, stiffgas_table_path
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def sgx():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from sgx import lib
+    lib.load()
+    return lib
+
+
+def scaled_err(a, b):
+    floor = 1e-6 * np.max(np.abs(b))
+    return np.abs(a - b) / np.maximum(np.abs(b), floor)
+
+
+def test_mixed_lookup_matches_reference(sgx):
+    import ctypes as C
+    fx = golden("spiner_lookup")
+    path, sha = stiffgas_table_path()
+    assert sha == str(fx["table_sha256"])
+    tab = sgx.spiner_eos(path, 1)
+    try:
+        rho = torch.as_tensor(fx["rho"], device="cuda")
+        sie = torch.as_tensor(fx["sie"], device="cuda")
+        T, P, cv, bm, cs = (torch.zeros_like(rho) for _ in range(5))
+        q = sgx.Q_TEMPERATURE | sgx.Q_PRESSURE | sgx.Q_BULK_MODULUS | sgx.Q_SPECIFIC_HEAT
+        sgx.fill_eos(tab, rho, T, sie, P, cv, bm, q, cs=cs, precision=sgx.PREC_MIXED)
+        torch.cuda.synchronize()
+        errT = rel_err(T.cpu().numpy(), fx["fill_T"])
+        assert errT.max() <= 1e-12, errT.max()
+        for name, t in (("P", P), ("bmod", bm), ("cv", cv)):
+            e = scaled_err(t.cpu().numpy(), fx["fill_" + name])
+            assert e.max() <= 1e-11, (name, e.max())
+        want_cs = np.sqrt(fx["fill_bmod"] / fx["rho"])
+        assert scaled_err(cs.cpu().numpy(), want_cs).max() <= 1e-11
+    finally:
+        sgx.load().sgx_eos_finalize(C.byref(tab))
+
+
+def test_mixed_lookup_full_size_against_fp64(sgx):
+    """2^22 queries: mixed vs plain FP64 on device, size-independent bounds."""
+    import ctypes as C
+    from sgx import sp5lite
+    path, _ = stiffgas_table_path()
+    tab = sgx.spiner_eos(path, 1)
+    try:
+        n = 1 << 22
+        rho_h, sie_h = sp5lite.stiffgas_queries(n, seed=99)
+        rho = torch.as_tensor(rho_h, device="cuda")
+        sie = torch.as_tensor(sie_h, device="cuda")
+        out = {}
+        for prec in (sgx.PREC_FP64, sgx.PREC_MIXED):
+            T, P, bm, cs = (torch.zeros_like(rho) for _ in range(4))
+            q = sgx.Q_TEMPERATURE | sgx.Q_PRESSURE | sgx.Q_BULK_MODULUS
+            sgx.fill_eos(tab, rho, T, sie, P, None, bm, q, cs=cs, precision=prec)
+            torch.cuda.synchronize()
+            out[prec] = [x.cpu().numpy() for x in (T, P, bm, cs)]
+        a, b = out[sgx.PREC_MIXED], out[sgx.PREC_FP64]
+        assert np.all(np.isfinite(a[0]))
+        assert rel_err(a[0], b[0]).max() <= 1e-12
+        for k in (1, 2, 3):
+            assert scaled_err(a[k], b[k]).max() <= 1e-11
+    finally:
+        sgx.load().sgx_eos_finalize(C.byref(tab))
+
+
+def test_mixed_rejects_unsupported_calls(sgx):
+    e = sgx.make_eos(1, (0.4, 0.718e7))
+    x = torch.ones(4, dtype=torch.float64, device="cuda")
+    with pytest.raises(RuntimeError, match="mixed precision"):
+        sgx.fill_eos(e, x, x.clone(), x.clone(), x.clone(), None, x.clone(),
+                     sgx.Q_TEMPERATURE, precision=sgx.PREC_MIXED)
