@@ -70,6 +70,7 @@ struct SpinerTable {
   const double *f1[NF1D];
   const dq4 *sie4, *P4, *bmod4; // corner-packed [nRho-1][nT-1]
   const fq4 *sie4f;               // corner-packed FP32 copy of sie
+  const float *sieCold32, *sielTMax32; // FP32 copies of the on-table bounds
 };
 
 // ---- interpolation (DataBox::interpToReal) ----

@@ -400,6 +400,10 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
   }
   offf = off;
   off = align(off + ncell * sizeof(fq4));
+  const size_t offc32 = off;
+  off = align(off + static_cast<size_t>(nR) * sizeof(float));
+  const size_t offm32 = off;
+  off = align(off + static_cast<size_t>(nR) * sizeof(float));
   const size_t bytes = off;
   std::vector<unsigned char> img(bytes, 0);
   for (int k = 0; k < NF2D; ++k)
@@ -428,6 +432,12 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
         std::memcpy(q + (static_cast<size_t>(j) * (nT - 1) + i) * sizeof(fq4), c, sizeof(c));
       }
   }
+  for (int j = 0; j < nR; ++j) {
+    const float c = static_cast<float>(h.f1[F_SIECOLD][j]);
+    const float m = static_cast<float>(h.f1[F_SIELTMAX][j]);
+    std::memcpy(img.data() + offc32 + j * sizeof(float), &c, sizeof(float));
+    std::memcpy(img.data() + offm32 + j * sizeof(float), &m, sizeof(float));
+  }
   void *dev = nullptr;
   cudaError_t e = cudaMalloc(&dev, bytes);
   if (e != cudaSuccess) {
@@ -444,6 +454,8 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
   td.P4 = reinterpret_cast<const dq4 *>(d + offq[1]);
   td.bmod4 = reinterpret_cast<const dq4 *>(d + offq[2]);
   td.sie4f = reinterpret_cast<const fq4 *>(d + offf);
+  td.sieCold32 = reinterpret_cast<const float *>(d + offc32);
+  td.sielTMax32 = reinterpret_cast<const float *>(d + offm32);
   std::memcpy(img.data(), &td, sizeof(td));
   e = cudaMemcpy(dev, img.data(), bytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
