@@ -129,7 +129,10 @@ typedef struct sgx_mix_params {
 } sgx_mix_params;
 
 /* Per-cell result of a PTE solve (the reference's SolverStatus,
- * mixed_cell_models.hpp:80-87, plus the iteration count). */
+ * mixed_cell_models.hpp:80-87, plus the iteration count). small_step_iters
+ * holds the count in bits 0-5; bit 6 is set when the mixed-precision path
+ * re-solved the cell with the FP64 iteration; bit 7 when a path that aborts
+ * in the reference (e.g. a failed Gruneisen root find) was taken. */
 typedef struct sgx_pte_status {
   double residual;
   int32_t niter;

@@ -29,7 +29,9 @@ UNITS = [
     ("sgx_capi", "sgx_capi.cu", ["--fmad=false"]),
     ("sgx_table", "sgx_table.cu", ["--fmad=false"]),
 ] + [(f"sgx_pte_fp64_n{n}", "sgx_pte_fp64_n.cu", ["--fmad=false", f"-DSGX_PTE_N={n}"])
-     for n in range(1, 7)]
+     for n in range(1, 7)] + [
+    (f"sgx_pte_mixed_n{n}", "sgx_pte_mixed_n.cu", ["--fmad=true", f"-DSGX_PTE_N={n}"])
+    for n in range(1, 7)]
 
 
 def nvcc():

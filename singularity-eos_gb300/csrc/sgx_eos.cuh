@@ -32,62 +32,66 @@ constexpr double ROOM_TEMPERATURE = 293;
 constexpr double ATMOSPHERIC_PRESSURE = 1e6;
 
 // ---------------------------------------------------------------------------
-// Gruneisen helpers (eos_gruneisen.hpp:191-195, 331-371)
-SGX_HD double gru_gamma(const sgx_eos &e, const double rho_in) {
+// Gruneisen helpers (eos_gruneisen.hpp:191-195, 331-371), templated on the
+// arithmetic type (double reproduces the reference; float serves the FP32
+// iteration phase of the mixed-precision solver).
+template <typename T> SGX_HD T gru_gamma(const sgx_eos &e, const T rho_in) {
   const double *p = e.p;
-  const double rho = smin(rho_in, p[pi::rho_max]);
-  return rho < p[pi::rho0] ? p[pi::G0]
-                           : p[pi::G0] * p[pi::rho0] / rho +
-                                 p[pi::b] * (1 - p[pi::rho0] / rho);
+  const T rho = smin(rho_in, T(p[pi::rho_max]));
+  const T rho0 = T(p[pi::rho0]), G0 = T(p[pi::G0]);
+  return rho < rho0 ? G0 : G0 * rho0 / rho + T(p[pi::b]) * (1 - rho0 / rho);
 }
-SGX_HD double gru_P_rho_e(const sgx_eos &e, const double rho_in, const double sie) {
+template <typename T> SGX_HD T gru_P_rho_e(const sgx_eos &e, const T rho_in, const T sie) {
   const double *p = e.p;
-  const double rho = smin(rho_in, p[pi::rho_max]);
-  double P_H, E_H;
-  if (rho >= p[pi::rho0]) {
-    const double eta = 1 - p[pi::rho0] / rho;
-    const double s = p[pi::s1] * eta + p[pi::s2] * (eta * eta) + p[pi::s3] * (eta * (eta * eta));
-    P_H = p[pi::P0] + (p[pi::C0] * p[pi::C0]) * p[pi::rho0] * eta / ((1 - s) * (1 - s));
-    E_H = (P_H + p[pi::P0]) * eta / p[pi::rho0] / 2.;
+  const T rho = smin(rho_in, T(p[pi::rho_max]));
+  const T rho0 = T(p[pi::rho0]), C0 = T(p[pi::C0]), P0 = T(p[pi::P0]);
+  T P_H, E_H;
+  if (rho >= rho0) {
+    const T eta = 1 - rho0 / rho;
+    const T s = T(p[pi::s1]) * eta + T(p[pi::s2]) * (eta * eta) + T(p[pi::s3]) * (eta * (eta * eta));
+    P_H = P0 + (C0 * C0) * rho0 * eta / ((1 - s) * (1 - s));
+    E_H = (P_H + P0) * eta / rho0 / T(2.);
   } else {
-    P_H = p[pi::P0] + (p[pi::C0] * p[pi::C0]) * (rho - p[pi::rho0]);
-    E_H = 0.;
+    P_H = P0 + (C0 * C0) * (rho - rho0);
+    E_H = T(0.);
   }
-  return P_H + gru_gamma(e, rho) * rho * (sie - E_H);
+  return P_H + gru_gamma<T>(e, rho) * rho * (sie - E_H);
 }
-SGX_HD double gru_dPdrho_e(const sgx_eos &e, const double rho_in, const double sie) {
+template <typename T> SGX_HD T gru_dPdrho_e(const sgx_eos &e, const T rho_in, const T sie) {
   const double *p = e.p;
-  const double rho = smin(rho_in, p[pi::rho_max]);
-  if (rho < p[pi::rho0]) {
-    return (p[pi::C0] * p[pi::C0]) + gru_gamma(e, rho) * sie;
+  const T rho = smin(rho_in, T(p[pi::rho_max]));
+  const T rho0 = T(p[pi::rho0]), C0 = T(p[pi::C0]), P0 = T(p[pi::P0]);
+  if (rho < rho0) {
+    return (C0 * C0) + gru_gamma<T>(e, rho) * sie;
   }
-  const double eta = 1 - p[pi::rho0] / rho;
-  const double s = p[pi::s1] * eta + p[pi::s2] * (eta * eta) + p[pi::s3] * (eta * (eta * eta));
-  const double ds = p[pi::s1] + 2 * p[pi::s2] * eta + 3 * p[pi::s3] * (eta * eta);
-  const double deta = p[pi::rho0] / (rho * rho);
-  const double dGam = (p[pi::b] - p[pi::G0]) * deta;
-  const double C02 = p[pi::C0] * p[pi::C0];
-  const double oms2 = (1 - s) * (1 - s);
-  const double P_H = p[pi::P0] + C02 * p[pi::rho0] * eta / oms2;
-  const double dP_H = C02 * p[pi::rho0] / oms2 * deta * (1 + 2 * eta * ds / (1 - s));
-  const double E_H = (P_H + p[pi::P0]) * eta / p[pi::rho0] / 2.;
-  const double dE_H =
-      deta * (P_H + p[pi::P0]) / p[pi::rho0] / 2. + eta / p[pi::rho0] / 2 * dP_H;
-  const double G = gru_gamma(e, rho);
+  const T s1 = T(p[pi::s1]), s2 = T(p[pi::s2]), s3 = T(p[pi::s3]);
+  const T eta = 1 - rho0 / rho;
+  const T s = s1 * eta + s2 * (eta * eta) + s3 * (eta * (eta * eta));
+  const T ds = s1 + 2 * s2 * eta + 3 * s3 * (eta * eta);
+  const T deta = rho0 / (rho * rho);
+  const T dGam = (T(p[pi::b]) - T(p[pi::G0])) * deta;
+  const T C02 = C0 * C0;
+  const T oms2 = (1 - s) * (1 - s);
+  const T P_H = P0 + C02 * rho0 * eta / oms2;
+  const T dP_H = C02 * rho0 / oms2 * deta * (1 + 2 * eta * ds / (1 - s));
+  const T E_H = (P_H + P0) * eta / rho0 / T(2.);
+  const T dE_H = deta * (P_H + P0) / rho0 / T(2.) + eta / rho0 / 2 * dP_H;
+  const T G = gru_gamma<T>(e, rho);
   return dP_H + G * (sie - E_H) + rho * dGam * (sie - E_H) - rho * G * dE_H;
 }
-SGX_HD double gru_e_rho_T(const sgx_eos &e, const double T) {
-  return e.p[pi::gCv] * (T - e.p[pi::T0]);
+template <typename T> SGX_HD T gru_e_rho_T(const sgx_eos &e, const T temp) {
+  return T(e.p[pi::gCv]) * (temp - T(e.p[pi::T0]));
 }
-SGX_HD double gru_B_rho_e(const sgx_eos &e, const double rho_in, const double sie) {
+template <typename T> SGX_HD T gru_B_rho_e(const sgx_eos &e, const T rho_in, const T sie) {
   const double *p = e.p;
-  const double rho = smin(rho_in, p[pi::rho_max]);
-  if (rho < p[pi::rho0]) {
-    return rho * (p[pi::C0] * p[pi::C0]) + p[pi::G0] * (rho * sie + gru_P_rho_e(e, rho, sie));
+  const T rho = smin(rho_in, T(p[pi::rho_max]));
+  const T C0 = T(p[pi::C0]);
+  if (rho < T(p[pi::rho0])) {
+    return rho * (C0 * C0) + T(p[pi::G0]) * (rho * sie + gru_P_rho_e<T>(e, rho, sie));
   }
-  const double dPdr_e = gru_dPdrho_e(e, rho, sie);
-  const double dPde_r = rho * gru_gamma(e, rho);
-  return rho * dPdr_e + gru_P_rho_e(e, rho, sie) / rho * dPde_r;
+  const T dPdr_e = gru_dPdrho_e<T>(e, rho, sie);
+  const T dPde_r = rho * gru_gamma<T>(e, rho);
+  return rho * dPdr_e + gru_P_rho_e<T>(e, rho, sie) / rho * dPde_r;
 }
 
 // MaxStableDensityAtTemperature (eos_gruneisen.hpp:423-477). A reference
@@ -201,7 +205,7 @@ SGX_HD T eos_P_from_rho_sie(const sgx_eos &e, const T rho, const T sie) {
     return smax(lim<T>::small,
                 ratio(gm1 * rho * (sie - T(e.p[pi::qq])), T(1.0) - T(e.p[pi::bb]) * rho));
   case SGX_GRUNEISEN:
-    return T(gru_P_rho_e(e, double(rho), double(sie)));
+    return gru_P_rho_e<T>(e, rho, sie);
   }
   return T(0);
 }
@@ -219,8 +223,8 @@ SGX_HD T eos_P_from_rho_T(const sgx_eos &e, const T rho, const T temp) {
   case SGX_NOBLE_ABEL:
     return smax(lim<T>::small, ratio(gm1 * rho * Cv * temp, T(1.0) - T(e.p[pi::bb]) * rho));
   case SGX_GRUNEISEN: {
-    const double r = smin(double(rho), e.p[pi::rho_max]);
-    return T(gru_P_rho_e(e, r, gru_e_rho_T(e, double(temp))));
+    const T r = smin(rho, T(e.p[pi::rho_max]));
+    return gru_P_rho_e<T>(e, r, gru_e_rho_T<T>(e, temp));
   }
   }
   return T(0);
@@ -245,7 +249,7 @@ SGX_HD T eos_B_from_rho_sie(const sgx_eos &e, const T rho, const T sie) {
                 ratio(gm1 * (gm1 + T(1.0)) * rho * (sie - T(e.p[pi::qq])), omb * omb));
   }
   case SGX_GRUNEISEN:
-    return T(gru_B_rho_e(e, double(rho), double(sie)));
+    return gru_B_rho_e<T>(e, rho, sie);
   }
   return T(0);
 }
@@ -263,8 +267,8 @@ SGX_HD T eos_B_from_rho_T(const sgx_eos &e, const T rho, const T temp) {
     return smax(lim<T>::small, ratio(gm1 * (gm1 + T(1.0)) * rho * Cv * temp, omb * omb));
   }
   case SGX_GRUNEISEN: {
-    const double r = smin(double(rho), e.p[pi::rho_max]);
-    return T(gru_B_rho_e(e, r, gru_e_rho_T(e, double(temp))));
+    const T r = smin(rho, T(e.p[pi::rho_max]));
+    return gru_B_rho_e<T>(e, r, gru_e_rho_T<T>(e, temp));
   }
   }
   return T(0);
@@ -278,7 +282,7 @@ template <typename T> SGX_HD T eos_gamma(const sgx_eos &e, const T rho) {
   case SGX_NOBLE_ABEL:
     return ratio(T(e.p[pi::gm1]), (T(1.0) - T(e.p[pi::bb]) * rho));
   case SGX_GRUNEISEN:
-    return T(gru_gamma(e, smin(double(rho), e.p[pi::rho_max])));
+    return gru_gamma<T>(e, smin(rho, T(e.p[pi::rho_max])));
   }
   return T(0);
 }
@@ -292,7 +296,7 @@ template <typename T> SGX_HD T eos_min_sie(const sgx_eos &e, const T rho) {
   case SGX_STIFF_GAS:
     return eos_sie_from_rho_T<T>(e, rho, T(0.));
   case SGX_GRUNEISEN:
-    return T(gru_e_rho_T(e, 0.));
+    return gru_e_rho_T<T>(e, T(0.));
   }
   return T(0);
 }
@@ -305,7 +309,7 @@ SGX_HD double eos_max_density(const sgx_eos &e) {
 }
 SGX_HD double eos_rho_pmin(const sgx_eos &, const double) { return 0.0; }
 SGX_HD double eos_min_pressure(const sgx_eos &e) {
-  return e.type == SGX_GRUNEISEN ? gru_P_rho_e(e, 0, 0) : 0;
+  return e.type == SGX_GRUNEISEN ? gru_P_rho_e<double>(e, 0.0, 0.0) : 0;
 }
 // Gruneisen returns MaxStableDensityAtTemperature here, as the reference does
 // (eos_gruneisen.hpp:180-182).

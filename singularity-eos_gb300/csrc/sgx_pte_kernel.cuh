@@ -82,7 +82,8 @@ __global__ void __launch_bounds__(PTE_BLOCK) pte_cell_kernel(const PteArgs a) {
     o.converged = st.converged ? 1 : 0;
     o.slow_convergence_detected = st.slow ? 1 : 0;
     o.max_line_niter = static_cast<uint8_t>(st.max_line_niter);
-    o.small_step_iters = static_cast<uint8_t>(st.small_step_iters | (s.err_flags ? 0x80 : 0));
+    o.small_step_iters =
+        static_cast<uint8_t>((st.small_step_iters & 0x3F) | (s.err_flags ? 0x80 : 0));
     a.status[i] = o;
   }
 }

@@ -187,4 +187,5 @@ def status_view(status_u8):
     niter = raw[:, 8:12].copy().view(np.int32).ravel()
     return dict(residual=residual, niter=niter, converged=raw[:, 12].astype(bool),
                 slow=raw[:, 13].astype(bool), max_line_niter=raw[:, 14],
-                small_step_iters=raw[:, 15] & 0x7F, error=(raw[:, 15] & 0x80) != 0)
+                small_step_iters=raw[:, 15] & 0x3F, resolved_fp64=(raw[:, 15] & 0x40) != 0,
+                error=(raw[:, 15] & 0x80) != 0)

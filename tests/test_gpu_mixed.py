@@ -98,3 +98,46 @@ def test_mixed_rejects_unsupported_calls(sgx):
     with pytest.raises(RuntimeError, match="mixed precision"):
         sgx.fill_eos(e, x, x.clone(), x.clone(), x.clone(), None, x.clone(),
                      sgx.Q_TEMPERATURE, precision=sgx.PREC_MIXED)
+
+
+TIGHT = dict(pte_rel_tolerance_p=1e-13, pte_rel_tolerance_e=1e-13, pte_abs_tolerance_p=0.0,
+             pte_rel_tolerance_p_sufficient=1e-12, pte_rel_tolerance_e_sufficient=1e-12,
+             pte_abs_tolerance_p_sufficient=0.0)
+
+
+def run_pte(sgx, wl, precision, params=None):
+    eos_list = [sgx.make_eos(k, p) for k, p in wl["materials"]]
+    t = {k: torch.as_tensor(wl[k], device="cuda") for k in ("rho", "vfrac", "sie", "temp",
+                                                             "press")}
+    idx = torch.as_tensor(wl["eos_idx"], device="cuda") if wl["eos_idx"] is not None else None
+    n = wl["sie_tot"].shape[0]
+    status = torch.zeros(n * 16, dtype=torch.uint8, device="cuda")
+    sgx.pte_solve(sgx.PTE_RHOT, eos_list, idx, torch.as_tensor(wl["vfrac_tot"], device="cuda"),
+                  torch.as_tensor(wl["sie_tot"], device="cuda"), t["rho"], t["vfrac"], t["sie"],
+                  t["temp"], t["press"], params=params, status=status, precision=precision)
+    torch.cuda.synchronize()
+    return {k: v.cpu().numpy() for k, v in t.items()}, sgx.status_view(status)
+
+
+@pytest.mark.parametrize("kind", ["two_material", "batched"])
+def test_mixed_pte_accuracy(sgx, kind):
+    from sgx import workloads as W
+    wl = W.pte_two_material(65536, seed=5) if kind == "two_material" else \
+        W.pte_batched(1 << 18, seed=6)
+    ref, st_ref = run_pte(sgx, wl, sgx.PREC_FP64, params=sgx.mix_params(**TIGHT))
+    got, st = run_pte(sgx, wl, sgx.PREC_MIXED)
+    present = wl["eos_idx"] >= 0 if wl["eos_idx"] is not None else np.ones_like(wl["rho"], bool)
+    both = st["converged"] & st_ref["converged"]
+    resolved = st["resolved_fp64"].mean()
+    print(f"{kind}: converged mixed {st['converged'].mean():.4f} tight {st_ref['converged'].mean():.4f}"
+          f" fp64 re-solve {resolved:.4f}")
+    assert st["converged"].mean() >= st_ref["converged"].mean() - 1e-3
+    sel = both[None, :] & present
+    for k in ("temp", "press"):
+        e = scaled_err(got[k][sel], ref[k][sel])
+        print(f"  {k}: max {e.max():.2e} p99.9 {np.quantile(e, 0.999):.2e}")
+        assert np.quantile(e, 0.999) <= 1e-10, k
+    # closure constraints hold exactly in FP64 for polished cells
+    pol = st["converged"] & ~st["resolved_fp64"]
+    vsum = np.where(present, got["vfrac"], 0).sum(axis=0)
+    assert np.abs(vsum[pol] - wl["vfrac_tot"][pol]).max() <= 1e-13
