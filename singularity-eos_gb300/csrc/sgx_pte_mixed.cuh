@@ -2,7 +2,7 @@
 //
 //   1. FP32 phase: the reference's damped-Newton iteration
 //      (closure/mixed_cell_models.hpp:884-1193, 2188-2291) run entirely in
-//      float, to FP32-reachable tolerances (1e-5 relative). On GB300 the FP32
+//      float, to FP32-reachable tolerances (1e-4 relative). On GB300 the FP32
 //      pipe is ~64x the FP64 pipe, which bounds the plain path.
 //   2. FP64 polish: from the FP32 equilibrium (T, alpha_m), the energy and
 //      pressure state is rebuilt in FP64 from the cell's exact FP64 inputs
@@ -29,12 +29,12 @@ constexpr int SGX_POLISH_STEPS = 2;
 // FP32-phase controls: the reference's, with tolerances FP32 can reach.
 __device__ __forceinline__ MixP<float> fp32_params(const sgx_mix_params &q) {
   MixP<float> m(q);
-  m.tol_p = 1e-5f;
-  m.tol_e = 1e-5f;
-  m.abs_p = 1e-5f;
-  m.tol_p_suff = 1e-4f;
-  m.tol_e_suff = 1e-4f;
-  m.abs_p_suff = 1e-4f;
+  m.tol_p = 1e-4f;
+  m.tol_e = 1e-4f;
+  m.abs_p = 1e-4f;
+  m.tol_p_suff = 1e-3f;
+  m.tol_e_suff = 1e-3f;
+  m.abs_p_suff = 1e-3f;
   m.max_iter_per_mat = 32;
   m.small_step_thresh = 1e-7f;
   return m;
@@ -156,6 +156,35 @@ template <int N> __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_ke
     }
     s.Tnorm = 0.0;
     st = pte_solve<PteRhoT<double, N>, double>(s);
+    if (st.converged) {
+      // Polish the FP64 solution too, so every converged cell carries the
+      // same accuracy: back to the solver's scaled variables, then Newton.
+      double keep[5][N];
+#pragma unroll
+      for (int q = 0; q < N; ++q) {
+        keep[0][q] = s.rho[q];
+        keep[1][q] = s.vfrac[q];
+        keep[2][q] = s.sie[q];
+        keep[3][q] = s.temp[q];
+        keep[4][q] = s.press[q];
+      }
+      s.Tequil = s.temp[0] / s.Tnorm;
+      int extra = 0;
+      if (pte_polish<N>(s, SGX_POLISH_STEPS, extra)) {
+        s.finalize();
+        st.niter += extra;
+        st.residual = s.residual_norm();
+      } else {
+#pragma unroll
+        for (int q = 0; q < N; ++q) {
+          s.rho[q] = keep[0][q];
+          s.vfrac[q] = keep[1][q];
+          s.sie[q] = keep[2][q];
+          s.temp[q] = keep[3][q];
+          s.press[q] = keep[4][q];
+        }
+      }
+    }
   }
 #pragma unroll
   for (int q = 0; q < N; ++q) {
