@@ -725,9 +725,10 @@ template <typename T, int N> struct PtePT : PteBase<T, N, 2> {
 // ===========================================================================
 // PTESolver driver (:2188-2291)
 // ===========================================================================
-template <typename S, typename T> SGX_HD PteStatusLocal pte_solve(S &s) {
+// The damped-Newton loop of PTESolver (:2202-2285) from an initialised state
+// whose residual norm is `err`; fixup/finalize are left to the caller.
+template <typename S, typename T> SGX_HD PteStatusLocal pte_iterate(S &s, T err) {
   PteStatusLocal st;
-  T err = s.init();
   const MixP<T> &params = *s.P;
   bool converged = false, close_enough = false;
   const int pte_max_iter = S::n * params.max_iter_per_mat;
@@ -773,14 +774,41 @@ template <typename S, typename T> SGX_HD PteStatusLocal pte_solve(S &s) {
       break;
     }
   }
-  s.fixup();
-  s.finalize();
   st.residual = double(err);
   st.niter = niter;
   st.converged = converged;
   st.max_line_niter = max_line_niter;
   st.small_step_iters = small_step_iters;
   return st;
+}
+
+// PTESolver (:2188-2291)
+template <typename S, typename T> SGX_HD PteStatusLocal pte_solve(S &s) {
+  const T err = s.init();
+  PteStatusLocal st = pte_iterate<S, T>(s, err);
+  s.fixup();
+  s.finalize();
+  return st;
+}
+
+// FP64 continuation of the mixed-precision path: rebuilds the FP64 state at
+// the solver's current (Tequil, vfrac) -- every material's energy and
+// pressure evaluated -- and runs the same damped Newton loop under the
+// (tight) controls `tight`. Returns whether it converged; `taken` receives
+// the Newton iterations used. The caller finalizes.
+template <int N>
+SGX_HDI bool pte_polish(PteRhoT<double, N> &s, const MixP<double> &tight, int &taken) {
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+    s.dx[q] = 0.0;
+  const double err = s.test_update(0.0, true);
+  const MixP<double> *keep = s.P;
+  s.P = &tight;
+  const PteStatusLocal st = pte_iterate<PteRhoT<double, N>, double>(s, err);
+  s.P = keep;
+  s.fixup();
+  taken = st.niter;
+  return st.converged && (st.residual == st.residual);
 }
 
 } // namespace sgx

@@ -4,16 +4,16 @@
 //      (closure/mixed_cell_models.hpp:884-1193, 2188-2291) run entirely in
 //      float, to FP32-reachable tolerances (1e-4 relative). On GB300 the FP32
 //      pipe is ~64x the FP64 pipe, which bounds the plain path.
-//   2. FP64 polish: from the FP32 equilibrium (T, alpha_m), the energy and
-//      pressure state is rebuilt in FP64 from the cell's exact FP64 inputs
-//      (rhobar, uscale as InitBase computes them) and SGX_POLISH_STEPS full
-//      Newton steps of the same reduced system are taken in FP64 (finite-
-//      difference Jacobian, Jacobi-scaled solve, ScaleDx safety, no line
-//      search). The FP64 closure constraints (sum alpha = 1, sum u = u_tot) are
-//      enforced exactly by construction, as in TestUpdate.
-//   3. A cell whose FP32 phase fails, or whose polish does not reduce the FP64
-//      residual to the convergence tolerances, is re-solved by the FP64
-//      reference iteration in the same thread.
+//   2. FP64 polish: from the FP32 equilibrium (T, alpha_m) the state is
+//      rebuilt in FP64 from the cell's exact FP64 inputs (rhobar and uscale as
+//      InitBase computes them, every material's energy and pressure
+//      evaluated) and the same damped Newton loop continues in FP64 under
+//      tight controls (1e-12 relative residuals) -- typically two steps. The
+//      FP64 closure constraints (sum alpha = 1, sum u = u_tot) hold exactly by
+//      construction, as in TestUpdate.
+//   3. A cell whose FP32 phase fails, or whose polish does not converge, is
+//      re-solved by the FP64 reference iteration in the same thread and then
+//      polished the same way.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -24,7 +24,6 @@
 namespace sgx {
 
 constexpr int PTE_MIXED_BLOCK = 128;
-constexpr int SGX_POLISH_STEPS = 2;
 
 // FP32-phase controls: the reference's, with tolerances FP32 can reach.
 __device__ __forceinline__ MixP<float> fp32_params(const sgx_mix_params &q) {
@@ -40,29 +39,18 @@ __device__ __forceinline__ MixP<float> fp32_params(const sgx_mix_params &q) {
   return m;
 }
 
-// Rebuilds the FP64 state at (Tequil, vfrac) and takes `steps` Newton steps.
-// Returns true when the final FP64 residual meets the convergence test.
-template <int N>
-__device__ bool pte_polish(PteRhoT<double, N> &s, const int steps, int &taken) {
-  constexpr int n = N;
-#pragma unroll
-  for (int q = 0; q < n; ++q)
-    s.dx[q] = 0.0;
-  double err = s.test_update(0.0, true);
-  taken = 0;
-  for (int k = 0; k < steps; ++k) {
-    s.jacobian();
-    if (!s.solve()) return false;
-    const double scale = smin(1.0, s.scale_dx());
-    const double e2 = s.test_update(scale, true);
-    if (!(e2 == e2)) return false;
-    s.fixup();
-    err = e2;
-    ++taken;
-  }
-  bool conv, ok;
-  s.check(conv, ok);
-  return conv && (err == err);
+// FP64 polish controls: residuals to 1e-12 relative, at most 4 Newton
+// iterations per material.
+__device__ __forceinline__ MixP<double> polish_params(const sgx_mix_params &q) {
+  MixP<double> m(q);
+  m.tol_p = 1e-12;
+  m.tol_e = 1e-12;
+  m.abs_p = 1e-13;
+  m.tol_p_suff = 1e-10;
+  m.tol_e_suff = 1e-10;
+  m.abs_p_suff = 1e-11;
+  m.max_iter_per_mat = 4;
+  return m;
 }
 
 template <int N> __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_kernel(const PteArgs a) {
@@ -110,6 +98,7 @@ template <int N> __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_ke
   const PteStatusLocal st32 = pte_solve<PteRhoT<float, N>, float>(f);
   // ---- FP64 polish from the FP32 equilibrium ----
   const MixP<double> mp(a.params);
+  const MixP<double> tight = polish_params(a.params);
   PteRhoT<double, N> s;
   s.P = &mp;
   s.vfrac_total = a.vfrac_tot[i];
@@ -124,7 +113,9 @@ template <int N> __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_ke
   }
   bool done = false;
   int polish_steps = 0;
-  if (st32.converged && f.Tnorm > 0.0f) {
+  // the polish also rescues most cells whose FP32 phase stalled short of the
+  // FP32 tolerances; a non-finite FP32 state goes straight to the re-solve
+  if (f.Tnorm > 0.0f && f.Tequil > 0.0f && f.Tequil < 1e30f) {
     // InitBase's FP64 scalings from the exact inputs (:627-662)
     s.init_rhobar();
     const double utotal = s.rho_total * s.sie_total;
@@ -136,7 +127,7 @@ template <int N> __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_ke
 #pragma unroll
     for (int q = 0; q < N; ++q)
       s.vfrac[q] = static_cast<double>(f.vfrac[q]);
-    done = pte_polish<N>(s, SGX_POLISH_STEPS, polish_steps);
+    done = pte_polish<N>(s, tight, polish_steps);
     if (done) s.finalize();
   }
   PteStatusLocal st;
@@ -170,7 +161,7 @@ template <int N> __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_ke
       }
       s.Tequil = s.temp[0] / s.Tnorm;
       int extra = 0;
-      if (pte_polish<N>(s, SGX_POLISH_STEPS, extra)) {
+      if (pte_polish<N>(s, tight, extra)) {
         s.finalize();
         st.niter += extra;
         st.residual = s.residual_norm();
