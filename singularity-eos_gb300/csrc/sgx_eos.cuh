@@ -301,6 +301,53 @@ template <typename T> SGX_HD T eos_min_sie(const sgx_eos &e, const T rho) {
   return T(0);
 }
 
+// Partial derivatives of sie(rho, T) and P(rho, T) of the analytic models,
+// for the Jacobian of the mixed-precision solver, where finite differences in
+// FP32 cannot resolve a thermal energy that is small against a cold one.
+// Returns false for tabulated models.
+//   IdealGas  e = Cv T, P = gm1 rho Cv T
+//   StiffGas  e = Cv T + Pinf/rho + q, P = gm1 rho Cv T - Pinf
+//   NobleAbel e = Cv T + q, P = gm1 rho Cv T / (1 - b rho)
+//   Gruneisen e = Cv (T - T0), P = P(rho, e) (eos_gruneisen.hpp:331-371)
+template <typename T>
+SGX_HD bool eos_derivs(const sgx_eos &e, const T rho, const T temp, T &de_drho, T &de_dT,
+                       T &dP_drho, T &dP_dT) {
+  const T gm1 = T(e.p[pi::gm1]), Cv = T(e.p[pi::Cv]);
+  switch (e.type) {
+  case SGX_IDEAL_GAS:
+    de_drho = T(0);
+    de_dT = Cv;
+    dP_drho = gm1 * Cv * temp;
+    dP_dT = gm1 * rho * Cv;
+    return true;
+  case SGX_STIFF_GAS:
+    de_drho = -T(e.p[pi::Pinf]) / (rho * rho);
+    de_dT = Cv;
+    dP_drho = gm1 * Cv * temp;
+    dP_dT = gm1 * rho * Cv;
+    return true;
+  case SGX_NOBLE_ABEL: {
+    const T omb = T(1) - T(e.p[pi::bb]) * rho;
+    de_drho = T(0);
+    de_dT = Cv;
+    dP_drho = gm1 * Cv * temp / (omb * omb);
+    dP_dT = gm1 * rho * Cv / omb;
+    return true;
+  }
+  case SGX_GRUNEISEN: {
+    const T gCv = T(e.p[pi::gCv]);
+    const T r = smin(rho, T(e.p[pi::rho_max]));
+    const T sie = gru_e_rho_T<T>(e, temp);
+    de_drho = T(0);
+    de_dT = gCv;
+    dP_drho = gru_dPdrho_e<T>(e, r, sie);
+    dP_dT = gru_gamma<T>(e, r) * r * gCv;
+    return true;
+  }
+  }
+  return false;
+}
+
 // Bounds introspection (eos_base.hpp:594-613 defaults; Gruneisen overrides
 // at eos_gruneisen.hpp:176-183).
 SGX_HD double eos_min_temperature(const sgx_eos &) { return 0; }

@@ -408,6 +408,9 @@ template <typename T, int N> struct PteRhoT : PteBase<T, N, N> {
   T dpdv[N], dedv[N], dpdT[N], vtemp[N];
   T Tequil, Ttemp;
   int ms;
+  // Mixed-precision solver only: closed-form derivatives for the analytic
+  // models instead of the reference's finite differences.
+  bool use_analytic = false;
 
   SGX_HD void residual_eval() {
     const T esum = sum_neumaier(u, n);
@@ -473,8 +476,29 @@ template <typename T, int N> struct PteRhoT : PteBase<T, N, N> {
     conv = converged_p && converged_u;
     acceptable = acceptable_p && acceptable_u;
   }
+  // Closed-form counterpart of the finite-difference columns below (same
+  // scaled quantities: d(P_m/uscale)/d alpha_m, d u_m / d alpha_m,
+  // d(P_m/uscale)/dT and d u_m / dT with T scaled by Tnorm). False if a
+  // material is tabulated.
+  SGX_HD bool derivs_analytic(T &dedT_sum) {
+    dedT_sum = 0;
+#pragma unroll
+    for (int m = 0; m < n; m++) {
+      T de_drho, de_dT, dP_drho, dP_dT;
+      if (!eos_derivs<T>(*eos[m], rho[m], Tnorm * Tequil, de_drho, de_dT, dP_drho, dP_dT))
+        return false;
+      const T drho_dalpha = -rho[m] / vfrac[m];
+      dpdv[m] = smin(dP_drho * drho_dalpha / uscale, -sabs(P->max_dpdv));
+      dedv[m] = rhobar[m] * de_drho * drho_dalpha / uscale;
+      dpdT[m] = dP_dT * Tnorm / uscale;
+      dedT_sum += rhobar[m] * de_dT * Tnorm / uscale;
+    }
+    return true;
+  }
   SGX_HD void jacobian() {
     T dedT_sum = 0.0;
+    if (!(use_analytic && derivs_analytic(dedT_sum))) {
+    dedT_sum = 0.0;
 #pragma unroll
     for (int m = 0; m < n; m++) {
       const T dv = (vfrac[m] < T(0.5) ? T(1.0) : T(-1.0)) * vfrac[m] * P->derivative_eps;
@@ -489,6 +513,7 @@ template <typename T, int N> struct PteRhoT : PteBase<T, N, N> {
       p_pert = ratio(B::p_pref(m, rho[m], Tnorm * (Tequil + dT), e_pert), uscale);
       dpdT[m] = ratio((p_pert - press[m]), dT);
       dedT_sum += ratio(rhobar[m] * ratio(e_pert, uscale) - u[m], dT);
+    }
     }
 #pragma unroll
     for (int i = 0; i < n * n; ++i)

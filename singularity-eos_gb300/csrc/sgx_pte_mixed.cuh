@@ -1,19 +1,25 @@
 // Mixed-precision PTE (PTESolverRhoT), one thread per cell, N materials.
 //
-//   1. FP32 phase: the reference's damped-Newton iteration
-//      (closure/mixed_cell_models.hpp:884-1193, 2188-2291) run entirely in
-//      float, to FP32-reachable tolerances (1e-4 relative). On GB300 the FP32
-//      pipe is ~64x the FP64 pipe, which bounds the plain path.
-//   2. FP64 polish: from the FP32 equilibrium (T, alpha_m) the state is
-//      rebuilt in FP64 from the cell's exact FP64 inputs (rhobar and uscale as
-//      InitBase computes them, every material's energy and pressure
-//      evaluated) and the same damped Newton loop continues in FP64 under
-//      tight controls (1e-12 relative residuals) -- typically two steps. The
-//      FP64 closure constraints (sum alpha = 1, sum u = u_tot) hold exactly by
-//      construction, as in TestUpdate.
-//   3. A cell whose FP32 phase fails, or whose polish does not converge, is
-//      re-solved by the FP64 reference iteration in the same thread and then
-//      polished the same way.
+// The reduced PTE system of the reference (closure/mixed_cell_models.hpp:
+// 884-1193) in T and the N-1 free volume fractions, solved in two phases:
+//
+//   1. FP32 phase: the reference's damped Newton iteration (:2188-2291) run
+//      entirely in float to 1e-4 relative residuals. The Jacobian uses the
+//      closed-form derivatives of the analytic models (finite differences in
+//      FP32 cannot resolve a thermal energy that is small against a cold one);
+//      tabulated models keep finite differences, with a step of 2.5e-4 (the
+//      FP32 optimum) instead of 3e-6. On GB300 the FP32 pipe is ~64x the FP64
+//      pipe, which bounds the plain path.
+//   2. FP64 refinement: from the FP32 equilibrium (T, alpha_m), residual-
+//      correction steps x <- x + J32^-1 r64(x), where only the residual r64
+//      -- the energy closure sum(u_m) = u_tot and the pressure equalities --
+//      and the constraint sum(alpha_m) = 1 are evaluated in FP64 (from the
+//      cell's exact FP64 inputs, with rhobar and uscale as InitBase computes
+//      them); the Jacobian J32 and the solve stay in FP32. The iteration
+//      contracts by ~|I - J32^-1 J| ~ 1e-4 per step, so two or three steps
+//      reach 1e-12 relative residuals.
+//   3. A cell whose refinement does not converge is re-solved by the FP64
+//      reference iteration in the same thread.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -24,36 +30,125 @@
 namespace sgx {
 
 constexpr int PTE_MIXED_BLOCK = 128;
+constexpr int SGX_REFINE_STEPS = 6;
+constexpr double SGX_REFINE_TOL = 1e-12;
 
 // FP32-phase controls: the reference's, with tolerances FP32 can reach.
-__device__ __forceinline__ MixP<float> fp32_params(const sgx_mix_params &q) {
+SGX_HDI MixP<float> fp32_params(const sgx_mix_params &q) {
   MixP<float> m(q);
+  m.derivative_eps = 2.5e-4f;
   m.tol_p = 1e-4f;
   m.tol_e = 1e-4f;
   m.abs_p = 1e-4f;
   m.tol_p_suff = 1e-3f;
   m.tol_e_suff = 1e-3f;
   m.abs_p_suff = 1e-3f;
-  m.max_iter_per_mat = 32;
+  m.max_iter_per_mat = 8;
   m.small_step_thresh = 1e-7f;
   return m;
 }
 
-// FP64 polish controls: residuals to 1e-12 relative, at most 4 Newton
-// iterations per material.
-__device__ __forceinline__ MixP<double> polish_params(const sgx_mix_params &q) {
-  MixP<double> m(q);
-  m.tol_p = 1e-12;
-  m.tol_e = 1e-12;
-  m.abs_p = 1e-13;
-  m.tol_p_suff = 1e-10;
-  m.tol_e_suff = 1e-10;
-  m.abs_p_suff = 1e-11;
-  m.max_iter_per_mat = 4;
-  return m;
+// FP64 residual of the reduced system at (T, alpha) with the materials'
+// state (InitBase/TestUpdate/Residual, :627-662, 1010-1019, 1155-1187).
+template <int N> struct Refine {
+  const sgx_eos *eos[N];
+  double *lam[N];
+  double rhobar[N], alpha[N], rho[N], sie[N], u[N], press[N], res[N];
+  double T, Tnorm, uscale, utotal_scale;
+  int ms;
+
+  SGX_HDI bool eval() {
+#pragma unroll
+    for (int m = 0; m < N; ++m) {
+      if (!(alpha[m] > 0.0)) return false;
+      rho[m] = ratio(rhobar[m], alpha[m]);
+      const sgx_eos &e = *eos[m];
+      const double e_m = ev_sie_from_rho_T<double>(e, rho[m], Tnorm * T, lam[m]);
+      sie[m] = e_m;
+      u[m] = ratio(rhobar[m] * e_m, uscale);
+      const double P = (preferred_input(e) & Q_SIE)
+                           ? ev_P_from_rho_sie<double>(e, rho[m], e_m, lam[m])
+                           : ev_P_from_rho_T<double>(e, rho[m], Tnorm * T, lam[m]);
+      press[m] = ratio(P, uscale);
+    }
+    res[0] = utotal_scale - sum_neumaier(u, N);
+    int r = 1;
+#pragma unroll
+    for (int m = 0; m < N; ++m) {
+      if (m == ms) continue;
+      res[r++] = press[ms] - press[m];
+    }
+    return true;
+  }
+  // CheckPTE (:1021-1040) under the refinement tolerance.
+  SGX_HDI bool converged() const {
+    double mean_p = 0;
+#pragma unroll
+    for (int m = 0; m < N; ++m)
+      mean_p += alpha[m] * press[m];
+    double ep2 = 0;
+#pragma unroll
+    for (int r = 1; r < N; ++r)
+      ep2 += res[r] * res[r];
+#if defined(__CUDA_ARCH__)
+    const double ep = sqrt(ep2);
+#else
+    const double ep = __builtin_sqrt(ep2);
+#endif
+    return (ep < SGX_REFINE_TOL * sabs(mean_p) || ep < 0.1 * SGX_REFINE_TOL) &&
+           sabs(res[0]) < SGX_REFINE_TOL;
+  }
+};
+
+// Step 2: returns whether the FP64 residual reached the refinement tolerance.
+template <int N>
+SGX_HDI bool refine_cell(PteRhoT<float, N> &f, Refine<N> &R, int &steps) {
+  steps = 0;
+  if (!R.eval()) return false;
+  for (int k = 0; k < SGX_REFINE_STEPS; ++k) {
+    if (R.converged()) return true;
+    // FP32 Jacobian at the current state (same reduced system, same ms)
+    f.ms = R.ms;
+    f.Tequil = static_cast<float>(R.T);
+#pragma unroll
+    for (int m = 0; m < N; ++m) {
+      f.vfrac[m] = static_cast<float>(R.alpha[m]);
+      f.rho[m] = static_cast<float>(R.rho[m]);
+      f.u[m] = static_cast<float>(R.u[m]);
+      f.press[m] = static_cast<float>(R.press[m]);
+    }
+    f.jacobian();
+#pragma unroll
+    for (int r = 0; r < N; ++r)
+      f.residual[r] = static_cast<float>(R.res[r]);
+    if (!f.solve()) return false;
+    const float scale = smin(1.0f, f.scale_dx());
+    if (!(scale > 0.0f)) return false;
+    // FP64 update; the excluded material closes sum(alpha) = 1 exactly
+    R.T += static_cast<double>(f.dx[0]);
+    int idx = 1;
+#pragma unroll
+    for (int m = 0; m < N; ++m) {
+      if (m == R.ms) continue;
+      R.alpha[m] += static_cast<double>(f.dx[idx++]);
+    }
+    R.alpha[R.ms] = 1 - sum_neumaier(R.alpha, N, 0, R.ms);
+    ++steps;
+    if (!(R.T > 0.0) || !R.eval()) return false;
+    // A correction at roundoff level means the state is the FP64 fixed point:
+    // where a pressure is a small difference of large terms (a stiffened gas
+    // near P = 0) the residual itself cannot fall below its rounding noise.
+    float dmax = sabs(f.dx[0]) / static_cast<float>(R.T);
+#pragma unroll
+    for (int r = 1; r < N; ++r)
+      dmax = smax(dmax, sabs(f.dx[r]));
+    if (dmax < 1e-13f) return true;
+  }
+  return R.converged();
 }
 
-template <int N> __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_kernel(const PteArgs a) {
+template <int N>
+__global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_kernel(const PteArgs a) {
   __shared__ sgx_eos s_eos[MAX_EOS];
   for (int k = threadIdx.x; k < a.neos; k += blockDim.x)
     s_eos[k] = a.eos[k];
@@ -63,20 +158,7 @@ template <int N> __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_ke
   int slot[MAX_NMAT], eidx[MAX_NMAT];
   if (pte_gather(a, i, slot, eidx) != N) return;
   const long long nc = a.ncell;
-  double rho_in[N], vf_in[N], sie_in[N], t_in[N], p_in[N];
   double cache[N][3];
-#pragma unroll
-  for (int q = 0; q < N; ++q) {
-    const long long k = static_cast<long long>(slot[q]) * nc + i;
-    rho_in[q] = a.rho[k];
-    vf_in[q] = a.vfrac[k];
-    sie_in[q] = a.sie[k];
-    t_in[q] = a.temp[k];
-    p_in[q] = a.press[k];
-#pragma unroll
-    for (int l = 0; l < 3; ++l)
-      cache[q][l] = a.lambda ? a.lambda[(static_cast<long long>(slot[q]) * 3 + l) * nc + i] : 0.0;
-  }
   // ---- FP32 phase ----
   const MixP<float> mp32 = fp32_params(a.params);
   PteRhoT<float, N> f;
@@ -85,106 +167,99 @@ template <int N> __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_ke
   f.sie_total = static_cast<float>(a.sie_tot[i]);
   f.Tnorm = 0.0f;
   f.err_flags = 0;
+  f.use_analytic = true;
+  Refine<N> R;
 #pragma unroll
   for (int q = 0; q < N; ++q) {
-    f.eos[q] = &s_eos[eidx[q]];
-    f.lam[q] = cache[q];
-    f.rho[q] = static_cast<float>(rho_in[q]);
-    f.vfrac[q] = static_cast<float>(vf_in[q]);
-    f.sie[q] = static_cast<float>(sie_in[q]);
-    f.temp[q] = static_cast<float>(t_in[q]);
-    f.press[q] = static_cast<float>(p_in[q]);
+    const long long k = static_cast<long long>(slot[q]) * nc + i;
+#pragma unroll
+    for (int l = 0; l < 3; ++l)
+      cache[q][l] = a.lambda ? a.lambda[(static_cast<long long>(slot[q]) * 3 + l) * nc + i] : 0.0;
+    f.eos[q] = R.eos[q] = &s_eos[eidx[q]];
+    f.lam[q] = R.lam[q] = cache[q];
+    const double r_in = a.rho[k], v_in = a.vfrac[k];
+    R.rhobar[q] = r_in * v_in;
+    f.rho[q] = static_cast<float>(r_in);
+    f.vfrac[q] = static_cast<float>(v_in);
+    f.sie[q] = static_cast<float>(a.sie[k]);
+    f.temp[q] = static_cast<float>(a.temp[k]);
+    f.press[q] = static_cast<float>(a.press[k]);
   }
   const PteStatusLocal st32 = pte_solve<PteRhoT<float, N>, float>(f);
-  // ---- FP64 polish from the FP32 equilibrium ----
-  const MixP<double> mp(a.params);
-  const MixP<double> tight = polish_params(a.params);
-  PteRhoT<double, N> s;
-  s.P = &mp;
-  s.vfrac_total = a.vfrac_tot[i];
-  s.sie_total = a.sie_tot[i];
-  s.err_flags = 0;
-#pragma unroll
-  for (int q = 0; q < N; ++q) {
-    s.eos[q] = &s_eos[eidx[q]];
-    s.lam[q] = cache[q];
-    s.rho[q] = rho_in[q];
-    s.vfrac[q] = vf_in[q];
-  }
+  // ---- FP64 refinement from the FP32 equilibrium ----
+  // InitBase's scalings from the exact FP64 inputs (:388-399, 632-635)
+  const double rho_total = sum_neumaier(R.rhobar, N);
+  const double utotal = rho_total * a.sie_tot[i];
+  R.uscale = smax(sabs(utotal), 1.0e-14);
+  R.utotal_scale = ratio(utotal, R.uscale);
   bool done = false;
-  int polish_steps = 0;
-  // the polish also rescues most cells whose FP32 phase stalled short of the
-  // FP32 tolerances; a non-finite FP32 state goes straight to the re-solve
+  int steps = 0;
   if (f.Tnorm > 0.0f && f.Tequil > 0.0f && f.Tequil < 1e30f) {
-    // InitBase's FP64 scalings from the exact inputs (:627-662)
-    s.init_rhobar();
-    const double utotal = s.rho_total * s.sie_total;
-    s.uscale = smax(sabs(utotal), 1.0e-14);
-    s.utotal_scale = ratio(utotal, s.uscale);
-    s.Tnorm = static_cast<double>(f.Tnorm);
-    s.Tequil = static_cast<double>(f.Tequil);
-    s.ms = f.ms;
+    R.Tnorm = static_cast<double>(f.Tnorm);
+    R.T = static_cast<double>(f.Tequil);
+    R.ms = f.ms;
 #pragma unroll
     for (int q = 0; q < N; ++q)
-      s.vfrac[q] = static_cast<double>(f.vfrac[q]);
-    done = pte_polish<N>(s, tight, polish_steps);
-    if (done) s.finalize();
+      R.alpha[q] = static_cast<double>(f.vfrac[q]);
+    R.alpha[R.ms] = 1 - sum_neumaier(R.alpha, N, 0, R.ms);
+    done = refine_cell<N>(f, R, steps);
   }
   PteStatusLocal st;
+  double out_rho[N], out_vf[N], out_sie[N], out_T[N], out_P[N];
   if (done) {
     st.converged = true;
-    st.niter = st32.niter + polish_steps;
-    st.residual = s.residual_norm();
-  } else {
-    // the FP64 reference iteration from the original inputs
+    st.niter = st32.niter + steps;
+    double r2 = 0;
+#pragma unroll
+    for (int r = 0; r < N; ++r)
+      r2 += R.res[r] * R.res[r];
+    st.residual = 0.5 * r2;
 #pragma unroll
     for (int q = 0; q < N; ++q) {
-      s.rho[q] = rho_in[q];
-      s.vfrac[q] = vf_in[q];
-      s.sie[q] = sie_in[q];
-      s.temp[q] = t_in[q];
-      s.press[q] = p_in[q];
+      out_rho[q] = R.rho[q];
+      out_vf[q] = R.alpha[q];
+      out_sie[q] = R.sie[q];
+      out_T[q] = R.T * R.Tnorm;
+      out_P[q] = R.press[q] * R.uscale;
     }
+  } else {
+    // the FP64 reference iteration from the original inputs
+    const MixP<double> mp(a.params);
+    PteRhoT<double, N> s;
+    s.P = &mp;
+    s.vfrac_total = a.vfrac_tot[i];
+    s.sie_total = a.sie_tot[i];
     s.Tnorm = 0.0;
+    s.err_flags = 0;
+#pragma unroll
+    for (int q = 0; q < N; ++q) {
+      const long long k = static_cast<long long>(slot[q]) * nc + i;
+      s.eos[q] = &s_eos[eidx[q]];
+      s.lam[q] = cache[q];
+      s.rho[q] = a.rho[k];
+      s.vfrac[q] = a.vfrac[k];
+      s.sie[q] = a.sie[k];
+      s.temp[q] = a.temp[k];
+      s.press[q] = a.press[k];
+    }
     st = pte_solve<PteRhoT<double, N>, double>(s);
-    if (st.converged) {
-      // Polish the FP64 solution too, so every converged cell carries the
-      // same accuracy: back to the solver's scaled variables, then Newton.
-      double keep[5][N];
 #pragma unroll
-      for (int q = 0; q < N; ++q) {
-        keep[0][q] = s.rho[q];
-        keep[1][q] = s.vfrac[q];
-        keep[2][q] = s.sie[q];
-        keep[3][q] = s.temp[q];
-        keep[4][q] = s.press[q];
-      }
-      s.Tequil = s.temp[0] / s.Tnorm;
-      int extra = 0;
-      if (pte_polish<N>(s, tight, extra)) {
-        s.finalize();
-        st.niter += extra;
-        st.residual = s.residual_norm();
-      } else {
-#pragma unroll
-        for (int q = 0; q < N; ++q) {
-          s.rho[q] = keep[0][q];
-          s.vfrac[q] = keep[1][q];
-          s.sie[q] = keep[2][q];
-          s.temp[q] = keep[3][q];
-          s.press[q] = keep[4][q];
-        }
-      }
+    for (int q = 0; q < N; ++q) {
+      out_rho[q] = s.rho[q];
+      out_vf[q] = s.vfrac[q];
+      out_sie[q] = s.sie[q];
+      out_T[q] = s.temp[q];
+      out_P[q] = s.press[q];
     }
   }
 #pragma unroll
   for (int q = 0; q < N; ++q) {
     const long long k = static_cast<long long>(slot[q]) * nc + i;
-    a.rho[k] = s.rho[q];
-    a.vfrac[k] = s.vfrac[q];
-    a.sie[k] = s.sie[q];
-    a.temp[k] = s.temp[q];
-    a.press[k] = s.press[q];
+    a.rho[k] = out_rho[q];
+    a.vfrac[k] = out_vf[q];
+    a.sie[k] = out_sie[q];
+    a.temp[k] = out_T[q];
+    a.press[k] = out_P[q];
     if (a.lambda) {
 #pragma unroll
       for (int l = 0; l < 3; ++l)
@@ -198,8 +273,7 @@ template <int N> __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_ke
     o.converged = st.converged ? 1 : 0;
     o.slow_convergence_detected = st.slow ? 1 : 0;
     o.max_line_niter = static_cast<uint8_t>(st.max_line_niter);
-    o.small_step_iters = static_cast<uint8_t>((st.small_step_iters & 0x3F) | (done ? 0 : 0x40) |
-                                              (s.err_flags ? 0x80 : 0));
+    o.small_step_iters = static_cast<uint8_t>((st.small_step_iters & 0x3F) | (done ? 0 : 0x40));
     a.status[i] = o;
   }
 }
