@@ -26,6 +26,10 @@ struct PteArgs {
   double *rho, *vfrac, *sie, *temp, *press, *lambda;
   sgx_pte_status *status;
   sgx_mix_params params;
+  // Mixed path only: cells whose FP32 solve + FP64 refinement fail are queued
+  // here (retry_idx[0 .. *retry_count)) for a second, FP64 pass.
+  int *retry_idx;
+  unsigned *retry_count;
 };
 
 // Per-cell PTE, FP64, following the reference iteration exactly.

@@ -18,8 +18,11 @@
 //      them); the Jacobian J32 and the solve stay in FP32. The iteration
 //      contracts by ~|I - J32^-1 J| ~ 1e-4 per step, so two or three steps
 //      reach 1e-12 relative residuals.
-//   3. A cell whose refinement does not converge is re-solved by the FP64
-//      reference iteration in the same thread.
+//   3. A cell whose refinement does not converge is appended to a retry queue
+//      and left untouched; a second kernel drains the compacted queue with the
+//      FP64 reference iteration (then refines it the same way), so the few hard
+//      cells -- some need hundreds of iterations -- no longer hold up the
+//      warps of the easy ones.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -147,6 +150,41 @@ SGX_HDI bool refine_cell(PteRhoT<float, N> &f, Refine<N> &R, int &steps) {
   return R.converged();
 }
 
+// Writes one cell's equilibrium state, lambda cache and status.
+template <int N>
+__device__ __forceinline__ void pte_store(const PteArgs &a, const long long i,
+                                          const int (&slot)[MAX_NMAT], const double *rho,
+                                          const double *vf, const double *sie, const double *T,
+                                          const double *P, const double (&cache)[N][3],
+                                          const PteStatusLocal &st, const int flags) {
+  const long long nc = a.ncell;
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+    const long long k = static_cast<long long>(slot[q]) * nc + i;
+    a.rho[k] = rho[q];
+    a.vfrac[k] = vf[q];
+    a.sie[k] = sie[q];
+    a.temp[k] = T[q];
+    a.press[k] = P[q];
+    if (a.lambda) {
+#pragma unroll
+      for (int l = 0; l < 3; ++l)
+        a.lambda[(static_cast<long long>(slot[q]) * 3 + l) * nc + i] = cache[q][l];
+    }
+  }
+  if (a.status) {
+    sgx_pte_status o;
+    o.residual = st.residual;
+    o.niter = st.niter;
+    o.converged = st.converged ? 1 : 0;
+    o.slow_convergence_detected = st.slow ? 1 : 0;
+    o.max_line_niter = static_cast<uint8_t>(st.max_line_niter);
+    o.small_step_iters = static_cast<uint8_t>((st.small_step_iters & 0x3F) | flags);
+    a.status[i] = o;
+  }
+}
+
+// Pass 1: every cell with N materials, FP32 solve + FP64 refinement.
 template <int N>
 __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_kernel(const PteArgs a) {
   __shared__ sgx_eos s_eos[MAX_EOS];
@@ -204,27 +242,46 @@ __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_kernel(const PteArg
     R.alpha[R.ms] = 1 - sum_neumaier(R.alpha, N, 0, R.ms);
     done = refine_cell<N>(f, R, steps);
   }
+  if (!done) {
+    const unsigned pos = atomicAdd(a.retry_count, 1u);
+    a.retry_idx[pos] = static_cast<int>(i);
+    return;
+  }
   PteStatusLocal st;
-  double out_rho[N], out_vf[N], out_sie[N], out_T[N], out_P[N];
-  if (done) {
-    st.converged = true;
-    st.niter = st32.niter + steps;
-    double r2 = 0;
+  st.converged = true;
+  st.niter = st32.niter + steps;
+  double r2 = 0;
 #pragma unroll
-    for (int r = 0; r < N; ++r)
-      r2 += R.res[r] * R.res[r];
-    st.residual = 0.5 * r2;
+  for (int r = 0; r < N; ++r)
+    r2 += R.res[r] * R.res[r];
+  st.residual = 0.5 * r2;
+  double out_T[N], out_P[N];
 #pragma unroll
-    for (int q = 0; q < N; ++q) {
-      out_rho[q] = R.rho[q];
-      out_vf[q] = R.alpha[q];
-      out_sie[q] = R.sie[q];
-      out_T[q] = R.T * R.Tnorm;
-      out_P[q] = R.press[q] * R.uscale;
-    }
-  } else {
-    // the FP64 reference iteration from the original inputs
-    const MixP<double> mp(a.params);
+  for (int q = 0; q < N; ++q) {
+    out_T[q] = R.T * R.Tnorm;
+    out_P[q] = R.press[q] * R.uscale;
+  }
+  pte_store<N>(a, i, slot, R.rho, R.alpha, R.sie, out_T, out_P, cache, st, 0);
+}
+
+// Pass 2: the queued cells with N materials, FP64 reference iteration
+// (:2188-2291) from the original inputs, then the same FP64 refinement.
+template <int N>
+__global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_retry_kernel(const PteArgs a) {
+  __shared__ sgx_eos s_eos[MAX_EOS];
+  for (int k = threadIdx.x; k < a.neos; k += blockDim.x)
+    s_eos[k] = a.eos[k];
+  __syncthreads();
+  const unsigned count = *a.retry_count;
+  const long long nc = a.ncell;
+  const MixP<double> mp(a.params);
+  const MixP<float> mp32 = fp32_params(a.params);
+  for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < count;
+       t += gridDim.x * blockDim.x) {
+    const long long i = a.retry_idx[t];
+    int slot[MAX_NMAT], eidx[MAX_NMAT];
+    if (pte_gather(a, i, slot, eidx) != N) continue;
+    double cache[N][3];
     PteRhoT<double, N> s;
     s.P = &mp;
     s.vfrac_total = a.vfrac_tot[i];
@@ -234,6 +291,9 @@ __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_kernel(const PteArg
 #pragma unroll
     for (int q = 0; q < N; ++q) {
       const long long k = static_cast<long long>(slot[q]) * nc + i;
+#pragma unroll
+      for (int l = 0; l < 3; ++l)
+        cache[q][l] = a.lambda ? a.lambda[(static_cast<long long>(slot[q]) * 3 + l) * nc + i] : 0.0;
       s.eos[q] = &s_eos[eidx[q]];
       s.lam[q] = cache[q];
       s.rho[q] = a.rho[k];
@@ -242,7 +302,8 @@ __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_kernel(const PteArg
       s.temp[q] = a.temp[k];
       s.press[q] = a.press[k];
     }
-    st = pte_solve<PteRhoT<double, N>, double>(s);
+    PteStatusLocal st = pte_solve<PteRhoT<double, N>, double>(s);
+    double out_rho[N], out_vf[N], out_sie[N], out_T[N], out_P[N];
 #pragma unroll
     for (int q = 0; q < N; ++q) {
       out_rho[q] = s.rho[q];
@@ -251,36 +312,59 @@ __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_kernel(const PteArg
       out_T[q] = s.temp[q];
       out_P[q] = s.press[q];
     }
-  }
+    if (st.converged) {
+      // refine the FP64 solution to the same tolerance as pass 1
+      PteRhoT<float, N> f;
+      f.P = &mp32;
+      f.use_analytic = true;
+      f.vfrac_total = static_cast<float>(s.vfrac_total);
+      f.Tnorm = static_cast<float>(s.Tnorm);
+      f.uscale = static_cast<float>(s.uscale);
+      Refine<N> R;
 #pragma unroll
-  for (int q = 0; q < N; ++q) {
-    const long long k = static_cast<long long>(slot[q]) * nc + i;
-    a.rho[k] = out_rho[q];
-    a.vfrac[k] = out_vf[q];
-    a.sie[k] = out_sie[q];
-    a.temp[k] = out_T[q];
-    a.press[k] = out_P[q];
-    if (a.lambda) {
+      for (int q = 0; q < N; ++q) {
+        f.eos[q] = R.eos[q] = s.eos[q];
+        f.lam[q] = R.lam[q] = cache[q];
+        f.rhobar[q] = static_cast<float>(s.rhobar[q]);
+        R.rhobar[q] = s.rhobar[q];
+        R.alpha[q] = s.vfrac[q];
+      }
+      R.uscale = s.uscale;
+      R.utotal_scale = s.utotal_scale;
+      R.Tnorm = s.Tnorm;
+      R.T = s.temp[0] / s.Tnorm;
+      R.ms = s.ms;
+      int steps = 0;
+      if (refine_cell<N>(f, R, steps)) {
+        st.niter += steps;
 #pragma unroll
-      for (int l = 0; l < 3; ++l)
-        a.lambda[(static_cast<long long>(slot[q]) * 3 + l) * nc + i] = cache[q][l];
+        for (int q = 0; q < N; ++q) {
+          out_rho[q] = R.rho[q];
+          out_vf[q] = R.alpha[q];
+          out_sie[q] = R.sie[q];
+          out_T[q] = R.T * R.Tnorm;
+          out_P[q] = R.press[q] * R.uscale;
+        }
+      }
     }
-  }
-  if (a.status) {
-    sgx_pte_status o;
-    o.residual = st.residual;
-    o.niter = st.niter;
-    o.converged = st.converged ? 1 : 0;
-    o.slow_convergence_detected = st.slow ? 1 : 0;
-    o.max_line_niter = static_cast<uint8_t>(st.max_line_niter);
-    o.small_step_iters = static_cast<uint8_t>((st.small_step_iters & 0x3F) | (done ? 0 : 0x40));
-    a.status[i] = o;
+    pte_store<N>(a, i, slot, out_rho, out_vf, out_sie, out_T, out_P, cache, st, 0x40);
   }
 }
 
 template <int N> cudaError_t launch_pte_mixed_n(const PteArgs &a, cudaStream_t stream) {
   const long long blocks = (a.ncell + PTE_MIXED_BLOCK - 1) / PTE_MIXED_BLOCK;
   pte_mixed_kernel<N><<<static_cast<unsigned>(blocks), PTE_MIXED_BLOCK, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+template <int N> cudaError_t launch_pte_retry_n(const PteArgs &a, cudaStream_t stream) {
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  // sized for the worst case but never more than a few waves; threads past
+  // the queue length exit at once
+  long long blocks = (a.ncell + PTE_MIXED_BLOCK - 1) / PTE_MIXED_BLOCK;
+  if (blocks > 4LL * sms) blocks = 4LL * sms;
+  pte_retry_kernel<N><<<static_cast<unsigned>(blocks), PTE_MIXED_BLOCK, 0, stream>>>(a);
   return cudaGetLastError();
 }
 

@@ -8,4 +8,5 @@
 
 namespace sgx {
 template cudaError_t launch_pte_mixed_n<SGX_PTE_N>(const PteArgs &, cudaStream_t);
+template cudaError_t launch_pte_retry_n<SGX_PTE_N>(const PteArgs &, cudaStream_t);
 } // namespace sgx
