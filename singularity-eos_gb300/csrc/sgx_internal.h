@@ -26,11 +26,18 @@ struct PteArgs {
   double *rho, *vfrac, *sie, *temp, *press, *lambda;
   sgx_pte_status *status;
   sgx_mix_params params;
-  // Mixed path only: cells whose FP32 solve + FP64 refinement fail are queued
-  // here (retry_idx[0 .. *retry_count)) for a second, FP64 pass.
+  // Mixed path only (device scratch):
+  //  - perm: cell ids grouped by material count, the cells with n materials
+  //    at perm[sum(bins[0..n)) ...] (null when every cell holds nmat);
+  //  - bins[0..8): cells per material count; bins[8..16): scatter cursors;
+  //    bins[16..24): retry-queue length per material count;
+  //  - retry_idx: cells whose FP32 solve + FP64 refinement failed, queued for
+  //    a second, FP64 pass (reused by each material count in turn).
+  const int *perm;
+  unsigned *bins;
   int *retry_idx;
-  unsigned *retry_count;
 };
+constexpr int PTE_BINS = 8;
 
 // Per-cell PTE, FP64, following the reference iteration exactly.
 cudaError_t launch_pte_fp64(const PteArgs &a, cudaStream_t stream);

@@ -1,10 +1,18 @@
 // Dispatch of the mixed-precision PTE kernels (one instantiation per
-// material count, built from sgx_pte_mixed_n.cu): pass 1 for every material
-// count, then pass 2 over the compacted retry queue.
+// material count, built from sgx_pte_mixed_n.cu).
 //
-// The queue (one int per cell plus a counter) is stream-ordered scratch from
-// the device's default memory pool (cudaMallocAsync / cudaFreeAsync on the
-// caller's stream), so concurrent calls on different streams never share it.
+// With an index map (cells holding different numbers of materials), the
+// cells are first binned by material count -- a counting kernel, then a
+// scatter of cell ids into perm[] grouped by count -- so that each per-count
+// kernel runs full warps instead of masking off the lanes of the other
+// counts. Then, for each count N in turn: pass 1 (FP32 solve + FP64
+// refinement) over the N-bin, and pass 2 (FP64 re-solve) over the cells
+// pass 1 queued.
+//
+// The scratch (a 256-byte counter block, perm[ncell], retry_idx[ncell]) is
+// stream-ordered memory from the device's default pool (cudaMallocAsync /
+// cudaFreeAsync on the caller's stream), so calls on different streams never
+// share it.
 #include <cuda_runtime.h>
 
 #include "sgx_internal.h"
@@ -15,6 +23,60 @@ template <int N> cudaError_t launch_pte_mixed_n(const PteArgs &a, cudaStream_t s
 template <int N> cudaError_t launch_pte_retry_n(const PteArgs &a, cudaStream_t stream);
 
 namespace {
+
+constexpr int BIN_BLOCK = 256;
+
+__device__ __forceinline__ int pte_count(const PteArgs &a, const long long i) {
+  int n = 0;
+  for (int m = 0; m < a.nmat; ++m) {
+    const int ie = a.eos_idx[static_cast<long long>(m) * a.ncell + i];
+    n += (ie >= 0 && ie < a.neos) ? 1 : 0;
+  }
+  return n;
+}
+
+// bins[n] = number of cells with n materials.
+__global__ void __launch_bounds__(BIN_BLOCK) pte_bin_count(const PteArgs a) {
+  __shared__ unsigned h[PTE_BINS];
+  if (threadIdx.x < PTE_BINS) h[threadIdx.x] = 0;
+  __syncthreads();
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < a.ncell;
+       i += stride)
+    atomicAdd(&h[pte_count(a, i)], 1u);
+  __syncthreads();
+  if (threadIdx.x < PTE_BINS && h[threadIdx.x]) atomicAdd(&a.bins[threadIdx.x], h[threadIdx.x]);
+}
+
+// perm[offset(n) + k] = cell id, cells of equal count taken warp by warp
+// (ascending within a warp, so neighbouring lanes of the solve kernels
+// mostly touch nearby cells).
+__global__ void __launch_bounds__(BIN_BLOCK) pte_bin_scatter(const PteArgs a, int *perm) {
+  __shared__ unsigned off[PTE_BINS];
+  if (threadIdx.x == 0) {
+    unsigned s = 0;
+    for (int n = 0; n < PTE_BINS; ++n) {
+      off[n] = s;
+      s += a.bins[n];
+    }
+  }
+  __syncthreads();
+  unsigned *cursor = a.bins + PTE_BINS;
+  const unsigned lane = threadIdx.x & 31u;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  // warp-uniform trip count: every lane runs every round
+  for (long long base = static_cast<long long>(blockIdx.x) * blockDim.x; base < a.ncell;
+       base += stride) {
+    const long long i = base + threadIdx.x;
+    const int n = i < a.ncell ? pte_count(a, i) : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, n);
+    const int leader = __ffs(peers) - 1;
+    unsigned pos = 0;
+    if (n >= 0 && static_cast<int>(lane) == leader) pos = atomicAdd(&cursor[n], __popc(peers));
+    pos = __shfl_sync(0xffffffffu, pos, leader);
+    if (n >= 0) perm[off[n] + pos + __popc(peers & ((1u << lane) - 1u))] = static_cast<int>(i);
+  }
+}
 
 template <bool RETRY> cudaError_t launch_n(const int n, const PteArgs &a, cudaStream_t s) {
   switch (n) {
@@ -30,29 +92,50 @@ template <bool RETRY> cudaError_t launch_n(const int n, const PteArgs &a, cudaSt
 
 } // namespace
 
-cudaError_t launch_pte_mixed_with(const PteArgs &args, cudaStream_t stream) {
-  const int lo = args.eos_idx ? 1 : args.nmat;
-  const int hi = args.nmat < PTE_MAX_N ? args.nmat : PTE_MAX_N;
-  cudaError_t e = cudaMemsetAsync(args.retry_count, 0, sizeof(unsigned), stream);
-  for (int n = lo; n <= hi && e == cudaSuccess; ++n)
-    e = launch_n<false>(n, args, stream);
-  for (int n = lo; n <= hi && e == cudaSuccess; ++n)
-    e = launch_n<true>(n, args, stream);
+// Runs the binning and both passes with caller-provided scratch: bins (the
+// 3 * PTE_BINS counters), and perm (when eos_idx is set) and retry_idx of
+// ncell ints each.
+cudaError_t launch_pte_mixed_with(const PteArgs &args, int *perm, cudaStream_t stream) {
+  PteArgs a = args;
+  a.perm = nullptr;
+  cudaError_t e = cudaMemsetAsync(a.bins, 0, 3 * PTE_BINS * sizeof(unsigned), stream);
+  if (e != cudaSuccess) return e;
+  const int lo = a.eos_idx ? 1 : a.nmat;
+  const int hi = a.nmat < PTE_MAX_N ? a.nmat : PTE_MAX_N;
+  if (a.eos_idx) {
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess)
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long want = (a.ncell + BIN_BLOCK - 1) / BIN_BLOCK;
+    const long long cap = 4LL * sms;
+    const int grid = static_cast<int>(want < cap ? want : cap);
+    pte_bin_count<<<grid, BIN_BLOCK, 0, stream>>>(a);
+    pte_bin_scatter<<<grid, BIN_BLOCK, 0, stream>>>(a, perm);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    a.perm = perm;
+  }
+  for (int n = lo; n <= hi && e == cudaSuccess; ++n) {
+    e = launch_n<false>(n, a, stream);
+    if (e == cudaSuccess) e = launch_n<true>(n, a, stream);
+  }
   return e;
 }
 
 cudaError_t launch_pte_mixed(const PteArgs &a, cudaStream_t stream) {
   if (a.ncell <= 0) return cudaSuccess;
   if (a.solver != SGX_PTE_RHOT) return cudaErrorNotSupported;
-  if (a.ncell > 0x7fffffffLL) return cudaErrorInvalidValue; // queue holds int32 cell ids
+  if (a.ncell > 0x7fffffffLL) return cudaErrorInvalidValue; // int32 cell ids in perm / queue
   PteArgs args = a;
   void *scratch = nullptr;
-  const size_t bytes = 256 + static_cast<size_t>(a.ncell) * sizeof(int);
+  const size_t n4 = ((static_cast<size_t>(a.ncell) * sizeof(int) + 255) / 256) * 256;
+  const size_t bytes = 256 + (a.eos_idx ? 2 : 1) * n4;
   cudaError_t e = cudaMallocAsync(&scratch, bytes, stream);
   if (e != cudaSuccess) return e;
-  args.retry_count = static_cast<unsigned *>(scratch);
-  args.retry_idx = reinterpret_cast<int *>(static_cast<char *>(scratch) + 256);
-  e = launch_pte_mixed_with(args, stream);
+  char *p = static_cast<char *>(scratch);
+  args.bins = reinterpret_cast<unsigned *>(p);
+  args.retry_idx = reinterpret_cast<int *>(p + 256);
+  int *perm = a.eos_idx ? reinterpret_cast<int *>(p + 256 + n4) : nullptr;
+  e = launch_pte_mixed_with(args, perm, stream);
   const cudaError_t f = cudaFreeAsync(scratch, stream);
   return e != cudaSuccess ? e : f;
 }

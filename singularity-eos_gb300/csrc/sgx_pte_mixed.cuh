@@ -184,6 +184,22 @@ __device__ __forceinline__ void pte_store(const PteArgs &a, const long long i,
   }
 }
 
+// Cell id of the t-th cell with N materials (false past the bin's end).
+template <int N> __device__ __forceinline__ bool pte_bin_cell(const PteArgs &a, long long t,
+                                                              long long &i) {
+  if (!a.perm) {
+    i = t;
+    return t < a.ncell;
+  }
+  unsigned off = 0;
+#pragma unroll
+  for (int n = 0; n < N; ++n)
+    off += a.bins[n];
+  if (t >= a.bins[N]) return false;
+  i = a.perm[off + t];
+  return true;
+}
+
 // Pass 1: every cell with N materials, FP32 solve + FP64 refinement.
 template <int N>
 __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_kernel(const PteArgs a) {
@@ -191,8 +207,9 @@ __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_kernel(const PteArg
   for (int k = threadIdx.x; k < a.neos; k += blockDim.x)
     s_eos[k] = a.eos[k];
   __syncthreads();
-  const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= a.ncell) return;
+  long long i;
+  if (!pte_bin_cell<N>(a, static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x, i))
+    return;
   int slot[MAX_NMAT], eidx[MAX_NMAT];
   if (pte_gather(a, i, slot, eidx) != N) return;
   const long long nc = a.ncell;
@@ -243,7 +260,7 @@ __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_kernel(const PteArg
     done = refine_cell<N>(f, R, steps);
   }
   if (!done) {
-    const unsigned pos = atomicAdd(a.retry_count, 1u);
+    const unsigned pos = atomicAdd(&a.bins[2 * PTE_BINS + N], 1u);
     a.retry_idx[pos] = static_cast<int>(i);
     return;
   }
@@ -264,15 +281,17 @@ __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_kernel(const PteArg
   pte_store<N>(a, i, slot, R.rho, R.alpha, R.sie, out_T, out_P, cache, st, 0);
 }
 
-// Pass 2: the queued cells with N materials, FP64 reference iteration
-// (:2188-2291) from the original inputs, then the same FP64 refinement.
+// Pass 2: the queued cells with N materials (pass 1 for N and pass 2 for N
+// run back to back on one stream, so the queue holds only them), FP64
+// reference iteration (:2188-2291) from the original inputs, then the same
+// FP64 refinement.
 template <int N>
 __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_retry_kernel(const PteArgs a) {
   __shared__ sgx_eos s_eos[MAX_EOS];
   for (int k = threadIdx.x; k < a.neos; k += blockDim.x)
     s_eos[k] = a.eos[k];
   __syncthreads();
-  const unsigned count = *a.retry_count;
+  const unsigned count = a.bins[2 * PTE_BINS + N];
   const long long nc = a.ncell;
   const MixP<double> mp(a.params);
   const MixP<float> mp32 = fp32_params(a.params);
