@@ -221,6 +221,32 @@ int sgx_pte_solve(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list, 
                   double *lambda, const sgx_mix_params *params, sgx_pte_status *status,
                   int precision, sgx_stream_t stream);
 
+/* Largest ncell sgx_pte_solve_noalloc accepts. */
+#define SGX_PTE_NOALLOC_MAX_CELLS 1048576
+
+/* sgx_pte_solve with precision SGX_PREC_MIXED and solver SGX_PTE_RHOT, for
+ * callers that must not allocate device memory at solve time (host codes
+ * that hand all device memory to their own allocator at start-up). It has
+ * no reference counterpart. Arguments and results are those of
+ * sgx_pte_solve; the solver's scratch (8 bytes per cell plus 256 bytes) is a
+ * static device array of the library sized for SGX_PTE_NOALLOC_MAX_CELLS
+ * cells, so nothing is allocated.
+ *  - ncell > SGX_PTE_NOALLOC_MAX_CELLS returns SGX_ERR_INVALID before any
+ *    device work; split the batch or call sgx_pte_solve.
+ *  - solver other than SGX_PTE_RHOT returns SGX_ERR_UNSUPPORTED.
+ *  - The first call on a device looks up the array's device address (with
+ *    that device current) and caches it; make that first call before any
+ *    stream capture begins.
+ *  - There is one array per device: calls that overlap in time on the same
+ *    device (other streams, other host threads) race on it and give wrong
+ *    results. Order them on one stream or serialise them. */
+int sgx_pte_solve_noalloc(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list,
+                          int neos, const int32_t *eos_idx, const double *vfrac_tot,
+                          const double *sie_tot, double *rho, double *vfrac, double *sie,
+                          double *temp, double *press, double *lambda,
+                          const sgx_mix_params *params, sgx_pte_status *status,
+                          sgx_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

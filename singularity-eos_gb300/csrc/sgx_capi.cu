@@ -292,4 +292,63 @@ int sgx_pte_solve(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list, 
   return SGX_OK;
 }
 
+// The mixed RhoT solve with static scratch (sgx_noalloc.cu); argument checks
+// as sgx_pte_solve's, plus the scratch capacity, all before any CUDA call.
+int sgx_pte_solve_noalloc(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list,
+                          int neos, const int32_t *eos_idx, const double *vfrac_tot,
+                          const double *sie_tot, double *rho, double *vfrac, double *sie,
+                          double *temp, double *press, double *lambda,
+                          const sgx_mix_params *params, sgx_pte_status *status,
+                          sgx_stream_t stream) {
+  static const char *who = "sgx_pte_solve_noalloc";
+  if (solver != SGX_PTE_RHOT && solver != SGX_PTE_PT)
+    return fail(SGX_ERR_INVALID, std::string(who) + ": bad solver");
+  if (solver != SGX_PTE_RHOT)
+    return fail(SGX_ERR_UNSUPPORTED, std::string(who) + ": only SGX_PTE_RHOT");
+  if (nmat < 1 || nmat > sgx::PTE_MAX_N)
+    return fail(SGX_ERR_UNSUPPORTED, std::string(who) + ": nmat must be in 1..6");
+  if (neos < 1 || neos > sgx::MAX_EOS || !eos_list)
+    return fail(SGX_ERR_INVALID, std::string(who) + ": neos must be in 1..16");
+  if (!eos_idx && neos < nmat)
+    return fail(SGX_ERR_INVALID, std::string(who) + ": eos_idx NULL needs neos >= nmat");
+  if (ncell < 0) return fail(SGX_ERR_INVALID, std::string(who) + ": ncell < 0");
+  if (ncell > SGX_PTE_NOALLOC_MAX_CELLS)
+    return fail(SGX_ERR_INVALID,
+                std::string(who) + ": ncell = " + std::to_string(ncell) +
+                    " exceeds the static scratch capacity of SGX_PTE_NOALLOC_MAX_CELLS = " +
+                    std::to_string(SGX_PTE_NOALLOC_MAX_CELLS) +
+                    " cells; split the batch or call sgx_pte_solve");
+  if (ncell == 0) return SGX_OK;
+  if (!vfrac_tot || !sie_tot || !rho || !vfrac || !sie || !temp || !press)
+    return fail(SGX_ERR_INVALID, std::string(who) + ": null array");
+  for (int k = 0; k < neos; ++k)
+    if (!valid_type(eos_list[k].type))
+      return fail(SGX_ERR_INVALID, std::string(who) + ": bad eos");
+  sgx::PteArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.solver = solver;
+  a.nmat = nmat;
+  a.ncell = ncell;
+  a.neos = neos;
+  for (int k = 0; k < neos; ++k)
+    a.eos[k] = eos_list[k];
+  a.eos_idx = eos_idx;
+  a.vfrac_tot = vfrac_tot;
+  a.sie_tot = sie_tot;
+  a.rho = rho;
+  a.vfrac = vfrac;
+  a.sie = sie;
+  a.temp = temp;
+  a.press = press;
+  a.lambda = lambda;
+  a.status = status;
+  if (params)
+    a.params = *params;
+  else
+    sgx_mix_params_default(&a.params);
+  const cudaError_t e = sgx::launch_pte_mixed_noalloc(a, reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, who);
+  return SGX_OK;
+}
+
 } // extern "C"

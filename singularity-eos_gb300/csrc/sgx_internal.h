@@ -43,6 +43,11 @@ constexpr int PTE_BINS = 8;
 cudaError_t launch_pte_fp64(const PteArgs &a, cudaStream_t stream);
 // Per-cell PTE, FP32 iterations then FP64 refinement.
 cudaError_t launch_pte_mixed(const PteArgs &a, cudaStream_t stream);
+// The same with caller-provided scratch: a.bins (3 * PTE_BINS counters),
+// a.retry_idx and, when a.eos_idx is set, perm (ncell ints each).
+cudaError_t launch_pte_mixed_with(const PteArgs &a, int *perm, cudaStream_t stream);
+// The same with the scratch in a static device array (sgx_noalloc.cu).
+cudaError_t launch_pte_mixed_noalloc(const PteArgs &a, cudaStream_t stream);
 
 struct EvalArgs {
   sgx_eos eos;

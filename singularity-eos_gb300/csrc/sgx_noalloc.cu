@@ -1,0 +1,77 @@
+// The mixed-precision PTE dispatch of sgx_mixed.cu with its scratch in a
+// fixed device array of this module instead of pool memory.
+//
+// Who needs it: host codes that reserve, at start-up, all the device memory
+// they will ever use for their own allocator and forbid allocations after
+// that. For them the stream-ordered pool allocation inside the mixed path of
+// sgx_pte_solve can fail, or break the memory budget they planned. Here the
+// scratch -- the 256-byte counter block, the cell ids binned by material
+// count and the retry queue, 8 bytes per cell -- is a static __device__
+// array sized for SGX_PTE_NOALLOC_MAX_CELLS cells (8 MiB + 256 B), part of
+// the module's image. No call here allocates device or pinned memory.
+//
+// The array's device address is looked up once per device, with that device
+// current, and cached; the first call on a device does this look-up (which
+// also loads this module onto the device) and should come before any stream
+// capture begins. There is one array per device, so calls that overlap in
+// time on one device -- from two streams or two host threads -- race on it.
+#include <mutex>
+
+#include <cuda_runtime.h>
+
+#include "sgx_internal.h"
+
+namespace {
+
+constexpr size_t NOALLOC_IDS_BYTES =
+    (static_cast<size_t>(SGX_PTE_NOALLOC_MAX_CELLS) * sizeof(int) + 255) / 256 * 256;
+constexpr size_t NOALLOC_BYTES = 256 + 2 * NOALLOC_IDS_BYTES;
+
+} // namespace
+
+static __device__ __align__(256) unsigned char sgx_pte_noalloc_scratch[NOALLOC_BYTES];
+
+namespace sgx {
+
+namespace {
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_scratch_mu;
+char *g_scratch[NOALLOC_MAX_DEVICES];
+
+cudaError_t scratch_on_current_device(char **out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, sgx_pte_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_scratch[dev] = static_cast<char *>(p);
+  }
+  *out = g_scratch[dev];
+  return cudaSuccess;
+}
+
+} // namespace
+
+cudaError_t launch_pte_mixed_noalloc(const PteArgs &a, cudaStream_t stream) {
+  if (a.ncell <= 0) return cudaSuccess;
+  if (a.solver != SGX_PTE_RHOT) return cudaErrorNotSupported;
+  if (a.ncell > SGX_PTE_NOALLOC_MAX_CELLS) return cudaErrorInvalidValue;
+  char *p = nullptr;
+  const cudaError_t e = scratch_on_current_device(&p);
+  if (e != cudaSuccess) return e;
+  PteArgs args = a;
+  // launch_pte_mixed_with zeroes the counter block (bin counts, scatter
+  // cursors, queue lengths) on the stream before its first kernel; the id
+  // arrays are written before they are read and need no clearing.
+  args.bins = reinterpret_cast<unsigned *>(p);
+  args.retry_idx = reinterpret_cast<int *>(p + 256);
+  int *perm = a.eos_idx ? reinterpret_cast<int *>(p + 256 + NOALLOC_IDS_BYTES) : nullptr;
+  return launch_pte_mixed_with(args, perm, stream);
+}
+
+} // namespace sgx

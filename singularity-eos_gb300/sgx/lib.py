@@ -24,8 +24,9 @@ EXPORTED = [
     "sgx_eos_table_bytes", "sgx_eos_spiner_dump", "sgx_eos_eval", "sgx_eos_fill",
     "sgx_eos_fill_ex",
     "sgx_mix_params_default", "sgx_pte_rhot_required_scratch", "sgx_pte_pt_required_scratch",
-    "sgx_pte_solve",
+    "sgx_pte_solve", "sgx_pte_solve_noalloc",
 ]
+PTE_NOALLOC_MAX_CELLS = 1 << 20  # SGX_PTE_NOALLOC_MAX_CELLS
 
 
 class SgxEos(C.Structure):
@@ -93,6 +94,8 @@ def load():
     lib.sgx_mix_params_default.argtypes = [C.POINTER(MixParams)]
     lib.sgx_pte_solve.argtypes = [I, I, C.c_int64, P, I, P, P, P, P, P, P, P, P, P,
                                   C.POINTER(MixParams), P, I, P]
+    lib.sgx_pte_solve_noalloc.argtypes = [I, I, C.c_int64, P, I, P, P, P, P, P, P, P, P, P,
+                                          C.POINTER(MixParams), P, P]
     _lib = lib
     return lib
 
@@ -176,6 +179,20 @@ def pte_solve(solver, eos_list, eos_idx, vfrac_tot, sie_tot, rho, vfrac, sie, te
         solver, nmat, ncell, C.cast(arr, C.c_void_p), len(eos_list), ptr(eos_idx),
         ptr(vfrac_tot), ptr(sie_tot), ptr(rho), ptr(vfrac), ptr(sie), ptr(temp), ptr(press),
         ptr(lam), C.byref(params) if params is not None else None, ptr(status), precision,
+        stream_ptr(stream)))
+
+
+def pte_solve_noalloc(eos_list, eos_idx, vfrac_tot, sie_tot, rho, vfrac, sie, temp, press,
+                      lam=None, params=None, status=None, stream=None):
+    """pte_solve(PTE_RHOT, ..., precision=PREC_MIXED) through the entry point
+    whose scratch is a static device array (at most PTE_NOALLOC_MAX_CELLS
+    cells; calls must not overlap in time on one device)."""
+    nmat, ncell = rho.shape
+    arr = (SgxEos * len(eos_list))(*eos_list)
+    check(load().sgx_pte_solve_noalloc(
+        PTE_RHOT, nmat, ncell, C.cast(arr, C.c_void_p), len(eos_list), ptr(eos_idx),
+        ptr(vfrac_tot), ptr(sie_tot), ptr(rho), ptr(vfrac), ptr(sie), ptr(temp), ptr(press),
+        ptr(lam), C.byref(params) if params is not None else None, ptr(status),
         stream_ptr(stream)))
 
 
