@@ -54,6 +54,19 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def fp_peaks():
+    """FP64 / FP32 FMA throughput of this device, from the probe that
+    singularity-eos_gb300/build.py builds (None when it is missing)."""
+    exe = os.path.join(ROOT, "singularity-eos_gb300", "lib", "sgx_fma_peak")
+    if not os.path.exists(exe):
+        return None
+    try:
+        r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+        return json.loads(r.stdout.strip().splitlines()[-1]) if r.returncode == 0 else None
+    except (subprocess.SubprocessError, ValueError, IndexError):
+        return None
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle sampling during the timed region."""
 
@@ -140,24 +153,23 @@ def time_steps(fn, steps, warmup, stream):
     return start.elapsed_time(stop) / 1e3
 
 
-def lookup_inputs(table_dir):
+def lookup_inputs(table_dir, n):
     from sgx import sp5lite
     path = os.path.join(table_dir, "stiffgas.sp5")
     sp5lite.stiffgas_table(path)
-    rho, sie = sp5lite.stiffgas_queries(N_LOOKUP, seed=2024)
+    rho, sie = sp5lite.stiffgas_queries(n, seed=2024)
     return path, rho, sie
 
 
-def run_ours(args):
+def bench_lookup(args, world, local, stream, out):
+    """The headline workload: FillEos(T|P|bmod) + cs over --queries queries,
+    mixed precision (headline) and plain FP64, plus the e2e leg."""
     import torch
-    from sgx import lib, workloads as W
-    world, rank, local = dist_setup()
-    torch.cuda.set_device(local)
-    stream = torch.cuda.current_stream()
+    from sgx import lib
+    n = args.queries
     hbm, hbm_kind = peaks()
-    out = {}
     with tempfile.TemporaryDirectory() as td:
-        path, rho_h, sie_h = lookup_inputs(td)
+        path, rho_h, sie_h = lookup_inputs(td, n)
         tab = lib.spiner_eos(path, 1)
         rho = torch.as_tensor(rho_h, device="cuda")
         sie = torch.as_tensor(sie_h, device="cuda")
@@ -178,8 +190,8 @@ def run_ours(args):
             barrier(world)
             dt = max_over_ranks(dt, world)
             per_launch = dt / steps
-            results[name] = dict(value=world * N_LOOKUP * steps / dt, ms=per_launch * 1e3,
-                                 gbs=LOOKUP_BYTES_PER_QUERY * N_LOOKUP / per_launch / 1e9,
+            results[name] = dict(value=world * n * steps / dt, ms=per_launch * 1e3,
+                                 gbs=LOOKUP_BYTES_PER_QUERY * n / per_launch / 1e9,
                                  clocks=clk.summary(), steps=steps)
         m = results["mixed"]
         out["clocks"] = m["clocks"]
@@ -187,38 +199,51 @@ def run_ours(args):
                            "frac": m["gbs"] / hbm, "traffic": None,
                            "peak_kind": hbm_kind + " (burst copy)",
                            "kernel": "spiner_fill_mixed (sgx_lookup_mixed.cu)",
-                           "bytes_per_query": LOOKUP_BYTES_PER_QUERY}
+                           "bytes_per_query": LOOKUP_BYTES_PER_QUERY,
+                           # the kernel is bound by the FP64 pipe, not HBM (ncu capture
+                           # in profiles/spiner_fill_mixed_lookup_4M.md)
+                           "fp64_pipe_pct_active_ncu": 83.7}
         f = results["fp64"]
         out["plain_fp64"] = {"value": f["value"], "unit": "lookups/s", "ms_per_step": f["ms"],
                              "hbm_frac": f["gbs"] / hbm, "clocks": f["clocks"],
                              "kernel": "fill_kernel (sgx_fp64.cu)"}
-        # e2e: host buffers in pinned memory, copies inside the timed region
-        rho_p = torch.as_tensor(rho_h).pin_memory()
-        sie_p = torch.as_tensor(sie_h).pin_memory()
-        outs_p = [torch.empty(N_LOOKUP, dtype=torch.float64).pin_memory() for _ in range(4)]
+        if not args.no_e2e:
+            # e2e: host buffers in pinned memory, copies inside the timed region
+            rho_p = torch.as_tensor(rho_h).pin_memory()
+            sie_p = torch.as_tensor(sie_h).pin_memory()
+            outs_p = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(4)]
 
-        def e2e_step():
-            rho.copy_(rho_p, non_blocking=True)
-            sie.copy_(sie_p, non_blocking=True)
-            lib.fill_eos(tab, rho, T, sie, P, None, B, Q_OUT, cs=CS, precision=lib.PREC_MIXED,
-                         stream=stream)
-            for h, d in zip(outs_p, (T, P, B, CS)):
-                h.copy_(d, non_blocking=True)
+            def e2e_step():
+                rho.copy_(rho_p, non_blocking=True)
+                sie.copy_(sie_p, non_blocking=True)
+                lib.fill_eos(tab, rho, T, sie, P, None, B, Q_OUT, cs=CS,
+                             precision=lib.PREC_MIXED, stream=stream)
+                for h, d in zip(outs_p, (T, P, B, CS)):
+                    h.copy_(d, non_blocking=True)
 
-        e2e_steps = max(1, min(args.steps, 5))
-        barrier(world)
-        dte = max_over_ranks(time_steps(e2e_step, e2e_steps, 1, stream), world)
-        out["e2e"] = {"value": world * N_LOOKUP * e2e_steps / dte, "unit": "lookups/s",
-                      "h2d_bytes_per_step": 16 * N_LOOKUP, "d2h_bytes_per_step": 32 * N_LOOKUP}
+            e2e_steps = max(1, min(args.steps, 5))
+            barrier(world)
+            dte = max_over_ranks(time_steps(e2e_step, e2e_steps, 1, stream), world)
+            out["e2e"] = {"value": world * n * e2e_steps / dte, "unit": "lookups/s",
+                          "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 32 * n}
         lib.load().sgx_eos_finalize(__import__("ctypes").byref(tab))
         out["value"], out["ms_per_step"] = m["value"], m["ms"]
         out["gpu_launches"] = m["steps"]
 
-    # PTE workloads: plain FP64 (the reference iteration) and mixed precision
-    # (FP32 iterations + FP64 polish to 1e-12 residuals)
+
+def bench_pte(args, world, stream, out):
+    """PTE closure: plain FP64 (the reference iteration) and mixed precision
+    (FP32 iterations + FP64 refinement), on the two-material and the uneven
+    batched workloads."""
+    import torch
+    from sgx import lib, workloads as W
     pte = {}
-    for name, wl_fn, n in (("pte_2mat_65536", W.pte_two_material, N_PTE2),
-                           ("pte_batched_2^22", W.pte_batched, N_PTE_BATCH)):
+    cases = []
+    if args.only in ("all", "pte", "pte2"):
+        cases.append((f"pte_2mat_{args.pte2_cells}", W.pte_two_material, args.pte2_cells))
+    if args.only in ("all", "pte", "ptebatch"):
+        cases.append((f"pte_batched_{args.pte_cells}", W.pte_batched, args.pte_cells))
+    for name, wl_fn, n in cases:
         wl = wl_fn(n, seed=77)
         eos_list = [lib.make_eos(k, p) for k, p in wl["materials"]]
         base = {k: torch.as_tensor(wl[k], device="cuda") for k in
@@ -230,6 +255,9 @@ def run_ours(args):
         status = torch.empty(n * 16, dtype=torch.uint8, device="cuda")
         entry = {}
         for prec, pname in ((lib.PREC_FP64, "fp64"), (lib.PREC_MIXED, "mixed")):
+            if args.pte_prec not in ("both", pname):
+                continue
+
             def pstep():
                 for k in work:
                     work[k].copy_(base[k])
@@ -238,14 +266,31 @@ def run_ours(args):
                               precision=prec, stream=stream)
 
             ps = max(1, min(args.steps, 5))
-            dt = max_over_ranks(time_steps(pstep, ps, 2, stream), world)
+            dt = max_over_ranks(time_steps(pstep, ps, args.warmup, stream), world)
             sv = lib.status_view(status)
             entry[pname] = {"cells_per_s": world * n * ps / dt, "ms_per_step": dt / ps * 1e3,
                             "converged_frac": float(sv["converged"].mean()),
                             "fp64_resolve_frac": float(sv["resolved_fp64"].mean())}
-        entry["mixed_over_fp64"] = entry["mixed"]["cells_per_s"] / entry["fp64"]["cells_per_s"]
+        if "fp64" in entry and "mixed" in entry:
+            entry["mixed_over_fp64"] = entry["mixed"]["cells_per_s"] / \
+                entry["fp64"]["cells_per_s"]
         pte[name] = entry
     out["pte"] = pte
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    out = {}
+    if args.only in ("all", "lookup"):
+        bench_lookup(args, world, local, stream, out)
+    if args.only != "lookup":
+        bench_pte(args, world, stream, out)
+    fp = fp_peaks()
+    if fp:
+        out["fp_peaks"] = fp
     return out, world, rank
 
 
@@ -284,12 +329,21 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    # smaller cases and single legs, for profiling runs
+    ap.add_argument("--queries", type=int, default=N_LOOKUP)
+    ap.add_argument("--pte-cells", type=int, default=N_PTE_BATCH)
+    ap.add_argument("--pte2-cells", type=int, default=N_PTE2)
+    ap.add_argument("--only", default="all",
+                    choices=["all", "lookup", "pte", "pte2", "ptebatch"])
+    ap.add_argument("--pte-prec", default="both", choices=["both", "fp64", "mixed"])
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     config = {"workload": "vector tabulated EOS lookup (FillEos T|P|bmod + sound speed), "
                           "2^24 queries, 256x256 NQT-log StiffGas-sampled rho-T table",
-              "queries": N_LOOKUP, "table": "256x256", "l2": "inputs (256 MB) larger than L2"}
+              "queries": args.queries, "table": "256x256",
+              "l2": f"inputs ({16 * args.queries >> 20} MB) vs 129 MB L2"}
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:
             return
@@ -307,14 +361,19 @@ def main():
     out, world, rank = run_ours(args)
     if rank != 0:
         return
+    if "value" not in out:  # a PTE-only profiling run: no headline line
+        print(json.dumps({"pte": out["pte"], "fp_peaks": out.get("fp_peaks")}))
+        return
     line = {"metric": METRIC, "value": out["value"], "unit": "lookups/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64 (f32 bracket search)",
             "data": "synthetic (seeded; StiffGas-sampled table)", "config": config,
-            "e2e": out["e2e"], "roofline": out["roofline"], "clocks": out["clocks"],
+            "e2e": out.get("e2e"), "roofline": out["roofline"], "clocks": out["clocks"],
             "gpu_launches": out["gpu_launches"], "plain_fp64": out["plain_fp64"],
-            "pte": out["pte"]}
+            "pte": out.get("pte"), "fp_peaks": out.get("fp_peaks")}
+    if "e2e" not in out:
+        line["e2e"] = None
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline()
     print(json.dumps(line))
