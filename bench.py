@@ -41,6 +41,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 N_LOOKUP = 1 << 24
 N_PTE2 = 65536
 N_PTE_BATCH = 1 << 22
+N_HELM = 1 << 22
 LOOKUP_BYTES_PER_QUERY = 16 + 32  # rho, sie in; T, P, bmod, cs out (float64)
 Q_OUT = 8 | 4 | 32                # temperature | pressure | bulk modulus
 METRIC = "PTE mixed cells/s & EOS lookups/s, 1 GB300, batched+FP32-refined vs plain FP64"
@@ -278,6 +279,50 @@ def bench_pte(args, world, stream, out):
     out["pte"] = pte
 
 
+def bench_helm(args, world, stream, out):
+    """Helmholtz EOS, default options (radiation, ions, degenerate electrons,
+    Coulomb corrections) on the synthetic electron table: per cell, the
+    forward FillEos (rho, T -> sie) builds the inputs once; the timed step is
+    the inversion FillEos(rho, sie -> T, P, bmod) + cs from a cold lT cache
+    (no guess: the cache is reset every step, so every cell runs its full
+    Newton iteration)."""
+    import torch
+    from sgx import helmtable, lib
+    n = args.helm_cells
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "helm_table.dat")
+        helmtable.helm_table(path)
+        eos = lib.helmholtz_eos(path)
+        rho_h, T_h, abar, zbar = helmtable.helm_queries(n, seed=77)
+        rho = torch.as_tensor(rho_h, device="cuda")
+        Tin = torch.as_tensor(T_h, device="cuda")
+        lam0 = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+        lam0[:, 0] = torch.as_tensor(abar, device="cuda")
+        lam0[:, 1] = torch.as_tensor(zbar, device="cuda")
+        lam0[:, 2] = float("nan")
+        lam = lam0.clone()
+        sie = torch.empty_like(rho)
+        lib.fill_eos(eos, rho, Tin, sie, None, None, None, lib.Q_SIE, lam=lam, lam_stride=3,
+                     stream=stream)
+        T, P, B, CS = (torch.empty_like(rho) for _ in range(4))
+        q = lib.Q_TEMPERATURE | lib.Q_PRESSURE | lib.Q_BULK_MODULUS
+
+        def step():
+            lam.copy_(lam0)
+            lib.fill_eos(eos, rho, T, sie, P, None, B, q, lam=lam, lam_stride=3, cs=CS,
+                         stream=stream)
+
+        steps = max(1, min(args.steps, 5))
+        dt = max_over_ranks(time_steps(step, steps, args.warmup, stream), world)
+        rel = ((T - Tin).abs() / Tin).cpu().numpy()
+        out["helmholtz"] = {
+            "workload": f"Helmholtz T(rho,sie)+P+bmod+cs, {n} cells, synthetic 271x101 table",
+            "cells_per_s": world * n * steps / dt, "ms_per_step": dt / steps * 1e3,
+            "dtype": "f64", "recovered_T_1e-8_frac": float((rel <= 1e-8).mean()),
+            "kernel": "helm_fill_kernel (sgx_helm.cu)"}
+        lib.load().sgx_eos_finalize(__import__("ctypes").byref(eos))
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_setup()
@@ -286,8 +331,10 @@ def run_ours(args):
     out = {}
     if args.only in ("all", "lookup"):
         bench_lookup(args, world, local, stream, out)
-    if args.only != "lookup":
+    if args.only in ("all", "pte", "pte2", "ptebatch"):
         bench_pte(args, world, stream, out)
+    if args.only in ("all", "helm"):
+        bench_helm(args, world, stream, out)
     fp = fp_peaks()
     if fp:
         out["fp_peaks"] = fp
@@ -333,8 +380,9 @@ def main():
     ap.add_argument("--queries", type=int, default=N_LOOKUP)
     ap.add_argument("--pte-cells", type=int, default=N_PTE_BATCH)
     ap.add_argument("--pte2-cells", type=int, default=N_PTE2)
+    ap.add_argument("--helm-cells", type=int, default=N_HELM)
     ap.add_argument("--only", default="all",
-                    choices=["all", "lookup", "pte", "pte2", "ptebatch"])
+                    choices=["all", "lookup", "pte", "pte2", "ptebatch", "helm"])
     ap.add_argument("--pte-prec", default="both", choices=["both", "fp64", "mixed"])
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
@@ -361,8 +409,8 @@ def main():
     out, world, rank = run_ours(args)
     if rank != 0:
         return
-    if "value" not in out:  # a PTE-only profiling run: no headline line
-        print(json.dumps({"pte": out["pte"], "fp_peaks": out.get("fp_peaks")}))
+    if "value" not in out:  # a profiling run of one leg: no headline line
+        print(json.dumps({k: out.get(k) for k in ("pte", "helmholtz", "fp_peaks")}))
         return
     line = {"metric": METRIC, "value": out["value"], "unit": "lookups/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["ms_per_step"],
@@ -371,7 +419,7 @@ def main():
             "data": "synthetic (seeded; StiffGas-sampled table)", "config": config,
             "e2e": out.get("e2e"), "roofline": out["roofline"], "clocks": out["clocks"],
             "gpu_launches": out["gpu_launches"], "plain_fp64": out["plain_fp64"],
-            "pte": out.get("pte"), "fp_peaks": out.get("fp_peaks")}
+            "pte": out.get("pte"), "helmholtz": out.get("helmholtz"), "fp_peaks": out.get("fp_peaks")}
     if "e2e" not in out:
         line["e2e"] = None
     if not args.no_cpu_baseline and world == 1:

@@ -166,6 +166,31 @@ int sgx_eos_gruneisen(sgx_eos *out, double C0, double s1, double s2, double s3,
  * tables (SpinerEOSDependsRhoT::loadDataboxes_, eos_spiner_rho_temp.hpp:545-687)
  * and makes the table resident on the current device. */
 int sgx_eos_spiner_rhot(sgx_eos *out, const char *path, int matid, int reproducible);
+/* Option bits of sgx_eos_helmholtz (Helmholtz::Options, eos_helmholtz.hpp:420-441). */
+enum {
+  SGX_HELM_RAD = 1,            /* ENABLE_RAD */
+  SGX_HELM_GAS = 2,            /* ENABLE_GAS */
+  SGX_HELM_COUL = 4,           /* ENABLE_COULOMB_CORRECTIONS */
+  SGX_HELM_ION = 8,            /* GAS_IONIZED */
+  SGX_HELM_ELE = 16,           /* GAS_DEGENERATE */
+  SGX_HELM_DEFAULT = 31,       /* the reference's defaults: all of the above */
+  SGX_HELM_REGULA_FALSI = 32,  /* USE_NEWTON_RAPHSON = false */
+  SGX_HELM_CACHE_READBACK = 64 /* reproduce the reference's lT cache read-back (below) */
+};
+/* Loads the electron free-energy table of the Helmholtz EOS from a file in
+ * the reference's helm_table.dat layout (HelmElectrons::InitDataFile_,
+ * eos_helmholtz.hpp:962-989) and makes it resident on the current device;
+ * replaces Helmholtz(filename, options) + GetOnDevice(). Abar, Zbar and the
+ * log10 T cache come in per element through lambda rows [Abar, Zbar, lT]
+ * (Helmholtz::Lambda, :409-416), so every lookup needs lambda (stride >= 3).
+ * T(rho, sie) stores the root in the lT cache. The reference ends
+ * lTFromRhoSie_ (:957) by reading the cache back over the root, which with a
+ * plain array lambda returns the guess instead of the root;
+ * SGX_HELM_CACHE_READBACK reproduces that. */
+int sgx_eos_helmholtz(sgx_eos *out, const char *path, int options);
+/* Node values and fields of a Helmholtz table in the reference's DBLIST order
+ * (rho_, T_, f_ .. xfdt_; eos_helmholtz.hpp:281-292); returns the count or -1. */
+long sgx_eos_helmholtz_dump(const sgx_eos *eos, double *out, long cap);
 /* Releases a tabulated EOS's device table (no-op for analytic models). */
 int sgx_eos_finalize(sgx_eos *eos);
 /* Size in bytes of the device table behind a tabulated EOS (0 if analytic). */

@@ -189,6 +189,27 @@ class Oracle:
             raise RuntimeError(f"{self.prefix}_eos_bounds failed")
         return out
 
+    def helm_dump(self, path):
+        f = self._fn("helm_dump")
+        f.restype = C.c_long
+        n = f(path.encode(), None, C.c_long(0))
+        if n < 0:
+            raise RuntimeError("helm_dump failed")
+        out = np.zeros(n)
+        f(path.encode(), _dp(out), C.c_long(n))
+        return out
+
+    def helm_T_from_rho_sie(self, path, rho, sie, abar, zbar):
+        """T(rho, sie) of the default-option Helmholtz EOS without the lT
+        cache read-back (reference library only)."""
+        n = rho.shape[0]
+        T = np.zeros(n)
+        rc = self._fn("helm_T_from_rho_sie")(path.encode(), C.c_int(n), _dp(rho), _dp(sie),
+                                             _dp(abar), _dp(zbar), _dp(T))
+        if rc != 0:
+            raise RuntimeError("helm_T_from_rho_sie failed")
+        return T
+
     def spiner_dump(self, path, matid):
         scal = np.zeros(8)
         n = self._fn("spiner_dump")(path.encode(), C.c_int(matid), None, C.c_long(0),

@@ -446,6 +446,78 @@ long sgref_spiner_dump(const char *path, int matid, double *out, long cap, doubl
   }
 }
 
+// The Helmholtz table as the reference holds it after loading
+// (HelmElectrons::DumpDynamicMemory: node values, then the 21 fields in
+// DBLIST order, eos_helmholtz.hpp:281-292).
+long sgref_helm_dump(const char *path, double *out, long cap) {
+  try {
+    Helmholtz eos{std::string(path)};
+    const long n = static_cast<long>(eos.DynamicMemorySizeInBytes() / sizeof(double));
+    if (out && cap >= n) eos.DumpDynamicMemory(reinterpret_cast<char *>(out));
+    eos.Finalize();
+    return n;
+  } catch (const std::exception &ex) {
+    std::fprintf(stderr, "sgref_helm_dump: %s\n", ex.what());
+    return -1;
+  }
+}
+
+// T(rho, sie) of the Helmholtz EOS as lTFromRhoSie_ (eos_helmholtz.hpp:867-960)
+// intends it, without the final read of the lT cache over the root: the
+// reference's own RootFinding1D::newton_raphson and regula_falsi over the
+// reference's public e(rho, T) and cv(rho, T), from the analytic guess
+// (lTAnalytic_, :728-731), for the default options. The lambda cache is
+// absent here, so the reference's defect does not arise.
+int sgref_helm_T_from_rho_sie(const char *path, int n, const double *rho, const double *sie,
+                              const double *abar, const double *zbar, double *T) {
+  try {
+    const Helmholtz eos{std::string(path)};
+    for (int i = 0; i < n; ++i) {
+      const Real r = rho[i], e = sie[i];
+      auto eval = [&](const Real t, Real &ee, Real &cv) {
+        Real lam[3] = {abar[i], zbar[i], 0.0};
+        ee = eos.InternalEnergyFromDensityTemperature(r, t, lam);
+        cv = eos.SpecificHeatFromDensityTemperature(r, t, lam);
+      };
+      const Real abari = robust::ratio(1.0, abar[i]);
+      const Real ni = abari * r * HelmIon::NA;
+      const Real ne = zbar[i] * ni;
+      Real lTguess = std::log10((2.0 / 3.0) * robust::ratio(e * r, ni + ne) * HelmIon::KBi);
+      if (!((3.0 <= lTguess) && (lTguess <= 13.0))) lTguess = 8;
+      const Real Tguess = math_utils::pow10(lTguess);
+      const Real Ta = math_utils::pow10(3.0), Tb = math_utils::pow10(13.0);
+      Real Tr = 0;
+      auto status = RootFinding1D::newton_raphson(
+          [&](Real t) {
+            Real ee, cv;
+            eval(t, ee, cv);
+            return std::make_tuple(ee, cv);
+          },
+          e, Tguess, Ta, Tb, 1e-10, Tr, nullptr, false, false);
+      if (status != RootFinding1D::Status::SUCCESS) {
+        status = RootFinding1D::regula_falsi(
+            [&](Real t) {
+              Real ee, cv;
+              eval(t, ee, cv);
+              return ee;
+            },
+            e, Tguess, Ta, Tb, 1e-14, 1e-14, Tr, nullptr, false);
+        if (status != RootFinding1D::Status::SUCCESS)
+          Tr = math_utils::pow10(
+              std::log10((2.0 / 3.0) * robust::ratio(e * r, ni + ne) * HelmIon::KBi));
+      }
+      Real lT = std::log10(Tr);
+      if (lT < 3.0) lT = 3.0;
+      if (lT > 13.0) lT = 13.0;
+      T[i] = math_utils::pow10(lT);
+    }
+  } catch (const std::exception &ex) {
+    std::fprintf(stderr, "sgref_helm_T_from_rho_sie: %s\n", ex.what());
+    return 1;
+  }
+  return 0;
+}
+
 // FastMath NQT transforms (logs.hpp:188-214, 282-292), element-wise.
 void sgref_nqt(int which, int n, const double *x, double *y) {
   for (int i = 0; i < n; ++i)

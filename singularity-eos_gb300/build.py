@@ -29,6 +29,7 @@ UNITS = [
     ("sgx_capi", "sgx_capi.cu", ["--fmad=false"]),
     ("sgx_table", "sgx_table.cu", ["--fmad=false"]),
     ("sgx_noalloc", "sgx_noalloc.cu", ["--fmad=false"]),
+    ("sgx_helm", "sgx_helm.cu", ["--fmad=false"]),
 ] + [(f"sgx_pte_fp64_n{n}", "sgx_pte_fp64_n.cu", ["--fmad=false", f"-DSGX_PTE_N={n}"])
      for n in range(1, 7)] + [
     (f"sgx_pte_mixed_n{n}", "sgx_pte_mixed_n.cu", ["--fmad=true", f"-DSGX_PTE_N={n}"])

@@ -27,7 +27,9 @@ int cuda_fail(cudaError_t e, const char *what) {
   return fail(SGX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-bool valid_type(int t) { return t >= SGX_IDEAL_GAS && t <= SGX_SPINER_RHOT; }
+bool valid_type(int t) { return t >= SGX_IDEAL_GAS && t <= SGX_HELMHOLTZ; }
+// Models the PTE kernels dispatch on (Helmholtz is a lookup-only model here).
+bool pte_type(int t) { return t >= SGX_IDEAL_GAS && t <= SGX_SPINER_RHOT; }
 
 } // namespace
 
@@ -145,6 +147,31 @@ int sgx_eos_spiner_rhot(sgx_eos *out, const char *path, int matid, int reproduci
   return SGX_OK;
 }
 
+int sgx_eos_helmholtz(sgx_eos *out, const char *path, int options) {
+  if (!out || !path) return fail(SGX_ERR_INVALID, "sgx_eos_helmholtz: null");
+  if (options & ~127) return fail(SGX_ERR_INVALID, "sgx_eos_helmholtz: unknown option bits");
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+    return fail(SGX_ERR_NO_DEVICE, "sgx_eos_helmholtz: no CUDA device");
+  std::string msg;
+  uint64_t handle = 0;
+  const int rc = sgx::table_load_helm(path, &handle, msg);
+  if (rc != SGX_OK) return fail(rc, msg);
+  std::memset(out, 0, sizeof(*out));
+  out->type = SGX_HELMHOLTZ;
+  out->flags = options;
+  out->table = handle;
+  return SGX_OK;
+}
+
+long sgx_eos_helmholtz_dump(const sgx_eos *eos, double *out, long cap) {
+  if (!eos || eos->type != SGX_HELMHOLTZ || !eos->table) {
+    fail(SGX_ERR_INVALID, "sgx_eos_helmholtz_dump: not a Helmholtz EOS");
+    return -1;
+  }
+  return sgx::table_dump(eos->table, out, cap);
+}
+
 int sgx_eos_finalize(sgx_eos *eos) {
   if (!eos) return fail(SGX_ERR_INVALID, "sgx_eos_finalize: null");
   if (eos->table) {
@@ -178,6 +205,15 @@ int sgx_eos_eval(const sgx_eos *eos, int fn, int64_t n, const double *in1, const
   if (!in1 || !out || (!in2 && fn != SGX_FN_MIN_SIE_FROM_RHO))
     return fail(SGX_ERR_INVALID, "sgx_eos_eval: null array");
   if (lambda && lambda_stride < 2) return fail(SGX_ERR_INVALID, "sgx_eos_eval: lambda_stride < 2");
+  if (eos->type == SGX_HELMHOLTZ) {
+    // Abar and Zbar come in through lambda (SafeMustGet in the reference)
+    if (!lambda || lambda_stride < 3)
+      return fail(SGX_ERR_INVALID, "sgx_eos_eval: Helmholtz needs lambda rows [Abar, Zbar, lT]");
+    if (fn == SGX_FN_MIN_SIE_FROM_RHO)
+      return fail(SGX_ERR_UNSUPPORTED,
+                  "sgx_eos_eval: MinInternalEnergyFromDensity needs a temperature of 0, "
+                  "outside the Helmholtz table");
+  }
   sgx::EvalArgs a;
   a.eos = *eos;
   a.fn = fn;
@@ -187,7 +223,9 @@ int sgx_eos_eval(const sgx_eos *eos, int fn, int64_t n, const double *in1, const
   a.out = out;
   a.lambda = lambda;
   a.lambda_stride = lambda_stride;
-  const cudaError_t e = sgx::launch_eval_fp64(a, reinterpret_cast<cudaStream_t>(stream));
+  const cudaError_t e = eos->type == SGX_HELMHOLTZ
+                            ? sgx::launch_helm_eval(a, reinterpret_cast<cudaStream_t>(stream))
+                            : sgx::launch_eval_fp64(a, reinterpret_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "sgx_eos_eval");
   return SGX_OK;
 }
@@ -202,6 +240,20 @@ int sgx_eos_fill_ex(const sgx_eos *eos, int64_t n, double *rho, double *temp, do
   if (lambda && lambda_stride < 2) return fail(SGX_ERR_INVALID, "sgx_eos_fill: lambda_stride < 2");
   if (precision != SGX_PREC_FP64 && precision != SGX_PREC_MIXED)
     return fail(SGX_ERR_INVALID, "sgx_eos_fill: bad precision");
+  if (eos->type == SGX_HELMHOLTZ) {
+    // Helmholtz::FillEos (eos_helmholtz.hpp:818-865)
+    if (!lambda || lambda_stride < 3)
+      return fail(SGX_ERR_INVALID, "sgx_eos_fill: Helmholtz needs lambda rows [Abar, Zbar, lT]");
+    if (output & SGX_Q_DENSITY)
+      return fail(SGX_ERR_INVALID, "sgx_eos_fill: Density output not supported by this EOS");
+    if ((output & SGX_Q_TEMPERATURE) && (output & SGX_Q_SIE))
+      return fail(SGX_ERR_INVALID, "sgx_eos_fill: Either specific internal energy or "
+                                   "temperature must be provided.");
+    if ((output & SGX_Q_TEMPERATURE) ? !sie : !temp)
+      return fail(SGX_ERR_INVALID, "sgx_eos_fill: the input (sie or temp) array is null");
+    if (precision != SGX_PREC_FP64)
+      return fail(SGX_ERR_UNSUPPORTED, "sgx_eos_fill: Helmholtz runs in FP64 only");
+  }
   sgx::FillArgs a;
   a.eos = *eos;
   a.n = n;
@@ -228,6 +280,8 @@ int sgx_eos_fill_ex(const sgx_eos *eos, int64_t n, double *rho, double *temp, do
                   "sgx_eos_fill: mixed precision needs a tabulated rho-T EOS, (rho, sie) "
                   "inputs and T among the outputs");
     e = sgx::launch_fill_mixed(a, reinterpret_cast<cudaStream_t>(stream));
+  } else if (eos->type == SGX_HELMHOLTZ) {
+    e = sgx::launch_helm_fill(a, reinterpret_cast<cudaStream_t>(stream));
   } else {
     e = sgx::launch_fill_fp64(a, reinterpret_cast<cudaStream_t>(stream));
   }
@@ -261,6 +315,8 @@ int sgx_pte_solve(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list, 
     return fail(SGX_ERR_INVALID, "sgx_pte_solve: null array");
   for (int k = 0; k < neos; ++k)
     if (!valid_type(eos_list[k].type)) return fail(SGX_ERR_INVALID, "sgx_pte_solve: bad eos");
+    else if (!pte_type(eos_list[k].type))
+      return fail(SGX_ERR_UNSUPPORTED, "sgx_pte_solve: Helmholtz is not available in PTE");
   sgx::PteArgs a;
   std::memset(&a, 0, sizeof(a));
   a.solver = solver;
@@ -324,6 +380,8 @@ int sgx_pte_solve_noalloc(int solver, int nmat, int64_t ncell, const sgx_eos *eo
   for (int k = 0; k < neos; ++k)
     if (!valid_type(eos_list[k].type))
       return fail(SGX_ERR_INVALID, std::string(who) + ": bad eos");
+    else if (!pte_type(eos_list[k].type))
+      return fail(SGX_ERR_UNSUPPORTED, std::string(who) + ": Helmholtz is not available in PTE");
   sgx::PteArgs a;
   std::memset(&a, 0, sizeof(a));
   a.solver = solver;

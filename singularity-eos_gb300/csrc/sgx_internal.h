@@ -71,5 +71,8 @@ struct FillArgs {
 cudaError_t launch_fill_fp64(const FillArgs &a, cudaStream_t stream);
 // Tabulated rho-T FillEos from (rho, sie): FP32 bracket search + FP64 solve.
 cudaError_t launch_fill_mixed(const FillArgs &a, cudaStream_t stream);
+// Helmholtz vector lookups and FillEos (lambda rows [Abar, Zbar, lT]).
+cudaError_t launch_helm_eval(const EvalArgs &a, cudaStream_t stream);
+cudaError_t launch_helm_fill(const FillArgs &a, cudaStream_t stream);
 
 } // namespace sgx

@@ -22,14 +22,18 @@
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <map>
+#include <sstream>
 #include <mutex>
 #include <vector>
 
 #include <cuda_runtime.h>
 
 #include "../../include/sgx.h"
+#include "sgx_helm.cuh"
 #include "sgx_spiner.cuh"
 #include "sgx_table.h"
 
@@ -142,6 +146,7 @@ struct Resident {
   size_t bytes = 0;
   int device = 0;
   HostTable host;
+  std::vector<double> dump; // non-empty: the dump of a non-Spiner table
 };
 std::mutex g_mu;
 std::map<uint64_t, Resident> g_tables;
@@ -479,6 +484,125 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
   return SGX_OK;
 }
 
+// HelmElectrons::InitDataFile_ (eos/eos_helmholtz.hpp:962-989): four blocks
+// of whitespace-separated values, each over j (temperature) then i (electron
+// density, fastest); then the node values 10^x of both grids, computed on
+// the host as math_utils::pow10 does (exp(ln10 * x)).
+int table_load_helm(const char *path, uint64_t *handle, std::string &msg) {
+  std::ifstream file(path, std::ios::binary);
+  if (!file.is_open()) {
+    msg = std::string("HelmElectrons file ") + path + " not found!";
+    return SGX_ERR_IO;
+  }
+  std::stringstream ss;
+  ss << file.rdbuf();
+  const std::string text = ss.str();
+  const char *cur = text.c_str();
+  constexpr int NT = HELM_NT, NR = HELM_NRHO;
+  const int nper[4] = {9, 4, 4, 4};
+  // fields[b][k][j * NR + i]
+  std::vector<std::vector<double>> fields[4];
+  for (int b = 0; b < 4; ++b) {
+    fields[b].assign(nper[b], std::vector<double>(static_cast<size_t>(NT) * NR));
+    for (int j = 0; j < NT; ++j)
+      for (int i = 0; i < NR; ++i)
+        for (int k = 0; k < nper[b]; ++k) {
+          char *end = nullptr;
+          const double v = std::strtod(cur, &end);
+          if (end == cur) {
+            msg = "Error reading the Helmholtz free energy table at j = " + std::to_string(j) +
+                  ", i = " + std::to_string(i);
+            return SGX_ERR_IO;
+          }
+          fields[b][k][static_cast<size_t>(j) * NR + i] = v;
+          cur = end;
+        }
+  }
+  HelmTable t{};
+  t.lRhoMin = -12.0;
+  t.lRhoMax = 15.0;
+  t.dlRho = (t.lRhoMax - t.lRhoMin) / static_cast<double>(NR - 1);
+  t.inv_dlRho = 1 / t.dlRho;
+  t.lTMin = 3.0;
+  t.lTMax = 13.0;
+  t.dlT = (t.lTMax - t.lTMin) / static_cast<double>(NT - 1);
+  t.inv_dlT = 1 / t.dlT;
+  t.rhoMin = 1e-12; // ipow10<-12>(): 1 / 10^12, correctly rounded
+  t.rhoMax = 1e15;
+  std::vector<double> rho(NR), T(NT);
+  for (int i = 0; i < NR; ++i)
+    rho[i] = std::exp(helm::LN10 * (t.lRhoMin + i * t.dlRho));
+  for (int j = 0; j < NT; ++j)
+    T[j] = std::exp(helm::LN10 * (t.lTMin + j * t.dlT));
+  // per-cell records in the order the kernels read them
+  const std::vector<double> *f5[9] = {&fields[0][0], &fields[0][2], &fields[0][4],
+                                      &fields[0][1], &fields[0][3], &fields[0][5],
+                                      &fields[0][6], &fields[0][7], &fields[0][8]};
+  // block 1 columns: f fd ft fdd ftt fdt fddt fdtt fddtt -> record order
+  // f, ft, ftt, fd, fdd, fdt, fddt, fdtt, fddtt
+  const int cub[4] = {0, 2, 1, 3}; // dpdf dpdfd dpdft dpdfdt -> val, dT, dD, dDdT
+  const size_t ncell = static_cast<size_t>(NT - 1) * (NR - 1);
+  std::vector<double> cells(ncell * HELM_REC);
+  for (int j = 0; j < NT - 1; ++j)
+    for (int i = 0; i < NR - 1; ++i) {
+      double *r = cells.data() + (static_cast<size_t>(j) * (NR - 1) + i) * HELM_REC;
+      const size_t c[4] = {static_cast<size_t>(j) * NR + i, static_cast<size_t>(j) * NR + i + 1,
+                           static_cast<size_t>(j + 1) * NR + i,
+                           static_cast<size_t>(j + 1) * NR + i + 1};
+      int o = 0;
+      for (int f = 0; f < 9; ++f)
+        for (int q = 0; q < 4; ++q)
+          r[o++] = (*f5[f])[c[q]];
+      for (int b = 1; b < 4; ++b)
+        for (int f = 0; f < 4; ++f)
+          for (int q = 0; q < 4; ++q)
+            r[o++] = fields[b][cub[f]][c[q]];
+    }
+  const size_t off_cells = 256;
+  const size_t off_rho = off_cells + cells.size() * 8;
+  const size_t off_T = off_rho + NR * 8;
+  const size_t bytes = off_T + NT * 8;
+  void *dev = nullptr;
+  cudaError_t e = cudaMalloc(&dev, bytes);
+  if (e != cudaSuccess) {
+    msg = std::string("cudaMalloc of table: ") + cudaGetErrorString(e);
+    return SGX_ERR_CUDA;
+  }
+  unsigned char *d = static_cast<unsigned char *>(dev);
+  t.cells = reinterpret_cast<const double *>(d + off_cells);
+  t.rho = reinterpret_cast<const double *>(d + off_rho);
+  t.T = reinterpret_cast<const double *>(d + off_T);
+  std::vector<unsigned char> img(bytes, 0);
+  std::memcpy(img.data(), &t, sizeof(t));
+  std::memcpy(img.data() + off_cells, cells.data(), cells.size() * 8);
+  std::memcpy(img.data() + off_rho, rho.data(), NR * 8);
+  std::memcpy(img.data() + off_T, T.data(), NT * 8);
+  e = cudaMemcpy(dev, img.data(), bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(dev);
+    msg = std::string("cudaMemcpy of table: ") + cudaGetErrorString(e);
+    return SGX_ERR_CUDA;
+  }
+  Resident r;
+  r.dev = dev;
+  r.bytes = bytes;
+  cudaGetDevice(&r.device);
+  // dump: the node values and the fields in the reference's DBLIST order
+  // (rho_, T_, f_ .. fddtt_, dpdf_ .., ef_ .., xf_ ..; eos_helmholtz.hpp:281-292)
+  r.dump = rho;
+  r.dump.insert(r.dump.end(), T.begin(), T.end());
+  for (int b = 0; b < 4; ++b)
+    for (auto &v : fields[b])
+      r.dump.insert(r.dump.end(), v.begin(), v.end());
+  const uint64_t key = reinterpret_cast<uint64_t>(dev);
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_tables[key] = std::move(r);
+  }
+  *handle = key;
+  return SGX_OK;
+}
+
 int table_free(uint64_t handle, std::string &msg) {
   std::lock_guard<std::mutex> lk(g_mu);
   auto it = g_tables.find(handle);
@@ -501,6 +625,11 @@ long table_dump(uint64_t handle, double *out, long cap) {
   std::lock_guard<std::mutex> lk(g_mu);
   auto it = g_tables.find(handle);
   if (it == g_tables.end()) return -1;
+  if (!it->second.dump.empty()) {
+    const long total = static_cast<long>(it->second.dump.size());
+    if (out && cap >= total) std::memcpy(out, it->second.dump.data(), total * 8);
+    return total;
+  }
   const HostTable &h = it->second.host;
   // DBLIST order (eos_spiner_rho_temp.hpp:253-257); mF_ is empty.
   std::vector<const std::vector<double> *> order;

@@ -12,9 +12,13 @@ namespace sgx {
 // device. *handle receives the device address of the table header.
 int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *handle,
                       std::string &msg);
+// Loads a Helmholtz electron free-energy table (the reference's ASCII
+// helm_table.dat layout) and uploads the per-cell Hermite records.
+int table_load_helm(const char *path, uint64_t *handle, std::string &msg);
 int table_free(uint64_t handle, std::string &msg);
 size_t table_bytes(uint64_t handle);
-// Derived tables in the reference's DBLIST order; returns the count or -1.
+// Spiner: derived tables in the reference's DBLIST order; Helmholtz: node
+// values and fields in its DBLIST order. Returns the count or -1.
 long table_dump(uint64_t handle, double *out, long cap);
 
 // Gruneisen::ComputeRhoMax (eos_gruneisen.hpp:231-329), without the 0.99

@@ -24,8 +24,9 @@ EXPORTED = [
     "sgx_eos_table_bytes", "sgx_eos_spiner_dump", "sgx_eos_eval", "sgx_eos_fill",
     "sgx_eos_fill_ex",
     "sgx_mix_params_default", "sgx_pte_rhot_required_scratch", "sgx_pte_pt_required_scratch",
-    "sgx_pte_solve", "sgx_pte_solve_noalloc",
+    "sgx_pte_solve", "sgx_pte_solve_noalloc", "sgx_eos_helmholtz", "sgx_eos_helmholtz_dump",
 ]
+HELM_DEFAULT, HELM_REGULA_FALSI, HELM_CACHE_READBACK = 31, 32, 64
 PTE_NOALLOC_MAX_CELLS = 1 << 20  # SGX_PTE_NOALLOC_MAX_CELLS
 
 
@@ -94,6 +95,9 @@ def load():
     lib.sgx_mix_params_default.argtypes = [C.POINTER(MixParams)]
     lib.sgx_pte_solve.argtypes = [I, I, C.c_int64, P, I, P, P, P, P, P, P, P, P, P,
                                   C.POINTER(MixParams), P, I, P]
+    lib.sgx_eos_helmholtz.argtypes = [C.POINTER(SgxEos), C.c_char_p, I]
+    lib.sgx_eos_helmholtz_dump.argtypes = [C.POINTER(SgxEos), P, C.c_long]
+    lib.sgx_eos_helmholtz_dump.restype = C.c_long
     lib.sgx_pte_solve_noalloc.argtypes = [I, I, C.c_int64, P, I, P, P, P, P, P, P, P, P, P,
                                           C.POINTER(MixParams), P, P]
     _lib = lib
@@ -139,6 +143,13 @@ def spiner_eos(path, matid, reproducible=False):
     lib = load()
     e = SgxEos()
     check(lib.sgx_eos_spiner_rhot(C.byref(e), path.encode(), int(matid), int(reproducible)))
+    return e
+
+
+def helmholtz_eos(path, options=HELM_DEFAULT):
+    lib = load()
+    e = SgxEos()
+    check(lib.sgx_eos_helmholtz(C.byref(e), path.encode(), int(options)))
     return e
 
 

@@ -6,7 +6,7 @@ sources with the shims in oracle/shims) on small seeded inputs and stores
 inputs and outputs as .npz. The GPU parity tests compare the CUDA library
 against these files on machines where the reference sources are absent.
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [name ...]   (default: all)
 """
 import hashlib
 import os
@@ -97,6 +97,50 @@ def spiner_fixture(ref, path, nq=4096, seed=5):
     return out
 
 
+def helm_fixture(ref, path, n=2048, seed=31):
+    """Helmholtz EOS on the synthetic table, default options (all on): the
+    forward FillEos, the vector member functions, the inversion as the
+    reference performs it (reading the lT cache back over the root) and as
+    it is meant (sgref_helm_T_from_rho_sie), and the loaded table."""
+    from sgx import helmtable
+    rho, T, abar, zbar = helmtable.helm_queries(n, seed=seed)
+    out = dict(rho=rho, T=T, abar=abar, zbar=zbar)
+    d = rb.eos_desc(rb.HELMHOLTZ, [], path=path, flags=31)
+
+    def lam_fresh(lT=np.nan):
+        lam = np.zeros(3 * n)
+        lam[0::3], lam[1::3], lam[2::3] = abar, zbar, lT
+        return lam
+
+    sie, P, cv, bm = (np.zeros(n) for _ in range(4))
+    lam = lam_fresh()
+    ref.fill_eos(d, rho.copy(), T.copy(), sie, P, cv, bm,
+                 rb.Q_SIE | rb.Q_PRESSURE | rb.Q_SPECIFIC_HEAT | rb.Q_BULK_MODULUS,
+                 lam=lam, lam_stride=3)
+    out.update(fwd_sie=sie, fwd_P=P, fwd_cv=cv, fwd_bmod=bm, fwd_lam=lam.copy())
+    for fn in (1, 2, 4, 6, 8):
+        out[f"fn{fn}"] = ref.eos_vec(d, fn, rho, T, lam=lam_fresh(), lam_stride=3)
+    # the reference's inversion: with the cache from the forward call the
+    # root is replaced by the cached log10 T
+    Tr, Pr, cvr, bmr = (np.zeros(n) for _ in range(4))
+    lam_rb = lam.copy()
+    ref.fill_eos(d, rho.copy(), Tr, sie.copy(), Pr, cvr, bmr,
+                 rb.Q_TEMPERATURE | rb.Q_PRESSURE | rb.Q_SPECIFIC_HEAT | rb.Q_BULK_MODULUS,
+                 lam=lam_rb, lam_stride=3)
+    out.update(rb_T=Tr, rb_P=Pr, rb_cv=cvr, rb_bmod=bmr)
+    for fn in (3, 5, 7, 9):
+        out[f"rb_fn{fn}"] = ref.eos_vec(d, fn, rho, sie, lam=lam.copy(), lam_stride=3)
+    # ... and with an out-of-table cache value
+    out["rb_invalid_T"] = ref.eos_vec(d, 0, rho, sie, lam=lam_fresh(-1.0), lam_stride=3)
+    out["fix_T"] = ref.helm_T_from_rho_sie(path, rho, sie, abar, zbar)
+    dump = ref.helm_dump(path)
+    nodes = helmtable.NRHO + helmtable.NTEMP
+    out["dump_nodes"] = dump[:nodes].copy()
+    out["dump_fields_sha256"] = np.array(hashlib.sha256(dump[nodes:].tobytes()).hexdigest())
+    out["dump_len"] = np.int64(dump.size)
+    return out
+
+
 def main():
     if not rb.have_reference():
         sys.exit("oracle/_ref/libsgref.so not built; run oracle/build_ref.sh")
@@ -136,7 +180,16 @@ def main():
             o["in_" + k] = wl[k]
             o["out_" + k] = r[k]
         fx["pte_rhot_spiner"] = o
+    with tempfile.TemporaryDirectory() as td:
+        from sgx import helmtable
+        path = os.path.join(td, "helm_table.dat")
+        sha = helmtable.helm_table(path)
+        fx["helmholtz"] = helm_fixture(ref, path)
+        fx["helmholtz"]["table_sha256"] = np.array(sha)
+    only = set(sys.argv[1:])
     for name, d in fx.items():
+        if only and name not in only:
+            continue
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
         print(name, {k: getattr(v, "shape", None) for k, v in list(d.items())[:4]})
 

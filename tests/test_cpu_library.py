@@ -84,3 +84,42 @@ def test_table_image_is_deterministic(tmp_path):
     sp5lite.stiffgas_table(str(a))
     sp5lite.stiffgas_table(str(b))
     assert a.read_bytes() == b.read_bytes()
+
+
+def test_helm_table_is_reproducible(tmp_path):
+    """The synthetic Helmholtz table is bit-identical to the one the golden
+    fixture was made with (decimal arithmetic for the node transcendentals,
+    only + - * / on arrays)."""
+    from common import golden
+    from sgx import helmtable
+    sha = helmtable.helm_table(str(tmp_path / "helm_table.dat"))
+    assert sha == str(golden("helmholtz")["table_sha256"])
+
+
+def test_helm_table_derivatives_are_exact():
+    """Every tabulated derivative is the derivative of the free energy (the
+    Hermite interpolation relies on it), checked symbolically."""
+    sp = pytest.importorskip("sympy")
+    import mpmath
+    from sgx import helmtable as H
+    d, T = sp.symbols("d T", positive=True)
+    a23 = sp.Rational(2, 3)
+    F = (-H.A_GAS * T * (sp.Rational(3, 2) * sp.log(T) - sp.log(d) + H.C0)
+         + H.K_DEG * d**a23 - H.B_TH * T**2 / (d**a23 + H.D0))
+    P = d**2 * sp.diff(F, d)
+    eta = sp.log(d) - sp.Rational(3, 2) * sp.log(T) + H.C1 + H.K2 * d**a23 / T
+    X = H.NA * d + H.X0 * T**3
+    want = [[F, sp.diff(F, d), sp.diff(F, T), sp.diff(F, d, 2), sp.diff(F, T, 2),
+             sp.diff(F, d, T), sp.diff(F, d, 2, T), sp.diff(F, d, T, 2), sp.diff(F, d, 2, T, 2)],
+            [sp.diff(P, d), sp.diff(P, d, 2), sp.diff(P, d, T), sp.diff(P, d, 2, T)],
+            [eta, sp.diff(eta, d), sp.diff(eta, T), sp.diff(eta, d, T)],
+            [X, sp.diff(X, d), sp.diff(X, T), sp.diff(X, d, T)]]
+    blocks = H._fields()
+    mpmath.mp.dps = 40
+    for j, i in ((0, 0), (40, 100), (70, 200), (100, 270), (13, 137)):
+        (dv, _, _, _, _, _), (tv, _) = H._node_values()
+        dd, tt = float(dv.ravel()[i]), float(tv.ravel()[j])
+        for exprs, blk in zip(want, blocks):
+            for e, v in zip(exprs, blk):
+                ref = float(sp.lambdify((d, T), e, "mpmath")(mpmath.mpf(dd), mpmath.mpf(tt)))
+                assert abs(v[j, i] - ref) <= 1e-11 * max(abs(ref), 1e-300) + 1e-300, (j, i)
