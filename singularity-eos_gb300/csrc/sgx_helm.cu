@@ -110,6 +110,125 @@ __global__ void __launch_bounds__(HELM_BLOCK) helm_fill_kernel(const FillArgs a)
   if (bad && a.err) atomicOr(a.err, 1);
 }
 
+// Two-pass inversion FillEos (outputs include T, inputs rho and sie): pass 1
+// runs every element's Newton iteration for at most HELM_PASS1_ITERS steps
+// and finishes the ones that stop; the others are queued with their exact
+// iteration state (x, iteration count) and pass 2 resumes them over the
+// compacted queue, up to the reference's 100 iterations and its fallbacks.
+// Each element's result is the one a single pass gives; the hard elements
+// (hundreds of evaluations where e(T) is not monotone) no longer hold up
+// the warps of the easy ones.
+constexpr int HELM_PASS1_ITERS = 12;
+
+struct HelmQueue {
+  int *id;
+  double *x;
+  int *iter;
+  unsigned *count;
+  int *id_rf;         // pass 2 -> 3: Newton ran out of iterations
+  unsigned *count_rf;
+};
+
+__device__ __forceinline__ void store_fill(const FillArgs &a, const long long i, const double rho,
+                                           const double temp, const double sie,
+                                           const double press, const double cv,
+                                           const double bmod) {
+  if (a.cs) a.cs[i] = sqrt(bmod / rho);
+  if ((a.output & Q_TEMPERATURE) && a.temp) a.temp[i] = temp;
+  if ((a.output & Q_SIE) && a.sie) a.sie[i] = sie;
+  if ((a.output & Q_PRESSURE) && a.press) a.press[i] = press;
+  if ((a.output & Q_CV) && a.cv) a.cv[i] = cv;
+  if ((a.output & Q_BMOD) && a.bmod) a.bmod[i] = bmod;
+}
+
+__global__ void __launch_bounds__(HELM_BLOCK) helm_invert_pass1(const FillArgs a, HelmQueue q) {
+  using namespace helm;
+  __shared__ HelmTable st;
+  if (threadIdx.x == 0) st = *reinterpret_cast<const HelmTable *>(a.eos.table);
+  __syncthreads();
+  const int opt = a.eos.flags;
+  const unsigned output = a.output | (a.cs ? Q_BMOD : 0u);
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < a.n;
+       i += stride) {
+    const double rho = a.rho[i];
+    const double sie = a.sie[i];
+    double *lam = a.lambda + i * a.lambda_stride;
+    const Cell c = cell(rho, lam[0], lam[1]);
+    Inversion v = inversion_begin(st, opt, c, sie, lam);
+    const bool done =
+        newton_e_steps(st, opt, c, sie, v.Ta, v.Tb, HELM_EOS_EPS, v.x, v.iter, HELM_PASS1_ITERS);
+    if (!done) {
+      const unsigned pos = atomicAdd(q.count, 1u);
+      q.id[pos] = static_cast<int>(i);
+      q.x[pos] = v.x;
+      q.iter[pos] = v.iter;
+      continue;
+    }
+    const double temp = pow10e(inversion_end(st, opt, c, v, true, lam));
+    double e_out = sie, press = 0.0, cv = 0.0, bmod = 0.0;
+    helm_fill_tail(st, opt, c, temp, e_out, press, cv, bmod, output);
+    store_fill(a, i, rho, temp, e_out, press, cv, bmod);
+  }
+}
+
+__global__ void __launch_bounds__(HELM_BLOCK) helm_invert_pass2(const FillArgs a, HelmQueue q) {
+  using namespace helm;
+  __shared__ HelmTable st;
+  if (threadIdx.x == 0) st = *reinterpret_cast<const HelmTable *>(a.eos.table);
+  __syncthreads();
+  const int opt = a.eos.flags;
+  const unsigned output = a.output | (a.cs ? Q_BMOD : 0u);
+  const unsigned count = *q.count;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < count;
+       k += gridDim.x * blockDim.x) {
+    const long long i = q.id[k];
+    const double rho = a.rho[i];
+    const double sie = a.sie[i];
+    double *lam = a.lambda + i * a.lambda_stride;
+    const Cell c = cell(rho, lam[0], lam[1]);
+    Inversion v = inversion_begin(st, opt, c, sie, lam);
+    v.x = q.x[k];
+    v.iter = q.iter[k];
+    const bool done =
+        newton_e_steps(st, opt, c, sie, v.Ta, v.Tb, HELM_EOS_EPS, v.x, v.iter, NEWTON_MAX_ITER);
+    if (!done) {
+      q.id_rf[atomicAdd(q.count_rf, 1u)] = static_cast<int>(i);
+      continue;
+    }
+    const double temp = pow10e(inversion_end(st, opt, c, v, true, lam));
+    double e_out = sie, press = 0.0, cv = 0.0, bmod = 0.0;
+    helm_fill_tail(st, opt, c, temp, e_out, press, cv, bmod, output);
+    store_fill(a, i, rho, temp, e_out, press, cv, bmod);
+  }
+}
+
+// Pass 3: the elements whose Newton iteration used all 100 steps go on to
+// the reference's regula falsi (up to 1000 more evaluations) and, failing
+// that, the analytic estimate.
+__global__ void __launch_bounds__(HELM_BLOCK) helm_invert_pass3(const FillArgs a, HelmQueue q) {
+  using namespace helm;
+  __shared__ HelmTable st;
+  if (threadIdx.x == 0) st = *reinterpret_cast<const HelmTable *>(a.eos.table);
+  __syncthreads();
+  const int opt = a.eos.flags;
+  const unsigned output = a.output | (a.cs ? Q_BMOD : 0u);
+  const unsigned count = *q.count_rf;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < count;
+       k += gridDim.x * blockDim.x) {
+    const long long i = q.id_rf[k];
+    const double rho = a.rho[i];
+    const double sie = a.sie[i];
+    double *lam = a.lambda + i * a.lambda_stride;
+    const Cell c = cell(rho, lam[0], lam[1]);
+    const Inversion v = inversion_begin(st, opt, c, sie, lam);
+    const double temp = pow10e(inversion_end(st, opt, c, v, false, lam));
+    double e_out = sie, press = 0.0, cv = 0.0, bmod = 0.0;
+    helm_fill_tail(st, opt, c, temp, e_out, press, cv, bmod, output);
+    store_fill(a, i, rho, temp, e_out, press, cv, bmod);
+  }
+}
+
 int helm_grid(const long long n) {
   int dev = 0, sms = 152;
   if (cudaGetDevice(&dev) == cudaSuccess)
@@ -129,8 +248,43 @@ cudaError_t launch_helm_eval(const EvalArgs &a, cudaStream_t stream) {
 
 cudaError_t launch_helm_fill(const FillArgs &a, cudaStream_t stream) {
   if (a.n <= 0) return cudaSuccess;
-  helm_fill_kernel<<<helm_grid(a.n), HELM_BLOCK, 0, stream>>>(a);
-  return cudaGetLastError();
+  const int opt = a.eos.flags;
+  const bool iterate = (opt & HELM_RAD) || (opt & HELM_ELE) || (opt & HELM_COUL);
+  const bool two_pass = (a.output & Q_TEMPERATURE) && iterate && !(opt & HELM_REGULA_FALSI) &&
+                        a.n <= 0x7fffffffLL;
+  if (!two_pass) {
+    helm_fill_kernel<<<helm_grid(a.n), HELM_BLOCK, 0, stream>>>(a);
+    return cudaGetLastError();
+  }
+  // queues: 256 B counter block, then x[n], id[n], iter[n], id_rf[n]
+  const size_t n = static_cast<size_t>(a.n);
+  const size_t ids = (n * sizeof(int) + 255) / 256 * 256;
+  const size_t xs = (n * sizeof(double) + 255) / 256 * 256;
+  void *scratch = nullptr;
+  cudaError_t e = cudaMallocAsync(&scratch, 256 + 3 * ids + xs, stream);
+  if (e != cudaSuccess) return e;
+  char *p = static_cast<char *>(scratch);
+  HelmQueue q;
+  q.count = reinterpret_cast<unsigned *>(p);
+  q.count_rf = reinterpret_cast<unsigned *>(p + 64);
+  q.x = reinterpret_cast<double *>(p + 256);
+  q.id = reinterpret_cast<int *>(p + 256 + xs);
+  q.iter = reinterpret_cast<int *>(p + 256 + xs + ids);
+  q.id_rf = reinterpret_cast<int *>(p + 256 + xs + 2 * ids);
+  e = cudaMemsetAsync(p, 0, 256, stream);
+  if (e == cudaSuccess) {
+    helm_invert_pass1<<<helm_grid(a.n), HELM_BLOCK, 0, stream>>>(a, q);
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess)
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long want = (a.n + HELM_BLOCK - 1) / HELM_BLOCK;
+    const int grid2 = static_cast<int>(want < 4LL * sms ? want : 4LL * sms);
+    helm_invert_pass2<<<grid2, HELM_BLOCK, 0, stream>>>(a, q);
+    helm_invert_pass3<<<grid2, HELM_BLOCK, 0, stream>>>(a, q);
+    e = cudaGetLastError();
+  }
+  const cudaError_t f = cudaFreeAsync(scratch, stream);
+  return e != cudaSuccess ? e : f;
 }
 
 } // namespace sgx

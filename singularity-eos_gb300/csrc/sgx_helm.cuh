@@ -555,67 +555,96 @@ SGX_HDI double gamma3(const double rho, const double T, const double p[5], const
   return x + 1.0;
 }
 
-// RootFinding1D::newton_raphson (root_finding.hpp:246-310) on e(T) with
-// fail_on_bound_root = false.
-SGX_HDN RootStatus newton_e(const HelmTable &t, const int opt, const Cell &c,
-                            const double ytarget, const double guess, const double a,
-                            const double b, const double ytol, double &xroot) {
-  double x = guess, xold = 0.0;
-  int iter;
-  for (iter = 0; iter < NEWTON_MAX_ITER; iter++) {
+// Iterations iter .. iter_end - 1 of RootFinding1D::newton_raphson
+// (root_finding.hpp:246-310) on e(T), from x, with fail_on_bound_root =
+// false. Resumable: returns true when the iteration stopped (converged, or
+// stepped out of [a, b], which the reference then accepts), false when
+// iter_end was reached first; x and iter carry the state across calls, so
+// running 0..k and then k..100 gives the same result as 0..100.
+SGX_HDN bool newton_e_steps(const HelmTable &t, const int opt, const Cell &c,
+                            const double ytarget, const double a, const double b,
+                            const double ytol, double &x, int &iter, const int iter_end) {
+  for (; iter < iter_end; iter++) {
     double p[5], e[5], s[5], eta[5], nep[5];
     evaluate(t, opt, c, x, p, e, s, eta, nep, true);
     const double yg = e[VAL], dfunc = e[DDT];
-    if (sabs(yg - ytarget) < sabs(ytol * ytarget)) break;
-    xold = x;
+    if (sabs(yg - ytarget) < sabs(ytol * ytarget)) return true;
+    const double xold = x;
     x = x - (yg - ytarget) / dfunc;
-    if ((x <= a && xold <= a) || (x >= b && xold >= b)) break;
+    if ((x <= a && xold <= a) || (x >= b && xold >= b)) return true;
     x = smax(smin(x, b), a);
   }
-  xroot = x;
-  return iter >= NEWTON_MAX_ITER ? RootStatus::FAIL : RootStatus::SUCCESS;
+  return false;
 }
 
-// lTFromRhoSie_ (:867-960). lam: [Abar, Zbar, lT] or null. The reference
-// ends with a SafeGet of the lT cache, which with a numerically indexed
-// lambda replaces the root by the cached guess; HELM_CACHE_READBACK keeps
-// that behaviour, otherwise the root is stored into the cache.
-SGX_HDN double lT_from_rho_sie(const HelmTable &t, const int opt, const Cell &c, const double e,
-                               double *lam) {
+// One inversion T(rho, e) (lTFromRhoSie_, :867-960) between its phases.
+struct Inversion {
+  double e, Tguess, Ta, Tb, ni, ne, x;
+  int iter;
+  bool iterate; // a root find is needed (radiation, electrons or Coulomb on)
+  bool newton;  // Newton-Raphson first (Options::USE_NEWTON_RAPHSON)
+};
+
+// Initial guess: the lT cache when it lies in the table, else the ideal-gas
+// estimate, else 10^8 K.
+SGX_HDI Inversion inversion_begin(const HelmTable &t, const int opt, const Cell &c,
+                                  const double e, const double *lam) {
+  Inversion v;
+  v.e = e;
   const double abari = ratio(1.0, c.abar);
-  const double ni = abari * c.rho * NA;
-  const double ne = c.zbar * ni;
-  const double ionized = (opt & HELM_ION) ? 1.0 : 0.0;
-  double lT, T = 0.0;
-  if ((opt & HELM_RAD) || (opt & HELM_ELE) || (opt & HELM_COUL)) {
+  v.ni = abari * c.rho * NA;
+  v.ne = c.zbar * v.ni;
+  v.iterate = (opt & HELM_RAD) || (opt & HELM_ELE) || (opt & HELM_COUL);
+  v.newton = !(opt & HELM_REGULA_FALSI);
+  v.iter = 0;
+  v.Tguess = v.Ta = v.Tb = v.x = 0.0;
+  if (v.iterate) {
     double lTguess = lam ? lam[2] : NAN;
     if (!((t.lTMin <= lTguess) && (lTguess <= t.lTMax))) {
-      lTguess = lT_analytic(c.rho, e, ni, ne);
+      lTguess = lT_analytic(c.rho, e, v.ni, v.ne);
       if (!((t.lTMin <= lTguess) && (lTguess <= t.lTMax))) lTguess = 8;
     }
-    const double Tguess = pow10e(lTguess);
-    const double Ta = pow10e(t.lTMin), Tb = pow10e(t.lTMax);
+    v.Tguess = pow10e(lTguess);
+    v.Ta = pow10e(t.lTMin);
+    v.Tb = pow10e(t.lTMax);
+    v.x = v.Tguess;
+  }
+  return v;
+}
+
+// After the Newton phase (newton_done: it stopped before its iteration
+// limit): the regula-falsi and analytic fallbacks, the clamp to the table
+// and the lT cache. The reference ends with a SafeGet of the cache, which
+// with a numerically indexed lambda replaces the root by the cached guess;
+// HELM_CACHE_READBACK keeps that behaviour, otherwise the root is stored
+// into the cache. Returns log10 T.
+SGX_HDN double inversion_end(const HelmTable &t, const int opt, const Cell &c,
+                             const Inversion &v, const bool newton_done, double *lam) {
+  const double ionized = (opt & HELM_ION) ? 1.0 : 0.0;
+  double lT, T = 0.0;
+  if (v.iterate) {
     auto e_of_T = [&](const double x) {
       double p[5], ee[5], s[5], eta[5], nep[5];
       evaluate(t, opt, c, x, p, ee, s, eta, nep, true);
       return ee[VAL];
     };
     bool ok;
-    if (!(opt & HELM_REGULA_FALSI)) {
-      ok = newton_e(t, opt, c, e, Tguess, Ta, Tb, HELM_EOS_EPS, T) == RootStatus::SUCCESS;
+    if (v.newton) {
+      ok = newton_done;
+      T = v.x;
       if (!ok)
-        ok = regula_falsi(e_of_T, e, Tguess, Ta, Tb, ROOT_THRESH, ROOT_THRESH, T) ==
+        ok = regula_falsi(e_of_T, v.e, v.Tguess, v.Ta, v.Tb, ROOT_THRESH, ROOT_THRESH, T) ==
              RootStatus::SUCCESS;
     } else {
-      ok = regula_falsi(e_of_T, e, Tguess, Ta, Tb, ROOT_THRESH, ROOT_THRESH, T) ==
+      ok = regula_falsi(e_of_T, v.e, v.Tguess, v.Ta, v.Tb, ROOT_THRESH, ROOT_THRESH, T) ==
            RootStatus::SUCCESS;
     }
     if (!ok) {
-      lT = lT_analytic(c.rho, e, ni, ionized * ne);
+      lT = lT_analytic(c.rho, v.e, v.ni, ionized * v.ne);
       T = pow10e(lT);
     }
   } else {
-    lT = lT_analytic(c.rho, e, ni, ionized * ne);
+    lT = lT_analytic(c.rho, v.e, v.ni, ionized * v.ne);
     T = pow10e(lT);
   }
   lT = log10(T);
@@ -630,7 +659,31 @@ SGX_HDN double lT_from_rho_sie(const HelmTable &t, const int opt, const Cell &c,
   return lT;
 }
 
+// lTFromRhoSie_ in one pass. lam: [Abar, Zbar, lT] or null.
+SGX_HDN double lT_from_rho_sie(const HelmTable &t, const int opt, const Cell &c, const double e,
+                               double *lam) {
+  Inversion v = inversion_begin(t, opt, c, e, lam);
+  bool done = false;
+  if (v.iterate && v.newton)
+    done = newton_e_steps(t, opt, c, e, v.Ta, v.Tb, HELM_EOS_EPS, v.x, v.iter, NEWTON_MAX_ITER);
+  return inversion_end(t, opt, c, v, done, lam);
+}
+
 } // namespace helm
+
+// The end of Helmholtz::FillEos (:847-864): the full evaluation at temp and
+// the requested outputs.
+SGX_HDN void helm_fill_tail(const HelmTable &t, const int opt, const helm::Cell &c,
+                            const double temp, double &energy, double &press, double &cv,
+                            double &bmod, const unsigned output) {
+  using namespace helm;
+  double p[5], e[5], s[5], eta[5], nep[5];
+  evaluate(t, opt, c, temp, p, e, s, eta, nep, false);
+  if (output & Q_SIE) energy = e[0];
+  if (output & Q_PRESSURE) press = p[0];
+  if (output & Q_CV) cv = e[DDT];
+  if (output & Q_BMOD) bmod = smax(lim<double>::eps, p[0] * gamma1(c.rho, temp, p, e));
+}
 
 // Helmholtz::FillEos (:818-865) for one element; lam = [Abar, Zbar, lT].
 // err: 1 = an output combination the reference rejects, 2 = no lambda.
@@ -649,20 +702,12 @@ SGX_HDN void helm_fill(const HelmTable &t, const int opt, double rho, double &te
     return;
   }
   const Cell c = cell(rho, lam[0], lam[1]);
-  double lT;
   if (need_temp) {
-    lT = lT_from_rho_sie(t, opt, c, energy, lam);
-    temp = pow10e(lT);
+    temp = pow10e(lT_from_rho_sie(t, opt, c, energy, lam));
   } else {
-    lT = log10(temp);
-    lam[2] = lT;
+    lam[2] = log10(temp);
   }
-  double p[5], e[5], s[5], eta[5], nep[5];
-  evaluate(t, opt, c, temp, p, e, s, eta, nep, false);
-  if (output & Q_SIE) energy = e[0];
-  if (output & Q_PRESSURE) press = p[0];
-  if (output & Q_CV) cv = e[DDT];
-  if (output & Q_BMOD) bmod = smax(lim<double>::eps, p[0] * gamma1(rho, temp, p, e));
+  helm_fill_tail(t, opt, c, temp, energy, press, cv, bmod, output);
 }
 
 } // namespace sgx

@@ -221,3 +221,36 @@ def test_helmholtz_argument_checks(sgx, table):
             sgx.helmholtz_eos("/nonexistent/helm_table.dat")
     finally:
         lib.sgx_eos_finalize(C.byref(eos))
+
+
+@pytest.mark.parametrize("options", [31, 31 | 64])
+def test_two_pass_inversion_is_bitwise_single_pass(sgx, table, options):
+    """FillEos with T among the outputs runs the inversion in two passes
+    (bounded Newton steps, then the queued cells resumed); each element must
+    come out exactly as the one-pass member functions give it."""
+    from sgx import helmtable
+    n = 1 << 16
+    rho_h, T_h, abar, zbar = helmtable.helm_queries(n, seed=99)
+    eos = sgx.helmholtz_eos(table[0], options)
+    try:
+        lam_h = np.zeros(3 * n)
+        lam_h[0::3], lam_h[1::3], lam_h[2::3] = abar, zbar, np.nan
+        rho, Tin = dev(rho_h), dev(T_h)
+        sie = torch.empty_like(rho)
+        sgx.fill_eos(eos, rho, Tin, sie, None, None, None, sgx.Q_SIE, lam=dev(lam_h),
+                     lam_stride=3)
+        lam2 = dev(lam_h)
+        T, P, cv, bm = (torch.empty_like(rho) for _ in range(4))
+        q = sgx.Q_TEMPERATURE | sgx.Q_PRESSURE | sgx.Q_SPECIFIC_HEAT | sgx.Q_BULK_MODULUS
+        sgx.fill_eos(eos, rho, T, sie, P, cv, bm, q, lam=lam2, lam_stride=3)
+        for fn, got in ((0, T), (3, P), (5, cv), (7, bm)):
+            lam1 = dev(lam_h)
+            out = torch.empty_like(rho)
+            sgx.eval_eos(eos, fn, rho, sie, out, lam=lam1, lam_stride=3)
+            a, b = got.cpu().numpy(), out.cpu().numpy()
+            assert np.array_equal(a.view(np.uint64), b.view(np.uint64)), fn
+            if fn == 0:
+                assert np.array_equal(lam2.cpu().numpy().view(np.uint64),
+                                      lam1.cpu().numpy().view(np.uint64))
+    finally:
+        sgx.load().sgx_eos_finalize(C.byref(eos))
