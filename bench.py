@@ -323,6 +323,118 @@ def bench_helm(args, world, stream, out):
         lib.load().sgx_eos_finalize(__import__("ctypes").byref(eos))
 
 
+def bench_serve(args, stream, out):
+    """Serving loop on a seeded Poisson stream of closure requests, each of
+    log-uniform size in [1e3, 1e6] cells with 2-4 materials drawn from the
+    batched workload's 8 EOS plus the tabulated StiffGas, under a 64 GB
+    device budget. Saturation throughput: all requests submitted at once.
+    Latency: p50/p99 of submit-to-completion at fractions of saturation.
+    Baseline: the plain per-call FP64 path (one sgx_pte_solve per request in
+    arrival order, with its host copies, serial). Request outputs are not
+    kept (requests that share a payload write the same output arrays)."""
+    import ctypes
+    import torch
+    from sgx import lib, sp5lite, workloads as W
+    rng = np.random.default_rng(2025)
+    npay = args.serve_payloads
+    sizes = np.exp(rng.uniform(np.log(1e3), np.log(1e6), npay)).astype(int)
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "stiffgas.sp5")
+        sp5lite.stiffgas_table(path)
+        tab = lib.spiner_eos(path, 1)
+        eos = [lib.make_eos(k, p) for k, p in W.material_pool(0)] + [tab]
+        keep = []
+
+        def pin(a):
+            t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+            keep.append(t)
+            return t.numpy()
+
+        pays = []
+        for i, n in enumerate(sizes):
+            r = W.serve_request(int(n), seed=500 + i, pool=list(range(9)))
+            r = {k: (pin(v) if isinstance(v, np.ndarray) else v) for k, v in r.items()}
+            for k in ("rho", "vfrac", "sie", "temp", "press"):
+                r[k + "_out"] = pin(np.zeros_like(r[k + "_in"]))
+            pays.append(r)
+
+        def schedule(rate, nreq, seed):
+            g = np.random.default_rng(seed)
+            t = np.cumsum(g.exponential(1.0 / rate, nreq)) if rate else np.zeros(nreq)
+            return t, g.integers(0, npay, nreq)
+
+        def run_server(rate, nreq, seed):
+            srv = lib.Server(eos, hbm_budget_bytes=64 << 30, max_inflight=args.serve_slots,
+                             precision=lib.PREC_MIXED)
+            try:
+                arr, which = schedule(rate, nreq, seed)
+                tickets, t0 = [], time.perf_counter()
+                for a, w in zip(arr, which):
+                    while time.perf_counter() - t0 < a:
+                        time.sleep(min(1e-4, max(0.0, a - (time.perf_counter() - t0))))
+                    tickets.append(srv.submit(pays[w]))
+                lat = np.array([srv.wait(t) for t in tickets])
+                wall = time.perf_counter() - t0
+                cells = int(sum(sizes[w] for w in which))
+            finally:
+                srv.close()
+            return lat, wall, cells
+
+        def run_percall(rate, nreq, seed):
+            arr, which = schedule(rate, nreq, seed)
+            dev = {}
+            lat, t0 = [], time.perf_counter()
+            for a, w in zip(arr, which):
+                now = time.perf_counter() - t0
+                if now < a:
+                    time.sleep(a - now)
+                r = pays[w]
+                d = {k: torch.as_tensor(r[k + "_in"]).to("cuda", non_blocking=True)
+                     for k in ("rho", "vfrac", "sie", "temp", "press")}
+                idx = torch.as_tensor(r["eos_idx"]).to("cuda", non_blocking=True)
+                vt = torch.as_tensor(r["vfrac_tot"]).to("cuda", non_blocking=True)
+                st = torch.as_tensor(r["sie_tot"]).to("cuda", non_blocking=True)
+                lib.pte_solve(lib.PTE_RHOT, eos, idx, vt, st, d["rho"], d["vfrac"], d["sie"],
+                              d["temp"], d["press"], precision=lib.PREC_FP64, stream=stream)
+                for k in ("rho", "vfrac", "sie", "temp", "press"):
+                    torch.from_numpy(r[k + "_out"]).copy_(d[k], non_blocking=True)
+                torch.cuda.synchronize()
+                lat.append(time.perf_counter() - t0 - a)
+            wall = time.perf_counter() - t0
+            return np.array(lat), wall, int(sum(sizes[w] for w in which))
+
+        def summary(lat, wall, cells, rate):
+            return {"rate_req_per_s": rate, "requests": int(lat.size),
+                    "p50_ms": float(np.median(lat) * 1e3),
+                    "p99_ms": float(np.quantile(lat, 0.99) * 1e3),
+                    "cells_per_s": cells / wall}
+
+        nreq = args.serve_requests
+        run_server(0, 4, 1)  # warm-up: module loads, pool growth
+        lat, wall, cells = run_server(0, nreq, 11)
+        sat = cells / wall
+        sat_rate = nreq / wall
+        points = []
+        for frac in (0.25, 0.5, 0.75, 0.9):
+            rate = frac * sat_rate
+            points.append(dict(summary(*run_server(rate, nreq, 12), rate), load=frac))
+        base_lat, base_wall, base_cells = run_percall(0, max(8, nreq // 4), 11)
+        base_sat = base_cells / base_wall
+        base_pts = []
+        for frac in (0.25, 0.5):
+            rate = frac * base_sat / (cells / nreq)
+            base_pts.append(dict(summary(*run_percall(rate, max(8, nreq // 4), 12), rate),
+                                 load=frac))
+        out["serve"] = {
+            "workload": f"Poisson closure requests, {npay} payloads of log-uniform 1e3-1e6 cells, "
+                        "2-4 of 9 EOS (8 analytic + tabulated), 64 GB budget",
+            "slots": args.serve_slots, "precision": "mixed (FP32 + FP64 refinement)",
+            "saturation_cells_per_s": sat, "saturation_req_per_s": sat_rate,
+            "points": points,
+            "baseline_percall_fp64": {"saturation_cells_per_s": base_sat, "points": base_pts}}
+        lib.load().sgx_eos_finalize(ctypes.byref(tab))
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_setup()
@@ -335,6 +447,8 @@ def run_ours(args):
         bench_pte(args, world, stream, out)
     if args.only in ("all", "helm"):
         bench_helm(args, world, stream, out)
+    if args.only in ("all", "serve") and world == 1:
+        bench_serve(args, stream, out)
     fp = fp_peaks()
     if fp:
         out["fp_peaks"] = fp
@@ -381,8 +495,11 @@ def main():
     ap.add_argument("--pte-cells", type=int, default=N_PTE_BATCH)
     ap.add_argument("--pte2-cells", type=int, default=N_PTE2)
     ap.add_argument("--helm-cells", type=int, default=N_HELM)
+    ap.add_argument("--serve-requests", type=int, default=32)
+    ap.add_argument("--serve-payloads", type=int, default=16)
+    ap.add_argument("--serve-slots", type=int, default=8)
     ap.add_argument("--only", default="all",
-                    choices=["all", "lookup", "pte", "pte2", "ptebatch", "helm"])
+                    choices=["all", "lookup", "pte", "pte2", "ptebatch", "helm", "serve"])
     ap.add_argument("--pte-prec", default="both", choices=["both", "fp64", "mixed"])
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
@@ -410,7 +527,7 @@ def main():
     if rank != 0:
         return
     if "value" not in out:  # a profiling run of one leg: no headline line
-        print(json.dumps({k: out.get(k) for k in ("pte", "helmholtz", "fp_peaks")}))
+        print(json.dumps({k: out.get(k) for k in ("pte", "helmholtz", "serve", "fp_peaks")}))
         return
     line = {"metric": METRIC, "value": out["value"], "unit": "lookups/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["ms_per_step"],
@@ -419,7 +536,8 @@ def main():
             "data": "synthetic (seeded; StiffGas-sampled table)", "config": config,
             "e2e": out.get("e2e"), "roofline": out["roofline"], "clocks": out["clocks"],
             "gpu_launches": out["gpu_launches"], "plain_fp64": out["plain_fp64"],
-            "pte": out.get("pte"), "helmholtz": out.get("helmholtz"), "fp_peaks": out.get("fp_peaks")}
+            "pte": out.get("pte"), "helmholtz": out.get("helmholtz"),
+            "serve": out.get("serve"), "fp_peaks": out.get("fp_peaks")}
     if "e2e" not in out:
         line["e2e"] = None
     if not args.no_cpu_baseline and world == 1:

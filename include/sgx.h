@@ -272,6 +272,68 @@ int sgx_pte_solve_noalloc(int solver, int nmat, int64_t ncell, const sgx_eos *eo
                           const sgx_mix_params *params, sgx_pte_status *status,
                           sgx_stream_t stream);
 
+/* ---- Serving: a device-resident request loop for PTE closure batches ----
+ * No reference counterpart: the reference is a library called once per
+ * batch (get_sg_eos, singularity_eos.hpp:114-132). The server keeps the EOS
+ * tables and a device arena of hbm_budget_bytes resident, admits submitted
+ * requests in arrival order whenever an in-flight slot (a CUDA stream) and
+ * arena space for the request's arrays and solver scratch are free, and runs
+ * each admitted request (host->device copy, PTE solve, device->host copy) on
+ * its slot, so requests that arrive while others are on the GPU overlap
+ * with them. A request's result is the one sgx_pte_solve gives for the same
+ * inputs. Requests larger than the whole arena are rejected at submission. */
+typedef struct sgx_server sgx_server;
+
+typedef struct sgx_server_config {
+  size_t hbm_budget_bytes; /* device arena for request arrays and scratch */
+  int max_inflight;        /* concurrent requests on the device (1..64) */
+  int solver;              /* SGX_PTE_RHOT (SGX_PTE_PT with SGX_PREC_FP64 only) */
+  int precision;           /* SGX_PREC_FP64 or SGX_PREC_MIXED */
+  const sgx_eos *eos_list; /* host array, copied; tables must stay resident */
+  int neos;                /* 1..16 */
+  const sgx_mix_params *params; /* NULL = defaults */
+} sgx_server_config;
+
+/* One closure request: host arrays in the layout of sgx_pte_solve
+ * ([nmat][ncell], cell fastest). Inputs are read when the request is
+ * admitted and outputs written when it completes; the caller keeps every
+ * array alive and unmodified until sgx_server_wait reports completion.
+ * Host arrays from sgx_host_alloc (page-locked) let the copies overlap with
+ * other requests' kernels. eos_idx may be NULL (material m uses eos_list[m]);
+ * status may be NULL. */
+typedef struct sgx_pte_request {
+  int nmat;
+  int64_t ncell;
+  const int32_t *eos_idx;
+  const double *vfrac_tot, *sie_tot;
+  const double *rho_in, *vfrac_in, *sie_in, *temp_in, *press_in;
+  double *rho_out, *vfrac_out, *sie_out, *temp_out, *press_out;
+  sgx_pte_status *status;
+} sgx_pte_request;
+
+typedef struct sgx_server_stats {
+  uint64_t submitted, completed, failed;
+  uint64_t cells_completed;
+  int inflight, queued;
+  size_t arena_used, arena_peak;
+} sgx_server_stats;
+
+int sgx_server_create(const sgx_server_config *cfg, sgx_server **out);
+/* Queues a request; *ticket identifies it. Never blocks on the device. */
+int sgx_server_submit(sgx_server *s, const sgx_pte_request *req, uint64_t *ticket);
+/* Waits up to timeout_s seconds (< 0: forever) for a request. Returns SGX_OK
+ * when it completed (latency_s, if not NULL, receives submit-to-completion
+ * seconds), SGX_ERR_TIMEOUT when it is still pending, or the request's error.
+ * A completed ticket can be waited on once. */
+int sgx_server_wait(sgx_server *s, uint64_t ticket, double timeout_s, double *latency_s);
+int sgx_server_stats_get(sgx_server *s, sgx_server_stats *out);
+/* Waits for every request, then releases the arena, the streams and the
+ * worker thread. */
+int sgx_server_destroy(sgx_server *s);
+/* Page-locked host memory for request arrays (cudaHostAlloc / cudaFreeHost). */
+void *sgx_host_alloc(size_t bytes);
+void sgx_host_free(void *p);
+
 #ifdef __cplusplus
 }
 #endif

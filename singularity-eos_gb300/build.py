@@ -30,6 +30,7 @@ UNITS = [
     ("sgx_table", "sgx_table.cu", ["--fmad=false"]),
     ("sgx_noalloc", "sgx_noalloc.cu", ["--fmad=false"]),
     ("sgx_helm", "sgx_helm.cu", ["--fmad=false"]),
+    ("sgx_server", "sgx_server.cu", ["--fmad=false"]),
 ] + [(f"sgx_pte_fp64_n{n}", "sgx_pte_fp64_n.cu", ["--fmad=false", f"-DSGX_PTE_N={n}"])
      for n in range(1, 7)] + [
     (f"sgx_pte_mixed_n{n}", "sgx_pte_mixed_n.cu", ["--fmad=true", f"-DSGX_PTE_N={n}"])
@@ -78,7 +79,8 @@ def build(verbose=False):
             logs[futs[f]] = log
         probe.result()
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), "-shared", "-o", tmp] + sorted(objs) + ARCH + ["-cudart", "shared"]
+    cmd = [nvcc(), "-shared", "-o", tmp] + sorted(objs) + ARCH + ["-cudart", "shared",
+                                                                  "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

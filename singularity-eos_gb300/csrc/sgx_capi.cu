@@ -33,6 +33,10 @@ bool pte_type(int t) { return t >= SGX_IDEAL_GAS && t <= SGX_SPINER_RHOT; }
 
 } // namespace
 
+namespace sgx {
+int set_error(int code, const std::string &msg) { return fail(code, msg); }
+} // namespace sgx
+
 extern "C" {
 
 const char *sgx_version(void) { return "sgx 0.1 (sm_103a)"; }

@@ -2,6 +2,8 @@
 // translation units (sgx_fp64.cu, sgx_mixed.cu).
 #pragma once
 
+#include <string>
+
 #include <cuda_runtime.h>
 
 #include "../../include/sgx.h"
@@ -38,6 +40,9 @@ struct PteArgs {
   int *retry_idx;
 };
 constexpr int PTE_BINS = 8;
+
+// Sets the calling thread's sgx_last_error() message; returns code.
+int set_error(int code, const std::string &msg);
 
 // Per-cell PTE, FP64, following the reference iteration exactly.
 cudaError_t launch_pte_fp64(const PteArgs &a, cudaStream_t stream);

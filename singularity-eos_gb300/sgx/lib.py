@@ -25,6 +25,8 @@ EXPORTED = [
     "sgx_eos_fill_ex",
     "sgx_mix_params_default", "sgx_pte_rhot_required_scratch", "sgx_pte_pt_required_scratch",
     "sgx_pte_solve", "sgx_pte_solve_noalloc", "sgx_eos_helmholtz", "sgx_eos_helmholtz_dump",
+    "sgx_server_create", "sgx_server_submit", "sgx_server_wait", "sgx_server_stats_get",
+    "sgx_server_destroy", "sgx_host_alloc", "sgx_host_free",
 ]
 HELM_DEFAULT, HELM_REGULA_FALSI, HELM_CACHE_READBACK = 31, 32, 64
 PTE_NOALLOC_MAX_CELLS = 1 << 20  # SGX_PTE_NOALLOC_MAX_CELLS
@@ -63,6 +65,27 @@ class PteStatus(C.Structure):
                 ("small_step_iters", C.c_uint8)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_inflight", C.c_int),
+                ("solver", C.c_int), ("precision", C.c_int), ("eos_list", C.c_void_p),
+                ("neos", C.c_int), ("params", C.c_void_p)]
+
+
+class PteRequest(C.Structure):
+    _fields_ = [("nmat", C.c_int), ("ncell", C.c_int64), ("eos_idx", C.c_void_p),
+                ("vfrac_tot", C.c_void_p), ("sie_tot", C.c_void_p),
+                ("rho_in", C.c_void_p), ("vfrac_in", C.c_void_p), ("sie_in", C.c_void_p),
+                ("temp_in", C.c_void_p), ("press_in", C.c_void_p),
+                ("rho_out", C.c_void_p), ("vfrac_out", C.c_void_p), ("sie_out", C.c_void_p),
+                ("temp_out", C.c_void_p), ("press_out", C.c_void_p), ("status", C.c_void_p)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("cells_completed", C.c_uint64), ("inflight", C.c_int), ("queued", C.c_int),
+                ("arena_used", C.c_size_t), ("arena_peak", C.c_size_t)]
+
+
 _lib = None
 
 
@@ -98,6 +121,16 @@ def load():
     lib.sgx_eos_helmholtz.argtypes = [C.POINTER(SgxEos), C.c_char_p, I]
     lib.sgx_eos_helmholtz_dump.argtypes = [C.POINTER(SgxEos), P, C.c_long]
     lib.sgx_eos_helmholtz_dump.restype = C.c_long
+    lib.sgx_server_create.argtypes = [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]
+    lib.sgx_server_submit.argtypes = [C.c_void_p, C.POINTER(PteRequest),
+                                      C.POINTER(C.c_uint64)]
+    lib.sgx_server_wait.argtypes = [C.c_void_p, C.c_uint64, C.c_double,
+                                    C.POINTER(C.c_double)]
+    lib.sgx_server_stats_get.argtypes = [C.c_void_p, C.POINTER(ServerStats)]
+    lib.sgx_server_destroy.argtypes = [C.c_void_p]
+    lib.sgx_host_alloc.argtypes = [C.c_size_t]
+    lib.sgx_host_alloc.restype = C.c_void_p
+    lib.sgx_host_free.argtypes = [C.c_void_p]
     lib.sgx_pte_solve_noalloc.argtypes = [I, I, C.c_int64, P, I, P, P, P, P, P, P, P, P, P,
                                           C.POINTER(MixParams), P, P]
     _lib = lib
@@ -205,6 +238,64 @@ def pte_solve_noalloc(eos_list, eos_idx, vfrac_tot, sie_tot, rho, vfrac, sie, te
         ptr(vfrac_tot), ptr(sie_tot), ptr(rho), ptr(vfrac), ptr(sie), ptr(temp), ptr(press),
         ptr(lam), C.byref(params) if params is not None else None, ptr(status),
         stream_ptr(stream)))
+
+
+class Server:
+    """The serving loop (sgx_server_*). Request arrays are host numpy arrays
+    (page-locked ones, e.g. from torch pin_memory, let copies overlap);
+    they must stay alive until wait() returns for the ticket."""
+
+    def __init__(self, eos_list, hbm_budget_bytes=1 << 30, max_inflight=8,
+                 precision=PREC_MIXED, solver=PTE_RHOT, params=None):
+        lib = load()
+        self._eos = (SgxEos * len(eos_list))(*eos_list)
+        self._params = params
+        cfg = ServerConfig(hbm_budget_bytes, max_inflight, solver, precision,
+                           C.cast(self._eos, C.c_void_p), len(eos_list),
+                           C.cast(C.byref(params), C.c_void_p) if params is not None else None)
+        h = C.c_void_p()
+        check(lib.sgx_server_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+        self._keep = {}
+
+    def submit(self, req):
+        """req: dict with nmat, ncell, eos_idx (or None), vfrac_tot, sie_tot,
+        the five *_in and five *_out arrays and status (or None)."""
+        def p(a):
+            return None if a is None else C.c_void_p(a.ctypes.data)
+        r = PteRequest(req["nmat"], req["ncell"], p(req.get("eos_idx")), p(req["vfrac_tot"]),
+                       p(req["sie_tot"]), *(p(req[k + "_in"]) for k in
+                                            ("rho", "vfrac", "sie", "temp", "press")),
+                       *(p(req[k + "_out"]) for k in ("rho", "vfrac", "sie", "temp", "press")),
+                       p(req.get("status")))
+        t = C.c_uint64()
+        check(load().sgx_server_submit(self.h, C.byref(r), C.byref(t)))
+        self._keep[t.value] = req
+        return t.value
+
+    def wait(self, ticket, timeout=-1.0):
+        """Returns the submit-to-completion latency in seconds, or None on
+        timeout."""
+        lat = C.c_double()
+        rc = load().sgx_server_wait(self.h, ticket, timeout, C.byref(lat))
+        if rc == 6:
+            return None
+        self._keep.pop(ticket, None)
+        check(rc)
+        return lat.value
+
+    def stats(self):
+        st = ServerStats()
+        check(load().sgx_server_stats_get(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def close(self):
+        if self.h:
+            load().sgx_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
 
 
 def status_view(status_u8):

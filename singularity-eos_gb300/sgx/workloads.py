@@ -82,3 +82,30 @@ def pte_batched(ncell, seed=0, nmax=5, mix=(0.55, 0.25, 0.12, 0.08)):
                 vfrac_tot=np.ones(ncell), sie_tot=sie_tot,
                 rho=np.ascontiguousarray(rho), vfrac=np.ascontiguousarray(vfrac),
                 sie=z.copy(), temp=z.copy(), press=z.copy(), counts=counts)
+
+
+def serve_request(ncell, seed, pool, nmax=4):
+    """One closure request of the serving workload: 2..nmax materials per
+    cell drawn without replacement from `pool` (a list of EOS indices into
+    the server's EOS list), volume fractions Dirichlet(1,...,1), total
+    density log-uniform on [1e-3, 10] g/cc, sie uniform on [1e9, 1e11]
+    erg/g; zero temperature and pressure guesses. Returns a dict of
+    contiguous arrays in the sgx_pte_request layout ([nmax][ncell])."""
+    rng = np.random.default_rng(seed)
+    counts = rng.integers(2, nmax + 1, size=ncell)
+    eos_idx = np.full((nmax, ncell), -1, np.int32)
+    order = np.argsort(rng.random((ncell, len(pool))), axis=1)
+    pool = np.asarray(pool, np.int32)
+    for m in range(nmax):
+        present = counts > m
+        eos_idx[m, present] = pool[order[present, m]]
+    expo = rng.exponential(1.0, (nmax, ncell))
+    expo[eos_idx < 0] = 0.0
+    vfrac = expo / expo.sum(axis=0)
+    rho_tot = np.exp(rng.uniform(np.log(1e-3), np.log(10.0), ncell))
+    rho = np.where(eos_idx >= 0, rho_tot[None, :], 0.0)
+    z = np.zeros((nmax, ncell))
+    return dict(nmat=nmax, ncell=ncell, eos_idx=np.ascontiguousarray(eos_idx),
+                vfrac_tot=np.ones(ncell), sie_tot=rng.uniform(1e9, 1e11, ncell),
+                rho_in=np.ascontiguousarray(rho), vfrac_in=np.ascontiguousarray(vfrac),
+                sie_in=z.copy(), temp_in=z.copy(), press_in=z.copy())
