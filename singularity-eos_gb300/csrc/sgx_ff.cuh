@@ -1,0 +1,162 @@
+// Float-float ("ff") arithmetic: a value carried as an unevaluated sum
+// hi + lo of two floats, |lo| <= ulp(hi) / 2, about 48 significant bits.
+// On GB300 the FP32 pipe issues 64 times the FP64 pipe's operations, so a
+// kernel that needs ~1e-14 relative accuracy runs faster in ff than in FP64
+// even at 10-20 FP32 operations per ff operation.
+//
+// The building blocks are the error-free transformations of Knuth (two-sum)
+// and Dekker (quick two-sum), with the exact product error from fmaf; the
+// composite operations follow the classical double-word algorithms (Dekker
+// 1971; Bailey's double-double, restated for floats). Conversions between
+// double and ff go through the IEEE bit patterns with integer operations
+// only, so they never occupy the FP64 pipe; they are exact for normal values
+// whose exponents the callers check (ff_from_double_ok).
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace sgx {
+
+struct ff {
+  float hi, lo;
+};
+
+__device__ __forceinline__ ff ff_make(const float hi, const float lo = 0.0f) { return {hi, lo}; }
+
+// Every rounding the transformations below rely on is written with the _rn
+// intrinsics, which the compiler never fuses into an FMA: a fused
+// multiply-add in place of a separate product and sum would change s and
+// break the exactness of the error terms.
+#define FADD __fadd_rn
+#define FSUB __fsub_rn
+#define FMUL __fmul_rn
+
+// s + e == a + b exactly (Knuth).
+__device__ __forceinline__ ff two_sum(const float a, const float b) {
+  const float s = FADD(a, b);
+  const float bb = FSUB(s, a);
+  const float e = FADD(FSUB(a, FSUB(s, bb)), FSUB(b, bb));
+  return {s, e};
+}
+// Same when |a| >= |b| (Dekker).
+__device__ __forceinline__ ff quick_two_sum(const float a, const float b) {
+  const float s = FADD(a, b);
+  return {s, FSUB(b, FSUB(s, a))};
+}
+// p + e == a * b exactly.
+__device__ __forceinline__ ff two_prod(const float a, const float b) {
+  const float p = FMUL(a, b);
+  return {p, fmaf(a, b, -p)};
+}
+
+__device__ __forceinline__ ff ff_add(const ff x, const ff y) {
+  ff s = two_sum(x.hi, y.hi);
+  const ff t = two_sum(x.lo, y.lo);
+  s.lo = FADD(s.lo, t.hi);
+  s = quick_two_sum(s.hi, s.lo);
+  s.lo = FADD(s.lo, t.lo);
+  return quick_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ ff ff_neg(const ff x) { return {-x.hi, -x.lo}; }
+__device__ __forceinline__ ff ff_sub(const ff x, const ff y) { return ff_add(x, ff_neg(y)); }
+
+__device__ __forceinline__ ff ff_mul(const ff x, const ff y) {
+  ff p = two_prod(x.hi, y.hi);
+  p.lo = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, p.lo));
+  return quick_two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ ff ff_mul_f(const ff x, const float y) {
+  ff p = two_prod(x.hi, y);
+  p.lo = fmaf(x.lo, y, p.lo);
+  return quick_two_sum(p.hi, p.lo);
+}
+
+// x / y: a float quotient refined twice with exact residuals.
+__device__ __forceinline__ ff ff_div(const ff x, const ff y) {
+  const float r = 1.0f / y.hi;
+  const float q1 = FMUL(x.hi, r);
+  ff rem = ff_sub(x, ff_mul_f(y, q1));
+  const float q2 = FMUL(rem.hi, r);
+  rem = ff_sub(rem, ff_mul_f(y, q2));
+  const float q3 = FMUL(rem.hi, r);
+  const ff q = quick_two_sum(q1, q2);
+  return ff_add(q, ff_make(q3));
+}
+
+// sqrt(x) for x > 0: a float root refined by one Newton step in ff.
+__device__ __forceinline__ ff ff_sqrt(const ff x) {
+  const float s = sqrtf(x.hi);
+  const ff s2 = two_prod(s, s);
+  const ff d = ff_sub(x, s2);
+  return ff_add(ff_make(s), ff_make(FMUL(d.hi, 0.5f / s)));
+}
+
+__device__ __forceinline__ bool ff_gt(const ff a, const ff b) {
+  return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo);
+}
+__device__ __forceinline__ bool ff_lt(const ff a, const ff b) {
+  return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo);
+}
+
+// ---- conversions through the bit patterns ----
+
+// Whether d2ff below represents x to ~48 bits: x == 0, or its binary
+// exponent in [-74, 127] (then hi is a normal float and lo does not
+// underflow).
+__device__ __forceinline__ bool ff_from_double_ok(const double x) {
+  const int e = static_cast<int>((__double_as_longlong(x) >> 52) & 0x7ff) - 1023;
+  return x == 0.0 || (e >= -74 && e <= 127);
+}
+
+// hi: x truncated to 24 significant bits; lo: the remaining 29 bits,
+// rounded to 24. Integer and FP32 operations only.
+__device__ __forceinline__ ff d2ff(const double x) {
+  const long long b = __double_as_longlong(x);
+  const int ex = static_cast<int>((b >> 52) & 0x7ff);
+  if (ex == 0) return {0.0f, 0.0f};
+  const int e = ex - 1023;
+  const unsigned sign = static_cast<unsigned>((b >> 32) & 0x80000000u);
+  const long long mant = b & ((1LL << 52) - 1);
+  const float hi = __uint_as_float(sign | (static_cast<unsigned>(e + 127) << 23) |
+                                   static_cast<unsigned>(mant >> 29));
+  const unsigned rest = static_cast<unsigned>(mant & ((1LL << 29) - 1));
+  // rest * 2^(e - 52), with the sign of x; e - 52 + 127 >= 1 under the
+  // ff_from_double_ok range
+  const float scale = __uint_as_float(static_cast<unsigned>(e - 52 + 127) << 23);
+  const float lo = __uint_as_float(__float_as_uint(static_cast<float>(rest) * scale) | sign);
+  return {hi, lo};
+}
+
+// The double with the value of a float (normal floats, zero, inf, NaN;
+// subnormal floats become zero), by moving the fields.
+__device__ __forceinline__ double f2d_bits(const float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned long long sign = static_cast<unsigned long long>(u & 0x80000000u) << 32;
+  const unsigned ex = (u >> 23) & 0xff;
+  const unsigned long long mant = static_cast<unsigned long long>(u & 0x7fffff) << 29;
+  if (ex == 0) return __longlong_as_double(static_cast<long long>(sign));
+  const unsigned long long e64 = ex == 0xff ? 0x7ffULL : static_cast<unsigned long long>(ex + 896);
+  return __longlong_as_double(static_cast<long long>(sign | (e64 << 52) | mant));
+}
+
+// hi + lo as a double: one FP64 addition.
+__device__ __forceinline__ double ff2d(const ff x) { return f2d_bits(x.hi) + f2d_bits(x.lo); }
+
+// A float that holds an integer of magnitude < 2^62, as int64 (shift of the
+// significand by the exponent); values below 1 give 0.
+__device__ __forceinline__ long long f2ll_bits(const float f) {
+  const unsigned u = __float_as_uint(f);
+  const int ex = static_cast<int>((u >> 23) & 0xff) - 127;
+  if (ex < 0) return 0;
+  const long long m = static_cast<long long>((u & 0x7fffff) | 0x800000);
+  const long long v = ex >= 23 ? (m << (ex - 23)) : (m >> (23 - ex));
+  return (u & 0x80000000u) ? -v : v;
+}
+
+#undef FADD
+#undef FSUB
+#undef FMUL
+
+} // namespace sgx

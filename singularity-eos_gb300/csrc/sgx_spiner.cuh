@@ -30,6 +30,17 @@ struct alignas(32) dq4 {
 struct alignas(16) fq4 {
   float x, y, z, w;
 };
+// One interpolation cell in difference form, for the float-float lookup:
+// f(a, b) = x + a dT + b dR + a b dRT over the cell's unit square (a: T
+// weight, b: density weight), the differences formed in FP64 on the host.
+// sie keeps FP64 (the root's numerator sie - x - b dR cancels where the cold
+// energy dominates); the other fields are float pairs (hi, lo).
+struct alignas(32) SieRec {
+  double x, dT, dR, dRT;
+};
+struct alignas(16) FfRec {
+  float x[2], dT[2], dR[2], dRT[2];
+};
 
 struct Grid1D {
   double min, max, dx, inv_dx;
@@ -71,6 +82,11 @@ struct SpinerTable {
   const dq4 *sie4, *P4, *bmod4; // corner-packed [nRho-1][nT-1]
   const fq4 *sie4f;               // corner-packed FP32 copy of sie
   const float *sieCold32, *sielTMax32; // FP32 copies of the on-table bounds
+  // float-float records [nRho-1][nT-1]; ff_ok = 0 when a value is outside
+  // the float exponent range (the lookups then take the FP64 iteration)
+  const SieRec *sieR;
+  const FfRec *PR, *bmodR;
+  int ff_ok;
 };
 
 // ---- interpolation (DataBox::interpToReal) ----

@@ -405,6 +405,12 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
   }
   offf = off;
   off = align(off + ncell * sizeof(fq4));
+  const size_t offsr = off;
+  off = align(off + ncell * sizeof(SieRec));
+  const size_t offpr = off;
+  off = align(off + ncell * sizeof(FfRec));
+  const size_t offbr = off;
+  off = align(off + ncell * sizeof(FfRec));
   const size_t offc32 = off;
   off = align(off + static_cast<size_t>(nR) * sizeof(float));
   const size_t offm32 = off;
@@ -437,6 +443,41 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
         std::memcpy(q + (static_cast<size_t>(j) * (nT - 1) + i) * sizeof(fq4), c, sizeof(c));
       }
   }
+  {
+    // difference-form records; values beyond the float range disable them
+    bool ok = true;
+    auto split = [&ok](const double v, float out[2]) {
+      if (!(std::fabs(v) <= 1e37)) ok = false;
+      const double w = std::fabs(v) < 1e-30 ? 0.0 : v;
+      out[0] = static_cast<float>(w);
+      out[1] = static_cast<float>(w - static_cast<double>(out[0]));
+    };
+    const std::vector<double> &fs = h.f2[F_SIE], &fp = h.f2[F_P], &fb = h.f2[F_BMOD];
+    for (int j = 0; j < nR - 1; ++j)
+      for (int i = 0; i < nT - 1; ++i) {
+        const size_t c = static_cast<size_t>(j) * (nT - 1) + i;
+        const size_t k00 = static_cast<size_t>(j) * nT + i, k01 = k00 + 1, k10 = k00 + nT,
+                     k11 = k10 + 1;
+        SieRec sr;
+        sr.x = fs[k00];
+        sr.dT = fs[k01] - fs[k00];
+        sr.dR = fs[k10] - fs[k00];
+        sr.dRT = (fs[k11] - fs[k10]) - (fs[k01] - fs[k00]);
+        std::memcpy(img.data() + offsr + c * sizeof(SieRec), &sr, sizeof(sr));
+        const std::vector<double> *pf[2] = {&fp, &fb};
+        const size_t offr[2] = {offpr, offbr};
+        for (int q = 0; q < 2; ++q) {
+          const std::vector<double> &f = *pf[q];
+          FfRec r;
+          split(f[k00], r.x);
+          split(f[k01] - f[k00], r.dT);
+          split(f[k10] - f[k00], r.dR);
+          split((f[k11] - f[k10]) - (f[k01] - f[k00]), r.dRT);
+          std::memcpy(img.data() + offr[q] + c * sizeof(FfRec), &r, sizeof(r));
+        }
+      }
+    t.ff_ok = ok ? 1 : 0;
+  }
   for (int j = 0; j < nR; ++j) {
     const float c = static_cast<float>(h.f1[F_SIECOLD][j]);
     const float m = static_cast<float>(h.f1[F_SIELTMAX][j]);
@@ -461,6 +502,9 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
   td.sie4f = reinterpret_cast<const fq4 *>(d + offf);
   td.sieCold32 = reinterpret_cast<const float *>(d + offc32);
   td.sielTMax32 = reinterpret_cast<const float *>(d + offm32);
+  td.sieR = reinterpret_cast<const SieRec *>(d + offsr);
+  td.PR = reinterpret_cast<const FfRec *>(d + offpr);
+  td.bmodR = reinterpret_cast<const FfRec *>(d + offbr);
   std::memcpy(img.data(), &td, sizeof(td));
   e = cudaMemcpy(dev, img.data(), bytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
