@@ -221,6 +221,21 @@ int sgx_eos_fill_ex(const sgx_eos *eos, int64_t n, double *rho, double *temp, do
                     double *press, double *cv, double *bmod, double *cs, uint32_t output,
                     double *lambda, int lambda_stride, int precision, sgx_stream_t stream);
 
+/* FillEos over HOST arrays (the arguments of sgx_eos_fill_ex with host
+ * pointers and no stream). Blocks until the outputs are in the host arrays.
+ * When every array is page-locked (sgx_host_alloc, cudaHostAlloc) and the
+ * GPU uses the host's page tables (a coherent CPU-GPU system such as Grace
+ * over NVLink-C2C), the kernel reads and writes the host arrays in place.
+ * Otherwise the library streams the arrays through the device in chunks of
+ * 2^21 elements on three streams, so the copies of one chunk overlap the
+ * kernel of the next; inputs are the non-null arrays whose bit is not in
+ * output (rho always, lambda both ways), outputs the arrays whose bit is in
+ * output, cs and lambda. No reference counterpart beyond FillEos on host
+ * data. */
+int sgx_eos_fill_host(const sgx_eos *eos, int64_t n, double *rho, double *temp, double *sie,
+                      double *press, double *cv, double *bmod, double *cs, uint32_t output,
+                      double *lambda, int lambda_stride, int precision);
+
 /* ---- PTE ---- */
 int sgx_mix_params_default(sgx_mix_params *p);
 int sgx_pte_rhot_required_scratch(int nmat);

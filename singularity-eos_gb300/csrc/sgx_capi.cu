@@ -293,6 +293,114 @@ int sgx_eos_fill_ex(const sgx_eos *eos, int64_t n, double *rho, double *temp, do
   return SGX_OK;
 }
 
+// FillEos over host arrays, streamed through the device in chunks: on each
+// of three streams in turn, the chunk's inputs go up, sgx_eos_fill_ex runs on
+// them and its outputs come back, so the copies of one chunk overlap the
+// kernel of the next and the copies of the one after. Inputs are the
+// non-null arrays whose bit is not in output (rho always; lambda both ways);
+// outputs are the arrays whose bit is in output, cs and lambda.
+int sgx_eos_fill_host(const sgx_eos *eos, int64_t n, double *rho, double *temp, double *sie,
+                      double *press, double *cv, double *bmod, double *cs, uint32_t output,
+                      double *lambda, int lambda_stride, int precision) {
+  if (!eos || !valid_type(eos->type)) return fail(SGX_ERR_INVALID, "sgx_eos_fill_host: bad eos");
+  if (n < 0) return fail(SGX_ERR_INVALID, "sgx_eos_fill_host: n < 0");
+  if (n == 0) return SGX_OK;
+  if (!rho) return fail(SGX_ERR_INVALID, "sgx_eos_fill_host: rho is required");
+  if (lambda && lambda_stride < 2)
+    return fail(SGX_ERR_INVALID, "sgx_eos_fill_host: lambda_stride < 2");
+  struct Arr {
+    double *h;
+    int width;
+    bool in, out;
+  };
+  Arr arr[8] = {{rho, 1, !(output & SGX_Q_DENSITY), (output & SGX_Q_DENSITY) != 0},
+                {temp, 1, !(output & SGX_Q_TEMPERATURE), (output & SGX_Q_TEMPERATURE) != 0},
+                {sie, 1, !(output & SGX_Q_SIE), (output & SGX_Q_SIE) != 0},
+                {press, 1, !(output & SGX_Q_PRESSURE), (output & SGX_Q_PRESSURE) != 0},
+                {cv, 1, !(output & SGX_Q_SPECIFIC_HEAT), (output & SGX_Q_SPECIFIC_HEAT) != 0},
+                {bmod, 1, !(output & SGX_Q_BULK_MODULUS), (output & SGX_Q_BULK_MODULUS) != 0},
+                {cs, 1, false, true},
+                {lambda, lambda_stride, true, true}};
+  // On a coherent CPU-GPU system (the GPU walks the host's page tables, as on
+  // Grace over NVLink-C2C) a kernel reads and writes page-locked host memory
+  // at link bandwidth: run the fill in place on the mapped host arrays, the
+  // transfers overlapping the arithmetic inside the kernel.
+  {
+    int dev = 0, coherent = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&coherent, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
+    double *mapped[8] = {};
+    bool all_mapped = coherent != 0;
+    for (int k = 0; k < 8 && all_mapped; ++k) {
+      if (!arr[k].h) continue;
+      cudaPointerAttributes at;
+      if (cudaPointerGetAttributes(&at, arr[k].h) != cudaSuccess ||
+          at.type != cudaMemoryTypeHost || !at.devicePointer) {
+        cudaGetLastError(); // clear a lookup failure on unregistered memory
+        all_mapped = false;
+        break;
+      }
+      mapped[k] = static_cast<double *>(at.devicePointer);
+    }
+    if (all_mapped) {
+      cudaStream_t s0 = nullptr;
+      cudaError_t e0 = cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking);
+      if (e0 != cudaSuccess) return cuda_fail(e0, "sgx_eos_fill_host");
+      const int r0 = sgx_eos_fill_ex(eos, n, mapped[0], mapped[1], mapped[2], mapped[3],
+                                     mapped[4], mapped[5], mapped[6], output, mapped[7],
+                                     lambda_stride, precision, reinterpret_cast<sgx_stream_t>(s0));
+      e0 = cudaStreamSynchronize(s0);
+      cudaStreamDestroy(s0);
+      if (r0 != SGX_OK) return r0;
+      if (e0 != cudaSuccess) return cuda_fail(e0, "sgx_eos_fill_host");
+      return SGX_OK;
+    }
+  }
+  constexpr int S = 3;
+  const int64_t chunk = n < (int64_t(1) << 21) ? n : (int64_t(1) << 21);
+  cudaStream_t st[S] = {};
+  double *dev[S][8] = {};
+  int rc = SGX_OK;
+  cudaError_t e = cudaSuccess;
+  for (int s = 0; s < S && e == cudaSuccess; ++s) {
+    e = cudaStreamCreateWithFlags(&st[s], cudaStreamNonBlocking);
+    for (int k = 0; k < 8 && e == cudaSuccess; ++k)
+      if (arr[k].h)
+        e = cudaMallocAsync(reinterpret_cast<void **>(&dev[s][k]),
+                            static_cast<size_t>(chunk) * arr[k].width * sizeof(double), st[s]);
+  }
+  for (int64_t off = 0, c = 0; off < n && e == cudaSuccess && rc == SGX_OK; off += chunk, ++c) {
+    const int s = static_cast<int>(c % S);
+    const int64_t len = (n - off) < chunk ? (n - off) : chunk;
+    for (int k = 0; k < 8 && e == cudaSuccess; ++k)
+      if (arr[k].h && arr[k].in)
+        e = cudaMemcpyAsync(dev[s][k], arr[k].h + off * arr[k].width,
+                            static_cast<size_t>(len) * arr[k].width * sizeof(double),
+                            cudaMemcpyHostToDevice, st[s]);
+    if (e != cudaSuccess) break;
+    rc = sgx_eos_fill_ex(eos, len, dev[s][0], dev[s][1], dev[s][2], dev[s][3], dev[s][4],
+                         dev[s][5], dev[s][6], output, dev[s][7], lambda_stride, precision,
+                         reinterpret_cast<sgx_stream_t>(st[s]));
+    if (rc != SGX_OK) break;
+    for (int k = 0; k < 8 && e == cudaSuccess; ++k)
+      if (arr[k].h && arr[k].out)
+        e = cudaMemcpyAsync(arr[k].h + off * arr[k].width, dev[s][k],
+                            static_cast<size_t>(len) * arr[k].width * sizeof(double),
+                            cudaMemcpyDeviceToHost, st[s]);
+  }
+  for (int s = 0; s < S; ++s) {
+    if (!st[s]) continue;
+    for (int k = 0; k < 8; ++k)
+      if (dev[s][k]) cudaFreeAsync(dev[s][k], st[s]);
+    const cudaError_t f = cudaStreamSynchronize(st[s]);
+    if (e == cudaSuccess) e = f;
+    cudaStreamDestroy(st[s]);
+  }
+  if (rc != SGX_OK) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "sgx_eos_fill_host");
+  return SGX_OK;
+}
+
 int sgx_eos_fill(const sgx_eos *eos, int64_t n, double *rho, double *temp, double *sie,
                  double *press, double *cv, double *bmod, uint32_t output, double *lambda,
                  int lambda_stride, sgx_stream_t stream) {

@@ -26,7 +26,7 @@ EXPORTED = [
     "sgx_mix_params_default", "sgx_pte_rhot_required_scratch", "sgx_pte_pt_required_scratch",
     "sgx_pte_solve", "sgx_pte_solve_noalloc", "sgx_eos_helmholtz", "sgx_eos_helmholtz_dump",
     "sgx_server_create", "sgx_server_submit", "sgx_server_wait", "sgx_server_stats_get",
-    "sgx_server_destroy", "sgx_host_alloc", "sgx_host_free",
+    "sgx_server_destroy", "sgx_host_alloc", "sgx_host_free", "sgx_eos_fill_host",
 ]
 HELM_DEFAULT, HELM_REGULA_FALSI, HELM_CACHE_READBACK = 31, 32, 64
 PTE_NOALLOC_MAX_CELLS = 1 << 20  # SGX_PTE_NOALLOC_MAX_CELLS
@@ -121,6 +121,8 @@ def load():
     lib.sgx_eos_helmholtz.argtypes = [C.POINTER(SgxEos), C.c_char_p, I]
     lib.sgx_eos_helmholtz_dump.argtypes = [C.POINTER(SgxEos), P, C.c_long]
     lib.sgx_eos_helmholtz_dump.restype = C.c_long
+    lib.sgx_eos_fill_host.argtypes = [C.POINTER(SgxEos), C.c_int64, P, P, P, P, P, P, P,
+                                      C.c_uint32, P, I, I]
     lib.sgx_server_create.argtypes = [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]
     lib.sgx_server_submit.argtypes = [C.c_void_p, C.POINTER(PteRequest),
                                       C.POINTER(C.c_uint64)]
@@ -211,6 +213,17 @@ def fill_eos(eos, rho, temp, sie, press, cv, bmod, output, lam=None, lam_stride=
         check(load().sgx_eos_fill_ex(C.byref(eos), n, ptr(rho), ptr(temp), ptr(sie),
                                      ptr(press), ptr(cv), ptr(bmod), ptr(cs), output, ptr(lam),
                                      lam_stride, precision, stream_ptr(stream)))
+
+
+def fill_eos_host(eos, rho, temp, sie, press, cv, bmod, output, lam=None, lam_stride=0,
+                  cs=None, precision=PREC_FP64):
+    """FillEos over host numpy arrays (float64, contiguous), streamed through
+    the device by the library."""
+    def p(a):
+        return None if a is None else C.c_void_p(a.ctypes.data)
+    check(load().sgx_eos_fill_host(C.byref(eos), rho.size, p(rho), p(temp), p(sie), p(press),
+                                   p(cv), p(bmod), p(cs), output, p(lam), lam_stride,
+                                   precision))
 
 
 def pte_solve(solver, eos_list, eos_idx, vfrac_tot, sie_tot, rho, vfrac, sie, temp, press,

@@ -141,3 +141,31 @@ def test_mixed_pte_accuracy(sgx, kind):
     pol = st["converged"] & ~st["resolved_fp64"]
     vsum = np.where(present, got["vfrac"], 0).sum(axis=0)
     assert np.abs(vsum[pol] - wl["vfrac_tot"][pol]).max() <= 1e-13
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_host_array_fill_matches_device_fill(sgx, precision):
+    """sgx_eos_fill_host (chunks streamed through three streams) gives
+    exactly the device call's results, across chunk boundaries."""
+    import ctypes as C
+    from sgx import sp5lite
+    path, _ = stiffgas_table_path()
+    tab = sgx.spiner_eos(path, 1)
+    try:
+        n = (1 << 22) + 12345  # three chunks, the last partial
+        rho_h, sie_h = sp5lite.stiffgas_queries(n, seed=5)
+        host = [torch.empty(n, dtype=torch.float64).pin_memory().numpy() for _ in range(4)]
+        lam_h = torch.full((2 * n,), float("nan"), dtype=torch.float64).pin_memory().numpy()
+        q = sgx.Q_TEMPERATURE | sgx.Q_PRESSURE | sgx.Q_BULK_MODULUS
+        sgx.fill_eos_host(tab, rho_h, host[0], sie_h, host[1], None, host[2], q, lam=lam_h,
+                          lam_stride=2, cs=host[3], precision=precision)
+        rho, sie = torch.as_tensor(rho_h, device="cuda"), torch.as_tensor(sie_h, device="cuda")
+        T, P, bm, cs = (torch.zeros_like(rho) for _ in range(4))
+        lam = torch.full((2 * n,), float("nan"), dtype=torch.float64, device="cuda")
+        sgx.fill_eos(tab, rho, T, sie, P, None, bm, q, lam=lam, lam_stride=2, cs=cs,
+                     precision=precision)
+        torch.cuda.synchronize()
+        for h, d in zip(host + [lam_h], (T, P, bm, cs, lam)):
+            assert np.array_equal(h.view(np.uint64), d.cpu().numpy().view(np.uint64))
+    finally:
+        sgx.load().sgx_eos_finalize(C.byref(tab))
