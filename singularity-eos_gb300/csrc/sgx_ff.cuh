@@ -141,8 +141,35 @@ __device__ __forceinline__ double f2d_bits(const float f) {
   return __longlong_as_double(static_cast<long long>(sign | (e64 << 52) | mant));
 }
 
-// hi + lo as a double: one FP64 addition.
-__device__ __forceinline__ double ff2d(const ff x) { return f2d_bits(x.hi) + f2d_bits(x.lo); }
+// hi + lo as a double, by integer operations: lo's significand is aligned
+// to hi's 2^(e-52) grid (bits below that grid are dropped, an error below
+// 2^-52 relative) and added to hi's; one renormalisation step covers the
+// carry or borrow. hi must be a normal float or zero (lo may be anything).
+__device__ __forceinline__ double ff2d(const ff x) {
+  const unsigned uh = __float_as_uint(x.hi), ul = __float_as_uint(x.lo);
+  const int eh = static_cast<int>((uh >> 23) & 0xff), el = static_cast<int>((ul >> 23) & 0xff);
+  if (eh == 0 || eh == 0xff) return f2d_bits(x.hi);
+  // hi as a 53-bit integer significand m (units 2^(eh-127-52))
+  long long m = static_cast<long long>((uh & 0x7fffff) | 0x800000) << 29;
+  if (el != 0) {
+    const long long ml = static_cast<long long>((ul & 0x7fffff) | 0x800000);
+    const int shift = eh - el; // lo = ml * 2^(el-127-23): 29 - shift bits above the grid
+    const long long add = shift <= 29 ? (ml << (29 - shift)) : (shift < 53 ? ml >> (shift - 29) : 0);
+    m += ((uh ^ ul) & 0x80000000u) ? -add : add;
+  }
+  int e = eh;
+  if (m >= (1LL << 53)) {
+    m >>= 1;
+    ++e;
+  } else if (m < (1LL << 52)) {
+    m <<= 1;
+    --e;
+  }
+  const unsigned long long sign = static_cast<unsigned long long>(uh & 0x80000000u) << 32;
+  return __longlong_as_double(static_cast<long long>(
+      sign | (static_cast<unsigned long long>(e + 896) << 52) |
+      (static_cast<unsigned long long>(m) & ((1ULL << 52) - 1))));
+}
 
 // A float that holds an integer of magnitude < 2^62, as int64 (shift of the
 // significand by the exponent); values below 1 give 0.

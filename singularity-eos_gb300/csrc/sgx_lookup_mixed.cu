@@ -35,6 +35,7 @@
 #include "sgx_dispatch.cuh"
 #include "sgx_ff.cuh"
 #include "sgx_internal.h"
+#include "sgx_table.h"
 
 namespace sgx {
 
@@ -76,9 +77,11 @@ __device__ __forceinline__ SieRec load_sie(const SieRec *p) {
   return {u.x, u.y, v.x, v.y};
 }
 
-__global__ void __launch_bounds__(LOOKUP_BLOCK, 3) spiner_fill_mixed(const FillArgs a) {
+__global__ void __launch_bounds__(LOOKUP_BLOCK, 3) spiner_fill_mixed(const FillArgs a,
+                                                                     const int stage_coarse) {
   __shared__ SpinerTable st;
   __shared__ FfConsts sc;
+  extern __shared__ float2 s_coarse[]; // [nRho-1][SP_COARSE] when staged
   if (threadIdx.x == 0) {
     st = sp_table(a.eos);
     sc.rho_min_f = d2ff(st.gRho.min).hi;
@@ -91,6 +94,12 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, 3) spiner_fill_mixed(const FillA
     sc.eps = d2ff(lim<double>::eps);
   }
   __syncthreads();
+  if (stage_coarse) {
+    const int nco = (st.nRho - 1) * SP_COARSE;
+    for (int k = threadIdx.x; k < nco; k += blockDim.x)
+      s_coarse[k] = __ldg(st.sieCoarse + k);
+    __syncthreads();
+  }
   const SpinerTable &t = st;
   const unsigned out = a.output;
   const int nc = t.nT - 1;
@@ -138,8 +147,7 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, 3) spiner_fill_mixed(const FillA
         fast = u >= 0.0 && u <= static_cast<double>(t.nRho - 2);
         j = fast ? static_cast<int>(u) : 0;
       }
-      const double xl = __dadd_rn(t.gRho.min, __dmul_rn(static_cast<double>(j), t.gRho.dx));
-      b1 = __dmul_rn(__dsub_rn(lRho, xl), t.gRho.inv_dx);
+      b1 = __dmul_rn(__dsub_rn(lRho, __ldg(t.rhoNodes + j)), t.gRho.inv_dx);
       B = ff_from_double_ok(b1) ? d2ff(b1) : ff_make(0.0f);
       fast = fast && B.hi >= 0.0f && B.hi <= 1.0f;
     }
@@ -151,9 +159,24 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, 3) spiner_fill_mixed(const FillA
       const float sm0 = fmaf(b1f, t.sielTMax32[j + 1], b0f * t.sielTMax32[j]);
       fast = ef > sc0 + 1e-6f * fabsf(sc0) && ef < sm0 - 1e-6f * fabsf(sm0);
       if (fast) {
-        // 3. bracketing cell in FP32
+        // 3. bracketing cell in FP32: first among every coarse_stride-th
+        //    node (shared memory), then within that stretch
         const fq4 *row32 = t.sie4f + static_cast<long long>(j) * nc;
         int lo = 0, hi = nc - 1;
+        if (stage_coarse) {
+          const float2 *cr = s_coarse + j * SP_COARSE;
+          int kl = 0, kh = SP_COARSE - 1;
+          while (kl < kh) {
+            const int mid = (kl + kh + 1) >> 1;
+            const float2 q = cr[mid];
+            if (fmaf(b1f, q.y, b0f * q.x) <= ef)
+              kl = mid;
+            else
+              kh = mid - 1;
+          }
+          lo = kl * t.coarse_stride;
+          hi = min(lo + t.coarse_stride - 1, nc - 1);
+        }
         while (lo < hi) {
           const int mid = (lo + hi + 1) >> 1;
           const fq4 q = row32[mid];
@@ -255,10 +278,15 @@ cudaError_t launch_fill_mixed(const FillArgs &a, cudaStream_t stream) {
   int dev = 0, sms = 152;
   if (cudaGetDevice(&dev) == cudaSuccess)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  // the coarse index of the T search, staged per block when it fits
+  const int nrho = table_nrho(a.eos.table);
+  const size_t coarse = nrho > 1 ? static_cast<size_t>(nrho - 1) * SP_COARSE * sizeof(float2) : 0;
+  const int stage = (coarse > 0 && coarse <= 40 * 1024) ? 1 : 0;
+  // persistent grid: the blocks resident at once, each staging the index once
   const long long want = (a.n + LOOKUP_BLOCK - 1) / LOOKUP_BLOCK;
-  const long long cap = static_cast<long long>(sms) * 8;
+  const long long cap = static_cast<long long>(sms) * 3;
   const int grid = static_cast<int>(want < cap ? want : cap);
-  spiner_fill_mixed<<<grid, LOOKUP_BLOCK, 0, stream>>>(a);
+  spiner_fill_mixed<<<grid, LOOKUP_BLOCK, stage ? coarse : 0, stream>>>(a, stage);
   return cudaGetLastError();
 }
 

@@ -86,8 +86,15 @@ struct SpinerTable {
   // the float exponent range (the lookups then take the FP64 iteration)
   const SieRec *sieR;
   const FfRec *PR, *bmodR;
+  const double *rhoNodes; // Grid1D node positions min + j * dx, rounded as weights() rounds them
+  // every coarse_stride-th T node of each density cell's two rows
+  // ([nRho-1][SP_COARSE], (sie(j, i), sie(j+1, i)), +inf past the last cell),
+  // staged in shared memory by the lookup to shorten its search
+  const float2 *sieCoarse;
+  int coarse_stride;
   int ff_ok;
 };
+constexpr int SP_COARSE = 16;
 
 // ---- interpolation (DataBox::interpToReal) ----
 SGX_HD double interp1(const Grid1D &g, const double *d, const double x) {

@@ -411,6 +411,10 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
   off = align(off + ncell * sizeof(FfRec));
   const size_t offbr = off;
   off = align(off + ncell * sizeof(FfRec));
+  const size_t offxl = off;
+  off = align(off + static_cast<size_t>(nR) * sizeof(double));
+  const size_t offco = off;
+  off = align(off + static_cast<size_t>(nR - 1) * SP_COARSE * sizeof(float2));
   const size_t offc32 = off;
   off = align(off + static_cast<size_t>(nR) * sizeof(float));
   const size_t offm32 = off;
@@ -477,6 +481,25 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
         }
       }
     t.ff_ok = ok ? 1 : 0;
+    for (int j = 0; j < nR; ++j) {
+      const double xl = t.gRho.min + j * t.gRho.dx; // as Grid1D::weights (no contraction)
+      std::memcpy(img.data() + offxl + j * sizeof(double), &xl, sizeof(double));
+    }
+    const int nc = nT - 1;
+    t.coarse_stride = (nc + SP_COARSE - 1) / SP_COARSE;
+    for (int j = 0; j < nR - 1; ++j)
+      for (int k = 0; k < SP_COARSE; ++k) {
+        const int i = k * t.coarse_stride;
+        float2 v;
+        if (i < nc) {
+          v.x = static_cast<float>(fs[static_cast<size_t>(j) * nT + i]);
+          v.y = static_cast<float>(fs[static_cast<size_t>(j + 1) * nT + i]);
+        } else {
+          v.x = v.y = INFINITY;
+        }
+        std::memcpy(img.data() + offco + (static_cast<size_t>(j) * SP_COARSE + k) * sizeof(float2),
+                    &v, sizeof(v));
+      }
   }
   for (int j = 0; j < nR; ++j) {
     const float c = static_cast<float>(h.f1[F_SIECOLD][j]);
@@ -505,6 +528,8 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
   td.sieR = reinterpret_cast<const SieRec *>(d + offsr);
   td.PR = reinterpret_cast<const FfRec *>(d + offpr);
   td.bmodR = reinterpret_cast<const FfRec *>(d + offbr);
+  td.rhoNodes = reinterpret_cast<const double *>(d + offxl);
+  td.sieCoarse = reinterpret_cast<const float2 *>(d + offco);
   std::memcpy(img.data(), &td, sizeof(td));
   e = cudaMemcpy(dev, img.data(), bytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
@@ -657,6 +682,12 @@ int table_free(uint64_t handle, std::string &msg) {
   cudaFree(it->second.dev);
   g_tables.erase(it);
   return SGX_OK;
+}
+
+int table_nrho(uint64_t handle) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_tables.find(handle);
+  return (it == g_tables.end() || !it->second.dump.empty()) ? 0 : it->second.host.t.nRho;
 }
 
 size_t table_bytes(uint64_t handle) {

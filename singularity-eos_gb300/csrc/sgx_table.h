@@ -17,6 +17,8 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
 int table_load_helm(const char *path, uint64_t *handle, std::string &msg);
 int table_free(uint64_t handle, std::string &msg);
 size_t table_bytes(uint64_t handle);
+// Density nodes of a resident Spiner table (0 if unknown).
+int table_nrho(uint64_t handle);
 // Spiner: derived tables in the reference's DBLIST order; Helmholtz: node
 // values and fields in its DBLIST order. Returns the count or -1.
 long table_dump(uint64_t handle, double *out, long cap);
