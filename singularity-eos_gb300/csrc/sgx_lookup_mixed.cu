@@ -94,10 +94,13 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, 3) spiner_fill_mixed(const FillA
     sc.eps = d2ff(lim<double>::eps);
   }
   __syncthreads();
+  // shared rows padded to SP_COARSE + 1 entries: lanes probing the same
+  // entry of different rows then fall in different banks
+  constexpr int CS = SP_COARSE + 1;
   if (stage_coarse) {
     const int nco = (st.nRho - 1) * SP_COARSE;
     for (int k = threadIdx.x; k < nco; k += blockDim.x)
-      s_coarse[k] = __ldg(st.sieCoarse + k);
+      s_coarse[(k / SP_COARSE) * CS + k % SP_COARSE] = __ldg(st.sieCoarse + k);
     __syncthreads();
   }
   const SpinerTable &t = st;
@@ -108,10 +111,17 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, 3) spiner_fill_mixed(const FillA
                           (t.gCold.n == t.gRho.n) &&
                           ff_from_double_ok(t.gRho.min) && ff_from_double_ok(t.gT.min);
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
-  for (long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; e < a.n;
-       e += stride) {
-    const double rho = a.rho[e];
-    const double sie = a.sie[e];
+  // the next element's inputs are loaded while this one is computed
+  long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  double rho_next = e < a.n ? __ldg(a.rho + e) : 0.0;
+  double sie_next = e < a.n ? __ldg(a.sie + e) : 0.0;
+  for (; e < a.n; e += stride) {
+    const double rho = rho_next;
+    const double sie = sie_next;
+    if (e + stride < a.n) {
+      rho_next = __ldg(a.rho + e + stride);
+      sie_next = __ldg(a.sie + e + stride);
+    }
     double *lam = a.lambda ? a.lambda + e * a.lambda_stride : nullptr;
     bool fast = table_fast && rho > 0.0 && ff_from_double_ok(rho);
     int j = 0, i = 0;
@@ -164,7 +174,7 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, 3) spiner_fill_mixed(const FillA
         const fq4 *row32 = t.sie4f + static_cast<long long>(j) * nc;
         int lo = 0, hi = nc - 1;
         if (stage_coarse) {
-          const float2 *cr = s_coarse + j * SP_COARSE;
+          const float2 *cr = s_coarse + j * CS;
           int kl = 0, kh = SP_COARSE - 1;
           while (kl < kh) {
             const int mid = (kl + kh + 1) >> 1;
@@ -280,7 +290,8 @@ cudaError_t launch_fill_mixed(const FillArgs &a, cudaStream_t stream) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   // the coarse index of the T search, staged per block when it fits
   const int nrho = table_nrho(a.eos.table);
-  const size_t coarse = nrho > 1 ? static_cast<size_t>(nrho - 1) * SP_COARSE * sizeof(float2) : 0;
+  const size_t coarse =
+      nrho > 1 ? static_cast<size_t>(nrho - 1) * (SP_COARSE + 1) * sizeof(float2) : 0;
   const int stage = (coarse > 0 && coarse <= 40 * 1024) ? 1 : 0;
   // persistent grid: the blocks resident at once, each staging the index once
   const long long want = (a.n + LOOKUP_BLOCK - 1) / LOOKUP_BLOCK;
