@@ -77,7 +77,7 @@ __device__ __forceinline__ SieRec load_sie(const SieRec *p) {
   return {u.x, u.y, v.x, v.y};
 }
 
-__global__ void __launch_bounds__(LOOKUP_BLOCK, 3) spiner_fill_mixed(const FillArgs a,
+__global__ void __launch_bounds__(LOOKUP_BLOCK, 4) spiner_fill_mixed(const FillArgs a,
                                                                      const int stage_coarse) {
   __shared__ SpinerTable st;
   __shared__ FfConsts sc;
@@ -295,7 +295,7 @@ cudaError_t launch_fill_mixed(const FillArgs &a, cudaStream_t stream) {
   const int stage = (coarse > 0 && coarse <= 40 * 1024) ? 1 : 0;
   // persistent grid: the blocks resident at once, each staging the index once
   const long long want = (a.n + LOOKUP_BLOCK - 1) / LOOKUP_BLOCK;
-  const long long cap = static_cast<long long>(sms) * 3;
+  const long long cap = static_cast<long long>(sms) * 4;
   const int grid = static_cast<int>(want < cap ? want : cap);
   spiner_fill_mixed<<<grid, LOOKUP_BLOCK, stage ? coarse : 0, stream>>>(a, stage);
   return cudaGetLastError();
