@@ -287,6 +287,28 @@ int sgx_pte_solve_noalloc(int solver, int nmat, int64_t ncell, const sgx_eos *eo
                           const sgx_mix_params *params, sgx_pte_status *status,
                           sgx_stream_t stream);
 
+/* get_sg_eos (singularity_eos.hpp:114-132; eos/get_sg_eos.cpp:35-280) in its
+ * (rho, sie) input modes, input_int 0 and 1 (the (rho, T), (rho, P) and
+ * (P, T) modes, -3..-1, return SGX_ERR_UNSUPPORTED). Per cell offsets[k]-1
+ * (1-based, as the Fortran interface passes them), k < ncell: the mass
+ * fractions are normalised, materials above mass_frac_cutoff take part in a
+ * PTESolverRhoT solve (a single one in a T(rho, sie), P(rho, T) lookup), and
+ * press, temp (eV), bmod, cv (per eV), dpde, frac_vol, frac_ie and the
+ * optional frac_bmod / frac_dpde / frac_cv (NULL to skip) are written; pmax
+ * becomes max(pmax, press); sie and spvol are inputs. Unlike the reference
+ * (host arrays, copied to and from the device per call) every array here is a
+ * device array: per-cell [cell_dim], per-material LayoutLeft
+ * [nmat][cell_dim]. eos_offsets (host, [nmat], 1-based) picks each material's
+ * entry of the host list eos. Cells with no material above the cutoff get
+ * zero pressure and temperature. precision: SGX_PREC_FP64 (the reference
+ * iteration) or SGX_PREC_MIXED. */
+int sgx_get_sg_eos(int nmat, int ncell, int cell_dim, int input_int, const int *eos_offsets,
+                   const sgx_eos *eos, int neos, const int *offsets, double *press,
+                   double *pmax, double *vol, double *spvol, double *sie, double *temp,
+                   double *bmod, double *dpde, double *cv, double *frac_mass, double *frac_vol,
+                   double *frac_ie, double *frac_bmod, double *frac_dpde, double *frac_cv,
+                   double mass_frac_cutoff, int precision, sgx_stream_t stream);
+
 /* ---- Serving: a device-resident request loop for PTE closure batches ----
  * No reference counterpart: the reference is a library called once per
  * batch (get_sg_eos, singularity_eos.hpp:114-132). The server keeps the EOS

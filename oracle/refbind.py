@@ -210,6 +210,27 @@ class Oracle:
             raise RuntimeError("helm_T_from_rho_sie failed")
         return T
 
+    def get_sg_eos_rho_e(self, descs, eos_offsets, offsets, cells, fracs, cutoff):
+        """get_sg_eos in (rho, sie) mode over host arrays (reference library
+        only); cells / fracs are updated in place, as the reference does."""
+        nmat, cell_dim = fracs["frac_mass"].shape
+        arr = (EosDesc * len(descs))(*descs)
+        eo = np.ascontiguousarray(eos_offsets, np.int32)
+        off = np.ascontiguousarray(offsets, np.int32)
+        conv = np.zeros(off.size, np.int32)
+        f = self._fn("get_sg_eos_rho_e")
+        f.restype = C.c_int
+        rc = f(C.c_int(nmat), C.c_int(off.size), C.c_int(cell_dim), _ip(eo), arr,
+               C.c_int(len(descs)), _ip(off),
+               *(_dp(cells[k]) for k in ("press", "pmax", "vol", "spvol", "sie", "temp", "bmod",
+                                         "dpde", "cv")),
+               *(_dp(fracs.get(k)) for k in ("frac_mass", "frac_vol", "frac_ie", "frac_bmod",
+                                             "frac_dpde", "frac_cv")),
+               C.c_double(cutoff), _ip(conv))
+        if rc != 0:
+            raise RuntimeError("get_sg_eos_rho_e failed")
+        return conv
+
     def spiner_dump(self, path, matid):
         scal = np.zeros(8)
         n = self._fn("spiner_dump")(path.encode(), C.c_int(matid), None, C.c_long(0),

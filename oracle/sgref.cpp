@@ -518,6 +518,118 @@ int sgref_helm_T_from_rho_sie(const char *path, int n, const double *rho, const 
   return 0;
 }
 
+// get_sg_eos in its (rho, sie) input modes (get_sg_eos.cpp:35-280). The
+// reference compiles get_sg_eos only under Kokkos (get_sg_eos.cpp:75), so
+// this restates its per-cell driver -- init_functor (get_sg_eos_functors.hpp:
+// 28-118), the PTESolverRhoT solve or the pure-cell lookup
+// (get_sg_eos_rho_e.cpp:30-88), final_functor (get_sg_eos_functors.hpp:
+// 185-300) -- around the reference's own solver and EOS calls, serially.
+// Arrays are host, LayoutLeft: per-material (i, m) at i + m * cell_dim.
+int sgref_get_sg_eos_rho_e(int nmat, int ncell, int cell_dim, const int *eos_offsets,
+                           const sgref_eos *descs, int neos, const int *offsets, double *press,
+                           double *pmax, double *vol, double *spvol, double *sie, double *temp,
+                           double *bmod, double *dpde, double *cv, double *frac_mass,
+                           double *frac_vol, double *frac_ie, double *frac_bmod,
+                           double *frac_dpde, double *frac_cv, double mass_frac_cutoff,
+                           int32_t *converged) {
+  try {
+    std::vector<EOS> eos = make_all(descs, neos);
+    constexpr double ev2k = 1.160451930280894026e4;
+    auto FM = [&](int i, int m) -> double & { return frac_mass[i + m * cell_dim]; };
+    std::vector<int> idxs(nmat), mats(nmat);
+    std::vector<double> vfrac_pte(nmat), sie_pte(nmat), temp_pte(nmat), press_pte(nmat),
+        rho_pte(nmat);
+    for (int iloop = 0; iloop < ncell; ++iloop) {
+      const int i = offsets[iloop] - 1;
+      double mass_sum = 0.0, vfrac_sum = 0.0;
+      int npte = 0;
+      // init_functor with t_mult = 0, s_mult = 1, p_mult = 0
+      for (int m = 0; m < nmat; ++m) {
+        mass_sum += FM(i, m);
+        idxs[m] = eos_offsets[m] - 1;
+        frac_vol[i + m * cell_dim] = FM(i, m);
+        frac_ie[i + m * cell_dim] = sie[i] * FM(i, m) * 1.0;
+      }
+      for (int m = 0; m < nmat; ++m)
+        FM(i, m) /= mass_sum;
+      for (int m = 0; m < nmat; ++m) {
+        if (FM(i, m) > mass_frac_cutoff) {
+          idxs[npte] = eos_offsets[m] - 1;
+          mats[npte] = m;
+          npte += 1;
+        }
+        vfrac_pte[m] = 0.0;
+        sie_pte[m] = 0.0;
+        temp_pte[m] = 0.0;
+        press_pte[m] = 0.0;
+      }
+      for (int mp = 0; mp < npte; ++mp) {
+        const int m = mats[mp];
+        vfrac_pte[mp] = FM(i, m);
+        vfrac_sum += vfrac_pte[mp];
+        rho_pte[mp] = FM(i, m) / spvol[i] / vfrac_pte[mp];
+        temp_pte[mp] = temp[i] * ev2k * 0.0;
+        press_pte[mp] = press[i] * 0.0;
+        sie_pte[mp] = sie[i] * FM(i, m) * 1.0;
+      }
+      std::vector<double> scratch(
+          PTESolverRhoTRequiredScratch(nmat) + nmat * MAX_NUM_LAMBDAS + 8, 0.0);
+      const int neq = npte + 1;
+      mix_impl::CacheAccessor cache(scratch.data() + neq * (neq + 4) + 2 * npte);
+      bool pte_converged = true;
+      if (npte > 1) {
+        CellEOS ceos{eos.data(), idxs.data()};
+        double *pr = rho_pte.data(), *pv = vfrac_pte.data(), *ps = sie_pte.data(),
+               *pt = temp_pte.data(), *pp = press_pte.data();
+        PTESolverRhoT<CellEOS, double *, mix_impl::CacheAccessor> method(
+            npte, ceos, vfrac_sum, sie[i], pr, pv, ps, pt, pp, cache, scratch.data());
+        pte_converged = PTESolver(method).converged;
+      } else {
+        const EOS &e0 = eos[idxs[0]];
+        temp_pte[0] = e0.TemperatureFromDensityInternalEnergy(rho_pte[0], sie_pte[0], cache[0]);
+        press_pte[0] = e0.PressureFromDensityTemperature(rho_pte[0], temp_pte[0], cache[0]);
+      }
+      if (converged) converged[iloop] = pte_converged ? 1 : 0;
+      // final_functor with t_mult = 1, s_mult = 0, p_mult = 1
+      temp[i] = 0.0;
+      press[i] = 0.0;
+      bmod[i] = 0.0;
+      cv[i] = 0.0;
+      dpde[i] = 0.0;
+      for (int mp = 0; mp < npte; ++mp) {
+        const int m = mats[mp];
+        press[i] += press_pte[mp] * vfrac_pte[mp] * 1.0;
+        temp[i] += temp_pte[mp] * vfrac_pte[mp] * 1.0;
+        const double ie_m = sie_pte[mp] * FM(i, m) * mass_sum;
+        sie[i] += ie_m * 0.0;
+        frac_ie[i + m * cell_dim] = ie_m;
+        frac_vol[i + m * cell_dim] = vfrac_pte[mp] * vol[i];
+        const EOS &em = eos[idxs[mp]];
+        const double bmod_m =
+            em.BulkModulusFromDensityTemperature(rho_pte[mp], temp_pte[mp], cache[mp]);
+        bmod[i] += bmod_m * vfrac_pte[mp];
+        const double cv_m =
+            ev2k * em.SpecificHeatFromDensityTemperature(rho_pte[mp], temp_pte[mp], cache[mp]);
+        cv[i] += cv_m * FM(i, m);
+        const double dpde_m =
+            em.GruneisenParamFromDensityTemperature(rho_pte[mp], temp_pte[mp], cache[mp]);
+        dpde[i] += dpde_m * vfrac_pte[mp];
+        if (frac_bmod) frac_bmod[i + m * cell_dim] = bmod_m;
+        if (frac_cv) frac_cv[i + m * cell_dim] = cv_m;
+        if (frac_dpde) frac_dpde[i + m * cell_dim] = dpde_m;
+      }
+      temp[i] /= ev2k;
+      for (int m = 0; m < nmat; ++m)
+        FM(i, m) *= mass_sum;
+      pmax[i] = press[i] > pmax[i] ? press[i] : pmax[i];
+    }
+  } catch (const std::exception &ex) {
+    std::fprintf(stderr, "sgref_get_sg_eos_rho_e: %s\n", ex.what());
+    return 1;
+  }
+  return 0;
+}
+
 // FastMath NQT transforms (logs.hpp:188-214, 282-292), element-wise.
 void sgref_nqt(int which, int n, const double *x, double *y) {
   for (int i = 0; i < n; ++i)

@@ -27,6 +27,7 @@ EXPORTED = [
     "sgx_pte_solve", "sgx_pte_solve_noalloc", "sgx_eos_helmholtz", "sgx_eos_helmholtz_dump",
     "sgx_server_create", "sgx_server_submit", "sgx_server_wait", "sgx_server_stats_get",
     "sgx_server_destroy", "sgx_host_alloc", "sgx_host_free", "sgx_eos_fill_host",
+    "sgx_get_sg_eos",
 ]
 HELM_DEFAULT, HELM_REGULA_FALSI, HELM_CACHE_READBACK = 31, 32, 64
 PTE_NOALLOC_MAX_CELLS = 1 << 20  # SGX_PTE_NOALLOC_MAX_CELLS
@@ -123,6 +124,7 @@ def load():
     lib.sgx_eos_helmholtz_dump.restype = C.c_long
     lib.sgx_eos_fill_host.argtypes = [C.POINTER(SgxEos), C.c_int64, P, P, P, P, P, P, P,
                                       C.c_uint32, P, I, I]
+    lib.sgx_get_sg_eos.argtypes = [I, I, I, I, P, P, I, P] + [P] * 15 + [D, I, P]
     lib.sgx_server_create.argtypes = [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]
     lib.sgx_server_submit.argtypes = [C.c_void_p, C.POINTER(PteRequest),
                                       C.POINTER(C.c_uint64)]
@@ -309,6 +311,25 @@ class Server:
 
     def __del__(self):
         self.close()
+
+
+def get_sg_eos(eos_list, eos_offsets, offsets, cells, fracs, mass_frac_cutoff,
+               precision=PREC_FP64, input_int=1, stream=None):
+    """get_sg_eos over device tensors. cells: dict of the nine [cell_dim]
+    arrays (press, pmax, vol, spvol, sie, temp, bmod, dpde, cv); fracs: dict
+    of [nmat, cell_dim] arrays (frac_mass, frac_vol, frac_ie and optionally
+    frac_bmod, frac_dpde, frac_cv); eos_offsets: 1-based host ints."""
+    nmat, cell_dim = fracs["frac_mass"].shape
+    arr = (SgxEos * len(eos_list))(*eos_list)
+    eo = (C.c_int * nmat)(*[int(x) for x in eos_offsets])
+    check(load().sgx_get_sg_eos(
+        nmat, offsets.numel(), cell_dim, input_int, C.cast(eo, C.c_void_p),
+        C.cast(arr, C.c_void_p), len(eos_list), ptr(offsets),
+        *(ptr(cells[k]) for k in ("press", "pmax", "vol", "spvol", "sie", "temp", "bmod",
+                                  "dpde", "cv")),
+        *(ptr(fracs.get(k)) for k in ("frac_mass", "frac_vol", "frac_ie", "frac_bmod",
+                                      "frac_dpde", "frac_cv")),
+        mass_frac_cutoff, precision, stream_ptr(stream)))
 
 
 def status_view(status_u8):

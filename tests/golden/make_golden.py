@@ -141,6 +141,47 @@ def helm_fixture(ref, path, n=2048, seed=31):
     return out
 
 
+SGEOS_CELLS = ("press", "pmax", "vol", "spvol", "sie", "temp", "bmod", "dpde", "cv")
+SGEOS_FRACS = ("frac_mass", "frac_vol", "frac_ie", "frac_bmod", "frac_dpde", "frac_cv")
+
+
+def sgeos_fixture(ref, cell_dim=700, ncell=512, seed=41, cutoff=1e-8):
+    """get_sg_eos (rho, sie) on four materials (IdealGas, StiffGas, NobleAbel,
+    copper Gruneisen): mass fractions with some materials absent or below
+    the cutoff, pure cells among them, cells addressed through a 1-based
+    offset list."""
+    rng = np.random.default_rng(seed)
+    mats = [W.IDEAL_AIR, W.STIFF_WATER, W.NOBLE_ABEL_GAS, W.GRUNEISEN_CU]
+    nmat = len(mats)
+    fm = rng.exponential(1.0, (nmat, cell_dim))
+    kind = rng.random(cell_dim)
+    fm[:, kind < 0.2] *= (rng.random((nmat, (kind < 0.2).sum())) < 0.3)  # some absent
+    pure = kind > 0.9
+    fm[:, pure] = 0.0
+    fm[rng.integers(0, nmat, pure.sum()), np.flatnonzero(pure)] = 1.0
+    tiny = rng.random((nmat, cell_dim)) < 0.05
+    fm[tiny] = 1e-12  # below the cutoff
+    fm[0, fm.sum(axis=0) == 0] = 1.0
+    fm *= rng.uniform(0.5, 2.0, cell_dim)  # not normalised
+    rho = np.exp(rng.uniform(np.log(1e-3), np.log(10.0), cell_dim))
+    cells = dict(press=rng.uniform(0, 1e10, cell_dim), pmax=rng.uniform(0, 1e12, cell_dim),
+                 vol=rng.uniform(0.5, 2.0, cell_dim), spvol=1.0 / rho,
+                 sie=rng.uniform(1e9, 1e11, cell_dim), temp=rng.uniform(0, 1e3, cell_dim),
+                 bmod=np.zeros(cell_dim), dpde=np.zeros(cell_dim), cv=np.zeros(cell_dim))
+    fracs = dict(frac_mass=np.ascontiguousarray(fm), frac_vol=np.zeros((nmat, cell_dim)),
+                 frac_ie=np.zeros((nmat, cell_dim)), frac_bmod=np.zeros((nmat, cell_dim)),
+                 frac_dpde=np.zeros((nmat, cell_dim)), frac_cv=np.zeros((nmat, cell_dim)))
+    offsets = (rng.permutation(cell_dim)[:ncell] + 1).astype(np.int32)
+    eos_offsets = np.array([1, 2, 3, 4], np.int32)
+    out = {"in_" + k: v.copy() for k, v in {**cells, **fracs}.items()}
+    conv = ref.get_sg_eos_rho_e([desc(m) for m in mats], eos_offsets, offsets, cells, fracs,
+                                cutoff)
+    out.update({"out_" + k: v for k, v in {**cells, **fracs}.items()})
+    out.update(materials=mats_array(mats), offsets=offsets, eos_offsets=eos_offsets,
+               cutoff=np.float64(cutoff), converged=conv)
+    return out
+
+
 def main():
     if not rb.have_reference():
         sys.exit("oracle/_ref/libsgref.so not built; run oracle/build_ref.sh")
@@ -180,6 +221,7 @@ def main():
             o["in_" + k] = wl[k]
             o["out_" + k] = r[k]
         fx["pte_rhot_spiner"] = o
+    fx["get_sg_eos"] = sgeos_fixture(ref)
     with tempfile.TemporaryDirectory() as td:
         from sgx import helmtable
         path = os.path.join(td, "helm_table.dat")
