@@ -131,13 +131,8 @@ def barrier(world):
 
 
 def max_over_ranks(x, world):
-    if world == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from sgx.shard import max_over_ranks as reduce_max
+    return reduce_max(x, world, device="cuda")
 
 
 def time_steps(fn, steps, warmup, stream):
