@@ -43,6 +43,7 @@ N_PTE2 = 65536
 N_PTE_BATCH = 1 << 22
 N_HELM = 1 << 22
 LOOKUP_BYTES_PER_QUERY = 16 + 32  # rho, sie in; T, P, bmod, cs out (float64)
+LOOKUP_TRAFFIC_2_24 = (283.95 + 486.50) * 1e6  # measured DRAM bytes per 2^24-query launch
 Q_OUT = 8 | 4 | 32                # temperature | pressure | bulk modulus
 METRIC = "PTE mixed cells/s & EOS lookups/s, 1 GB300, batched+FP32-refined vs plain FP64"
 
@@ -81,7 +82,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -191,14 +192,18 @@ def bench_lookup(args, world, local, stream, out):
                                  clocks=clk.summary(), steps=steps)
         m = results["mixed"]
         out["clocks"] = m["clocks"]
+        # DRAM bytes of one 2^24-query launch, dram__bytes_read.sum +
+        # dram__bytes_write.sum from one ncu capture (profiles/
+        # spiner_fill_mixed_lookup.md), scaled to this launch's queries
+        traffic = LOOKUP_TRAFFIC_2_24 * n / float(1 << 24)
         out["roofline"] = {"bound": "hbm", "achieved": m["gbs"], "peak": hbm, "unit": "GB/s",
-                           "frac": m["gbs"] / hbm, "traffic": None,
+                           "frac": m["gbs"] / hbm, "traffic": traffic,
                            "peak_kind": hbm_kind + " (burst copy)",
                            "kernel": "spiner_fill_mixed (sgx_lookup_mixed.cu)",
                            "bytes_per_query": LOOKUP_BYTES_PER_QUERY,
                            # the kernel is bound by the FP64 pipe, not HBM (ncu capture
                            # in profiles/spiner_fill_mixed_lookup_4M.md)
-                           "fp64_pipe_pct_active_ncu": 83.7}
+                           "fp64_pipe_pct_active_ncu": 43.8}
         f = results["fp64"]
         out["plain_fp64"] = {"value": f["value"], "unit": "lookups/s", "ms_per_step": f["ms"],
                              "hbm_frac": f["gbs"] / hbm, "clocks": f["clocks"],
