@@ -142,7 +142,20 @@ typedef struct sgx_pte_status {
   uint8_t small_step_iters;
 } sgx_pte_status;
 
-enum { SGX_PTE_RHOT = 0, SGX_PTE_PT = 1 };
+/* PTE solvers (closure/mixed_cell_models.hpp):
+ *  SGX_PTE_RHOT     PTESolverRhoT   :884-1193, unknowns T and n-1 volume fractions
+ *  SGX_PTE_PT       PTESolverPT     :1207-1446, unknowns T and P
+ *  SGX_PTE_RHOU     PTESolverRhoU   :1934-2183, unknowns n volume fractions and
+ *                                   n energy densities
+ *  SGX_PTE_FIXED_T  PTESolverFixedT :1462-1660, volume fractions at a given T
+ *  SGX_PTE_FIXED_P  PTESolverFixedP :1676-1919, volume fractions and T at a given P */
+enum {
+  SGX_PTE_RHOT = 0,
+  SGX_PTE_PT = 1,
+  SGX_PTE_RHOU = 2,
+  SGX_PTE_FIXED_T = 3,
+  SGX_PTE_FIXED_P = 4
+};
 
 /* Precision of the PTE / lookup arithmetic.
  * SGX_PREC_FP64: the plain path; follows the reference's iteration exactly.
@@ -238,17 +251,29 @@ int sgx_eos_fill_host(const sgx_eos *eos, int64_t n, double *rho, double *temp, 
 
 /* ---- PTE ---- */
 int sgx_mix_params_default(sgx_mix_params *p);
+/* Scratch doubles the reference's solver of that kind takes per cell
+ * (PTESolverRhoTRequiredScratch :873-881, PTESolverPTRequiredScratch
+ * :1198-1206, PTESolverFixedTRequiredScratch :1451-1457,
+ * PTESolverFixedPRequiredScratch :1665-1671, PTESolverRhoURequiredScratch
+ * :1924-1929). The GPU solvers keep this state in registers. */
 int sgx_pte_rhot_required_scratch(int nmat);
 int sgx_pte_pt_required_scratch(int nmat);
+int sgx_pte_fixed_t_required_scratch(int nmat);
+int sgx_pte_fixed_p_required_scratch(int nmat);
+int sgx_pte_rhou_required_scratch(int nmat);
 
 /* Solves PTE in every cell.
- *  solver     SGX_PTE_RHOT or SGX_PTE_PT
+ *  solver     SGX_PTE_RHOT, SGX_PTE_PT, SGX_PTE_RHOU, SGX_PTE_FIXED_T or
+ *             SGX_PTE_FIXED_P (the last three with SGX_PREC_FP64 only)
  *  nmat       material slots per cell (1..6, the Jacobian is at most 6x6);
  *             [nmat][ncell], cell index fastest
  *  eos_list   host array of neos EOS values (neos <= 16)
  *  eos_idx    device [nmat][ncell] index into eos_list, -1 = material absent;
  *             NULL = material m uses eos_list[m] in every cell
- *  vfrac_tot, sie_tot   device [ncell]
+ *  vfrac_tot, sie_tot   device [ncell]; sie_tot carries the solver's scalar
+ *             constructor argument: the cell's specific internal energy for
+ *             RHOT, PT and RHOU, the temperature T_true for FIXED_T, the
+ *             pressure P for FIXED_P
  *  rho, vfrac, sie, temp, press   device [nmat][ncell], in/out (the reference's
  *             initial guesses in, equilibrium state out)
  *  lambda     device [nmat][3][ncell] per-material cache, or NULL
@@ -260,6 +285,39 @@ int sgx_pte_solve(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list, 
                   double *rho, double *vfrac, double *sie, double *temp, double *press,
                   double *lambda, const sgx_mix_params *params, sgx_pte_status *status,
                   int precision, sgx_stream_t stream);
+
+/* ApproxTemperatureFromRhoMatU (closure/mixed_cell_models.hpp:790-847) per
+ * cell: the temperature at which the materials' energy densities
+ * rho_m vfrac_m e_m(rho_m, T) add up to u_tot, by bisection in NQT log2 T
+ * (at most 10 steps, then one linear interpolation), clamped to
+ * [1e-9, 1e9] K. A rough initial guess, as the reference intends.
+ *  eos_list, neos, eos_idx   as for sgx_pte_solve
+ *  u_tot      device [ncell], total internal energy density (rho * sie)
+ *  rho, vfrac device [nmat][ncell] (read only)
+ *  Tguess     device [ncell] or NULL (no guess)
+ *  lambda     device [nmat][3][ncell] or NULL
+ *  temp_out   device [ncell] */
+int sgx_pte_approx_temperature(int nmat, int64_t ncell, const sgx_eos *eos_list, int neos,
+                               const int32_t *eos_idx, const double *u_tot, const double *rho,
+                               const double *vfrac, const double *Tguess, double *lambda,
+                               double *temp_out, sgx_stream_t stream);
+
+/* MixUtils::EnforceMassVolumesSum (mixed_cell_models.hpp:93-117) per cell:
+ * the present material with the largest volume fraction takes
+ * tot_vol - sum(others), its density rescaled so its mass is kept.
+ * eos_idx (device [nmat][ncell], -1 = absent) or NULL = all slots present;
+ * tot_vol device [ncell]; rho, vfrac device [nmat][ncell], in/out. */
+int sgx_mix_enforce_mass_volumes_sum(int nmat, int64_t ncell, const int32_t *eos_idx,
+                                     const double *tot_vol, double *rho, double *vfrac,
+                                     sgx_stream_t stream);
+
+/* MixUtils::EnforceEnergiesSum (mixed_cell_models.hpp:119-150) per cell: the
+ * present material with the largest |rho vfrac sie| takes the energy that
+ * makes sum(rho_m vfrac_m sie_m) = tot_rho * tot_sie. tot_rho, tot_sie
+ * device [ncell]; rho, vfrac device [nmat][ncell]; sie in/out. */
+int sgx_mix_enforce_energies_sum(int nmat, int64_t ncell, const int32_t *eos_idx,
+                                 const double *tot_rho, const double *tot_sie, const double *rho,
+                                 const double *vfrac, double *sie, sgx_stream_t stream);
 
 /* Largest ncell sgx_pte_solve_noalloc accepts. */
 #define SGX_PTE_NOALLOC_MAX_CELLS 1048576

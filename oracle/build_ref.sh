@@ -11,7 +11,7 @@ if [ ! -d "$ref/singularity-eos" ]; then
   exit 0
 fi
 mkdir -p "$here/_ref"
-g++ -std=c++17 -O2 -fPIC -shared -fopenmp -ffp-contract=off -DNDEBUG \
+g++ -std=c++17 -O2 -fPIC -shared -fopenmp -ffp-contract=off -fno-lifetime-dse -DNDEBUG \
   -DSINGULARITY_USE_SPINER -DSINGULARITY_USE_SPINER_WITH_HDF5 \
   -DSINGULARITY_USE_HELMHOLTZ -DSINGULARITY_BUILD_CLOSURE \
   -I "$here/shims" -I "$ref" \

@@ -132,7 +132,10 @@ class Oracle:
 
     def pte(self, solver, descs, eos_idx, vfrac_tot, sie_tot, rho, vfrac, sie, temp,
             press, params=None, lam=None, nthreads=1):
-        """Runs PTESolverRhoT (solver=0) or PTESolverPT (solver=1) per cell.
+        """Runs PTESolverRhoT (solver=0), PTESolverPT (1), PTESolverRhoU (2),
+        PTESolverFixedT (3) or PTESolverFixedP (4) per cell; sie_tot carries
+        each cell's scalar constructor argument (T_true for FixedT, P for
+        FixedP).
         Per-material arrays are [nmat_max, ncell] float64 and are updated in
         place. Returns (converged, niter, residual)."""
         nmat, ncell = rho.shape
@@ -210,26 +213,54 @@ class Oracle:
             raise RuntimeError("helm_T_from_rho_sie failed")
         return T
 
-    def get_sg_eos_rho_e(self, descs, eos_offsets, offsets, cells, fracs, cutoff):
-        """get_sg_eos in (rho, sie) mode over host arrays (reference library
-        only); cells / fracs are updated in place, as the reference does."""
+    def get_sg_eos(self, input_int, descs, eos_offsets, offsets, cells, fracs, cutoff):
+        """get_sg_eos over host arrays (reference library only) in any input
+        mode (1/0 rho-sie, -1 P-T, -2 rho-P, -3 rho-T); cells / fracs are
+        updated in place, as the reference does. Returns the per-cell
+        converged flags."""
         nmat, cell_dim = fracs["frac_mass"].shape
         arr = (EosDesc * len(descs))(*descs)
         eo = np.ascontiguousarray(eos_offsets, np.int32)
         off = np.ascontiguousarray(offsets, np.int32)
         conv = np.zeros(off.size, np.int32)
-        f = self._fn("get_sg_eos_rho_e")
+        f = self._fn("get_sg_eos")
         f.restype = C.c_int
-        rc = f(C.c_int(nmat), C.c_int(off.size), C.c_int(cell_dim), _ip(eo), arr,
-               C.c_int(len(descs)), _ip(off),
+        rc = f(C.c_int(nmat), C.c_int(off.size), C.c_int(cell_dim), C.c_int(input_int), _ip(eo),
+               arr, C.c_int(len(descs)), _ip(off),
                *(_dp(cells[k]) for k in ("press", "pmax", "vol", "spvol", "sie", "temp", "bmod",
                                          "dpde", "cv")),
                *(_dp(fracs.get(k)) for k in ("frac_mass", "frac_vol", "frac_ie", "frac_bmod",
                                              "frac_dpde", "frac_cv")),
                C.c_double(cutoff), _ip(conv))
         if rc != 0:
-            raise RuntimeError("get_sg_eos_rho_e failed")
+            raise RuntimeError("get_sg_eos failed")
         return conv
+
+    def get_sg_eos_rho_e(self, descs, eos_offsets, offsets, cells, fracs, cutoff):
+        """get_sg_eos in (rho, sie) mode."""
+        return self.get_sg_eos(1, descs, eos_offsets, offsets, cells, fracs, cutoff)
+
+    def approx_temperature(self, descs, eos_idx, u_tot, rho, vfrac, Tguess=None, lam=None):
+        """ApproxTemperatureFromRhoMatU per cell (reference library only)."""
+        nmat, ncell = rho.shape
+        arr = (EosDesc * len(descs))(*descs)
+        out = np.zeros(ncell)
+        f = self._fn("approx_temperature")
+        f.restype = C.c_int
+        rc = f(C.c_int(nmat), C.c_int(ncell), arr, C.c_int(len(descs)), _ip(eos_idx),
+               _dp(u_tot), _dp(rho), _dp(vfrac), _dp(Tguess), _dp(lam), _dp(out))
+        if rc != 0:
+            raise RuntimeError("approx_temperature failed")
+        return out
+
+    def enforce_sums(self, which, eos_idx, tot, rho, vfrac, tot_rho=None, sie=None):
+        """MixUtils::EnforceMassVolumesSum (which=0) / EnforceEnergiesSum
+        (which=1) per cell, in place (reference library only)."""
+        nmat, ncell = rho.shape
+        f = self._fn("enforce_sums")
+        f.restype = C.c_int
+        f(C.c_int(which), C.c_int(nmat), C.c_int(ncell), _ip(eos_idx), _dp(tot), _dp(tot_rho),
+          _dp(rho), _dp(vfrac), _dp(sie))
 
     def spiner_dump(self, path, matid):
         scal = np.zeros(8)

@@ -8,15 +8,19 @@
 // reference sources are present (oracle/build_ref.sh).
 //
 // Each entry point calls the reference's own API the way its callers do:
-//   - PTE: PTESolverRhoT / PTESolverPT + PTESolver(), as
-//     get_sg_eos_rho_e.cpp:30-88 and test_pte.cpp:200-245 drive them;
+//   - PTE: PTESolverRhoT / PTESolverPT / PTESolverRhoU / PTESolverFixedT /
+//     PTESolverFixedP + PTESolver(), as get_sg_eos_rho_e.cpp:30-88,
+//     get_sg_eos_rho_t.cpp, get_sg_eos_rho_p.cpp and test_pte.cpp:200-245
+//     drive them;
 //   - vector lookups: the Variant vector overloads (eos_base.hpp:169-230,
 //     eos_variant.hpp:56-143) with a 2-D lambda indexer shaped like
 //     lambdaIndexer2D (singularity_eos.cpp:39-49);
 //   - FillEos vector (eos_base.hpp:503-531).
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <memory>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -150,6 +154,29 @@ std::vector<EOS> make_all(const sgref_eos *descs, int neos) {
   return v;
 }
 
+// Builds a solver in zero-filled storage. PTESolverFixedP reads its
+// uscale and utotal_scale members in GetTguess before it sets them
+// (mixed_cell_models.hpp:522-535 via :1754); zeroed storage (with
+// -fno-lifetime-dse, so the fill is kept) makes that read well defined.
+template <class M> struct Zeroed {
+  alignas(M) unsigned char buf[sizeof(M)];
+  M *m = nullptr;
+  template <class... A> explicit Zeroed(A &&...a) {
+    std::memset(buf, 0, sizeof(buf));
+    m = new (buf) M(std::forward<A>(a)...);
+  }
+  ~Zeroed() { m->~M(); }
+};
+
+// The solvers' constructors differ in their scalar arguments: RhoT, PT and
+// RhoU take (sie_tot, ..., Tnorm, params), FixedT (T_true, ..., params) and
+// FixedP (P, ..., params). `target` is that scalar.
+template <template <class, class, class> class Solver> constexpr bool takes_tnorm() {
+  return true;
+}
+template <> constexpr bool takes_tnorm<PTESolverFixedT>() { return false; }
+template <> constexpr bool takes_tnorm<PTESolverFixedP>() { return false; }
+
 template <template <class, class, class> class Solver>
 void pte_run(int nmat_max, int ncell, const sgref_eos *descs, int neos,
              const int32_t *eos_idx, const double *vfrac_tot, const double *sie_tot,
@@ -195,9 +222,16 @@ void pte_run(int nmat_max, int ncell, const sgref_eos *descs, int neos,
                                   8);
       mix_impl::CacheAccessor cacc(cache);
       double *pr = r, *pv = v, *pe = e, *pt = t, *pp = p;
-      Solver<CellEOS, double *, mix_impl::CacheAccessor> method(
-          n, ceos, vfrac_tot[i], sie_tot[i], pr, pv, pe, pt, pp, cacc, scratch.data(), 0.0,
-          mp);
+      using M = Solver<CellEOS, double *, mix_impl::CacheAccessor>;
+      double *ps = scratch.data();
+      std::unique_ptr<Zeroed<M>> z;
+      if constexpr (takes_tnorm<Solver>())
+        z.reset(new Zeroed<M>(n, ceos, vfrac_tot[i], sie_tot[i], pr, pv, pe, pt, pp, cacc, ps,
+                              0.0, mp));
+      else
+        z.reset(
+            new Zeroed<M>(n, ceos, vfrac_tot[i], sie_tot[i], pr, pv, pe, pt, pp, cacc, ps, mp));
+      M &method = *z->m;
       SolverStatus st = PTESolver(method);
       int q = 0;
       for (int m = 0; m < nmat_max; ++m) {
@@ -258,23 +292,30 @@ void sgref_mix_params_default(sgref_mix_params *q) {
   q->pte_reduced_system_exclude_idx = m.pte_reduced_system_exclude_idx;
 }
 
-// solver: 0 = PTESolverRhoT, 1 = PTESolverPT. Arrays are [nmat_max][ncell]
-// (cell index fastest, the LayoutLeft of get_sg_eos.hpp:30-31); eos_idx of -1
-// marks an absent material. lambda (nullable) is [nmat_max][3][ncell].
+// solver: 0 = PTESolverRhoT, 1 = PTESolverPT, 2 = PTESolverRhoU,
+// 3 = PTESolverFixedT, 4 = PTESolverFixedP; sie_tot holds each cell's scalar
+// constructor argument (sie_tot, or T_true for FixedT, P for FixedP).
+// Arrays are [nmat_max][ncell] (cell index fastest, the LayoutLeft of
+// get_sg_eos.hpp:30-31); eos_idx of -1 marks an absent material. lambda
+// (nullable) is [nmat_max][3][ncell].
 int sgref_pte(int solver, int nmat_max, int ncell, const sgref_eos *descs, int neos,
               const int32_t *eos_idx, const double *vfrac_tot, const double *sie_tot,
               double *rho, double *vfrac, double *sie, double *temp, double *press,
               double *lambda, const sgref_mix_params *params, int32_t *converged,
               int32_t *niter, double *residual, int nthreads) {
   try {
-    if (solver == 0)
-      pte_run<PTESolverRhoT>(nmat_max, ncell, descs, neos, eos_idx, vfrac_tot, sie_tot,
-                             rho, vfrac, sie, temp, press, lambda, params, converged,
-                             niter, residual, nthreads);
-    else
-      pte_run<PTESolverPT>(nmat_max, ncell, descs, neos, eos_idx, vfrac_tot, sie_tot, rho,
-                           vfrac, sie, temp, press, lambda, params, converged, niter,
-                           residual, nthreads);
+#define SGREF_PTE_RUN(S)                                                                   \
+  pte_run<S>(nmat_max, ncell, descs, neos, eos_idx, vfrac_tot, sie_tot, rho, vfrac, sie,    \
+             temp, press, lambda, params, converged, niter, residual, nthreads)
+    switch (solver) {
+    case 0: SGREF_PTE_RUN(PTESolverRhoT); break;
+    case 1: SGREF_PTE_RUN(PTESolverPT); break;
+    case 2: SGREF_PTE_RUN(PTESolverRhoU); break;
+    case 3: SGREF_PTE_RUN(PTESolverFixedT); break;
+    case 4: SGREF_PTE_RUN(PTESolverFixedP); break;
+    default: return 1;
+    }
+#undef SGREF_PTE_RUN
   } catch (const std::exception &ex) {
     std::fprintf(stderr, "sgref_pte: %s\n", ex.what());
     return 1;
@@ -518,20 +559,25 @@ int sgref_helm_T_from_rho_sie(const char *path, int n, const double *rho, const 
   return 0;
 }
 
-// get_sg_eos in its (rho, sie) input modes (get_sg_eos.cpp:35-280). The
-// reference compiles get_sg_eos only under Kokkos (get_sg_eos.cpp:75), so
-// this restates its per-cell driver -- init_functor (get_sg_eos_functors.hpp:
-// 28-118), the PTESolverRhoT solve or the pure-cell lookup
-// (get_sg_eos_rho_e.cpp:30-88), final_functor (get_sg_eos_functors.hpp:
-// 185-300) -- around the reference's own solver and EOS calls, serially.
-// Arrays are host, LayoutLeft: per-material (i, m) at i + m * cell_dim.
-int sgref_get_sg_eos_rho_e(int nmat, int ncell, int cell_dim, const int *eos_offsets,
-                           const sgref_eos *descs, int neos, const int *offsets, double *press,
-                           double *pmax, double *vol, double *spvol, double *sie, double *temp,
-                           double *bmod, double *dpde, double *cv, double *frac_mass,
-                           double *frac_vol, double *frac_ie, double *frac_bmod,
-                           double *frac_dpde, double *frac_cv, double mass_frac_cutoff,
-                           int32_t *converged) {
+// get_sg_eos (get_sg_eos.cpp:35-280) in all its input modes. The reference
+// compiles get_sg_eos only under Kokkos (get_sg_eos.cpp:75), so this
+// restates its per-cell drivers around the reference's own solver, root
+// finder and EOS calls, serially:
+//   input_int 0, 1  (rho, sie)  get_sg_eos_rho_e.cpp:30-88, PTESolverRhoT
+//   input_int -3    (rho, T)    get_sg_eos_rho_t.cpp:21-110, PTESolverFixedT
+//   input_int -2    (rho, P)    get_sg_eos_rho_p.cpp:21-118, PTESolverFixedP
+//   input_int -1    (P, T)      get_sg_eos_p_t.cpp:23-102, no solve
+// with init_functor (get_sg_eos_functors.hpp:28-118) and final_functor
+// (:185-300). The lambda cache sits inside the solver scratch at the
+// reference's offsets. Arrays are host, LayoutLeft: per-material (i, m) at
+// i + m * cell_dim.
+int sgref_get_sg_eos(int nmat, int ncell, int cell_dim, int input_int, const int *eos_offsets,
+                     const sgref_eos *descs, int neos, const int *offsets, double *press,
+                     double *pmax, double *vol, double *spvol, double *sie, double *temp,
+                     double *bmod, double *dpde, double *cv, double *frac_mass,
+                     double *frac_vol, double *frac_ie, double *frac_bmod, double *frac_dpde,
+                     double *frac_cv, double mass_frac_cutoff, int32_t *converged) {
+  if (input_int < -3 || input_int > 1) return 1;
   try {
     std::vector<EOS> eos = make_all(descs, neos);
     constexpr double ev2k = 1.160451930280894026e4;
@@ -539,93 +585,285 @@ int sgref_get_sg_eos_rho_e(int nmat, int ncell, int cell_dim, const int *eos_off
     std::vector<int> idxs(nmat), mats(nmat);
     std::vector<double> vfrac_pte(nmat), sie_pte(nmat), temp_pte(nmat), press_pte(nmat),
         rho_pte(nmat);
+    // scratch per cell: the largest solver's need plus the lambda cache
+    const std::size_t nscr =
+        std::max({static_cast<std::size_t>(PTESolverRhoTRequiredScratch(nmat)),
+                  static_cast<std::size_t>(PTESolverFixedTRequiredScratch(nmat)),
+                  static_cast<std::size_t>(PTESolverFixedPRequiredScratch(nmat))}) +
+        nmat * MAX_NUM_LAMBDAS + 8;
     for (int iloop = 0; iloop < ncell; ++iloop) {
       const int i = offsets[iloop] - 1;
       double mass_sum = 0.0, vfrac_sum = 0.0;
       int npte = 0;
-      // init_functor with t_mult = 0, s_mult = 1, p_mult = 0
-      for (int m = 0; m < nmat; ++m) {
-        mass_sum += FM(i, m);
-        idxs[m] = eos_offsets[m] - 1;
-        frac_vol[i + m * cell_dim] = FM(i, m);
-        frac_ie[i + m * cell_dim] = sie[i] * FM(i, m) * 1.0;
-      }
-      for (int m = 0; m < nmat; ++m)
-        FM(i, m) /= mass_sum;
-      for (int m = 0; m < nmat; ++m) {
-        if (FM(i, m) > mass_frac_cutoff) {
-          idxs[npte] = eos_offsets[m] - 1;
-          mats[npte] = m;
-          npte += 1;
-        }
-        vfrac_pte[m] = 0.0;
-        sie_pte[m] = 0.0;
-        temp_pte[m] = 0.0;
-        press_pte[m] = 0.0;
-      }
-      for (int mp = 0; mp < npte; ++mp) {
-        const int m = mats[mp];
-        vfrac_pte[mp] = FM(i, m);
-        vfrac_sum += vfrac_pte[mp];
-        rho_pte[mp] = FM(i, m) / spvol[i] / vfrac_pte[mp];
-        temp_pte[mp] = temp[i] * ev2k * 0.0;
-        press_pte[mp] = press[i] * 0.0;
-        sie_pte[mp] = sie[i] * FM(i, m) * 1.0;
-      }
-      std::vector<double> scratch(
-          PTESolverRhoTRequiredScratch(nmat) + nmat * MAX_NUM_LAMBDAS + 8, 0.0);
-      const int neq = npte + 1;
-      mix_impl::CacheAccessor cache(scratch.data() + neq * (neq + 4) + 2 * npte);
+      std::vector<double> scratch(nscr, 0.0);
       bool pte_converged = true;
-      if (npte > 1) {
+      double t_mult = 0.0, s_mult = 0.0, p_mult = 0.0; // final_functor's
+      if (input_int == -1) {
+        // (P, T): every material at the cell's P and T (get_sg_eos_p_t.cpp:40-86)
+        mix_impl::CacheAccessor cache(scratch.data());
+        for (int m = 0; m < nmat; ++m) {
+          mass_sum += FM(i, m);
+          idxs[m] = eos_offsets[m] - 1;
+          mats[m] = m;
+          temp_pte[m] = temp[i] * ev2k;
+          press_pte[m] = press[i];
+        }
+        for (int m = 0; m < nmat; ++m)
+          FM(i, m) /= mass_sum;
+        double vfrac_tot = 0.0, sie_tot = 0.0;
+        for (int m = 0; m < nmat; ++m) {
+          eos[idxs[m]].DensityEnergyFromPressureTemperature(press_pte[m], temp_pte[m], cache[m],
+                                                            rho_pte[m], sie_pte[m]);
+          vfrac_pte[m] = FM(i, m) / rho_pte[m] * mass_sum;
+          vfrac_tot += vfrac_pte[m];
+          sie_tot += sie_pte[m] * FM(i, m);
+        }
+        sie[i] = sie_tot;
+        vol[i] = vfrac_tot;
+        spvol[i] = vol[i] / mass_sum;
+        for (int m = 0; m < nmat; ++m)
+          vfrac_pte[m] /= vfrac_tot;
+        npte = nmat;
+        if (converged) converged[iloop] = 1;
+        // final_functor below with t_mult = s_mult = p_mult = 0
+      }
+      {
+        // init_functor (get_sg_eos_functors.hpp:60-118)
+        double it = 0.0, is = 0.0, ip = 0.0;
+        if (input_int >= 0) is = 1.0;      // (rho, sie): t 0, s 1, p 0
+        else if (input_int == -3) it = 1.0; // (rho, T):   t 1, s 0, p 0
+        else if (input_int == -2) ip = 1.0; // (rho, P):   t 0, s 0, p 1
+        if (input_int != -1) {
+          for (int m = 0; m < nmat; ++m) {
+            mass_sum += FM(i, m);
+            idxs[m] = eos_offsets[m] - 1;
+            frac_vol[i + m * cell_dim] = FM(i, m);
+            frac_ie[i + m * cell_dim] = sie[i] * FM(i, m) * is;
+          }
+          for (int m = 0; m < nmat; ++m)
+            FM(i, m) /= mass_sum;
+          for (int m = 0; m < nmat; ++m) {
+            if (FM(i, m) > mass_frac_cutoff) {
+              idxs[npte] = eos_offsets[m] - 1;
+              mats[npte] = m;
+              npte += 1;
+            }
+            vfrac_pte[m] = 0.0;
+            sie_pte[m] = 0.0;
+            temp_pte[m] = 0.0;
+            press_pte[m] = 0.0;
+          }
+          for (int mp = 0; mp < npte; ++mp) {
+            const int m = mats[mp];
+            vfrac_pte[mp] = FM(i, m);
+            vfrac_sum += vfrac_pte[mp];
+            rho_pte[mp] = FM(i, m) / spvol[i] / vfrac_pte[mp];
+            temp_pte[mp] = temp[i] * ev2k * it;
+            press_pte[mp] = press[i] * ip;
+            sie_pte[mp] = sie[i] * FM(i, m) * is;
+          }
+        }
+      }
+      {
+        // the solve (or pure-cell lookups) of each mode
+        int neq = 0;
+        if (input_int >= 0) neq = npte + 1;       // get_sg_eos_rho_e.cpp:50
+        else if (input_int == -3) neq = npte;     // get_sg_eos_rho_t.cpp:53
+        else if (input_int == -2) neq = npte + 1; // get_sg_eos_rho_p.cpp:50
+        mix_impl::CacheAccessor cache(input_int == -1
+                                          ? scratch.data()
+                                          : scratch.data() + neq * (neq + 4) + 2 * npte);
         CellEOS ceos{eos.data(), idxs.data()};
         double *pr = rho_pte.data(), *pv = vfrac_pte.data(), *ps = sie_pte.data(),
                *pt = temp_pte.data(), *pp = press_pte.data();
-        PTESolverRhoT<CellEOS, double *, mix_impl::CacheAccessor> method(
-            npte, ceos, vfrac_sum, sie[i], pr, pv, ps, pt, pp, cache, scratch.data());
-        pte_converged = PTESolver(method).converged;
-      } else {
-        const EOS &e0 = eos[idxs[0]];
-        temp_pte[0] = e0.TemperatureFromDensityInternalEnergy(rho_pte[0], sie_pte[0], cache[0]);
-        press_pte[0] = e0.PressureFromDensityTemperature(rho_pte[0], temp_pte[0], cache[0]);
+        if (input_int >= 0) {
+          if (npte > 1) {
+            PTESolverRhoT<CellEOS, double *, mix_impl::CacheAccessor> method(
+                npte, ceos, vfrac_sum, sie[i], pr, pv, ps, pt, pp, cache, scratch.data());
+            pte_converged = PTESolver(method).converged;
+          } else {
+            const EOS &e0 = eos[idxs[0]];
+            temp_pte[0] =
+                e0.TemperatureFromDensityInternalEnergy(rho_pte[0], sie_pte[0], cache[0]);
+            press_pte[0] = e0.PressureFromDensityTemperature(rho_pte[0], temp_pte[0], cache[0]);
+          }
+          t_mult = 1.0, s_mult = 0.0, p_mult = 1.0;
+        } else if (input_int == -3) {
+          double sie_tot_true = 0.0;
+          if (npte > 1) {
+            Zeroed<PTESolverFixedT<CellEOS, double *, mix_impl::CacheAccessor>> z(
+                npte, ceos, vfrac_sum, temp_pte[0], pr, pv, ps, pt, pp, cache, scratch.data());
+            pte_converged = PTESolver(*z.m).converged;
+            for (int mp = 0; mp < npte; ++mp)
+              sie_tot_true += sie_pte[mp] * FM(i, mats[mp]);
+          } else {
+            const EOS &e0 = eos[idxs[0]];
+            sie_pte[0] = e0.InternalEnergyFromDensityTemperature(rho_pte[0], temp_pte[0], cache[0]);
+            sie_tot_true = sie_pte[0];
+            press_pte[0] = e0.PressureFromDensityTemperature(rho_pte[0], temp_pte[0], cache[0]);
+          }
+          sie[i] = sie_tot_true;
+          t_mult = 0.0, s_mult = 0.0, p_mult = 1.0;
+        } else if (input_int == -2) {
+          double sie_tot_true = 0.0;
+          if (npte > 1) {
+            Zeroed<PTESolverFixedP<CellEOS, double *, mix_impl::CacheAccessor>> z(
+                npte, ceos, vfrac_sum, press_pte[0], pr, pv, ps, pt, pp, cache, scratch.data());
+            pte_converged = PTESolver(*z.m).converged;
+            for (int mp = 0; mp < npte; ++mp)
+              sie_tot_true += sie_pte[mp] * FM(i, mats[mp]);
+          } else {
+            const EOS &e0 = eos[idxs[0]];
+            auto p_from_t = [&](const Real &t_i) {
+              return e0.PressureFromDensityTemperature(rho_pte[0], t_i, cache[0]);
+            };
+            Real r_rho{}, r_temp{}, r_sie{}, r_press{}, r_cv{}, r_bmod{}, r_dpde{}, r_dvdt{};
+            e0.ValuesAtReferenceState(r_rho, r_temp, r_sie, r_press, r_cv, r_bmod, r_dpde,
+                                      r_dvdt);
+            // the reference leaves temp_i uninitialised when every root
+            // finder gives up without writing it; 0 here
+            Real temp_i = 0.0;
+            RootFinding1D::findRoot(p_from_t, press[i], r_temp, 1.e-10 * r_temp,
+                                    1.e10 * r_temp, 1.e-12, 1.e-12, temp_i);
+            sie_pte[0] = e0.InternalEnergyFromDensityTemperature(rho_pte[0], temp_i, cache[0]);
+            sie_tot_true = sie_pte[0];
+            temp_pte[0] = temp_i;
+          }
+          sie[i] = sie_tot_true;
+          t_mult = 1.0, s_mult = 0.0, p_mult = 0.0;
+        }
+        if (converged && input_int != -1) converged[iloop] = pte_converged ? 1 : 0;
+        // final_functor (get_sg_eos_functors.hpp:185-300)
+        const bool do_t = t_mult == 1.0, do_s = s_mult == 1.0, do_p = p_mult == 1.0;
+        if (do_t) temp[i] = 0.0;
+        if (do_p) press[i] = 0.0;
+        if (do_s) sie[i] = 0.0;
+        bmod[i] = 0.0;
+        cv[i] = 0.0;
+        dpde[i] = 0.0;
+        for (int mp = 0; mp < npte; ++mp) {
+          const int m = mats[mp];
+          press[i] += press_pte[mp] * vfrac_pte[mp] * p_mult;
+          temp[i] += temp_pte[mp] * vfrac_pte[mp] * t_mult;
+          const double ie_m = sie_pte[mp] * FM(i, m) * mass_sum;
+          sie[i] += ie_m * s_mult;
+          frac_ie[i + m * cell_dim] = ie_m;
+          frac_vol[i + m * cell_dim] = vfrac_pte[mp] * vol[i];
+          const EOS &em = eos[idxs[mp]];
+          const double bmod_m =
+              em.BulkModulusFromDensityTemperature(rho_pte[mp], temp_pte[mp], cache[mp]);
+          bmod[i] += bmod_m * vfrac_pte[mp];
+          const double cv_m = ev2k * em.SpecificHeatFromDensityTemperature(
+                                         rho_pte[mp], temp_pte[mp], cache[mp]);
+          cv[i] += cv_m * FM(i, m);
+          const double dpde_m =
+              em.GruneisenParamFromDensityTemperature(rho_pte[mp], temp_pte[mp], cache[mp]);
+          dpde[i] += dpde_m * vfrac_pte[mp];
+          if (frac_bmod) frac_bmod[i + m * cell_dim] = bmod_m;
+          if (frac_cv) frac_cv[i + m * cell_dim] = cv_m;
+          if (frac_dpde) frac_dpde[i + m * cell_dim] = dpde_m;
+        }
+        if (do_t) temp[i] /= ev2k;
+        if (do_s) sie[i] /= mass_sum;
+        for (int m = 0; m < nmat; ++m)
+          FM(i, m) *= mass_sum;
+        pmax[i] = press[i] > pmax[i] ? press[i] : pmax[i];
       }
-      if (converged) converged[iloop] = pte_converged ? 1 : 0;
-      // final_functor with t_mult = 1, s_mult = 0, p_mult = 1
-      temp[i] = 0.0;
-      press[i] = 0.0;
-      bmod[i] = 0.0;
-      cv[i] = 0.0;
-      dpde[i] = 0.0;
-      for (int mp = 0; mp < npte; ++mp) {
-        const int m = mats[mp];
-        press[i] += press_pte[mp] * vfrac_pte[mp] * 1.0;
-        temp[i] += temp_pte[mp] * vfrac_pte[mp] * 1.0;
-        const double ie_m = sie_pte[mp] * FM(i, m) * mass_sum;
-        sie[i] += ie_m * 0.0;
-        frac_ie[i + m * cell_dim] = ie_m;
-        frac_vol[i + m * cell_dim] = vfrac_pte[mp] * vol[i];
-        const EOS &em = eos[idxs[mp]];
-        const double bmod_m =
-            em.BulkModulusFromDensityTemperature(rho_pte[mp], temp_pte[mp], cache[mp]);
-        bmod[i] += bmod_m * vfrac_pte[mp];
-        const double cv_m =
-            ev2k * em.SpecificHeatFromDensityTemperature(rho_pte[mp], temp_pte[mp], cache[mp]);
-        cv[i] += cv_m * FM(i, m);
-        const double dpde_m =
-            em.GruneisenParamFromDensityTemperature(rho_pte[mp], temp_pte[mp], cache[mp]);
-        dpde[i] += dpde_m * vfrac_pte[mp];
-        if (frac_bmod) frac_bmod[i + m * cell_dim] = bmod_m;
-        if (frac_cv) frac_cv[i + m * cell_dim] = cv_m;
-        if (frac_dpde) frac_dpde[i + m * cell_dim] = dpde_m;
-      }
-      temp[i] /= ev2k;
-      for (int m = 0; m < nmat; ++m)
-        FM(i, m) *= mass_sum;
-      pmax[i] = press[i] > pmax[i] ? press[i] : pmax[i];
     }
   } catch (const std::exception &ex) {
-    std::fprintf(stderr, "sgref_get_sg_eos_rho_e: %s\n", ex.what());
+    std::fprintf(stderr, "sgref_get_sg_eos: %s\n", ex.what());
     return 1;
+  }
+  return 0;
+}
+
+// The (rho, sie) entry kept under its own name.
+int sgref_get_sg_eos_rho_e(int nmat, int ncell, int cell_dim, const int *eos_offsets,
+                           const sgref_eos *descs, int neos, const int *offsets, double *press,
+                           double *pmax, double *vol, double *spvol, double *sie, double *temp,
+                           double *bmod, double *dpde, double *cv, double *frac_mass,
+                           double *frac_vol, double *frac_ie, double *frac_bmod,
+                           double *frac_dpde, double *frac_cv, double mass_frac_cutoff,
+                           int32_t *converged) {
+  return sgref_get_sg_eos(nmat, ncell, cell_dim, 1, eos_offsets, descs, neos, offsets, press,
+                          pmax, vol, spvol, sie, temp, bmod, dpde, cv, frac_mass, frac_vol,
+                          frac_ie, frac_bmod, frac_dpde, frac_cv, mass_frac_cutoff, converged);
+}
+
+// ApproxTemperatureFromRhoMatU (mixed_cell_models.hpp:790-847) per cell over
+// [nmat_max][ncell] arrays (eos_idx -1 = absent; lambda nullable
+// [nmat_max][3][ncell]; Tguess nullable).
+int sgref_approx_temperature(int nmat_max, int ncell, const sgref_eos *descs, int neos,
+                             const int32_t *eos_idx, const double *u_tot, const double *rho,
+                             const double *vfrac, const double *Tguess, double *lambda,
+                             double *temp_out) {
+  try {
+    std::vector<EOS> eos = make_all(descs, neos);
+    for (int i = 0; i < ncell; ++i) {
+      int idx[16], slot[16], n = 0;
+      double r[16], v[16], cache[16 * MAX_NUM_LAMBDAS];
+      for (int m = 0; m < nmat_max; ++m) {
+        const std::size_t k = static_cast<std::size_t>(m) * ncell + i;
+        const int ie = eos_idx ? eos_idx[k] : m;
+        if (ie < 0) continue;
+        idx[n] = ie;
+        slot[n] = m;
+        r[n] = rho[k];
+        v[n] = vfrac[k];
+        for (std::size_t l = 0; l < MAX_NUM_LAMBDAS; ++l)
+          cache[n * MAX_NUM_LAMBDAS + l] =
+              lambda ? lambda[(static_cast<std::size_t>(m) * MAX_NUM_LAMBDAS + l) * ncell + i]
+                     : 0.0;
+        ++n;
+      }
+      CellEOS ceos{eos.data(), idx};
+      mix_impl::CacheAccessor cacc(cache);
+      double *pr = r, *pv = v;
+      temp_out[i] = ApproxTemperatureFromRhoMatU(n, ceos, u_tot[i], pr, pv,
+                                                 Tguess ? Tguess[i] : 0.0, cacc);
+      if (lambda)
+        for (int q = 0; q < n; ++q)
+          for (std::size_t l = 0; l < MAX_NUM_LAMBDAS; ++l)
+            lambda[(static_cast<std::size_t>(slot[q]) * MAX_NUM_LAMBDAS + l) * ncell + i] =
+                cache[q * MAX_NUM_LAMBDAS + l];
+    }
+  } catch (const std::exception &ex) {
+    std::fprintf(stderr, "sgref_approx_temperature: %s\n", ex.what());
+    return 1;
+  }
+  return 0;
+}
+
+// MixUtils::EnforceMassVolumesSum (which = 0; uses tot) and EnforceEnergiesSum
+// (which = 1; uses tot_rho, tot) (mixed_cell_models.hpp:93-150) per cell
+// over the present slots.
+int sgref_enforce_sums(int which, int nmat_max, int ncell, const int32_t *eos_idx,
+                       const double *tot, const double *tot_rho, double *rho, double *vfrac,
+                       double *sie) {
+  for (int i = 0; i < ncell; ++i) {
+    int slot[16], n = 0;
+    double r[16], v[16], e[16];
+    for (int m = 0; m < nmat_max; ++m) {
+      const std::size_t k = static_cast<std::size_t>(m) * ncell + i;
+      if (eos_idx && eos_idx[k] < 0) continue;
+      slot[n] = m;
+      r[n] = rho[k];
+      v[n] = vfrac[k];
+      e[n] = sie ? sie[k] : 0.0;
+      ++n;
+    }
+    if (n == 0) continue;
+    double *pr = r, *pv = v, *pe = e;
+    if (which == 0)
+      MixUtils::EnforceMassVolumesSum(n, tot[i], pr, pv);
+    else
+      MixUtils::EnforceEnergiesSum(n, tot_rho[i], tot[i], pr, pv, pe);
+    for (int q = 0; q < n; ++q) {
+      const std::size_t k = static_cast<std::size_t>(slot[q]) * ncell + i;
+      rho[k] = r[q];
+      vfrac[k] = v[q];
+      if (sie) sie[k] = e[q];
+    }
   }
   return 0;
 }

@@ -82,6 +82,15 @@ int sgx_mix_params_default(sgx_mix_params *p) {
 // state in registers; the numbers are reported for API compatibility.
 int sgx_pte_rhot_required_scratch(int nmat) { return nmat * nmat + 4 * nmat + 6 * nmat; }
 int sgx_pte_pt_required_scratch(int nmat) { return 2 * 2 + 4 * 2 + 2 * nmat; }
+int sgx_pte_fixed_t_required_scratch(int nmat) {
+  return nmat * nmat + 4 * nmat + 2 * nmat + 2 * nmat;
+}
+int sgx_pte_fixed_p_required_scratch(int nmat) {
+  return (nmat + 1) * (nmat + 1) + 4 * (nmat + 1) + 2 * nmat + 3 * nmat;
+}
+int sgx_pte_rhou_required_scratch(int nmat) {
+  return 4 * nmat * nmat + 4 * 2 * nmat + 8 * nmat;
+}
 
 int sgx_eos_ideal_gas(sgx_eos *out, double gm1, double Cv) {
   if (!out) return fail(SGX_ERR_INVALID, "sgx_eos_ideal_gas: null");
@@ -413,8 +422,12 @@ int sgx_pte_solve(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list, 
                   double *rho, double *vfrac, double *sie, double *temp, double *press,
                   double *lambda, const sgx_mix_params *params, sgx_pte_status *status,
                   int precision, sgx_stream_t stream) {
-  if (solver != SGX_PTE_RHOT && solver != SGX_PTE_PT)
+  if (solver < SGX_PTE_RHOT || solver > SGX_PTE_FIXED_P)
     return fail(SGX_ERR_INVALID, "sgx_pte_solve: bad solver");
+  if (precision != SGX_PREC_FP64 && precision != SGX_PREC_MIXED)
+    return fail(SGX_ERR_INVALID, "sgx_pte_solve: bad precision");
+  if (precision == SGX_PREC_MIXED && solver != SGX_PTE_RHOT)
+    return fail(SGX_ERR_UNSUPPORTED, "sgx_pte_solve: SGX_PREC_MIXED is for SGX_PTE_RHOT only");
   if (nmat < 1 || nmat > sgx::PTE_MAX_N)
     return fail(SGX_ERR_UNSUPPORTED, "sgx_pte_solve: nmat must be in 1..6");
   if (neos < 1 || neos > sgx::MAX_EOS || !eos_list)

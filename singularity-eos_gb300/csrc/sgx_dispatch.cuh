@@ -83,6 +83,14 @@ SGX_HD double ev_min_density(const sgx_eos &e) {
   if (is_spiner(e)) return sp_rho(sp_table(e), sp_table(e).lRhoMin);
   return 0;
 }
+// The temperature ValuesAtReferenceState reports (eos_ideal.hpp:178-190,
+// eos_stiff.hpp:153-164, eos_noble_abel.hpp:167-178: room temperature;
+// eos_gruneisen.hpp:554-567: T0; eos_spiner_rho_temp.hpp:1104-1115: TNormal_).
+SGX_HD double ev_reference_T(const sgx_eos &e) {
+  if (is_spiner(e)) return sp_table(e).TNormal;
+  if (e.type == SGX_GRUNEISEN) return e.p[7];
+  return ROOM_TEMPERATURE;
+}
 SGX_HD double ev_rho_pmin(const sgx_eos &e, const double T) {
   if (is_spiner(e)) return sp_rho_pmin(sp_table(e), T);
   return eos_rho_pmin(e, T);

@@ -13,6 +13,7 @@
 namespace sgx {
 
 template <int N> cudaError_t launch_pte_fp64_n(const PteArgs &a, cudaStream_t stream);
+template <int N> cudaError_t launch_pte_ext_n(const PteArgs &a, cudaStream_t stream);
 
 namespace {
 
@@ -69,15 +70,16 @@ cudaError_t launch_pte_fp64(const PteArgs &a, cudaStream_t stream) {
   // Without an index map every cell holds exactly nmat materials.
   const int lo = a.eos_idx ? 1 : a.nmat;
   const int hi = a.nmat < PTE_MAX_N ? a.nmat : PTE_MAX_N;
+  const bool ext = a.solver != SGX_PTE_RHOT && a.solver != SGX_PTE_PT;
   cudaError_t e = cudaSuccess;
   for (int n = lo; n <= hi && e == cudaSuccess; ++n) {
     switch (n) {
-    case 1: e = launch_pte_fp64_n<1>(a, stream); break;
-    case 2: e = launch_pte_fp64_n<2>(a, stream); break;
-    case 3: e = launch_pte_fp64_n<3>(a, stream); break;
-    case 4: e = launch_pte_fp64_n<4>(a, stream); break;
-    case 5: e = launch_pte_fp64_n<5>(a, stream); break;
-    case 6: e = launch_pte_fp64_n<6>(a, stream); break;
+    case 1: e = ext ? launch_pte_ext_n<1>(a, stream) : launch_pte_fp64_n<1>(a, stream); break;
+    case 2: e = ext ? launch_pte_ext_n<2>(a, stream) : launch_pte_fp64_n<2>(a, stream); break;
+    case 3: e = ext ? launch_pte_ext_n<3>(a, stream) : launch_pte_fp64_n<3>(a, stream); break;
+    case 4: e = ext ? launch_pte_ext_n<4>(a, stream) : launch_pte_fp64_n<4>(a, stream); break;
+    case 5: e = ext ? launch_pte_ext_n<5>(a, stream) : launch_pte_fp64_n<5>(a, stream); break;
+    case 6: e = ext ? launch_pte_ext_n<6>(a, stream) : launch_pte_fp64_n<6>(a, stream); break;
     }
   }
   return e;

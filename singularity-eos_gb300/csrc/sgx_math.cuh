@@ -58,6 +58,22 @@ SGX_HD float sabs(float a) {
 #endif
 }
 
+// std::sqrt (correctly rounded on both sides).
+SGX_HD double ssqrt(double a) {
+#if defined(__CUDA_ARCH__)
+  return sqrt(a);
+#else
+  return __builtin_sqrt(a);
+#endif
+}
+SGX_HD float ssqrt(float a) {
+#if defined(__CUDA_ARCH__)
+  return sqrtf(a);
+#else
+  return __builtin_sqrtf(a);
+#endif
+}
+
 // robust::sgn (robust_utils.hpp:50-56): sgn(0) = +1.
 template <typename T> SGX_HD int rsgn(T v) { return (T(0) <= v) - (v < T(0)); }
 // robust::ratio (robust_utils.hpp:58-61): a / (b + sgn(b) * SMALL).
@@ -274,6 +290,124 @@ SGX_HD RootStatus regula_falsi(const F &f, const double ytarget, const double gu
   if (iters) *iters = iteration_count;
   xroot = 0.5 * (a + b);
   return iteration_count == max_iter ? RootStatus::FAIL : RootStatus::SUCCESS;
+}
+
+SGX_HD bool nan_or_inf(const double x) { return x != x || sabs(x) > DBL_MAX; }
+
+// secant (root_finding.hpp:379-472): central-difference Newton steps,
+// clamped to [xmin, xmax], up to SECANT_NITER_MAX (1000) iterations.
+template <typename F>
+SGX_HD RootStatus secant(const F &f, const double ytarget, const double xguess,
+                         const double xmin, const double xmax, const double xtol,
+                         const double ytol, double &xroot) {
+  double x = xguess, x_last = xguess;
+  for (int iter = 0; iter < 1000; ++iter) {
+    x_last = x;
+    const double dx = sabs(1.e-7 * x) + xtol;
+    const double y = f(x) - ytarget;
+    const double yp = f(x + dx);
+    const double ym = f(x - dx);
+    const double dyNum = yp - ym;
+    const double dyDen = (2. * dx);
+    const double dy = dyNum / dyDen;
+    x -= y / dy;
+    if (x < xmin) x = xmin;
+    if (x > xmax) x = xmax;
+    if (nan_or_inf(x)) return RootStatus::FAIL;
+    if (sabs(x - x_last) / (sabs(x) + xtol) < xtol) break;
+  }
+  xroot = x;
+  const double y = f(x);
+  const double frac_error = sabs(y - ytarget) / (sabs(y) + ytol);
+  const bool failed =
+      sabs(x - x_last) > xtol || sabs(frac_error) > ytol || nan_or_inf(x);
+  return failed ? RootStatus::FAIL : RootStatus::SUCCESS;
+}
+
+// bisect (root_finding.hpp:474-596): grows a bracket around the guess by
+// 1 % steps (x1.1 each, up to BISECT_REG_MAX = 1000), then halves it up to
+// BISECT_NITER_MAX (1000) times.
+template <typename F>
+SGX_HD RootStatus bisect(const F &f, const double ytarget, const double xguess,
+                         const double xmin, const double xmax, const double xtol,
+                         const double ytol, double &xroot) {
+  double xl = 0, xr = 0, fl = 0, fr = 0;
+  double grow = 0.01;
+  double x = xguess;
+  if (sabs(x) < xtol) x += 2. * xtol;
+  for (int i = 0; i < 1000; ++i) {
+    const double dx = sabs(grow * x);
+    xl = x - dx;
+    xr = x + dx;
+    fl = f(xl) - ytarget;
+    fr = f(xr) - ytarget;
+    grow *= 1.1;
+    if (fl * fr < 0.0 || xl < xmin || xr > xmax) break;
+    if (i > 1000 - 2) return RootStatus::FAIL;
+  }
+  if (xr > xmax) {
+    xr = xmax;
+    fr = f(xr) - ytarget;
+  }
+  if (xl < xmin) {
+    xl = xmin;
+    fl = f(xl) - ytarget;
+  }
+  if (fl * fr > 0) {
+    xl = xmin;
+    fl = f(xl) - ytarget;
+    if (fl * fr > 0) {
+      xr = xmax;
+      fr = f(xr) - ytarget;
+      if (fl * fr > 0) return RootStatus::FAIL;
+    }
+  }
+  for (int i = 0; i < 1000; ++i) {
+    const double xm = 0.5 * (xl + xr);
+    const double fm = f(xm) - ytarget;
+    if (fl * fm <= 0) {
+      xr = xm;
+      fr = fm;
+    } else {
+      xl = xm;
+      fl = fm;
+    }
+    if (xr - xl < xtol) {
+      xroot = 0.5 * (xl + xr);
+      return RootStatus::SUCCESS;
+    }
+  }
+  xroot = 0.5 * (xl + xr);
+  return RootStatus::FAIL;
+}
+
+// findRoot (root_finding.hpp:312-372): the ends first, then secant from the
+// guess, then bisection. xroot keeps its value where no stage writes it.
+template <typename F>
+SGX_HD RootStatus find_root(const F &f, const double ytarget, double xguess, const double xmin,
+                            const double xmax, const double xtol, const double ytol,
+                            double &xroot) {
+  const double fmax = f(xmax);
+  const double errmax = sabs(fmax - ytarget) / (sabs(fmax) + ytol);
+  if (errmax < ytol) {
+    xroot = xmax;
+    return RootStatus::SUCCESS;
+  }
+  const double fmin = f(xmin);
+  const double errmin = sabs(fmin - ytarget) / (sabs(fmin) + ytol);
+  if (errmin < ytol) {
+    xroot = xmin;
+    return RootStatus::SUCCESS;
+  }
+  if (xguess >= xmax) xguess = xmax - xtol;
+  if (xguess <= xmin) xguess = xmin + xtol;
+  RootStatus status = secant(f, ytarget, xguess, xmin, xmax, xtol, ytol, xroot);
+  if (status == RootStatus::SUCCESS) return status;
+  status = bisect(f, ytarget, xguess, xmin, xmax, xtol, ytol, xroot);
+  if (nan_or_inf(xroot)) return RootStatus::FAIL;
+  if (xroot < xmin) return RootStatus::FAIL;
+  if (xroot > xmax) return RootStatus::FAIL;
+  return status;
 }
 
 } // namespace sgx

@@ -175,6 +175,7 @@ template <typename T> struct MixP {
   bool iterate_t_guess;
   T derivative_eps, tol_p, tol_e, tol_v, abs_p, slow_thresh;
   T tol_p_suff, tol_e_suff, tol_v_suff, abs_p_suff;
+  T tol_t, abs_t, tol_t_suff, abs_t_suff, min_dtde;
   int max_iter_per_mat;
   T ls_alpha;
   int ls_max_iter;
@@ -195,6 +196,11 @@ template <typename T> struct MixP {
     tol_e_suff = T(q.pte_rel_tolerance_e_sufficient);
     tol_v_suff = T(q.pte_rel_tolerance_v_sufficient);
     abs_p_suff = T(q.pte_abs_tolerance_p_sufficient);
+    tol_t = T(q.pte_rel_tolerance_t);
+    abs_t = T(q.pte_abs_tolerance_t);
+    tol_t_suff = T(q.pte_rel_tolerance_t_sufficient);
+    abs_t_suff = T(q.pte_abs_tolerance_t_sufficient);
+    min_dtde = T(q.min_dtde);
     max_iter_per_mat = int(q.pte_max_iter_per_mat);
     ls_alpha = T(q.line_search_alpha);
     ls_max_iter = int(q.line_search_max_iter);
@@ -224,11 +230,36 @@ template <typename T, int N, int NEQ> struct PteBase {
   int niter;
   int err_flags; // non-zero when a reference abort path was taken
 
+  // The constructor arguments: the cell's specific internal energy (or
+  // the fixed T or P of PTESolverFixedT / FixedP, which override this) and
+  // the temperature normalisation passed in (0: none).
+  SGX_HD void configure(const T target) {
+    sie_total = target;
+    Tnorm = T(0.0);
+  }
   SGX_HD T e_of(int m, T r, T t) const { return ev_sie_from_rho_T<T>(*eos[m], r, t, lam[m]); }
+  SGX_HD T p_of(int m, T r, T t) const { return ev_P_from_rho_T<T>(*eos[m], r, t, lam[m]); }
+  SGX_HD T t_of(int m, T r, T e) const { return ev_T_from_rho_sie<T>(*eos[m], r, e, lam[m]); }
   // GetPressureFromPreferred with do_e_lookup = false (:583-597)
   SGX_HD T p_pref(int m, T r, T t, T e) const {
     if (preferred_input(*eos[m]) & Q_SIE) return ev_P_from_rho_sie<T>(*eos[m], r, e, lam[m]);
     return ev_P_from_rho_T<T>(*eos[m], r, t, lam[m]);
+  }
+  // GetPressureFromPreferred with do_e_lookup = true
+  SGX_HD T p_pref_lookup(int m, T r, T t) const {
+    if (preferred_input(*eos[m]) & Q_SIE)
+      return ev_P_from_rho_sie<T>(*eos[m], r, e_of(m, r, t), lam[m]);
+    return ev_P_from_rho_T<T>(*eos[m], r, t, lam[m]);
+  }
+  SGX_HD void fixup() {}
+  // PTESolverBase::Finalize (:351-357)
+  SGX_HD void finalize() {
+#pragma unroll
+    for (int m = 0; m < n; m++) {
+      temp[m] *= Tnorm;
+      u[m] *= uscale;
+      press[m] *= uscale;
+    }
   }
 
   SGX_HD void init_rhobar() {
@@ -741,6 +772,540 @@ template <typename T, int N> struct PtePT : PteBase<T, N, 2> {
       u[m] = ratio(sie[m] * rhobar[m], uscale);
       temp[m] = Tequil;
       press[m] = Pequil;
+    }
+    residual_eval();
+    return B::residual_norm();
+  }
+};
+
+// ===========================================================================
+// PTESolverFixedT (:1451-1637): volume fractions at a given temperature
+// ===========================================================================
+// Unknowns: the n volume fractions. Residuals: the volume sum and the n-1
+// pressure differences P_m - P_{m+1}. The temperature is the constructor's
+// T_true (the per-cell target); temp[] is passed through (x Tnorm = 1).
+template <typename T, int N> struct PteFixedT : PteBase<T, N, N> {
+  using B = PteBase<T, N, N>;
+  using B::dx;
+  using B::jac;
+  using B::P;
+  using B::press;
+  using B::residual;
+  using B::rho;
+  using B::rhobar;
+  using B::sie;
+  using B::Tnorm;
+  using B::u;
+  using B::uscale;
+  using B::vfrac;
+  using B::vfrac_total;
+  static constexpr int n = N;
+  T dpdv[N], vtemp[N];
+  T Tequil, Ttemp;
+
+  // ctor (:1497-1508): base(sie_tot = 1, Tnorm = T_true), then Tnorm = 1
+  SGX_HD void configure(const T T_true) {
+    this->sie_total = T(1.0);
+    Tequil = T_true;
+    Ttemp = T_true;
+    Tnorm = T(1.0);
+  }
+  SGX_HD void residual_eval() {
+    const T vsum = sum_neumaier(vfrac, n);
+    residual[0] = vfrac_total - vsum;
+#pragma unroll
+    for (int m = 0; m < n - 1; ++m)
+      residual[1 + m] = press[m] - press[m + 1];
+  }
+  // Init (:1520-1548)
+  SGX_HD T init() {
+    Tnorm = T(1.0);
+    B::init_rhobar();
+    B::set_vfrac_from_T(Tequil);
+    uscale = T(0.0);
+#pragma unroll
+    for (int m = 0; m < n; m++) {
+      rho[m] = ratio(rhobar[m], vfrac[m]);
+      sie[m] = B::e_of(m, rho[m], Tequil);
+      uscale += sabs(sie[m]) * rho[m];
+      press[m] = B::p_of(m, rho[m], Tequil);
+    }
+    uscale = smax(uscale, T(1.0e-14));
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      press[m] = ratio(press[m], uscale);
+      u[m] = sie[m] * ratio(rhobar[m], uscale);
+    }
+    residual_eval();
+    return B::residual_norm();
+  }
+  // CheckPTE (:1560-1578)
+  SGX_HD void check(bool &conv, bool &acceptable) const {
+    T mean_p = vfrac[0] * press[0];
+    T error_p = 0;
+#pragma unroll
+    for (int m = 1; m < n; ++m) {
+      mean_p += vfrac[m] * press[m];
+      error_p += residual[m] * residual[m];
+    }
+    error_p = ssqrt(error_p);
+    const T error_v = sabs(residual[0]);
+    const bool converged_p = (error_p < P->tol_p * sabs(mean_p) || error_p < P->abs_p);
+    const bool converged_v = error_v < P->tol_v;
+    const bool acceptable_p =
+        (error_p < P->tol_p_suff * sabs(mean_p) || error_p < P->abs_p_suff);
+    const bool acceptable_v = error_v < P->tol_v_suff;
+    conv = converged_p && converged_v;
+    acceptable = acceptable_p && acceptable_v;
+  }
+  // Jacobian (:1580-1606)
+  SGX_HD void jacobian() {
+#pragma unroll
+    for (int m = 0; m < n; m++) {
+      const T dv = (vfrac[m] < T(0.5) ? T(1.0) : T(-1.0)) * vfrac[m] * P->derivative_eps;
+      const T vf_pert = vfrac[m] + dv;
+      const T rho_pert = ratio(rhobar[m], vf_pert);
+      const T p_pert = ratio(B::p_of(m, rho_pert, Tequil), uscale);
+      dpdv[m] = smin(ratio((p_pert - press[m]), dv), -sabs(P->max_dpdv));
+    }
+#pragma unroll
+    for (int i = 0; i < n * n; ++i)
+      jac[i] = T(0.0);
+#pragma unroll
+    for (int m = 0; m < n; ++m)
+      jac[m] = T(1.0);
+#pragma unroll
+    for (int m = 0; m < n - 1; m++) {
+      jac[(m + 1) * n + m] = -dpdv[m];
+      jac[(m + 1) * n + m + 1] = dpdv[m + 1];
+    }
+  }
+  // ScaleDx (:1608-1633)
+  SGX_HD T scale_dx() {
+    T scale = 1.0;
+#pragma unroll
+    for (int m = 0; m < n; ++m)
+      if (scale * dx[m] < -P->vfrac_safety_fac * vfrac[m])
+        scale = ratio(-P->vfrac_safety_fac * vfrac[m], dx[m]);
+#pragma unroll
+    for (int m = 0; m < n; m++) {
+      const T rho_min = T(ev_rho_pmin(*this->eos[m], double(Tequil)));
+      const T alpha_max = ratio(rhobar[m], rho_min);
+      if (alpha_max < vfrac[m]) continue;
+      if (scale * dx[m] > T(0.5) * (alpha_max - vfrac[m]))
+        scale = ratio(T(0.5) * (alpha_max - vfrac[m]), dx[m]);
+    }
+#pragma unroll
+    for (int i = 0; i < n; ++i)
+      dx[i] *= scale;
+    return scale;
+  }
+  // TestUpdate (:1637-1660)
+  SGX_HD T test_update(const T scale, const bool cache_state = false) {
+    if (cache_state) {
+#pragma unroll
+      for (int m = 0; m < n; ++m)
+        vtemp[m] = vfrac[m];
+    }
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      vfrac[m] = vtemp[m] + scale * dx[m];
+      rho[m] = ratio(rhobar[m], vfrac[m]);
+      u[m] = rhobar[m] * B::e_of(m, rho[m], Tequil);
+      sie[m] = ratio(u[m], rhobar[m]);
+      u[m] = ratio(u[m], uscale);
+      press[m] = ratio(B::p_of(m, rho[m], Tequil), uscale);
+    }
+    residual_eval();
+    return B::residual_norm();
+  }
+};
+
+// ===========================================================================
+// PTESolverFixedP (:1665-1919): volume fractions and temperature at a given
+// pressure
+// ===========================================================================
+// Unknowns: the n volume fractions and T. Residuals: P - P_m for every
+// material and the volume sum. The pressure is the constructor's P (the
+// per-cell target).
+template <typename T, int N> struct PteFixedP : PteBase<T, N, N + 1> {
+  using B = PteBase<T, N, N + 1>;
+  using B::dx;
+  using B::jac;
+  using B::P;
+  using B::press;
+  using B::residual;
+  using B::rho;
+  using B::rhobar;
+  using B::sie;
+  using B::temp;
+  using B::Tnorm;
+  using B::u;
+  using B::uscale;
+  using B::vfrac;
+  using B::vfrac_total;
+  static constexpr int n = N;
+  static constexpr int neq = N + 1;
+  T dpdv[N], dpdT[N], vtemp[N];
+  T Tequil, Ttemp, Pequil;
+
+  // ctor (:1722-1734): base(sie_tot = 1, Tnorm = 0). The reference's
+  // GetTguess reads uscale and utotal_scale before this solver sets them
+  // (its Newton step on the energy sum, :522-535); they are zero here,
+  // which is what the reference computes when that memory is zero.
+  SGX_HD void configure(const T Ptarget) {
+    this->sie_total = T(1.0);
+    Tnorm = T(0.0);
+    Pequil = Ptarget;
+    uscale = T(0.0);
+    this->utotal_scale = T(0.0);
+  }
+  SGX_HD void residual_eval() {
+    const T vsum = sum_neumaier(vfrac, n);
+#pragma unroll
+    for (int m = 0; m < n; ++m)
+      residual[m] = ratio(Pequil, uscale) - press[m];
+    residual[n] = vfrac_total - vsum;
+  }
+  // Init (:1746-1779)
+  SGX_HD T init() {
+    B::init_rhobar();
+    const T Tguess = B::get_tguess();
+    Tnorm = Tguess;
+    uscale = smax(sabs(Pequil), T(1.0e-14));
+#pragma unroll
+    for (int m = 0; m < n; m++) {
+      temp[m] = T(1.0);
+      sie[m] = B::e_of(m, rho[m], Tguess);
+    }
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      u[m] = ratio(sie[m] * rhobar[m], uscale);
+      press[m] = ratio(B::p_of(m, rho[m], Tguess), uscale);
+    }
+    residual_eval();
+    Tequil = temp[0];
+    Ttemp = Tequil;
+    return B::residual_norm();
+  }
+  // CheckPTE (:1790-1808)
+  SGX_HD void check(bool &conv, bool &acceptable) const {
+    T error_p = 0;
+#pragma unroll
+    for (int m = 0; m < n; ++m)
+      error_p += residual[m] * residual[m];
+    error_p = ssqrt(error_p);
+    error_p *= uscale;
+    const T error_v = sabs(residual[neq - 1]);
+    const bool converged_p = (error_p < P->tol_p || error_p < P->abs_p);
+    const bool converged_v = error_v < P->tol_v;
+    const bool acceptable_p = (error_p < P->tol_p_suff || error_p < P->abs_p_suff);
+    const bool acceptable_v = error_v < P->tol_v_suff;
+    conv = converged_p && converged_v;
+    acceptable = acceptable_p && acceptable_v;
+  }
+  // Jacobian (:1810-1852)
+  SGX_HD void jacobian() {
+#pragma unroll
+    for (int m = 0; m < n; m++) {
+      const T dv = (vfrac[m] < T(0.5) ? T(1.0) : T(-1.0)) * vfrac[m] * P->derivative_eps;
+      const T vf_pert = vfrac[m] + dv;
+      const T rho_pert = ratio(rhobar[m], vf_pert);
+      T p_pert = ratio(B::p_pref_lookup(m, rho_pert, Tnorm * Tequil), uscale);
+      dpdv[m] = smin(ratio((p_pert - press[m]), dv), -sabs(P->max_dpdv));
+      const T dT = Tequil * P->derivative_eps;
+      p_pert = ratio(B::p_pref_lookup(m, rho[m], Tnorm * (Tequil + dT)), uscale);
+      dpdT[m] = ratio((p_pert - press[m]), dT);
+    }
+#pragma unroll
+    for (int i = 0; i < neq * neq; ++i)
+      jac[i] = T(0.0);
+#pragma unroll
+    for (int m = 0; m < n; m++) {
+      jac[m * neq + m] = dpdv[m];
+      jac[m * neq + n] = dpdT[m];
+    }
+#pragma unroll
+    for (int m = 0; m < neq - 1; ++m)
+      jac[(neq - 1) * neq + m] = T(1.0);
+  }
+  // ScaleDx (:1854-1885)
+  SGX_HD T scale_dx() {
+    T scale = 1.0;
+#pragma unroll
+    for (int m = 0; m < n; ++m)
+      if (scale * dx[m] < -P->vfrac_safety_fac * vfrac[m])
+        scale = -P->vfrac_safety_fac * ratio(vfrac[m], dx[m]);
+    const T Tnew = Tequil + scale * dx[n];
+#pragma unroll
+    for (int m = 0; m < n; m++) {
+      const T rho_min = T(smax(ev_rho_pmin(*this->eos[m], double(Tnorm * Tequil)),
+                               ev_rho_pmin(*this->eos[m], double(Tnorm * Tnew))));
+      const T alpha_max = ratio(rhobar[m], rho_min);
+      if (alpha_max < vfrac[m]) continue;
+      if (scale * dx[m] > T(0.5) * (alpha_max - vfrac[m]))
+        scale = T(0.5) * ratio(alpha_max - vfrac[m], dx[m]);
+    }
+    if (scale * dx[n] < T(-0.95) * Tequil) scale = T(-0.95) * ratio(Tequil, dx[n]);
+#pragma unroll
+    for (int i = 0; i < neq; ++i)
+      dx[i] *= scale;
+    return scale;
+  }
+  // TestUpdate (:1889-1913)
+  SGX_HD T test_update(const T scale, const bool cache_state = false) {
+    if (cache_state) {
+      Ttemp = Tequil;
+#pragma unroll
+      for (int m = 0; m < n; ++m)
+        vtemp[m] = vfrac[m];
+    }
+    Tequil = Ttemp + scale * dx[n];
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      vfrac[m] = vtemp[m] + scale * dx[m];
+      rho[m] = ratio(rhobar[m], vfrac[m]);
+      u[m] = rhobar[m] * B::e_of(m, rho[m], Tnorm * Tequil);
+      press[m] = ratio(B::p_of(m, rho[m], Tnorm * Tequil), uscale);
+      sie[m] = ratio(u[m], rhobar[m]);
+      u[m] = ratio(u[m], uscale);
+      temp[m] = Tequil;
+    }
+    residual_eval();
+    return B::residual_norm();
+  }
+};
+
+// ===========================================================================
+// PTESolverRhoU (:1921-2183): full system in volume fractions and energies
+// ===========================================================================
+// Unknowns: the n volume fractions and the n scaled energy densities u_m.
+// Residuals: volume sum, energy sum, n-1 pressure differences and n-1
+// temperature differences; each material's T comes from T(rho, sie).
+template <typename T, int N> struct PteRhoU : PteBase<T, N, 2 * N> {
+  using B = PteBase<T, N, 2 * N>;
+  using B::dx;
+  using B::jac;
+  using B::P;
+  using B::press;
+  using B::residual;
+  using B::rho;
+  using B::rho_total;
+  using B::rhobar;
+  using B::sie;
+  using B::temp;
+  using B::Tnorm;
+  using B::u;
+  using B::uscale;
+  using B::utotal_scale;
+  using B::vfrac;
+  using B::vfrac_total;
+  static constexpr int n = N;
+  static constexpr int neq = 2 * N;
+  T dpdv[N], dtdv[N], dpde[N], dtde[N], vtemp[N], utemp[N];
+
+  // Out-of-range writes are dropped: for n = 1 the reference's fixed
+  // Jacobian positions (:2094-2101) fall past the 2 x 2 matrix (into the
+  // next scratch array, which Solve overwrites).
+  SGX_HD void jset(const int idx, const T v) {
+    if (idx < neq * neq) jac[idx] = v;
+  }
+  SGX_HD void residual_eval() {
+    const T vsum = sum_neumaier(vfrac, n);
+    const T esum = sum_neumaier(u, n);
+    residual[0] = vfrac_total - vsum;
+    residual[1] = utotal_scale - esum;
+#pragma unroll
+    for (int m = 0; m < n - 1; ++m)
+      residual[2 + m] = press[m + 1] - press[m];
+#pragma unroll
+    for (int m = n + 1; m < neq; m++)
+      residual[m] = temp[m - n] - temp[m - n - 1];
+  }
+  // PTESolverBase::GetIdealPTE + TryIdealPTE (:676-763): replace the
+  // initial state by the ideal-gas PTE estimate when its residual is lower.
+  SGX_HD void try_ideal_pte() {
+    T rhoBsum = 0.0, Asum = 0.0;
+#pragma unroll
+    for (int m = 0; m < n; m++) {
+      Asum += vfrac[m] * ratio(press[m], temp[m]);
+      rhoBsum += rho[m] * vfrac[m] * ratio(sie[m], temp[m]);
+    }
+    Asum *= uscale / Tnorm;
+    rhoBsum /= Tnorm;
+    const T Tideal = uscale / rhoBsum / Tnorm;
+    const T Pideal = ratio(Tnorm * Tideal * Asum, uscale * vfrac_total);
+    T etemp[N], ptemp[N], vkeep[N], rtemp[N], res[neq];
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      etemp[m] = u[m];
+      ptemp[m] = press[m];
+      vkeep[m] = vfrac[m];
+      rtemp[m] = rho[m];
+    }
+    T res_norm_old = 0.0;
+#pragma unroll
+    for (int m = 0; m < neq; ++m) {
+      res[m] = residual[m];
+      res_norm_old += res[m] * res[m];
+    }
+    const T alpha = ratio(Pideal, Tideal);
+    for (int m = 0; m < n; ++m) {
+      vfrac[m] *= ratio(press[m], (temp[m] * alpha));
+      if (Tnorm * Tideal < T(0) ||
+          ratio(rhobar[m], vfrac[m]) < T(ev_rho_pmin(*this->eos[m], double(Tnorm * Tideal)))) {
+        for (int q = 0; q <= m; q++)
+          vfrac[q] = vkeep[q];
+        return;
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      rho[m] = ratio(rhobar[m], vfrac[m]);
+      const T sie_m = B::e_of(m, rho[m], Tnorm * Tideal);
+      u[m] = rhobar[m] * ratio(sie_m, uscale);
+      press[m] = ratio(B::p_pref(m, rho[m], Tnorm * Tideal, sie_m), uscale);
+    }
+    residual_eval();
+    T res_norm_new = 0.0;
+#pragma unroll
+    for (int m = 0; m < neq; m++)
+      res_norm_new += residual[m] * residual[m];
+    if (res_norm_new > res_norm_old) {
+#pragma unroll
+      for (int m = 0; m < n; ++m) {
+        vfrac[m] = vkeep[m];
+        rho[m] = rtemp[m];
+        u[m] = etemp[m];
+        press[m] = ptemp[m];
+      }
+#pragma unroll
+      for (int m = 0; m < neq; ++m)
+        residual[m] = res[m];
+    } else {
+#pragma unroll
+      for (int m = 0; m < n; ++m) {
+        temp[m] = Tideal;
+        sie[m] = uscale * ratio(u[m], rhobar[m]);
+      }
+    }
+  }
+  // Init (:2000-2006)
+  SGX_HD T init() {
+    B::init_base();
+    residual_eval();
+    try_ideal_pte();
+    return B::residual_norm();
+  }
+  // CheckPTE (:2022-2050)
+  SGX_HD void check(bool &conv, bool &acceptable) const {
+    T mean_p = vfrac[0] * press[0];
+    T mean_t = rhobar[0] * temp[0];
+    T error_p = 0.0, error_t = 0.0;
+#pragma unroll
+    for (int m = 1; m < n; ++m) {
+      mean_p += vfrac[m] * press[m];
+      mean_t += rhobar[m] * temp[m];
+      error_p += residual[m + 1] * residual[m + 1];
+      error_t += residual[m + n] * residual[m + n];
+    }
+    mean_t = ratio(mean_t, rho_total);
+    error_p = ssqrt(error_p);
+    error_t = ssqrt(error_t);
+    const bool converged_p = (error_p < P->tol_p * sabs(mean_p) || error_p < P->abs_p);
+    const bool converged_t = (error_t < P->tol_t * mean_t || error_t < P->abs_t);
+    const bool acceptable_p =
+        (error_p < P->tol_p_suff * sabs(mean_p) || error_p < P->abs_p_suff);
+    const bool acceptable_t = (error_t < P->tol_t_suff * mean_t || error_t < P->abs_t_suff);
+    conv = converged_p && converged_t;
+    acceptable = acceptable_p && acceptable_t;
+  }
+  // Jacobian (:2052-2116)
+  SGX_HD void jacobian() {
+#pragma unroll
+    for (int m = 0; m < n; m++) {
+      const T dv = (vfrac[m] < T(0.5) ? T(1.0) : T(-1.0)) * vfrac[m] * P->derivative_eps;
+      const T vf_pert = vfrac[m] + dv;
+      const T rho_pert = ratio(rhobar[m], vf_pert);
+      T t_pert = ratio(B::t_of(m, rho_pert, sie[m]), Tnorm);
+      T p_pert = ratio(B::p_pref(m, rho_pert, Tnorm * t_pert, sie[m]), uscale);
+      dpdv[m] = smin(ratio(p_pert - press[m], dv), -sabs(P->max_dpdv));
+      dtdv[m] = ratio(t_pert - temp[m], dv);
+      const T de = sabs(u[m]) * P->derivative_eps;
+      const T e_pert = ratio(u[m] + de, rhobar[m]);
+      t_pert = ratio(B::t_of(m, rho[m], uscale * e_pert), Tnorm);
+      p_pert = ratio(B::p_pref(m, rho[m], Tnorm * t_pert, uscale * e_pert), uscale);
+      dpde[m] = ratio(p_pert - press[m], de);
+      dtde[m] = ratio(t_pert - temp[m], de);
+      if (sabs(dtde[m]) < P->min_dtde) dtde[m] = P->derivative_eps;
+    }
+#pragma unroll
+    for (int i = 0; i < neq * neq; ++i)
+      jac[i] = T(0.0);
+    constexpr int w = 2 * N; // row length
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      jset(m, T(1.0));
+      jset(w + n + m, T(1.0));
+    }
+    jset(2 * w, dpdv[0]);
+    jset(n * w + n - 1, -dpdv[n - 1]);
+    jset((n + 1) * w, dtdv[0]);
+    jset((2 * n - 1) * w + n - 1, -dtdv[n - 1]);
+    jset(2 * w + n, dpde[0]);
+    jset(n * w + 2 * n - 1, -dpde[n - 1]);
+    jset((n + 1) * w + n, dtde[0]);
+    jset((2 * n - 1) * w + 2 * n - 1, -dtde[n - 1]);
+#pragma unroll
+    for (int m = 1; m < n - 1; ++m) {
+      jset((1 + m) * w + m, -dpdv[m]);
+      jset((2 + m) * w + m, dpdv[m]);
+      jset((n + m) * w + m, -dtdv[m]);
+      jset((n + m + 1) * w + m, dtdv[m]);
+      jset((1 + m) * w + n + m, -dpde[m]);
+      jset((2 + m) * w + n + m, dpde[m]);
+      jset((n + m) * w + n + m, -dtde[m]);
+      jset((n + m + 1) * w + n + m, dtde[m]);
+    }
+  }
+  // ScaleDx (:2118-2151)
+  SGX_HD T scale_dx() {
+    T scale = 1.0;
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      if (scale * dx[m] < T(-0.1) * vfrac[m]) scale = T(-0.1) * ratio(vfrac[m], dx[m]);
+      const T dt = (dtdv[m] * dx[m] + dtde[m] * dx[m + n]);
+      if (scale * dt < T(-0.1) * temp[m]) scale = T(-0.1) * ratio(temp[m], dt);
+      const T tt = temp[m] + scale * dt;
+      const T rho_min = T(smax(ev_rho_pmin(*this->eos[m], double(Tnorm * temp[m])),
+                               ev_rho_pmin(*this->eos[m], double(Tnorm * tt))));
+      const T alpha_max = ratio(rhobar[m], rho_min);
+      if (alpha_max < vfrac[m]) continue;
+      if (scale * dx[m] > T(0.5) * (alpha_max - vfrac[m]))
+        scale = T(0.5) * ratio(alpha_max - vfrac[m], dx[m]);
+    }
+#pragma unroll
+    for (int i = 0; i < neq; ++i)
+      dx[i] *= scale;
+    return scale;
+  }
+  // TestUpdate (:2155-2178)
+  SGX_HD T test_update(const T scale, const bool cache_state = false) {
+    if (cache_state) {
+#pragma unroll
+      for (int m = 0; m < n; ++m) {
+        vtemp[m] = vfrac[m];
+        utemp[m] = u[m];
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      vfrac[m] = vtemp[m] + scale * dx[m];
+      rho[m] = ratio(rhobar[m], vfrac[m]);
+      u[m] = utemp[m] + scale * dx[n + m];
+      sie[m] = uscale * ratio(u[m], rhobar[m]);
+      temp[m] = ratio(B::t_of(m, rho[m], sie[m]), Tnorm);
+      press[m] = ratio(B::p_pref(m, rho[m], Tnorm * temp[m], sie[m]), uscale);
     }
     residual_eval();
     return B::residual_norm();

@@ -3,9 +3,12 @@
 // exactly N materials (the others return at once), so a warp never mixes
 // system sizes and each instantiation is compiled in its own translation unit.
 //
-// One thread per cell: gather the cell's materials, run PTESolverRhoT or
-// PTESolverPT + PTESolver() (closure/mixed_cell_models.hpp:884-1446,
-// 2188-2291), scatter the equilibrium state. get_sg_eos_rho_e.cpp:30-88 is
+// One thread per cell: gather the cell's materials, run one of the solvers
+// (PTESolverRhoT, PTESolverPT, PTESolverFixedT, PTESolverFixedP,
+// PTESolverRhoU; closure/mixed_cell_models.hpp:884-2183) through PTESolver()
+// (:2188-2291), scatter the equilibrium state. The per-cell target array
+// carries the solver's scalar constructor argument: sie_tot for RhoT, PT and
+// RhoU, T_true for FixedT, P for FixedP. get_sg_eos_rho_e.cpp:30-88 is
 // the reference's per-cell loop.
 #pragma once
 
@@ -48,8 +51,7 @@ __global__ void __launch_bounds__(PTE_BLOCK) pte_cell_kernel(const PteArgs a) {
   double cache[N][3];
   s.P = &mp;
   s.vfrac_total = a.vfrac_tot[i];
-  s.sie_total = a.sie_tot[i];
-  s.Tnorm = 0.0;
+  s.configure(a.sie_tot[i]);
   s.err_flags = 0;
   for (int q = 0; q < N; ++q) {
     const long long k = static_cast<long long>(slot[q]) * nc + i;
@@ -94,6 +96,20 @@ template <int N> cudaError_t launch_pte_fp64_n(const PteArgs &a, cudaStream_t st
     pte_cell_kernel<PtePT, N><<<static_cast<unsigned>(blocks), PTE_BLOCK, 0, stream>>>(a);
   else
     pte_cell_kernel<PteRhoT, N><<<static_cast<unsigned>(blocks), PTE_BLOCK, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+// The three solvers beyond RhoT and PT, compiled in their own translation
+// units (sgx_pte_ext_n.cu).
+template <int N> cudaError_t launch_pte_ext_n(const PteArgs &a, cudaStream_t stream) {
+  const long long blocks = (a.ncell + PTE_BLOCK - 1) / PTE_BLOCK;
+  const unsigned g = static_cast<unsigned>(blocks);
+  switch (a.solver) {
+  case SGX_PTE_FIXED_T: pte_cell_kernel<PteFixedT, N><<<g, PTE_BLOCK, 0, stream>>>(a); break;
+  case SGX_PTE_FIXED_P: pte_cell_kernel<PteFixedP, N><<<g, PTE_BLOCK, 0, stream>>>(a); break;
+  case SGX_PTE_RHOU: pte_cell_kernel<PteRhoU, N><<<g, PTE_BLOCK, 0, stream>>>(a); break;
+  default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 

@@ -1,18 +1,28 @@
-// get_sg_eos in its (rho, sie) input modes (singularity-eos
-// eos/get_sg_eos.cpp:35-280, get_sg_eos_rho_e.cpp:30-88): per cell, the mass
-// fractions are normalised, the materials above the mass-fraction cutoff take
-// part in a PTESolverRhoT solve (or, alone, a T(rho, sie) and P(rho, T)
-// lookup), and the cell's pressure, temperature, bulk modulus, heat capacity
-// and dP/de are formed from the material states (get_sg_eos_functors.hpp).
+// get_sg_eos (singularity-eos eos/get_sg_eos.cpp:35-280) in all its input
+// modes: per cell, the mass fractions are normalised, the materials above
+// the mass-fraction cutoff take part in a PTE solve (or, alone, in direct
+// lookups), and the cell's pressure, temperature, energy, bulk modulus, heat
+// capacity and dP/de are formed from the material states
+// (get_sg_eos_functors.hpp).
+//
+//   input_int 0, 1  (rho, sie)  PTESolverRhoT    get_sg_eos_rho_e.cpp:30-88
+//   input_int -3    (rho, T)    PTESolverFixedT  get_sg_eos_rho_t.cpp:21-110
+//   input_int -2    (rho, P)    PTESolverFixedP  get_sg_eos_rho_p.cpp:21-118
+//   input_int -1    (P, T)      no solve         get_sg_eos_p_t.cpp:23-102
 //
 // Three stages on one stream: sgeos_init packs each cell's participating
 // materials into the [slot][cell] arrays of the PTE kernels (init_functor,
-// :28-118), the PTE kernels of sgx_pte_solve run on them (cells with fewer
-// than two participating materials carry no material and are skipped), and
-// sgeos_final does the pure-cell lookups and the averages (final_functor,
-// :185-300). Per-cell arrays are [cell_dim]; per-material arrays are
-// LayoutLeft [nmat][cell_dim] (element (i, m) at i + m * cell_dim); offsets
-// are the reference's 1-based cell indices.
+// :28-118; the whole (P, T) mode), the PTE kernels of sgx_pte_solve run on
+// them (cells with fewer than two participating materials carry no
+// material and are skipped), and sgeos_final does the pure-cell lookups and
+// the averages (final_functor, :185-300). Per-cell arrays are [cell_dim];
+// per-material arrays are LayoutLeft [nmat][cell_dim] (element (i, m) at
+// i + m * cell_dim); offsets are the reference's 1-based cell indices.
+//
+// The reference places each cell's lambda cache inside the solver scratch,
+// where it overlaps solver arrays (get_sg_eos_rho_e.cpp:50-52,
+// get_sg_eos_rho_t.cpp:50-54); here it has its own array. The two agree for
+// every EOS that does not write its lambda (all but the tabulated ones).
 #include <cstring>
 #include <string>
 
@@ -30,6 +40,7 @@ constexpr int SG_BLOCK = 128;
 
 struct SgArgs {
   int nmat, ncell, cell_dim, neos;
+  int mode; // input_int
   sgx_eos eos[MAX_EOS];
   int eos_of[MAX_NMAT]; // eos_offsets - 1
   const int *offsets;
@@ -44,17 +55,72 @@ struct SgArgs {
   int *npte, *mats;
 };
 
+// (P, T) input (get_sg_eos_p_t.cpp:33-86): every material at the cell's
+// P and T, volumes from the resulting densities; no solve.
+__device__ void sgeos_init_pt(const SgArgs &a, const sgx_eos *eos, const int iloop, const int i) {
+  const long long nc = a.ncell, cd = a.cell_dim;
+  double mass_sum = 0.0;
+  for (int m = 0; m < a.nmat; ++m) {
+    const long long k = m * nc + iloop;
+    mass_sum += a.frac_mass[i + m * cd];
+    a.mats[k] = m;
+    a.eos_idx[k] = -1;
+    a.ptemp[k] = a.temp[i] * EV2K;
+    a.ppress[k] = a.press[i];
+  }
+  for (int m = 0; m < a.nmat; ++m)
+    a.frac_mass[i + m * cd] /= mass_sum;
+  double vfrac_tot = 0.0, sie_tot = 0.0;
+  for (int m = 0; m < a.nmat; ++m) {
+    const long long k = m * nc + iloop;
+    double cache[3] = {0.0, 0.0, 0.0};
+    double r = 0.0, e = 0.0;
+    int err = 0;
+    ev_rho_sie_from_PT(eos[a.eos_of[m]], a.ppress[k], a.ptemp[k], r, e, cache, &err);
+    for (int l = 0; l < 3; ++l)
+      a.lambda[(m * 3LL + l) * nc + iloop] = cache[l];
+    a.rho[k] = r;
+    a.psie[k] = e;
+    const double fm = a.frac_mass[i + m * cd];
+    a.vfrac[k] = fm / r * mass_sum;
+    vfrac_tot += a.vfrac[k];
+    sie_tot += e * fm;
+  }
+  a.sie[i] = sie_tot;
+  a.vol[i] = vfrac_tot;
+  a.spvol[i] = a.vol[i] / mass_sum;
+  for (int m = 0; m < a.nmat; ++m)
+    a.vfrac[m * nc + iloop] /= vfrac_tot;
+  a.mass_sum[iloop] = mass_sum;
+  a.npte[iloop] = a.nmat;
+  a.vfrac_tot[iloop] = vfrac_tot;
+  a.sie_tot[iloop] = 0.0;
+}
+
 __global__ void __launch_bounds__(SG_BLOCK) sgeos_init(const SgArgs a) {
+  __shared__ sgx_eos s_eos[MAX_EOS];
+  for (int k = threadIdx.x; k < a.neos; k += blockDim.x)
+    s_eos[k] = a.eos[k];
+  __syncthreads();
   const int iloop = blockIdx.x * blockDim.x + threadIdx.x;
   if (iloop >= a.ncell) return;
   const long long nc = a.ncell, cd = a.cell_dim;
   const int i = a.offsets[iloop] - 1;
+  if (a.mode == -1) {
+    sgeos_init_pt(a, s_eos, iloop, i);
+    return;
+  }
+  // init_functor's multipliers: (rho, sie) t 0 s 1 p 0; (rho, T) t 1 s 0 p 0;
+  // (rho, P) t 0 s 0 p 1
+  const double t_mult = a.mode == -3 ? 1.0 : 0.0;
+  const double s_mult = a.mode >= 0 ? 1.0 : 0.0;
+  const double p_mult = a.mode == -2 ? 1.0 : 0.0;
   double mass_sum = 0.0;
   for (int m = 0; m < a.nmat; ++m) {
     const double fm = a.frac_mass[i + m * cd];
     mass_sum += fm;
     a.frac_vol[i + m * cd] = fm;
-    a.frac_ie[i + m * cd] = a.sie[i] * fm * 1.0;
+    a.frac_ie[i + m * cd] = a.sie[i] * fm * s_mult;
   }
   for (int m = 0; m < a.nmat; ++m)
     a.frac_mass[i + m * cd] /= mass_sum;
@@ -71,9 +137,9 @@ __global__ void __launch_bounds__(SG_BLOCK) sgeos_init(const SgArgs a) {
       a.vfrac[k] = fm;
       vfrac_sum += fm;
       a.rho[k] = fm / a.spvol[i] / fm;
-      a.ptemp[k] = a.temp[i] * EV2K * 0.0;
-      a.ppress[k] = a.press[i] * 0.0;
-      a.psie[k] = a.sie[i] * fm * 1.0;
+      a.ptemp[k] = a.temp[i] * EV2K * t_mult;
+      a.ppress[k] = a.press[i] * p_mult;
+      a.psie[k] = a.sie[i] * fm * s_mult;
       a.eos_idx[k] = npte > 1 ? a.eos_of[m] : -1;
       a.mats[k] = m;
     } else {
@@ -85,7 +151,9 @@ __global__ void __launch_bounds__(SG_BLOCK) sgeos_init(const SgArgs a) {
       a.lambda[(mp * 3LL + l) * nc + iloop] = 0.0;
   }
   a.vfrac_tot[iloop] = vfrac_sum;
-  a.sie_tot[iloop] = a.sie[i];
+  // the solver's scalar argument: sie (RhoT), T_true = temp_pte(0)
+  // (FixedT), P = press_pte(0) (FixedP)
+  a.sie_tot[iloop] = a.mode == -3 ? a.ptemp[iloop] : a.mode == -2 ? a.ppress[iloop] : a.sie[i];
   a.mass_sum[iloop] = mass_sum;
   a.npte[iloop] = npte;
 }
@@ -107,22 +175,64 @@ __global__ void __launch_bounds__(SG_BLOCK) sgeos_final(const SgArgs a) {
   for (int mp = 0; mp < npte; ++mp)
     for (int l = 0; l < 3; ++l)
       cache[mp][l] = lam(mp)[l * nc];
-  if (npte == 1) {
-    // pure cell (get_sg_eos_rho_e.cpp:76-83)
-    const sgx_eos &e = s_eos[a.eos_of[a.mats[iloop]]];
-    const double r = a.rho[iloop];
-    const double t = ev_T_from_rho_sie<double>(e, r, a.psie[iloop], cache[0]);
-    a.ptemp[iloop] = t;
-    a.ppress[iloop] = ev_P_from_rho_T<double>(e, r, t, cache[0]);
+  // final_functor's multipliers per mode
+  double t_mult = 0.0, p_mult = 0.0;
+  if (a.mode >= 0) {
+    // (rho, sie) pure cell (get_sg_eos_rho_e.cpp:76-83)
+    if (npte == 1) {
+      const sgx_eos &e = s_eos[a.eos_of[a.mats[iloop]]];
+      const double r = a.rho[iloop];
+      const double t = ev_T_from_rho_sie<double>(e, r, a.psie[iloop], cache[0]);
+      a.ptemp[iloop] = t;
+      a.ppress[iloop] = ev_P_from_rho_T<double>(e, r, t, cache[0]);
+    }
+    t_mult = 1.0, p_mult = 1.0;
+  } else if (a.mode == -3 || a.mode == -2) {
+    double sie_tot_true = 0.0;
+    if (npte > 1) {
+      for (int mp = 0; mp < npte; ++mp) {
+        const long long k = mp * nc + iloop;
+        sie_tot_true += a.psie[k] * a.frac_mass[i + a.mats[k] * cd];
+      }
+    } else {
+      const sgx_eos &e = s_eos[a.eos_of[a.mats[iloop]]];
+      const double r = a.rho[iloop];
+      if (a.mode == -3) {
+        // get_sg_eos_rho_t.cpp:78-90
+        const double t = a.ptemp[iloop];
+        a.psie[iloop] = ev_sie_from_rho_T<double>(e, r, t, cache[0]);
+        sie_tot_true = a.psie[iloop];
+        a.ppress[iloop] = ev_P_from_rho_T<double>(e, r, t, cache[0]);
+      } else {
+        // get_sg_eos_rho_p.cpp:76-96: T from P(rho, T) = P by findRoot
+        // between 1e-10 and 1e10 times the reference temperature
+        double *c0 = cache[0];
+        auto p_from_t = [&](const double t) { return ev_P_from_rho_T<double>(e, r, t, c0); };
+        const double r_temp = ev_reference_T(e);
+        double temp_i = 0.0;
+        find_root(p_from_t, a.press[i], r_temp, 1.e-10 * r_temp, 1.e10 * r_temp, 1.e-12,
+                  1.e-12, temp_i);
+        a.psie[iloop] = ev_sie_from_rho_T<double>(e, r, temp_i, cache[0]);
+        sie_tot_true = a.psie[iloop];
+        a.ptemp[iloop] = temp_i;
+      }
+    }
+    a.sie[i] = sie_tot_true;
+    if (a.mode == -3)
+      p_mult = 1.0;
+    else
+      t_mult = 1.0;
   }
-  double press = 0.0, temp = 0.0, bmod = 0.0, cv = 0.0, dpde = 0.0, sie = a.sie[i];
+  const bool do_t = t_mult == 1.0, do_p = p_mult == 1.0;
+  double press = do_p ? 0.0 : a.press[i], temp = do_t ? 0.0 : a.temp[i];
+  double bmod = 0.0, cv = 0.0, dpde = 0.0, sie = a.sie[i];
   for (int mp = 0; mp < npte; ++mp) {
     const long long k = mp * nc + iloop;
     const int m = a.mats[k];
     const double vf = a.vfrac[k], r = a.rho[k], t = a.ptemp[k];
     const double fm = a.frac_mass[i + m * cd];
-    press += a.ppress[k] * vf * 1.0;
-    temp += t * vf * 1.0;
+    press += a.ppress[k] * vf * p_mult;
+    temp += t * vf * t_mult;
     const double ie_m = a.psie[k] * fm * mass_sum;
     sie += ie_m * 0.0;
     a.frac_ie[i + m * cd] = ie_m;
@@ -139,7 +249,7 @@ __global__ void __launch_bounds__(SG_BLOCK) sgeos_final(const SgArgs a) {
     if (a.frac_dpde) a.frac_dpde[i + m * cd] = dpde_m;
   }
   a.press[i] = press;
-  a.temp[i] = temp / EV2K;
+  a.temp[i] = do_t ? temp / EV2K : temp;
   a.sie[i] = sie;
   a.bmod[i] = bmod;
   a.cv[i] = cv;
@@ -162,10 +272,7 @@ extern "C" int sgx_get_sg_eos(int nmat, int ncell, int cell_dim, int input_int,
                               double *frac_cv, double mass_frac_cutoff, int precision,
                               sgx_stream_t stream) {
   using namespace sgx;
-  if (input_int == -3 || input_int == -2 || input_int == -1)
-    return set_error(SGX_ERR_UNSUPPORTED, "sgx_get_sg_eos: only the (rho, sie) input modes "
-                                          "0 and 1 are available");
-  if (input_int != 0 && input_int != 1)
+  if (input_int < -3 || input_int > 1)
     return set_error(SGX_ERR_INVALID, "sgx_get_sg_eos: bad input_int");
   if (nmat < 1 || nmat > PTE_MAX_N)
     return set_error(SGX_ERR_UNSUPPORTED, "sgx_get_sg_eos: nmat must be in 1..6");
@@ -176,6 +283,9 @@ extern "C" int sgx_get_sg_eos(int nmat, int ncell, int cell_dim, int input_int,
     return set_error(SGX_ERR_INVALID, "sgx_get_sg_eos: eos list / offsets");
   if (precision != SGX_PREC_FP64 && precision != SGX_PREC_MIXED)
     return set_error(SGX_ERR_INVALID, "sgx_get_sg_eos: bad precision");
+  if (precision == SGX_PREC_MIXED && (input_int == -3 || input_int == -2))
+    return set_error(SGX_ERR_UNSUPPORTED,
+                     "sgx_get_sg_eos: SGX_PREC_MIXED is for the (rho, sie) and (P, T) modes");
   if (!offsets || !press || !pmax || !vol || !spvol || !sie || !temp || !bmod || !dpde || !cv ||
       !frac_mass || !frac_vol || !frac_ie)
     return set_error(SGX_ERR_INVALID, "sgx_get_sg_eos: null array");
@@ -185,6 +295,7 @@ extern "C" int sgx_get_sg_eos(int nmat, int ncell, int cell_dim, int input_int,
   a.ncell = ncell;
   a.cell_dim = cell_dim;
   a.neos = neos;
+  a.mode = input_int;
   for (int k = 0; k < neos; ++k) {
     if (eos[k].type < SGX_IDEAL_GAS || eos[k].type > SGX_SPINER_RHOT)
       return set_error(SGX_ERR_UNSUPPORTED, "sgx_get_sg_eos: EOS not available in PTE");
@@ -230,10 +341,12 @@ extern "C" int sgx_get_sg_eos(int nmat, int ncell, int cell_dim, int input_int,
   const int grid = (ncell + SG_BLOCK - 1) / SG_BLOCK;
   sgeos_init<<<grid, SG_BLOCK, 0, s>>>(a);
   e = cudaGetLastError();
-  if (e == cudaSuccess) {
+  if (e == cudaSuccess && input_int != -1) {
     PteArgs pa;
     std::memset(&pa, 0, sizeof(pa));
-    pa.solver = SGX_PTE_RHOT;
+    pa.solver = input_int == -3 ? SGX_PTE_FIXED_T
+                : input_int == -2 ? SGX_PTE_FIXED_P
+                                  : SGX_PTE_RHOT;
     pa.nmat = nmat;
     pa.ncell = ncell;
     pa.neos = neos;

@@ -72,6 +72,7 @@ enum SpinerField1D {
 struct SpinerTable {
   Grid1D gT, gRho, gCold; // T grid (fastest), rho grid, cold-curve grid
   double lRhoMin, lRhoMax, rhoMax, lTMin, lTMax, TMax, PMin, lRhoOffset, lTOffset;
+  double TNormal; // reference-state temperature (ValuesAtReferenceState)
   int nRho, nT;
   int reproducible;
   // 1 when sie increases strictly along T in every density row, which makes

@@ -320,6 +320,16 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
   t.lTMin = t.gT.min;
   t.lTMax = t.gT.max;
   t.TMax = from_log(t.lTMax, t.lTOffset);
+  // reference-state temperature: room temperature if it lies inside the
+  // table, else the middle of the log-T range (loadDataboxes_ :671-677)
+  t.TNormal = ROOM_TEMPERATURE;
+  {
+    double lTNormal = sp_lT(t, t.TNormal);
+    if (!(t.lTMin < lTNormal && lTNormal < t.lTMax)) {
+      lTNormal = 0.5 * (t.lTMin + t.lTMax);
+      t.TNormal = sp_T(t, lTNormal);
+    }
+  }
   const int nR = h.nRho, nT = h.nT;
   // fixBulkModulus_ (:689-714)
   for (int j = 0; j < nR; j++) {

@@ -15,7 +15,7 @@ Q_DENSITY, Q_SIE, Q_PRESSURE, Q_TEMPERATURE, Q_SPECIFIC_HEAT, Q_BULK_MODULUS = 1
 (FN_T_FROM_RHO_SIE, FN_SIE_FROM_RHO_T, FN_P_FROM_RHO_T, FN_P_FROM_RHO_SIE, FN_CV_FROM_RHO_T,
  FN_CV_FROM_RHO_SIE, FN_B_FROM_RHO_T, FN_B_FROM_RHO_SIE, FN_G_FROM_RHO_T, FN_G_FROM_RHO_SIE,
  FN_MIN_SIE_FROM_RHO) = range(11)
-PTE_RHOT, PTE_PT = 0, 1
+PTE_RHOT, PTE_PT, PTE_RHOU, PTE_FIXED_T, PTE_FIXED_P = 0, 1, 2, 3, 4
 PREC_FP64, PREC_MIXED = 0, 1
 
 EXPORTED = [
@@ -24,6 +24,9 @@ EXPORTED = [
     "sgx_eos_table_bytes", "sgx_eos_spiner_dump", "sgx_eos_eval", "sgx_eos_fill",
     "sgx_eos_fill_ex",
     "sgx_mix_params_default", "sgx_pte_rhot_required_scratch", "sgx_pte_pt_required_scratch",
+    "sgx_pte_fixed_t_required_scratch", "sgx_pte_fixed_p_required_scratch",
+    "sgx_pte_rhou_required_scratch", "sgx_pte_approx_temperature",
+    "sgx_mix_enforce_mass_volumes_sum", "sgx_mix_enforce_energies_sum",
     "sgx_pte_solve", "sgx_pte_solve_noalloc", "sgx_eos_helmholtz", "sgx_eos_helmholtz_dump",
     "sgx_server_create", "sgx_server_submit", "sgx_server_wait", "sgx_server_stats_get",
     "sgx_server_destroy", "sgx_host_alloc", "sgx_host_free", "sgx_eos_fill_host",
@@ -137,6 +140,9 @@ def load():
     lib.sgx_host_free.argtypes = [C.c_void_p]
     lib.sgx_pte_solve_noalloc.argtypes = [I, I, C.c_int64, P, I, P, P, P, P, P, P, P, P, P,
                                           C.POINTER(MixParams), P, P]
+    lib.sgx_pte_approx_temperature.argtypes = [I, C.c_int64, P, I, P, P, P, P, P, P, P, P]
+    lib.sgx_mix_enforce_mass_volumes_sum.argtypes = [I, C.c_int64, P, P, P, P, P]
+    lib.sgx_mix_enforce_energies_sum.argtypes = [I, C.c_int64, P, P, P, P, P, P, P]
     _lib = lib
     return lib
 
@@ -239,6 +245,31 @@ def pte_solve(solver, eos_list, eos_idx, vfrac_tot, sie_tot, rho, vfrac, sie, te
         ptr(vfrac_tot), ptr(sie_tot), ptr(rho), ptr(vfrac), ptr(sie), ptr(temp), ptr(press),
         ptr(lam), C.byref(params) if params is not None else None, ptr(status), precision,
         stream_ptr(stream)))
+
+
+def approx_temperature(eos_list, eos_idx, u_tot, rho, vfrac, temp_out, Tguess=None, lam=None,
+                       stream=None):
+    """ApproxTemperatureFromRhoMatU per cell on device tensors."""
+    nmat, ncell = rho.shape
+    arr = (SgxEos * len(eos_list))(*eos_list)
+    check(load().sgx_pte_approx_temperature(
+        nmat, ncell, C.cast(arr, C.c_void_p), len(eos_list), ptr(eos_idx), ptr(u_tot), ptr(rho),
+        ptr(vfrac), ptr(Tguess), ptr(lam), ptr(temp_out), stream_ptr(stream)))
+
+
+def enforce_mass_volumes_sum(eos_idx, tot_vol, rho, vfrac, stream=None):
+    """MixUtils::EnforceMassVolumesSum per cell on device tensors."""
+    nmat, ncell = rho.shape
+    check(load().sgx_mix_enforce_mass_volumes_sum(nmat, ncell, ptr(eos_idx), ptr(tot_vol),
+                                                  ptr(rho), ptr(vfrac), stream_ptr(stream)))
+
+
+def enforce_energies_sum(eos_idx, tot_rho, tot_sie, rho, vfrac, sie, stream=None):
+    """MixUtils::EnforceEnergiesSum per cell on device tensors."""
+    nmat, ncell = rho.shape
+    check(load().sgx_mix_enforce_energies_sum(nmat, ncell, ptr(eos_idx), ptr(tot_rho),
+                                              ptr(tot_sie), ptr(rho), ptr(vfrac), ptr(sie),
+                                              stream_ptr(stream)))
 
 
 def pte_solve_noalloc(eos_list, eos_idx, vfrac_tot, sie_tot, rho, vfrac, sie, temp, press,

@@ -141,15 +141,52 @@ def helm_fixture(ref, path, n=2048, seed=31):
     return out
 
 
+def mixutil_fixture(ref, ncell=2048, seed=121):
+    """ApproxTemperatureFromRhoMatU, EnforceMassVolumesSum and
+    EnforceEnergiesSum on the batched workload's cells after a PTESolverRhoT
+    solve, with the volume fractions and energies perturbed by 1e-6 so that
+    the sums need fixing, and a temperature guess in half the cells."""
+    wl = W.pte_batched(ncell, seed=seed)
+    descs = [desc(m) for m in wl["materials"]]
+    r = {k: wl[k].copy() for k in ("rho", "vfrac", "sie", "temp", "press")}
+    ref.pte(0, descs, wl["eos_idx"], wl["vfrac_tot"], wl["sie_tot"], r["rho"], r["vfrac"],
+            r["sie"], r["temp"], r["press"], params=ref.mix_params())
+    rng = np.random.default_rng(seed + 1)
+    present = wl["eos_idx"] >= 0
+    rho = np.where(present, r["rho"], 0.0)
+    vfrac = np.where(present, r["vfrac"] * (1 + 1e-6 * rng.standard_normal(rho.shape)), 0.0)
+    sie = np.where(present, r["sie"] * (1 + 1e-6 * rng.standard_normal(rho.shape)), 0.0)
+    rho_tot = (wl["rho"] * wl["vfrac"]).sum(axis=0)
+    u_tot = rho_tot * wl["sie_tot"]
+    tguess = np.where(rng.random(ncell) < 0.5, 0.0,
+                      np.abs(r["temp"][0]) * rng.uniform(0.5, 2.0, ncell))
+    out = dict(materials=mats_array(wl["materials"]), eos_idx=wl["eos_idx"], rho=rho,
+               vfrac=vfrac, sie=sie, rho_tot=rho_tot, sie_tot=wl["sie_tot"], u_tot=u_tot,
+               tguess=tguess, vfrac_tot=wl["vfrac_tot"])
+    out["approx_T"] = ref.approx_temperature(descs, wl["eos_idx"], u_tot, rho, vfrac)
+    out["approx_T_guess"] = ref.approx_temperature(descs, wl["eos_idx"], u_tot, rho, vfrac,
+                                                   Tguess=tguess)
+    r1, v1 = rho.copy(), vfrac.copy()
+    ref.enforce_sums(0, wl["eos_idx"], wl["vfrac_tot"], r1, v1)
+    out["vol_rho"], out["vol_vfrac"] = r1, v1
+    e2 = sie.copy()
+    ref.enforce_sums(1, wl["eos_idx"], wl["sie_tot"], rho.copy(), vfrac.copy(), tot_rho=rho_tot,
+                     sie=e2)
+    out["energy_sie"] = e2
+    return out
+
+
 SGEOS_CELLS = ("press", "pmax", "vol", "spvol", "sie", "temp", "bmod", "dpde", "cv")
 SGEOS_FRACS = ("frac_mass", "frac_vol", "frac_ie", "frac_bmod", "frac_dpde", "frac_cv")
 
 
-def sgeos_fixture(ref, cell_dim=700, ncell=512, seed=41, cutoff=1e-8):
-    """get_sg_eos (rho, sie) on four materials (IdealGas, StiffGas, NobleAbel,
-    copper Gruneisen): mass fractions with some materials absent or below
-    the cutoff, pure cells among them, cells addressed through a 1-based
-    offset list."""
+def sgeos_fixture(ref, cell_dim=700, ncell=512, seed=41, cutoff=1e-8, mode=1):
+    """get_sg_eos on four materials (IdealGas, StiffGas, NobleAbel, copper
+    Gruneisen) in input mode `mode` (1 rho-sie, -1 P-T, -2 rho-P, -3 rho-T):
+    mass fractions with some materials absent or below the cutoff, pure
+    cells among them, cells addressed through a 1-based offset list. The
+    (rho, sie) mode keeps its original inputs; the others draw T from
+    [0.01, 10] eV and P from [1e8, 1e10] microbar."""
     rng = np.random.default_rng(seed)
     mats = [W.IDEAL_AIR, W.STIFF_WATER, W.NOBLE_ABEL_GAS, W.GRUNEISEN_CU]
     nmat = len(mats)
@@ -168,17 +205,20 @@ def sgeos_fixture(ref, cell_dim=700, ncell=512, seed=41, cutoff=1e-8):
                  vol=rng.uniform(0.5, 2.0, cell_dim), spvol=1.0 / rho,
                  sie=rng.uniform(1e9, 1e11, cell_dim), temp=rng.uniform(0, 1e3, cell_dim),
                  bmod=np.zeros(cell_dim), dpde=np.zeros(cell_dim), cv=np.zeros(cell_dim))
+    if mode != 1:
+        cells["press"] = rng.uniform(1e8, 1e10, cell_dim)
+        cells["temp"] = rng.uniform(0.01, 10.0, cell_dim)
     fracs = dict(frac_mass=np.ascontiguousarray(fm), frac_vol=np.zeros((nmat, cell_dim)),
                  frac_ie=np.zeros((nmat, cell_dim)), frac_bmod=np.zeros((nmat, cell_dim)),
                  frac_dpde=np.zeros((nmat, cell_dim)), frac_cv=np.zeros((nmat, cell_dim)))
     offsets = (rng.permutation(cell_dim)[:ncell] + 1).astype(np.int32)
     eos_offsets = np.array([1, 2, 3, 4], np.int32)
     out = {"in_" + k: v.copy() for k, v in {**cells, **fracs}.items()}
-    conv = ref.get_sg_eos_rho_e([desc(m) for m in mats], eos_offsets, offsets, cells, fracs,
-                                cutoff)
+    conv = ref.get_sg_eos(mode, [desc(m) for m in mats], eos_offsets, offsets, cells, fracs,
+                          cutoff)
     out.update({"out_" + k: v for k, v in {**cells, **fracs}.items()})
     out.update(materials=mats_array(mats), offsets=offsets, eos_offsets=eos_offsets,
-               cutoff=np.float64(cutoff), converged=conv)
+               cutoff=np.float64(cutoff), converged=conv, mode=np.int32(mode))
     return out
 
 
@@ -199,6 +239,17 @@ def main():
     wl["materials"] = wl["materials"][:7]  # ideal, stiff and Noble-Abel only
     wl["eos_idx"] = np.where(wl["eos_idx"] == 7, 6, wl["eos_idx"]).astype(np.int32)
     fx["pte_pt_batched"] = pte_fixture(ref, wl, 1)
+    # PTESolverRhoU, PTESolverFixedT (target T), PTESolverFixedP (target P)
+    for solver, tag, seed in ((2, "rhou", 107), (3, "fixedt", 109), (4, "fixedp", 111)):
+        for shape, make in (("2mat", W.pte_two_material), ("batched", W.pte_batched)):
+            wl = make(1024, seed=seed + (shape == "batched"))
+            n = wl["sie_tot"].size
+            trng = np.random.default_rng(seed + 50)
+            if solver == 3:
+                wl["sie_tot"] = np.exp(trng.uniform(np.log(300.0), np.log(3e4), n))
+            elif solver == 4:
+                wl["sie_tot"] = np.exp(trng.uniform(np.log(1e8), np.log(1e11), n))
+            fx[f"pte_{tag}_{shape}"] = pte_fixture(ref, wl, solver)
     fx["eos_vector"] = vector_fixture(
         ref, [W.IDEAL_AIR, W.STIFF_WATER, W.NOBLE_ABEL_GAS, W.GRUNEISEN_CU])
     with tempfile.TemporaryDirectory() as td:
@@ -222,6 +273,9 @@ def main():
             o["out_" + k] = r[k]
         fx["pte_rhot_spiner"] = o
     fx["get_sg_eos"] = sgeos_fixture(ref)
+    fx["mix_utils"] = mixutil_fixture(ref)
+    for mode, tag in ((-3, "rho_t"), (-2, "rho_p"), (-1, "p_t")):
+        fx[f"get_sg_eos_{tag}"] = sgeos_fixture(ref, seed=42 - mode, mode=mode)
     with tempfile.TemporaryDirectory() as td:
         from sgx import helmtable
         path = os.path.join(td, "helm_table.dat")

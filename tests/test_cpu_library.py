@@ -63,6 +63,14 @@ def test_constructors_and_validation_need_no_gpu(lib):
     assert m.pte_max_iter_per_mat == 128 and m.line_search_max_iter == 6
     assert lib.sgx_pte_rhot_required_scratch(5) == 25 + 20 + 30
     assert lib.sgx_pte_pt_required_scratch(3) == 4 + 8 + 6
+    # PTESolverFixedT/FixedP/RhoURequiredScratch (mixed_cell_models.hpp:1451-1457,
+    # 1665-1671, 1924-1929)
+    assert lib.sgx_pte_fixed_t_required_scratch(3) == 9 + 12 + 6 + 6
+    assert lib.sgx_pte_fixed_p_required_scratch(3) == 16 + 16 + 6 + 9
+    assert lib.sgx_pte_rhou_required_scratch(3) == 36 + 24 + 24
+    # mixed precision is for PTESolverRhoT only
+    rc = lib.sgx_pte_solve(3, 1, 10, C.cast(arr, C.c_void_p), 1, *([None] * 10), None, 1, None)
+    assert rc == 5
 
 
 def test_missing_table_reports_io_error(lib, tmp_path):

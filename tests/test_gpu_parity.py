@@ -53,7 +53,9 @@ def check_pte(fx, out, st, label):
 
 
 @pytest.mark.parametrize("name", ["pte_rhot_2mat", "pte_rhot_batched", "pte_pt_2mat",
-                                  "pte_pt_batched"])
+                                  "pte_pt_batched", "pte_rhou_2mat", "pte_rhou_batched",
+                                  "pte_fixedt_2mat", "pte_fixedt_batched", "pte_fixedp_2mat",
+                                  "pte_fixedp_batched"])
 def test_pte_matches_reference(sgx, name):
     fx = golden(name)
     eos_list = [sgx.make_eos(k, p) for k, p in materials_from_rows(fx["materials"])]

@@ -1,8 +1,9 @@
-"""sgx_get_sg_eos against the reference's get_sg_eos driver in its (rho, sie)
-mode (tests/golden/get_sg_eos.npz, made by the oracle around the reference's
-own PTESolverRhoT and EOS calls): every per-cell and per-material output,
-within 1e-12 relative (the n >= 3 solves factor the Jacobian with a
-different QR than the oracle), untouched cells left as they were."""
+"""sgx_get_sg_eos against the reference's get_sg_eos driver in each input
+mode (tests/golden/get_sg_eos*.npz, made by the oracle around the
+reference's own PTESolverRhoT / FixedT / FixedP, root finder and EOS calls):
+every per-cell and per-material output, within 1e-12 relative (the n >= 3
+solves factor the Jacobian with a different QR than the oracle), untouched
+cells left as they were."""
 import numpy as np
 import pytest
 
@@ -28,8 +29,10 @@ def run(sgx, fx, precision):
     eos = [sgx.make_eos(k, p) for k, p in materials_from_rows(fx["materials"])]
     dev = {k: torch.as_tensor(fx["in_" + k], device="cuda").clone() for k in CELLS + FRACS}
     offsets = torch.as_tensor(fx["offsets"], device="cuda")
+    mode = int(fx["mode"]) if "mode" in fx else 1
     sgx.get_sg_eos(eos, fx["eos_offsets"], offsets, {k: dev[k] for k in CELLS},
-                   {k: dev[k] for k in FRACS}, float(fx["cutoff"]), precision=precision)
+                   {k: dev[k] for k in FRACS}, float(fx["cutoff"]), precision=precision,
+                   input_int=mode)
     torch.cuda.synchronize()
     return {k: v.cpu().numpy() for k, v in dev.items()}
 
@@ -43,8 +46,10 @@ def close(got, want, rtol, label):
     assert err.max(initial=0.0) <= rtol, f"{label}: max rel err {err.max():.3e}"
 
 
-def test_get_sg_eos_rho_e_matches_reference(sgx):
-    fx = golden("get_sg_eos")
+@pytest.mark.parametrize("name", ["get_sg_eos", "get_sg_eos_rho_t", "get_sg_eos_rho_p",
+                                  "get_sg_eos_p_t"])
+def test_get_sg_eos_matches_reference(sgx, name):
+    fx = golden(name)
     got = run(sgx, fx, 0)
     for k in CELLS + FRACS:
         close(got[k], fx["out_" + k], 1e-12, k)
@@ -67,12 +72,17 @@ def test_get_sg_eos_mixed_precision_agrees(sgx):
         assert (np.abs(g[fin] - w[fin]) / scale).max() <= 2e-5, k
 
 
-def test_get_sg_eos_rejects_other_input_modes(sgx):
+def test_get_sg_eos_rejects_bad_modes(sgx):
     import ctypes as C
     lib = sgx.load()
     e = (sgx.SgxEos * 1)(sgx.make_eos(1, (0.4, 0.718e7)))
     eo = (C.c_int * 1)(1)
-    for mode in (-3, -2, -1):
+    for mode in (-4, 2):
         rc = lib.sgx_get_sg_eos(1, 4, 4, mode, C.cast(eo, C.c_void_p), C.cast(e, C.c_void_p), 1,
                                 *([None] * 16), 0.0, 0, None)
+        assert rc == 1
+    # the fixed-T / fixed-P solves have no mixed-precision form
+    for mode in (-3, -2):
+        rc = lib.sgx_get_sg_eos(1, 4, 4, mode, C.cast(eo, C.c_void_p), C.cast(e, C.c_void_p), 1,
+                                *([None] * 16), 0.0, 1, None)
         assert rc == 5
