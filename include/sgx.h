@@ -319,6 +319,19 @@ int sgx_mix_enforce_energies_sum(int nmat, int64_t ncell, const int32_t *eos_idx
                                  const double *tot_rho, const double *tot_sie, const double *rho,
                                  const double *vfrac, double *sie, sgx_stream_t stream);
 
+/* Launch-shape knobs, process-wide. Results do not depend on them.
+ *  SGX_TUNE_LOOKUP_BLOCKS_PER_SM  4..6 (default 5): resident blocks per SM
+ *      of the mixed-precision tabulated lookup (register budget 64/48/40).
+ *  SGX_TUNE_LOOKUP_STAGE  0..2 (default 2): how that lookup stages the
+ *      table's coarse search index in shared memory: 0 not at all, 1 by
+ *      vector loads, 2 by one bulk copy (TMA).
+ *  SGX_TUNE_L2_PERSIST  0/1 (default 0): mark the table's lines persisting
+ *      in L2 (an access-policy window on the lookup's launch; sets aside
+ *      L2 for persisting lines in this process's context). */
+enum { SGX_TUNE_LOOKUP_BLOCKS_PER_SM = 1, SGX_TUNE_LOOKUP_STAGE = 2, SGX_TUNE_L2_PERSIST = 3 };
+int sgx_tune_set(int knob, int value);
+int sgx_tune_get(int knob, int *value);
+
 /* Largest ncell sgx_pte_solve_noalloc accepts. */
 #define SGX_PTE_NOALLOC_MAX_CELLS 1048576
 

@@ -375,8 +375,8 @@ int sgx_eos_fill_host(const sgx_eos *eos, int64_t n, double *rho, double *temp, 
     e = cudaStreamCreateWithFlags(&st[s], cudaStreamNonBlocking);
     for (int k = 0; k < 8 && e == cudaSuccess; ++k)
       if (arr[k].h)
-        e = cudaMallocAsync(reinterpret_cast<void **>(&dev[s][k]),
-                            static_cast<size_t>(chunk) * arr[k].width * sizeof(double), st[s]);
+        e = sgx::scratch_alloc(reinterpret_cast<void **>(&dev[s][k]),
+                               static_cast<size_t>(chunk) * arr[k].width * sizeof(double), st[s]);
   }
   for (int64_t off = 0, c = 0; off < n && e == cudaSuccess && rc == SGX_OK; off += chunk, ++c) {
     const int s = static_cast<int>(c % S);
@@ -400,7 +400,7 @@ int sgx_eos_fill_host(const sgx_eos *eos, int64_t n, double *rho, double *temp, 
   for (int s = 0; s < S; ++s) {
     if (!st[s]) continue;
     for (int k = 0; k < 8; ++k)
-      if (dev[s][k]) cudaFreeAsync(dev[s][k], st[s]);
+      if (dev[s][k]) sgx::scratch_free(dev[s][k], st[s]);
     const cudaError_t f = cudaStreamSynchronize(st[s]);
     if (e == cudaSuccess) e = f;
     cudaStreamDestroy(st[s]);

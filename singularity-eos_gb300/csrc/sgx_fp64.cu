@@ -3,8 +3,10 @@
 // sgx_pte_fp64_n.cu). Compiled with --fmad=false so that every expression
 // rounds exactly as the reference does when built without FP contraction.
 //
-//   eval_kernel   the EosBase vector overloads (eos/eos_base.hpp:169-230)
-//   fill_kernel   vector FillEos (eos/eos_base.hpp:503-531)
+//   eval_kernel      the EosBase vector overloads (eos/eos_base.hpp:169-230)
+//   fill_kernel      vector FillEos (eos/eos_base.hpp:503-531)
+//   spiner_fill_ref  tabulated FillEos for the elements the mixed-precision
+//                    lookup (sgx_lookup_mixed.cu) leaves to FP64
 #include <cuda_runtime.h>
 
 #include "sgx_internal.h"
@@ -54,6 +56,70 @@ __global__ void fill_kernel(const FillArgs a) {
   if (bad && a.err) atomicOr(a.err, 1);
 }
 
+// The reference's FP64 path (eos_spiner_rho_temp.hpp:1052-1101) for the
+// elements whose bit in `left` is set.
+__device__ void ref_element(const SpinerTable &t, const FillArgs &a, const long long e) {
+  const unsigned out = a.output;
+  const double rho = a.rho[e], sie = a.sie[e];
+  double *lam = a.lambda ? a.lambda + e * a.lambda_stride : nullptr;
+  const double lRho = sp_lRho(t, rho);
+  TableStatus ws;
+  const double lT = sp_lT_from_lRho_sie(t, lRho, sie, ws, lam);
+  const double temp = sp_T(t, lT);
+  ws = sp_loc_rho_T(t, lRho, lT);
+  if ((out & Q_TEMPERATURE) && a.temp) a.temp[e] = temp;
+  if ((out & Q_PRESSURE) && a.press) a.press[e] = sp_P_from(t, rho, lRho, temp, lT, ws);
+  if ((out & Q_CV) && a.cv) a.cv[e] = sp_cv_from(t, lRho, lT, ws);
+  if ((out & Q_BMOD) || a.cs) {
+    const double bmod = sp_bmod_from(t, rho, lRho, temp, lT, ws);
+    if ((out & Q_BMOD) && a.bmod) a.bmod[e] = bmod;
+    if (a.cs) a.cs[e] = sqrt(bmod / rho);
+  }
+  if (lam) {
+    lam[0] = lRho;
+    lam[1] = lT;
+  }
+}
+
+// Each block takes REF_WORDS consecutive mask words per round (REF_WORDS
+// x 32 elements), lists their set bits in shared memory and then runs the
+// list with all its threads, so that a sparse mask still fills the lanes.
+constexpr int REF_BLOCK = 256;
+constexpr int REF_WPT = 2; // mask words per thread per round
+constexpr int REF_WORDS = REF_BLOCK * REF_WPT;
+
+__global__ void __launch_bounds__(REF_BLOCK)
+    spiner_fill_ref(const FillArgs a, const unsigned *__restrict__ left) {
+  __shared__ SpinerTable st;
+  __shared__ unsigned count;
+  __shared__ unsigned short list[REF_WORDS * 32]; // element offsets within the round
+  if (threadIdx.x == 0) st = sp_table(a.eos);
+  const long long nwords = (a.n + 31) >> 5;
+  for (long long base = static_cast<long long>(blockIdx.x) * REF_WORDS; base < nwords;
+       base += static_cast<long long>(gridDim.x) * REF_WORDS) {
+    if (threadIdx.x == 0) count = 0;
+    __syncthreads();
+    for (int q = 0; q < REF_WPT; ++q) {
+      const int wi = q * REF_BLOCK + threadIdx.x;
+      const long long w = base + wi;
+      unsigned m = w < nwords ? left[w] : 0u;
+      if (m) {
+        unsigned pos = atomicAdd(&count, static_cast<unsigned>(__popc(m)));
+        while (m) {
+          const int b = __ffs(m) - 1;
+          m &= m - 1;
+          list[pos++] = static_cast<unsigned short>(wi * 32 + b);
+        }
+      }
+    }
+    __syncthreads();
+    const unsigned total = count;
+    for (unsigned k = threadIdx.x; k < total; k += REF_BLOCK)
+      ref_element(st, a, (base << 5) + list[k]);
+    __syncthreads();
+  }
+}
+
 int grid_for(long long n, int block) {
   int dev = 0, sms = 152;
   if (cudaGetDevice(&dev) == cudaSuccess)
@@ -88,6 +154,19 @@ cudaError_t launch_pte_fp64(const PteArgs &a, cudaStream_t stream) {
 cudaError_t launch_eval_fp64(const EvalArgs &a, cudaStream_t stream) {
   if (a.n <= 0) return cudaSuccess;
   eval_kernel<<<grid_for(a.n, 256), 256, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_ref(const FillArgs &a, const unsigned *left, cudaStream_t stream) {
+  if (a.n <= 0) return cudaSuccess;
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long words = (a.n + 31) >> 5;
+  const long long blocks = (words + REF_WORDS - 1) / REF_WORDS;
+  const long long cap = static_cast<long long>(sms) * 4;
+  spiner_fill_ref<<<static_cast<int>(blocks < cap ? blocks : cap), REF_BLOCK, 0, stream>>>(a,
+                                                                                        left);
   return cudaGetLastError();
 }
 

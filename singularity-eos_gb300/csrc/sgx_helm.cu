@@ -261,7 +261,7 @@ cudaError_t launch_helm_fill(const FillArgs &a, cudaStream_t stream) {
   const size_t ids = (n * sizeof(int) + 255) / 256 * 256;
   const size_t xs = (n * sizeof(double) + 255) / 256 * 256;
   void *scratch = nullptr;
-  cudaError_t e = cudaMallocAsync(&scratch, 256 + 3 * ids + xs, stream);
+  cudaError_t e = scratch_alloc(&scratch, 256 + 3 * ids + xs, stream);
   if (e != cudaSuccess) return e;
   char *p = static_cast<char *>(scratch);
   HelmQueue q;
@@ -283,7 +283,7 @@ cudaError_t launch_helm_fill(const FillArgs &a, cudaStream_t stream) {
     helm_invert_pass3<<<grid2, HELM_BLOCK, 0, stream>>>(a, q);
     e = cudaGetLastError();
   }
-  const cudaError_t f = cudaFreeAsync(scratch, stream);
+  const cudaError_t f = scratch_free(scratch, stream);
   return e != cudaSuccess ? e : f;
 }
 

@@ -44,6 +44,14 @@ constexpr int PTE_BINS = 8;
 // Sets the calling thread's sgx_last_error() message; returns code.
 int set_error(int code, const std::string &msg);
 
+// Tuning knobs (sgx_tune_set); the value a launcher uses now.
+int tune_get(int knob);
+
+// Stream-ordered scratch from the library's per-device memory pool
+// (sgx_pool.cu); freed with scratch_free on a stream.
+cudaError_t scratch_alloc(void **p, size_t bytes, cudaStream_t stream);
+cudaError_t scratch_free(void *p, cudaStream_t stream);
+
 // Per-cell PTE, FP64, following the reference iteration exactly.
 cudaError_t launch_pte_fp64(const PteArgs &a, cudaStream_t stream);
 // Per-cell PTE, FP32 iterations then FP64 refinement.
@@ -76,6 +84,9 @@ struct FillArgs {
 cudaError_t launch_fill_fp64(const FillArgs &a, cudaStream_t stream);
 // Tabulated rho-T FillEos from (rho, sie): FP32 bracket search + FP64 solve.
 cudaError_t launch_fill_mixed(const FillArgs &a, cudaStream_t stream);
+// The reference's FP64 tabulated FillEos for the elements whose bit is set
+// in `left` (one bit per element, 32 per word).
+cudaError_t launch_fill_ref(const FillArgs &a, const unsigned *left, cudaStream_t stream);
 // Helmholtz vector lookups and FillEos (lambda rows [Abar, Zbar, lT]).
 cudaError_t launch_helm_eval(const EvalArgs &a, cudaStream_t stream);
 cudaError_t launch_helm_fill(const FillArgs &a, cudaStream_t stream);

@@ -30,6 +30,17 @@
 // conditioning of the root itself (about eps * sie / (dsie/dlT) where the
 // cold energy dominates), P, bmod and cs within 1e-10 of the larger of the
 // value and 1e-6 of the batch's largest magnitude.
+//
+// Two kernels: spiner_fill_fast runs the steps above and marks, one bit per
+// element, what it leaves to spiner_fill_ref (sgx_fp64.cu, compiled without
+// FMA contraction, so those elements are bit-identical to the plain path),
+// which runs the reference's FP64 iteration on the marked elements only. Keeping that iteration out of
+// the fast kernel keeps its registers within the 4-blocks-per-SM budget
+// without spilling. Predicates on doubles are integer tests of the bit
+// patterns, so the FP64 pipe sees only the nine roundings that must be the
+// reference's.
+#include <mutex>
+
 #include <cuda_runtime.h>
 
 #include "sgx_dispatch.cuh"
@@ -77,11 +88,109 @@ __device__ __forceinline__ SieRec load_sie(const SieRec *p) {
   return {u.x, u.y, v.x, v.y};
 }
 
-__global__ void __launch_bounds__(LOOKUP_BLOCK, 4) spiner_fill_mixed(const FillArgs a,
-                                                                     const int stage_coarse) {
+// Integer tests of a double's bit pattern (no FP64 pipe).
+__device__ __forceinline__ bool d_is_zero(const double x) {
+  return (__double_as_longlong(x) & 0x7fffffffffffffffLL) == 0;
+}
+// x > 0 and not NaN (for the callers' range checks that follow)
+__device__ __forceinline__ bool d_positive(const double x) { return __double_as_longlong(x) > 0; }
+// ff_from_double_ok without a floating-point compare
+__device__ __forceinline__ bool ff_ok_bits(const double x) {
+  const long long b = __double_as_longlong(x);
+  const int e = static_cast<int>((b >> 52) & 0x7ff) - 1023;
+  return (b & 0x7fffffffffffffffLL) == 0 || (e >= -74 && e <= 127);
+}
+
+// One bulk copy (cp.async.bulk, the TMA engine) of `bytes` (a multiple of
+// 16, both addresses 16-byte aligned) from global to shared memory, issued
+// by thread 0 and completed on an mbarrier that every thread of the block
+// waits on. The wait is bounded: if the copy has not landed after
+// BULK_WAIT_LIMIT polls (it lands in about a microsecond), the block
+// returns false and searches without the staged index, after a second
+// bounded wait for the copy so that it never lands in a finished block.
+constexpr int BULK_WAIT_LIMIT = 1 << 22;
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ bool mbar_try_wait(const unsigned bar, const unsigned parity) {
+  unsigned done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+__device__ bool bulk_stage(void *dst, const void *src, const unsigned bytes) {
+  __shared__ __align__(8) unsigned long long mbar;
+  const unsigned bar = smem_addr(&mbar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+                 "[%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+  }
+  bool done = false;
+  for (int it = 0; it < BULK_WAIT_LIMIT && !done; ++it)
+    done = mbar_try_wait(bar, 0);
+  // the block agrees: staged only if every thread saw the copy land
+  const bool all = __syncthreads_and(done) != 0;
+  if (!all)
+    for (int it = 0; it < BULK_WAIT_LIMIT && !done; ++it)
+      done = mbar_try_wait(bar, 0);
+  return all;
+}
+
+// getLocDependsRhoSie_ (eos_spiner_rho_temp.hpp:1377-1392) at the density
+// cell (j, b1), in FP64 with the reference's roundings (no contraction):
+// true when sie is on the table.
+__device__ __noinline__ bool on_table_fp64(const SpinerTable &t, const int j, const double b1,
+                                           const double sie) {
+  const double w0 = __dsub_rn(1.0, b1);
+  const double *c = t.f1[F_SIECOLD];
+  const double *m = t.f1[F_SIELTMAX];
+  const double cold = __dadd_rn(__dmul_rn(w0, c[j]), __dmul_rn(b1, c[j + 1]));
+  const double top = __dadd_rn(__dmul_rn(w0, m[j]), __dmul_rn(b1, m[j + 1]));
+  if (sie >= __dsub_rn(top, __dmul_rn(SP_SOFT_THRESH, fabs(top)))) return false;
+  return !(sie <= __dadd_rn(cold, __dmul_rn(SP_SOFT_THRESH, fabs(cold))));
+}
+
+// The reference's lT when its regula falsi cannot bracket sie inside
+// [lTMin, lTMax] (on the table, but below the interpolant's value at lTMin
+// or above it at lTMax, which a coarse table produces between density
+// nodes): lTFromlRhoSie_ (:1222-1246) then returns its guess, the lambda
+// cache when it lies in range or the middle of the range. Also the cell
+// (i, a) of that lT, as Grid1D::weights rounds them.
+__device__ __noinline__ double unbracketed_lT(const SpinerTable &t, const double *lam, int &i,
+                                              double &a1) {
+  double lT = __dmul_rn(0.5, __dadd_rn(t.lTMin, t.lTMax));
+  if (lam != nullptr) {
+    const double c = lam[1];
+    if ((t.lTMin <= c) && (c <= t.lTMax)) lT = c;
+  }
+  const double u = __dmul_rn(__dsub_rn(lT, t.gT.min), t.gT.inv_dx);
+  i = !(u >= 0.0) ? 0 : (u > static_cast<double>(t.gT.n - 2) ? t.gT.n - 2 : static_cast<int>(u));
+  const double xl = __dadd_rn(t.gT.min, __dmul_rn(static_cast<double>(i), t.gT.dx));
+  a1 = __dmul_rn(__dsub_rn(lT, xl), t.gT.inv_dx);
+  return lT;
+}
+
+// MINB: resident blocks per SM the registers are budgeted for (4: 64
+// registers, 5: 48, 6: 40).
+template <int MINB>
+__global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
+    spiner_fill_fast(const FillArgs a, const int stage_coarse, unsigned *__restrict__ left) {
   __shared__ SpinerTable st;
   __shared__ FfConsts sc;
-  extern __shared__ float2 s_coarse[]; // [nRho-1][SP_COARSE] when staged
+  extern __shared__ __align__(16) float2 s_coarse[]; // [nRho-1][SP_COARSE_ROW] when staged
   if (threadIdx.x == 0) {
     st = sp_table(a.eos);
     sc.rho_min_f = d2ff(st.gRho.min).hi;
@@ -94,27 +203,38 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, 4) spiner_fill_mixed(const FillA
     sc.eps = d2ff(lim<double>::eps);
   }
   __syncthreads();
-  // shared rows padded to SP_COARSE + 1 entries: lanes probing the same
-  // entry of different rows then fall in different banks
-  constexpr int CS = SP_COARSE + 1;
-  if (stage_coarse) {
-    const int nco = (st.nRho - 1) * SP_COARSE;
-    for (int k = threadIdx.x; k < nco; k += blockDim.x)
-      s_coarse[(k / SP_COARSE) * CS + k % SP_COARSE] = __ldg(st.sieCoarse + k);
+  // the coarse index, [nRho-1][SP_COARSE_ROW] float2, into shared memory:
+  // stage_coarse 1 by vector loads, 2 by one bulk copy (TMA) completing on
+  // an mbarrier; 0 leaves the whole search in global memory
+  constexpr int CS = SP_COARSE_ROW;
+  int staged = stage_coarse;
+  if (stage_coarse == 1) {
+    const int n4 = (st.nRho - 1) * CS / 2;
+    const float4 *src = reinterpret_cast<const float4 *>(st.sieCoarse);
+    float4 *dst = reinterpret_cast<float4 *>(s_coarse);
+    for (int k = threadIdx.x; k < n4; k += blockDim.x)
+      dst[k] = __ldg(src + k);
     __syncthreads();
+  } else if (stage_coarse == 2) {
+    const unsigned bytes = static_cast<unsigned>((st.nRho - 1) * CS * sizeof(float2));
+    if (!bulk_stage(s_coarse, st.sieCoarse, bytes)) staged = 0;
   }
   const SpinerTable &t = st;
   const unsigned out = a.output;
   const int nc = t.nT - 1;
-  const bool table_fast = t.ff_ok && t.sie_monotone_T && t.lRhoOffset == 0.0 &&
+  const bool table_fast = t.ff_ok && t.sie_monotone_T && d_is_zero(t.lRhoOffset) &&
                           (t.gCold.min == t.gRho.min) && (t.gCold.dx == t.gRho.dx) &&
-                          (t.gCold.n == t.gRho.n) &&
-                          ff_from_double_ok(t.gRho.min) && ff_from_double_ok(t.gT.min);
+                          (t.gCold.n == t.gRho.n) && ff_ok_bits(t.gRho.min) &&
+                          ff_ok_bits(t.gT.min);
+  const bool t_offset = !d_is_zero(t.lTOffset);
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
   // the next element's inputs are loaded while this one is computed
   long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
   double rho_next = e < a.n ? __ldg(a.rho + e) : 0.0;
   double sie_next = e < a.n ? __ldg(a.sie + e) : 0.0;
+  // Every warp covers 32 consecutive elements starting at a multiple of 32
+  // (blocks and the stride are multiples of 256), so each iteration's
+  // ballot is exactly one word of the left-over mask.
   for (; e < a.n; e += stride) {
     const double rho = rho_next;
     const double sie = sie_next;
@@ -122,8 +242,9 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, 4) spiner_fill_mixed(const FillA
       rho_next = __ldg(a.rho + e + stride);
       sie_next = __ldg(a.sie + e + stride);
     }
-    double *lam = a.lambda ? a.lambda + e * a.lambda_stride : nullptr;
-    bool fast = table_fast && rho > 0.0 && ff_from_double_ok(rho);
+    bool fast = table_fast && d_positive(rho) && ff_ok_bits(rho) && ff_ok_bits(sie);
+    bool done = false;
+    double lt_guess = 0.0; // the reference's guess, when it is the answer
     int j = 0, i = 0;
     double lRho = 0.0, b1 = 0.0;
     ff B{0.f, 0.f}, A{0.f, 0.f};
@@ -158,22 +279,24 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, 4) spiner_fill_mixed(const FillA
         j = fast ? static_cast<int>(u) : 0;
       }
       b1 = __dmul_rn(__dsub_rn(lRho, __ldg(t.rhoNodes + j)), t.gRho.inv_dx);
-      B = ff_from_double_ok(b1) ? d2ff(b1) : ff_make(0.0f);
+      B = ff_ok_bits(b1) ? d2ff(b1) : ff_make(0.0f);
       fast = fast && B.hi >= 0.0f && B.hi <= 1.0f;
     }
     if (fast) {
       // 2. on-table, outside the guard band
       const float b1f = B.hi, b0f = 1.0f - B.hi;
-      const float ef = static_cast<float>(sie);
+      const float ef = d2ff(sie).hi;
       const float sc0 = fmaf(b1f, t.sieCold32[j + 1], b0f * t.sieCold32[j]);
       const float sm0 = fmaf(b1f, t.sielTMax32[j + 1], b0f * t.sielTMax32[j]);
-      fast = ef > sc0 + 1e-6f * fabsf(sc0) && ef < sm0 - 1e-6f * fabsf(sm0);
+      // inside the guard band FP64 decides, as the reference does
+      if (!(ef > sc0 + 1e-6f * fabsf(sc0) && ef < sm0 - 1e-6f * fabsf(sm0)))
+        fast = on_table_fp64(t, j, b1, sie);
       if (fast) {
         // 3. bracketing cell in FP32: first among every coarse_stride-th
         //    node (shared memory), then within that stretch
         const fq4 *row32 = t.sie4f + static_cast<long long>(j) * nc;
         int lo = 0, hi = nc - 1;
-        if (stage_coarse) {
+        if (staged) {
           const float2 *cr = s_coarse + j * CS;
           int kl = 0, kh = SP_COARSE - 1;
           while (kl < kh) {
@@ -199,12 +322,13 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, 4) spiner_fill_mixed(const FillA
         // 4. a in the cell (neighbours when FP32 picked the wrong one)
         const SieRec *row = t.sieR + static_cast<long long>(j) * nc;
         bool ok = false;
+        int edge = 0; // -1 / +1: sie below / above the whole row pair
         for (int k = 0; k < 4; ++k) {
           const SieRec r = load_sie(row + i);
           // sie = x + a (dT + b dRT) + b dR: numerator and denominator in FP64
           const double num = fma(-b1, r.dR, sie - r.x);
           const double den = fma(b1, r.dRT, r.dT);
-          if (!ff_from_double_ok(num) || !ff_from_double_ok(den) || den == 0.0) break;
+          if (!ff_ok_bits(num) || !ff_ok_bits(den) || d_is_zero(den)) break;
           A = ff_div(d2ff(num), d2ff(den));
           if (A.hi < 0.0f && i > 0) {
             --i;
@@ -215,15 +339,24 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, 4) spiner_fill_mixed(const FillA
             continue;
           }
           ok = A.hi >= 0.0f && A.hi <= 1.0f;
+          if (!ok) edge = (i == 0 && A.hi < -1e-6f) ? -1 : (i == nc - 1 && A.hi > 1.000001f) ? 1 : 0;
           break;
         }
         fast = ok;
+        if (!ok && edge != 0 && !t.reproducible) {
+          // unbracketed: the reference's answer is its guess
+          double a64;
+          lt_guess = unbracketed_lT(t, a.lambda ? a.lambda + e * a.lambda_stride : nullptr, i, a64);
+          A = d2ff(a64);
+          fast = true;
+        }
       }
     }
     if (fast) {
       // 5. lT, then T = 10^lT by the NQT pow in integers
       using namespace nqt;
-      const ff LT = ff_add(ff_mul(ff_add(ff_of_int(i), A), sc.t_dx), sc.t_min);
+      const ff LT = d_is_zero(lt_guess) ? ff_add(ff_mul(ff_add(ff_of_int(i), A), sc.t_dx), sc.t_min)
+                                        : d2ff(lt_guess);
       const ff P52 = ff_mul(LT, sc.p2_scale);
       if (fabsf(P52.hi) >= 1.1e12f && ff_gt(LT, sc.lt_lo) && ff_lt(LT, sc.lt_hi)) {
         constexpr long long ca = 9007199254740992LL, cc = 18014398509481984LL;
@@ -235,7 +368,7 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, 4) spiner_fill_mixed(const FillA
         const ff SQ = ff_sqrt(NF);
         const long long fsqrt = f2ll_bits(SQ.hi * 67108864.0f) + f2ll_bits(SQ.lo * 67108864.0f);
         double temp = __longlong_as_double(x_as_int + ca - fsqrt - frac + one_as_int);
-        if (t.lTOffset != 0.0) temp -= t.lTOffset;
+        if (t_offset) temp -= t.lTOffset;
         const long long ci = static_cast<long long>(j) * nc + i;
         const ff AB = ff_mul(A, B);
         if ((out & Q_TEMPERATURE) && a.temp) a.temp[e] = temp;
@@ -253,35 +386,44 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, 4) spiner_fill_mixed(const FillA
                             (1.0 - b1) * (a1 * d[1] + (1.0 - a1) * d[0]);
           a.cv[e] = cv > lim<double>::eps ? cv : lim<double>::eps;
         }
-        if (lam) {
+        if (a.lambda) {
+          double *lam = a.lambda + e * a.lambda_stride;
           lam[0] = lRho;
-          lam[1] = ff2d(LT);
+          lam[1] = d_is_zero(lt_guess) ? ff2d(LT) : lt_guess;
         }
-        continue;
+        done = true;
       }
     }
-    // The reference's FP64 path (eos_spiner_rho_temp.hpp:1052-1101).
-    lRho = sp_lRho(t, rho);
-    TableStatus w;
-    const double lT = sp_lT_from_lRho_sie(t, lRho, sie, w, lam);
-    const double temp = sp_T(t, lT);
-    w = sp_loc_rho_T(t, lRho, lT);
-    if ((out & Q_TEMPERATURE) && a.temp) a.temp[e] = temp;
-    if ((out & Q_PRESSURE) && a.press) a.press[e] = sp_P_from(t, rho, lRho, temp, lT, w);
-    if ((out & Q_CV) && a.cv) a.cv[e] = sp_cv_from(t, lRho, lT, w);
-    if ((out & Q_BMOD) || a.cs) {
-      const double bmod = sp_bmod_from(t, rho, lRho, temp, lT, w);
-      if ((out & Q_BMOD) && a.bmod) a.bmod[e] = bmod;
-      if (a.cs) a.cs[e] = sqrt(bmod / rho);
-    }
-    if (lam) {
-      lam[0] = lRho;
-      lam[1] = lT;
-    }
+    const unsigned mask = __ballot_sync(__activemask(), !done);
+    if ((threadIdx.x & 31) == __ffs(__activemask()) - 1) left[e >> 5] = mask;
   }
 }
 
 } // namespace
+
+// Sets aside L2 for persisting lines once per device (up to the device's
+// maximum, at most the table's size); false where the device has none.
+bool l2_persist_ready(const uint64_t table) {
+  static std::mutex mu;
+  static size_t set_aside[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+  const size_t want = table_bytes(table);
+  std::lock_guard<std::mutex> lk(mu);
+  if (set_aside[dev] < want) {
+    int maxp = 0, maxw = 0;
+    cudaDeviceGetAttribute(&maxp, cudaDevAttrMaxPersistingL2CacheSize, dev);
+    cudaDeviceGetAttribute(&maxw, cudaDevAttrMaxAccessPolicyWindowSize, dev);
+    if (maxp <= 0 || static_cast<size_t>(maxw) < want) return false;
+    const size_t size = want < static_cast<size_t>(maxp) ? want : static_cast<size_t>(maxp);
+    if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, size) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    set_aside[dev] = size;
+  }
+  return true;
+}
 
 cudaError_t launch_fill_mixed(const FillArgs &a, cudaStream_t stream) {
   if (a.n <= 0) return cudaSuccess;
@@ -291,14 +433,59 @@ cudaError_t launch_fill_mixed(const FillArgs &a, cudaStream_t stream) {
   // the coarse index of the T search, staged per block when it fits
   const int nrho = table_nrho(a.eos.table);
   const size_t coarse =
-      nrho > 1 ? static_cast<size_t>(nrho - 1) * (SP_COARSE + 1) * sizeof(float2) : 0;
-  const int stage = (coarse > 0 && coarse <= 40 * 1024) ? 1 : 0;
-  // persistent grid: the blocks resident at once, each staging the index once
+      nrho > 1 ? static_cast<size_t>(nrho - 1) * SP_COARSE_ROW * sizeof(float2) : 0;
+  const int stage =
+      (coarse > 0 && coarse <= 40 * 1024) ? tune_get(SGX_TUNE_LOOKUP_STAGE) : 0;
+  // the left-over mask, one bit per element
+  const size_t words = static_cast<size_t>((a.n + 31) >> 5);
+  void *left = nullptr;
+  cudaError_t e = scratch_alloc(&left, words * sizeof(unsigned), stream);
+  if (e != cudaSuccess) return e;
+  // persistent grid: the blocks resident at once (registers budgeted for
+  // minb per SM, shared memory permitting), each staging the index once
+  const int minb = tune_get(SGX_TUNE_LOOKUP_BLOCKS_PER_SM);
+  const size_t smem = stage ? coarse : 0;
+  int resident = 0;
+  if (minb == 6)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, spiner_fill_fast<6>, LOOKUP_BLOCK,
+                                                  smem);
+  else if (minb == 5)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, spiner_fill_fast<5>, LOOKUP_BLOCK,
+                                                  smem);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, spiner_fill_fast<4>, LOOKUP_BLOCK,
+                                                  smem);
+  const int per_sm = resident > 0 ? (resident < minb ? resident : minb) : 1;
   const long long want = (a.n + LOOKUP_BLOCK - 1) / LOOKUP_BLOCK;
-  const long long cap = static_cast<long long>(sms) * 4;
+  const long long cap = static_cast<long long>(sms) * per_sm;
   const int grid = static_cast<int>(want < cap ? want : cap);
-  spiner_fill_mixed<<<grid, LOOKUP_BLOCK, stage ? coarse : 0, stream>>>(a, stage);
-  return cudaGetLastError();
+  unsigned *lp = static_cast<unsigned *>(left);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(LOOKUP_BLOCK);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  // the table's lines persist in L2 across the streaming inputs and outputs
+  cudaLaunchAttribute attr[1];
+  if (tune_get(SGX_TUNE_L2_PERSIST) && l2_persist_ready(a.eos.table)) {
+    attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
+    attr[0].val.accessPolicyWindow.base_ptr = reinterpret_cast<void *>(a.eos.table);
+    attr[0].val.accessPolicyWindow.num_bytes = table_bytes(a.eos.table);
+    attr[0].val.accessPolicyWindow.hitRatio = 1.0f;
+    attr[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    attr[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+  }
+  if (minb == 6)
+    e = cudaLaunchKernelEx(&cfg, spiner_fill_fast<6>, a, stage, lp);
+  else if (minb == 5)
+    e = cudaLaunchKernelEx(&cfg, spiner_fill_fast<5>, a, stage, lp);
+  else
+    e = cudaLaunchKernelEx(&cfg, spiner_fill_fast<4>, a, stage, lp);
+  if (e == cudaSuccess) e = launch_fill_ref(a, static_cast<const unsigned *>(left), stream);
+  const cudaError_t f = scratch_free(left, stream);
+  return e != cudaSuccess ? e : f;
 }
 
 } // namespace sgx

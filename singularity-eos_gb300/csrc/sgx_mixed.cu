@@ -10,8 +10,8 @@
 // pass 1 queued.
 //
 // The scratch (a 256-byte counter block, perm[ncell], retry_idx[ncell]) is
-// stream-ordered memory from the device's default pool (cudaMallocAsync /
-// cudaFreeAsync on the caller's stream), so calls on different streams never
+// stream-ordered memory from the library's pool (scratch_alloc /
+// scratch_free on the caller's stream), so calls on different streams never
 // share it.
 #include <cuda_runtime.h>
 
@@ -129,14 +129,14 @@ cudaError_t launch_pte_mixed(const PteArgs &a, cudaStream_t stream) {
   void *scratch = nullptr;
   const size_t n4 = ((static_cast<size_t>(a.ncell) * sizeof(int) + 255) / 256) * 256;
   const size_t bytes = 256 + (a.eos_idx ? 2 : 1) * n4;
-  cudaError_t e = cudaMallocAsync(&scratch, bytes, stream);
+  cudaError_t e = scratch_alloc(&scratch, bytes, stream);
   if (e != cudaSuccess) return e;
   char *p = static_cast<char *>(scratch);
   args.bins = reinterpret_cast<unsigned *>(p);
   args.retry_idx = reinterpret_cast<int *>(p + 256);
   int *perm = a.eos_idx ? reinterpret_cast<int *>(p + 256 + n4) : nullptr;
   e = launch_pte_mixed_with(args, perm, stream);
-  const cudaError_t f = cudaFreeAsync(scratch, stream);
+  const cudaError_t f = scratch_free(scratch, stream);
   return e != cudaSuccess ? e : f;
 }
 

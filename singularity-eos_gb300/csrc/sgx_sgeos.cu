@@ -318,7 +318,7 @@ extern "C" int sgx_get_sg_eos(int nmat, int ncell, int cell_dim, int input_int,
   auto up = [](size_t b) { return (b + 255) / 256 * 256; };
   const size_t bytes = up(4 * nm) * 2 + up(8 * n) * 3 + up(8 * nm) * 5 + up(24 * nm) + up(4 * n);
   void *scratch = nullptr;
-  cudaError_t e = cudaMallocAsync(&scratch, bytes, s);
+  cudaError_t e = scratch_alloc(&scratch, bytes, s);
   if (e != cudaSuccess) return set_error(SGX_ERR_CUDA, "sgx_get_sg_eos: scratch allocation");
   char *p = static_cast<char *>(scratch);
   auto take = [&](size_t b) {
@@ -365,7 +365,7 @@ extern "C" int sgx_get_sg_eos(int nmat, int ncell, int cell_dim, int input_int,
     sgeos_final<<<grid, SG_BLOCK, 0, s>>>(a);
     e = cudaGetLastError();
   }
-  const cudaError_t f = cudaFreeAsync(scratch, s);
+  const cudaError_t f = scratch_free(scratch, s);
   if (e == cudaSuccess) e = f;
   if (e != cudaSuccess)
     return set_error(SGX_ERR_CUDA, std::string("sgx_get_sg_eos: ") + cudaGetErrorString(e));

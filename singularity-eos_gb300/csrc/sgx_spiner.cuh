@@ -89,13 +89,19 @@ struct SpinerTable {
   const FfRec *PR, *bmodR;
   const double *rhoNodes; // Grid1D node positions min + j * dx, rounded as weights() rounds them
   // every coarse_stride-th T node of each density cell's two rows
-  // ([nRho-1][SP_COARSE], (sie(j, i), sie(j+1, i)), +inf past the last cell),
-  // staged in shared memory by the lookup to shorten its search
+  // ([nRho-1][SP_COARSE_ROW], (sie(j, i), sie(j+1, i)), +inf past the last
+  // cell and in the row padding), staged in shared memory by the lookup to
+  // shorten its search
   const float2 *sieCoarse;
   int coarse_stride;
   int ff_ok;
 };
 constexpr int SP_COARSE = 16;
+// Row length of the coarse index in memory: 16 entries and 2 of padding,
+// 144 bytes, so that rows and the whole index are multiples of 16 bytes (a
+// bulk copy's unit) and lanes probing the same entry of different rows
+// spread over the banks.
+constexpr int SP_COARSE_ROW = SP_COARSE + 2;
 
 // ---- interpolation (DataBox::interpToReal) ----
 SGX_HD double interp1(const Grid1D &g, const double *d, const double x) {

@@ -424,7 +424,7 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
   const size_t offxl = off;
   off = align(off + static_cast<size_t>(nR) * sizeof(double));
   const size_t offco = off;
-  off = align(off + static_cast<size_t>(nR - 1) * SP_COARSE * sizeof(float2));
+  off = align(off + static_cast<size_t>(nR - 1) * SP_COARSE_ROW * sizeof(float2));
   const size_t offc32 = off;
   off = align(off + static_cast<size_t>(nR) * sizeof(float));
   const size_t offm32 = off;
@@ -498,16 +498,17 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
     const int nc = nT - 1;
     t.coarse_stride = (nc + SP_COARSE - 1) / SP_COARSE;
     for (int j = 0; j < nR - 1; ++j)
-      for (int k = 0; k < SP_COARSE; ++k) {
+      for (int k = 0; k < SP_COARSE_ROW; ++k) {
         const int i = k * t.coarse_stride;
         float2 v;
-        if (i < nc) {
+        if (k < SP_COARSE && i < nc) {
           v.x = static_cast<float>(fs[static_cast<size_t>(j) * nT + i]);
           v.y = static_cast<float>(fs[static_cast<size_t>(j + 1) * nT + i]);
         } else {
           v.x = v.y = INFINITY;
         }
-        std::memcpy(img.data() + offco + (static_cast<size_t>(j) * SP_COARSE + k) * sizeof(float2),
+        std::memcpy(img.data() + offco +
+                        (static_cast<size_t>(j) * SP_COARSE_ROW + k) * sizeof(float2),
                     &v, sizeof(v));
       }
   }

@@ -16,6 +16,7 @@ Q_DENSITY, Q_SIE, Q_PRESSURE, Q_TEMPERATURE, Q_SPECIFIC_HEAT, Q_BULK_MODULUS = 1
  FN_CV_FROM_RHO_SIE, FN_B_FROM_RHO_T, FN_B_FROM_RHO_SIE, FN_G_FROM_RHO_T, FN_G_FROM_RHO_SIE,
  FN_MIN_SIE_FROM_RHO) = range(11)
 PTE_RHOT, PTE_PT, PTE_RHOU, PTE_FIXED_T, PTE_FIXED_P = 0, 1, 2, 3, 4
+TUNE_LOOKUP_BLOCKS_PER_SM, TUNE_LOOKUP_STAGE, TUNE_L2_PERSIST = 1, 2, 3
 PREC_FP64, PREC_MIXED = 0, 1
 
 EXPORTED = [
@@ -26,7 +27,8 @@ EXPORTED = [
     "sgx_mix_params_default", "sgx_pte_rhot_required_scratch", "sgx_pte_pt_required_scratch",
     "sgx_pte_fixed_t_required_scratch", "sgx_pte_fixed_p_required_scratch",
     "sgx_pte_rhou_required_scratch", "sgx_pte_approx_temperature",
-    "sgx_mix_enforce_mass_volumes_sum", "sgx_mix_enforce_energies_sum",
+    "sgx_mix_enforce_mass_volumes_sum", "sgx_mix_enforce_energies_sum", "sgx_tune_set",
+    "sgx_tune_get",
     "sgx_pte_solve", "sgx_pte_solve_noalloc", "sgx_eos_helmholtz", "sgx_eos_helmholtz_dump",
     "sgx_server_create", "sgx_server_submit", "sgx_server_wait", "sgx_server_stats_get",
     "sgx_server_destroy", "sgx_host_alloc", "sgx_host_free", "sgx_eos_fill_host",
@@ -140,6 +142,8 @@ def load():
     lib.sgx_host_free.argtypes = [C.c_void_p]
     lib.sgx_pte_solve_noalloc.argtypes = [I, I, C.c_int64, P, I, P, P, P, P, P, P, P, P, P,
                                           C.POINTER(MixParams), P, P]
+    lib.sgx_tune_set.argtypes = [I, I]
+    lib.sgx_tune_get.argtypes = [I, C.POINTER(C.c_int)]
     lib.sgx_pte_approx_temperature.argtypes = [I, C.c_int64, P, I, P, P, P, P, P, P, P, P]
     lib.sgx_mix_enforce_mass_volumes_sum.argtypes = [I, C.c_int64, P, P, P, P, P]
     lib.sgx_mix_enforce_energies_sum.argtypes = [I, C.c_int64, P, P, P, P, P, P, P]
