@@ -13,16 +13,20 @@
 //   1. lRho: the NQT log (logs.hpp:188-200) in integers and two FP64
 //      scalings, the density cell and its weight b in FP64, all rounded as
 //      in the reference (the interpolant has a kink at each density node).
-//   2. on-table classification in FP32 with a 1e-6 guard band (elements in
-//      the band, off-table states, unbracketed targets, non-monotone tables
-//      and tables with values outside the float range take the reference's
-//      FP64 iteration unchanged);
+//   2. on-table classification in FP32 with a 1e-6 guard band; inside the
+//      band the reference's FP64 test decides, and a state off the table's
+//      bottom is answered from the cold curves right there (in FP64, with
+//      the reference's roundings). Off-top states, non-monotone tables and
+//      tables with values outside the float range take the reference's FP64
+//      iteration unchanged;
 //   3. binary search for the bracketing T cell over the FP32 corner-packed
 //      copy of sie (8 probes for 256 nodes, one 16-byte load each);
 //   4. the cell's bilinear form in difference form, sie = s00 + a dT + b dR
 //      + a b dRT (differences formed in FP64 at load), solved for a: the
 //      numerator sie - s00 - b dR, which cancels where the cold energy
-//      dominates, and the denominator by FP64 fma, the quotient in ff;
+//      dominates, and the denominator by FP64 fma, the quotient in ff. A
+//      target under (over) the whole row pair is one the reference's regula
+//      falsi cannot bracket: its answer is then its guess, reproduced here;
 //   5. T = 10^lT by the NQT pow (logs.hpp:202-214) in integers, with its
 //      square root in float-float; P, bmod and cs from their difference-form
 //      cells at (a, b), each rounded to double once.
@@ -74,18 +78,22 @@ __device__ __forceinline__ ff ff_cell(const FfRec &r, const ff A, const ff B, co
   return ff_add(x, ff_add(t, ff_add(d, c)));
 }
 
+// One 32-byte record per lane in one 256-bit load (records are 32-byte
+// aligned): a random gather then costs one instruction per record.
 __device__ __forceinline__ FfRec load_rec(const FfRec *p) {
-  const float4 u = __ldg(reinterpret_cast<const float4 *>(p));
-  const float4 v = __ldg(reinterpret_cast<const float4 *>(p) + 1);
   FfRec r;
-  r.x[0] = u.x, r.x[1] = u.y, r.dT[0] = u.z, r.dT[1] = u.w;
-  r.dR[0] = v.x, r.dR[1] = v.y, r.dRT[0] = v.z, r.dRT[1] = v.w;
+  asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=f"(r.x[0]), "=f"(r.x[1]), "=f"(r.dT[0]), "=f"(r.dT[1]), "=f"(r.dR[0]), "=f"(r.dR[1]),
+        "=f"(r.dRT[0]), "=f"(r.dRT[1])
+      : "l"(p));
   return r;
 }
 __device__ __forceinline__ SieRec load_sie(const SieRec *p) {
-  const double2 u = __ldg(reinterpret_cast<const double2 *>(p));
-  const double2 v = __ldg(reinterpret_cast<const double2 *>(p) + 1);
-  return {u.x, u.y, v.x, v.y};
+  SieRec r;
+  asm("ld.global.nc.v4.f64 {%0,%1,%2,%3}, [%4];"
+      : "=d"(r.x), "=d"(r.dT), "=d"(r.dR), "=d"(r.dRT)
+      : "l"(p));
+  return r;
 }
 
 // Integer tests of a double's bit pattern (no FP64 pipe).
@@ -149,18 +157,49 @@ __device__ bool bulk_stage(void *dst, const void *src, const unsigned bytes) {
   return all;
 }
 
+// A 1-D table at the density cell (j, b1) as interpToReal rounds it
+// (w0 d[j] + w1 d[j+1], w0 = 1 - w1), without contraction.
+__device__ __forceinline__ double interp_cell(const double *d, const int j, const double b1) {
+  return __dadd_rn(__dmul_rn(__dsub_rn(1.0, b1), d[j]), __dmul_rn(b1, d[j + 1]));
+}
+
 // getLocDependsRhoSie_ (eos_spiner_rho_temp.hpp:1377-1392) at the density
-// cell (j, b1), in FP64 with the reference's roundings (no contraction):
-// true when sie is on the table.
-__device__ __noinline__ bool on_table_fp64(const SpinerTable &t, const int j, const double b1,
+// cell (j, b1), in FP64 with the reference's roundings: 0 on the table,
+// 1 off its bottom (at or under the cold curve), 2 off its top.
+__device__ __noinline__ int table_loc_fp64(const SpinerTable &t, const int j, const double b1,
                                            const double sie) {
-  const double w0 = __dsub_rn(1.0, b1);
-  const double *c = t.f1[F_SIECOLD];
-  const double *m = t.f1[F_SIELTMAX];
-  const double cold = __dadd_rn(__dmul_rn(w0, c[j]), __dmul_rn(b1, c[j + 1]));
-  const double top = __dadd_rn(__dmul_rn(w0, m[j]), __dmul_rn(b1, m[j + 1]));
-  if (sie >= __dsub_rn(top, __dmul_rn(SP_SOFT_THRESH, fabs(top)))) return false;
-  return !(sie <= __dadd_rn(cold, __dmul_rn(SP_SOFT_THRESH, fabs(cold))));
+  const double cold = interp_cell(t.f1[F_SIECOLD], j, b1);
+  const double top = interp_cell(t.f1[F_SIELTMAX], j, b1);
+  if (sie >= __dsub_rn(top, __dmul_rn(SP_SOFT_THRESH, fabs(top)))) return 2;
+  if (sie <= __dadd_rn(cold, __dmul_rn(SP_SOFT_THRESH, fabs(cold)))) return 1;
+  return 0;
+}
+
+// FillEos off the table's bottom (eos_spiner_rho_temp.hpp:1201-1207 and the
+// cold-curve branches of PFromRholRhoTlT_, CvFromlRholT_ and
+// bModFromRholRhoTlT_, :1320-1375): lT = lTMin and P, cv and bmod from the
+// cold curves at the density cell, in FP64 with the reference's roundings.
+__device__ __noinline__ void fill_off_bottom(const SpinerTable &t, const FillArgs &a,
+                                             const long long e, const double rho,
+                                             const double lRho, const int j, const double b1) {
+  const unsigned out = a.output;
+  if ((out & Q_TEMPERATURE) && a.temp) a.temp[e] = t.TatlTMin;
+  if ((out & Q_PRESSURE) && a.press) a.press[e] = interp_cell(t.f1[F_PCOLD], j, b1);
+  if ((out & Q_CV) && a.cv) {
+    const double cv = interp_cell(t.f1[F_DEDTCOLD], j, b1);
+    a.cv[e] = cv > lim<double>::eps ? cv : lim<double>::eps;
+  }
+  if ((out & Q_BMOD) || a.cs) {
+    double bmod = interp_cell(t.f1[F_BMODCOLD], j, b1);
+    bmod = bmod > lim<double>::eps ? bmod : lim<double>::eps;
+    if ((out & Q_BMOD) && a.bmod) a.bmod[e] = bmod;
+    if (a.cs) a.cs[e] = __dsqrt_rn(__ddiv_rn(bmod, rho));
+  }
+  if (a.lambda) {
+    double *lam = a.lambda + e * a.lambda_stride;
+    lam[0] = lRho;
+    lam[1] = t.lTMin;
+  }
 }
 
 // The reference's lT when its regula falsi cannot bracket sie inside
@@ -227,6 +266,8 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
                           (t.gCold.n == t.gRho.n) && ff_ok_bits(t.gRho.min) &&
                           ff_ok_bits(t.gT.min);
   const bool t_offset = !d_is_zero(t.lTOffset);
+  // getLocDependsRhoT_(lRho, lTMin) is OffBottom (lTMin > 0)
+  const bool bottom_ok = t.lTMin <= (1 + SP_SOFT_THRESH) * t.lTMin;
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
   // the next element's inputs are loaded while this one is computed
   long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -270,15 +311,24 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
       // of a node, where the FP64 index is taken
       const float uf = (d2ff(lRho).hi - sc.rho_min_f) * sc.rho_inv_f;
       const float jf = floorf(uf);
-      if (uf - jf > 1e-4f && uf - jf < 1.0f - 1e-4f) {
+      bool exact = !(uf - jf > 1e-4f && uf - jf < 1.0f - 1e-4f) || !(jf >= 0.0f) ||
+                   jf > static_cast<float>(t.nRho - 2);
+      if (!exact) {
         j = static_cast<int>(jf);
-        fast = jf >= 0.0f && jf <= static_cast<float>(t.nRho - 2);
-      } else {
-        const double u = __dmul_rn(__dsub_rn(lRho, t.gRho.min), t.gRho.inv_dx);
-        fast = u >= 0.0 && u <= static_cast<double>(t.nRho - 2);
-        j = fast ? static_cast<int>(u) : 0;
+        b1 = __dmul_rn(__dsub_rn(lRho, __ldg(t.rhoNodes + j)), t.gRho.inv_dx);
+        // a wrong estimate shows as a weight outside [0, 1] (tested on the
+        // bit pattern: non-negative doubles order as their integers)
+        const long long bb = __double_as_longlong(b1);
+        exact = !(bb >= 0 && bb <= 0x3FF0000000000000LL);
       }
-      b1 = __dmul_rn(__dsub_rn(lRho, __ldg(t.rhoNodes + j)), t.gRho.inv_dx);
+      if (exact) {
+        // Grid1D::index: the last cell takes everything above it (the weight
+        // check below keeps only the table's own range)
+        const double u = __dmul_rn(__dsub_rn(lRho, t.gRho.min), t.gRho.inv_dx);
+        fast = u >= 0.0;
+        j = !fast ? 0 : (u > static_cast<double>(t.nRho - 2) ? t.nRho - 2 : static_cast<int>(u));
+        b1 = __dmul_rn(__dsub_rn(lRho, __ldg(t.rhoNodes + j)), t.gRho.inv_dx);
+      }
       B = ff_ok_bits(b1) ? d2ff(b1) : ff_make(0.0f);
       fast = fast && B.hi >= 0.0f && B.hi <= 1.0f;
     }
@@ -288,9 +338,17 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
       const float ef = d2ff(sie).hi;
       const float sc0 = fmaf(b1f, t.sieCold32[j + 1], b0f * t.sieCold32[j]);
       const float sm0 = fmaf(b1f, t.sielTMax32[j + 1], b0f * t.sielTMax32[j]);
-      // inside the guard band FP64 decides, as the reference does
-      if (!(ef > sc0 + 1e-6f * fabsf(sc0) && ef < sm0 - 1e-6f * fabsf(sm0)))
-        fast = on_table_fp64(t, j, b1, sie);
+      // inside the guard band FP64 decides, as the reference does; off the
+      // bottom (where lT = lTMin is itself classified off the bottom) the
+      // cold curves give the answer here
+      if (!(ef > sc0 + 1e-6f * fabsf(sc0) && ef < sm0 - 1e-6f * fabsf(sm0))) {
+        const int loc = table_loc_fp64(t, j, b1, sie);
+        fast = loc == 0;
+        if (loc == 1 && bottom_ok) {
+          fill_off_bottom(t, a, e, rho, lRho, j, b1);
+          done = true;
+        }
+      }
       if (fast) {
         // 3. bracketing cell in FP32: first among every coarse_stride-th
         //    node (shared memory), then within that stretch
@@ -358,6 +416,8 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
       const ff LT = d_is_zero(lt_guess) ? ff_add(ff_mul(ff_add(ff_of_int(i), A), sc.t_dx), sc.t_min)
                                         : d2ff(lt_guess);
       const ff P52 = ff_mul(LT, sc.p2_scale);
+      // on the table in T too (getLocDependsRhoT_); a root within 1e-8 of
+      // either end takes the FP64 pass, whose off-table forms then apply
       if (fabsf(P52.hi) >= 1.1e12f && ff_gt(LT, sc.lt_lo) && ff_lt(LT, sc.lt_hi)) {
         constexpr long long ca = 9007199254740992LL, cc = 18014398509481984LL;
         const long long x_as_int = f2ll_bits(P52.hi) + f2ll_bits(P52.lo);

@@ -73,6 +73,7 @@ struct SpinerTable {
   Grid1D gT, gRho, gCold; // T grid (fastest), rho grid, cold-curve grid
   double lRhoMin, lRhoMax, rhoMax, lTMin, lTMax, TMax, PMin, lRhoOffset, lTOffset;
   double TNormal; // reference-state temperature (ValuesAtReferenceState)
+  double TatlTMin; // T_(lTMin_): the temperature returned off the table's bottom
   int nRho, nT;
   int reproducible;
   // 1 when sie increases strictly along T in every density row, which makes

@@ -320,6 +320,7 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
   t.lTMin = t.gT.min;
   t.lTMax = t.gT.max;
   t.TMax = from_log(t.lTMax, t.lTOffset);
+  t.TatlTMin = from_log(t.lTMin, t.lTOffset);
   // reference-state temperature: room temperature if it lies inside the
   // table, else the middle of the log-T range (loadDataboxes_ :671-677)
   t.TNormal = ROOM_TEMPERATURE;
@@ -497,11 +498,13 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
     }
     const int nc = nT - 1;
     t.coarse_stride = (nc + SP_COARSE - 1) / SP_COARSE;
+    // entries 0..SP_COARSE-1: nodes k * coarse_stride; entry SP_COARSE: the
+    // last node (the end of the last stretch); the rest +inf
     for (int j = 0; j < nR - 1; ++j)
       for (int k = 0; k < SP_COARSE_ROW; ++k) {
-        const int i = k * t.coarse_stride;
+        const int i = k < SP_COARSE ? k * t.coarse_stride : nc;
         float2 v;
-        if (k < SP_COARSE && i < nc) {
+        if (k <= SP_COARSE && i <= nc && (k == SP_COARSE || i < nc)) {
           v.x = static_cast<float>(fs[static_cast<size_t>(j) * nT + i]);
           v.y = static_cast<float>(fs[static_cast<size_t>(j + 1) * nT + i]);
         } else {
