@@ -222,8 +222,32 @@ def bench_lookup(args, world, local, stream, out):
             e2e_steps = max(1, min(args.steps, 5))
             barrier(world)
             dte = max_over_ranks(time_steps(e2e_step, e2e_steps, 1, stream), world)
+            # the host link's own bound for these bytes: plain copy-engine
+            # copies of the step's inputs (H2D) and outputs (D2H), concurrent
+            h_in = torch.empty(2 * n, dtype=torch.float64).pin_memory()
+            h_out = torch.empty(4 * n, dtype=torch.float64).pin_memory()
+            d_in = torch.empty(2 * n, dtype=torch.float64, device="cuda")
+            d_out = torch.empty(4 * n, dtype=torch.float64, device="cuda")
+            s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+
+            def copy_step():
+                with torch.cuda.stream(s_in):
+                    d_in.copy_(h_in, non_blocking=True)
+                with torch.cuda.stream(s_out):
+                    h_out.copy_(d_out, non_blocking=True)
+                torch.cuda.synchronize()
+
+            import time as _t
+            copy_step()
+            t0 = _t.perf_counter()
+            for _ in range(e2e_steps):
+                copy_step()
+            link_s = (_t.perf_counter() - t0) / e2e_steps
+            del h_in, h_out, d_in, d_out
             out["e2e"] = {"value": world * n * e2e_steps / dte, "unit": "lookups/s",
-                          "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 32 * n}
+                          "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 32 * n,
+                          "host_link_copy_ms": link_s * 1e3,
+                          "frac_of_host_link": link_s / (dte / e2e_steps)}
         lib.load().sgx_eos_finalize(__import__("ctypes").byref(tab))
         out["value"], out["ms_per_step"] = m["value"], m["ms"]
         # two kernels per FillEos: the float-float pass and the FP64 pass

@@ -327,8 +327,16 @@ int sgx_mix_enforce_energies_sum(int nmat, int64_t ncell, const int32_t *eos_idx
  *      vector loads, 2 by one bulk copy (TMA).
  *  SGX_TUNE_L2_PERSIST  0/1 (default 0): mark the table's lines persisting
  *      in L2 (an access-policy window on the lookup's launch; sets aside
- *      L2 for persisting lines in this process's context). */
-enum { SGX_TUNE_LOOKUP_BLOCKS_PER_SM = 1, SGX_TUNE_LOOKUP_STAGE = 2, SGX_TUNE_L2_PERSIST = 3 };
+ *      L2 for persisting lines in this process's context).
+ *  SGX_TUNE_HOST_FILL_STAGED  0/1 (default 0): sgx_eos_fill_host copies
+ *      through device buffers even where the kernel could work on the host
+ *      arrays in place. */
+enum {
+  SGX_TUNE_LOOKUP_BLOCKS_PER_SM = 1,
+  SGX_TUNE_LOOKUP_STAGE = 2,
+  SGX_TUNE_L2_PERSIST = 3,
+  SGX_TUNE_HOST_FILL_STAGED = 4
+};
 int sgx_tune_set(int knob, int value);
 int sgx_tune_get(int knob, int *value);
 

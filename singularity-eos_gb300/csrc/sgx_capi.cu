@@ -339,7 +339,7 @@ int sgx_eos_fill_host(const sgx_eos *eos, int64_t n, double *rho, double *temp, 
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&coherent, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
     double *mapped[8] = {};
-    bool all_mapped = coherent != 0;
+    bool all_mapped = coherent != 0 && !sgx::tune_get(SGX_TUNE_HOST_FILL_STAGED);
     for (int k = 0; k < 8 && all_mapped; ++k) {
       if (!arr[k].h) continue;
       cudaPointerAttributes at;

@@ -71,6 +71,7 @@ Knob g_knobs[] = {
     {{5}, 4, 6}, // SGX_TUNE_LOOKUP_BLOCKS_PER_SM
     {{2}, 0, 2}, // SGX_TUNE_LOOKUP_STAGE
     {{0}, 0, 1}, // SGX_TUNE_L2_PERSIST
+    {{0}, 0, 1}, // SGX_TUNE_HOST_FILL_STAGED
 };
 constexpr int NKNOBS = sizeof(g_knobs) / sizeof(g_knobs[0]);
 } // namespace
