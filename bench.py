@@ -43,7 +43,7 @@ N_PTE2 = 65536
 N_PTE_BATCH = 1 << 22
 N_HELM = 1 << 22
 LOOKUP_BYTES_PER_QUERY = 16 + 32  # rho, sie in; T, P, bmod, cs out (float64)
-LOOKUP_TRAFFIC_2_24 = (283.95 + 486.50) * 1e6  # measured DRAM bytes per 2^24-query launch
+LOOKUP_TRAFFIC_2_24 = (283.67 + 489.62 + 2.19) * 1e6  # measured DRAM bytes per 2^24-query step
 Q_OUT = 8 | 4 | 32                # temperature | pressure | bulk modulus
 METRIC = "PTE mixed cells/s & EOS lookups/s, 1 GB300, batched+FP32-refined vs plain FP64"
 
@@ -192,18 +192,20 @@ def bench_lookup(args, world, local, stream, out):
                                  clocks=clk.summary(), steps=steps)
         m = results["mixed"]
         out["clocks"] = m["clocks"]
-        # DRAM bytes of one 2^24-query launch, dram__bytes_read.sum +
-        # dram__bytes_write.sum from one ncu capture (profiles/
-        # spiner_fill_mixed_lookup_4M.md), scaled to this launch's queries
+        # DRAM bytes of one 2^24-query step (both kernels),
+        # dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture
+        # (profiles/spiner_fill_fast_lookup.md), scaled to this step's queries
         traffic = LOOKUP_TRAFFIC_2_24 * n / float(1 << 24)
         out["roofline"] = {"bound": "hbm", "achieved": m["gbs"], "peak": hbm, "unit": "GB/s",
                            "frac": m["gbs"] / hbm, "traffic": traffic,
                            "peak_kind": hbm_kind + " (burst copy)",
-                           "kernel": "spiner_fill_mixed (sgx_lookup_mixed.cu)",
+                           "kernel": "spiner_fill_fast + spiner_fill_ref (sgx_lookup_mixed.cu, "
+                                     "sgx_fp64.cu); achieved over the whole step",
                            "bytes_per_query": LOOKUP_BYTES_PER_QUERY,
-                           # the kernel is bound by the FP64 pipe, not HBM (ncu capture
-                           # in profiles/spiner_fill_mixed_lookup_4M.md)
-                           "fp64_pipe_pct_active_ncu": 49.1}
+                           # neither HBM nor one pipe binds: FP64 pipe 49%, L1 data
+                           # pipe 65%, issue 68% (ncu capture in
+                           # profiles/spiner_fill_fast_lookup.md)
+                           "fp64_pipe_pct_active_ncu": 48.6, "l1_lsu_pct_ncu": 64.7}
         f = results["fp64"]
         out["plain_fp64"] = {"value": f["value"], "unit": "lookups/s", "ms_per_step": f["ms"],
                              "hbm_frac": f["gbs"] / hbm, "clocks": f["clocks"],
