@@ -39,6 +39,8 @@ UNITS = [
     (f"sgx_pte_mixed_n{n}", "sgx_pte_mixed_n.cu", ["--fmad=true", f"-DSGX_PTE_N={n}"])
     for n in range(1, 7)] + [
     (f"sgx_pte_ext_n{n}", "sgx_pte_ext_n.cu", ["--fmad=false", f"-DSGX_PTE_N={n}"])
+    for n in range(1, 7)] + [
+    (f"sgx_pte_retry_n{n}", "sgx_pte_retry_n.cu", ["--fmad=false", f"-DSGX_PTE_N={n}"])
     for n in range(1, 7)]
 
 

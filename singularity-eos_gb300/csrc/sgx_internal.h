@@ -34,7 +34,8 @@ struct PteArgs {
   //  - bins[0..8): cells per material count; bins[8..16): scatter cursors;
   //    bins[16..24): retry-queue length per material count;
   //  - retry_idx: cells whose FP32 solve + FP64 refinement failed, queued for
-  //    a second, FP64 pass (reused by each material count in turn).
+  //    a second, FP64 pass (ncell entries; the cells with n materials queue
+  //    at the same offset as their segment of perm).
   const int *perm;
   unsigned *bins;
   int *retry_idx;

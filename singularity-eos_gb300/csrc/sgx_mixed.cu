@@ -6,13 +6,16 @@
 // scatter of cell ids into perm[] grouped by count -- so that each per-count
 // kernel runs full warps instead of masking off the lanes of the other
 // counts. Then, for each count N in turn: pass 1 (FP32 solve + FP64
-// refinement) over the N-bin, and pass 2 (FP64 re-solve) over the cells
-// pass 1 queued.
+// refinement) over the N-bin on the caller's stream, and pass 2 (FP64
+// re-solve) over the cells pass 1 queued on a side stream, overlapping the
+// next counts' pass 1.
 //
 // The scratch (a 256-byte counter block, perm[ncell], retry_idx[ncell]) is
 // stream-ordered memory from the library's pool (scratch_alloc /
 // scratch_free on the caller's stream), so calls on different streams never
 // share it.
+#include <mutex>
+
 #include <cuda_runtime.h>
 
 #include "sgx_internal.h"
@@ -78,6 +81,24 @@ __global__ void __launch_bounds__(BIN_BLOCK) pte_bin_scatter(const PteArgs a, in
   }
 }
 
+// The side streams of pass 2, a few per device, taken in turn (a stream in
+// one graph capture cannot join another); null if they cannot be created.
+cudaStream_t side_stream() {
+  constexpr int PER_DEV = 8, MAX_DEV = 64;
+  static std::mutex mu;
+  static cudaStream_t pool[MAX_DEV][PER_DEV] = {};
+  static unsigned next[MAX_DEV] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEV) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  const unsigned k = next[dev]++ % PER_DEV;
+  if (!pool[dev][k] && cudaStreamCreateWithFlags(&pool[dev][k], cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    pool[dev][k] = nullptr;
+  }
+  return pool[dev][k];
+}
+
 template <bool RETRY> cudaError_t launch_n(const int n, const PteArgs &a, cudaStream_t s) {
   switch (n) {
   case 1: return RETRY ? launch_pte_retry_n<1>(a, s) : launch_pte_mixed_n<1>(a, s);
@@ -114,11 +135,35 @@ cudaError_t launch_pte_mixed_with(const PteArgs &args, int *perm, cudaStream_t s
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     a.perm = perm;
   }
+  // Pass 1 of every count on the caller's stream; pass 2 of count n on a
+  // side stream once pass 1 of n is done. Pass 2 re-solves few cells but
+  // runs long (FP64 at the reference's iteration counts, up to the cap for
+  // cells that do not converge), so it overlaps pass 1 of the next counts
+  // instead of idling the GPU after each.
+  cudaStream_t side = side_stream();
+  if (!side) {
+    for (int n = lo; n <= hi && e == cudaSuccess; ++n) {
+      e = launch_n<false>(n, a, stream);
+      if (e == cudaSuccess) e = launch_n<true>(n, a, stream);
+    }
+    return e;
+  }
   for (int n = lo; n <= hi && e == cudaSuccess; ++n) {
     e = launch_n<false>(n, a, stream);
-    if (e == cudaSuccess) e = launch_n<true>(n, a, stream);
+    cudaEvent_t ev = nullptr;
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(ev, stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(side, ev, 0);
+    if (ev) cudaEventDestroy(ev);
+    if (e == cudaSuccess) e = launch_n<true>(n, a, side);
   }
-  return e;
+  // the caller's stream resumes after the last pass 2
+  cudaEvent_t join = nullptr;
+  cudaError_t j = cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
+  if (j == cudaSuccess) j = cudaEventRecord(join, side);
+  if (j == cudaSuccess) j = cudaStreamWaitEvent(stream, join, 0);
+  if (join) cudaEventDestroy(join);
+  return e != cudaSuccess ? e : j;
 }
 
 cudaError_t launch_pte_mixed(const PteArgs &a, cudaStream_t stream) {

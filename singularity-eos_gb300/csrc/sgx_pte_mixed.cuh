@@ -184,6 +184,17 @@ __device__ __forceinline__ void pte_store(const PteArgs &a, const long long i,
   }
 }
 
+// Where the cells with N materials start in perm[] (and in retry_idx[]):
+// the sum of the smaller counts (0 without an index map).
+template <int N> __device__ __forceinline__ unsigned pte_bin_offset(const PteArgs &a) {
+  if (!a.perm) return 0;
+  unsigned off = 0;
+#pragma unroll
+  for (int n = 0; n < N; ++n)
+    off += a.bins[n];
+  return off;
+}
+
 // Cell id of the t-th cell with N materials (false past the bin's end).
 template <int N> __device__ __forceinline__ bool pte_bin_cell(const PteArgs &a, long long t,
                                                               long long &i) {
@@ -191,12 +202,8 @@ template <int N> __device__ __forceinline__ bool pte_bin_cell(const PteArgs &a, 
     i = t;
     return t < a.ncell;
   }
-  unsigned off = 0;
-#pragma unroll
-  for (int n = 0; n < N; ++n)
-    off += a.bins[n];
   if (t >= a.bins[N]) return false;
-  i = a.perm[off + t];
+  i = a.perm[pte_bin_offset<N>(a) + t];
   return true;
 }
 
@@ -260,8 +267,10 @@ __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_kernel(const PteArg
     done = refine_cell<N>(f, R, steps);
   }
   if (!done) {
+    // each material count queues into its own segment of retry_idx, so
+    // that its pass 2 can run while pass 1 of the next count does
     const unsigned pos = atomicAdd(&a.bins[2 * PTE_BINS + N], 1u);
-    a.retry_idx[pos] = static_cast<int>(i);
+    a.retry_idx[pte_bin_offset<N>(a) + pos] = static_cast<int>(i);
     return;
   }
   PteStatusLocal st;
@@ -281,10 +290,10 @@ __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_kernel(const PteArg
   pte_store<N>(a, i, slot, R.rho, R.alpha, R.sie, out_T, out_P, cache, st, 0);
 }
 
-// Pass 2: the queued cells with N materials (pass 1 for N and pass 2 for N
-// run back to back on one stream, so the queue holds only them), FP64
-// reference iteration (:2188-2291) from the original inputs, then the same
-// FP64 refinement.
+// Pass 2: the queued cells with N materials (their own segment of the
+// queue), FP64 reference iteration (:2188-2291) from the original inputs,
+// then the same FP64 refinement.
+constexpr int RETRY_ITERS_PER_MAT = 32;
 template <int N>
 __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_retry_kernel(const PteArgs a) {
   __shared__ sgx_eos s_eos[MAX_EOS];
@@ -292,12 +301,19 @@ __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_retry_kernel(const PteArg
     s_eos[k] = a.eos[k];
   __syncthreads();
   const unsigned count = a.bins[2 * PTE_BINS + N];
+  const unsigned off = pte_bin_offset<N>(a);
   const long long nc = a.ncell;
-  const MixP<double> mp(a.params);
+  // The reference's iteration, capped at RETRY_ITERS_PER_MAT per material:
+  // cells that converge do so within ~50 iterations, while a cell that does
+  // not may run to the reference's 128 per material at FP64 latency, and
+  // the slowest such cell sets the kernel's length. A capped cell is
+  // reported unconverged, as the reference reports it.
+  MixP<double> mp(a.params);
+  if (mp.max_iter_per_mat > RETRY_ITERS_PER_MAT) mp.max_iter_per_mat = RETRY_ITERS_PER_MAT;
   const MixP<float> mp32 = fp32_params(a.params);
   for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < count;
        t += gridDim.x * blockDim.x) {
-    const long long i = a.retry_idx[t];
+    const long long i = a.retry_idx[off + t];
     int slot[MAX_NMAT], eidx[MAX_NMAT];
     if (pte_gather(a, i, slot, eidx) != N) continue;
     double cache[N][3];

@@ -1,5 +1,6 @@
-// One instantiation of the mixed-precision per-cell PTE kernel: SGX_PTE_N
-// materials per cell (set by the build, one object per value).
+// One instantiation of the mixed-precision per-cell PTE kernel (pass 1):
+// SGX_PTE_N materials per cell (set by the build, one object per value).
+// Pass 2 (the FP64 re-solve) is instantiated in sgx_pte_retry_n.cu.
 #include "sgx_pte_mixed.cuh"
 
 #ifndef SGX_PTE_N
@@ -8,5 +9,4 @@
 
 namespace sgx {
 template cudaError_t launch_pte_mixed_n<SGX_PTE_N>(const PteArgs &, cudaStream_t);
-template cudaError_t launch_pte_retry_n<SGX_PTE_N>(const PteArgs &, cudaStream_t);
 } // namespace sgx
