@@ -347,7 +347,7 @@ int sgx_tune_get(int knob, int *value);
  * callers that must not allocate device memory at solve time (host codes
  * that hand all device memory to their own allocator at start-up). It has
  * no reference counterpart. Arguments and results are those of
- * sgx_pte_solve; the solver's scratch (8 bytes per cell plus 256 bytes) is a
+ * sgx_pte_solve; the solver's scratch (8 bytes per cell plus 153 KiB) is a
  * static device array of the library sized for SGX_PTE_NOALLOC_MAX_CELLS
  * cells, so nothing is allocated.
  *  - ncell > SGX_PTE_NOALLOC_MAX_CELLS returns SGX_ERR_INVALID before any

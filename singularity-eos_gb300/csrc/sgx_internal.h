@@ -31,8 +31,9 @@ struct PteArgs {
   // Mixed path only (device scratch):
   //  - perm: cell ids grouped by material count, the cells with n materials
   //    at perm[sum(bins[0..n)) ...] (null when every cell holds nmat);
-  //  - bins[0..8): cells per material count; bins[8..16): scatter cursors;
-  //    bins[16..24): retry-queue length per material count;
+  //  - bins[0..8): cells per material count; bins[8..16): unused;
+  //    bins[16..24): retry-queue length per material count; from byte 256
+  //    the signature histogram and cursors (PTE_BINS_BYTES in all);
   //  - retry_idx: cells whose FP32 solve + FP64 refinement failed, queued for
   //    a second, FP64 pass (ncell entries; the cells with n materials queue
   //    at the same offset as their segment of perm).
@@ -41,6 +42,14 @@ struct PteArgs {
   int *retry_idx;
 };
 constexpr int PTE_BINS = 8;
+// Cells are binned by material count and by the ordered EOS types of their
+// materials (5 kinds that take part in PTE): 5^n signatures for n
+// materials, n-major, sum over n = 1..6.
+constexpr int PTE_SIG_KINDS = 5;
+constexpr int PTE_SIG_KEYS = 5 + 25 + 125 + 625 + 3125 + 15625;
+// The counter block of the mixed path: 3 * PTE_BINS counters (256 bytes),
+// then the signature histogram and its scatter cursors.
+constexpr size_t PTE_BINS_BYTES = 256 + 2 * PTE_SIG_KEYS * sizeof(unsigned);
 
 // Sets the calling thread's sgx_last_error() message; returns code.
 int set_error(int code, const std::string &msg);
@@ -57,8 +66,8 @@ cudaError_t scratch_free(void *p, cudaStream_t stream);
 cudaError_t launch_pte_fp64(const PteArgs &a, cudaStream_t stream);
 // Per-cell PTE, FP32 iterations then FP64 refinement.
 cudaError_t launch_pte_mixed(const PteArgs &a, cudaStream_t stream);
-// The same with caller-provided scratch: a.bins (3 * PTE_BINS counters),
-// a.retry_idx and, when a.eos_idx is set, perm (ncell ints each).
+// The same with caller-provided scratch: a.bins (PTE_BINS_BYTES), a.retry_idx
+// and, when a.eos_idx is set, perm (ncell ints each).
 cudaError_t launch_pte_mixed_with(const PteArgs &a, int *perm, cudaStream_t stream);
 // The same with the scratch in a static device array (sgx_noalloc.cu).
 cudaError_t launch_pte_mixed_noalloc(const PteArgs &a, cudaStream_t stream);

@@ -2,15 +2,15 @@
 // material count, built from sgx_pte_mixed_n.cu).
 //
 // With an index map (cells holding different numbers of materials), the
-// cells are first binned by material count -- a counting kernel, then a
-// scatter of cell ids into perm[] grouped by count -- so that each per-count
-// kernel runs full warps instead of masking off the lanes of the other
-// counts. Then, for each count N in turn: pass 1 (FP32 solve + FP64
+// cells are first binned by material count and, within a count, by the
+// ordered EOS kinds of their materials -- a counting kernel, a scan of the
+// signature histogram and a scatter of cell ids into perm[] -- so that each
+// per-count kernel runs full warps whose lanes take the same EOS branches. Then, for each count N in turn: pass 1 (FP32 solve + FP64
 // refinement) over the N-bin on the caller's stream, and pass 2 (FP64
 // re-solve) over the cells pass 1 queued on a side stream, overlapping the
 // next counts' pass 1.
 //
-// The scratch (a 256-byte counter block, perm[ncell], retry_idx[ncell]) is
+// The scratch (the counter block, perm[ncell], retry_idx[ncell]) is
 // stream-ordered memory from the library's pool (scratch_alloc /
 // scratch_free on the caller's stream), so calls on different streams never
 // share it.
@@ -29,55 +29,109 @@ namespace {
 
 constexpr int BIN_BLOCK = 256;
 
-__device__ __forceinline__ int pte_count(const PteArgs &a, const long long i) {
-  int n = 0;
+// The cell's material count and signature key: the ordered EOS kinds of
+// its present materials, base 5, offset by the keys of smaller counts (a
+// count above PTE_MAX_N gets key -1 and is left out, as the solve skips it).
+__device__ __forceinline__ int pte_key(const PteArgs &a, const sgx_eos *eos, const long long i,
+                                       int &n) {
+  int sig = 0, pw = 1;
+  n = 0;
   for (int m = 0; m < a.nmat; ++m) {
     const int ie = a.eos_idx[static_cast<long long>(m) * a.ncell + i];
-    n += (ie >= 0 && ie < a.neos) ? 1 : 0;
+    if (ie < 0 || ie >= a.neos) continue;
+    int kind = eos[ie].type - SGX_IDEAL_GAS;
+    kind = kind < 0 ? 0 : (kind >= PTE_SIG_KINDS ? PTE_SIG_KINDS - 1 : kind);
+    sig += kind * pw;
+    pw *= PTE_SIG_KINDS;
+    ++n;
   }
-  return n;
+  if (n < 1 || n > PTE_MAX_N) return -1;
+  // keys of counts 1..n-1: 5 + 25 + ... = (5^n - 5) / 4
+  return (pw - PTE_SIG_KINDS) / (PTE_SIG_KINDS - 1) + sig;
 }
 
-// bins[n] = number of cells with n materials.
+// bins[n] = cells with n materials; hist[key] = cells with that signature.
 __global__ void __launch_bounds__(BIN_BLOCK) pte_bin_count(const PteArgs a) {
   __shared__ unsigned h[PTE_BINS];
+  __shared__ sgx_eos s_eos[MAX_EOS];
+  for (int k = threadIdx.x; k < a.neos; k += blockDim.x)
+    s_eos[k] = a.eos[k];
   if (threadIdx.x < PTE_BINS) h[threadIdx.x] = 0;
   __syncthreads();
-  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
-  for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < a.ncell;
-       i += stride)
-    atomicAdd(&h[pte_count(a, i)], 1u);
-  __syncthreads();
-  if (threadIdx.x < PTE_BINS && h[threadIdx.x]) atomicAdd(&a.bins[threadIdx.x], h[threadIdx.x]);
-}
-
-// perm[offset(n) + k] = cell id, cells of equal count taken warp by warp
-// (ascending within a warp, so neighbouring lanes of the solve kernels
-// mostly touch nearby cells).
-__global__ void __launch_bounds__(BIN_BLOCK) pte_bin_scatter(const PteArgs a, int *perm) {
-  __shared__ unsigned off[PTE_BINS];
-  if (threadIdx.x == 0) {
-    unsigned s = 0;
-    for (int n = 0; n < PTE_BINS; ++n) {
-      off[n] = s;
-      s += a.bins[n];
-    }
-  }
-  __syncthreads();
-  unsigned *cursor = a.bins + PTE_BINS;
+  unsigned *hist = a.bins + 256 / sizeof(unsigned);
   const unsigned lane = threadIdx.x & 31u;
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
   // warp-uniform trip count: every lane runs every round
   for (long long base = static_cast<long long>(blockIdx.x) * blockDim.x; base < a.ncell;
        base += stride) {
     const long long i = base + threadIdx.x;
-    const int n = i < a.ncell ? pte_count(a, i) : -1;
-    const unsigned peers = __match_any_sync(0xffffffffu, n);
+    int n = 0;
+    const int key = i < a.ncell ? pte_key(a, s_eos, i, n) : -1;
+    if (i < a.ncell) atomicAdd(&h[n < PTE_BINS ? n : 0], 1u);
+    // one atomic per distinct key in the warp
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    if (key >= 0 && static_cast<int>(lane) == __ffs(peers) - 1)
+      atomicAdd(&hist[key], static_cast<unsigned>(__popc(peers)));
+  }
+  __syncthreads();
+  if (threadIdx.x < PTE_BINS && h[threadIdx.x]) atomicAdd(&a.bins[threadIdx.x], h[threadIdx.x]);
+}
+
+// Exclusive scan of the signature histogram into the cursors (one block):
+// cursor[key] = first position of that key's cells in perm. Keys are
+// count-major, so the cells of each count stay one contiguous segment, at
+// the offset the per-count kernels compute from bins[].
+constexpr int SCAN_BLOCK = 1024;
+__global__ void __launch_bounds__(SCAN_BLOCK) pte_sig_scan(const PteArgs a) {
+  __shared__ unsigned part[SCAN_BLOCK];
+  const unsigned *hist = a.bins + 256 / sizeof(unsigned);
+  unsigned *cursor = a.bins + 256 / sizeof(unsigned) + PTE_SIG_KEYS;
+  constexpr int PER = (PTE_SIG_KEYS + SCAN_BLOCK - 1) / SCAN_BLOCK;
+  const int k0 = threadIdx.x * PER;
+  unsigned sum = 0;
+  for (int k = k0; k < k0 + PER && k < PTE_SIG_KEYS; ++k)
+    sum += hist[k];
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  // Hillis-Steele inclusive scan of the partial sums
+  for (int d = 1; d < SCAN_BLOCK; d <<= 1) {
+    const unsigned v = threadIdx.x >= static_cast<unsigned>(d) ? part[threadIdx.x - d] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  // cells without a material (count 0) come first in the count order but
+  // have no signature: the keyed segments start after them
+  unsigned run = a.bins[0] + (threadIdx.x ? part[threadIdx.x - 1] : 0u);
+  for (int k = k0; k < k0 + PER && k < PTE_SIG_KEYS; ++k) {
+    cursor[k] = run;
+    run += hist[k];
+  }
+}
+
+// perm[cursor[key]++] = cell id, one atomic per distinct key in a warp
+// (ascending within a warp, so neighbouring lanes of the solve kernels
+// mostly touch nearby cells).
+__global__ void __launch_bounds__(BIN_BLOCK) pte_bin_scatter(const PteArgs a, int *perm) {
+  __shared__ sgx_eos s_eos[MAX_EOS];
+  for (int k = threadIdx.x; k < a.neos; k += blockDim.x)
+    s_eos[k] = a.eos[k];
+  __syncthreads();
+  unsigned *cursor = a.bins + 256 / sizeof(unsigned) + PTE_SIG_KEYS;
+  const unsigned lane = threadIdx.x & 31u;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long base = static_cast<long long>(blockIdx.x) * blockDim.x; base < a.ncell;
+       base += stride) {
+    const long long i = base + threadIdx.x;
+    int n = 0;
+    const int key = i < a.ncell ? pte_key(a, s_eos, i, n) : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
     const int leader = __ffs(peers) - 1;
     unsigned pos = 0;
-    if (n >= 0 && static_cast<int>(lane) == leader) pos = atomicAdd(&cursor[n], __popc(peers));
+    if (key >= 0 && static_cast<int>(lane) == leader)
+      pos = atomicAdd(&cursor[key], static_cast<unsigned>(__popc(peers)));
     pos = __shfl_sync(0xffffffffu, pos, leader);
-    if (n >= 0) perm[off[n] + pos + __popc(peers & ((1u << lane) - 1u))] = static_cast<int>(i);
+    if (key >= 0) perm[pos + __popc(peers & ((1u << lane) - 1u))] = static_cast<int>(i);
   }
 }
 
@@ -119,7 +173,7 @@ template <bool RETRY> cudaError_t launch_n(const int n, const PteArgs &a, cudaSt
 cudaError_t launch_pte_mixed_with(const PteArgs &args, int *perm, cudaStream_t stream) {
   PteArgs a = args;
   a.perm = nullptr;
-  cudaError_t e = cudaMemsetAsync(a.bins, 0, 3 * PTE_BINS * sizeof(unsigned), stream);
+  cudaError_t e = cudaMemsetAsync(a.bins, 0, a.eos_idx ? PTE_BINS_BYTES : 256, stream);
   if (e != cudaSuccess) return e;
   const int lo = a.eos_idx ? 1 : a.nmat;
   const int hi = a.nmat < PTE_MAX_N ? a.nmat : PTE_MAX_N;
@@ -131,6 +185,7 @@ cudaError_t launch_pte_mixed_with(const PteArgs &args, int *perm, cudaStream_t s
     const long long cap = 4LL * sms;
     const int grid = static_cast<int>(want < cap ? want : cap);
     pte_bin_count<<<grid, BIN_BLOCK, 0, stream>>>(a);
+    pte_sig_scan<<<1, SCAN_BLOCK, 0, stream>>>(a);
     pte_bin_scatter<<<grid, BIN_BLOCK, 0, stream>>>(a, perm);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     a.perm = perm;
@@ -173,13 +228,14 @@ cudaError_t launch_pte_mixed(const PteArgs &a, cudaStream_t stream) {
   PteArgs args = a;
   void *scratch = nullptr;
   const size_t n4 = ((static_cast<size_t>(a.ncell) * sizeof(int) + 255) / 256) * 256;
-  const size_t bytes = 256 + (a.eos_idx ? 2 : 1) * n4;
+  const size_t nb = (PTE_BINS_BYTES + 255) / 256 * 256;
+  const size_t bytes = nb + (a.eos_idx ? 2 : 1) * n4;
   cudaError_t e = scratch_alloc(&scratch, bytes, stream);
   if (e != cudaSuccess) return e;
   char *p = static_cast<char *>(scratch);
   args.bins = reinterpret_cast<unsigned *>(p);
-  args.retry_idx = reinterpret_cast<int *>(p + 256);
-  int *perm = a.eos_idx ? reinterpret_cast<int *>(p + 256 + n4) : nullptr;
+  args.retry_idx = reinterpret_cast<int *>(p + nb);
+  int *perm = a.eos_idx ? reinterpret_cast<int *>(p + nb + n4) : nullptr;
   e = launch_pte_mixed_with(args, perm, stream);
   const cudaError_t f = scratch_free(scratch, stream);
   return e != cudaSuccess ? e : f;

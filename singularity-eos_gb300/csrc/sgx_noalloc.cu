@@ -5,10 +5,10 @@
 // they will ever use for their own allocator and forbid allocations after
 // that. For them the stream-ordered pool allocation inside the mixed path of
 // sgx_pte_solve can fail, or break the memory budget they planned. Here the
-// scratch -- the 256-byte counter block, the cell ids binned by material
-// count and the retry queue, 8 bytes per cell -- is a static __device__
-// array sized for SGX_PTE_NOALLOC_MAX_CELLS cells (8 MiB + 256 B), part of
-// the module's image. No call here allocates device or pinned memory.
+// scratch -- the counter block with the signature histogram (153 KiB), the
+// cell ids binned by material count and the retry queue, 8 bytes per cell --
+// is a static __device__ array sized for SGX_PTE_NOALLOC_MAX_CELLS cells
+// (8 MiB + 153 KiB), part of the module's image. No call here allocates device or pinned memory.
 //
 // The array's device address is looked up once per device, with that device
 // current, and cached; the first call on a device does this look-up (which
@@ -25,7 +25,8 @@ namespace {
 
 constexpr size_t NOALLOC_IDS_BYTES =
     (static_cast<size_t>(SGX_PTE_NOALLOC_MAX_CELLS) * sizeof(int) + 255) / 256 * 256;
-constexpr size_t NOALLOC_BYTES = 256 + 2 * NOALLOC_IDS_BYTES;
+constexpr size_t NOALLOC_BINS = (sgx::PTE_BINS_BYTES + 255) / 256 * 256;
+constexpr size_t NOALLOC_BYTES = NOALLOC_BINS + 2 * NOALLOC_IDS_BYTES;
 
 } // namespace
 
@@ -69,8 +70,8 @@ cudaError_t launch_pte_mixed_noalloc(const PteArgs &a, cudaStream_t stream) {
   // cursors, queue lengths) on the stream before its first kernel; the id
   // arrays are written before they are read and need no clearing.
   args.bins = reinterpret_cast<unsigned *>(p);
-  args.retry_idx = reinterpret_cast<int *>(p + 256);
-  int *perm = a.eos_idx ? reinterpret_cast<int *>(p + 256 + NOALLOC_IDS_BYTES) : nullptr;
+  args.retry_idx = reinterpret_cast<int *>(p + NOALLOC_BINS);
+  int *perm = a.eos_idx ? reinterpret_cast<int *>(p + NOALLOC_BINS + NOALLOC_IDS_BYTES) : nullptr;
   return launch_pte_mixed_with(args, perm, stream);
 }
 

@@ -118,7 +118,7 @@ struct Layout {
     o += up(sizeof(sgx_pte_status) * n);
     bins = retry = perm = o;
     if (mixed) {
-      o += GRAIN; // 3 * PTE_BINS counters
+      o += up(PTE_BINS_BYTES); // counters and the signature histogram
       retry = o;
       o += up(4 * n);
       perm = o;
