@@ -319,7 +319,7 @@ int sgx_mix_enforce_energies_sum(int nmat, int64_t ncell, const int32_t *eos_idx
                                  const double *tot_rho, const double *tot_sie, const double *rho,
                                  const double *vfrac, double *sie, sgx_stream_t stream);
 
-/* Launch-shape knobs, process-wide. Results do not depend on them.
+/* Launch-shape and iteration knobs, process-wide.
  *  SGX_TUNE_LOOKUP_BLOCKS_PER_SM  4..6 (default 5): resident blocks per SM
  *      of the mixed-precision tabulated lookup (register budget 64/48/40).
  *  SGX_TUNE_LOOKUP_STAGE  0..2 (default 2): how that lookup stages the
@@ -330,12 +330,21 @@ int sgx_mix_enforce_energies_sum(int nmat, int64_t ncell, const int32_t *eos_idx
  *      L2 for persisting lines in this process's context).
  *  SGX_TUNE_HOST_FILL_STAGED  0/1 (default 0): sgx_eos_fill_host copies
  *      through device buffers even where the kernel could work on the host
- *      arrays in place. */
+ *      arrays in place.
+ *  SGX_TUNE_PTE_FP32_ITERS  2..64 (default 8): FP32 Newton iterations per
+ *      material in pass 1 of the mixed PTE path.
+ *  SGX_TUNE_PTE_RETRY_ITERS  4..128 (default 8): iterations per material of
+ *      the FP64 re-solve (pass 2) of the mixed PTE path; a cell that has not
+ *      converged by then is reported unconverged. These two change which
+ *      cells converge (never their converged values beyond the stated
+ *      tolerance); the others change nothing but speed. */
 enum {
   SGX_TUNE_LOOKUP_BLOCKS_PER_SM = 1,
   SGX_TUNE_LOOKUP_STAGE = 2,
   SGX_TUNE_L2_PERSIST = 3,
-  SGX_TUNE_HOST_FILL_STAGED = 4
+  SGX_TUNE_HOST_FILL_STAGED = 4,
+  SGX_TUNE_PTE_FP32_ITERS = 5,
+  SGX_TUNE_PTE_RETRY_ITERS = 6
 };
 int sgx_tune_set(int knob, int value);
 int sgx_tune_get(int knob, int *value);

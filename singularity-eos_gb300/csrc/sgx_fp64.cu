@@ -131,13 +131,25 @@ int grid_for(long long n, int block) {
 
 } // namespace
 
-cudaError_t launch_pte_fp64(const PteArgs &a, cudaStream_t stream) {
-  if (a.ncell <= 0) return cudaSuccess;
-  // Without an index map every cell holds exactly nmat materials.
+cudaError_t launch_pte_fp64_with(const PteArgs &args, unsigned *bins, int *perm,
+                                 cudaStream_t stream) {
+  if (args.ncell <= 0) return cudaSuccess;
+  PteArgs a = args;
+  a.perm = nullptr;
+  // Without an index map every cell holds exactly nmat materials; with one,
+  // the cells are binned by count and EOS-kind signature first
+  // (sgx_mixed.cu), so that each per-count kernel runs full warps.
+  cudaError_t e = cudaSuccess;
+  if (a.eos_idx) {
+    a.bins = bins;
+    e = cudaMemsetAsync(a.bins, 0, PTE_BINS_BYTES, stream);
+    if (e == cudaSuccess) e = launch_pte_binning(a, perm, stream);
+    if (e != cudaSuccess) return e;
+    a.perm = perm;
+  }
   const int lo = a.eos_idx ? 1 : a.nmat;
   const int hi = a.nmat < PTE_MAX_N ? a.nmat : PTE_MAX_N;
   const bool ext = a.solver != SGX_PTE_RHOT && a.solver != SGX_PTE_PT;
-  cudaError_t e = cudaSuccess;
   for (int n = lo; n <= hi && e == cudaSuccess; ++n) {
     switch (n) {
     case 1: e = ext ? launch_pte_ext_n<1>(a, stream) : launch_pte_fp64_n<1>(a, stream); break;
@@ -149,6 +161,20 @@ cudaError_t launch_pte_fp64(const PteArgs &a, cudaStream_t stream) {
     }
   }
   return e;
+}
+
+cudaError_t launch_pte_fp64(const PteArgs &a, cudaStream_t stream) {
+  if (a.ncell <= 0) return cudaSuccess;
+  if (!a.eos_idx) return launch_pte_fp64_with(a, nullptr, nullptr, stream);
+  if (a.ncell > 0x7fffffffLL) return cudaErrorInvalidValue; // int32 cell ids in perm
+  const size_t nb = (PTE_BINS_BYTES + 255) / 256 * 256;
+  void *scratch = nullptr;
+  cudaError_t e = scratch_alloc(&scratch, nb + static_cast<size_t>(a.ncell) * sizeof(int), stream);
+  if (e != cudaSuccess) return e;
+  e = launch_pte_fp64_with(a, static_cast<unsigned *>(scratch),
+                           reinterpret_cast<int *>(static_cast<char *>(scratch) + nb), stream);
+  const cudaError_t f = scratch_free(scratch, stream);
+  return e != cudaSuccess ? e : f;
 }
 
 cudaError_t launch_eval_fp64(const EvalArgs &a, cudaStream_t stream) {

@@ -40,6 +40,8 @@ struct PteArgs {
   const int *perm;
   unsigned *bins;
   int *retry_idx;
+  // iteration limits per material of pass 1 (FP32) and pass 2 (FP64)
+  int fp32_iters, retry_iters;
 };
 constexpr int PTE_BINS = 8;
 // Cells are binned by material count and by the ordered EOS types of their
@@ -64,6 +66,13 @@ cudaError_t scratch_free(void *p, cudaStream_t stream);
 
 // Per-cell PTE, FP64, following the reference iteration exactly.
 cudaError_t launch_pte_fp64(const PteArgs &a, cudaStream_t stream);
+// The same with caller-provided binning scratch when a.eos_idx is set: bins
+// (PTE_BINS_BYTES) and perm (ncell ints).
+cudaError_t launch_pte_fp64_with(const PteArgs &a, unsigned *bins, int *perm,
+                                 cudaStream_t stream);
+// Bins the cells of a (eos_idx set; a.bins zeroed, PTE_BINS_BYTES) by
+// material count and EOS-kind signature into perm (ncell ints).
+cudaError_t launch_pte_binning(const PteArgs &a, int *perm, cudaStream_t stream);
 // Per-cell PTE, FP32 iterations then FP64 refinement.
 cudaError_t launch_pte_mixed(const PteArgs &a, cudaStream_t stream);
 // The same with caller-provided scratch: a.bins (PTE_BINS_BYTES), a.retry_idx

@@ -167,27 +167,34 @@ template <bool RETRY> cudaError_t launch_n(const int n, const PteArgs &a, cudaSt
 
 } // namespace
 
+// The count, scan and scatter kernels of the binning (a.bins zeroed).
+cudaError_t launch_pte_binning(const PteArgs &a, int *perm, cudaStream_t stream) {
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long want = (a.ncell + BIN_BLOCK - 1) / BIN_BLOCK;
+  const long long cap = 4LL * sms;
+  const int grid = static_cast<int>(want < cap ? want : cap);
+  pte_bin_count<<<grid, BIN_BLOCK, 0, stream>>>(a);
+  pte_sig_scan<<<1, SCAN_BLOCK, 0, stream>>>(a);
+  pte_bin_scatter<<<grid, BIN_BLOCK, 0, stream>>>(a, perm);
+  return cudaGetLastError();
+}
+
 // Runs the binning and both passes with caller-provided scratch: bins (the
 // 3 * PTE_BINS counters), and perm (when eos_idx is set) and retry_idx of
 // ncell ints each.
 cudaError_t launch_pte_mixed_with(const PteArgs &args, int *perm, cudaStream_t stream) {
   PteArgs a = args;
   a.perm = nullptr;
+  a.fp32_iters = tune_get(SGX_TUNE_PTE_FP32_ITERS);
+  a.retry_iters = tune_get(SGX_TUNE_PTE_RETRY_ITERS);
   cudaError_t e = cudaMemsetAsync(a.bins, 0, a.eos_idx ? PTE_BINS_BYTES : 256, stream);
   if (e != cudaSuccess) return e;
   const int lo = a.eos_idx ? 1 : a.nmat;
   const int hi = a.nmat < PTE_MAX_N ? a.nmat : PTE_MAX_N;
   if (a.eos_idx) {
-    int dev = 0, sms = 152;
-    if (cudaGetDevice(&dev) == cudaSuccess)
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const long long want = (a.ncell + BIN_BLOCK - 1) / BIN_BLOCK;
-    const long long cap = 4LL * sms;
-    const int grid = static_cast<int>(want < cap ? want : cap);
-    pte_bin_count<<<grid, BIN_BLOCK, 0, stream>>>(a);
-    pte_sig_scan<<<1, SCAN_BLOCK, 0, stream>>>(a);
-    pte_bin_scatter<<<grid, BIN_BLOCK, 0, stream>>>(a, perm);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = launch_pte_binning(a, perm, stream)) != cudaSuccess) return e;
     a.perm = perm;
   }
   // Pass 1 of every count on the caller's stream; pass 2 of count n on a

@@ -72,6 +72,8 @@ Knob g_knobs[] = {
     {{2}, 0, 2}, // SGX_TUNE_LOOKUP_STAGE
     {{0}, 0, 1}, // SGX_TUNE_L2_PERSIST
     {{0}, 0, 1}, // SGX_TUNE_HOST_FILL_STAGED
+    {{8}, 2, 64},  // SGX_TUNE_PTE_FP32_ITERS
+    {{8}, 4, 128},  // SGX_TUNE_PTE_RETRY_ITERS
 };
 constexpr int NKNOBS = sizeof(g_knobs) / sizeof(g_knobs[0]);
 } // namespace

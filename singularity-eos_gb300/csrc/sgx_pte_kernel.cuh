@@ -1,7 +1,9 @@
 // The per-cell PTE kernel of the plain FP64 path, templated on the number of
 // materials N present in a cell. One launch per N covers the cells that hold
-// exactly N materials (the others return at once), so a warp never mixes
-// system sizes and each instantiation is compiled in its own translation unit.
+// exactly N materials, taken from their segment of the binned cell ids (by
+// count and EOS-kind signature, so a warp runs one system size and mostly
+// one set of EOS branches); each instantiation is compiled in its own
+// translation unit.
 //
 // One thread per cell: gather the cell's materials, run one of the solvers
 // (PTESolverRhoT, PTESolverPT, PTESolverFixedT, PTESolverFixedP,
@@ -35,14 +37,38 @@ __device__ __forceinline__ int pte_gather(const PteArgs &a, long long i, int (&s
   return n;
 }
 
+// Where the cells with N materials start in perm[] (and in retry_idx[]):
+// the sum of the smaller counts (0 without an index map).
+template <int N> __device__ __forceinline__ unsigned pte_bin_offset(const PteArgs &a) {
+  if (!a.perm) return 0;
+  unsigned off = 0;
+#pragma unroll
+  for (int n = 0; n < N; ++n)
+    off += a.bins[n];
+  return off;
+}
+
+// Cell id of the t-th cell with N materials (false past the bin's end).
+template <int N> __device__ __forceinline__ bool pte_bin_cell(const PteArgs &a, long long t,
+                                                              long long &i) {
+  if (!a.perm) {
+    i = t;
+    return t < a.ncell;
+  }
+  if (t >= a.bins[N]) return false;
+  i = a.perm[pte_bin_offset<N>(a) + t];
+  return true;
+}
+
 template <template <typename, int> class Solver, int N>
 __global__ void __launch_bounds__(PTE_BLOCK) pte_cell_kernel(const PteArgs a) {
   __shared__ sgx_eos s_eos[MAX_EOS];
   for (int k = threadIdx.x; k < a.neos; k += blockDim.x)
     s_eos[k] = a.eos[k];
   __syncthreads();
-  const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= a.ncell) return;
+  long long i;
+  if (!pte_bin_cell<N>(a, static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x, i))
+    return;
   int slot[MAX_NMAT], eidx[MAX_NMAT];
   if (pte_gather(a, i, slot, eidx) != N) return;
   const MixP<double> mp(a.params);

@@ -37,7 +37,7 @@ constexpr int SGX_REFINE_STEPS = 6;
 constexpr double SGX_REFINE_TOL = 1e-12;
 
 // FP32-phase controls: the reference's, with tolerances FP32 can reach.
-SGX_HDI MixP<float> fp32_params(const sgx_mix_params &q) {
+SGX_HDI MixP<float> fp32_params(const sgx_mix_params &q, const int iters_per_mat = 8) {
   MixP<float> m(q);
   m.derivative_eps = 2.5e-4f;
   m.tol_p = 1e-4f;
@@ -46,7 +46,7 @@ SGX_HDI MixP<float> fp32_params(const sgx_mix_params &q) {
   m.tol_p_suff = 1e-3f;
   m.tol_e_suff = 1e-3f;
   m.abs_p_suff = 1e-3f;
-  m.max_iter_per_mat = 8;
+  m.max_iter_per_mat = iters_per_mat;
   m.small_step_thresh = 1e-7f;
   return m;
 }
@@ -184,29 +184,6 @@ __device__ __forceinline__ void pte_store(const PteArgs &a, const long long i,
   }
 }
 
-// Where the cells with N materials start in perm[] (and in retry_idx[]):
-// the sum of the smaller counts (0 without an index map).
-template <int N> __device__ __forceinline__ unsigned pte_bin_offset(const PteArgs &a) {
-  if (!a.perm) return 0;
-  unsigned off = 0;
-#pragma unroll
-  for (int n = 0; n < N; ++n)
-    off += a.bins[n];
-  return off;
-}
-
-// Cell id of the t-th cell with N materials (false past the bin's end).
-template <int N> __device__ __forceinline__ bool pte_bin_cell(const PteArgs &a, long long t,
-                                                              long long &i) {
-  if (!a.perm) {
-    i = t;
-    return t < a.ncell;
-  }
-  if (t >= a.bins[N]) return false;
-  i = a.perm[pte_bin_offset<N>(a) + t];
-  return true;
-}
-
 // Pass 1: every cell with N materials, FP32 solve + FP64 refinement.
 template <int N>
 __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_kernel(const PteArgs a) {
@@ -222,7 +199,7 @@ __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_kernel(const PteArg
   const long long nc = a.ncell;
   double cache[N][3];
   // ---- FP32 phase ----
-  const MixP<float> mp32 = fp32_params(a.params);
+  const MixP<float> mp32 = fp32_params(a.params, a.fp32_iters);
   PteRhoT<float, N> f;
   f.P = &mp32;
   f.vfrac_total = static_cast<float>(a.vfrac_tot[i]);
@@ -293,7 +270,6 @@ __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_kernel(const PteArg
 // Pass 2: the queued cells with N materials (their own segment of the
 // queue), FP64 reference iteration (:2188-2291) from the original inputs,
 // then the same FP64 refinement.
-constexpr int RETRY_ITERS_PER_MAT = 32;
 template <int N>
 __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_retry_kernel(const PteArgs a) {
   __shared__ sgx_eos s_eos[MAX_EOS];
@@ -303,13 +279,13 @@ __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_retry_kernel(const PteArg
   const unsigned count = a.bins[2 * PTE_BINS + N];
   const unsigned off = pte_bin_offset<N>(a);
   const long long nc = a.ncell;
-  // The reference's iteration, capped at RETRY_ITERS_PER_MAT per material:
+  // The reference's iteration, capped at a.retry_iters per material:
   // cells that converge do so within ~50 iterations, while a cell that does
   // not may run to the reference's 128 per material at FP64 latency, and
   // the slowest such cell sets the kernel's length. A capped cell is
   // reported unconverged, as the reference reports it.
   MixP<double> mp(a.params);
-  if (mp.max_iter_per_mat > RETRY_ITERS_PER_MAT) mp.max_iter_per_mat = RETRY_ITERS_PER_MAT;
+  if (mp.max_iter_per_mat > a.retry_iters) mp.max_iter_per_mat = a.retry_iters;
   const MixP<float> mp32 = fp32_params(a.params);
   for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < count;
        t += gridDim.x * blockDim.x) {

@@ -117,10 +117,10 @@ struct Layout {
     status = o;
     o += up(sizeof(sgx_pte_status) * n);
     bins = retry = perm = o;
-    if (mixed) {
+    if (mixed || r.eos_idx) {
       o += up(PTE_BINS_BYTES); // counters and the signature histogram
       retry = o;
-      o += up(4 * n);
+      o += mixed ? up(4 * n) : 0;
       perm = o;
       o += r.eos_idx ? up(4 * n) : 0;
     }
@@ -220,7 +220,8 @@ struct Server {
         e = launch_pte_mixed_with(a, r.eos_idx ? reinterpret_cast<int *>(b + L.perm) : nullptr,
                                   s);
       } else {
-        e = launch_pte_fp64(a, s);
+        e = launch_pte_fp64_with(a, reinterpret_cast<unsigned *>(b + L.bins),
+                                 r.eos_idx ? reinterpret_cast<int *>(b + L.perm) : nullptr, s);
       }
     }
     double *out[5] = {r.rho_out, r.vfrac_out, r.sie_out, r.temp_out, r.press_out};
