@@ -87,10 +87,22 @@ enum {
   SGX_FN_MIN_SIE_FROM_RHO = 10 /* MinInternalEnergyFromDensity (in2 unused) */
 };
 
-/* One EOS instance: a 128-byte trivially copyable value (the analogue of the
+/* Modifier bits of sgx_eos.mods (eos/modifiers/). The reference's EOS
+ * variant holds a model, Shifted<model>, Scaled<model>,
+ * Scaled<Shifted<model>> and BilinearRamp<any of these>
+ * (eos/eos_type_lists.hpp:80-96), so the wrappers always nest as
+ * BilinearRamp(Scaled(Shifted(model))), outermost first. */
+enum {
+  SGX_MOD_SHIFTED = 1, /* ShiftedEOS (eos/modifiers/shifted_eos.hpp) */
+  SGX_MOD_SCALED = 2,  /* ScaledEOS (eos/modifiers/scaled_eos.hpp) */
+  SGX_MOD_RAMP = 4     /* BilinearRampEOS (eos/modifiers/ramps_eos.hpp) */
+};
+
+/* One EOS instance: a 208-byte trivially copyable value (the analogue of the
  * reference's GetOnDevice() copy). Analytic models keep their parameters in
  * p[]; tabulated models also hold a device table owned by the library, freed
- * by sgx_eos_finalize. */
+ * by sgx_eos_finalize. Modifiers are set by sgx_eos_modify_* and
+ * sgx_eos_apply_modifiers. */
 typedef struct sgx_eos {
   int32_t type;  /* SGX_* model code */
   int32_t flags; /* model options (Spiner: bit0 reproducibility mode;
@@ -101,6 +113,12 @@ typedef struct sgx_eos {
                     StiffGas:  gm1, Cv, Pinf, qq
                     NobleAbel: gm1, Cv, bb, qq
                     Gruneisen: C0, s1, s2, s3, G0, b, rho0, T0, P0, Cv, rho_max */
+  uint32_t mods;     /* SGX_MOD_* bits; 0 for a bare model */
+  uint32_t mods_reserved;
+  double shift;      /* ShiftedEOS shift_ */
+  double scale;      /* ScaledEOS scale_ */
+  double inv_scale;  /* ScaledEOS inv_scale_ = 1 / scale_ */
+  double ramp[6];    /* BilinearRampEOS r0_, a_, b_, c_, rmid_, Pmid_ */
 } sgx_eos;
 
 /* Field-for-field singularity::MixParams (mixed_cell_models.hpp:43-78). */
@@ -204,6 +222,39 @@ int sgx_eos_helmholtz(sgx_eos *out, const char *path, int options);
 /* Node values and fields of a Helmholtz table in the reference's DBLIST order
  * (rho_, T_, f_ .. xfdt_; eos_helmholtz.hpp:281-292); returns the count or -1. */
 long sgx_eos_helmholtz_dump(const sgx_eos *eos, double *out, long cap);
+/* ---- Modifiers (eos/modifiers/) ----
+ * Each wraps *eos in place, as eos.Modify<W>(args) does in the reference
+ * (eos_variant.hpp:213-223), and checks the wrapper's CheckParams. Only the nestings
+ * the reference's variant holds are accepted: Shifted of a bare model,
+ * Scaled of a bare or shifted model, BilinearRamp of any of those
+ * (SGX_ERR_UNSUPPORTED otherwise, and for Helmholtz). Modified EOS run on
+ * the FP64 paths; the mixed-precision paths return SGX_ERR_UNSUPPORTED. */
+/* ShiftedEOS(t, shift) (shifted_eos.hpp:53-61): shift must be a number. */
+int sgx_eos_modify_shifted(sgx_eos *eos, double shift);
+/* ScaledEOS(t, scale) (scaled_eos.hpp:53-66): scale and 1/scale nonzero
+ * and numbers. */
+int sgx_eos_modify_scaled(sgx_eos *eos, double scale);
+/* BilinearRampEOS(t, r0, a, b, c) (ramps_eos.hpp:86-104): r0 > 0, a > 0,
+ * b >= 0, a != b; rmid = r0 (a - b c) / (a - b) and Pmid = a (rmid/r0 - 1)
+ * must be numbers. */
+int sgx_eos_modify_bilinear_ramp(sgx_eos *eos, double r0, double a, double b, double c);
+/* pAlpha2BilinearRampParams (ramps_eos.hpp:43-77): the ramp through the
+ * p-alpha crush curve of *eos (alpha0 > 1, elastic limit Pe, full
+ * compaction Pc) from its reference state and two root finds of
+ * P(alpha0 rho, T0) = Pe and P(rho, T0) = Pc. The root finds run on the
+ * current device (tabulated models need their table there). */
+int sgx_eos_p_alpha_ramp_params(const sgx_eos *eos, double alpha0, double Pe, double Pc,
+                                double *r0, double *a, double *b, double *c);
+/* The modifier step of the reference's init_sg_* functions
+ * (singularity_eos.cpp:67-79 and the SGAPPLYMOD macros of
+ * singularity_eos_init_utils.hpp): enabled[0] scaled by vals[0],
+ * enabled[1] shifted by vals[1], enabled[2] a bilinear ramp with
+ * (r0, a, b, c) = vals[2..5], enabled[3] a ramp whose parameters come from
+ * sgx_eos_p_alpha_ramp_params(alpha0, Pe, Pc = vals[2..4]) of the shifted
+ * and scaled EOS and are written back into vals[2..5], as the reference
+ * does. Entries equal to 1 enable; *eos must be a bare model. */
+int sgx_eos_apply_modifiers(sgx_eos *eos, const int enabled[4], double vals[6]);
+
 /* Releases a tabulated EOS's device table (no-op for analytic models). */
 int sgx_eos_finalize(sgx_eos *eos);
 /* Size in bytes of the device table behind a tabulated EOS (0 if analytic). */

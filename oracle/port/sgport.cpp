@@ -1236,6 +1236,11 @@ struct sgref_eos {
   int32_t type, flags, matid, pad;
   double p[16];
   const char *path;
+  // modifiers (ShiftedEOS, ScaledEOS, BilinearRampEOS); this port restates
+  // bare models only and rejects a modified EOS
+  int32_t mods, pad2;
+  double shift, scale;
+  double ramp[4];
 };
 struct sgref_mix_params {
   int32_t verbose, iterate_t_guess;
@@ -1266,6 +1271,7 @@ std::map<std::string, port::Table> &tables() {
 bool make_eos(const sgref_eos *d, int n, std::vector<port::Eos> &out) {
   out.resize(n);
   for (int k = 0; k < n; ++k) {
+    if (d[k].mods != 0) return false;
     out[k].type = d[k].type;
     for (int q = 0; q < 16; ++q)
       out[k].p[q] = d[k].p[q];

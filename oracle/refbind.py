@@ -40,6 +40,11 @@ class EosDesc(C.Structure):
         ("pad", C.c_int32),
         ("p", C.c_double * 16),
         ("path", C.c_char_p),
+        ("mods", C.c_int32),
+        ("pad2", C.c_int32),
+        ("shift", C.c_double),
+        ("scale", C.c_double),
+        ("ramp", C.c_double * 4),
     ]
 
 
@@ -79,7 +84,10 @@ class MixParams(C.Structure):
     ]
 
 
-def eos_desc(type_, params=(), path=None, matid=0, flags=0):
+def eos_desc(type_, params=(), path=None, matid=0, flags=0, shift=None, scale=None,
+             ramp=None):
+    """An EOS description; shift / scale / ramp (r0, a, b, c) wrap the model
+    in ShiftedEOS / ScaledEOS / BilinearRampEOS, nested ramp(scaled(shifted))."""
     d = EosDesc()
     d.type = type_
     d.flags = flags
@@ -87,6 +95,16 @@ def eos_desc(type_, params=(), path=None, matid=0, flags=0):
     for i, v in enumerate(params):
         d.p[i] = float(v)
     d.path = path.encode() if path else None
+    if shift is not None:
+        d.mods |= 1
+        d.shift = float(shift)
+    if scale is not None:
+        d.mods |= 2
+        d.scale = float(scale)
+    if ramp is not None:
+        d.mods |= 4
+        for i, v in enumerate(ramp):
+            d.ramp[i] = float(v)
     return d
 
 
@@ -261,6 +279,29 @@ class Oracle:
         f.restype = C.c_int
         f(C.c_int(which), C.c_int(nmat), C.c_int(ncell), _ip(eos_idx), _dp(tot), _dp(tot_rho),
           _dp(rho), _dp(vfrac), _dp(sie))
+
+    def p_alpha(self, desc, alpha0, Pe, Pc):
+        """pAlpha2BilinearRampParams of the (shifted / scaled) EOS desc
+        (reference library only): returns (r0, a, b, c)."""
+        out = np.zeros(4)
+        f = self._fn("p_alpha")
+        f.restype = C.c_int
+        rc = f(C.byref(desc), C.c_double(alpha0), C.c_double(Pe), C.c_double(Pc), _dp(out))
+        if rc != 0:
+            raise RuntimeError("p_alpha failed")
+        return out
+
+    def init_mods(self, desc, enabled, vals):
+        """The modifier step of init_sg_* on the bare model of desc (reference
+        library only): returns vals as the reference leaves them."""
+        en = np.ascontiguousarray(enabled, np.int32)
+        v = np.ascontiguousarray(vals, np.float64).copy()
+        f = self._fn("init_mods")
+        f.restype = C.c_int
+        rc = f(C.byref(desc), _ip(en), _dp(v))
+        if rc != 0:
+            raise RuntimeError("init_mods failed")
+        return v
 
     def spiner_dump(self, path, matid):
         scal = np.zeros(8)

@@ -26,6 +26,7 @@
 
 #include <singularity-eos/closure/mixed_cell_models.hpp>
 #include <singularity-eos/eos/eos.hpp>
+#include <singularity-eos/eos/singularity_eos_init_utils.hpp>
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -44,6 +45,12 @@ struct sgref_eos {
   int32_t pad;
   double p[16];
   const char *path;
+  // modifiers: bit 0 ShiftedEOS(shift), bit 1 ScaledEOS(scale), bit 2
+  // BilinearRampEOS(ramp[0..3] = r0, a, b, c), nested ramp(scaled(shifted))
+  int32_t mods;
+  int32_t pad2;
+  double shift, scale;
+  double ramp[4];
 };
 
 // Field-for-field copy of singularity::MixParams (mixed_cell_models.hpp:43-78).
@@ -75,7 +82,7 @@ struct sgref_mix_params {
 
 namespace {
 
-EOS make_eos(const sgref_eos &d) {
+EOS make_model(const sgref_eos &d) {
   switch (d.type) {
   case 1:
     return IdealGas(d.p[0], d.p[1]);
@@ -95,6 +102,15 @@ EOS make_eos(const sgref_eos &d) {
   }
   PORTABLE_ALWAYS_THROW_OR_ABORT("sgref: unknown EOS type");
   return IdealGas(0.4, 1.0);
+}
+
+// The model wrapped by the Variant's own Modify (eos_variant.hpp:213-223).
+EOS make_eos(const sgref_eos &d) {
+  EOS eos = make_model(d);
+  if (d.mods & 1) eos = eos.Modify<ShiftedEOS>(d.shift);
+  if (d.mods & 2) eos = eos.Modify<ScaledEOS>(d.scale);
+  if (d.mods & 4) eos = eos.Modify<BilinearRampEOS>(d.ramp[0], d.ramp[1], d.ramp[2], d.ramp[3]);
+  return eos;
 }
 
 MixParams to_mix(const sgref_mix_params *q) {
@@ -417,6 +433,76 @@ int sgref_rho_sie_from_pt(const sgref_eos *desc, int n, const double *P, const d
     eos.Finalize();
   } catch (const std::exception &ex) {
     std::fprintf(stderr, "sgref_rho_sie_from_pt: %s\n", ex.what());
+    return 1;
+  }
+  return 0;
+}
+
+// pAlpha2BilinearRampParams (ramps_eos.hpp:43-77) of the EOS desc describes
+// (its shift and scale; a ramp in desc is ignored). out = r0, a, b, c.
+int sgref_p_alpha(const sgref_eos *desc, double alpha0, double Pe, double Pc, double *out) {
+  try {
+    sgref_eos d = *desc;
+    d.mods &= 3;
+    EOS eos = make_eos(d);
+    Real r0, a, b, c;
+    pAlpha2BilinearRampParams(eos, alpha0, Pe, Pc, r0, a, b, c);
+    out[0] = r0;
+    out[1] = a;
+    out[2] = b;
+    out[3] = c;
+    eos.Finalize();
+  } catch (const std::exception &ex) {
+    std::fprintf(stderr, "sgref_p_alpha: %s\n", ex.what());
+    return 1;
+  }
+  return 0;
+}
+
+// The modifier step of init_sg_IdealGas and its siblings
+// (singularity_eos.cpp:67-79), with the reference's own SGAPPLYMODSIMPLE /
+// SGAPPLYMOD macros (singularity_eos_init_utils.hpp), for the bare model of
+// desc: vals[2..5] are rewritten by the p-alpha conversion when enabled[3]
+// is 1, exactly as there.
+int sgref_init_mods(const sgref_eos *desc, const int *enabled, double *vals) {
+  auto run = [&](auto &&mk) {
+    EOS eosi = SGAPPLYMODSIMPLE(mk());
+    if (enabled[3] == 1) {
+      singularity::pAlpha2BilinearRampParams(eosi, vals[2], vals[3], vals[4], vals[2],
+                                             vals[3], vals[4], vals[5]);
+    }
+    EOS eos_ = SGAPPLYMOD(mk());
+    eos_.Finalize();
+    eosi.Finalize();
+  };
+  try {
+    const sgref_eos &d = *desc;
+    switch (d.type) {
+    case 1:
+      run([&] { return IdealGas(d.p[0], d.p[1]); });
+      break;
+    case 2:
+      run([&] { return StiffGas(d.p[0], d.p[1], d.p[2], d.p[3]); });
+      break;
+    case 3:
+      run([&] { return NobleAbel(d.p[0], d.p[1], d.p[2], d.p[3]); });
+      break;
+    case 4:
+      run([&] {
+        return Gruneisen(d.p[0], d.p[1], d.p[2], d.p[3], d.p[4], d.p[5], d.p[6], d.p[7],
+                         d.p[8], d.p[9]);
+      });
+      break;
+    case 5:
+      run([&] {
+        return SpinerEOSDependsRhoT(std::string(d.path), d.matid, (d.flags & 1) != 0);
+      });
+      break;
+    default:
+      return 1;
+    }
+  } catch (const std::exception &ex) {
+    std::fprintf(stderr, "sgref_init_mods: %s\n", ex.what());
     return 1;
   }
   return 0;

@@ -11,8 +11,20 @@
 #include <singularity-eos/eos/eos_noble_abel.hpp>
 #include <singularity-eos/eos/eos_spiner_rho_temp.hpp>
 #include <singularity-eos/eos/eos_stiff.hpp>
+#include <singularity-eos/eos/modifiers/ramps_eos.hpp>
+#include <singularity-eos/eos/modifiers/scaled_eos.hpp>
+#include <singularity-eos/eos/modifiers/shifted_eos.hpp>
 namespace singularity {
-using EOS = Variant<IdealGas, StiffGas, NobleAbel, Gruneisen, SpinerEOSDependsRhoT,
-                    Helmholtz>;
+// Each hot-path model bare, shifted, scaled and scaled-shifted, and each of
+// those under a bilinear ramp: the nestings of the reference's default
+// variant (eos_type_lists.hpp:80-96). Helmholtz is carried bare.
+#define SGX_ORACLE_MODS(M)                                                               \
+  M, ShiftedEOS<M>, ScaledEOS<M>, ScaledEOS<ShiftedEOS<M>>, BilinearRampEOS<M>,          \
+      BilinearRampEOS<ShiftedEOS<M>>, BilinearRampEOS<ScaledEOS<M>>,                     \
+      BilinearRampEOS<ScaledEOS<ShiftedEOS<M>>>
+using EOS = Variant<SGX_ORACLE_MODS(IdealGas), SGX_ORACLE_MODS(StiffGas),
+                    SGX_ORACLE_MODS(NobleAbel), SGX_ORACLE_MODS(Gruneisen),
+                    SGX_ORACLE_MODS(SpinerEOSDependsRhoT), Helmholtz>;
+#undef SGX_ORACLE_MODS
 } // namespace singularity
 #endif

@@ -30,11 +30,26 @@ int cuda_fail(cudaError_t e, const char *what) {
 bool valid_type(int t) { return t >= SGX_IDEAL_GAS && t <= SGX_HELMHOLTZ; }
 // Models the PTE kernels dispatch on (Helmholtz is a lookup-only model here).
 bool pte_type(int t) { return t >= SGX_IDEAL_GAS && t <= SGX_SPINER_RHOT; }
+// Modifier bits must be known ones; Helmholtz carries none; the
+// mixed-precision paths take bare models only.
+int check_mods(const sgx_eos &e, const bool mixed, const char *who) {
+  if (e.mods & ~static_cast<uint32_t>(SGX_MOD_SHIFTED | SGX_MOD_SCALED | SGX_MOD_RAMP))
+    return fail(SGX_ERR_INVALID, std::string(who) + ": unknown modifier bits");
+  if (e.mods && e.type == SGX_HELMHOLTZ)
+    return fail(SGX_ERR_UNSUPPORTED, std::string(who) + ": Helmholtz takes no modifiers");
+  if (e.mods && mixed)
+    return fail(SGX_ERR_UNSUPPORTED,
+                std::string(who) + ": the mixed-precision path takes unmodified EOS only");
+  return SGX_OK;
+}
 
 } // namespace
 
 namespace sgx {
 int set_error(int code, const std::string &msg) { return fail(code, msg); }
+int check_eos_mods(const sgx_eos &e, const bool mixed, const char *who) {
+  return check_mods(e, mixed, who);
+}
 } // namespace sgx
 
 extern "C" {
@@ -218,6 +233,7 @@ int sgx_eos_eval(const sgx_eos *eos, int fn, int64_t n, const double *in1, const
   if (!in1 || !out || (!in2 && fn != SGX_FN_MIN_SIE_FROM_RHO))
     return fail(SGX_ERR_INVALID, "sgx_eos_eval: null array");
   if (lambda && lambda_stride < 2) return fail(SGX_ERR_INVALID, "sgx_eos_eval: lambda_stride < 2");
+  if (const int rc = check_mods(*eos, false, "sgx_eos_eval")) return rc;
   if (eos->type == SGX_HELMHOLTZ) {
     // Abar and Zbar come in through lambda (SafeMustGet in the reference)
     if (!lambda || lambda_stride < 3)
@@ -253,6 +269,7 @@ int sgx_eos_fill_ex(const sgx_eos *eos, int64_t n, double *rho, double *temp, do
   if (lambda && lambda_stride < 2) return fail(SGX_ERR_INVALID, "sgx_eos_fill: lambda_stride < 2");
   if (precision != SGX_PREC_FP64 && precision != SGX_PREC_MIXED)
     return fail(SGX_ERR_INVALID, "sgx_eos_fill: bad precision");
+  if (const int rc = check_mods(*eos, precision == SGX_PREC_MIXED, "sgx_eos_fill")) return rc;
   if (eos->type == SGX_HELMHOLTZ) {
     // Helmholtz::FillEos (eos_helmholtz.hpp:818-865)
     if (!lambda || lambda_stride < 3)
@@ -330,6 +347,11 @@ int sgx_eos_fill_host(const sgx_eos *eos, int64_t n, double *rho, double *temp, 
                 {bmod, 1, !(output & SGX_Q_BULK_MODULUS), (output & SGX_Q_BULK_MODULUS) != 0},
                 {cs, 1, false, true},
                 {lambda, lambda_stride, true, true}};
+  // a modified EOS may write any quantity (see fill_kernel): every array goes
+  // both ways
+  if (eos->mods)
+    for (int k = 0; k < 6; ++k)
+      arr[k].in = arr[k].out = true;
   // On a coherent CPU-GPU system (the GPU walks the host's page tables, as on
   // Grace over NVLink-C2C) a kernel reads and writes page-locked host memory
   // at link bandwidth: run the fill in place on the mapped host arrays, the
@@ -442,6 +464,8 @@ int sgx_pte_solve(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list, 
     if (!valid_type(eos_list[k].type)) return fail(SGX_ERR_INVALID, "sgx_pte_solve: bad eos");
     else if (!pte_type(eos_list[k].type))
       return fail(SGX_ERR_UNSUPPORTED, "sgx_pte_solve: Helmholtz is not available in PTE");
+    else if (const int rc = check_mods(eos_list[k], precision == SGX_PREC_MIXED, "sgx_pte_solve"))
+      return rc;
   sgx::PteArgs a;
   std::memset(&a, 0, sizeof(a));
   a.solver = solver;
@@ -507,6 +531,8 @@ int sgx_pte_solve_noalloc(int solver, int nmat, int64_t ncell, const sgx_eos *eo
       return fail(SGX_ERR_INVALID, std::string(who) + ": bad eos");
     else if (!pte_type(eos_list[k].type))
       return fail(SGX_ERR_UNSUPPORTED, std::string(who) + ": Helmholtz is not available in PTE");
+    else if (const int rc = check_mods(eos_list[k], true, who))
+      return rc;
   sgx::PteArgs a;
   std::memset(&a, 0, sizeof(a));
   a.solver = solver;

@@ -3,12 +3,31 @@
 // models come from sgx_eos.cuh, the tabulated rho-T model from
 // sgx_spiner.cuh. `lam` is the per-element lambda row (nullable); only the
 // tabulated model reads or writes it.
+//
+// Two levels: md_* evaluates the bare model; ev_* (what every kernel calls)
+// adds the modifiers of sgx_eos.mods around it, nested as the reference's
+// variant nests them, BilinearRamp(Scaled(Shifted(model))). A bare model
+// (mods == 0) takes one predictable branch to md_*.
 #pragma once
 
 #include "sgx_eos.cuh"
 #include "sgx_spiner.cuh"
 
+// The translation units of the mixed-precision paths, which take bare models
+// only (the C API rejects a modified EOS there), define SGX_BARE_MODELS
+// before including this header: the modifier arithmetic compiles out of
+// their kernels. Their copy of the dispatch sits in its own inline namespace,
+// so the two variants of these inline functions never share a symbol.
+#ifdef SGX_BARE_MODELS
+#define SGX_MODS(e) 0u
+#define SGX_DISPATCH_BEGIN inline namespace bare_models {
+#else
+#define SGX_MODS(e) ((e).mods)
+#define SGX_DISPATCH_BEGIN inline namespace all_models {
+#endif
+
 namespace sgx {
+SGX_DISPATCH_BEGIN
 
 SGX_HD const SpinerTable &sp_table(const sgx_eos &e) {
   return *reinterpret_cast<const SpinerTable *>(static_cast<uintptr_t>(e.table));
@@ -16,94 +35,143 @@ SGX_HD const SpinerTable &sp_table(const sgx_eos &e) {
 SGX_HD bool is_spiner(const sgx_eos &e) { return e.type == SGX_SPINER_RHOT; }
 
 template <typename T>
-SGX_HD T ev_T_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
+SGX_HD T md_T_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
   if (is_spiner(e)) return T(sp_T_from_rho_sie(sp_table(e), double(rho), double(sie), lam));
   return eos_T_from_rho_sie<T>(e, rho, sie);
 }
 template <typename T>
-SGX_HD T ev_sie_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
+SGX_HD T md_sie_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
   if (is_spiner(e)) return T(sp_sie_from_rho_T(sp_table(e), double(rho), double(temp), lam));
   return eos_sie_from_rho_T<T>(e, rho, temp);
 }
 template <typename T>
-SGX_HD T ev_P_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
+SGX_HD T md_P_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
   if (is_spiner(e)) return T(sp_P_from_rho_T(sp_table(e), double(rho), double(temp), lam));
   return eos_P_from_rho_T<T>(e, rho, temp);
 }
 template <typename T>
-SGX_HD T ev_P_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
+SGX_HD T md_P_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
   if (is_spiner(e)) return T(sp_P_from_rho_sie(sp_table(e), double(rho), double(sie), lam));
   return eos_P_from_rho_sie<T>(e, rho, sie);
 }
 template <typename T>
-SGX_HD T ev_cv_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
+SGX_HD T md_cv_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
   if (is_spiner(e)) return T(sp_cv_from_rho_T(sp_table(e), double(rho), double(temp), lam));
   return eos_cv<T>(e);
 }
 template <typename T>
-SGX_HD T ev_cv_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
+SGX_HD T md_cv_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
   if (is_spiner(e)) return T(sp_cv_from_rho_sie(sp_table(e), double(rho), double(sie), lam));
   return eos_cv<T>(e);
 }
 template <typename T>
-SGX_HD T ev_B_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
+SGX_HD T md_B_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
   if (is_spiner(e)) return T(sp_bmod_from_rho_T(sp_table(e), double(rho), double(temp), lam));
   return eos_B_from_rho_T<T>(e, rho, temp);
 }
 template <typename T>
-SGX_HD T ev_B_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
+SGX_HD T md_B_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
   if (is_spiner(e)) return T(sp_bmod_from_rho_sie(sp_table(e), double(rho), double(sie), lam));
   return eos_B_from_rho_sie<T>(e, rho, sie);
 }
 template <typename T>
-SGX_HD T ev_gamma_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
+SGX_HD T md_gamma_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
   if (is_spiner(e)) return T(sp_gamma_from_rho_T(sp_table(e), double(rho), double(temp), lam));
   return eos_gamma<T>(e, rho);
 }
 template <typename T>
-SGX_HD T ev_gamma_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
+SGX_HD T md_gamma_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
   if (is_spiner(e)) return T(sp_gamma_from_rho_sie(sp_table(e), double(rho), double(sie), lam));
   return eos_gamma<T>(e, rho);
 }
-template <typename T> SGX_HD T ev_min_sie(const sgx_eos &e, T rho) {
+template <typename T> SGX_HD T md_min_sie(const sgx_eos &e, T rho) {
   if (is_spiner(e)) return T(sp_min_sie(sp_table(e), double(rho)));
   return eos_min_sie<T>(e, rho);
 }
 
 // Bounds (eos_base.hpp:594-613; SpinerEOSDependsRhoT :241-246, :1117-1123)
-SGX_HD double ev_min_temperature(const sgx_eos &e) {
+SGX_HD double md_min_temperature(const sgx_eos &e) {
   if (is_spiner(e)) return sp_T(sp_table(e), sp_table(e).lTMin);
   return eos_min_temperature(e);
 }
-SGX_HD double ev_max_density(const sgx_eos &e) {
+SGX_HD double md_max_density(const sgx_eos &e) {
   if (is_spiner(e)) return sp_table(e).rhoMax;
   return eos_max_density(e);
 }
-SGX_HD double ev_min_density(const sgx_eos &e) {
+SGX_HD double md_min_density(const sgx_eos &e) {
   if (is_spiner(e)) return sp_rho(sp_table(e), sp_table(e).lRhoMin);
   return 0;
 }
 // The temperature ValuesAtReferenceState reports (eos_ideal.hpp:178-190,
 // eos_stiff.hpp:153-164, eos_noble_abel.hpp:167-178: room temperature;
 // eos_gruneisen.hpp:554-567: T0; eos_spiner_rho_temp.hpp:1104-1115: TNormal_).
-SGX_HD double ev_reference_T(const sgx_eos &e) {
+SGX_HD double md_reference_T(const sgx_eos &e) {
   if (is_spiner(e)) return sp_table(e).TNormal;
   if (e.type == SGX_GRUNEISEN) return e.p[7];
   return ROOM_TEMPERATURE;
 }
-SGX_HD double ev_rho_pmin(const sgx_eos &e, const double T) {
+// Density, temperature, pressure and bulk modulus of ValuesAtReferenceState,
+// per model: eos_ideal.hpp:41-45 + :178-190 (STP: 1e6, room temperature),
+// eos_stiff.hpp:40-48 + :153-164, eos_noble_abel.hpp:40-48 + :167-178,
+// eos_gruneisen.hpp:554-567 (rho0, T0, and P, bmod at sie = 0),
+// eos_spiner_rho_temp.hpp:1104-1115 (the load-time normal state).
+SGX_HDI void md_reference_state(const sgx_eos &e, double &rho, double &temp, double &press,
+                                double &bmod) {
+  const double gm1 = e.p[pi::gm1], Cv = e.p[pi::Cv];
+  const double T0 = ROOM_TEMPERATURE, P0 = ATMOSPHERIC_PRESSURE;
+  switch (e.type) {
+  case SGX_IDEAL_GAS:
+    rho = P0 / (gm1 * Cv * T0);
+    temp = T0;
+    press = P0;
+    bmod = (gm1 + 1) * gm1 * rho * Cv * T0;
+    return;
+  case SGX_STIFF_GAS: {
+    const double Pinf = e.p[pi::Pinf];
+    rho = ratio(P0 + Pinf, gm1 * Cv * T0);
+    temp = T0;
+    press = P0;
+    bmod = gm1 * (gm1 + 1.0) * ratio(P0 + Pinf, gm1 * Cv * T0) * Cv * T0;
+    return;
+  }
+  case SGX_NOBLE_ABEL: {
+    const double bb = e.p[pi::bb];
+    rho = ratio(P0, gm1 * Cv * T0 + bb * P0);
+    temp = T0;
+    press = P0;
+    bmod = ratio(rho * Cv * T0 * gm1 * (gm1 + 1.0), (1.0 - bb * rho) * (1.0 - bb * rho));
+    return;
+  }
+  case SGX_GRUNEISEN:
+    rho = e.p[pi::rho0];
+    temp = e.p[pi::T0];
+    press = eos_P_from_rho_sie<double>(e, rho, 0.0);
+    bmod = eos_B_from_rho_sie<double>(e, rho, 0.0);
+    return;
+  case SGX_SPINER_RHOT: {
+    const SpinerTable &t = sp_table(e);
+    rho = t.rhoNormal;
+    temp = t.TNormal;
+    press = t.PNormal;
+    bmod = t.bModNormal;
+    return;
+  }
+  }
+  rho = temp = press = bmod = 0.0;
+}
+SGX_HD double md_rho_pmin(const sgx_eos &e, const double T) {
   if (is_spiner(e)) return sp_rho_pmin(sp_table(e), T);
   return eos_rho_pmin(e, T);
 }
-SGX_HD double ev_min_pressure(const sgx_eos &e) {
+SGX_HD double md_min_pressure(const sgx_eos &e) {
   if (is_spiner(e)) return sp_table(e).PMin;
   return eos_min_pressure(e);
 }
-SGX_HDI double ev_max_pressure_at_T(const sgx_eos &e, const double T, int *err) {
+SGX_HDI double md_max_pressure_at_T(const sgx_eos &e, const double T, int *err) {
   if (is_spiner(e)) return 1e100;
   return eos_max_pressure_at_T(e, T, err);
 }
-SGX_HDI void ev_rho_sie_from_PT(const sgx_eos &e, const double P, const double T, double &rho,
+SGX_HDI void md_rho_sie_from_PT(const sgx_eos &e, const double P, const double T, double &rho,
                                 double &sie, double *lam, int *err) {
   if (is_spiner(e)) {
     sp_rho_sie_from_PT(sp_table(e), P, T, rho, sie, lam);
@@ -117,7 +185,7 @@ SGX_HDI void ev_rho_sie_from_PT(const sgx_eos &e, const double P, const double T
 //   IdealGas  eos_ideal.hpp:236-262     StiffGas  eos_stiff.hpp:203-229
 //   NobleAbel eos_noble_abel.hpp:216-242  Gruneisen eos_gruneisen.hpp:527-546
 //   SpinerEOSDependsRhoT eos_spiner_rho_temp.hpp:1052-1101
-SGX_HDI void ev_fill(const sgx_eos &e, double &rho, double &temp, double &sie, double &press,
+SGX_HDI void md_fill(const sgx_eos &e, double &rho, double &temp, double &sie, double &press,
                      double &cv, double &bmod, const unsigned output, double *lam, int *err) {
   const double gm1 = e.p[pi::gm1];
   switch (e.type) {
@@ -215,6 +283,230 @@ SGX_HDI void ev_fill(const sgx_eos &e, double &rho, double &temp, double &sie, d
   *err = 1;
 }
 
+// ---------------------------------------------------------------------------
+// Modifiers (eos/modifiers/). Each reads its parameters from the sgx_eos
+// value; the arithmetic is the reference's, operation for operation.
+
+// BilinearRampEOS::get_ramp_pressure / get_ramp_density / get_ramp_dpdrho
+// (ramps_eos.hpp:113-133). ramp[] = r0, a, b, c, rmid, Pmid.
+SGX_HD double ramp_pressure(const sgx_eos &e, const double rho) {
+  const double r_r0 = ratio(rho, e.ramp[0]);
+  return rho < e.ramp[0]   ? 0.0
+         : rho < e.ramp[4] ? e.ramp[1] * (r_r0 - 1.0)
+                           : e.ramp[2] * (r_r0 - e.ramp[3]);
+}
+SGX_HD double ramp_density(const sgx_eos &e, const double P) {
+  return P < e.ramp[5] ? e.ramp[0] * (ratio(P, e.ramp[1]) + 1.0)
+                       : e.ramp[0] * (ratio(P, e.ramp[2]) + e.ramp[3]);
+}
+SGX_HD double ramp_dpdrho(const sgx_eos &e, const double rho) {
+  return rho < e.ramp[4] ? ratio(e.ramp[1], e.ramp[0]) : ratio(e.ramp[2], e.ramp[0]);
+}
+
+// Each ev_* below calls its md_* once, on the arguments the wrapped model
+// sees, and applies the modifiers' output arithmetic around that call, so a
+// kernel carries one copy of the model code whether or not an EOS is
+// modified. For T = float (the mixed-precision paths, which take bare
+// models only) the transforms are never active.
+template <typename T> SGX_HD T mrho(const sgx_eos &e, const T rho) {
+  return (SGX_MODS(e) & SGX_MOD_SCALED) ? T(e.scale) * rho : rho;
+}
+template <typename T> SGX_HD T msie(const sgx_eos &e, T sie) {
+  if (SGX_MODS(e) & SGX_MOD_SCALED) sie = T(e.inv_scale) * sie;
+  if (SGX_MODS(e) & SGX_MOD_SHIFTED) sie = sie - T(e.shift);
+  return sie;
+}
+// BilinearRampEOS pressure (ramps_eos.hpp:149-154, 186-191): the ramp's
+// pressure where the EOS lies below it.
+template <typename T> SGX_HD T ramp_max(const sgx_eos &e, const T rho, const T p_eos) {
+  if (!(SGX_MODS(e) & SGX_MOD_RAMP)) return p_eos;
+  const T p_ramp = T(ramp_pressure(e, double(rho)));
+  return p_eos < p_ramp ? p_ramp : p_eos;
+}
+// BilinearRampEOS bulk modulus (ramps_eos.hpp:170-181, 203-212): below the
+// ramp, rho times the ramp's slope; the wrapped pressure decides.
+SGX_HDN bool ramp_below_rho_sie(const sgx_eos &e, const double rho, const double r,
+                                const double s, double *lam) {
+  const double p_ramp = ramp_pressure(e, rho);
+  const double p_eos = md_P_from_rho_sie<double>(e, r, s, lam);
+  return p_eos < p_ramp;
+}
+SGX_HDN bool ramp_below_rho_T(const sgx_eos &e, const double rho, const double r,
+                              const double temp, double *lam) {
+  const double p_ramp = ramp_pressure(e, rho);
+  const double p_eos = md_P_from_rho_T<double>(e, r, temp, lam);
+  return p_eos < p_ramp;
+}
+
+// Functions of (rho, sie): ScaledEOS passes (scale_ rho, sie / scale_)
+// (scaled_eos.hpp:68-133), ShiftedEOS sie - shift_ (shifted_eos.hpp:66-106).
+template <typename T>
+SGX_HD T ev_T_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
+  return md_T_from_rho_sie<T>(e, mrho(e, rho), msie(e, sie), lam);
+}
+template <typename T>
+SGX_HD T ev_P_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
+  return ramp_max(e, rho, md_P_from_rho_sie<T>(e, mrho(e, rho), msie(e, sie), lam));
+}
+template <typename T>
+SGX_HD T ev_cv_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
+  return md_cv_from_rho_sie<T>(e, mrho(e, rho), msie(e, sie), lam);
+}
+template <typename T>
+SGX_HD T ev_B_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
+  const T r = mrho(e, rho), s = msie(e, sie);
+  if ((SGX_MODS(e) & SGX_MOD_RAMP) && ramp_below_rho_sie(e, double(rho), double(r), double(s), lam))
+    return rho * T(ramp_dpdrho(e, double(rho)));
+  return md_B_from_rho_sie<T>(e, r, s, lam);
+}
+template <typename T>
+SGX_HD T ev_gamma_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
+  return md_gamma_from_rho_sie<T>(e, mrho(e, rho), msie(e, sie), lam);
+}
+// Functions of (rho, T): ScaledEOS passes scale_ rho.
+template <typename T>
+SGX_HD T ev_P_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
+  return ramp_max(e, rho, md_P_from_rho_T<T>(e, mrho(e, rho), temp, lam));
+}
+template <typename T>
+SGX_HD T ev_cv_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
+  return md_cv_from_rho_T<T>(e, mrho(e, rho), temp, lam);
+}
+template <typename T>
+SGX_HD T ev_B_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
+  const T r = mrho(e, rho);
+  if ((SGX_MODS(e) & SGX_MOD_RAMP) && ramp_below_rho_T(e, double(rho), double(r), double(temp), lam))
+    return rho * T(ramp_dpdrho(e, double(rho)));
+  return md_B_from_rho_T<T>(e, r, temp, lam);
+}
+template <typename T>
+SGX_HD T ev_gamma_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
+  return md_gamma_from_rho_T<T>(e, mrho(e, rho), temp, lam);
+}
+// InternalEnergyFromDensityTemperature: ShiftedEOS adds shift_
+// (shifted_eos.hpp:72-76); ScaledEOS multiplies by scale_ and passes rho
+// unscaled (scaled_eos.hpp:77-81).
+template <typename T>
+SGX_HD T ev_sie_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
+  T energy = md_sie_from_rho_T<T>(e, rho, temp, lam);
+  if (SGX_MODS(e) & SGX_MOD_SHIFTED) energy = energy + T(e.shift);
+  if (SGX_MODS(e) & SGX_MOD_SCALED) energy = T(e.scale) * energy;
+  return energy;
+}
+// MinInternalEnergyFromDensity: ScaledEOS passes scale_ rho and leaves the
+// result unscaled (scaled_eos.hpp:84-88); ShiftedEOS adds shift_ (:83-86).
+template <typename T> SGX_HD T ev_min_sie(const sgx_eos &e, T rho) {
+  T m = md_min_sie<T>(e, mrho(e, rho));
+  if (SGX_MODS(e) & SGX_MOD_SHIFTED) m = m + T(e.shift);
+  return m;
+}
+
+// Bounds. ScaledEOS divides the density bounds by scale_
+// (scaled_eos.hpp:254-275); ShiftedEOS and BilinearRampEOS forward them
+// (SG_ADD_MODIFIER_INTROSPECTION_METHODS, eos_base.hpp:134-153;
+// ramps_eos.hpp:248-265).
+SGX_HD double ev_min_temperature(const sgx_eos &e) { return md_min_temperature(e); }
+SGX_HD double ev_max_density(const sgx_eos &e) {
+  return (SGX_MODS(e) & SGX_MOD_SCALED) ? e.inv_scale * md_max_density(e) : md_max_density(e);
+}
+SGX_HD double ev_min_density(const sgx_eos &e) {
+  return (SGX_MODS(e) & SGX_MOD_SCALED) ? e.inv_scale * md_min_density(e) : md_min_density(e);
+}
+SGX_HD double ev_rho_pmin(const sgx_eos &e, const double T) {
+  return (SGX_MODS(e) & SGX_MOD_SCALED) ? e.inv_scale * md_rho_pmin(e, T) : md_rho_pmin(e, T);
+}
+SGX_HD double ev_min_pressure(const sgx_eos &e) { return md_min_pressure(e); }
+SGX_HDI double ev_max_pressure_at_T(const sgx_eos &e, const double T, int *err) {
+  return md_max_pressure_at_T(e, T, err);
+}
+// The temperature of ValuesAtReferenceState; no modifier changes it.
+SGX_HD double ev_reference_T(const sgx_eos &e) { return md_reference_T(e); }
+// ValuesAtReferenceState through the modifiers: ScaledEOS divides rho by
+// scale_ (scaled_eos.hpp:183-190); P, T and bmod pass through
+// (shifted_eos.hpp:406-412, ramps_eos.hpp:528-533).
+SGX_HDI void ev_reference_state(const sgx_eos &e, double &rho, double &temp, double &press,
+                                double &bmod) {
+  md_reference_state(e, rho, temp, press, bmod);
+  if (SGX_MODS(e) & SGX_MOD_SCALED) rho = rho * e.inv_scale;
+}
+// DensityEnergyFromPressureTemperature: ShiftedEOS adds shift_ to sie
+// (shifted_eos.hpp:398-403), ScaledEOS then divides rho and multiplies sie
+// by scale_ (scaled_eos.hpp:244-250); BilinearRampEOS forwards (:521-525).
+SGX_HDI void ev_rho_sie_from_PT(const sgx_eos &e, const double P, const double T, double &rho,
+                                double &sie, double *lam, int *err) {
+  md_rho_sie_from_PT(e, P, T, rho, sie, lam, err);
+  if (SGX_MODS(e) & SGX_MOD_SHIFTED) sie = sie + e.shift;
+  if (SGX_MODS(e) & SGX_MOD_SCALED) {
+    rho = rho * e.inv_scale;
+    sie = sie * e.scale;
+  }
+}
+
+// FillEos through the modifiers. ShiftedEOS and ScaledEOS switch on the
+// model's PreferredInput and abort on any value but rho-T or rho-sie
+// (shifted_eos.hpp:150-167, scaled_eos.hpp:160-181), which takes in
+// IdealGas (it prefers all four); the abort becomes *err = 1 here.
+SGX_HDI void fill_shifted(const sgx_eos &e, double &rho, double &temp, double &sie,
+                          double &press, double &cv, double &bmod, const unsigned output,
+                          double *lam, int *err) {
+  if (!(SGX_MODS(e) & SGX_MOD_SHIFTED)) {
+    md_fill(e, rho, temp, sie, press, cv, bmod, output, lam, err);
+    return;
+  }
+  const unsigned pref = preferred_input(e);
+  if (pref == (Q_DENSITY | Q_TEMPERATURE)) {
+    md_fill(e, rho, temp, sie, press, cv, bmod, output, lam, err);
+    sie = sie + e.shift;
+  } else if (pref == (Q_DENSITY | Q_SIE)) {
+    double senergy = sie - e.shift;
+    md_fill(e, rho, temp, senergy, press, cv, bmod, output, lam, err);
+  } else {
+    *err = 1;
+  }
+}
+SGX_HDI void fill_scaled(const sgx_eos &e, double &rho, double &temp, double &sie,
+                         double &press, double &cv, double &bmod, const unsigned output,
+                         double *lam, int *err) {
+  if (!(SGX_MODS(e) & SGX_MOD_SCALED)) {
+    fill_shifted(e, rho, temp, sie, press, cv, bmod, output, lam, err);
+    return;
+  }
+  const unsigned pref = preferred_input(e);
+  double srho = e.scale * rho;
+  if (pref == (Q_DENSITY | Q_TEMPERATURE)) {
+    fill_shifted(e, srho, temp, sie, press, cv, bmod, output, lam, err);
+    sie = e.scale * sie;
+  } else if (pref == (Q_DENSITY | Q_SIE)) {
+    double senergy = e.inv_scale * sie;
+    fill_shifted(e, srho, temp, senergy, press, cv, bmod, output, lam, err);
+  } else {
+    *err = 1;
+  }
+}
+// BilinearRampEOS::FillEos (ramps_eos.hpp:221-243): the pressure comes from
+// the ramped P(rho, sie) or P(rho, T), the wrapped EOS fills the rest, a
+// density output is capped by the ramp's density at that pressure, and
+// bmod is always recomputed from the ramped bulk modulus.
+SGX_HDI void ev_fill(const sgx_eos &e, double &rho, double &temp, double &sie, double &press,
+                     double &cv, double &bmod, const unsigned output, double *lam, int *err) {
+  if (!(SGX_MODS(e) & SGX_MOD_RAMP)) {
+    fill_scaled(e, rho, temp, sie, press, cv, bmod, output, lam, err);
+    return;
+  }
+  const unsigned ramp_out = output & ~Q_PRESSURE;
+  if (output & Q_PRESSURE) {
+    if (!(output & Q_SIE))
+      press = ev_P_from_rho_sie<double>(e, rho, sie, lam);
+    else if (!(output & Q_TEMPERATURE))
+      press = ev_P_from_rho_T<double>(e, rho, temp, lam);
+  }
+  fill_scaled(e, rho, temp, sie, press, cv, bmod, ramp_out, lam, err);
+  double rho_ramp = rho;
+  if (output & Q_DENSITY) rho_ramp = ramp_density(e, press);
+  rho = rho_ramp < rho ? rho_ramp : rho;
+  bmod = ev_B_from_rho_sie<double>(e, rho, sie, lam);
+}
+
 // One vector-lookup element (EosBase vector members, eos_base.hpp:421-494).
 SGX_HDI double ev_eval(const sgx_eos &e, const int fn, const double a, const double b,
                        double *lam) {
@@ -245,4 +537,5 @@ SGX_HDI double ev_eval(const sgx_eos &e, const int fn, const double a, const dou
   return 0.0;
 }
 
+} // inline namespace
 } // namespace sgx

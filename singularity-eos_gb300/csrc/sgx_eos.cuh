@@ -304,7 +304,7 @@ template <typename T> SGX_HD T eos_min_sie(const sgx_eos &e, const T rho) {
 // Partial derivatives of sie(rho, T) and P(rho, T) of the analytic models,
 // for the Jacobian of the mixed-precision solver, where finite differences in
 // FP32 cannot resolve a thermal energy that is small against a cold one.
-// Returns false for tabulated models.
+// Returns false for tabulated and modified models.
 //   IdealGas  e = Cv T, P = gm1 rho Cv T
 //   StiffGas  e = Cv T + Pinf/rho + q, P = gm1 rho Cv T - Pinf
 //   NobleAbel e = Cv T + q, P = gm1 rho Cv T / (1 - b rho)
@@ -312,6 +312,7 @@ template <typename T> SGX_HD T eos_min_sie(const sgx_eos &e, const T rho) {
 template <typename T>
 SGX_HD bool eos_derivs(const sgx_eos &e, const T rho, const T temp, T &de_drho, T &de_dT,
                        T &dP_drho, T &dP_dT) {
+  if (e.mods) return false; // modified models differentiate by finite differences
   const T gm1 = T(e.p[pi::gm1]), Cv = T(e.p[pi::Cv]);
   switch (e.type) {
   case SGX_IDEAL_GAS:

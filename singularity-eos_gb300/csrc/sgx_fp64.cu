@@ -41,17 +41,26 @@ __global__ void fill_kernel(const FillArgs a) {
     double sie = a.sie ? a.sie[i] : 0.0;
     double press = a.press ? a.press[i] : 0.0;
     double cv = 0.0, bmod = 0.0;
+    if (e.mods) {
+      cv = a.cv ? a.cv[i] : 0.0;
+      bmod = a.bmod ? a.bmod[i] : 0.0;
+    }
     double *lam = a.lambda ? a.lambda + i * a.lambda_stride : nullptr;
     int err = 0;
     ev_fill(e, rho, temp, sie, press, cv, bmod, a.output | (a.cs ? Q_BMOD : 0u), lam, &err);
     bad |= err;
     if (a.cs) a.cs[i] = sqrt(bmod / rho);
-    if ((a.output & Q_DENSITY) && a.rho) a.rho[i] = rho;
-    if ((a.output & Q_TEMPERATURE) && a.temp) a.temp[i] = temp;
-    if ((a.output & Q_SIE) && a.sie) a.sie[i] = sie;
-    if ((a.output & Q_PRESSURE) && a.press) a.press[i] = press;
-    if ((a.output & Q_CV) && a.cv) a.cv[i] = cv;
-    if ((a.output & Q_BMOD) && a.bmod) a.bmod[i] = bmod;
+    // The reference's FillEos takes every quantity by reference; a modifier
+    // can write one that is not an output (ShiftedEOS adds its shift to an
+    // input sie of a rho-T model, BilinearRampEOS always rewrites bmod), so
+    // a modified EOS writes back every array it was given.
+    const unsigned wb = e.mods ? ~0u : a.output;
+    if ((wb & Q_DENSITY) && a.rho) a.rho[i] = rho;
+    if ((wb & Q_TEMPERATURE) && a.temp) a.temp[i] = temp;
+    if ((wb & Q_SIE) && a.sie) a.sie[i] = sie;
+    if ((wb & Q_PRESSURE) && a.press) a.press[i] = press;
+    if ((wb & Q_CV) && a.cv) a.cv[i] = cv;
+    if ((wb & Q_BMOD) && a.bmod) a.bmod[i] = bmod;
   }
   if (bad && a.err) atomicOr(a.err, 1);
 }

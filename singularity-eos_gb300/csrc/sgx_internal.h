@@ -55,6 +55,10 @@ constexpr size_t PTE_BINS_BYTES = 256 + 2 * PTE_SIG_KEYS * sizeof(unsigned);
 
 // Sets the calling thread's sgx_last_error() message; returns code.
 int set_error(int code, const std::string &msg);
+// SGX_OK, or the error (with its message set) for an EOS whose modifier bits
+// are unknown, that is Helmholtz with modifiers, or that has modifiers on a
+// mixed-precision path.
+int check_eos_mods(const sgx_eos &e, bool mixed, const char *who);
 
 // Tuning knobs (sgx_tune_set); the value a launcher uses now.
 int tune_get(int knob);

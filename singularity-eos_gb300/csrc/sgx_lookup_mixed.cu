@@ -43,6 +43,8 @@
 // without spilling. Predicates on doubles are integer tests of the bit
 // patterns, so the FP64 pipe sees only the nine roundings that must be the
 // reference's.
+// a mixed-precision path: bare models only (see sgx_dispatch.cuh)
+#define SGX_BARE_MODELS
 #include <mutex>
 
 #include <cuda_runtime.h>

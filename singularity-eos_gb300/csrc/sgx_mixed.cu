@@ -5,7 +5,8 @@
 // cells are first binned by material count and, within a count, by the
 // ordered EOS kinds of their materials -- a counting kernel, a scan of the
 // signature histogram and a scatter of cell ids into perm[] -- so that each
-// per-count kernel runs full warps whose lanes take the same EOS branches. Then, for each count N in turn: pass 1 (FP32 solve + FP64
+// per-count kernel runs full warps whose lanes take the same EOS branches.
+// Then, for each count N in turn: pass 1 (FP32 solve + FP64
 // refinement) over the N-bin on the caller's stream, and pass 2 (FP64
 // re-solve) over the cells pass 1 queued on a side stream, overlapping the
 // next counts' pass 1.
@@ -14,6 +15,8 @@
 // stream-ordered memory from the library's pool (scratch_alloc /
 // scratch_free on the caller's stream), so calls on different streams never
 // share it.
+// a mixed-precision path: bare models only (see sgx_dispatch.cuh)
+#define SGX_BARE_MODELS
 #include <mutex>
 
 #include <cuda_runtime.h>

@@ -1,6 +1,8 @@
 // One instantiation of the mixed-precision per-cell PTE kernel (pass 1):
 // SGX_PTE_N materials per cell (set by the build, one object per value).
 // Pass 2 (the FP64 re-solve) is instantiated in sgx_pte_retry_n.cu.
+// a mixed-precision path: bare models only (see sgx_dispatch.cuh)
+#define SGX_BARE_MODELS
 #include "sgx_pte_mixed.cuh"
 
 #ifndef SGX_PTE_N

@@ -4,6 +4,8 @@
 // iteration rounds as the reference does: a cell that does not converge
 // then stops where the reference stops (most within 50 iterations) instead
 // of wandering to the iteration cap.
+// a mixed-precision path: bare models only (see sgx_dispatch.cuh)
+#define SGX_BARE_MODELS
 #include "sgx_pte_mixed.cuh"
 
 #ifndef SGX_PTE_N

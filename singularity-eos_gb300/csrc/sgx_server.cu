@@ -328,6 +328,10 @@ int sgx_server_create(const sgx_server_config *cfg, sgx_server **out) {
   for (int k = 0; k < cfg->neos; ++k)
     if (cfg->eos_list[k].type < SGX_IDEAL_GAS || cfg->eos_list[k].type > SGX_SPINER_RHOT)
       return set_error(SGX_ERR_UNSUPPORTED, "sgx_server_create: EOS not available in PTE");
+    else if (const int rc = sgx::check_eos_mods(cfg->eos_list[k],
+                                                cfg->precision == SGX_PREC_MIXED,
+                                                "sgx_server_create"))
+      return rc;
   if (cfg->hbm_budget_bytes < (1u << 20))
     return set_error(SGX_ERR_INVALID, "sgx_server_create: hbm_budget_bytes below 1 MiB");
   auto *h = new sgx_server;

@@ -299,6 +299,8 @@ extern "C" int sgx_get_sg_eos(int nmat, int ncell, int cell_dim, int input_int,
   for (int k = 0; k < neos; ++k) {
     if (eos[k].type < SGX_IDEAL_GAS || eos[k].type > SGX_SPINER_RHOT)
       return set_error(SGX_ERR_UNSUPPORTED, "sgx_get_sg_eos: EOS not available in PTE");
+    if (const int rc = check_eos_mods(eos[k], precision == SGX_PREC_MIXED, "sgx_get_sg_eos"))
+      return rc;
     a.eos[k] = eos[k];
   }
   for (int m = 0; m < nmat; ++m) {

@@ -73,6 +73,8 @@ struct SpinerTable {
   Grid1D gT, gRho, gCold; // T grid (fastest), rho grid, cold-curve grid
   double lRhoMin, lRhoMax, rhoMax, lTMin, lTMax, TMax, PMin, lRhoOffset, lTOffset;
   double TNormal; // reference-state temperature (ValuesAtReferenceState)
+  // reference-state density, pressure and bulk modulus (:663-684)
+  double rhoNormal, PNormal, bModNormal;
   double TatlTMin; // T_(lTMin_): the temperature returned off the table's bottom
   int nRho, nT;
   int reproducible;

@@ -324,13 +324,22 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
   // reference-state temperature: room temperature if it lies inside the
   // table, else the middle of the log-T range (loadDataboxes_ :671-677)
   t.TNormal = ROOM_TEMPERATURE;
-  {
-    double lTNormal = sp_lT(t, t.TNormal);
-    if (!(t.lTMin < lTNormal && lTNormal < t.lTMax)) {
-      lTNormal = 0.5 * (t.lTMin + t.lTMax);
-      t.TNormal = sp_T(t, lTNormal);
-    }
+  double lTNormal = sp_lT(t, t.TNormal);
+  if (!(t.lTMin < lTNormal && lTNormal < t.lTMax)) {
+    lTNormal = 0.5 * (t.lTMin + t.lTMax);
+    t.TNormal = sp_T(t, lTNormal);
   }
+  // reference-state density: the file's normalDensity (:559-561), or the
+  // middle of the log-density range when that lies off the table (:665-670)
+  double rhoNormal = 0.0;
+  attr("normalDensity", rhoNormal);
+  rhoNormal = std::fabs(rhoNormal);
+  double lRhoNormal = sp_lRho(t, rhoNormal);
+  if (!(t.lRhoMin < lRhoNormal && lRhoNormal < t.lRhoMax)) {
+    lRhoNormal = 0.5 * (t.lRhoMin + t.lRhoMax);
+    rhoNormal = sp_rho(t, lRhoNormal);
+  }
+  t.rhoNormal = rhoNormal;
   const int nR = h.nRho, nT = h.nT;
   // fixBulkModulus_ (:689-714)
   for (int j = 0; j < nR; j++) {
@@ -396,6 +405,10 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
     h.f1[F_GM1MAX][j] = ratio(h.f2[F_DPDE][j * nT + nT - 1], rho);
     h.f1[F_SIELTMAX][j] = h.f2[F_SIE][j * nT + nT - 1];
   }
+
+  // reference-state pressure and (fixed) bulk modulus (:679-681)
+  t.PNormal = interp2(t, t.f2[F_P], lRhoNormal, lTNormal);
+  t.bModNormal = interp2(t, t.f2[F_BMOD], lRhoNormal, lTNormal);
 
   // ---- device image ----
   auto align = [](size_t x) { return (x + 255) & ~size_t(255); };

@@ -33,15 +33,19 @@ EXPORTED = [
     "sgx_pte_solve", "sgx_pte_solve_noalloc", "sgx_eos_helmholtz", "sgx_eos_helmholtz_dump",
     "sgx_server_create", "sgx_server_submit", "sgx_server_wait", "sgx_server_stats_get",
     "sgx_server_destroy", "sgx_host_alloc", "sgx_host_free", "sgx_eos_fill_host",
-    "sgx_get_sg_eos",
+    "sgx_get_sg_eos", "sgx_eos_modify_shifted", "sgx_eos_modify_scaled",
+    "sgx_eos_modify_bilinear_ramp", "sgx_eos_p_alpha_ramp_params", "sgx_eos_apply_modifiers",
 ]
+MOD_SHIFTED, MOD_SCALED, MOD_RAMP = 1, 2, 4
 HELM_DEFAULT, HELM_REGULA_FALSI, HELM_CACHE_READBACK = 31, 32, 64
 PTE_NOALLOC_MAX_CELLS = 1 << 20  # SGX_PTE_NOALLOC_MAX_CELLS
 
 
 class SgxEos(C.Structure):
     _fields_ = [("type", C.c_int32), ("flags", C.c_int32), ("table", C.c_uint64),
-                ("p", C.c_double * 14)]
+                ("p", C.c_double * 14), ("mods", C.c_uint32), ("mods_reserved", C.c_uint32),
+                ("shift", C.c_double), ("scale", C.c_double), ("inv_scale", C.c_double),
+                ("ramp", C.c_double * 6)]
 
 
 class MixParams(C.Structure):
@@ -148,6 +152,13 @@ def load():
     lib.sgx_pte_approx_temperature.argtypes = [I, C.c_int64, P, I, P, P, P, P, P, P, P, P]
     lib.sgx_mix_enforce_mass_volumes_sum.argtypes = [I, C.c_int64, P, P, P, P, P]
     lib.sgx_mix_enforce_energies_sum.argtypes = [I, C.c_int64, P, P, P, P, P, P, P]
+    lib.sgx_eos_modify_shifted.argtypes = [C.POINTER(SgxEos), D]
+    lib.sgx_eos_modify_scaled.argtypes = [C.POINTER(SgxEos), D]
+    lib.sgx_eos_modify_bilinear_ramp.argtypes = [C.POINTER(SgxEos), D, D, D, D]
+    lib.sgx_eos_p_alpha_ramp_params.argtypes = [C.POINTER(SgxEos), D, D, D] + [
+        C.POINTER(C.c_double)] * 4
+    lib.sgx_eos_apply_modifiers.argtypes = [C.POINTER(SgxEos), C.POINTER(C.c_int),
+                                            C.POINTER(C.c_double)]
     _lib = lib
     return lib
 
@@ -199,6 +210,39 @@ def helmholtz_eos(path, options=HELM_DEFAULT):
     e = SgxEos()
     check(lib.sgx_eos_helmholtz(C.byref(e), path.encode(), int(options)))
     return e
+
+
+def modify(eos, shift=None, scale=None, ramp=None):
+    """A copy of eos wrapped as the reference's modifiers nest:
+    BilinearRamp(Scaled(Shifted(model))); ramp = (r0, a, b, c)."""
+    lib = load()
+    e = SgxEos.from_buffer_copy(eos)
+    if shift is not None:
+        check(lib.sgx_eos_modify_shifted(C.byref(e), float(shift)))
+    if scale is not None:
+        check(lib.sgx_eos_modify_scaled(C.byref(e), float(scale)))
+    if ramp is not None:
+        check(lib.sgx_eos_modify_bilinear_ramp(C.byref(e), *[float(v) for v in ramp]))
+    return e
+
+
+def p_alpha_ramp_params(eos, alpha0, Pe, Pc):
+    """pAlpha2BilinearRampParams: (r0, a, b, c) of the ramp through the
+    p-alpha crush curve of eos."""
+    out = [C.c_double() for _ in range(4)]
+    check(load().sgx_eos_p_alpha_ramp_params(C.byref(eos), float(alpha0), float(Pe), float(Pc),
+                                             *[C.byref(o) for o in out]))
+    return tuple(o.value for o in out)
+
+
+def apply_modifiers(eos, enabled, vals):
+    """The modifier step of the reference's init_sg_* on a bare model:
+    returns (modified copy, vals as the call leaves them)."""
+    e = SgxEos.from_buffer_copy(eos)
+    en = (C.c_int * 4)(*[int(v) for v in enabled])
+    vv = (C.c_double * 6)(*[float(v) for v in vals])
+    check(load().sgx_eos_apply_modifiers(C.byref(e), en, vv))
+    return e, list(vv)
 
 
 def mix_params(**kw):

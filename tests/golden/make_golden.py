@@ -222,6 +222,157 @@ def sgeos_fixture(ref, cell_dim=700, ncell=512, seed=41, cutoff=1e-8, mode=1):
     return out
 
 
+def mods_row(shift=None, scale=None, ramp=None):
+    """[bits, shift, scale, r0, a, b, c]: bit 0 shifted, 1 scaled, 2 ramped."""
+    row = np.zeros(7)
+    if shift is not None:
+        row[0] += 1
+        row[1] = shift
+    if scale is not None:
+        row[0] += 2
+        row[2] = scale
+    if ramp is not None:
+        row[0] += 4
+        row[3:7] = ramp
+    return row
+
+
+def mdesc(mat, row, path=None):
+    """desc() of a model (or, with path, the tabulated one) with the
+    modifiers of a mods_row."""
+    bits = int(row[0])
+    kw = dict(shift=row[1] if bits & 1 else None, scale=row[2] if bits & 2 else None,
+              ramp=row[3:7] if bits & 4 else None)
+    if path is not None:
+        return rb.eos_desc(rb.SPINER_RHOT, [], path=path, matid=1, **kw)
+    return rb.eos_desc(mat[0], mat[1], **kw)
+
+
+# (model, shift, scale, p-alpha (alpha0, Pe, Pc) or None); model None = the
+# tabulated StiffGas table
+MOD_CASES = [
+    ((rb.IDEAL, (0.5, 2.0)), 0.1, 2.0, None),  # test_eos_modifiers.cpp:125-139
+    (W.STIFF_WATER, None, 1.5, None),
+    (W.NOBLE_ABEL_GAS, 1e8, None, None),
+    (W.GRUNEISEN_CU, 1e8, 1.5, (1.2, 1e9, 1e10)),
+    (W.IDEAL_AIR, None, None, (1.5, 5e6, 1e7)),
+    (W.STIFF_WATER, 1e8, 1.02, (1.3, 1e9, 5e9)),
+    (None, 1e8, 1.5, None),
+    (None, None, None, (1.5, 1e11, 1e12)),
+    (None, 1e8, 1.5, (1.5, 1e11, 1e12)),
+]
+
+
+def modifiers_fixture(ref, path, n=512, seed=61):
+    """ShiftedEOS / ScaledEOS / BilinearRampEOS around each model: vector
+    lookups, FillEos, pAlpha2BilinearRampParams and the init_sg_* modifier
+    step."""
+    rng = np.random.default_rng(seed)
+    out = {}
+    mats, rows = [], []
+    for k, (mat, shift, scale, pa) in enumerate(MOD_CASES):
+        base = mods_row(shift, scale)
+        d0 = mdesc(mat, base, path if mat is None else None)
+        ramp = None
+        if pa is not None:
+            ramp = ref.p_alpha(d0, *pa)
+            out[f"c{k}_palpha_in"] = np.array(pa)
+            out[f"c{k}_palpha"] = ramp
+        row = mods_row(shift, scale, ramp)
+        mats.append(mat if mat is not None else (rb.SPINER_RHOT, ()))
+        rows.append(row)
+        d = mdesc(mat, row, path if mat is None else None)
+        if mat is None:
+            rho, sie = sp5lite.stiffgas_queries(n, seed=seed + k)
+            T = np.exp(rng.uniform(np.log(50.0), np.log(3e6), n))
+        else:
+            lo, hi = (1e-3, 20.0) if ramp is None else (0.3 * ramp[0], 30 * ramp[0])
+            rho = np.exp(rng.uniform(np.log(lo), np.log(hi), n))
+            T = np.exp(rng.uniform(np.log(50.0), np.log(1e5), n))
+            if k == 0:  # the unit-scale gas of the reference's test, and its point
+                sie = rng.uniform(0.05, 5.0, n)
+                rho[0], sie[0] = 2.0, 0.5
+            else:
+                sie = rng.uniform(1e8, 1e11, n)
+        out[f"c{k}_rho"], out[f"c{k}_sie"], out[f"c{k}_T"] = rho, sie, T
+        for fn in ALL_FN:
+            second = T if fn in (1, 2, 4, 6, 8) else sie
+            out[f"c{k}_fn{fn}"] = ref.eos_vec(d, fn, rho, second)
+        # FillEos with (rho, sie) in; IdealGas under ShiftedEOS / ScaledEOS
+        # aborts in the reference (PreferredInput has all four bits) and is
+        # left out
+        if not (mat is not None and mat[0] == rb.IDEAL and row[0] % 4):
+            a = dict(rho=rho.copy(), temp=np.zeros(n), sie=sie.copy(), press=np.zeros(n),
+                     cv=np.zeros(n), bmod=np.zeros(n))
+            ref.fill_eos(d, a["rho"], a["temp"], a["sie"], a["press"], a["cv"], a["bmod"], Q_TPB)
+            for q, v in a.items():
+                out[f"c{k}_fill_{q}"] = v
+        # FillEos of a density under a ramp: (P, T) in, (rho, sie) out
+        if ramp is not None and mat is not None:
+            P = np.exp(rng.uniform(np.log(1e5), np.log(5e10), n))
+            a = dict(rho=np.zeros(n), temp=T.copy(), sie=np.zeros(n), press=P.copy(),
+                     cv=np.zeros(n), bmod=np.zeros(n))
+            ref.fill_eos(d, a["rho"], a["temp"], a["sie"], a["press"], a["cv"], a["bmod"],
+                         rb.Q_DENSITY | rb.Q_SIE)
+            for q, v in a.items():
+                out[f"c{k}_fillrho_{q}"] = v
+            out[f"c{k}_fillrho_P"] = P
+    out["materials"] = mats_array(mats)
+    out["mods"] = np.array(rows)
+    # the tabulated p-alpha whose first root sits on the bracket's end: a and
+    # the ramp are infinite (no ramp can be built from them)
+    out["palpha_edge_in"] = np.array([1.3, 1e9, 5e9])
+    out["palpha_edge"] = ref.p_alpha(mdesc(None, mods_row(), path), 1.3, 1e9, 5e9)
+    # the init_sg_* modifier step (test_eos_modifiers.cpp:225-247 and others)
+    inits = [((rb.IDEAL, (0.5, 2.0)), [0, 0, 0, 1], [0.0, 0.0, 1.5, 5e7, 1e8, 0.0]),
+             ((rb.IDEAL, (0.5, 2.0)), [0, 0, 1, 0], [0.0, 0.0, 1e9, 1.0, 2.0, 1.0]),
+             (W.STIFF_WATER, [1, 1, 0, 1], [1.02, 1e8, 1.3, 1e9, 5e9, 0.0]),
+             (W.GRUNEISEN_CU, [1, 0, 0, 1], [1.5, 0.0, 1.2, 1e9, 1e10, 0.0]),
+             (W.NOBLE_ABEL_GAS, [0, 1, 0, 0], [0.0, 1e8, 0.0, 0.0, 0.0, 0.0])]
+    out["init_materials"] = mats_array([m for m, _, _ in inits])
+    out["init_enabled"] = np.array([e for _, e, _ in inits], np.int32)
+    out["init_vals_in"] = np.array([v for _, _, v in inits])
+    out["init_vals_out"] = np.array([ref.init_mods(desc(m), e, v) for m, e, v in inits])
+    return out
+
+
+def modified_pte_fixture(ref, solver, seed):
+    """PTE over materials with modifiers: an ideal gas under a p-alpha ramp
+    next to a shifted and scaled stiff gas (two materials), and the batched
+    workload with three of its materials modified."""
+    out = {}
+    air_ramp = ref.p_alpha(desc(W.IDEAL_AIR), 1.5, 5e6, 1e7)
+    wl = W.pte_two_material(512, seed=seed)
+    rows = [mods_row(ramp=air_ramp), mods_row(1e8, 1.02)]
+    wl2 = W.pte_batched(1024, seed=seed + 1)
+    if solver == 1:  # as pte_pt_batched: ideal, stiff and Noble-Abel only
+        wl2["materials"] = wl2["materials"][:7]
+        wl2["eos_idx"] = np.where(wl2["eos_idx"] == 7, 6, wl2["eos_idx"]).astype(np.int32)
+    rows2 = [mods_row() for _ in wl2["materials"]]
+    rows2[0] = mods_row(ramp=air_ramp)
+    rows2[1] = mods_row(None, 1.02)
+    rows2[2] = mods_row(1e7, None)
+    rows2[5] = mods_row(1e8, 1.02)
+    for tag, w, rr in (("2mat", wl, rows), ("batched", wl2, rows2)):
+        mats = list(w["materials"])
+        descs = [mdesc(m, r) for m, r in zip(mats, rr)]
+        r = {k: w[k].copy() for k in ("rho", "vfrac", "sie", "temp", "press")}
+        conv, nit, res = ref.pte(solver, descs, w["eos_idx"], w["vfrac_tot"], w["sie_tot"],
+                                 r["rho"], r["vfrac"], r["sie"], r["temp"], r["press"],
+                                 params=ref.mix_params())
+        out[f"{tag}_materials"] = mats_array(mats)
+        out[f"{tag}_mods"] = np.array(rr)
+        out[f"{tag}_vfrac_tot"], out[f"{tag}_sie_tot"] = w["vfrac_tot"], w["sie_tot"]
+        if w["eos_idx"] is not None:
+            out[f"{tag}_eos_idx"] = w["eos_idx"]
+        out[f"{tag}_converged"], out[f"{tag}_niter"] = conv, nit
+        for k in ("rho", "vfrac", "sie", "temp", "press"):
+            out[f"{tag}_in_" + k] = w[k]
+            out[f"{tag}_out_" + k] = r[k]
+    out["solver"] = np.int32(solver)
+    return out
+
+
 def main():
     if not rb.have_reference():
         sys.exit("oracle/_ref/libsgref.so not built; run oracle/build_ref.sh")
@@ -272,6 +423,10 @@ def main():
             o["in_" + k] = wl[k]
             o["out_" + k] = r[k]
         fx["pte_rhot_spiner"] = o
+        fx["modifiers"] = modifiers_fixture(ref, path)
+        fx["modifiers"]["table_sha256"] = np.array(sha)
+    fx["pte_rhot_modified"] = modified_pte_fixture(ref, 0, 131)
+    fx["pte_pt_modified"] = modified_pte_fixture(ref, 1, 133)
     fx["get_sg_eos"] = sgeos_fixture(ref)
     fx["mix_utils"] = mixutil_fixture(ref)
     for mode, tag in ((-3, "rho_t"), (-2, "rho_p"), (-1, "p_t")):

@@ -131,3 +131,39 @@ def test_helm_table_derivatives_are_exact():
             for e, v in zip(exprs, blk):
                 ref = float(sp.lambdify((d, T), e, "mpmath")(mpmath.mpf(dd), mpmath.mpf(tt)))
                 assert abs(v[j, i] - ref) <= 1e-11 * max(abs(ref), 1e-300) + 1e-300, (j, i)
+
+
+def test_modifier_checks_without_gpu():
+    # the modifier calls are host-side value edits with the wrappers'
+    # CheckParams; no device is touched
+    from sgx import lib as L
+    L.load()
+    e = L.make_eos(L.IDEAL_GAS, (0.5, 2.0))
+    m = L.modify(e, shift=0.1, scale=2.0)
+    assert (m.mods, m.shift, m.scale, m.inv_scale) == (3, 0.1, 2.0, 0.5)
+    r = L.modify(m, ramp=(1.0, 3.0, 1.0, 0.5))
+    assert r.mods == 7
+    # rmid = r0 (a - b c) / (a - b), Pmid = a (rmid / r0 - 1)
+    assert list(r.ramp) == [1.0, 3.0, 1.0, 0.5, 1.0 * (3.0 - 1.0 * 0.5) / (3.0 - 1.0),
+                            3.0 * (1.0 * (3.0 - 1.0 * 0.5) / (3.0 - 1.0) / 1.0 - 1.0)]
+    with pytest.raises(RuntimeError, match="sgx error 5"):
+        L.modify(m, shift=1.0)  # Shifted<Scaled<...>> is not in the variant
+    with pytest.raises(RuntimeError, match="sgx error 5"):
+        L.modify(r, scale=2.0)
+    with pytest.raises(RuntimeError, match="sgx error 1"):
+        L.modify(e, scale=0.0)
+    with pytest.raises(RuntimeError, match="sgx error 1"):
+        L.modify(e, shift=float("nan"))
+    with pytest.raises(RuntimeError, match="sgx error 1"):
+        L.modify(e, ramp=(1.0, 2.0, 2.0, 0.0))  # a == b
+    with pytest.raises(RuntimeError, match="sgx error 1"):
+        L.modify(e, ramp=(0.0, 2.0, 1.0, 0.0))  # r0 > 0
+    # nothing enabled: the value comes back unchanged; a modified value is
+    # not accepted
+    same, vals = L.apply_modifiers(e, [0, 0, 0, 0], [0.0] * 6)
+    assert same.mods == 0 and vals == [0.0] * 6
+    with pytest.raises(RuntimeError, match="sgx error 1"):
+        L.apply_modifiers(m, [1, 0, 0, 0], [2.0, 0, 0, 0, 0, 0])
+    # shift and scale without a ramp need no device
+    sc, _ = L.apply_modifiers(e, [1, 1, 0, 0], [2.0, 0.1, 0, 0, 0, 0])
+    assert (sc.mods, sc.scale, sc.shift) == (3, 2.0, 0.1)

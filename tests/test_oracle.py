@@ -155,3 +155,83 @@ def test_port_vector_lookups_match_golden():
             second = fx[f"m{k}_T"] if fn in (1, 2, 4, 6, 8) else fx[f"m{k}_sie"]
             got = port.eos_vec(d, fn, fx[f"m{k}_rho"], second)
             assert bitwise_frac(got, fx[f"m{k}_fn{fn}"]) == 1.0, (kind, fn)
+
+
+# ---- modifiers: known answers of test/test_eos_modifiers.cpp ----------------
+
+needs_reference = pytest.mark.skipif(not rb.have_reference(),
+                                     reason="the compiled reference (oracle/_ref) is absent")
+
+
+@needs_reference
+def test_modifiers_known_answers():
+    ref = rb.reference()
+    # shifted by 0.1, then scaled by 2: P(rho = 2, sie = 0.5) == 0.3 exactly
+    # (test_eos_modifiers.cpp:125-139)
+    d = rb.eos_desc(rb.IDEAL, [0.5, 2.0], shift=0.1, scale=2.0)
+    assert ref.eos_vec(d, 3, np.array([2.0]), np.array([0.5]))[0] == 0.3
+    # a non-modifying modifier matches the bare model (:219-230)
+    rng = np.random.default_rng(3)
+    rho, sie = np.exp(rng.uniform(-3, 3, 64)), rng.uniform(0.1, 10, 64)
+    bare = rb.eos_desc(rb.IDEAL, [0.5, 2.0])
+    for kw in (dict(scale=1.0), dict(shift=0.0), dict(ramp=[1e9, 1.0, 2.0, 1.0])):
+        for fn in (0, 3, 5, 7, 9):
+            np.testing.assert_array_equal(ref.eos_vec(rb.eos_desc(rb.IDEAL, [0.5, 2.0], **kw),
+                                                      fn, rho, sie),
+                                          ref.eos_vec(bare, fn, rho, sie))
+
+
+@needs_reference
+def test_p_alpha_ramp_known_answers():
+    # the ramp from a p-alpha model through init_sg_IdealGas
+    # (test_eos_modifiers.cpp:231-314): parameters, pressures on both slopes
+    # and beyond, bulk moduli on both slopes
+    ref = rb.reference()
+    gm1, Cv = 0.5, 2.0
+    Pe, Pc, alpha0, T0 = 5.e7, 1.e8, 1.5, 293.0
+    vals = ref.init_mods(rb.eos_desc(rb.IDEAL, [gm1, Cv]), [0, 0, 0, 1],
+                         [0.0, 0.0, alpha0, Pe, Pc, 0.0])
+    rho0 = 1.e6 / (gm1 * Cv * T0)
+    r0 = rho0 / alpha0
+    r1 = Pc / (gm1 * Cv * T0)
+    rmid = Pe / (gm1 * Cv * T0 * alpha0)
+    a = r0 * Pe / (rmid - r0)
+    b = r0 * (Pc - Pe) / (r1 - rmid)
+    c = (Pc * rmid - Pe * r1) / (r0 * (Pc - Pe))
+    np.testing.assert_allclose(vals[2:], [r0, a, b, c], rtol=1e-12)
+    d = rb.eos_desc(rb.IDEAL, [gm1, Cv], ramp=vals[2:])
+    rho_t1, rho_t2 = 0.5 * (r0 + rmid), 0.5 * (rmid + r1)
+    rho = np.array([rmid, rho_t1, rho_t2, 0.8 * r0, 1.2 * r0])
+    P = ref.eos_vec(d, 2, rho, np.full(5, T0))
+    np.testing.assert_allclose(P, [alpha0 * gm1 * Cv * rmid * T0, a * (rho_t1 / r0 - 1.0),
+                                   b * (rho_t2 / r0 - c), 0.8 * r0 * gm1 * Cv * T0,
+                                   1.2 * r0 * gm1 * Cv * T0], rtol=1e-12)
+    B = ref.eos_vec(d, 6, np.array([rho_t1, rho_t2, 0.8 * r0, 1.2 * r1]), np.full(4, T0))
+    np.testing.assert_allclose(B, [rho_t1 * a / r0, rho_t2 * b / r0,
+                                   0.8 * r0 * gm1 * (gm1 + 1.0) * Cv * T0,
+                                   1.2 * r1 * gm1 * (gm1 + 1.0) * Cv * T0], rtol=1e-12)
+
+
+@needs_reference
+def test_modifier_fixture_is_current():
+    # the committed fixture is what the compiled reference gives today
+    ref = rb.reference()
+    fx = golden("modifiers")
+    mats = materials_from_rows(fx["materials"])
+    for k, (mat, row) in enumerate(zip(mats, fx["mods"])):
+        if mat[0] == rb.SPINER_RHOT:
+            continue
+        bits = int(row[0])
+        d = rb.eos_desc(mat[0], mat[1], shift=row[1] if bits & 1 else None,
+                        scale=row[2] if bits & 2 else None, ramp=row[3:7] if bits & 4 else None)
+        for fn in (2, 3, 6, 7):
+            second = fx[f"c{k}_T"] if fn in (2, 6) else fx[f"c{k}_sie"]
+            np.testing.assert_array_equal(ref.eos_vec(d, fn, fx[f"c{k}_rho"], second),
+                                          fx[f"c{k}_fn{fn}"])
+
+
+def test_port_rejects_modified_eos():
+    # the port restates bare models only and says so
+    d = rb.eos_desc(rb.IDEAL, [0.4, 0.718e7], shift=1.0)
+    with pytest.raises(RuntimeError):
+        rb.port().eos_vec(d, 3, np.array([1.0]), np.array([1.0]))
