@@ -37,6 +37,9 @@ UNITS = [
     ("sgx_modifiers", "sgx_modifiers.cu", ["--fmad=false"]),
 ] + [(f"sgx_pte_fp64_n{n}", "sgx_pte_fp64_n.cu", ["--fmad=false", f"-DSGX_PTE_N={n}"])
      for n in range(1, 7)] + [
+    (f"sgx_pte_fp64_bare_n{n}", "sgx_pte_fp64_n.cu",
+     ["--fmad=false", f"-DSGX_PTE_N={n}", "-DSGX_BARE_MODELS"])
+    for n in range(1, 7)] + [
     (f"sgx_pte_mixed_n{n}", "sgx_pte_mixed_n.cu", ["--fmad=true", f"-DSGX_PTE_N={n}"])
     for n in range(1, 7)] + [
     (f"sgx_pte_ext_n{n}", "sgx_pte_ext_n.cu", ["--fmad=false", f"-DSGX_PTE_N={n}"])

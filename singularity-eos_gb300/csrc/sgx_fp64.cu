@@ -15,9 +15,27 @@
 namespace sgx {
 
 template <int N> cudaError_t launch_pte_fp64_n(const PteArgs &a, cudaStream_t stream);
+template <int N> cudaError_t launch_pte_fp64_n_bare(const PteArgs &a, cudaStream_t stream);
 template <int N> cudaError_t launch_pte_ext_n(const PteArgs &a, cudaStream_t stream);
 
 namespace {
+
+using PteLauncher = cudaError_t (*)(const PteArgs &, cudaStream_t);
+
+template <int N> PteLauncher pte_launcher_n(const bool ext, const bool mods) {
+  if (ext) return launch_pte_ext_n<N>;
+  return mods ? launch_pte_fp64_n<N> : launch_pte_fp64_n_bare<N>;
+}
+PteLauncher pte_launcher(const int n, const bool ext, const bool mods) {
+  switch (n) {
+  case 1: return pte_launcher_n<1>(ext, mods);
+  case 2: return pte_launcher_n<2>(ext, mods);
+  case 3: return pte_launcher_n<3>(ext, mods);
+  case 4: return pte_launcher_n<4>(ext, mods);
+  case 5: return pte_launcher_n<5>(ext, mods);
+  default: return pte_launcher_n<6>(ext, mods);
+  }
+}
 
 __global__ void eval_kernel(const EvalArgs a) {
   const sgx_eos e = a.eos;
@@ -159,16 +177,12 @@ cudaError_t launch_pte_fp64_with(const PteArgs &args, unsigned *bins, int *perm,
   const int lo = a.eos_idx ? 1 : a.nmat;
   const int hi = a.nmat < PTE_MAX_N ? a.nmat : PTE_MAX_N;
   const bool ext = a.solver != SGX_PTE_RHOT && a.solver != SGX_PTE_PT;
-  for (int n = lo; n <= hi && e == cudaSuccess; ++n) {
-    switch (n) {
-    case 1: e = ext ? launch_pte_ext_n<1>(a, stream) : launch_pte_fp64_n<1>(a, stream); break;
-    case 2: e = ext ? launch_pte_ext_n<2>(a, stream) : launch_pte_fp64_n<2>(a, stream); break;
-    case 3: e = ext ? launch_pte_ext_n<3>(a, stream) : launch_pte_fp64_n<3>(a, stream); break;
-    case 4: e = ext ? launch_pte_ext_n<4>(a, stream) : launch_pte_fp64_n<4>(a, stream); break;
-    case 5: e = ext ? launch_pte_ext_n<5>(a, stream) : launch_pte_fp64_n<5>(a, stream); break;
-    case 6: e = ext ? launch_pte_ext_n<6>(a, stream) : launch_pte_fp64_n<6>(a, stream); break;
-    }
-  }
+  // RhoT and PT over bare models run the build without modifier code
+  bool mods = false;
+  for (int k = 0; k < a.neos; ++k)
+    mods = mods || a.eos[k].mods != 0;
+  for (int n = lo; n <= hi && e == cudaSuccess; ++n)
+    e = pte_launcher(n, ext, mods)(a, stream);
   return e;
 }
 

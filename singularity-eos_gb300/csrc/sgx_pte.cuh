@@ -19,6 +19,7 @@
 #include "sgx_dispatch.cuh"
 
 namespace sgx {
+SGX_DISPATCH_BEGIN
 
 struct PteStatusLocal {
   double residual = 0;
@@ -1401,4 +1402,5 @@ SGX_HDI bool pte_polish(PteRhoT<double, N> &s, const MixP<double> &tight, int &t
   return st.converged && (st.residual == st.residual);
 }
 
+} // inline namespace
 } // namespace sgx

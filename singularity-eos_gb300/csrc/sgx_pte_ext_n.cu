@@ -8,5 +8,6 @@
 #endif
 
 namespace sgx {
-template cudaError_t launch_pte_ext_n<SGX_PTE_N>(const PteArgs &, cudaStream_t);
+template cudaError_t SGX_PTE_LAUNCHER(launch_pte_ext_n)<SGX_PTE_N>(const PteArgs &,
+                                                          cudaStream_t);
 } // namespace sgx

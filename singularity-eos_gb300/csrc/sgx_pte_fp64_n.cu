@@ -1,5 +1,6 @@
 // One instantiation of the FP64 per-cell PTE kernel: SGX_PTE_N materials per
-// cell (set by the build, one object per value). Compiled with --fmad=false.
+// cell (set by the build, one object per value). Compiled with --fmad=false,
+// twice: as is, and with SGX_BARE_MODELS for lists without modifiers.
 #include "sgx_pte_kernel.cuh"
 
 #ifndef SGX_PTE_N
@@ -7,5 +8,6 @@
 #endif
 
 namespace sgx {
-template cudaError_t launch_pte_fp64_n<SGX_PTE_N>(const PteArgs &, cudaStream_t);
+template cudaError_t SGX_PTE_LAUNCHER(launch_pte_fp64_n)<SGX_PTE_N>(const PteArgs &,
+                                                          cudaStream_t);
 } // namespace sgx

@@ -19,7 +19,20 @@
 #include "sgx_internal.h"
 #include "sgx_pte.cuh"
 
+// The plain FP64 path is built twice: for lists that hold a modified EOS
+// (the modifier arithmetic of sgx_dispatch.cuh compiled in) and, with
+// SGX_BARE_MODELS defined, for lists of bare models, whose kernels carry no
+// modifier code (it costs the bare kernels registers and 5-9% of their
+// speed). The kernels live in the dispatch's inline namespace; the
+// launchers get a _bare suffix in the second build.
+#ifdef SGX_BARE_MODELS
+#define SGX_PTE_LAUNCHER(name) name##_bare
+#else
+#define SGX_PTE_LAUNCHER(name) name
+#endif
+
 namespace sgx {
+SGX_DISPATCH_BEGIN
 
 constexpr int PTE_BLOCK = 128;
 
@@ -116,7 +129,10 @@ __global__ void __launch_bounds__(PTE_BLOCK) pte_cell_kernel(const PteArgs a) {
   }
 }
 
-template <int N> cudaError_t launch_pte_fp64_n(const PteArgs &a, cudaStream_t stream) {
+} // inline namespace
+
+template <int N>
+cudaError_t SGX_PTE_LAUNCHER(launch_pte_fp64_n)(const PteArgs &a, cudaStream_t stream) {
   const long long blocks = (a.ncell + PTE_BLOCK - 1) / PTE_BLOCK;
   if (a.solver == SGX_PTE_PT)
     pte_cell_kernel<PtePT, N><<<static_cast<unsigned>(blocks), PTE_BLOCK, 0, stream>>>(a);
@@ -127,7 +143,8 @@ template <int N> cudaError_t launch_pte_fp64_n(const PteArgs &a, cudaStream_t st
 
 // The three solvers beyond RhoT and PT, compiled in their own translation
 // units (sgx_pte_ext_n.cu).
-template <int N> cudaError_t launch_pte_ext_n(const PteArgs &a, cudaStream_t stream) {
+template <int N>
+cudaError_t SGX_PTE_LAUNCHER(launch_pte_ext_n)(const PteArgs &a, cudaStream_t stream) {
   const long long blocks = (a.ncell + PTE_BLOCK - 1) / PTE_BLOCK;
   const unsigned g = static_cast<unsigned>(blocks);
   switch (a.solver) {
