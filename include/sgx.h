@@ -28,6 +28,10 @@
  *   sgx_mix_params_default  MixParams defaults (mixed_cell_models.hpp:43-78)
  *   sgx_pte_rhot_required_scratch  PTESolverRhoTRequiredScratch (:873-881)
  *   sgx_pte_pt_required_scratch    PTESolverPTRequiredScratch (:1198-1206)
+ *   sgx_eos_modify_*     ShiftedEOS / ScaledEOS / BilinearRampEOS around a
+ *                        model (eos/modifiers/), as Variant::Modify builds them
+ *   sgx_eos_apply_modifiers  the modifier step of init_sg_*
+ *                        (eos/singularity_eos.cpp:67-79)
  */
 #ifndef SGX_H_
 #define SGX_H_
