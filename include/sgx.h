@@ -273,6 +273,19 @@ long sgx_eos_spiner_dump(const sgx_eos *eos, double *out, long cap);
 int sgx_eos_eval(const sgx_eos *eos, int fn, int64_t n, const double *in1,
                  const double *in2, double *out, double *lambda, int lambda_stride,
                  sgx_stream_t stream);
+/* PTDerivativesFromPreferred (eos/eos_base.hpp:410-419, eos_variant.hpp:
+ * 386-398) at n states (rho, sie, press, temp): dedP_T = (dsie/dP)_T,
+ * drdP_T = (drho/dP)_T, dedT_P = (dsie/dT)_P, drdT_P = (drho/dT)_P.
+ * IdealGas answers in closed form (eos_ideal.hpp:152-168); the other models
+ * by the reference's one-sided differences of
+ * DensityEnergyFromPressureTemperature (PTDerivativesByFiniteDifferences,
+ * eos_base.hpp:299-320); modifiers as theirs do. The reference has only the
+ * scalar member; this is its per-element loop. lambda as in sgx_eos_eval.
+ * Helmholtz returns SGX_ERR_UNSUPPORTED. */
+int sgx_eos_pt_derivatives(const sgx_eos *eos, int64_t n, const double *rho, const double *sie,
+                           const double *press, const double *temp, double *dedP_T,
+                           double *drdP_T, double *dedT_P, double *drdT_P, double *lambda,
+                           int lambda_stride, sgx_stream_t stream);
 /* Vector FillEos: output is a bit set of SGX_Q_*; arrays not in output are
  * inputs. Any array that is neither read nor written may be NULL. */
 int sgx_eos_fill(const sgx_eos *eos, int64_t n, double *rho, double *temp, double *sie,

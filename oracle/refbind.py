@@ -280,6 +280,20 @@ class Oracle:
         f(C.c_int(which), C.c_int(nmat), C.c_int(ncell), _ip(eos_idx), _dp(tot), _dp(tot_rho),
           _dp(rho), _dp(vfrac), _dp(sie))
 
+    def pt_derivs(self, desc, rho, sie, P, T):
+        """PTDerivativesFromPreferred per element (reference library only):
+        returns (dedP_T, drdP_T, dedT_P, drdT_P)."""
+        n = rho.size
+        out = np.zeros(4 * n)
+        f = self._fn("pt_derivs")
+        f.restype = C.c_int
+        rc = f(C.byref(desc), C.c_int(n), _dp(np.ascontiguousarray(rho, np.float64)),
+               _dp(np.ascontiguousarray(sie, np.float64)), _dp(np.ascontiguousarray(P, np.float64)),
+               _dp(np.ascontiguousarray(T, np.float64)), _dp(out))
+        if rc != 0:
+            raise RuntimeError("pt_derivs failed")
+        return tuple(out.reshape(4, n))
+
     def p_alpha(self, desc, alpha0, Pe, Pc):
         """pAlpha2BilinearRampParams of the (shifted / scaled) EOS desc
         (reference library only): returns (r0, a, b, c)."""

@@ -438,6 +438,29 @@ int sgref_rho_sie_from_pt(const sgref_eos *desc, int n, const double *P, const d
   return 0;
 }
 
+// PTDerivativesFromPreferred through the Variant (eos_variant.hpp:386-398)
+// at n states; out = [dedP_T | drdP_T | dedT_P | drdT_P], n each.
+int sgref_pt_derivs(const sgref_eos *desc, int n, const double *rho, const double *sie,
+                    const double *P, const double *T, double *out) {
+  try {
+    EOS eos = make_eos(*desc);
+    for (int i = 0; i < n; ++i) {
+      Real a, b, c, d;
+      eos.PTDerivativesFromPreferred(rho[i], sie[i], P[i], T[i], static_cast<Real *>(nullptr),
+                                     a, b, c, d);
+      out[i] = a;
+      out[n + i] = b;
+      out[2 * n + i] = c;
+      out[3 * n + i] = d;
+    }
+    eos.Finalize();
+  } catch (const std::exception &ex) {
+    std::fprintf(stderr, "sgref_pt_derivs: %s\n", ex.what());
+    return 1;
+  }
+  return 0;
+}
+
 // pAlpha2BilinearRampParams (ramps_eos.hpp:43-77) of the EOS desc describes
 // (its shift and scale; a ramp in desc is ignored). out = r0, a, b, c.
 int sgref_p_alpha(const sgref_eos *desc, double alpha0, double Pe, double Pc, double *out) {

@@ -259,6 +259,40 @@ int sgx_eos_eval(const sgx_eos *eos, int fn, int64_t n, const double *in1, const
   return SGX_OK;
 }
 
+int sgx_eos_pt_derivatives(const sgx_eos *eos, int64_t n, const double *rho, const double *sie,
+                           const double *press, const double *temp, double *dedP_T,
+                           double *drdP_T, double *dedT_P, double *drdT_P, double *lambda,
+                           int lambda_stride, sgx_stream_t stream) {
+  static const char *who = "sgx_eos_pt_derivatives";
+  if (!eos || !valid_type(eos->type)) return fail(SGX_ERR_INVALID, std::string(who) + ": bad eos");
+  if (eos->type == SGX_HELMHOLTZ)
+    return fail(SGX_ERR_UNSUPPORTED,
+                std::string(who) + ": Helmholtz has no DensityEnergyFromPressureTemperature here");
+  if (const int rc = check_mods(*eos, false, who)) return rc;
+  if (n < 0) return fail(SGX_ERR_INVALID, std::string(who) + ": n < 0");
+  if (n == 0) return SGX_OK;
+  if (!rho || !sie || !press || !temp || !dedP_T || !drdP_T || !dedT_P || !drdT_P)
+    return fail(SGX_ERR_INVALID, std::string(who) + ": null array");
+  if (lambda && lambda_stride < 2)
+    return fail(SGX_ERR_INVALID, std::string(who) + ": lambda_stride < 2");
+  sgx::PtDerivArgs a;
+  a.eos = *eos;
+  a.n = n;
+  a.rho = rho;
+  a.sie = sie;
+  a.press = press;
+  a.temp = temp;
+  a.d[0] = dedP_T;
+  a.d[1] = drdP_T;
+  a.d[2] = dedT_P;
+  a.d[3] = drdT_P;
+  a.lambda = lambda;
+  a.lambda_stride = lambda_stride;
+  const cudaError_t e = sgx::launch_pt_derivs(a, reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, who);
+  return SGX_OK;
+}
+
 int sgx_eos_fill_ex(const sgx_eos *eos, int64_t n, double *rho, double *temp, double *sie,
                     double *press, double *cv, double *bmod, double *cs, uint32_t output,
                     double *lambda, int lambda_stride, int precision, sgx_stream_t stream) {

@@ -507,6 +507,83 @@ SGX_HDI void ev_fill(const sgx_eos &e, double &rho, double &temp, double &sie, d
   bmod = ev_B_from_rho_sie<double>(e, rho, sie, lam);
 }
 
+// ---------------------------------------------------------------------------
+// PTDerivativesFromPreferred: (dsie/dP)_T, (drho/dP)_T, (dsie/dT)_P and
+// (drho/dT)_P at a state (rho, sie, P, T).
+
+// PTDerivativesByFiniteDifferences (eos_base.hpp:299-320): one-sided
+// differences of DensityEnergyFromPressureTemperature with eps 3e-6 (the
+// default of EosBase::PTDerivativesFromPreferred, :410-419). The perturbed
+// state starts at 0 where the reference leaves it uninitialised.
+template <typename DEFPT>
+SGX_HDI void pt_derivs_fd(const DEFPT &defpt, const double rho, const double sie,
+                          const double P, const double T, double &dedP_T, double &drdP_T,
+                          double &dedT_P, double &drdT_P) {
+  constexpr double derivative_eps = 3.0e-6;
+  const double absP = smax(sabs(P), lim<double>::eps / derivative_eps);
+  const double dP = -rsgn(P) * absP * derivative_eps; // might be negative
+  const double absT = smax(sabs(T), lim<double>::eps / derivative_eps);
+  const double dT = absT * derivative_eps;
+  double r_pert = 0.0, e_pert = 0.0;
+  defpt(P + dP, T, r_pert, e_pert);
+  drdP_T = ratio(r_pert - rho, dP);
+  dedP_T = ratio(e_pert - sie, dP);
+  defpt(P, T + dT, r_pert, e_pert);
+  drdT_P = ratio(r_pert - rho, dT);
+  dedT_P = ratio(e_pert - sie, dT);
+}
+
+// The bare models: IdealGas in closed form (eos_ideal.hpp:152-168); the
+// others take the base class's finite differences (the tabulated model's own
+// version is commented out in eos_spiner_rho_temp.hpp:199-206, 1015-1048).
+SGX_HDI void md_pt_derivs(const sgx_eos &e, const double rho, const double sie, const double P,
+                          const double T, double *lam, double &dedP_T, double &drdP_T,
+                          double &dedT_P, double &drdT_P, int *err) {
+  if (e.type == SGX_IDEAL_GAS) {
+    const double gm1 = e.p[pi::gm1], Cv = e.p[pi::Cv];
+    dedP_T = 0;
+    dedT_P = Cv;
+    drdP_T = ratio(1.0, gm1 * sie);
+    drdT_P = -ratio(P, gm1 * Cv * T * T);
+    return;
+  }
+  auto defpt = [&](const double p, const double t, double &r, double &s) {
+    md_rho_sie_from_PT(e, p, t, r, s, lam, err);
+  };
+  pt_derivs_fd(defpt, rho, sie, P, T, dedP_T, drdP_T, dedT_P, drdT_P);
+}
+
+// Through the modifiers: BilinearRampEOS keeps the base class's finite
+// differences over its own DensityEnergyFromPressureTemperature, which
+// forwards to the wrapped EOS (ramps_eos.hpp:220, 521-525); ScaledEOS
+// evaluates at (scale rho, sie / scale) and rescales the four derivatives
+// (scaled_eos.hpp:148-159); ShiftedEOS evaluates at sie - shift
+// (shifted_eos.hpp:141-148).
+SGX_HDI void ev_pt_derivs(const sgx_eos &e, const double rho, const double sie, const double P,
+                          const double T, double *lam, double &dedP_T, double &drdP_T,
+                          double &dedT_P, double &drdT_P, int *err) {
+  if (SGX_MODS(e) & SGX_MOD_RAMP) {
+    auto defpt = [&](const double p, const double t, double &r, double &s) {
+      ev_rho_sie_from_PT(e, p, t, r, s, lam, err);
+    };
+    pt_derivs_fd(defpt, rho, sie, P, T, dedP_T, drdP_T, dedT_P, drdT_P);
+    return;
+  }
+  double r = rho, s = sie;
+  if (SGX_MODS(e) & SGX_MOD_SCALED) {
+    r = e.scale * rho;
+    s = e.inv_scale * sie;
+  }
+  if (SGX_MODS(e) & SGX_MOD_SHIFTED) s = s - e.shift;
+  md_pt_derivs(e, r, s, P, T, lam, dedP_T, drdP_T, dedT_P, drdT_P, err);
+  if (SGX_MODS(e) & SGX_MOD_SCALED) {
+    dedP_T *= e.scale;
+    drdP_T *= e.inv_scale;
+    dedT_P *= e.scale;
+    drdT_P *= e.inv_scale;
+  }
+}
+
 // One vector-lookup element (EosBase vector members, eos_base.hpp:421-494).
 SGX_HDI double ev_eval(const sgx_eos &e, const int fn, const double a, const double b,
                        double *lam) {

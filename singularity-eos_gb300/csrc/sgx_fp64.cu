@@ -5,6 +5,7 @@
 //
 //   eval_kernel      the EosBase vector overloads (eos/eos_base.hpp:169-230)
 //   fill_kernel      vector FillEos (eos/eos_base.hpp:503-531)
+//   pt_derivs_kernel PTDerivativesFromPreferred per element (eos_base.hpp:410-419)
 //   spiner_fill_ref  tabulated FillEos for the elements the mixed-precision
 //                    lookup (sgx_lookup_mixed.cu) leaves to FP64
 #include <cuda_runtime.h>
@@ -81,6 +82,22 @@ __global__ void fill_kernel(const FillArgs a) {
     if ((wb & Q_BMOD) && a.bmod) a.bmod[i] = bmod;
   }
   if (bad && a.err) atomicOr(a.err, 1);
+}
+
+__global__ void pt_derivs_kernel(const PtDerivArgs a) {
+  const sgx_eos e = a.eos;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < a.n;
+       i += stride) {
+    double *lam = a.lambda ? a.lambda + i * a.lambda_stride : nullptr;
+    double d0, d1, d2, d3;
+    int err = 0;
+    ev_pt_derivs(e, a.rho[i], a.sie[i], a.press[i], a.temp[i], lam, d0, d1, d2, d3, &err);
+    a.d[0][i] = d0;
+    a.d[1][i] = d1;
+    a.d[2][i] = d2;
+    a.d[3][i] = d3;
+  }
 }
 
 // The reference's FP64 path (eos_spiner_rho_temp.hpp:1052-1101) for the
@@ -216,6 +233,12 @@ cudaError_t launch_fill_ref(const FillArgs &a, const unsigned *left, cudaStream_
   const long long cap = static_cast<long long>(sms) * 4;
   spiner_fill_ref<<<static_cast<int>(blocks < cap ? blocks : cap), REF_BLOCK, 0, stream>>>(a,
                                                                                         left);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pt_derivs(const PtDerivArgs &a, cudaStream_t stream) {
+  if (a.n <= 0) return cudaSuccess;
+  pt_derivs_kernel<<<grid_for(a.n, 256), 256, 0, stream>>>(a);
   return cudaGetLastError();
 }
 

@@ -105,6 +105,17 @@ struct FillArgs {
   int *err; // device flag: set to 1 on an undefined input/output combination
 };
 cudaError_t launch_fill_fp64(const FillArgs &a, cudaStream_t stream);
+// PTDerivativesFromPreferred per element: d[0..3] = dedP_T, drdP_T, dedT_P,
+// drdT_P.
+struct PtDerivArgs {
+  sgx_eos eos;
+  long long n;
+  const double *rho, *sie, *press, *temp;
+  double *d[4];
+  double *lambda;
+  int lambda_stride;
+};
+cudaError_t launch_pt_derivs(const PtDerivArgs &a, cudaStream_t stream);
 // Tabulated rho-T FillEos from (rho, sie): FP32 bracket search + FP64 solve.
 cudaError_t launch_fill_mixed(const FillArgs &a, cudaStream_t stream);
 // The reference's FP64 tabulated FillEos for the elements whose bit is set

@@ -35,6 +35,7 @@ EXPORTED = [
     "sgx_server_destroy", "sgx_host_alloc", "sgx_host_free", "sgx_eos_fill_host",
     "sgx_get_sg_eos", "sgx_eos_modify_shifted", "sgx_eos_modify_scaled",
     "sgx_eos_modify_bilinear_ramp", "sgx_eos_p_alpha_ramp_params", "sgx_eos_apply_modifiers",
+    "sgx_eos_pt_derivatives",
 ]
 MOD_SHIFTED, MOD_SCALED, MOD_RAMP = 1, 2, 4
 HELM_DEFAULT, HELM_REGULA_FALSI, HELM_CACHE_READBACK = 31, 32, 64
@@ -159,6 +160,7 @@ def load():
         C.POINTER(C.c_double)] * 4
     lib.sgx_eos_apply_modifiers.argtypes = [C.POINTER(SgxEos), C.POINTER(C.c_int),
                                             C.POINTER(C.c_double)]
+    lib.sgx_eos_pt_derivatives.argtypes = [C.POINTER(SgxEos), C.c_int64] + [P] * 9 + [I, P]
     _lib = lib
     return lib
 
@@ -243,6 +245,17 @@ def apply_modifiers(eos, enabled, vals):
     vv = (C.c_double * 6)(*[float(v) for v in vals])
     check(load().sgx_eos_apply_modifiers(C.byref(e), en, vv))
     return e, list(vv)
+
+
+def pt_derivatives(eos, rho, sie, press, temp, lam=None, lam_stride=0, stream=None):
+    """PTDerivativesFromPreferred per element of device tensors: returns
+    (dedP_T, drdP_T, dedT_P, drdT_P)."""
+    import torch
+    out = [torch.empty_like(rho) for _ in range(4)]
+    check(load().sgx_eos_pt_derivatives(C.byref(eos), rho.numel(), ptr(rho), ptr(sie),
+                                        ptr(press), ptr(temp), *[ptr(o) for o in out],
+                                        ptr(lam), lam_stride, stream_ptr(stream)))
+    return tuple(out)
 
 
 def mix_params(**kw):

@@ -336,6 +336,42 @@ def modifiers_fixture(ref, path, n=512, seed=61):
     return out
 
 
+def pt_derivs_fixture(ref, path, n=256, seed=71):
+    """PTDerivativesFromPreferred at consistent states (sie and P from
+    (rho, T) of the same EOS): every model, bare and modified."""
+    rng = np.random.default_rng(seed)
+    air_ramp = ref.p_alpha(desc(W.IDEAL_AIR), 1.5, 5e6, 1e7)
+    cases = [  # (model or None for the table, mods row, rho range, T range)
+        (W.IDEAL_AIR, mods_row(), (1e-4, 1.0), (50.0, 1e5)),
+        (W.STIFF_WATER, mods_row(), (0.5, 3.0), (200.0, 5e3)),
+        (W.NOBLE_ABEL_GAS, mods_row(), (1e-4, 1.0), (50.0, 1e5)),
+        (W.GRUNEISEN_CU, mods_row(), (8.0, 11.0), (300.0, 3e3)),
+        (None, mods_row(), (0.5, 20.0), (300.0, 1e5)),
+        ((rb.IDEAL, (0.5, 2.0)), mods_row(0.1, 2.0), (0.5, 3.0), (1.0, 10.0)),
+        (W.IDEAL_AIR, mods_row(ramp=air_ramp), (0.3 * air_ramp[0], 30 * air_ramp[0]),
+         (50.0, 3e3)),
+        (W.STIFF_WATER, mods_row(1e8, 1.02), (0.5, 3.0), (200.0, 5e3)),
+        (None, mods_row(1e8, 1.5), (0.5, 10.0), (300.0, 1e5)),
+    ]
+    out = {}
+    mats, rows = [], []
+    for k, (mat, row, (rlo, rhi), (tlo, thi)) in enumerate(cases):
+        d = mdesc(mat, row, path if mat is None else None)
+        rho = np.exp(rng.uniform(np.log(rlo), np.log(rhi), n))
+        T = np.exp(rng.uniform(np.log(tlo), np.log(thi), n))
+        if k == 5:  # test_eos_modifiers.cpp:160-167
+            rho[0], T[0] = 1.5, 2.0
+        sie = ref.eos_vec(d, 1, rho, T)
+        P = ref.eos_vec(d, 2, rho, T)
+        out[f"c{k}_rho"], out[f"c{k}_sie"], out[f"c{k}_P"], out[f"c{k}_T"] = rho, sie, P, T
+        out[f"c{k}_d"] = np.array(ref.pt_derivs(d, rho, sie, P, T))
+        mats.append(mat if mat is not None else (rb.SPINER_RHOT, ()))
+        rows.append(row)
+    out["materials"] = mats_array(mats)
+    out["mods"] = np.array(rows)
+    return out
+
+
 def modified_pte_fixture(ref, solver, seed):
     """PTE over materials with modifiers: an ideal gas under a p-alpha ramp
     next to a shifted and scaled stiff gas (two materials), and the batched
@@ -425,6 +461,8 @@ def main():
         fx["pte_rhot_spiner"] = o
         fx["modifiers"] = modifiers_fixture(ref, path)
         fx["modifiers"]["table_sha256"] = np.array(sha)
+        fx["pt_derivs"] = pt_derivs_fixture(ref, path)
+        fx["pt_derivs"]["table_sha256"] = np.array(sha)
     fx["pte_rhot_modified"] = modified_pte_fixture(ref, 0, 131)
     fx["pte_pt_modified"] = modified_pte_fixture(ref, 1, 133)
     fx["get_sg_eos"] = sgeos_fixture(ref)

@@ -202,3 +202,23 @@ def test_mixed_precision_rejects_modified_eos(sgx, table):
     with pytest.raises(RuntimeError, match="unmodified EOS only"):
         sgx.pte_solve(0, [g, sgx.make_eos(1, (0.4, 0.718e7))], None, dev(np.ones(8)),
                       dev(np.full(8, 1e10)), *m, precision=1)
+
+
+def test_pt_derivatives(sgx, table):
+    # PTDerivativesFromPreferred for every model, bare and modified, at
+    # consistent states (tests/golden/make_golden.py pt_derivs)
+    fx = golden("pt_derivs")
+    assert str(fx["table_sha256"]) == str(golden("modifiers")["table_sha256"])
+    mats = materials_from_rows(fx["materials"])
+    worst = 1.0
+    for k, (mat, row) in enumerate(zip(mats, fx["mods"])):
+        e = case_eos(sgx, table, mat, row)
+        t = [dev(fx[f"c{k}_{q}"]) for q in ("rho", "sie", "P", "T")]
+        got = sgx.pt_derivatives(e, *t)
+        torch.cuda.synchronize()
+        for j, name in enumerate(("dedP_T", "drdP_T", "dedT_P", "drdT_P")):
+            worst = min(worst, close(got[j].cpu().numpy(), fx[f"c{k}_d"][j], f"case {k} {name}"))
+    # the ideal gas in closed form at the reference test's state
+    # (test_eos_modifiers.cpp:160-167): shifted by 0.1, scaled by 2
+    assert list(fx["c5_d"][:, 0]) == [0.0, 0.25, 4.0, -0.75]
+    print(f"PT derivatives: worst bitwise fraction {worst:.4f}")

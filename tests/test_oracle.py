@@ -235,3 +235,30 @@ def test_port_rejects_modified_eos():
     d = rb.eos_desc(rb.IDEAL, [0.4, 0.718e7], shift=1.0)
     with pytest.raises(RuntimeError):
         rb.port().eos_vec(d, 3, np.array([1.0]), np.array([1.0]))
+
+
+@needs_reference
+def test_pt_derivatives_known_answers():
+    # IdealGas answers in closed form (eos_ideal.hpp:152-168); StiffGas takes
+    # the base class's one-sided differences (eos_base.hpp:299-320), which
+    # must approach rho = (P + Pinf) / (gm1 Cv T), e = Cv T + Pinf / rho + q
+    ref = rb.reference()
+    gm1, Cv = 0.4, 0.718e7
+    rho, T = np.array([1e-3, 0.2, 3.0]), np.array([300.0, 2e3, 5e4])
+    d = rb.eos_desc(rb.IDEAL, [gm1, Cv])
+    sie, P = Cv * T, gm1 * rho * Cv * T
+    dedP, drdP, dedT, drdT = ref.pt_derivs(d, rho, sie, P, T)
+    np.testing.assert_array_equal(dedP, 0.0)
+    np.testing.assert_array_equal(dedT, Cv)
+    np.testing.assert_allclose(drdP, 1.0 / (gm1 * sie), rtol=1e-15)
+    np.testing.assert_allclose(drdT, -P / (gm1 * Cv * T * T), rtol=1e-15)
+    gm1, Cv, Pinf, q = 3.4, 1.816e7, 6e9, 0.0
+    d = rb.eos_desc(rb.STIFF, [gm1, Cv, Pinf, q])
+    rho, T = np.array([0.8, 1.0, 1.5]), np.array([300.0, 600.0, 1200.0])
+    sie = ref.eos_vec(d, 1, rho, T)
+    P = ref.eos_vec(d, 2, rho, T)
+    dedP, drdP, dedT, drdT = ref.pt_derivs(d, rho, sie, P, T)
+    drdP_exact = 1.0 / (gm1 * Cv * T)
+    np.testing.assert_allclose(drdP, drdP_exact, rtol=1e-4)
+    np.testing.assert_allclose(drdT, -(P + Pinf) / (gm1 * Cv * T * T), rtol=1e-4)
+    np.testing.assert_allclose(dedP, -Pinf / rho**2 * drdP_exact, rtol=1e-4)
