@@ -88,8 +88,15 @@ enum {
   SGX_FN_B_FROM_RHO_SIE = 7,  /* BulkModulusFromDensityInternalEnergy */
   SGX_FN_G_FROM_RHO_T = 8,    /* GruneisenParamFromDensityTemperature */
   SGX_FN_G_FROM_RHO_SIE = 9,  /* GruneisenParamFromDensityInternalEnergy */
-  SGX_FN_MIN_SIE_FROM_RHO = 10 /* MinInternalEnergyFromDensity (in2 unused) */
+  SGX_FN_MIN_SIE_FROM_RHO = 10, /* MinInternalEnergyFromDensity (in2 unused) */
+  SGX_FN_S_FROM_RHO_T = 11,     /* EntropyFromDensityTemperature */
+  SGX_FN_S_FROM_RHO_SIE = 12,   /* EntropyFromDensityInternalEnergy */
+  SGX_FN_SIE_FROM_RHO_P = 13    /* InternalEnergyFromDensityPressure (in2 = P) */
 };
+/* Entropy exists for IdealGas, StiffGas and NobleAbel (and their modified
+ * forms); Gruneisen and the tabulated model abort in the reference
+ * (EntropyIsNotEnabled) and return SGX_ERR_UNSUPPORTED here. Helmholtz takes
+ * functions 0..9. */
 
 /* Modifier bits of sgx_eos.mods (eos/modifiers/). The reference's EOS
  * variant holds a model, Shifted<model>, Scaled<model>,
@@ -192,6 +199,17 @@ const char *sgx_last_error(void);
 int sgx_eos_ideal_gas(sgx_eos *out, double gm1, double Cv);
 int sgx_eos_stiff_gas(sgx_eos *out, double gm1, double Cv, double Pinf, double qq);
 int sgx_eos_noble_abel(sgx_eos *out, double gm1, double Cv, double bb, double qq);
+/* The constructors with a reference state: IdealGas(gm1, Cv, EntropyT0,
+ * EntropyRho0) (eos_ideal.hpp:49-56) and StiffGas / NobleAbel(..., qp, T0,
+ * P0) (eos_stiff.hpp:52-59, eos_noble_abel.hpp:52-60). The reference state
+ * enters the entropy and ValuesAtReferenceState only; the short forms above
+ * use STP (293 K, 1e6) and qp = 0, as the reference's do. */
+int sgx_eos_ideal_gas_entropy(sgx_eos *out, double gm1, double Cv, double EntropyT0,
+                              double EntropyRho0);
+int sgx_eos_stiff_gas_ref(sgx_eos *out, double gm1, double Cv, double Pinf, double qq,
+                          double qp, double T0, double P0);
+int sgx_eos_noble_abel_ref(sgx_eos *out, double gm1, double Cv, double bb, double qq,
+                           double qp, double T0, double P0);
 /* rho_max <= 0 computes it from the Us-up polynomial
  * (Gruneisen::ComputeRhoMax, eos_gruneisen.hpp:231-329). */
 int sgx_eos_gruneisen(sgx_eos *out, double C0, double s1, double s2, double s3,

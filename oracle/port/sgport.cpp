@@ -1272,6 +1272,7 @@ bool make_eos(const sgref_eos *d, int n, std::vector<port::Eos> &out) {
   out.resize(n);
   for (int k = 0; k < n; ++k) {
     if (d[k].mods != 0) return false;
+    if (d[k].type <= 3 && (d[k].flags & 2)) return false; // short constructors only
     out[k].type = d[k].type;
     for (int q = 0; q < 16; ++q)
       out[k].p[q] = d[k].p[q];

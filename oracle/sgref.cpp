@@ -84,11 +84,16 @@ namespace {
 
 EOS make_model(const sgref_eos &d) {
   switch (d.type) {
+  // flags bit 1: the constructor with a reference state (IdealGas entropy
+  // reference in p[2..3]; StiffGas / NobleAbel qp, T0, P0 in p[4..6])
   case 1:
+    if (d.flags & 2) return IdealGas(d.p[0], d.p[1], d.p[2], d.p[3]);
     return IdealGas(d.p[0], d.p[1]);
   case 2:
+    if (d.flags & 2) return StiffGas(d.p[0], d.p[1], d.p[2], d.p[3], d.p[4], d.p[5], d.p[6]);
     return StiffGas(d.p[0], d.p[1], d.p[2], d.p[3]);
   case 3:
+    if (d.flags & 2) return NobleAbel(d.p[0], d.p[1], d.p[2], d.p[3], d.p[4], d.p[5], d.p[6]);
     return NobleAbel(d.p[0], d.p[1], d.p[2], d.p[3]);
   case 4:
     return Gruneisen(d.p[0], d.p[1], d.p[2], d.p[3], d.p[4], d.p[5], d.p[6], d.p[7],
@@ -342,6 +347,7 @@ int sgref_pte(int solver, int nmat_max, int ncell, const sgref_eos *descs, int n
 // Vector lookup through the Variant's vector overloads.
 // fn: 0 T(rho,e) 1 e(rho,T) 2 P(rho,T) 3 P(rho,e) 4 Cv(rho,T) 5 Cv(rho,e)
 //     6 B(rho,T) 7 B(rho,e) 8 G(rho,T) 9 G(rho,e) 10 emin(rho)
+//     11 S(rho,T) 12 S(rho,e) 13 e(rho,P)
 // lambda (nullable) is row-per-element with lambda_stride doubles.
 int sgref_eos_vec(const sgref_eos *desc, int fn, int n, const double *in1,
                   const double *in2, double *out, double *lambda, int lambda_stride) {
@@ -381,6 +387,15 @@ int sgref_eos_vec(const sgref_eos *desc, int fn, int n, const double *in1,
         break;
       case 10:
         eos.MinInternalEnergyFromDensity(in1, out, n, lam);
+        break;
+      case 11:
+        eos.EntropyFromDensityTemperature(in1, in2, out, n, lam);
+        break;
+      case 12:
+        eos.EntropyFromDensityInternalEnergy(in1, in2, out, n, lam);
+        break;
+      case 13:
+        eos.InternalEnergyFromDensityPressure(in1, in2, out, n, lam);
         break;
       default:
         PORTABLE_ALWAYS_THROW_OR_ABORT("sgref_eos_vec: unknown function");

@@ -12,6 +12,7 @@
 
 #include <cuda_runtime.h>
 
+#include "sgx_eos.cuh"
 #include "sgx_internal.h"
 #include "sgx_table.h"
 
@@ -107,18 +108,33 @@ int sgx_pte_rhou_required_scratch(int nmat) {
   return 4 * nmat * nmat + 4 * 2 * nmat + 8 * nmat;
 }
 
-int sgx_eos_ideal_gas(sgx_eos *out, double gm1, double Cv) {
+int sgx_eos_ideal_gas_entropy(sgx_eos *out, double gm1, double Cv, double EntropyT0,
+                              double EntropyRho0) {
   if (!out) return fail(SGX_ERR_INVALID, "sgx_eos_ideal_gas: null");
   // IdealGas::CheckParams (eos_ideal.hpp:65-76)
   if (!(Cv >= 0) || !(gm1 >= 0)) return fail(SGX_ERR_INVALID, "IdealGas: Cv and gm1 must be >= 0");
+  if (!(EntropyT0 >= 0))
+    return fail(SGX_ERR_INVALID, "Entropy reference temperature must be positive");
+  if (!(EntropyRho0 >= 0))
+    return fail(SGX_ERR_INVALID, "Entropy reference density must be positive");
   std::memset(out, 0, sizeof(*out));
   out->type = SGX_IDEAL_GAS;
   out->p[0] = gm1;
   out->p[1] = Cv;
+  out->p[sgx::pi::ST0] = EntropyT0;
+  out->p[sgx::pi::SRho0] = EntropyRho0;
   return SGX_OK;
 }
 
-int sgx_eos_stiff_gas(sgx_eos *out, double gm1, double Cv, double Pinf, double qq) {
+int sgx_eos_ideal_gas(sgx_eos *out, double gm1, double Cv) {
+  // IdealGas(gm1, Cv) (eos_ideal.hpp:41-47): the entropy reference is the
+  // STP state, T0 and rho0 = P0 / (gm1 Cv T0)
+  const double T0 = sgx::ROOM_TEMPERATURE, P0 = sgx::ATMOSPHERIC_PRESSURE;
+  return sgx_eos_ideal_gas_entropy(out, gm1, Cv, T0, P0 / (gm1 * Cv * T0));
+}
+
+int sgx_eos_stiff_gas_ref(sgx_eos *out, double gm1, double Cv, double Pinf, double qq,
+                          double qp, double T0, double P0) {
   if (!out) return fail(SGX_ERR_INVALID, "sgx_eos_stiff_gas: null");
   if (!(Cv >= 0) || !(gm1 >= 0)) return fail(SGX_ERR_INVALID, "StiffGas: Cv and gm1 must be >= 0");
   std::memset(out, 0, sizeof(*out));
@@ -127,10 +143,20 @@ int sgx_eos_stiff_gas(sgx_eos *out, double gm1, double Cv, double Pinf, double q
   out->p[1] = Cv;
   out->p[2] = Pinf;
   out->p[3] = qq;
+  out->p[sgx::pi::qp] = qp;
+  out->p[sgx::pi::rT0] = T0;
+  out->p[sgx::pi::rP0] = P0;
   return SGX_OK;
 }
 
-int sgx_eos_noble_abel(sgx_eos *out, double gm1, double Cv, double bb, double qq) {
+int sgx_eos_stiff_gas(sgx_eos *out, double gm1, double Cv, double Pinf, double qq) {
+  // StiffGas(gm1, Cv, Pinf, qq) (eos_stiff.hpp:40-50): qp 0, STP
+  return sgx_eos_stiff_gas_ref(out, gm1, Cv, Pinf, qq, 0.0, sgx::ROOM_TEMPERATURE,
+                               sgx::ATMOSPHERIC_PRESSURE);
+}
+
+int sgx_eos_noble_abel_ref(sgx_eos *out, double gm1, double Cv, double bb, double qq,
+                           double qp, double T0, double P0) {
   if (!out) return fail(SGX_ERR_INVALID, "sgx_eos_noble_abel: null");
   if (!(Cv > 0) || !(gm1 >= 0) || !(bb >= 0))
     return fail(SGX_ERR_INVALID, "NobleAbel: Cv > 0, gm1 >= 0 and b >= 0 required");
@@ -140,7 +166,16 @@ int sgx_eos_noble_abel(sgx_eos *out, double gm1, double Cv, double bb, double qq
   out->p[1] = Cv;
   out->p[2] = bb;
   out->p[3] = qq;
+  out->p[sgx::pi::qp] = qp;
+  out->p[sgx::pi::rT0] = T0;
+  out->p[sgx::pi::rP0] = P0;
   return SGX_OK;
+}
+
+int sgx_eos_noble_abel(sgx_eos *out, double gm1, double Cv, double bb, double qq) {
+  // NobleAbel(gm1, Cv, bb, qq) (eos_noble_abel.hpp:40-50): qp 0, STP
+  return sgx_eos_noble_abel_ref(out, gm1, Cv, bb, qq, 0.0, sgx::ROOM_TEMPERATURE,
+                                sgx::ATMOSPHERIC_PRESSURE);
 }
 
 int sgx_eos_gruneisen(sgx_eos *out, double C0, double s1, double s2, double s3, double G0,
@@ -226,8 +261,13 @@ long sgx_eos_spiner_dump(const sgx_eos *eos, double *out, long cap) {
 int sgx_eos_eval(const sgx_eos *eos, int fn, int64_t n, const double *in1, const double *in2,
                  double *out, double *lambda, int lambda_stride, sgx_stream_t stream) {
   if (!eos || !valid_type(eos->type)) return fail(SGX_ERR_INVALID, "sgx_eos_eval: bad eos");
-  if (fn < SGX_FN_T_FROM_RHO_SIE || fn > SGX_FN_MIN_SIE_FROM_RHO)
+  if (fn < SGX_FN_T_FROM_RHO_SIE || fn > SGX_FN_SIE_FROM_RHO_P)
     return fail(SGX_ERR_INVALID, "sgx_eos_eval: bad fn");
+  if ((fn == SGX_FN_S_FROM_RHO_T || fn == SGX_FN_S_FROM_RHO_SIE) &&
+      eos->type != SGX_IDEAL_GAS && eos->type != SGX_STIFF_GAS && eos->type != SGX_NOBLE_ABEL)
+    return fail(SGX_ERR_UNSUPPORTED, "sgx_eos_eval: Entropy is not enabled for this EOS");
+  if (fn > SGX_FN_MIN_SIE_FROM_RHO && eos->type == SGX_HELMHOLTZ)
+    return fail(SGX_ERR_UNSUPPORTED, "sgx_eos_eval: Helmholtz takes functions 0..9 here");
   if (n < 0) return fail(SGX_ERR_INVALID, "sgx_eos_eval: n < 0");
   if (n == 0) return SGX_OK;
   if (!in1 || !out || (!in2 && fn != SGX_FN_MIN_SIE_FROM_RHO))

@@ -108,6 +108,7 @@ SGX_HD double md_min_density(const sgx_eos &e) {
 SGX_HD double md_reference_T(const sgx_eos &e) {
   if (is_spiner(e)) return sp_table(e).TNormal;
   if (e.type == SGX_GRUNEISEN) return e.p[7];
+  if (e.type == SGX_STIFF_GAS || e.type == SGX_NOBLE_ABEL) return e.p[pi::rT0];
   return ROOM_TEMPERATURE;
 }
 // Density, temperature, pressure and bulk modulus of ValuesAtReferenceState,
@@ -127,19 +128,19 @@ SGX_HDI void md_reference_state(const sgx_eos &e, double &rho, double &temp, dou
     bmod = (gm1 + 1) * gm1 * rho * Cv * T0;
     return;
   case SGX_STIFF_GAS: {
-    const double Pinf = e.p[pi::Pinf];
-    rho = ratio(P0 + Pinf, gm1 * Cv * T0);
-    temp = T0;
-    press = P0;
-    bmod = gm1 * (gm1 + 1.0) * ratio(P0 + Pinf, gm1 * Cv * T0) * Cv * T0;
+    const double Pinf = e.p[pi::Pinf], sT0 = e.p[pi::rT0], sP0 = e.p[pi::rP0];
+    rho = ratio(sP0 + Pinf, gm1 * Cv * sT0);
+    temp = sT0;
+    press = sP0;
+    bmod = gm1 * (gm1 + 1.0) * ratio(sP0 + Pinf, gm1 * Cv * sT0) * Cv * sT0;
     return;
   }
   case SGX_NOBLE_ABEL: {
-    const double bb = e.p[pi::bb];
-    rho = ratio(P0, gm1 * Cv * T0 + bb * P0);
-    temp = T0;
-    press = P0;
-    bmod = ratio(rho * Cv * T0 * gm1 * (gm1 + 1.0), (1.0 - bb * rho) * (1.0 - bb * rho));
+    const double bb = e.p[pi::bb], nT0 = e.p[pi::rT0], nP0 = e.p[pi::rP0];
+    rho = ratio(nP0, gm1 * Cv * nT0 + bb * nP0);
+    temp = nT0;
+    press = nP0;
+    bmod = ratio(rho * Cv * nT0 * gm1 * (gm1 + 1.0), (1.0 - bb * rho) * (1.0 - bb * rho));
     return;
   }
   case SGX_GRUNEISEN:
@@ -508,6 +509,131 @@ SGX_HDI void ev_fill(const sgx_eos &e, double &rho, double &temp, double &sie, d
 }
 
 // ---------------------------------------------------------------------------
+// Entropy (the SG_EOS_VEC_FOR(Entropy) vector members, eos_base.hpp:497).
+// The analytic gases use their reference state, kept in p[] by the
+// constructors (STP, 293 K and 1e6, and qp = 0 unless given):
+//   IdealGas  eos_ideal.hpp:100-114 (EntropyT0, EntropyRho0)
+//   StiffGas  eos_stiff.hpp:93-109
+//   NobleAbel eos_noble_abel.hpp:100-119
+// Gruneisen and the tabulated model have no entropy (EntropyIsNotEnabled,
+// eos_base.hpp:588-600, which aborts); the C API rejects them.
+SGX_HDI double md_entropy_rho_T(const sgx_eos &e, const double rho, const double T) {
+  const double gm1 = e.p[pi::gm1], Cv = e.p[pi::Cv];
+  const double T0 = e.p[pi::rT0], P0 = e.p[pi::rP0], qp = e.p[pi::qp];
+  const double SMALL = lim<double>::small;
+  switch (e.type) {
+  case SGX_IDEAL_GAS:
+    return Cv * log(ratio(T, e.p[pi::ST0])) + gm1 * Cv * log(ratio(e.p[pi::SRho0], rho));
+  case SGX_STIFF_GAS: {
+    const double rho0 = ratio(P0 + e.p[pi::Pinf], gm1 * Cv * T0);
+    return Cv * log(ratio(T, T0) + SMALL) + gm1 * Cv * log(ratio(rho0, rho) + SMALL) + qp;
+  }
+  case SGX_NOBLE_ABEL: {
+    const double bb = e.p[pi::bb];
+    const double vol0 = ratio(gm1 * Cv * T0 + bb * P0, P0);
+    const double vol = ratio(1.0, rho);
+    return Cv * log(ratio(T, T0) + SMALL) +
+           gm1 * Cv * log(ratio(vol - bb, vol0 - bb) + SMALL) + qp;
+  }
+  }
+  return NAN;
+}
+SGX_HDI double md_entropy_rho_sie(const sgx_eos &e, const double rho, const double sie) {
+  const double gm1 = e.p[pi::gm1], Cv = e.p[pi::Cv];
+  const double T0 = e.p[pi::rT0], P0 = e.p[pi::rP0], qp = e.p[pi::qp];
+  const double SMALL = lim<double>::small;
+  switch (e.type) {
+  case SGX_IDEAL_GAS:
+    return md_entropy_rho_T(e, rho, eos_T_from_rho_sie<double>(e, rho, sie));
+  case SGX_STIFF_GAS: {
+    const double Pinf = e.p[pi::Pinf], qq = e.p[pi::qq];
+    const double vol0 = ratio(gm1 * Cv * T0, P0 + Pinf);
+    const double sie0 = ratio(P0 + (gm1 + 1.0) * Pinf, P0 + Pinf) * Cv * T0 + qq;
+    const double vol = ratio(1.0, rho);
+    return Cv * log(ratio((sie - qq - Pinf * vol), (sie0 - qq - Pinf * vol0)) + SMALL) +
+           Cv * gm1 * log(ratio(vol, vol0) + SMALL) + qp;
+  }
+  case SGX_NOBLE_ABEL: {
+    const double bb = e.p[pi::bb], qq = e.p[pi::qq];
+    const double vol0 = ratio(gm1 * Cv * T0 + bb * P0, P0);
+    const double sie0 = Cv * T0 + qq;
+    const double vol = ratio(1.0, rho);
+    return Cv * log(ratio(sie - qq, sie0 - qq) + SMALL) +
+           gm1 * Cv * log(ratio(vol - bb, vol0 - bb) + SMALL) + qp;
+  }
+  }
+  return NAN;
+}
+// Through the modifiers: ScaledEOS returns scale_ S(scale_ rho, sie / scale_)
+// (scaled_eos.hpp:92-97, 121-125); ShiftedEOS passes sie - shift_ and T as
+// is; BilinearRampEOS forwards.
+SGX_HDI double ev_entropy_rho_T(const sgx_eos &e, const double rho, const double T) {
+  const double S = md_entropy_rho_T(e, mrho(e, rho), T);
+  return (SGX_MODS(e) & SGX_MOD_SCALED) ? e.scale * S : S;
+}
+SGX_HDI double ev_entropy_rho_sie(const sgx_eos &e, const double rho, const double sie) {
+  const double S = md_entropy_rho_sie(e, mrho(e, rho), msie(e, sie));
+  return (SGX_MODS(e) & SGX_MOD_SCALED) ? e.scale * S : S;
+}
+
+// ---------------------------------------------------------------------------
+// InternalEnergyFromDensityPressure.
+
+// EosBase::InternalEnergyFromDensityPressure with sie in and out
+// (eos_base.hpp:685-707): regula falsi on P(rho, sie) between the energies
+// at the minimum temperature and at 1e20, from the middle when sie lies in
+// that range, else from sie. A root find that fails leaves what
+// regula_falsi leaves (the reference only warns).
+template <typename PF, typename EF>
+SGX_HDI void iefdp_base(const PF &P_of, const EF &e_of, const double minT, const double rho,
+                        const double P, double &sie) {
+  auto f = [&](const double s) { return P_of(rho, s); };
+  const double sie_min = e_of(rho, minT);
+  const double sie_max = e_of(rho, 1e20);
+  const double sie_guess =
+      (((sie_min < sie) && (sie < sie_max)) ? 0.5 * (sie_min + sie_max) : sie);
+  regula_falsi(f, P, sie_guess, sie_min, sie_max, lim<double>::eps, lim<double>::eps, sie);
+}
+// The bare models: IdealGas in closed form (eos_ideal.hpp:208-214), the
+// others through the base class.
+SGX_HDI void md_sie_from_rho_P(const sgx_eos &e, const double rho, const double P, double &sie,
+                               double *lam) {
+  if (e.type == SGX_IDEAL_GAS) {
+    sie = P / (e.p[pi::gm1] * rho);
+    return;
+  }
+  iefdp_base([&](const double r, const double s) { return md_P_from_rho_sie<double>(e, r, s, lam); },
+             [&](const double r, const double t) { return md_sie_from_rho_T<double>(e, r, t, lam); },
+             md_min_temperature(e), rho, P, sie);
+}
+// The sie-in-and-out member through the modifiers: BilinearRampEOS has none
+// and takes the base class's over its own P and sie (ramped pressure);
+// ScaledEOS passes scale_ rho (scaled_eos.hpp:141-146); ShiftedEOS shifts sie
+// in and back (shifted_eos.hpp:132-139).
+SGX_HDI void ev_sie_from_rho_P_inout(const sgx_eos &e, const double rho, const double P,
+                                     double &sie, double *lam) {
+  if (SGX_MODS(e) & SGX_MOD_RAMP) {
+    iefdp_base([&](const double r, const double s) { return ev_P_from_rho_sie<double>(e, r, s, lam); },
+               [&](const double r, const double t) { return ev_sie_from_rho_T<double>(e, r, t, lam); },
+               ev_min_temperature(e), rho, P, sie);
+    return;
+  }
+  if (SGX_MODS(e) & SGX_MOD_SHIFTED) sie -= e.shift;
+  md_sie_from_rho_P(e, mrho(e, rho), P, sie, lam);
+  if (SGX_MODS(e) & SGX_MOD_SHIFTED) sie += e.shift;
+}
+// The value-returning member the vector call loops over (eos_base.hpp:708-721):
+// start from the middle of the energy range, then the member above.
+SGX_HDI double ev_sie_from_rho_P(const sgx_eos &e, const double rho, const double P,
+                                 double *lam) {
+  const double sie_min = ev_sie_from_rho_T<double>(e, rho, ev_min_temperature(e), lam);
+  const double sie_max = ev_sie_from_rho_T<double>(e, rho, 1e20, lam);
+  double sie = 0.5 * (sie_min + sie_max);
+  ev_sie_from_rho_P_inout(e, rho, P, sie, lam);
+  return sie;
+}
+
+// ---------------------------------------------------------------------------
 // PTDerivativesFromPreferred: (dsie/dP)_T, (drho/dP)_T, (dsie/dT)_P and
 // (drho/dT)_P at a state (rho, sie, P, T).
 
@@ -610,6 +736,12 @@ SGX_HDI double ev_eval(const sgx_eos &e, const int fn, const double a, const dou
     return ev_gamma_from_rho_sie<double>(e, a, b, lam);
   case SGX_FN_MIN_SIE_FROM_RHO:
     return ev_min_sie<double>(e, a);
+  case SGX_FN_S_FROM_RHO_T:
+    return ev_entropy_rho_T(e, a, b);
+  case SGX_FN_S_FROM_RHO_SIE:
+    return ev_entropy_rho_sie(e, a, b);
+  case SGX_FN_SIE_FROM_RHO_P:
+    return ev_sie_from_rho_P(e, a, b, lam);
   }
   return 0.0;
 }

@@ -22,6 +22,11 @@ constexpr unsigned Q_CV = 16, Q_BMOD = 32;
 // Model parameter slots inside sgx_eos::p.
 namespace pi {
 constexpr int gm1 = 0, Cv = 1, Pinf = 2, qq = 3, bb = 2;
+// IdealGas entropy reference (EntropyT0, EntropyRho0; eos_ideal.hpp:49-56)
+constexpr int ST0 = 2, SRho0 = 3;
+// StiffGas / NobleAbel reference state (qp, T0, P0; eos_stiff.hpp:52-59,
+// eos_noble_abel.hpp:52-60)
+constexpr int qp = 4, rT0 = 5, rP0 = 6;
 // Gruneisen
 constexpr int C0 = 0, s1 = 1, s2 = 2, s3 = 3, G0 = 4, b = 5, rho0 = 6, T0 = 7, P0 = 8,
               gCv = 9, rho_max = 10;

@@ -35,7 +35,8 @@ EXPORTED = [
     "sgx_server_destroy", "sgx_host_alloc", "sgx_host_free", "sgx_eos_fill_host",
     "sgx_get_sg_eos", "sgx_eos_modify_shifted", "sgx_eos_modify_scaled",
     "sgx_eos_modify_bilinear_ramp", "sgx_eos_p_alpha_ramp_params", "sgx_eos_apply_modifiers",
-    "sgx_eos_pt_derivatives",
+    "sgx_eos_pt_derivatives", "sgx_eos_ideal_gas_entropy", "sgx_eos_stiff_gas_ref",
+    "sgx_eos_noble_abel_ref",
 ]
 MOD_SHIFTED, MOD_SCALED, MOD_RAMP = 1, 2, 4
 HELM_DEFAULT, HELM_REGULA_FALSI, HELM_CACHE_READBACK = 31, 32, 64
@@ -115,6 +116,9 @@ def load():
     lib.sgx_eos_ideal_gas.argtypes = [C.POINTER(SgxEos), D, D]
     lib.sgx_eos_stiff_gas.argtypes = [C.POINTER(SgxEos), D, D, D, D]
     lib.sgx_eos_noble_abel.argtypes = [C.POINTER(SgxEos), D, D, D, D]
+    lib.sgx_eos_ideal_gas_entropy.argtypes = [C.POINTER(SgxEos), D, D, D, D]
+    lib.sgx_eos_stiff_gas_ref.argtypes = [C.POINTER(SgxEos)] + [D] * 7
+    lib.sgx_eos_noble_abel_ref.argtypes = [C.POINTER(SgxEos)] + [D] * 7
     lib.sgx_eos_gruneisen.argtypes = [C.POINTER(SgxEos)] + [D] * 11
     lib.sgx_eos_spiner_rhot.argtypes = [C.POINTER(SgxEos), C.c_char_p, I, I]
     lib.sgx_eos_finalize.argtypes = [C.POINTER(SgxEos)]
@@ -186,10 +190,16 @@ def make_eos(kind, params):
     lib = load()
     e = SgxEos()
     p = list(params)
-    if kind == IDEAL_GAS:
+    if kind == IDEAL_GAS and len(p) >= 4:  # (gm1, Cv, EntropyT0, EntropyRho0)
+        check(lib.sgx_eos_ideal_gas_entropy(C.byref(e), *p[:4]))
+    elif kind == IDEAL_GAS:
         check(lib.sgx_eos_ideal_gas(C.byref(e), *p[:2]))
+    elif kind == STIFF_GAS and len(p) >= 7:  # (..., qp, T0, P0)
+        check(lib.sgx_eos_stiff_gas_ref(C.byref(e), *p[:7]))
     elif kind == STIFF_GAS:
         check(lib.sgx_eos_stiff_gas(C.byref(e), *p[:4]))
+    elif kind == NOBLE_ABEL and len(p) >= 7:
+        check(lib.sgx_eos_noble_abel_ref(C.byref(e), *p[:7]))
     elif kind == NOBLE_ABEL:
         check(lib.sgx_eos_noble_abel(C.byref(e), *p[:4]))
     elif kind == GRUNEISEN:

@@ -372,6 +372,63 @@ def pt_derivs_fixture(ref, path, n=256, seed=71):
     return out
 
 
+def vector_ext_fixture(ref, path, n=384, seed=81):
+    """EntropyFromDensityTemperature / EntropyFromDensityInternalEnergy
+    (fn 11, 12) and InternalEnergyFromDensityPressure (fn 13), bare and
+    modified; P inputs are P(rho, T) of the same EOS, so roots exist."""
+    rng = np.random.default_rng(seed)
+    air_ramp = ref.p_alpha(desc(W.IDEAL_AIR), 1.5, 5e6, 1e7)
+    cases = [  # (model or None, mods row, rho range, T range, entropy?)
+        (W.IDEAL_AIR, mods_row(), (1e-4, 1.0), (50.0, 1e5), True),
+        (W.STIFF_WATER, mods_row(), (0.5, 3.0), (200.0, 5e3), True),
+        (W.NOBLE_ABEL_GAS, mods_row(), (1e-4, 1.0), (50.0, 1e5), True),
+        (W.GRUNEISEN_CU, mods_row(), (8.0, 11.0), (300.0, 3e3), False),
+        (None, mods_row(), (0.5, 20.0), (300.0, 1e5), False),
+        ((rb.IDEAL, (0.5, 2.0)), mods_row(0.1, 2.0), (0.5, 3.0), (1.0, 10.0), True),
+        (W.IDEAL_AIR, mods_row(ramp=air_ramp), (0.3 * air_ramp[0], 30 * air_ramp[0]),
+         (50.0, 3e3), True),
+        (W.STIFF_WATER, mods_row(1e8, 1.02), (0.5, 3.0), (200.0, 5e3), True),
+        (None, mods_row(1e8, 1.5), (0.5, 10.0), (300.0, 1e5), False),
+    ]
+    out = {}
+    mats, rows = [], []
+    for k, (mat, row, (rlo, rhi), (tlo, thi), ent) in enumerate(cases):
+        d = mdesc(mat, row, path if mat is None else None)
+        rho = np.exp(rng.uniform(np.log(rlo), np.log(rhi), n))
+        T = np.exp(rng.uniform(np.log(tlo), np.log(thi), n))
+        sie = ref.eos_vec(d, 1, rho, T)
+        P = ref.eos_vec(d, 2, rho, T)
+        out[f"c{k}_rho"], out[f"c{k}_sie"], out[f"c{k}_P"], out[f"c{k}_T"] = rho, sie, P, T
+        if ent:
+            out[f"c{k}_fn11"] = ref.eos_vec(d, 11, rho, T)
+            out[f"c{k}_fn12"] = ref.eos_vec(d, 12, rho, sie)
+        out[f"c{k}_fn13"] = ref.eos_vec(d, 13, rho, P)
+        mats.append(mat if mat is not None else (rb.SPINER_RHOT, ()))
+        rows.append(row)
+    out["materials"] = mats_array(mats)
+    out["mods"] = np.array(rows)
+    # the constructors with a reference state (flags bit 1), at the states
+    # of the reference's own entropy tests (test_eos_ideal.cpp:44-90,
+    # test_eos_stiff.cpp:495-580) and at random ones
+    refs = [(rb.IDEAL, [0.4, 5.0, 100.0, 1e-3]),
+            (rb.STIFF, [1.35, 1816.e4, 1.0e9, 2030.00e+07, -23.0e+7, 200.0, 1e6]),
+            (rb.NOBLE_ABEL, [0.4, 0.718e7, 1e-3, 1e8, -2e7, 250.0, 2e6])]
+    for j, (kind, params) in enumerate(refs):
+        d = rb.eos_desc(kind, params, flags=2)
+        rho = np.exp(rng.uniform(np.log(1e-3), np.log(1.0), n))
+        T = np.exp(rng.uniform(np.log(50.0), np.log(1e4), n))
+        if j == 0:
+            rho[:3], T[:3] = [1e-3, 0.1, 1e-3], [100.0, 100.0, 10.0]
+        sie = ref.eos_vec(d, 1, rho, T)
+        if j == 1:
+            rho[0], sie[0] = 1.0218087167564040e-01, 3.7350567520918861e+10
+        out[f"r{j}_kind"], out[f"r{j}_params"] = np.int32(kind), np.array(params)
+        out[f"r{j}_rho"], out[f"r{j}_T"], out[f"r{j}_sie"] = rho, T, sie
+        out[f"r{j}_fn11"] = ref.eos_vec(d, 11, rho, T)
+        out[f"r{j}_fn12"] = ref.eos_vec(d, 12, rho, sie)
+    return out
+
+
 def modified_pte_fixture(ref, solver, seed):
     """PTE over materials with modifiers: an ideal gas under a p-alpha ramp
     next to a shifted and scaled stiff gas (two materials), and the batched
@@ -463,6 +520,8 @@ def main():
         fx["modifiers"]["table_sha256"] = np.array(sha)
         fx["pt_derivs"] = pt_derivs_fixture(ref, path)
         fx["pt_derivs"]["table_sha256"] = np.array(sha)
+        fx["eos_vector_ext"] = vector_ext_fixture(ref, path)
+        fx["eos_vector_ext"]["table_sha256"] = np.array(sha)
     fx["pte_rhot_modified"] = modified_pte_fixture(ref, 0, 131)
     fx["pte_pt_modified"] = modified_pte_fixture(ref, 1, 133)
     fx["get_sg_eos"] = sgeos_fixture(ref)

@@ -222,3 +222,52 @@ def test_pt_derivatives(sgx, table):
     # (test_eos_modifiers.cpp:160-167): shifted by 0.1, scaled by 2
     assert list(fx["c5_d"][:, 0]) == [0.0, 0.25, 4.0, -0.75]
     print(f"PT derivatives: worst bitwise fraction {worst:.4f}")
+
+
+def test_entropy_and_sie_from_rho_P(sgx, table):
+    # EntropyFromDensityTemperature / EntropyFromDensityInternalEnergy
+    # (fn 11, 12) and InternalEnergyFromDensityPressure (fn 13), bare and
+    # modified (tests/golden/make_golden.py eos_vector_ext). Entropy goes
+    # through log, whose CUDA and glibc results may differ in the last bit:
+    # it is held to 1e-12 of the largest magnitude in the batch.
+    fx = golden("eos_vector_ext")
+    assert str(fx["table_sha256"]) == str(golden("modifiers")["table_sha256"])
+    mats = materials_from_rows(fx["materials"])
+    for k, (mat, row) in enumerate(zip(mats, fx["mods"])):
+        e = case_eos(sgx, table, mat, row)
+        rho = dev(fx[f"c{k}_rho"])
+        for fn, second in ((11, "T"), (12, "sie"), (13, "P")):
+            key = f"c{k}_fn{fn}"
+            out = torch.empty_like(rho)
+            if key not in fx:
+                # Gruneisen and the table have no entropy
+                with pytest.raises(RuntimeError, match="sgx error 5"):
+                    sgx.eval_eos(e, fn, rho, dev(fx[f"c{k}_{second}"]), out)
+                continue
+            sgx.eval_eos(e, fn, rho, dev(fx[f"c{k}_{second}"]), out)
+            torch.cuda.synchronize()
+            got, ref = out.cpu().numpy(), fx[key]
+            if fn == 13:
+                close(got, ref, f"case {k} fn {fn}")
+            else:
+                np.testing.assert_allclose(got, ref, rtol=1e-12,
+                                           atol=1e-12 * np.abs(ref).max(),
+                                           err_msg=f"case {k} fn {fn}")
+
+
+def test_entropy_with_reference_states(sgx):
+    # the constructors with a reference state, at the reference's own test
+    # states (the first rows) and at random ones
+    fx = golden("eos_vector_ext")
+    for j in range(3):
+        e = sgx.make_eos(int(fx[f"r{j}_kind"]), tuple(fx[f"r{j}_params"]))
+        rho = dev(fx[f"r{j}_rho"])
+        for fn, second in ((11, "T"), (12, "sie")):
+            out = torch.empty_like(rho)
+            sgx.eval_eos(e, fn, rho, dev(fx[f"r{j}_{second}"]), out)
+            torch.cuda.synchronize()
+            ref = fx[f"r{j}_fn{fn}"]
+            np.testing.assert_allclose(out.cpu().numpy(), ref, rtol=1e-12,
+                                       atol=1e-12 * np.abs(ref).max(),
+                                       err_msg=f"ref case {j} fn {fn}")
+    assert fx["r0_fn11"][0] == 0.0 and fx["r1_fn12"][0] == -2.0044437857420778e+08

@@ -262,3 +262,22 @@ def test_pt_derivatives_known_answers():
     np.testing.assert_allclose(drdP, drdP_exact, rtol=1e-4)
     np.testing.assert_allclose(drdT, -(P + Pinf) / (gm1 * Cv * T * T), rtol=1e-4)
     np.testing.assert_allclose(dedP, -Pinf / rho**2 * drdP_exact, rtol=1e-4)
+
+
+@needs_reference
+def test_entropy_known_answers():
+    ref = rb.reference()
+    # test_eos_ideal.cpp:44-90: zero at the reference state, and the two
+    # closed forms when rho^3 or T^2 equals its reference
+    gm1, Cv, T0, rho0 = 0.4, 5.0, 100.0, 1e-3
+    d = rb.eos_desc(rb.IDEAL, [gm1, Cv, T0, rho0], flags=2)
+    S = ref.eos_vec(d, 11, np.array([rho0, 0.1, rho0]), np.array([T0, T0, 10.0]))
+    assert S[0] == 0.0
+    np.testing.assert_allclose(S[1:], [2. / 3. * gm1 * Cv * np.log(rho0),
+                                       -1. / 2. * Cv * np.log(T0)], rtol=1e-12)
+    # test_eos_stiff.cpp:495-580: S(rho, e) of the seven-parameter stiff gas
+    d = rb.eos_desc(rb.STIFF, [1.35, 1816.e4, 1.0e9, 2030.00e+07, -23.0e+7, 200.0, 1e6],
+                    flags=2)
+    S = ref.eos_vec(d, 12, np.array([1.0218087167564040e-01]),
+                    np.array([3.7350567520918861e+10]))
+    np.testing.assert_allclose(S, [-2.0044437857420778e+08], rtol=1e-12)
