@@ -280,16 +280,17 @@ class Oracle:
         f(C.c_int(which), C.c_int(nmat), C.c_int(ncell), _ip(eos_idx), _dp(tot), _dp(tot_rho),
           _dp(rho), _dp(vfrac), _dp(sie))
 
-    def pt_derivs(self, desc, rho, sie, P, T):
+    def pt_derivs(self, desc, rho, sie, P, T, lam=None, lam_stride=0):
         """PTDerivativesFromPreferred per element (reference library only):
-        returns (dedP_T, drdP_T, dedT_P, drdT_P)."""
+        returns (dedP_T, drdP_T, dedT_P, drdT_P); lam (rows of lam_stride,
+        updated in place) may be None."""
         n = rho.size
         out = np.zeros(4 * n)
         f = self._fn("pt_derivs")
         f.restype = C.c_int
         rc = f(C.byref(desc), C.c_int(n), _dp(np.ascontiguousarray(rho, np.float64)),
                _dp(np.ascontiguousarray(sie, np.float64)), _dp(np.ascontiguousarray(P, np.float64)),
-               _dp(np.ascontiguousarray(T, np.float64)), _dp(out))
+               _dp(np.ascontiguousarray(T, np.float64)), _dp(out), _dp(lam), C.c_int(lam_stride))
         if rc != 0:
             raise RuntimeError("pt_derivs failed")
         return tuple(out.reshape(4, n))

@@ -455,14 +455,18 @@ int sgref_rho_sie_from_pt(const sgref_eos *desc, int n, const double *P, const d
 
 // PTDerivativesFromPreferred through the Variant (eos_variant.hpp:386-398)
 // at n states; out = [dedP_T | drdP_T | dedT_P | drdT_P], n each.
+// lambda (nullable) is row-per-element with lambda_stride doubles. A null
+// lambda leaves SpinerEOSDependsRhoT::lRhoFromPlT_ reading an uninitialised
+// cache (eos_spiner_rho_temp.hpp:1147-1151), so fixtures pass rows of NaN.
 int sgref_pt_derivs(const sgref_eos *desc, int n, const double *rho, const double *sie,
-                    const double *P, const double *T, double *out) {
+                    const double *P, const double *T, double *out, double *lambda,
+                    int lambda_stride) {
   try {
     EOS eos = make_eos(*desc);
     for (int i = 0; i < n; ++i) {
       Real a, b, c, d;
-      eos.PTDerivativesFromPreferred(rho[i], sie[i], P[i], T[i], static_cast<Real *>(nullptr),
-                                     a, b, c, d);
+      Real *lam = lambda ? lambda + static_cast<std::size_t>(lambda_stride) * i : nullptr;
+      eos.PTDerivativesFromPreferred(rho[i], sie[i], P[i], T[i], lam, a, b, c, d);
       out[i] = a;
       out[n + i] = b;
       out[2 * n + i] = c;

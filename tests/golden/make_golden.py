@@ -364,7 +364,12 @@ def pt_derivs_fixture(ref, path, n=256, seed=71):
         sie = ref.eos_vec(d, 1, rho, T)
         P = ref.eos_vec(d, 2, rho, T)
         out[f"c{k}_rho"], out[f"c{k}_sie"], out[f"c{k}_P"], out[f"c{k}_T"] = rho, sie, P, T
-        out[f"c{k}_d"] = np.array(ref.pt_derivs(d, rho, sie, P, T))
+        # lambda rows of NaN: with none, the tabulated model's
+        # DensityEnergyFromPressureTemperature starts its root find from an
+        # uninitialised cache (eos_spiner_rho_temp.hpp:1147-1151)
+        lam = np.full(2 * n, np.nan)
+        out[f"c{k}_d"] = np.array(ref.pt_derivs(d, rho, sie, P, T, lam=lam, lam_stride=2))
+        out[f"c{k}_lambda"] = lam
         mats.append(mat if mat is not None else (rb.SPINER_RHOT, ()))
         rows.append(row)
     out["materials"] = mats_array(mats)

@@ -214,10 +214,12 @@ def test_pt_derivatives(sgx, table):
     for k, (mat, row) in enumerate(zip(mats, fx["mods"])):
         e = case_eos(sgx, table, mat, row)
         t = [dev(fx[f"c{k}_{q}"]) for q in ("rho", "sie", "P", "T")]
-        got = sgx.pt_derivatives(e, *t)
+        lam = dev(np.full(2 * t[0].numel(), np.nan))
+        got = sgx.pt_derivatives(e, *t, lam=lam, lam_stride=2)
         torch.cuda.synchronize()
         for j, name in enumerate(("dedP_T", "drdP_T", "dedT_P", "drdT_P")):
             worst = min(worst, close(got[j].cpu().numpy(), fx[f"c{k}_d"][j], f"case {k} {name}"))
+        close(lam.cpu().numpy(), fx[f"c{k}_lambda"], f"case {k} lambda")
     # the ideal gas in closed form at the reference test's state
     # (test_eos_modifiers.cpp:160-167): shifted by 0.1, scaled by 2
     assert list(fx["c5_d"][:, 0]) == [0.0, 0.25, 4.0, -0.75]
