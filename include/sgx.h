@@ -483,6 +483,45 @@ int sgx_get_sg_eos(int nmat, int ncell, int cell_dim, int input_int, const int *
                    double *frac_ie, double *frac_bmod, double *frac_dpde, double *frac_cv,
                    double mass_frac_cutoff, int precision, sgx_stream_t stream);
 
+/* ---- The reference's C interface (eos/singularity_eos.hpp:25-134) ----
+ * Same argument lists with an sgx_ prefix, over sgx_eos values. enabled /
+ * vals NULL take the reference's defaults (no modifiers); otherwise they
+ * are applied as sgx_eos_apply_modifiers does. get_sg_* arrays are device
+ * arrays; the lookups are ordered on the legacy default stream; stride -1
+ * or lambda_data NULL means no lambda (lambdaIndexer2D otherwise). */
+int sgx_init_sg_eos(int nmat, sgx_eos **eos);
+int sgx_init_sg_IdealGas(int matindex, sgx_eos *eos, double gm1, double Cv, const int *enabled,
+                         double *vals);
+int sgx_init_sg_StiffGas(int matindex, sgx_eos *eos, double gm1, double Cv, double Pinf,
+                         double qq, const int *enabled, double *vals);
+int sgx_init_sg_NobleAbel(int matindex, sgx_eos *eos, double gm1, double Cv, double bb,
+                          double qq, const int *enabled, double *vals);
+int sgx_init_sg_Gruneisen(int matindex, sgx_eos *eos, double C0, double s1, double s2,
+                          double s3, double G0, double b, double rho0, double T0, double P0,
+                          double Cv, const int *enabled, double *vals);
+/* split: TableSplit::Total (0) only. */
+int sgx_init_sg_SpinerDependsRhoT(int matindex, sgx_eos *eos, const char *filename, int id,
+                                  int split, const int *enabled, double *vals);
+int sgx_init_sg_Helmholtz(int matindex, sgx_eos *eos, const char *filename, int rad, int gas,
+                          int coul, int ion, int ele, int verbose, const int *enabled,
+                          double *vals);
+int sgx_get_sg_EntropyFromDensityInternalEnergy(int matindex, const sgx_eos *eos,
+                                                const double *rhos, const double *sies,
+                                                double *entropies, int len, int stride,
+                                                double *lambda_data);
+int sgx_get_sg_PressureFromDensityInternalEnergy(int matindex, const sgx_eos *eos,
+                                                 const double *rhos, const double *sies,
+                                                 double *pressures, int len, int stride,
+                                                 double *lambda_data);
+int sgx_get_sg_MinInternalEnergyFromDensity(int matindex, const sgx_eos *eos,
+                                            const double *rhos, double *sies, int len);
+int sgx_get_sg_BulkModulusFromDensityInternalEnergy(int matindex, const sgx_eos *eos,
+                                                    const double *rhos, const double *sies,
+                                                    double *bmods, int len, int stride,
+                                                    double *lambda_data);
+/* Releases every EOS's device table, then the array; *eos becomes NULL. */
+int sgx_finalize_sg_eos(int nmat, sgx_eos **eos);
+
 /* ---- Serving: a device-resident request loop for PTE closure batches ----
  * No reference counterpart: the reference is a library called once per
  * batch (get_sg_eos, singularity_eos.hpp:114-132). The server keeps the EOS

@@ -36,7 +36,11 @@ EXPORTED = [
     "sgx_get_sg_eos", "sgx_eos_modify_shifted", "sgx_eos_modify_scaled",
     "sgx_eos_modify_bilinear_ramp", "sgx_eos_p_alpha_ramp_params", "sgx_eos_apply_modifiers",
     "sgx_eos_pt_derivatives", "sgx_eos_ideal_gas_entropy", "sgx_eos_stiff_gas_ref",
-    "sgx_eos_noble_abel_ref",
+    "sgx_eos_noble_abel_ref", "sgx_init_sg_eos", "sgx_init_sg_IdealGas", "sgx_init_sg_StiffGas",
+    "sgx_init_sg_NobleAbel", "sgx_init_sg_Gruneisen", "sgx_init_sg_SpinerDependsRhoT",
+    "sgx_init_sg_Helmholtz", "sgx_get_sg_EntropyFromDensityInternalEnergy",
+    "sgx_get_sg_PressureFromDensityInternalEnergy", "sgx_get_sg_MinInternalEnergyFromDensity",
+    "sgx_get_sg_BulkModulusFromDensityInternalEnergy", "sgx_finalize_sg_eos",
 ]
 MOD_SHIFTED, MOD_SCALED, MOD_RAMP = 1, 2, 4
 HELM_DEFAULT, HELM_REGULA_FALSI, HELM_CACHE_READBACK = 31, 32, 64
@@ -165,6 +169,19 @@ def load():
     lib.sgx_eos_apply_modifiers.argtypes = [C.POINTER(SgxEos), C.POINTER(C.c_int),
                                             C.POINTER(C.c_double)]
     lib.sgx_eos_pt_derivatives.argtypes = [C.POINTER(SgxEos), C.c_int64] + [P] * 9 + [I, P]
+    PE = C.POINTER(SgxEos)
+    lib.sgx_init_sg_eos.argtypes = [I, C.POINTER(PE)]
+    lib.sgx_init_sg_IdealGas.argtypes = [I, PE, D, D, P, P]
+    lib.sgx_init_sg_StiffGas.argtypes = [I, PE, D, D, D, D, P, P]
+    lib.sgx_init_sg_NobleAbel.argtypes = [I, PE, D, D, D, D, P, P]
+    lib.sgx_init_sg_Gruneisen.argtypes = [I, PE] + [D] * 10 + [P, P]
+    lib.sgx_init_sg_SpinerDependsRhoT.argtypes = [I, PE, C.c_char_p, I, I, P, P]
+    lib.sgx_init_sg_Helmholtz.argtypes = [I, PE, C.c_char_p, I, I, I, I, I, I, P, P]
+    for name in ("Entropy", "Pressure", "BulkModulus"):
+        getattr(lib, f"sgx_get_sg_{name}FromDensityInternalEnergy").argtypes = [
+            I, PE, P, P, P, I, I, P]
+    lib.sgx_get_sg_MinInternalEnergyFromDensity.argtypes = [I, PE, P, P, I]
+    lib.sgx_finalize_sg_eos.argtypes = [I, C.POINTER(PE)]
     _lib = lib
     return lib
 

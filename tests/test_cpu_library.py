@@ -17,7 +17,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def declared_symbols():
     txt = open(os.path.join(ROOT, "include", "sgx.h")).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    return sorted(set(re.findall(r"\b(sgx_[a-z0-9_]+)\s*\(", txt)))
+    return sorted(set(re.findall(r"\b(sgx_[A-Za-z0-9_]+)\s*\(", txt)))
 
 
 @pytest.fixture(scope="module")
@@ -167,3 +167,24 @@ def test_modifier_checks_without_gpu():
     # shift and scale without a ramp need no device
     sc, _ = L.apply_modifiers(e, [1, 1, 0, 0], [2.0, 0.1, 0, 0, 0, 0])
     assert (sc.mods, sc.scale, sc.shift) == (3, 2.0, 0.1)
+
+
+def test_init_sg_interface_without_gpu():
+    # init_sg_eos / init_sg_<model> / finalize_sg_eos (singularity_eos.cpp)
+    # over sgx_eos values; shift and scale need no device
+    from sgx import lib as L
+    lib = L.load()
+    arr = C.POINTER(L.SgxEos)()
+    assert lib.sgx_init_sg_eos(3, C.byref(arr)) == 0
+    assert lib.sgx_init_sg_IdealGas(0, arr, 0.4, 0.718e7, None, None) == 0
+    en = (C.c_int * 4)(1, 1, 0, 0)
+    vals = (C.c_double * 6)(2.0, 0.1, 0, 0, 0, 0)
+    assert lib.sgx_init_sg_StiffGas(1, arr, 3.4, 1.816e7, 6e9, 0.0, en, vals) == 0
+    assert lib.sgx_init_sg_NobleAbel(2, arr, 0.4, 0.718e7, 1e-3, 0.0, None, None) == 0
+    assert (arr[0].type, arr[0].mods) == (L.IDEAL_GAS, 0)
+    assert (arr[1].type, arr[1].mods, arr[1].scale, arr[1].shift) == (L.STIFF_GAS, 3, 2.0, 0.1)
+    assert arr[2].type == L.NOBLE_ABEL
+    assert lib.sgx_init_sg_IdealGas(-1, arr, 0.4, 1.0, None, None) == 1  # matindex < 0
+    assert lib.sgx_init_sg_SpinerDependsRhoT(0, arr, b"x.sp5", 1, 1, None, None) == 5
+    assert lib.sgx_finalize_sg_eos(3, C.byref(arr)) == 0
+    assert not arr

@@ -273,3 +273,45 @@ def test_entropy_with_reference_states(sgx):
                                        atol=1e-12 * np.abs(ref).max(),
                                        err_msg=f"ref case {j} fn {fn}")
     assert fx["r0_fn11"][0] == 0.0 and fx["r1_fn12"][0] == -2.0044437857420778e+08
+
+
+def test_init_sg_and_get_sg_interface(sgx, table):
+    # the reference's C interface: init_sg_<model> with the modifier step,
+    # get_sg_* with and without a lambda indexer, finalize_sg_eos
+    lib = sgx.load()
+    fx = golden("modifiers")
+    arr = C.POINTER(sgx.SgxEos)()
+    assert lib.sgx_init_sg_eos(2, C.byref(arr)) == 0
+    en = (C.c_int * 4)(*[int(v) for v in fx["init_enabled"][0]])
+    vals = (C.c_double * 6)(*fx["init_vals_in"][0])
+    assert lib.sgx_init_sg_IdealGas(0, arr, 0.5, 2.0, en, vals) == 0  # the p-alpha ramp
+    np.testing.assert_allclose(list(vals), fx["init_vals_out"][0], rtol=PALPHA_RTOL)
+    assert lib.sgx_init_sg_StiffGas(1, arr, 3.4, 1.816e7, 6e9, 0.0, None, None) == 0
+    vec = golden("eos_vector")
+    rho, sie = dev(vec["m1_rho"]), dev(vec["m1_sie"])
+    out = torch.empty_like(rho)
+    P = C.c_void_p
+    n = rho.numel()
+    for name, fn in (("Pressure", 3), ("BulkModulus", 7)):
+        f = getattr(lib, f"sgx_get_sg_{name}FromDensityInternalEnergy")
+        assert f(1, arr, P(rho.data_ptr()), P(sie.data_ptr()), P(out.data_ptr()), n, -1, None) == 0
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(out.cpu().numpy(), vec[f"m1_fn{fn}"])
+    assert lib.sgx_get_sg_MinInternalEnergyFromDensity(1, arr, P(rho.data_ptr()),
+                                                       P(out.data_ptr()), n) == 0
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy(), vec["m1_fn10"])
+    assert lib.sgx_get_sg_EntropyFromDensityInternalEnergy(
+        1, arr, P(rho.data_ptr()), P(sie.data_ptr()), P(out.data_ptr()), n, -1, None) == 0
+    # the tabulated model through a lambda indexer (stride 2)
+    assert lib.sgx_finalize_sg_eos(2, C.byref(arr)) == 0 and not arr
+    spl = golden("spiner_lookup")
+    arr2 = (sgx.SgxEos * 1)(table)
+    r, s = dev(spl["rho"]), dev(spl["sie"])
+    lam = dev(np.full(2 * r.numel(), np.nan))
+    out = torch.empty_like(r)
+    assert lib.sgx_get_sg_PressureFromDensityInternalEnergy(
+        0, arr2, P(r.data_ptr()), P(s.data_ptr()), P(out.data_ptr()), r.numel(), 2,
+        P(lam.data_ptr())) == 0
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy(), spl["fn3"])
