@@ -483,6 +483,25 @@ int sgx_get_sg_eos(int nmat, int ncell, int cell_dim, int input_int, const int *
                    double *frac_ie, double *frac_bmod, double *frac_dpde, double *frac_cv,
                    double mass_frac_cutoff, int precision, sgx_stream_t stream);
 
+/* ---- PTE plans: one solve bound to fixed arrays, replayed as a CUDA graph ----
+ * sgx_pte_plan_create checks its arguments as sgx_pte_solve does, allocates
+ * the solve's scratch and captures the whole launch sequence (binning, both
+ * passes, the side-stream fork and join) into a graph. Each
+ * sgx_pte_plan_run is one graph launch on `stream` and solves whatever the
+ * bound arrays hold at that time, with the result sgx_pte_solve would give.
+ * Iteration knobs (sgx_tune_set) are read at creation. A plan belongs to the
+ * device current at creation; runs of one plan must not overlap (they share
+ * its scratch). No reference counterpart: the reference's closure is a
+ * per-cell loop the caller runs each cycle. */
+typedef struct sgx_pte_plan sgx_pte_plan;
+int sgx_pte_plan_create(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list, int neos,
+                        const int32_t *eos_idx, const double *vfrac_tot, const double *sie_tot,
+                        double *rho, double *vfrac, double *sie, double *temp, double *press,
+                        double *lambda, const sgx_mix_params *params, sgx_pte_status *status,
+                        int precision, sgx_pte_plan **out);
+int sgx_pte_plan_run(sgx_pte_plan *plan, sgx_stream_t stream);
+int sgx_pte_plan_destroy(sgx_pte_plan *plan);
+
 /* ---- The reference's C interface (eos/singularity_eos.hpp:25-134) ----
  * Same argument lists with an sgx_ prefix, over sgx_eos values. enabled /
  * vals NULL take the reference's defaults (no modifiers); otherwise they

@@ -36,6 +36,7 @@ UNITS = [
     ("sgx_pool", "sgx_pool.cu", ["--fmad=false"]),
     ("sgx_modifiers", "sgx_modifiers.cu", ["--fmad=false"]),
     ("sgx_sgapi", "sgx_sgapi.cu", ["--fmad=false"]),
+    ("sgx_plan", "sgx_plan.cu", ["--fmad=false"]),
 ] + [(f"sgx_pte_fp64_n{n}", "sgx_pte_fp64_n.cu", ["--fmad=false", f"-DSGX_PTE_N={n}"])
      for n in range(1, 7)] + [
     (f"sgx_pte_fp64_bare_n{n}", "sgx_pte_fp64_n.cu",

@@ -513,11 +513,17 @@ int sgx_eos_fill(const sgx_eos *eos, int64_t n, double *rho, double *temp, doubl
                          lambda_stride, SGX_PREC_FP64, stream);
 }
 
-int sgx_pte_solve(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list, int neos,
-                  const int32_t *eos_idx, const double *vfrac_tot, const double *sie_tot,
-                  double *rho, double *vfrac, double *sie, double *temp, double *press,
-                  double *lambda, const sgx_mix_params *params, sgx_pte_status *status,
-                  int precision, sgx_stream_t stream) {
+} // extern "C"
+
+namespace sgx {
+// The argument checks of sgx_pte_solve and its PteArgs; empty is set when
+// ncell is 0 (nothing to launch).
+int pte_prepare(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list, int neos,
+                const int32_t *eos_idx, const double *vfrac_tot, const double *sie_tot,
+                double *rho, double *vfrac, double *sie, double *temp, double *press,
+                double *lambda, const sgx_mix_params *params, sgx_pte_status *status,
+                int precision, PteArgs &a, bool &empty) {
+  empty = false;
   if (solver < SGX_PTE_RHOT || solver > SGX_PTE_FIXED_P)
     return fail(SGX_ERR_INVALID, "sgx_pte_solve: bad solver");
   if (precision != SGX_PREC_FP64 && precision != SGX_PREC_MIXED)
@@ -531,7 +537,10 @@ int sgx_pte_solve(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list, 
   if (!eos_idx && neos < nmat)
     return fail(SGX_ERR_INVALID, "sgx_pte_solve: eos_idx NULL needs neos >= nmat");
   if (ncell < 0) return fail(SGX_ERR_INVALID, "sgx_pte_solve: ncell < 0");
-  if (ncell == 0) return SGX_OK;
+  if (ncell == 0) {
+    empty = true;
+    return SGX_OK;
+  }
   if (!vfrac_tot || !sie_tot || !rho || !vfrac || !sie || !temp || !press)
     return fail(SGX_ERR_INVALID, "sgx_pte_solve: null array");
   for (int k = 0; k < neos; ++k)
@@ -540,7 +549,6 @@ int sgx_pte_solve(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list, 
       return fail(SGX_ERR_UNSUPPORTED, "sgx_pte_solve: Helmholtz is not available in PTE");
     else if (const int rc = check_mods(eos_list[k], precision == SGX_PREC_MIXED, "sgx_pte_solve"))
       return rc;
-  sgx::PteArgs a;
   std::memset(&a, 0, sizeof(a));
   a.solver = solver;
   a.nmat = nmat;
@@ -562,6 +570,24 @@ int sgx_pte_solve(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list, 
     a.params = *params;
   else
     sgx_mix_params_default(&a.params);
+  return SGX_OK;
+}
+} // namespace sgx
+
+extern "C" {
+
+int sgx_pte_solve(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list, int neos,
+                  const int32_t *eos_idx, const double *vfrac_tot, const double *sie_tot,
+                  double *rho, double *vfrac, double *sie, double *temp, double *press,
+                  double *lambda, const sgx_mix_params *params, sgx_pte_status *status,
+                  int precision, sgx_stream_t stream) {
+  sgx::PteArgs a;
+  bool empty = false;
+  if (const int rc = sgx::pte_prepare(solver, nmat, ncell, eos_list, neos, eos_idx, vfrac_tot,
+                                      sie_tot, rho, vfrac, sie, temp, press, lambda, params,
+                                      status, precision, a, empty))
+    return rc;
+  if (empty) return SGX_OK;
   cudaError_t e;
   if (precision == SGX_PREC_MIXED)
     e = sgx::launch_pte_mixed(a, reinterpret_cast<cudaStream_t>(stream));

@@ -53,6 +53,13 @@ constexpr int PTE_SIG_KEYS = 5 + 25 + 125 + 625 + 3125 + 15625;
 // then the signature histogram and its scatter cursors.
 constexpr size_t PTE_BINS_BYTES = 256 + 2 * PTE_SIG_KEYS * sizeof(unsigned);
 
+// The argument checks of sgx_pte_solve and the PteArgs they describe;
+// empty is set when there is nothing to launch (ncell 0).
+int pte_prepare(int solver, int nmat, int64_t ncell, const sgx_eos *eos_list, int neos,
+                const int32_t *eos_idx, const double *vfrac_tot, const double *sie_tot,
+                double *rho, double *vfrac, double *sie, double *temp, double *press,
+                double *lambda, const sgx_mix_params *params, sgx_pte_status *status,
+                int precision, PteArgs &a, bool &empty);
 // Sets the calling thread's sgx_last_error() message; returns code.
 int set_error(int code, const std::string &msg);
 // SGX_OK, or the error (with its message set) for an EOS whose modifier bits
@@ -80,8 +87,10 @@ cudaError_t launch_pte_binning(const PteArgs &a, int *perm, cudaStream_t stream)
 // Per-cell PTE, FP32 iterations then FP64 refinement.
 cudaError_t launch_pte_mixed(const PteArgs &a, cudaStream_t stream);
 // The same with caller-provided scratch: a.bins (PTE_BINS_BYTES), a.retry_idx
-// and, when a.eos_idx is set, perm (ncell ints each).
-cudaError_t launch_pte_mixed_with(const PteArgs &a, int *perm, cudaStream_t stream);
+// and, when a.eos_idx is set, perm (ncell ints each). Pass 2 runs on `side`
+// when given, else on a stream of the library's per-device pool.
+cudaError_t launch_pte_mixed_with(const PteArgs &a, int *perm, cudaStream_t stream,
+                                  cudaStream_t side = nullptr);
 // The same with the scratch in a static device array (sgx_noalloc.cu).
 cudaError_t launch_pte_mixed_noalloc(const PteArgs &a, cudaStream_t stream);
 

@@ -187,7 +187,8 @@ cudaError_t launch_pte_binning(const PteArgs &a, int *perm, cudaStream_t stream)
 // Runs the binning and both passes with caller-provided scratch: bins (the
 // 3 * PTE_BINS counters), and perm (when eos_idx is set) and retry_idx of
 // ncell ints each.
-cudaError_t launch_pte_mixed_with(const PteArgs &args, int *perm, cudaStream_t stream) {
+cudaError_t launch_pte_mixed_with(const PteArgs &args, int *perm, cudaStream_t stream,
+                                  cudaStream_t side_given) {
   PteArgs a = args;
   a.perm = nullptr;
   a.fp32_iters = tune_get(SGX_TUNE_PTE_FP32_ITERS);
@@ -205,7 +206,7 @@ cudaError_t launch_pte_mixed_with(const PteArgs &args, int *perm, cudaStream_t s
   // runs long (FP64 at the reference's iteration counts, up to the cap for
   // cells that do not converge), so it overlaps pass 1 of the next counts
   // instead of idling the GPU after each.
-  cudaStream_t side = side_stream();
+  cudaStream_t side = side_given ? side_given : side_stream();
   if (!side) {
     for (int n = lo; n <= hi && e == cudaSuccess; ++n) {
       e = launch_n<false>(n, a, stream);

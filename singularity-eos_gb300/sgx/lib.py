@@ -41,6 +41,7 @@ EXPORTED = [
     "sgx_init_sg_Helmholtz", "sgx_get_sg_EntropyFromDensityInternalEnergy",
     "sgx_get_sg_PressureFromDensityInternalEnergy", "sgx_get_sg_MinInternalEnergyFromDensity",
     "sgx_get_sg_BulkModulusFromDensityInternalEnergy", "sgx_finalize_sg_eos",
+    "sgx_pte_plan_create", "sgx_pte_plan_run", "sgx_pte_plan_destroy",
 ]
 MOD_SHIFTED, MOD_SCALED, MOD_RAMP = 1, 2, 4
 HELM_DEFAULT, HELM_REGULA_FALSI, HELM_CACHE_READBACK = 31, 32, 64
@@ -182,6 +183,10 @@ def load():
             I, PE, P, P, P, I, I, P]
     lib.sgx_get_sg_MinInternalEnergyFromDensity.argtypes = [I, PE, P, P, I]
     lib.sgx_finalize_sg_eos.argtypes = [I, C.POINTER(PE)]
+    lib.sgx_pte_plan_create.argtypes = [I, I, C.c_int64, P, I, P, P, P, P, P, P, P, P, P,
+                                        C.POINTER(MixParams), P, I, C.POINTER(C.c_void_p)]
+    lib.sgx_pte_plan_run.argtypes = [C.c_void_p, P]
+    lib.sgx_pte_plan_destroy.argtypes = [C.c_void_p]
     _lib = lib
     return lib
 
@@ -334,6 +339,38 @@ def pte_solve(solver, eos_list, eos_idx, vfrac_tot, sie_tot, rho, vfrac, sie, te
         ptr(vfrac_tot), ptr(sie_tot), ptr(rho), ptr(vfrac), ptr(sie), ptr(temp), ptr(press),
         ptr(lam), C.byref(params) if params is not None else None, ptr(status), precision,
         stream_ptr(stream)))
+
+
+class PtePlan:
+    """sgx_pte_plan over device tensors (kept alive with the plan): one
+    solve captured as a CUDA graph; run() replays it on the tensors'
+    current contents."""
+
+    def __init__(self, solver, eos_list, eos_idx, vfrac_tot, sie_tot, rho, vfrac, sie, temp,
+                 press, lam=None, params=None, status=None, precision=PREC_FP64):
+        nmat, ncell = rho.shape
+        self._keep = (eos_idx, vfrac_tot, sie_tot, rho, vfrac, sie, temp, press, lam, status)
+        arr = (SgxEos * len(eos_list))(*eos_list)
+        self._h = C.c_void_p()
+        check(load().sgx_pte_plan_create(
+            solver, nmat, ncell, C.cast(arr, C.c_void_p), len(eos_list), ptr(eos_idx),
+            ptr(vfrac_tot), ptr(sie_tot), ptr(rho), ptr(vfrac), ptr(sie), ptr(temp), ptr(press),
+            ptr(lam), C.byref(params) if params is not None else None, ptr(status), precision,
+            C.byref(self._h)))
+
+    def run(self, stream=None):
+        check(load().sgx_pte_plan_run(self._h, stream_ptr(stream)))
+
+    def close(self):
+        if self._h:
+            load().sgx_pte_plan_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def approx_temperature(eos_list, eos_idx, u_tot, rho, vfrac, temp_out, Tguess=None, lam=None,

@@ -130,3 +130,34 @@ def test_tabulated_lookups(sgx):
             assert rel_err(got, fx[f"fn{fn}"]).max() <= PARITY_RTOL, f"fn {fn}"
     finally:
         sgx.load().sgx_eos_finalize(C.byref(tab))
+
+
+@pytest.mark.parametrize("name", ["pte_rhot_2mat", "pte_rhot_batched"])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_pte_plan_replays_the_solve(sgx, name, precision):
+    # a plan (the solve captured as a CUDA graph) gives what sgx_pte_solve
+    # gives, run after run, on whatever the bound arrays hold
+    fx = golden(name)
+    eos_list = [sgx.make_eos(k, p) for k, p in materials_from_rows(fx["materials"])]
+    ref, st_ref = run_pte(sgx, fx, eos_list, precision=precision)
+    t = {k: dev(fx["in_" + k]) for k in ("rho", "vfrac", "sie", "temp", "press")}
+    idx = dev(fx["eos_idx"], torch.int32) if "eos_idx" in fx else None
+    ncell = fx["sie_tot"].shape[0]
+    status = torch.zeros(ncell * 16, dtype=torch.uint8, device="cuda")
+    plan = sgx.PtePlan(0, eos_list, idx, dev(fx["vfrac_tot"]), dev(fx["sie_tot"]), t["rho"],
+                       t["vfrac"], t["sie"], t["temp"], t["press"], status=status,
+                       precision=precision)
+    for _ in range(2):
+        for k in t:
+            t[k].copy_(dev(fx["in_" + k]))
+        status.zero_()
+        plan.run()
+        torch.cuda.synchronize()
+        for k in t:
+            np.testing.assert_array_equal(t[k].cpu().numpy(), ref[k], err_msg=k)
+        st = sgx.status_view(status)
+        np.testing.assert_array_equal(st["converged"], st_ref["converged"])
+        np.testing.assert_array_equal(st["niter"], st_ref["niter"])
+    plan.close()
+    if precision == 0:
+        check_pte(fx, ref, st_ref, name + " (plan)")
