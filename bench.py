@@ -178,6 +178,11 @@ def bench_lookup(args, world, local, stream, out):
                              stream=stream)
             return step
 
+        # the library's autotuner picks the launch shape on this batch (the
+        # knobs it sets never change a result); the timed steps run with it
+        shape = lib.autotune_fill(tab, rho, T, sie, P, None, B, Q_OUT, cs=CS, reps=2,
+                                  stream=stream)
+        out["autotuned"] = {"lookup_blocks_per_sm": shape[0], "lookup_stage": shape[1]}
         results = {}
         for prec, name in ((lib.PREC_FP64, "fp64"), (lib.PREC_MIXED, "mixed")):
             steps = args.steps if prec == lib.PREC_MIXED else max(1, min(args.steps, 5))

@@ -434,6 +434,17 @@ enum {
 };
 int sgx_tune_set(int knob, int value);
 int sgx_tune_get(int knob, int *value);
+/* The autotuner of the lookup's launch shape: times every
+ * (SGX_TUNE_LOOKUP_BLOCKS_PER_SM, SGX_TUNE_LOOKUP_STAGE) pair on the
+ * caller's own mixed-precision FillEos batch (the arguments of
+ * sgx_eos_fill_ex), 1 + reps calls per pair with CUDA events on `stream`,
+ * and keeps the fastest pair set; blocks_per_sm / stage (nullable) receive
+ * it. These knobs never change a lookup's result. Each trial is an ordinary
+ * call, so outputs (and a lambda cache) are written. */
+int sgx_tune_autotune_fill(const sgx_eos *eos, int64_t n, double *rho, double *temp,
+                           double *sie, double *press, double *cv, double *bmod, double *cs,
+                           uint32_t output, double *lambda, int lambda_stride, int reps,
+                           int *blocks_per_sm, int *stage, sgx_stream_t stream);
 
 /* Largest ncell sgx_pte_solve_noalloc accepts. */
 #define SGX_PTE_NOALLOC_MAX_CELLS 1048576

@@ -98,3 +98,63 @@ extern "C" int sgx_tune_get(int knob, int *value) {
   *value = g_knobs[knob].value.load();
   return SGX_OK;
 }
+
+// The autotuner of the lookup's launch shape: every (blocks per SM, staging)
+// pair on the caller's own batch, through the public call, timed with events
+// on the caller's stream; the fastest pair stays set. These two knobs change
+// how the work is spread and staged, never what a lookup returns, so the
+// choice is free to follow the hardware and the batch. Each trial is an
+// ordinary call: its outputs, and a lambda cache if given, are written.
+extern "C" int sgx_tune_autotune_fill(const sgx_eos *eos, int64_t n, double *rho, double *temp,
+                                      double *sie, double *press, double *cv, double *bmod,
+                                      double *cs, uint32_t output, double *lambda,
+                                      int lambda_stride, int reps, int *blocks_per_sm,
+                                      int *stage, sgx_stream_t stream) {
+  using namespace sgx;
+  static const char *who = "sgx_tune_autotune_fill";
+  if (!eos || n <= 0 || reps < 1 || reps > 1000)
+    return set_error(SGX_ERR_INVALID, std::string(who) + ": bad arguments");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const int keep_b = g_knobs[SGX_TUNE_LOOKUP_BLOCKS_PER_SM].value.load();
+  const int keep_s = g_knobs[SGX_TUNE_LOOKUP_STAGE].value.load();
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t ce = cudaEventCreate(&e0);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+  float best = 0.0f;
+  int best_b = keep_b, best_s = keep_s, rc = SGX_OK;
+  for (int b = g_knobs[SGX_TUNE_LOOKUP_BLOCKS_PER_SM].lo;
+       ce == cudaSuccess && rc == SGX_OK && b <= g_knobs[SGX_TUNE_LOOKUP_BLOCKS_PER_SM].hi; ++b)
+    for (int st = g_knobs[SGX_TUNE_LOOKUP_STAGE].lo;
+         ce == cudaSuccess && rc == SGX_OK && st <= g_knobs[SGX_TUNE_LOOKUP_STAGE].hi; ++st) {
+      g_knobs[SGX_TUNE_LOOKUP_BLOCKS_PER_SM].value.store(b);
+      g_knobs[SGX_TUNE_LOOKUP_STAGE].value.store(st);
+      // one untimed call (first use of this shape), then reps timed
+      rc = sgx_eos_fill_ex(eos, n, rho, temp, sie, press, cv, bmod, cs, output, lambda,
+                           lambda_stride, SGX_PREC_MIXED, stream);
+      if (rc == SGX_OK) ce = cudaEventRecord(e0, s);
+      for (int r = 0; r < reps && rc == SGX_OK && ce == cudaSuccess; ++r)
+        rc = sgx_eos_fill_ex(eos, n, rho, temp, sie, press, cv, bmod, cs, output, lambda,
+                             lambda_stride, SGX_PREC_MIXED, stream);
+      if (rc == SGX_OK && ce == cudaSuccess) ce = cudaEventRecord(e1, s);
+      if (rc == SGX_OK && ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+      float ms = 0.0f;
+      if (rc == SGX_OK && ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
+      if (rc == SGX_OK && ce == cudaSuccess && (best == 0.0f || ms < best)) {
+        best = ms;
+        best_b = b;
+        best_s = st;
+      }
+    }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  // keep the winner, or the previous setting if a trial failed
+  const bool ok = rc == SGX_OK && ce == cudaSuccess;
+  g_knobs[SGX_TUNE_LOOKUP_BLOCKS_PER_SM].value.store(ok ? best_b : keep_b);
+  g_knobs[SGX_TUNE_LOOKUP_STAGE].value.store(ok ? best_s : keep_s);
+  if (rc != SGX_OK) return rc;
+  if (ce != cudaSuccess)
+    return set_error(SGX_ERR_CUDA, std::string(who) + ": " + cudaGetErrorString(ce));
+  if (blocks_per_sm) *blocks_per_sm = best_b;
+  if (stage) *stage = best_s;
+  return SGX_OK;
+}

@@ -41,7 +41,7 @@ EXPORTED = [
     "sgx_init_sg_Helmholtz", "sgx_get_sg_EntropyFromDensityInternalEnergy",
     "sgx_get_sg_PressureFromDensityInternalEnergy", "sgx_get_sg_MinInternalEnergyFromDensity",
     "sgx_get_sg_BulkModulusFromDensityInternalEnergy", "sgx_finalize_sg_eos",
-    "sgx_pte_plan_create", "sgx_pte_plan_run", "sgx_pte_plan_destroy",
+    "sgx_pte_plan_create", "sgx_pte_plan_run", "sgx_pte_plan_destroy", "sgx_tune_autotune_fill",
 ]
 MOD_SHIFTED, MOD_SCALED, MOD_RAMP = 1, 2, 4
 HELM_DEFAULT, HELM_REGULA_FALSI, HELM_CACHE_READBACK = 31, 32, 64
@@ -187,6 +187,8 @@ def load():
                                         C.POINTER(MixParams), P, I, C.POINTER(C.c_void_p)]
     lib.sgx_pte_plan_run.argtypes = [C.c_void_p, P]
     lib.sgx_pte_plan_destroy.argtypes = [C.c_void_p]
+    lib.sgx_tune_autotune_fill.argtypes = [C.POINTER(SgxEos), C.c_int64] + [P] * 7 + [
+        C.c_uint32, P, I, I, C.POINTER(C.c_int), C.POINTER(C.c_int), P]
     _lib = lib
     return lib
 
@@ -339,6 +341,18 @@ def pte_solve(solver, eos_list, eos_idx, vfrac_tot, sie_tot, rho, vfrac, sie, te
         ptr(vfrac_tot), ptr(sie_tot), ptr(rho), ptr(vfrac), ptr(sie), ptr(temp), ptr(press),
         ptr(lam), C.byref(params) if params is not None else None, ptr(status), precision,
         stream_ptr(stream)))
+
+
+def autotune_fill(eos, rho, temp, sie, press, cv, bmod, output, cs=None, lam=None,
+                  lam_stride=0, reps=3, stream=None):
+    """sgx_tune_autotune_fill on device tensors: returns the (blocks per SM,
+    staging) pair it kept."""
+    b, st = C.c_int(), C.c_int()
+    check(load().sgx_tune_autotune_fill(
+        C.byref(eos), rho.numel(), ptr(rho), ptr(temp), ptr(sie), ptr(press), ptr(cv), ptr(bmod),
+        ptr(cs), output, ptr(lam), lam_stride, reps, C.byref(b), C.byref(st),
+        stream_ptr(stream)))
+    return b.value, st.value
 
 
 class PtePlan:

@@ -279,3 +279,45 @@ def test_host_array_fill_matches_device_fill(sgx, precision):
             assert np.array_equal(h.view(np.uint64), d.cpu().numpy().view(np.uint64))
     finally:
         sgx.load().sgx_eos_finalize(C.byref(tab))
+
+
+def test_autotune_fill_keeps_a_valid_shape_and_the_results(sgx):
+    # the autotuner tries every (blocks per SM, staging) pair on the batch,
+    # keeps the fastest, and the results stay the default's bits
+    import ctypes as C
+    from sgx import sp5lite
+    L = sgx.load()
+    path, _ = stiffgas_table_path()
+    tab = sgx.spiner_eos(path, 1)
+    saved = []
+    for k in (sgx.TUNE_LOOKUP_BLOCKS_PER_SM, sgx.TUNE_LOOKUP_STAGE):
+        v = C.c_int()
+        assert L.sgx_tune_get(k, C.byref(v)) == 0
+        saved.append(v.value)
+    try:
+        rho_h, sie_h = sp5lite.stiffgas_queries(1 << 20, seed=19)
+        rho = torch.as_tensor(rho_h, device="cuda")
+        sie = torch.as_tensor(sie_h, device="cuda")
+        q = sgx.Q_TEMPERATURE | sgx.Q_PRESSURE | sgx.Q_BULK_MODULUS
+
+        def run():
+            T, P, bm = (torch.zeros_like(rho) for _ in range(3))
+            sgx.fill_eos(tab, rho, T, sie, P, None, bm, q, precision=sgx.PREC_MIXED)
+            torch.cuda.synchronize()
+            return np.stack([x.cpu().numpy() for x in (T, P, bm)])
+
+        base = run()
+        T, P, bm = (torch.zeros_like(rho) for _ in range(3))
+        b, st = sgx.autotune_fill(tab, rho, T, sie, P, None, bm, q, reps=2)
+        assert 4 <= b <= 6 and 0 <= st <= 2
+        got = []
+        for k in (sgx.TUNE_LOOKUP_BLOCKS_PER_SM, sgx.TUNE_LOOKUP_STAGE):
+            v = C.c_int()
+            L.sgx_tune_get(k, C.byref(v))
+            got.append(v.value)
+        assert got == [b, st]
+        np.testing.assert_array_equal(run(), base)
+    finally:
+        for k, v in zip((sgx.TUNE_LOOKUP_BLOCKS_PER_SM, sgx.TUNE_LOOKUP_STAGE), saved):
+            L.sgx_tune_set(k, v)
+        L.sgx_eos_finalize(C.byref(tab))
