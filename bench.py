@@ -582,7 +582,8 @@ def main():
             "e2e": out.get("e2e"), "roofline": out["roofline"], "clocks": out["clocks"],
             "gpu_launches": out["gpu_launches"], "plain_fp64": out["plain_fp64"],
             "pte": out.get("pte"), "helmholtz": out.get("helmholtz"),
-            "serve": out.get("serve"), "fp_peaks": out.get("fp_peaks")}
+            "serve": out.get("serve"), "fp_peaks": out.get("fp_peaks"),
+            "autotuned": out.get("autotuned")}
     if "e2e" not in out:
         line["e2e"] = None
     if not args.no_cpu_baseline and world == 1:
