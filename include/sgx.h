@@ -423,14 +423,24 @@ int sgx_mix_enforce_energies_sum(int nmat, int64_t ncell, const int32_t *eos_idx
  *      the FP64 re-solve (pass 2) of the mixed PTE path; a cell that has not
  *      converged by then is reported unconverged. These two change which
  *      cells converge (never their converged values beyond the stated
- *      tolerance); the others change nothing but speed. */
+ *      tolerance); the others change nothing but speed.
+ *  SGX_TUNE_PTE_COUNT_ORDER  0/1 (default 0): the mixed path takes the
+ *      material counts from the smallest (0) or from the largest (1); pass 2
+ *      of one count overlaps pass 1 of the next, so the order decides
+ *      which pass 2 is left without overlap. Results do not change.
+ *  SGX_TUNE_PTE_MIXED_BLOCK  32..128 (default 128): threads per block of
+ *      the mixed path's pass 1 (rounded down to 32, 64 or 128). Results do
+ *      not change.
+ */
 enum {
   SGX_TUNE_LOOKUP_BLOCKS_PER_SM = 1,
   SGX_TUNE_LOOKUP_STAGE = 2,
   SGX_TUNE_L2_PERSIST = 3,
   SGX_TUNE_HOST_FILL_STAGED = 4,
   SGX_TUNE_PTE_FP32_ITERS = 5,
-  SGX_TUNE_PTE_RETRY_ITERS = 6
+  SGX_TUNE_PTE_RETRY_ITERS = 6,
+  SGX_TUNE_PTE_COUNT_ORDER = 7,
+  SGX_TUNE_PTE_MIXED_BLOCK = 8
 };
 int sgx_tune_set(int knob, int value);
 int sgx_tune_get(int knob, int *value);

@@ -214,7 +214,9 @@ cudaError_t launch_pte_mixed_with(const PteArgs &args, int *perm, cudaStream_t s
     }
     return e;
   }
-  for (int n = lo; n <= hi && e == cudaSuccess; ++n) {
+  const bool down = tune_get(SGX_TUNE_PTE_COUNT_ORDER) != 0;
+  for (int i = 0; i <= hi - lo && e == cudaSuccess; ++i) {
+    const int n = down ? hi - i : lo + i;
     e = launch_n<false>(n, a, stream);
     cudaEvent_t ev = nullptr;
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);

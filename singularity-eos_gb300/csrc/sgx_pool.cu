@@ -74,6 +74,8 @@ Knob g_knobs[] = {
     {{0}, 0, 1}, // SGX_TUNE_HOST_FILL_STAGED
     {{8}, 2, 64},  // SGX_TUNE_PTE_FP32_ITERS
     {{8}, 4, 128},  // SGX_TUNE_PTE_RETRY_ITERS
+    {{0}, 0, 1},    // SGX_TUNE_PTE_COUNT_ORDER
+    {{128}, 32, 128}, // SGX_TUNE_PTE_MIXED_BLOCK
 };
 constexpr int NKNOBS = sizeof(g_knobs) / sizeof(g_knobs[0]);
 } // namespace

@@ -73,8 +73,15 @@ template <int N> __device__ __forceinline__ bool pte_bin_cell(const PteArgs &a, 
   return true;
 }
 
+// True for a whole block past the end of the N-bin: it leaves before
+// staging the EOS list (launches are sized for every cell, the bin is not).
+template <int N> __device__ __forceinline__ bool pte_block_idle(const PteArgs &a) {
+  return a.perm && static_cast<long long>(blockIdx.x) * blockDim.x >= a.bins[N];
+}
+
 template <template <typename, int> class Solver, int N>
 __global__ void __launch_bounds__(PTE_BLOCK) pte_cell_kernel(const PteArgs a) {
+  if (pte_block_idle<N>(a)) return;
   __shared__ sgx_eos s_eos[MAX_EOS];
   for (int k = threadIdx.x; k < a.neos; k += blockDim.x)
     s_eos[k] = a.eos[k];

@@ -187,6 +187,7 @@ __device__ __forceinline__ void pte_store(const PteArgs &a, const long long i,
 // Pass 1: every cell with N materials, FP32 solve + FP64 refinement.
 template <int N>
 __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_kernel(const PteArgs a) {
+  if (pte_block_idle<N>(a)) return;
   __shared__ sgx_eos s_eos[MAX_EOS];
   for (int k = threadIdx.x; k < a.neos; k += blockDim.x)
     s_eos[k] = a.eos[k];
@@ -363,8 +364,12 @@ __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_retry_kernel(const PteArg
 }
 
 template <int N> cudaError_t launch_pte_mixed_n(const PteArgs &a, cudaStream_t stream) {
-  const long long blocks = (a.ncell + PTE_MIXED_BLOCK - 1) / PTE_MIXED_BLOCK;
-  pte_mixed_kernel<N><<<static_cast<unsigned>(blocks), PTE_MIXED_BLOCK, 0, stream>>>(a);
+  // smaller blocks free their SM slot sooner when their lanes' iteration
+  // counts differ (SGX_TUNE_PTE_MIXED_BLOCK: 32, 64 or 128 threads)
+  const int k = tune_get(SGX_TUNE_PTE_MIXED_BLOCK);
+  const int bs = k >= 128 ? 128 : (k >= 64 ? 64 : 32);
+  const long long blocks = (a.ncell + bs - 1) / bs;
+  pte_mixed_kernel<N><<<static_cast<unsigned>(blocks), bs, 0, stream>>>(a);
   return cudaGetLastError();
 }
 template <int N> cudaError_t launch_pte_retry_n(const PteArgs &a, cudaStream_t stream) {
