@@ -180,7 +180,7 @@ SGEOS_CELLS = ("press", "pmax", "vol", "spvol", "sie", "temp", "bmod", "dpde", "
 SGEOS_FRACS = ("frac_mass", "frac_vol", "frac_ie", "frac_bmod", "frac_dpde", "frac_cv")
 
 
-def sgeos_fixture(ref, cell_dim=700, ncell=512, seed=41, cutoff=1e-8, mode=1):
+def sgeos_fixture(ref, cell_dim=700, ncell=512, seed=41, cutoff=1e-8, mode=1, rows=None):
     """get_sg_eos on four materials (IdealGas, StiffGas, NobleAbel, copper
     Gruneisen) in input mode `mode` (1 rho-sie, -1 P-T, -2 rho-P, -3 rho-T):
     mass fractions with some materials absent or below the cutoff, pure
@@ -214,9 +214,12 @@ def sgeos_fixture(ref, cell_dim=700, ncell=512, seed=41, cutoff=1e-8, mode=1):
     offsets = (rng.permutation(cell_dim)[:ncell] + 1).astype(np.int32)
     eos_offsets = np.array([1, 2, 3, 4], np.int32)
     out = {"in_" + k: v.copy() for k, v in {**cells, **fracs}.items()}
-    conv = ref.get_sg_eos(mode, [desc(m) for m in mats], eos_offsets, offsets, cells, fracs,
-                          cutoff)
+    descs = [desc(m) for m in mats] if rows is None else \
+        [mdesc(m, r) for m, r in zip(mats, rows)]
+    conv = ref.get_sg_eos(mode, descs, eos_offsets, offsets, cells, fracs, cutoff)
     out.update({"out_" + k: v for k, v in {**cells, **fracs}.items()})
+    if rows is not None:  # modifiers per material (mods_row layout)
+        out["mods"] = np.array(rows)
     out.update(materials=mats_array(mats), offsets=offsets, eos_offsets=eos_offsets,
                cutoff=np.float64(cutoff), converged=conv, mode=np.int32(mode))
     return out
@@ -527,6 +530,11 @@ def main():
         fx["pt_derivs"]["table_sha256"] = np.array(sha)
         fx["eos_vector_ext"] = vector_ext_fixture(ref, path)
         fx["eos_vector_ext"]["table_sha256"] = np.array(sha)
+    air_ramp = ref.p_alpha(desc(W.IDEAL_AIR), 1.5, 5e6, 1e7)
+    sg_rows = [mods_row(ramp=air_ramp), mods_row(1e8, 1.02), mods_row(1e7, None),
+               mods_row(None, 1.01)]
+    fx["get_sg_eos_modified"] = sgeos_fixture(ref, seed=47, rows=sg_rows)
+    fx["get_sg_eos_p_t_modified"] = sgeos_fixture(ref, seed=48, mode=-1, rows=sg_rows)
     fx["pte_rhot_modified"] = modified_pte_fixture(ref, 0, 131)
     fx["pte_pt_modified"] = modified_pte_fixture(ref, 1, 133)
     fx["get_sg_eos"] = sgeos_fixture(ref)

@@ -27,6 +27,10 @@ def sgx():
 
 def run(sgx, fx, precision):
     eos = [sgx.make_eos(k, p) for k, p in materials_from_rows(fx["materials"])]
+    if "mods" in fx:  # ShiftedEOS / ScaledEOS / BilinearRampEOS per material
+        eos = [sgx.modify(e, shift=r[1] if int(r[0]) & 1 else None,
+                          scale=r[2] if int(r[0]) & 2 else None,
+                          ramp=r[3:7] if int(r[0]) & 4 else None) for e, r in zip(eos, fx["mods"])]
     dev = {k: torch.as_tensor(fx["in_" + k], device="cuda").clone() for k in CELLS + FRACS}
     offsets = torch.as_tensor(fx["offsets"], device="cuda")
     mode = int(fx["mode"]) if "mode" in fx else 1
@@ -47,7 +51,8 @@ def close(got, want, rtol, label):
 
 
 @pytest.mark.parametrize("name", ["get_sg_eos", "get_sg_eos_rho_t", "get_sg_eos_rho_p",
-                                  "get_sg_eos_p_t"])
+                                  "get_sg_eos_p_t", "get_sg_eos_modified",
+                                  "get_sg_eos_p_t_modified"])
 def test_get_sg_eos_matches_reference(sgx, name):
     fx = golden(name)
     got = run(sgx, fx, 0)
