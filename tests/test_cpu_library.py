@@ -188,3 +188,35 @@ def test_init_sg_interface_without_gpu():
     assert lib.sgx_init_sg_SpinerDependsRhoT(0, arr, b"x.sp5", 1, 1, None, None) == 5
     assert lib.sgx_finalize_sg_eos(3, C.byref(arr)) == 0
     assert not arr
+
+
+def test_plan_and_derivative_argument_checks_without_gpu():
+    # argument errors come back before any CUDA call
+    from sgx import lib as L
+    lib = L.load()
+    e = L.make_eos(L.IDEAL_GAS, (0.4, 0.718e7))
+    arr = (L.SgxEos * 1)(e)
+    out = C.c_void_p()
+    # bad solver, bad precision, null arrays
+    assert lib.sgx_pte_plan_create(9, 1, 8, C.cast(arr, C.c_void_p), 1, None, None, None, None,
+                                   None, None, None, None, None, None, None, 0,
+                                   C.byref(out)) == 1
+    assert lib.sgx_pte_plan_create(0, 1, 8, C.cast(arr, C.c_void_p), 1, None, None, None, None,
+                                   None, None, None, None, None, None, None, 7,
+                                   C.byref(out)) == 1
+    assert lib.sgx_pte_plan_create(0, 1, 8, C.cast(arr, C.c_void_p), 1, None, None, None, None,
+                                   None, None, None, None, None, None, None, 0,
+                                   C.byref(out)) == 1
+    assert not out.value
+    assert lib.sgx_pte_plan_run(None, None) == 1
+    assert lib.sgx_pte_plan_destroy(None) == 0
+    # PT derivatives: Helmholtz unsupported, null arrays invalid, n = 0 a no-op
+    h = L.SgxEos()
+    h.type = L.HELMHOLTZ if hasattr(L, "HELMHOLTZ") else 6
+    assert lib.sgx_eos_pt_derivatives(C.byref(h), 4, *([None] * 9), 0, None) == 5
+    assert lib.sgx_eos_pt_derivatives(C.byref(e), 4, *([None] * 9), 0, None) == 1
+    assert lib.sgx_eos_pt_derivatives(C.byref(e), 0, *([None] * 9), 0, None) == 0
+    # entropy of a model without one
+    g = L.make_eos(L.GRUNEISEN, (3.94e5, 1.489, 0.0, 0.0, 2.02, 0.47, 8.93, 298.0, 0.0, 3.9e6))
+    assert lib.sgx_eos_eval(C.byref(g), 11, 4, C.c_void_p(16), C.c_void_p(16), C.c_void_p(16),
+                            None, 0, None) == 5
