@@ -315,3 +315,40 @@ def test_init_sg_and_get_sg_interface(sgx, table):
         P(lam.data_ptr())) == 0
     torch.cuda.synchronize()
     np.testing.assert_array_equal(out.cpu().numpy(), spl["fn3"])
+
+
+def test_modified_fill_from_host_arrays(sgx, table):
+    # the host-array FillEos with a modified EOS moves every array both ways
+    # (a modifier may write a quantity that is not an output) and matches
+    # the reference like the device-array call
+    fx = golden("modifiers")
+    mats = materials_from_rows(fx["materials"])
+    for k in (5, 6):  # shifted+scaled+ramped stiff gas; shifted+scaled table
+        e = case_eos(sgx, table, mats[k], fx["mods"][k])
+        n = fx[f"c{k}_rho"].size
+        a = dict(rho=fx[f"c{k}_rho"].copy(), temp=np.zeros(n), sie=fx[f"c{k}_sie"].copy(),
+                 press=np.zeros(n), cv=np.zeros(n), bmod=np.zeros(n))
+        sgx.fill_eos_host(e, a["rho"], a["temp"], a["sie"], a["press"], a["cv"], a["bmod"], Q_TPB)
+        for q in a:
+            close(a[q], fx[f"c{k}_fill_{q}"], f"case {k} host fill {q}")
+
+
+def test_plan_with_modified_materials(sgx):
+    # a plan over a list with modified EOS runs the build with modifier code
+    fx = golden("pte_rhot_modified")
+    mats = materials_from_rows(fx["batched_materials"])
+    eos_list = [wrap(sgx, sgx.make_eos(*m), r) for m, r in zip(mats, fx["batched_mods"])]
+    t = {k: dev(fx["batched_in_" + k]) for k in ("rho", "vfrac", "sie", "temp", "press")}
+    idx = dev(fx["batched_eos_idx"], torch.int32)
+    ncell = fx["batched_sie_tot"].shape[0]
+    status = torch.zeros(ncell * 16, dtype=torch.uint8, device="cuda")
+    plan = sgx.PtePlan(0, eos_list, idx, dev(fx["batched_vfrac_tot"]), dev(fx["batched_sie_tot"]),
+                       t["rho"], t["vfrac"], t["sie"], t["temp"], t["press"], status=status)
+    plan.run()
+    torch.cuda.synchronize()
+    plan.close()
+    present = fx["batched_in_rho"] > 0
+    for k in ("press", "temp", "sie", "vfrac", "rho"):
+        close(t[k].cpu().numpy()[present], fx["batched_out_" + k][present], f"plan {k}")
+    st = sgx.status_view(status)
+    np.testing.assert_array_equal(st["converged"], fx["batched_converged"].astype(bool))
