@@ -347,6 +347,10 @@ int sgx_pte_pt_required_scratch(int nmat);
 int sgx_pte_fixed_t_required_scratch(int nmat);
 int sgx_pte_fixed_p_required_scratch(int nmat);
 int sgx_pte_rhou_required_scratch(int nmat);
+/* The ...RequiredScratchInBytes companions (mixed_cell_models.hpp:879-881,
+ * 1204-1206 and the other solvers'): the count above times sizeof(double)
+ * for solver SGX_PTE_*; 0 for a bad solver. */
+size_t sgx_pte_required_scratch_bytes(int solver, int nmat);
 
 /* Solves PTE in every cell.
  *  solver     SGX_PTE_RHOT, SGX_PTE_PT, SGX_PTE_RHOU, SGX_PTE_FIXED_T or

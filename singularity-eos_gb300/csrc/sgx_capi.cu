@@ -108,6 +108,19 @@ int sgx_pte_rhou_required_scratch(int nmat) {
   return 4 * nmat * nmat + 4 * 2 * nmat + 8 * nmat;
 }
 
+size_t sgx_pte_required_scratch_bytes(int solver, int nmat) {
+  int n = 0;
+  switch (solver) {
+  case SGX_PTE_RHOT: n = sgx_pte_rhot_required_scratch(nmat); break;
+  case SGX_PTE_PT: n = sgx_pte_pt_required_scratch(nmat); break;
+  case SGX_PTE_RHOU: n = sgx_pte_rhou_required_scratch(nmat); break;
+  case SGX_PTE_FIXED_T: n = sgx_pte_fixed_t_required_scratch(nmat); break;
+  case SGX_PTE_FIXED_P: n = sgx_pte_fixed_p_required_scratch(nmat); break;
+  default: return 0;
+  }
+  return static_cast<size_t>(n) * sizeof(double);
+}
+
 int sgx_eos_ideal_gas_entropy(sgx_eos *out, double gm1, double Cv, double EntropyT0,
                               double EntropyRho0) {
   if (!out) return fail(SGX_ERR_INVALID, "sgx_eos_ideal_gas: null");

@@ -43,6 +43,7 @@ EXPORTED = [
     "sgx_get_sg_PressureFromDensityInternalEnergy", "sgx_get_sg_MinInternalEnergyFromDensity",
     "sgx_get_sg_BulkModulusFromDensityInternalEnergy", "sgx_finalize_sg_eos",
     "sgx_pte_plan_create", "sgx_pte_plan_run", "sgx_pte_plan_destroy", "sgx_tune_autotune_fill",
+    "sgx_pte_required_scratch_bytes",
 ]
 MOD_SHIFTED, MOD_SCALED, MOD_RAMP = 1, 2, 4
 HELM_DEFAULT, HELM_REGULA_FALSI, HELM_CACHE_READBACK = 31, 32, 64
@@ -188,6 +189,8 @@ def load():
                                         C.POINTER(MixParams), P, I, C.POINTER(C.c_void_p)]
     lib.sgx_pte_plan_run.argtypes = [C.c_void_p, P]
     lib.sgx_pte_plan_destroy.argtypes = [C.c_void_p]
+    lib.sgx_pte_required_scratch_bytes.argtypes = [I, I]
+    lib.sgx_pte_required_scratch_bytes.restype = C.c_size_t
     lib.sgx_tune_autotune_fill.argtypes = [C.POINTER(SgxEos), C.c_int64] + [P] * 7 + [
         C.c_uint32, P, I, I, C.POINTER(C.c_int), C.POINTER(C.c_int), P]
     _lib = lib

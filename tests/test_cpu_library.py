@@ -68,6 +68,10 @@ def test_constructors_and_validation_need_no_gpu(lib):
     assert lib.sgx_pte_fixed_t_required_scratch(3) == 9 + 12 + 6 + 6
     assert lib.sgx_pte_fixed_p_required_scratch(3) == 16 + 16 + 6 + 9
     assert lib.sgx_pte_rhou_required_scratch(3) == 36 + 24 + 24
+    # the ...InBytes companions
+    assert lib.sgx_pte_required_scratch_bytes(0, 5) == 8 * (25 + 20 + 30)
+    assert lib.sgx_pte_required_scratch_bytes(2, 3) == 8 * (36 + 24 + 24)
+    assert lib.sgx_pte_required_scratch_bytes(9, 3) == 0
     # mixed precision is for PTESolverRhoT only
     rc = lib.sgx_pte_solve(3, 1, 10, C.cast(arr, C.c_void_p), 1, *([None] * 10), None, 1, None)
     assert rc == 5
