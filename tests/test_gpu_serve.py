@@ -125,3 +125,25 @@ def test_oversized_request_is_refused(sgx, eos_list):
     finally:
         srv.close()
     same(r, solve_alone(sgx, eos_list, r, 1))
+
+
+def test_modified_eos_serve_in_fp64_and_are_refused_in_mixed(sgx, eos_list):
+    # a list with ShiftedEOS / ScaledEOS / BilinearRampEOS members serves on
+    # the FP64 path with the results of sgx_pte_solve alone; the
+    # mixed-precision server takes bare models only
+    mod = list(eos_list)
+    mod[1] = sgx.modify(mod[1], scale=1.02)
+    mod[5] = sgx.modify(mod[5], shift=1e8, scale=1.02)
+    mod[8] = sgx.modify(mod[8], shift=1e8)  # the table
+    reqs = [make_request(n, seed=300 + i) for i, n in enumerate((3000, 20000, 700))]
+    srv = sgx.Server(mod, hbm_budget_bytes=256 << 20, max_inflight=3, precision=0)
+    try:
+        tickets = [srv.submit(r) for r in reqs]
+        for t in tickets:
+            srv.wait(t)
+    finally:
+        srv.close()
+    for r in reqs:
+        same(r, solve_alone(sgx, mod, r, 0))
+    with pytest.raises(RuntimeError, match="unmodified EOS only"):
+        sgx.Server(mod, hbm_budget_bytes=256 << 20, max_inflight=3, precision=1)
