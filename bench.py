@@ -57,9 +57,9 @@ def peaks():
 
 
 def fp_peaks():
-    """FP64 / FP32 FMA throughput of this device, from the probe that
-    singularity-eos_gb300/build.py builds (None when it is missing)."""
-    exe = os.path.join(ROOT, "singularity-eos_gb300", "lib", "sgx_fma_peak")
+    """FP64 / FP32 FMA throughput of this device, from the probe
+    fma_peak.cu that __graft_entry__.build() builds (None when missing)."""
+    exe = os.path.join(ROOT, "_build", "fma_peak")
     if not os.path.exists(exe):
         return None
     try:

@@ -1,5 +1,6 @@
-// sgx_fma_peak: measures the FP64 and FP32 FMA throughput of the current
-// device, the denominators of the pipe fractions bench.py reports for the
+// fma_peak: measures the FP64 and FP32 FMA throughput of the current
+// device (a benchmark probe beside bench.py, not part of the library): the
+// denominators of the pipe fractions bench.py reports for the
 // FP64-bound closure kernels (HBM bandwidth comes from a copy measurement).
 //
 // Each thread runs 8 independent FMA chains for `iters` rounds; a grid of

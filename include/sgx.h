@@ -473,9 +473,11 @@ int sgx_tune_autotune_fill(const sgx_eos *eos, int64_t n, double *rho, double *t
  *  - ncell > SGX_PTE_NOALLOC_MAX_CELLS returns SGX_ERR_INVALID before any
  *    device work; split the batch or call sgx_pte_solve.
  *  - solver other than SGX_PTE_RHOT returns SGX_ERR_UNSUPPORTED.
- *  - The first call on a device looks up the array's device address (with
- *    that device current) and caches it; make that first call before any
- *    stream capture begins.
+ *  - The first call in a CUDA context looks up the array's device address
+ *    (with that device current) and caches it for that context; make that
+ *    first call before any stream capture begins. After cudaDeviceReset, or
+ *    with another driver context current, the next call is again a first
+ *    call (the cache is keyed on the context's id, not the device).
  *  - There is one array per device: calls that overlap in time on the same
  *    device (other streams, other host threads) race on it and give wrong
  *    results. Order them on one stream or serialise them. */

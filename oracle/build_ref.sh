@@ -1,11 +1,12 @@
 #!/usr/bin/env bash
 # Builds oracle/_ref/libsgref.so: the reference's own hot-path headers,
 # unmodified, compiled against this folder's shims. TEST INFRASTRUCTURE
-# ONLY. Needs the reference sources (default /root/reference, or $SG_REF);
-# without them it exits 0 and builds nothing (the GPU machine has no copy).
+# ONLY. Needs the reference sources: $SG_REF, by default a checkout named
+# `reference` beside this repository; without them it exits 0 and builds
+# nothing (the GPU machine has no copy).
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
-ref="${SG_REF:-/root/reference}"
+ref="${SG_REF:-$here/../../reference}"
 if [ ! -d "$ref/singularity-eos" ]; then
   echo "build_ref: reference sources not found at $ref; skipping" >&2
   exit 0

@@ -68,29 +68,16 @@ def _compile(name, src, extra, verbose):
     return obj, r.stderr
 
 
-def _build_probe():
-    """The FMA-throughput probe bench.py runs (a separate executable)."""
-    exe = os.path.join(LIBDIR, "sgx_fma_peak")
-    cmd = [nvcc(), os.path.join(CSRC, "sgx_fma_peak.cu"), "-o", exe + ".tmp"] + ARCH + \
-        ["-std=c++17", "-O3"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"nvcc failed on sgx_fma_peak.cu:\n{r.stdout}\n{r.stderr}")
-    os.replace(exe + ".tmp", exe)
-
-
 def build(verbose=False):
     os.makedirs(LIBDIR, exist_ok=True)
     os.makedirs(OBJDIR, exist_ok=True)
-    with cf.ThreadPoolExecutor(max_workers=min(len(UNITS) + 1, os.cpu_count() or 4)) as ex:
-        probe = ex.submit(_build_probe)
+    with cf.ThreadPoolExecutor(max_workers=min(len(UNITS), os.cpu_count() or 4)) as ex:
         futs = {ex.submit(_compile, n, s, e, verbose): n for n, s, e in UNITS}
         objs, logs = [], {}
         for f in cf.as_completed(futs):
             obj, log = f.result()
             objs.append(obj)
             logs[futs[f]] = log
-        probe.result()
     tmp = LIB + ".tmp"
     cmd = [nvcc(), "-shared", "-o", tmp] + sorted(objs) + ARCH + ["-cudart", "shared",
                                                                   "-lpthread"]

@@ -437,6 +437,7 @@ class Server:
 
     def __init__(self, eos_list, hbm_budget_bytes=1 << 30, max_inflight=8,
                  precision=PREC_MIXED, solver=PTE_RHOT, params=None):
+        self.h = None  # set once sgx_server_create succeeds; close() checks it
         lib = load()
         self._eos = (SgxEos * len(eos_list))(*eos_list)
         self._params = params
