@@ -435,6 +435,11 @@ int sgx_mix_enforce_energies_sum(int nmat, int64_t ncell, const int32_t *eos_idx
  *  SGX_TUNE_PTE_MIXED_BLOCK  32..128 (default 128): threads per block of
  *      the mixed path's pass 1 (rounded down to 32, 64 or 128). Results do
  *      not change.
+ *  SGX_TUNE_PTE_GROUP_MIN_N  2..7 (default 3): pass 1 of the mixed path
+ *      solves cells with at least this many materials with a group of 2, 4
+ *      or 8 lanes per cell (one material per lane), and smaller cells with
+ *      one thread each; 7 keeps one thread per cell everywhere. Both forms
+ *      meet the same tolerance; their results differ in rounding.
  */
 enum {
   SGX_TUNE_LOOKUP_BLOCKS_PER_SM = 1,
@@ -444,7 +449,8 @@ enum {
   SGX_TUNE_PTE_FP32_ITERS = 5,
   SGX_TUNE_PTE_RETRY_ITERS = 6,
   SGX_TUNE_PTE_COUNT_ORDER = 7,
-  SGX_TUNE_PTE_MIXED_BLOCK = 8
+  SGX_TUNE_PTE_MIXED_BLOCK = 8,
+  SGX_TUNE_PTE_GROUP_MIN_N = 9
 };
 int sgx_tune_set(int knob, int value);
 int sgx_tune_get(int knob, int *value);
@@ -488,27 +494,43 @@ int sgx_pte_solve_noalloc(int solver, int nmat, int64_t ncell, const sgx_eos *eo
                           const sgx_mix_params *params, sgx_pte_status *status,
                           sgx_stream_t stream);
 
-/* get_sg_eos (singularity_eos.hpp:114-132; eos/get_sg_eos.cpp:35-280) in its
- * (rho, sie) input modes, input_int 0 and 1 (the (rho, T), (rho, P) and
- * (P, T) modes, -3..-1, return SGX_ERR_UNSUPPORTED). Per cell offsets[k]-1
- * (1-based, as the Fortran interface passes them), k < ncell: the mass
- * fractions are normalised, materials above mass_frac_cutoff take part in a
- * PTESolverRhoT solve (a single one in a T(rho, sie), P(rho, T) lookup), and
- * press, temp (eV), bmod, cv (per eV), dpde, frac_vol, frac_ie and the
- * optional frac_bmod / frac_dpde / frac_cv (NULL to skip) are written; pmax
- * becomes max(pmax, press); sie and spvol are inputs. Unlike the reference
- * (host arrays, copied to and from the device per call) every array here is a
- * device array: per-cell [cell_dim], per-material LayoutLeft
- * [nmat][cell_dim]. eos_offsets (host, [nmat], 1-based) picks each material's
- * entry of the host list eos. Cells with no material above the cutoff get
- * zero pressure and temperature. precision: SGX_PREC_FP64 (the reference
- * iteration) or SGX_PREC_MIXED. */
+/* get_sg_eos (singularity_eos.hpp:114-132; eos/get_sg_eos.cpp:35-280) over
+ * HOST arrays, as the reference takes them: every array is copied to the
+ * device, solved there, and copied back before the call returns (the
+ * reference deep-copies its host arrays to and from Kokkos views the same
+ * way, get_sg_eos.cpp:99-120). Per cell offsets[k]-1 (1-based, as the
+ * Fortran interface passes them), k < ncell: the mass fractions are
+ * normalised, materials above mass_frac_cutoff take part in the closure
+ * solve of the input mode, and press, temp, bmod, cv, dpde, frac_vol,
+ * frac_ie and the optional frac_bmod / frac_dpde / frac_cv (NULL to skip)
+ * are written; pmax becomes max(pmax, press). input_int as the reference's
+ * input_condition (get_sg_eos.cpp:65-71): 1 (rho, sie), 0 (rho, sie) with
+ * normalised mass fractions, -1 (P, T), -2 (rho, P), -3 (rho, T)
+ * (get_sg_eos_p_t.cpp, _rho_p.cpp, _rho_t.cpp). Per-cell arrays
+ * [cell_dim], per-material LayoutLeft [nmat][cell_dim]. eos_offsets (host,
+ * [nmat], 1-based) picks each material's entry of the host list eos (neos
+ * entries). Cells with no material above the cutoff get zero pressure and
+ * temperature. precision: SGX_PREC_FP64 (the reference iteration) or
+ * SGX_PREC_MIXED ((rho, sie) and (P, T) modes). The copies and the solve
+ * run on `stream`, which is synchronised before the return. */
 int sgx_get_sg_eos(int nmat, int ncell, int cell_dim, int input_int, const int *eos_offsets,
                    const sgx_eos *eos, int neos, const int *offsets, double *press,
                    double *pmax, double *vol, double *spvol, double *sie, double *temp,
                    double *bmod, double *dpde, double *cv, double *frac_mass, double *frac_vol,
                    double *frac_ie, double *frac_bmod, double *frac_dpde, double *frac_cv,
                    double mass_frac_cutoff, int precision, sgx_stream_t stream);
+/* The same over DEVICE arrays (offsets and every per-cell and per-material
+ * array in device memory; eos_offsets and eos stay host arrays), stream-
+ * ordered and without copies or synchronisation. No reference counterpart:
+ * it is get_sg_eos without its host copies, for callers whose fields already
+ * live on the device. */
+int sgx_get_sg_eos_device(int nmat, int ncell, int cell_dim, int input_int,
+                          const int *eos_offsets, const sgx_eos *eos, int neos,
+                          const int *offsets, double *press, double *pmax, double *vol,
+                          double *spvol, double *sie, double *temp, double *bmod, double *dpde,
+                          double *cv, double *frac_mass, double *frac_vol, double *frac_ie,
+                          double *frac_bmod, double *frac_dpde, double *frac_cv,
+                          double mass_frac_cutoff, int precision, sgx_stream_t stream);
 
 /* ---- PTE plans: one solve bound to fixed arrays, replayed as a CUDA graph ----
  * sgx_pte_plan_create checks its arguments as sgx_pte_solve does, allocates

@@ -67,6 +67,13 @@ __device__ __forceinline__ ff ff_mul(const ff x, const ff y) {
   p.lo = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, p.lo));
   return quick_two_sum(p.hi, p.lo);
 }
+// x y without the final renormalisation (for sums that accept an
+// unnormalised low part, such as ff_sum4).
+__device__ __forceinline__ ff ff_mul_nn(const ff x, const ff y) {
+  ff p = two_prod(x.hi, y.hi);
+  p.lo = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, p.lo));
+  return p;
+}
 __device__ __forceinline__ ff ff_mul_f(const ff x, const float y) {
   ff p = two_prod(x.hi, y);
   p.lo = fmaf(x.lo, y, p.lo);
@@ -91,6 +98,74 @@ __device__ __forceinline__ ff ff_sqrt(const ff x) {
   const ff s2 = two_prod(s, s);
   const ff d = ff_sub(x, s2);
   return ff_add(ff_make(s), ff_make(FMUL(d.hi, 0.5f / s)));
+}
+
+// ---- cheaper forms for the ~1e-14 a lookup needs (ff carries ~1e-14.5) ----
+
+// 1/x and 1/sqrt(x) to about one float ulp: the MUFU approximations, whose
+// error the one correction step of each caller below squares away.
+__device__ __forceinline__ float rcp_approx(const float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float rsqrt_approx(const float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// x / y (y.hi normal, non-zero): q1 = x.hi / y.hi from the approximate
+// reciprocal, then one correction q2 = (x - q1 y) / y with the residual
+// formed exactly in its leading part (x.hi - q1 y.hi cancels by Sterbenz).
+// Relative error about 2^-45.
+__device__ __forceinline__ ff ff_div_fast(const ff x, const ff y) {
+  const float r = rcp_approx(y.hi);
+  const float q1 = FMUL(x.hi, r);
+  const float ph = FMUL(y.hi, q1);
+  float pl = fmaf(y.hi, q1, -ph); // y.hi q1 = ph + pl exactly
+  pl = fmaf(y.lo, q1, pl);
+  const float rem = FADD(FSUB(x.hi, ph), FSUB(x.lo, pl));
+  return quick_two_sum(q1, FMUL(rem, r));
+}
+
+// sqrt(x), x.hi > 0 normal: s = sqrtf(x.hi) (correctly rounded) and one
+// Newton correction with the residual x - s^2 exact in its leading part.
+// Relative error about 2^-47.
+__device__ __forceinline__ ff ff_sqrt_fast(const ff x) {
+  const float s = sqrtf(x.hi);
+  const float sq = FMUL(s, s);
+  const float sqe = fmaf(s, s, -sq); // s^2 = sq + sqe exactly
+  const float d = FADD(FSUB(x.hi, sq), FSUB(x.lo, sqe));
+  return quick_two_sum(s, FMUL(d, FMUL(0.5f, rcp_approx(s))));
+}
+
+// sqrt(b / r) for b, r > 0 normal, as b (b r)^(-1/2): y0 = rsqrt(p.hi) for
+// p = b r, one Newton step y1 = y0 (1 + h / 2) with h = 1 - p y0^2 formed
+// exactly in its leading part, then b y1. Relative error about 2^-44.
+__device__ __forceinline__ ff ff_sqrt_ratio(const ff b, const ff r) {
+  const ff p = ff_mul(b, r);
+  const float y0 = rsqrt_approx(p.hi);
+  const float s = FMUL(y0, y0);
+  const float se = fmaf(y0, y0, -s); // y0^2 = s + se exactly
+  const float th = FMUL(p.hi, s);
+  float tl = fmaf(p.hi, s, -th); // p.hi s = th + tl exactly
+  tl = fmaf(p.hi, se, fmaf(p.lo, s, tl));
+  const float h = FSUB(FSUB(1.0f, th), tl);
+  const ff y1 = quick_two_sum(y0, FMUL(FMUL(0.5f, y0), h));
+  return ff_mul(b, y1);
+}
+
+// x + y0 + y1 + y2 for the lookup's bilinear forms: the four leading parts
+// summed by exact two-sums, every low part and rounding error added once in
+// float. The result's low part is not renormalised (ff2d accepts that).
+__device__ __forceinline__ ff ff_sum4(const ff x, const ff y0, const ff y1, const ff y2) {
+  const ff s0 = two_sum(x.hi, y0.hi);
+  const ff s1 = two_sum(s0.hi, y1.hi);
+  const ff s2 = two_sum(s1.hi, y2.hi);
+  const float lo = FADD(FADD(FADD(x.lo, y0.lo), FADD(y1.lo, y2.lo)),
+                        FADD(FADD(s0.lo, s1.lo), s2.lo));
+  return {s2.hi, lo};
 }
 
 __device__ __forceinline__ bool ff_gt(const ff a, const ff b) {

@@ -63,21 +63,23 @@ constexpr int LOOKUP_BLOCK = 256;
 // Constants of one table, in float-float, shared by a block.
 struct FfConsts {
   float rho_min_f, rho_inv_f; // density grid in FP32, for the cell estimate
-  ff t_min, t_dx;      // temperature grid: lT min and dlT
-  ff p2_scale;         // log10(2)^-1 * 2^52: lT -> NQT pow integer
-  ff lt_lo, lt_hi;     // on-table lT bounds (getLocDependsRhoT_)
+  ff t_min, t_dx;      // temperature grid: lT min and dlT (lambda cache)
+  ff p_min, p_dx;      // the same scaled by log10(2)^-1 * 2^52 (NQT pow integer)
+  ff p_lo, p_hi;       // on-table lT bounds (getLocDependsRhoT_), scaled alike
   ff eps;
 };
 
 __device__ __forceinline__ ff ff_of_int(const int i) { return ff_make(static_cast<float>(i)); }
 
 // The record's field f = x + a dT + b dR + a b dRT at (a, b); AB = a b.
+// The three products and the four-term sum leave their low parts
+// unnormalised; ff2d takes the sum as it is.
 __device__ __forceinline__ ff ff_cell(const FfRec &r, const ff A, const ff B, const ff AB) {
   const ff x = ff_make(r.x[0], r.x[1]);
-  const ff t = ff_mul(A, ff_make(r.dT[0], r.dT[1]));
-  const ff d = ff_mul(B, ff_make(r.dR[0], r.dR[1]));
-  const ff c = ff_mul(AB, ff_make(r.dRT[0], r.dRT[1]));
-  return ff_add(x, ff_add(t, ff_add(d, c)));
+  const ff t = ff_mul_nn(A, ff_make(r.dT[0], r.dT[1]));
+  const ff d = ff_mul_nn(B, ff_make(r.dR[0], r.dR[1]));
+  const ff c = ff_mul_nn(AB, ff_make(r.dRT[0], r.dRT[1]));
+  return ff_sum4(x, t, d, c);
 }
 
 // One 32-byte record per lane in one 256-bit load (records are 32-byte
@@ -101,6 +103,10 @@ __device__ __forceinline__ SieRec load_sie(const SieRec *p) {
 // Integer tests of a double's bit pattern (no FP64 pipe).
 __device__ __forceinline__ bool d_is_zero(const double x) {
   return (__double_as_longlong(x) & 0x7fffffffffffffffLL) == 0;
+}
+// The unbiased binary exponent of x (normal x).
+__device__ __forceinline__ int d_exp(const double x) {
+  return static_cast<int>((__double_as_longlong(x) >> 52) & 0x7ff) - 1023;
 }
 // x > 0 and not NaN (for the callers' range checks that follow)
 __device__ __forceinline__ bool d_positive(const double x) { return __double_as_longlong(x) > 0; }
@@ -238,9 +244,11 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
     sc.rho_inv_f = d2ff(st.gRho.inv_dx).hi;
     sc.t_min = d2ff(st.gT.min);
     sc.t_dx = d2ff(st.gT.dx);
-    sc.p2_scale = d2ff(nqt::log10_over_log2 * nqt::scale_up);
-    sc.lt_lo = d2ff((1 + SP_SOFT_THRESH) * st.lTMin);
-    sc.lt_hi = d2ff((1 - SP_SOFT_THRESH) * st.lTMax);
+    const ff p2 = d2ff(nqt::log10_over_log2 * nqt::scale_up);
+    sc.p_min = ff_mul(sc.t_min, p2);
+    sc.p_dx = ff_mul(sc.t_dx, p2);
+    sc.p_lo = ff_mul(d2ff((1 + SP_SOFT_THRESH) * st.lTMin), p2);
+    sc.p_hi = ff_mul(d2ff((1 - SP_SOFT_THRESH) * st.lTMax), p2);
     sc.eps = d2ff(lim<double>::eps);
   }
   __syncthreads();
@@ -388,8 +396,9 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
           // sie = x + a (dT + b dRT) + b dR: numerator and denominator in FP64
           const double num = fma(-b1, r.dR, sie - r.x);
           const double den = fma(b1, r.dRT, r.dT);
-          if (!ff_ok_bits(num) || !ff_ok_bits(den) || d_is_zero(den)) break;
-          A = ff_div(d2ff(num), d2ff(den));
+          // (ff_div_fast's reciprocal needs |den| < 2^126)
+          if (!ff_ok_bits(num) || !ff_ok_bits(den) || d_is_zero(den) || d_exp(den) > 120) break;
+          A = ff_div_fast(d2ff(num), d2ff(den));
           if (A.hi < 0.0f && i > 0) {
             --i;
             continue;
@@ -415,19 +424,22 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
     if (fast) {
       // 5. lT, then T = 10^lT by the NQT pow in integers
       using namespace nqt;
-      const ff LT = d_is_zero(lt_guess) ? ff_add(ff_mul(ff_add(ff_of_int(i), A), sc.t_dx), sc.t_min)
-                                        : d2ff(lt_guess);
-      const ff P52 = ff_mul(LT, sc.p2_scale);
+      // the NQT pow's integer argument lT log10(2)^-1 2^52, from the cell
+      // position i + a on the scaled grid
+      const bool rooted = d_is_zero(lt_guess);
+      const ff IA = rooted ? ff_add(ff_of_int(i), A) : ff_make(0.0f);
+      const ff P52 = rooted ? ff_add(ff_mul(IA, sc.p_dx), sc.p_min)
+                            : ff_mul(d2ff(lt_guess), d2ff(nqt::log10_over_log2 * nqt::scale_up));
       // on the table in T too (getLocDependsRhoT_); a root within 1e-8 of
       // either end takes the FP64 pass, whose off-table forms then apply
-      if (fabsf(P52.hi) >= 1.1e12f && ff_gt(LT, sc.lt_lo) && ff_lt(LT, sc.lt_hi)) {
+      if (fabsf(P52.hi) >= 1.1e12f && ff_gt(P52, sc.p_lo) && ff_lt(P52, sc.p_hi)) {
         constexpr long long ca = 9007199254740992LL, cc = 18014398509481984LL;
         const long long x_as_int = f2ll_bits(P52.hi) + f2ll_bits(P52.lo);
         const long long frac = x_as_int & mantissa_mask;
         const long long N = cc - 3 * frac; // in [2^52, 2^54]
         const ff NF = quick_two_sum(static_cast<float>(static_cast<int>(N >> 30)) * 1073741824.0f,
                                     static_cast<float>(static_cast<int>(N & ((1LL << 30) - 1))));
-        const ff SQ = ff_sqrt(NF);
+        const ff SQ = ff_sqrt_fast(NF);
         const long long fsqrt = f2ll_bits(SQ.hi * 67108864.0f) + f2ll_bits(SQ.lo * 67108864.0f);
         double temp = __longlong_as_double(x_as_int + ca - fsqrt - frac + one_as_int);
         if (t_offset) temp -= t.lTOffset;
@@ -436,10 +448,18 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
         if ((out & Q_TEMPERATURE) && a.temp) a.temp[e] = temp;
         if ((out & Q_PRESSURE) && a.press) a.press[e] = ff2d(ff_cell(load_rec(t.PR + ci), A, B, AB));
         if ((out & Q_BMOD) || a.cs) {
-          ff BM = ff_cell(load_rec(t.bmodR + ci), A, B, AB);
+          const ff bm = ff_cell(load_rec(t.bmodR + ci), A, B, AB);
+          ff BM = quick_two_sum(bm.hi, bm.lo);
           if (ff_lt(BM, sc.eps)) BM = sc.eps;
           if ((out & Q_BMOD) && a.bmod) a.bmod[e] = ff2d(BM);
-          if (a.cs) a.cs[e] = ff2d(ff_sqrt(ff_div(BM, d2ff(rho))));
+          if (a.cs) {
+            // sqrt(bmod / rho) by one rsqrt correction while b rho stays well
+            // inside the float range, by the exact ff quotient otherwise
+            const ff R = d2ff(rho);
+            const float pr = BM.hi * R.hi;
+            a.cs[e] = ff2d((pr > 1e-30f && pr < 1e30f) ? ff_sqrt_ratio(BM, R)
+                                                        : ff_sqrt(ff_div(BM, R)));
+          }
         }
         if ((out & Q_CV) && a.cv) {
           const double a1 = ff2d(A);
@@ -451,7 +471,7 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
         if (a.lambda) {
           double *lam = a.lambda + e * a.lambda_stride;
           lam[0] = lRho;
-          lam[1] = d_is_zero(lt_guess) ? ff2d(LT) : lt_guess;
+          lam[1] = rooted ? ff2d(ff_add(ff_mul(IA, sc.t_dx), sc.t_min)) : lt_guess;
         }
         done = true;
       }

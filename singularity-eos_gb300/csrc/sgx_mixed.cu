@@ -27,6 +27,7 @@ namespace sgx {
 
 template <int N> cudaError_t launch_pte_mixed_n(const PteArgs &a, cudaStream_t stream);
 template <int N> cudaError_t launch_pte_retry_n(const PteArgs &a, cudaStream_t stream);
+template <int N> cudaError_t launch_pte_group_n(const PteArgs &a, cudaStream_t stream);
 
 namespace {
 
@@ -157,6 +158,16 @@ cudaStream_t side_stream() {
 }
 
 template <bool RETRY> cudaError_t launch_n(const int n, const PteArgs &a, cudaStream_t s) {
+  // pass 1 of counts from SGX_TUNE_PTE_GROUP_MIN_N up: a lane group per cell
+  if (!RETRY && n >= 2 && n >= tune_get(SGX_TUNE_PTE_GROUP_MIN_N)) {
+    switch (n) {
+    case 2: return launch_pte_group_n<2>(a, s);
+    case 3: return launch_pte_group_n<3>(a, s);
+    case 4: return launch_pte_group_n<4>(a, s);
+    case 5: return launch_pte_group_n<5>(a, s);
+    case 6: return launch_pte_group_n<6>(a, s);
+    }
+  }
   switch (n) {
   case 1: return RETRY ? launch_pte_retry_n<1>(a, s) : launch_pte_mixed_n<1>(a, s);
   case 2: return RETRY ? launch_pte_retry_n<2>(a, s) : launch_pte_mixed_n<2>(a, s);

@@ -357,6 +357,31 @@ __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_retry_kernel(const PteArg
           out_T[q] = R.T * R.Tnorm;
           out_P[q] = R.press[q] * R.uscale;
         }
+      } else {
+        // The refinement's plain Newton steps can fail from a state the
+        // reference accepts far from equilibrium: its default tolerances
+        // are 1e-6, and a cell of pressure-preferring gases with zero
+        // pressure guesses passes its check at iteration 0 with P = 0. The
+        // FP64 damped Newton continues from there under tight controls; if
+        // it does not converge either, the reference's answer stands.
+        MixP<double> tight = mp;
+        tight.tol_p = tight.tol_e = 1e-13;
+        tight.abs_p = 0.0;
+        tight.tol_p_suff = tight.tol_e_suff = 1e-12;
+        tight.abs_p_suff = 0.0;
+        int taken = 0;
+        if (pte_polish<N>(s, tight, taken)) {
+          s.finalize();
+          st.niter += taken;
+#pragma unroll
+          for (int q = 0; q < N; ++q) {
+            out_rho[q] = s.rho[q];
+            out_vf[q] = s.vfrac[q];
+            out_sie[q] = s.sie[q];
+            out_T[q] = s.temp[q];
+            out_P[q] = s.press[q];
+          }
+        }
       }
     }
     pte_store<N>(a, i, slot, out_rho, out_vf, out_sie, out_T, out_P, cache, st, 0x40);

@@ -259,36 +259,46 @@ __global__ void __launch_bounds__(SG_BLOCK) sgeos_final(const SgArgs a) {
   a.pmax[i] = press > a.pmax[i] ? press : a.pmax[i];
 }
 
+// The argument checks shared by the host-array and device-array calls,
+// before any array is touched.
+int sgeos_check(const char *who, int nmat, int ncell, int cell_dim, int input_int,
+                const int *eos_offsets, const sgx_eos *eos, int neos, int precision) {
+  const std::string w(who);
+  if (input_int < -3 || input_int > 1) return set_error(SGX_ERR_INVALID, w + ": bad input_int");
+  if (nmat < 1 || nmat > PTE_MAX_N)
+    return set_error(SGX_ERR_UNSUPPORTED, w + ": nmat must be in 1..6");
+  if (ncell < 0 || cell_dim < ncell)
+    return set_error(SGX_ERR_INVALID, w + ": need 0 <= ncell <= cell_dim");
+  if (ncell == 0) return SGX_OK;
+  if (!eos || neos < 1 || neos > MAX_EOS || !eos_offsets)
+    return set_error(SGX_ERR_INVALID, w + ": eos list / offsets");
+  if (precision != SGX_PREC_FP64 && precision != SGX_PREC_MIXED)
+    return set_error(SGX_ERR_INVALID, w + ": bad precision");
+  if (precision == SGX_PREC_MIXED && (input_int == -3 || input_int == -2))
+    return set_error(SGX_ERR_UNSUPPORTED,
+                     w + ": SGX_PREC_MIXED is for the (rho, sie) and (P, T) modes");
+  return SGX_OK;
+}
+
 } // namespace
 
 } // namespace sgx
 
-extern "C" int sgx_get_sg_eos(int nmat, int ncell, int cell_dim, int input_int,
-                              const int *eos_offsets, const sgx_eos *eos, int neos,
-                              const int *offsets, double *press, double *pmax, double *vol,
-                              double *spvol, double *sie, double *temp, double *bmod,
-                              double *dpde, double *cv, double *frac_mass, double *frac_vol,
-                              double *frac_ie, double *frac_bmod, double *frac_dpde,
-                              double *frac_cv, double mass_frac_cutoff, int precision,
-                              sgx_stream_t stream) {
+extern "C" int sgx_get_sg_eos_device(int nmat, int ncell, int cell_dim, int input_int,
+                                     const int *eos_offsets, const sgx_eos *eos, int neos,
+                                     const int *offsets, double *press, double *pmax,
+                                     double *vol, double *spvol, double *sie, double *temp,
+                                     double *bmod, double *dpde, double *cv, double *frac_mass,
+                                     double *frac_vol, double *frac_ie, double *frac_bmod,
+                                     double *frac_dpde, double *frac_cv, double mass_frac_cutoff,
+                                     int precision, sgx_stream_t stream) {
   using namespace sgx;
-  if (input_int < -3 || input_int > 1)
-    return set_error(SGX_ERR_INVALID, "sgx_get_sg_eos: bad input_int");
-  if (nmat < 1 || nmat > PTE_MAX_N)
-    return set_error(SGX_ERR_UNSUPPORTED, "sgx_get_sg_eos: nmat must be in 1..6");
-  if (ncell < 0 || cell_dim < ncell)
-    return set_error(SGX_ERR_INVALID, "sgx_get_sg_eos: need 0 <= ncell <= cell_dim");
-  if (ncell == 0) return SGX_OK;
-  if (!eos || neos < 1 || neos > MAX_EOS || !eos_offsets)
-    return set_error(SGX_ERR_INVALID, "sgx_get_sg_eos: eos list / offsets");
-  if (precision != SGX_PREC_FP64 && precision != SGX_PREC_MIXED)
-    return set_error(SGX_ERR_INVALID, "sgx_get_sg_eos: bad precision");
-  if (precision == SGX_PREC_MIXED && (input_int == -3 || input_int == -2))
-    return set_error(SGX_ERR_UNSUPPORTED,
-                     "sgx_get_sg_eos: SGX_PREC_MIXED is for the (rho, sie) and (P, T) modes");
+  const int ck = sgeos_check("sgx_get_sg_eos_device", nmat, ncell, cell_dim, input_int,
+                             eos_offsets, eos, neos, precision);
+  if (ck != SGX_OK || ncell == 0) return ck;
   if (!offsets || !press || !pmax || !vol || !spvol || !sie || !temp || !bmod || !dpde || !cv ||
       !frac_mass || !frac_vol || !frac_ie)
-    return set_error(SGX_ERR_INVALID, "sgx_get_sg_eos: null array");
+    return set_error(SGX_ERR_INVALID, "sgx_get_sg_eos_device: null array");
   SgArgs a;
   std::memset(&a, 0, sizeof(a));
   a.nmat = nmat;
@@ -298,14 +308,14 @@ extern "C" int sgx_get_sg_eos(int nmat, int ncell, int cell_dim, int input_int,
   a.mode = input_int;
   for (int k = 0; k < neos; ++k) {
     if (eos[k].type < SGX_IDEAL_GAS || eos[k].type > SGX_SPINER_RHOT)
-      return set_error(SGX_ERR_UNSUPPORTED, "sgx_get_sg_eos: EOS not available in PTE");
-    if (const int rc = check_eos_mods(eos[k], precision == SGX_PREC_MIXED, "sgx_get_sg_eos"))
+      return set_error(SGX_ERR_UNSUPPORTED, "sgx_get_sg_eos_device: EOS not available in PTE");
+    if (const int rc = check_eos_mods(eos[k], precision == SGX_PREC_MIXED, "sgx_get_sg_eos_device"))
       return rc;
     a.eos[k] = eos[k];
   }
   for (int m = 0; m < nmat; ++m) {
     if (eos_offsets[m] < 1 || eos_offsets[m] > neos)
-      return set_error(SGX_ERR_INVALID, "sgx_get_sg_eos: eos_offsets out of range");
+      return set_error(SGX_ERR_INVALID, "sgx_get_sg_eos_device: eos_offsets out of range");
     a.eos_of[m] = eos_offsets[m] - 1;
   }
   a.offsets = offsets;
@@ -321,7 +331,7 @@ extern "C" int sgx_get_sg_eos(int nmat, int ncell, int cell_dim, int input_int,
   const size_t bytes = up(4 * nm) * 2 + up(8 * n) * 3 + up(8 * nm) * 5 + up(24 * nm) + up(4 * n);
   void *scratch = nullptr;
   cudaError_t e = scratch_alloc(&scratch, bytes, s);
-  if (e != cudaSuccess) return set_error(SGX_ERR_CUDA, "sgx_get_sg_eos: scratch allocation");
+  if (e != cudaSuccess) return set_error(SGX_ERR_CUDA, "sgx_get_sg_eos_device: scratch allocation");
   char *p = static_cast<char *>(scratch);
   auto take = [&](size_t b) {
     char *q = p;
@@ -370,6 +380,72 @@ extern "C" int sgx_get_sg_eos(int nmat, int ncell, int cell_dim, int input_int,
   const cudaError_t f = scratch_free(scratch, s);
   if (e == cudaSuccess) e = f;
   if (e != cudaSuccess)
-    return set_error(SGX_ERR_CUDA, std::string("sgx_get_sg_eos: ") + cudaGetErrorString(e));
+    return set_error(SGX_ERR_CUDA, std::string("sgx_get_sg_eos_device: ") + cudaGetErrorString(e));
+  return SGX_OK;
+}
+
+// get_sg_eos over host arrays, as the reference takes them: every array is
+// copied to device memory, the device call runs, and every array is copied
+// back before the call returns (get_sg_eos.cpp:99-120 and the deep copies at
+// its end do the same through Kokkos views). Arguments are checked by the
+// device call; the copies use the library's stream-ordered pool.
+extern "C" int sgx_get_sg_eos(int nmat, int ncell, int cell_dim, int input_int,
+                              const int *eos_offsets, const sgx_eos *eos, int neos,
+                              const int *offsets, double *press, double *pmax, double *vol,
+                              double *spvol, double *sie, double *temp, double *bmod,
+                              double *dpde, double *cv, double *frac_mass, double *frac_vol,
+                              double *frac_ie, double *frac_bmod, double *frac_dpde,
+                              double *frac_cv, double mass_frac_cutoff, int precision,
+                              sgx_stream_t stream) {
+  using namespace sgx;
+  static const char *who = "sgx_get_sg_eos";
+  const int ck = sgeos_check(who, nmat, ncell, cell_dim, input_int, eos_offsets, eos, neos,
+                             precision);
+  if (ck != SGX_OK || ncell == 0) return ck;
+  if (!offsets || !press || !pmax || !vol || !spvol || !sie || !temp || !bmod || !dpde || !cv ||
+      !frac_mass || !frac_vol || !frac_ie)
+    return set_error(SGX_ERR_INVALID, std::string(who) + ": null array");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  double *cells[9] = {press, pmax, vol, spvol, sie, temp, bmod, dpde, cv};
+  double *fracs[6] = {frac_mass, frac_vol, frac_ie, frac_bmod, frac_dpde, frac_cv};
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t cb = static_cast<size_t>(cell_dim) * sizeof(double);
+  const size_t fb = cb * static_cast<size_t>(nmat);
+  const size_t ob = static_cast<size_t>(ncell) * sizeof(int);
+  const size_t bytes = up(ob) + 9 * up(cb) + 6 * up(fb);
+  void *scratch = nullptr;
+  cudaError_t e = scratch_alloc(&scratch, bytes, s);
+  if (e != cudaSuccess) return set_error(SGX_ERR_CUDA, std::string(who) + ": device buffers");
+  char *p = static_cast<char *>(scratch);
+  int *d_off = reinterpret_cast<int *>(p);
+  p += up(ob);
+  double *d_cells[9], *d_fracs[6];
+  for (int k = 0; k < 9; ++k, p += up(cb))
+    d_cells[k] = reinterpret_cast<double *>(p);
+  for (int k = 0; k < 6; ++k, p += up(fb))
+    d_fracs[k] = fracs[k] ? reinterpret_cast<double *>(p) : nullptr;
+  e = cudaMemcpyAsync(d_off, offsets, ob, cudaMemcpyHostToDevice, s);
+  for (int k = 0; k < 9 && e == cudaSuccess; ++k)
+    e = cudaMemcpyAsync(d_cells[k], cells[k], cb, cudaMemcpyHostToDevice, s);
+  for (int k = 0; k < 6 && e == cudaSuccess; ++k)
+    if (fracs[k]) e = cudaMemcpyAsync(d_fracs[k], fracs[k], fb, cudaMemcpyHostToDevice, s);
+  int rc = SGX_OK;
+  if (e == cudaSuccess) {
+    rc = sgx_get_sg_eos_device(nmat, ncell, cell_dim, input_int, eos_offsets, eos, neos, d_off,
+                               d_cells[0], d_cells[1], d_cells[2], d_cells[3], d_cells[4],
+                               d_cells[5], d_cells[6], d_cells[7], d_cells[8], d_fracs[0],
+                               d_fracs[1], d_fracs[2], d_fracs[3], d_fracs[4], d_fracs[5],
+                               mass_frac_cutoff, precision, stream);
+    for (int k = 0; k < 9 && rc == SGX_OK && e == cudaSuccess; ++k)
+      e = cudaMemcpyAsync(cells[k], d_cells[k], cb, cudaMemcpyDeviceToHost, s);
+    for (int k = 0; k < 6 && rc == SGX_OK && e == cudaSuccess; ++k)
+      if (fracs[k]) e = cudaMemcpyAsync(fracs[k], d_fracs[k], fb, cudaMemcpyDeviceToHost, s);
+  }
+  const cudaError_t f = scratch_free(scratch, s);
+  if (e == cudaSuccess) e = f;
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (rc != SGX_OK) return rc;
+  if (e != cudaSuccess)
+    return set_error(SGX_ERR_CUDA, std::string(who) + ": " + cudaGetErrorString(e));
   return SGX_OK;
 }

@@ -18,7 +18,7 @@ Q_DENSITY, Q_SIE, Q_PRESSURE, Q_TEMPERATURE, Q_SPECIFIC_HEAT, Q_BULK_MODULUS = 1
 PTE_RHOT, PTE_PT, PTE_RHOU, PTE_FIXED_T, PTE_FIXED_P = 0, 1, 2, 3, 4
 TUNE_LOOKUP_BLOCKS_PER_SM, TUNE_LOOKUP_STAGE, TUNE_L2_PERSIST, TUNE_HOST_FILL_STAGED = 1, 2, 3, 4
 TUNE_PTE_FP32_ITERS, TUNE_PTE_RETRY_ITERS, TUNE_PTE_COUNT_ORDER = 5, 6, 7
-TUNE_PTE_MIXED_BLOCK = 8
+TUNE_PTE_MIXED_BLOCK, TUNE_PTE_GROUP_MIN_N = 8, 9
 PREC_FP64, PREC_MIXED = 0, 1
 
 EXPORTED = [
@@ -34,7 +34,7 @@ EXPORTED = [
     "sgx_pte_solve", "sgx_pte_solve_noalloc", "sgx_eos_helmholtz", "sgx_eos_helmholtz_dump",
     "sgx_server_create", "sgx_server_submit", "sgx_server_wait", "sgx_server_stats_get",
     "sgx_server_destroy", "sgx_host_alloc", "sgx_host_free", "sgx_eos_fill_host",
-    "sgx_get_sg_eos", "sgx_eos_modify_shifted", "sgx_eos_modify_scaled",
+    "sgx_get_sg_eos", "sgx_get_sg_eos_device", "sgx_eos_modify_shifted", "sgx_eos_modify_scaled",
     "sgx_eos_modify_bilinear_ramp", "sgx_eos_p_alpha_ramp_params", "sgx_eos_apply_modifiers",
     "sgx_eos_pt_derivatives", "sgx_eos_ideal_gas_entropy", "sgx_eos_stiff_gas_ref",
     "sgx_eos_noble_abel_ref", "sgx_init_sg_eos", "sgx_init_sg_IdealGas", "sgx_init_sg_StiffGas",
@@ -147,6 +147,7 @@ def load():
     lib.sgx_eos_fill_host.argtypes = [C.POINTER(SgxEos), C.c_int64, P, P, P, P, P, P, P,
                                       C.c_uint32, P, I, I]
     lib.sgx_get_sg_eos.argtypes = [I, I, I, I, P, P, I, P] + [P] * 15 + [D, I, P]
+    lib.sgx_get_sg_eos_device.argtypes = [I, I, I, I, P, P, I, P] + [P] * 15 + [D, I, P]
     lib.sgx_server_create.argtypes = [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]
     lib.sgx_server_submit.argtypes = [C.c_void_p, C.POINTER(PteRequest),
                                       C.POINTER(C.c_uint64)]
@@ -498,7 +499,7 @@ def get_sg_eos(eos_list, eos_offsets, offsets, cells, fracs, mass_frac_cutoff,
     nmat, cell_dim = fracs["frac_mass"].shape
     arr = (SgxEos * len(eos_list))(*eos_list)
     eo = (C.c_int * nmat)(*[int(x) for x in eos_offsets])
-    check(load().sgx_get_sg_eos(
+    check(load().sgx_get_sg_eos_device(
         nmat, offsets.numel(), cell_dim, input_int, C.cast(eo, C.c_void_p),
         C.cast(arr, C.c_void_p), len(eos_list), ptr(offsets),
         *(ptr(cells[k]) for k in ("press", "pmax", "vol", "spvol", "sie", "temp", "bmod",
@@ -506,6 +507,26 @@ def get_sg_eos(eos_list, eos_offsets, offsets, cells, fracs, mass_frac_cutoff,
         *(ptr(fracs.get(k)) for k in ("frac_mass", "frac_vol", "frac_ie", "frac_bmod",
                                       "frac_dpde", "frac_cv")),
         mass_frac_cutoff, precision, stream_ptr(stream)))
+
+
+def get_sg_eos_host(eos_list, eos_offsets, offsets, cells, fracs, mass_frac_cutoff,
+                    precision=PREC_FP64, input_int=1):
+    """get_sg_eos over host numpy arrays (contiguous; int32 offsets, float64
+    fields), updated in place, as the reference's interface takes them."""
+    nmat, cell_dim = fracs["frac_mass"].shape
+    arr = (SgxEos * len(eos_list))(*eos_list)
+    eo = (C.c_int * nmat)(*[int(x) for x in eos_offsets])
+
+    def p(a):
+        return None if a is None else C.c_void_p(a.ctypes.data)
+    check(load().sgx_get_sg_eos(
+        nmat, offsets.size, cell_dim, input_int, C.cast(eo, C.c_void_p),
+        C.cast(arr, C.c_void_p), len(eos_list), p(offsets),
+        *(p(cells[k]) for k in ("press", "pmax", "vol", "spvol", "sie", "temp", "bmod",
+                                "dpde", "cv")),
+        *(p(fracs.get(k)) for k in ("frac_mass", "frac_vol", "frac_ie", "frac_bmod",
+                                    "frac_dpde", "frac_cv")),
+        mass_frac_cutoff, precision, None))
 
 
 def status_view(status_u8):

@@ -1,16 +1,26 @@
 """The mixed-precision lookup path (FP32 bracket search + FP64 root and
-outputs) against the reference fixtures and against the plain FP64 path.
+outputs) and the mixed-precision PTE path against the reference fixtures
+and against the plain FP64 path.
 
-Error bar. Both paths return a root of the same piecewise-linear function
-sie(log10 T) at fixed rho; the reference stops regula falsi within 1e-14 in
-log10 T, the mixed path solves the bracketing cell exactly. Where sie is
-dominated by its cold (T-independent) part, rounding of sie itself limits
-the root to about eps * sie / (d sie / d log10 T): for this table up to
-~1e-12 relative in T at 100 K and low density. The tests therefore require
-T within 1e-11 relative everywhere and within 1e-12 for 99.9% of queries.
-P, bmod, cv and cs are interpolated at that T; their differences are bounded
-by 1e-10 relative to the larger of the value and 1e-6 of the batch's
-largest magnitude (P crosses zero inside the table)."""
+Error bars, per output and per element (plain relative error, no batch-wide
+floor):
+  * T: the reference stops regula falsi within 1e-14 in log10 T, the mixed
+    path solves the bracketing cell in closed form. Where sie is dominated by
+    its cold (T-independent) part, rounding of sie itself limits the root to
+    about eps * sie / (d sie / d log10 T): for this table up to ~5e-12
+    relative at 100 K and low density. T must be within 1e-11 relative
+    everywhere and within 1e-12 for 99.9% of queries.
+  * P, bmod, cv, cs: within 1e-10 relative of the FP64 value, or, where the
+    value is a small difference of large table entries (P crosses zero
+    inside the table), closer to the FP64 value than the FP64 value itself
+    moves when the input sie changes by 1e-14 relative (a backward-error
+    bound: the mixed answer is the FP64 answer of an input within ~50 ulp).
+  * PTE: T of every cell both solvers converge within 1e-10 relative of a
+    tight-tolerance FP64 solve (tolerances 1e-13); P within 1e-10 relative,
+    widened by that solve's own disagreement between the materials'
+    pressures and by the change of P_m(rho_m, T) when T moves by 1e-12
+    relative (a stiffened gas near P = 0 turns the solves' ~1e-13 in T into
+    ~1e-10 in P)."""
 import numpy as np
 import pytest
 
@@ -29,9 +39,29 @@ def sgx():
     return lib
 
 
-def scaled_err(a, b):
-    floor = 1e-6 * np.max(np.abs(b))
-    return np.abs(a - b) / np.maximum(np.abs(b), floor)
+def within(got, want, moved, rtol=1e-10):
+    """Per element: |got - want| <= rtol |want| + |moved - want|, where
+    moved is the FP64 value at an input perturbed by 1e-14 relative. Returns
+    the largest ratio of the error to that bound (<= 1 passes) and prints the
+    plain relative error."""
+    got, want, moved = (np.asarray(x, np.float64) for x in (got, want, moved))
+    err = np.abs(got - want)
+    bound = rtol * np.abs(want) + np.abs(moved - want)
+    e = rel_err(got, want)
+    print(f"  plain rel err: max {e.max():.2e} p99.9 {np.quantile(e, 0.999):.2e}; "
+          f"{int((e > rtol).sum())} above {rtol:g}")
+    r = np.where(err == 0, 0.0, err / np.maximum(bound, 1e-300))
+    return float(r.max())
+
+
+def fp64_moved(sgx, tab, rho, sie, q, lam=None, lam_stride=0):
+    """The FP64 path's T, P, bmod, cs at sie (1 + 1e-14)."""
+    sie_p = sie * (1.0 + 1e-14)
+    T, P, bm, cs = (torch.zeros_like(rho) for _ in range(4))
+    sgx.fill_eos(tab, rho, T, sie_p, P, None, bm, q, cs=cs, precision=sgx.PREC_FP64,
+                 lam=lam, lam_stride=lam_stride)
+    torch.cuda.synchronize()
+    return [x.cpu().numpy() for x in (T, P, bm, cs)]
 
 
 def check_T(got, want, bulk=True):
@@ -60,11 +90,19 @@ def test_mixed_lookup_matches_reference(sgx):
         sgx.fill_eos(tab, rho, T, sie, P, cv, bm, q, cs=cs, precision=sgx.PREC_MIXED)
         torch.cuda.synchronize()
         check_T(T.cpu().numpy(), fx["fill_T"])
-        for name, t in (("P", P), ("bmod", bm), ("cv", cv)):
-            e = scaled_err(t.cpu().numpy(), fx["fill_" + name])
-            assert e.max() <= 1e-10, (name, e.max())
+        # the FP64 path reproduces the fixture bit for bit (test_gpu_parity),
+        # so its perturbed run gives the fixture's sensitivity
+        Tm, Pm, bmm, csm = fp64_moved(sgx, tab, rho, sie, sgx.Q_TEMPERATURE | sgx.Q_PRESSURE |
+                                      sgx.Q_BULK_MODULUS)
+        cvm = torch.zeros_like(rho)
+        sgx.fill_eos(tab, rho, torch.zeros_like(rho), sie * (1.0 + 1e-14), torch.zeros_like(rho),
+                     cvm, torch.zeros_like(rho), q)
+        torch.cuda.synchronize()
+        for name, t, m in (("P", P, Pm), ("bmod", bm, bmm), ("cv", cv, cvm.cpu().numpy())):
+            r = within(t.cpu().numpy(), fx["fill_" + name], m)
+            assert r <= 1.0, (name, r)
         want_cs = np.sqrt(fx["fill_bmod"] / fx["rho"])
-        assert scaled_err(cs.cpu().numpy(), want_cs).max() <= 1e-10
+        assert within(cs.cpu().numpy(), want_cs, csm) <= 1.0
     finally:
         sgx.load().sgx_eos_finalize(C.byref(tab))
 
@@ -90,8 +128,11 @@ def test_mixed_lookup_full_size_against_fp64(sgx):
         a, b = out[sgx.PREC_MIXED], out[sgx.PREC_FP64]
         assert np.all(np.isfinite(a[0]))
         check_T(a[0], b[0])
-        for k in (1, 2, 3):
-            assert scaled_err(a[k], b[k]).max() <= 1e-10
+        moved = fp64_moved(sgx, tab, rho, sie, sgx.Q_TEMPERATURE | sgx.Q_PRESSURE |
+                           sgx.Q_BULK_MODULUS)
+        for k, name in ((1, "P"), (2, "bmod"), (3, "cs")):
+            r = within(a[k], b[k], moved[k])
+            assert r <= 1.0, (name, r)
     finally:
         sgx.load().sgx_eos_finalize(C.byref(tab))
 
@@ -191,8 +232,10 @@ def test_mixed_lookup_between_coarse_density_nodes(sgx):
                     out[prec].append(lam.cpu().numpy())
             a, b = out[sgx.PREC_MIXED], out[sgx.PREC_FP64]
             check_T(a[0], b[0], bulk=False)
+            lam_m = torch.as_tensor(lam_init, device="cuda").clone() if cached else None
+            moved = fp64_moved(sgx, tab, rho, sie, q, lam=lam_m, lam_stride=2 if cached else 0)
             for k in (1, 2, 3):
-                assert scaled_err(a[k], b[k]).max() <= 1e-10, k
+                assert within(a[k], b[k], moved[k]) <= 1.0, k
             if cached:
                 # the cache holds log10 rho (the reference's rounding, exactly)
                 # and log10 T (the root, within T's error / ln 10)
@@ -229,24 +272,72 @@ def run_pte(sgx, wl, precision, params=None):
     return {k: v.cpu().numpy() for k, v in t.items()}, sgx.status_view(status)
 
 
+@pytest.fixture
+def group_min_n(sgx, request):
+    """Sets SGX_TUNE_PTE_GROUP_MIN_N for one test, restoring it after."""
+    import ctypes as C
+    L = sgx.load()
+    v = C.c_int()
+    assert L.sgx_tune_get(sgx.TUNE_PTE_GROUP_MIN_N, C.byref(v)) == 0
+    assert L.sgx_tune_set(sgx.TUNE_PTE_GROUP_MIN_N, request.param) == 0
+    yield request.param
+    L.sgx_tune_set(sgx.TUNE_PTE_GROUP_MIN_N, v.value)
+
+
+@pytest.mark.parametrize("group_min_n", [3, 7], indirect=True,
+                         ids=["lane_groups_from_3", "thread_per_cell"])
 @pytest.mark.parametrize("kind", ["two_material", "batched"])
-def test_mixed_pte_accuracy(sgx, kind):
+def test_mixed_pte_accuracy(sgx, kind, group_min_n):
+    """Against a tight FP64 solve, every cell both converge: P and T within
+    1e-10 relative (P widened by the tight solve's own spread of the
+    materials' pressures); converged flags as the reference's default solve
+    within 1e-5 of the cells (pass 2 caps the FP64 re-solve at 8 iterations
+    per material, the reference at 128)."""
     from sgx import workloads as W
     wl = W.pte_two_material(65536, seed=5) if kind == "two_material" else \
         W.pte_batched(1 << 18, seed=6)
     ref, st_ref = run_pte(sgx, wl, sgx.PREC_FP64, params=sgx.mix_params(**TIGHT))
+    dflt, st_d = run_pte(sgx, wl, sgx.PREC_FP64)
     got, st = run_pte(sgx, wl, sgx.PREC_MIXED)
     present = wl["eos_idx"] >= 0 if wl["eos_idx"] is not None else np.ones_like(wl["rho"], bool)
     both = st["converged"] & st_ref["converged"]
-    resolved = st["resolved_fp64"].mean()
-    print(f"{kind}: converged mixed {st['converged'].mean():.4f} tight {st_ref['converged'].mean():.4f}"
-          f" fp64 re-solve {resolved:.4f}")
-    assert st["converged"].mean() >= st_ref["converged"].mean() - 1e-3
-    sel = both[None, :] & present
+    ncell = both.size
+    flag_diff = int((st["converged"] != st_d["converged"]).sum())
+    print(f"{kind}: converged mixed {st['converged'].mean():.5f} default {st_d['converged'].mean():.5f}"
+          f" tight {st_ref['converged'].mean():.5f}; fp64 re-solve {st['resolved_fp64'].mean():.4f};"
+          f" flags differing from the default solve: {flag_diff}")
+    assert flag_diff <= 1e-5 * ncell + 1
+    P_t = np.where(present, ref["press"], np.nan)
+    spread = np.nanmax(P_t, axis=0) - np.nanmin(P_t, axis=0)
+    # |P_m(rho_m, T (1 + 1e-12)) - P_m(rho_m, T)| per material slot
+    eos = [sgx.make_eos(kk, pp) for kk, pp in wl["materials"]]
+    idx = wl["eos_idx"] if wl["eos_idx"] is not None else \
+        np.repeat(np.arange(len(eos), dtype=np.int32)[:, None], ncell, axis=1)
+    moved = np.zeros_like(ref["press"])
+    for m in range(ref["press"].shape[0]):
+        r = torch.as_tensor(ref["rho"][m], device="cuda")
+        T0 = torch.as_tensor(ref["temp"][m], device="cuda")
+        for k, e in enumerate(eos):
+            sel = idx[m] == k
+            if not sel.any():
+                continue
+            p0, p1 = torch.zeros_like(r), torch.zeros_like(r)
+            sgx.eval_eos(e, sgx.FN_P_FROM_RHO_T, r, T0, p0)
+            sgx.eval_eos(e, sgx.FN_P_FROM_RHO_T, r, T0 * (1.0 + 1e-12), p1)
+            torch.cuda.synchronize()
+            moved[m, sel] = np.abs((p1 - p0).cpu().numpy())[sel]
+    dP = np.where(present, moved, 0.0).max(axis=0)
     for k in ("temp", "press"):
-        e = scaled_err(got[k][sel], ref[k][sel])
+        e = rel_err(got[k], ref[k])
+        e[~present] = 0.0
+        e = e.max(axis=0)[both]
         print(f"  {k}: max {e.max():.2e} p99.9 {np.quantile(e, 0.999):.2e}")
-        assert np.quantile(e, 0.999) <= 1e-10, k
+        if k == "temp":
+            assert e.max() <= 1e-10, e.max()
+        else:
+            err = np.where(present, np.abs(got[k] - ref[k]), 0.0).max(axis=0)
+            bound = 1e-10 * np.where(present, np.abs(ref[k]), np.inf).min(axis=0) + spread + dP
+            assert np.all(err[both] <= bound[both]), float((err / bound)[both].max())
     # closure constraints hold exactly in FP64 for polished cells
     pol = st["converged"] & ~st["resolved_fp64"]
     vsum = np.where(present, got["vfrac"], 0).sum(axis=0)

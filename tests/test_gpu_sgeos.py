@@ -1,5 +1,6 @@
-"""sgx_get_sg_eos against the reference's get_sg_eos driver in each input
-mode (tests/golden/get_sg_eos*.npz, made by the oracle around the
+"""sgx_get_sg_eos (host arrays, as the reference takes them) and
+sgx_get_sg_eos_device (device arrays) against the reference's get_sg_eos
+driver in each input mode (tests/golden/get_sg_eos*.npz, made by the oracle around the
 reference's own PTESolverRhoT / FixedT / FixedP, root finder and EOS calls):
 every per-cell and per-material output, within 1e-12 relative (the n >= 3
 solves factor the Jacobian with a different QR than the oracle), untouched
@@ -25,15 +26,21 @@ def sgx():
     return lib
 
 
-def run(sgx, fx, precision):
+def run(sgx, fx, precision, host=False):
     eos = [sgx.make_eos(k, p) for k, p in materials_from_rows(fx["materials"])]
     if "mods" in fx:  # ShiftedEOS / ScaledEOS / BilinearRampEOS per material
         eos = [sgx.modify(e, shift=r[1] if int(r[0]) & 1 else None,
                           scale=r[2] if int(r[0]) & 2 else None,
                           ramp=r[3:7] if int(r[0]) & 4 else None) for e, r in zip(eos, fx["mods"])]
+    mode = int(fx["mode"]) if "mode" in fx else 1
+    if host:
+        arrs = {k: np.ascontiguousarray(fx["in_" + k], np.float64).copy() for k in CELLS + FRACS}
+        sgx.get_sg_eos_host(eos, fx["eos_offsets"], np.ascontiguousarray(fx["offsets"], np.int32),
+                            {k: arrs[k] for k in CELLS}, {k: arrs[k] for k in FRACS},
+                            float(fx["cutoff"]), precision=precision, input_int=mode)
+        return arrs
     dev = {k: torch.as_tensor(fx["in_" + k], device="cuda").clone() for k in CELLS + FRACS}
     offsets = torch.as_tensor(fx["offsets"], device="cuda")
-    mode = int(fx["mode"]) if "mode" in fx else 1
     sgx.get_sg_eos(eos, fx["eos_offsets"], offsets, {k: dev[k] for k in CELLS},
                    {k: dev[k] for k in FRACS}, float(fx["cutoff"]), precision=precision,
                    input_int=mode)
@@ -50,12 +57,13 @@ def close(got, want, rtol, label):
     assert err.max(initial=0.0) <= rtol, f"{label}: max rel err {err.max():.3e}"
 
 
+@pytest.mark.parametrize("arrays", ["host", "device"])
 @pytest.mark.parametrize("name", ["get_sg_eos", "get_sg_eos_rho_t", "get_sg_eos_rho_p",
                                   "get_sg_eos_p_t", "get_sg_eos_modified",
                                   "get_sg_eos_p_t_modified"])
-def test_get_sg_eos_matches_reference(sgx, name):
+def test_get_sg_eos_matches_reference(sgx, name, arrays):
     fx = golden(name)
-    got = run(sgx, fx, 0)
+    got = run(sgx, fx, 0, host=arrays == "host")
     for k in CELLS + FRACS:
         close(got[k], fx["out_" + k], 1e-12, k)
     # cells outside the offset list are untouched
@@ -82,12 +90,17 @@ def test_get_sg_eos_rejects_bad_modes(sgx):
     lib = sgx.load()
     e = (sgx.SgxEos * 1)(sgx.make_eos(1, (0.4, 0.718e7)))
     eo = (C.c_int * 1)(1)
-    for mode in (-4, 2):
-        rc = lib.sgx_get_sg_eos(1, 4, 4, mode, C.cast(eo, C.c_void_p), C.cast(e, C.c_void_p), 1,
-                                *([None] * 16), 0.0, 0, None)
+    for fn in (lib.sgx_get_sg_eos, lib.sgx_get_sg_eos_device):
+        for mode in (-4, 2):
+            rc = fn(1, 4, 4, mode, C.cast(eo, C.c_void_p), C.cast(e, C.c_void_p), 1,
+                    *([None] * 16), 0.0, 0, None)
+            assert rc == 1
+        # the fixed-T / fixed-P solves have no mixed-precision form
+        for mode in (-3, -2):
+            rc = fn(1, 4, 4, mode, C.cast(eo, C.c_void_p), C.cast(e, C.c_void_p), 1,
+                    *([None] * 16), 0.0, 1, None)
+            assert rc == 5
+        # null arrays are refused before any copy
+        rc = fn(1, 4, 4, 1, C.cast(eo, C.c_void_p), C.cast(e, C.c_void_p), 1,
+                *([None] * 16), 0.0, 0, None)
         assert rc == 1
-    # the fixed-T / fixed-P solves have no mixed-precision form
-    for mode in (-3, -2):
-        rc = lib.sgx_get_sg_eos(1, 4, 4, mode, C.cast(eo, C.c_void_p), C.cast(e, C.c_void_p), 1,
-                                *([None] * 16), 0.0, 1, None)
-        assert rc == 5
