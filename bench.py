@@ -43,6 +43,7 @@ N_PTE2 = 65536
 N_PTE_BATCH = 1 << 22
 N_HELM = 1 << 22
 LOOKUP_BYTES_PER_QUERY = 16 + 32  # rho, sie in; T, P, bmod, cs out (float64)
+HELM_BYTES_PER_CELL = 32 + 32     # rho, sie, Abar, Zbar in; T, P, bmod, cs out
 LOOKUP_TRAFFIC_2_24 = (283.67 + 489.62 + 2.19) * 1e6  # measured DRAM bytes per 2^24-query step
 Q_OUT = 8 | 4 | 32                # temperature | pressure | bulk modulus
 METRIC = "PTE mixed cells/s & EOS lookups/s, 1 GB300, batched+FP32-refined vs plain FP64"
@@ -136,6 +137,20 @@ def max_over_ranks(x, world):
     return reduce_max(x, world, device="cuda")
 
 
+def rel_stats(a, b):
+    """max, p99.9 and count above 1e-10 of |a - b| / |b| over device tensors
+    (0 where a == b, NaN pairs excluded)."""
+    import torch
+    d = (a - b).abs() / b.abs().clamp_min(1e-300)
+    d = torch.where(a == b, torch.zeros_like(d), d)
+    d = d[~torch.isnan(d)]
+    if d.numel() == 0:
+        return {"max": 0.0, "p999": 0.0, "n_above_1e-10": 0}
+    k = max(1, int(round(0.999 * d.numel())))
+    return {"max": float(d.max()), "p999": float(torch.kthvalue(d.cpu(), k).values),
+            "n_above_1e-10": int((d > 1e-10).sum())}
+
+
 def time_steps(fn, steps, warmup, stream):
     import torch
     for _ in range(warmup):
@@ -184,6 +199,7 @@ def bench_lookup(args, world, local, stream, out):
                                   stream=stream)
         out["autotuned"] = {"lookup_blocks_per_sm": shape[0], "lookup_stage": shape[1]}
         results = {}
+        outs = {}
         for prec, name in ((lib.PREC_FP64, "fp64"), (lib.PREC_MIXED, "mixed")):
             steps = args.steps if prec == lib.PREC_MIXED else max(1, min(args.steps, 5))
             barrier(world)
@@ -195,11 +211,17 @@ def bench_lookup(args, world, local, stream, out):
             results[name] = dict(value=world * n * steps / dt, ms=per_launch * 1e3,
                                  gbs=LOOKUP_BYTES_PER_QUERY * n / per_launch / 1e9,
                                  clocks=clk.summary(), steps=steps)
+            outs[name] = [x.clone() for x in (T, P, B, CS)]
+        # per-output error of the mixed path against the plain FP64 path (which
+        # matches the oracle bit for bit), plain relative, every query
+        out["mixed_error"] = {k: rel_stats(a, b) for k, a, b in
+                              zip(("T", "P", "bmod", "cs"), outs["mixed"], outs["fp64"])}
+        del outs
         m = results["mixed"]
         out["clocks"] = m["clocks"]
         # DRAM bytes of one 2^24-query step (both kernels),
-        # dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture
-        # (profiles/spiner_fill_fast_lookup.md), scaled to this step's queries
+        # dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture,
+        # scaled to this step's queries (not re-measured by this run)
         traffic = LOOKUP_TRAFFIC_2_24 * n / float(1 << 24)
         out["roofline"] = {"bound": "hbm", "achieved": m["gbs"], "peak": hbm, "unit": "GB/s",
                            "frac": m["gbs"] / hbm, "traffic": traffic,
@@ -207,10 +229,9 @@ def bench_lookup(args, world, local, stream, out):
                            "kernel": "spiner_fill_fast + spiner_fill_ref (sgx_lookup_mixed.cu, "
                                      "sgx_fp64.cu); achieved over the whole step",
                            "bytes_per_query": LOOKUP_BYTES_PER_QUERY,
-                           # neither HBM nor one pipe binds: FP64 pipe 49%, L1 data
-                           # pipe 65%, issue 68% (ncu capture in
-                           # profiles/spiner_fill_fast_lookup.md)
-                           "fp64_pipe_pct_active_ncu": 48.6, "l1_lsu_pct_ncu": 64.7}
+                           "traffic_source": "ncu capture of one 2^24-query step, scaled "
+                                             "to the step's queries; a constant, not "
+                                             "measured by this run"}
         f = results["fp64"]
         out["plain_fp64"] = {"value": f["value"], "unit": "lookups/s", "ms_per_step": f["ms"],
                              "hbm_frac": f["gbs"] / hbm, "clocks": f["clocks"],
@@ -320,8 +341,72 @@ def bench_pte(args, world, stream, out):
         if "fp64" in entry and "mixed" in entry:
             entry["mixed_over_fp64"] = entry["mixed"]["cells_per_s"] / \
                 entry["fp64"]["cells_per_s"]
+            entry["mixed_error"] = pte_errors(lib, eos_list, idx, vt, st, base, wl, stream)
+        if world == 1 and not args.no_cpu_baseline:
+            entry["cpu_baseline"] = pte_cpu_baseline(wl)
         pte[name] = entry
     out["pte"] = pte
+
+
+TIGHT = dict(pte_rel_tolerance_p=1e-13, pte_rel_tolerance_e=1e-13, pte_abs_tolerance_p=0.0,
+             pte_rel_tolerance_p_sufficient=1e-12, pte_rel_tolerance_e_sufficient=1e-12,
+             pte_abs_tolerance_p_sufficient=0.0)
+
+
+def pte_errors(lib, eos_list, idx, vt, st, base, wl, stream):
+    """The mixed path's P and T per cell against a tight-tolerance FP64 solve
+    (tolerances 1e-13), over the cells both converge, plain relative; and
+    how many cells its converged flag differs from the default FP64 solve's
+    (the reference's own flag)."""
+    import torch
+    res = {}
+    for key, prec, params in (("tight", lib.PREC_FP64, lib.mix_params(**TIGHT)),
+                              ("default", lib.PREC_FP64, None),
+                              ("mixed", lib.PREC_MIXED, None)):
+        work = {k: v.clone() for k, v in base.items()}
+        status = torch.empty(vt.numel() * 16, dtype=torch.uint8, device="cuda")
+        lib.pte_solve(lib.PTE_RHOT, eos_list, idx, vt, st, work["rho"], work["vfrac"],
+                      work["sie"], work["temp"], work["press"], params=params, status=status,
+                      precision=prec, stream=stream)
+        torch.cuda.synchronize()
+        res[key] = (work, lib.status_view(status))
+    t, st_t = res["tight"]
+    m, st_m = res["mixed"]
+    both = torch.as_tensor(st_m["converged"] & st_t["converged"], device="cuda")
+    present = (idx >= 0) if idx is not None else torch.ones_like(t["press"], dtype=torch.bool)
+    e = {}
+    for k, name in (("press", "P"), ("temp", "T")):
+        r = (m[k] - t[k]).abs() / t[k].abs().clamp_min(1e-300)
+        r = torch.where(present & (m[k] != t[k]), r, torch.zeros_like(r)).amax(dim=0)
+        r = r[both]
+        kk = max(1, int(round(0.999 * r.numel())))
+        e[name] = {"max": float(r.max()), "p999": float(torch.kthvalue(r.cpu(), kk).values),
+                   "n_cells_above_1e-10": int((r > 1e-10).sum())}
+    e["cells_compared"] = int(both.sum())
+    e["against"] = "FP64 solve with tolerances 1e-13 (same cells converged in both)"
+    e["flags_differing_from_default_fp64"] = int(
+        (st_m["converged"] != res["default"][1]["converged"]).sum())
+    return e
+
+
+def pte_cpu_baseline(wl):
+    """The oracle restatement (oracle/port) of PTESolverRhoT on every host
+    core over the whole workload, best of 3."""
+    import refbind as rb
+    port = rb.port()
+    descs = [rb.eos_desc(k, p) for k, p in wl["materials"]]
+    best = None
+    for _ in range(3):
+        r = {k: wl[k].copy() for k in ("rho", "vfrac", "sie", "temp", "press")}
+        t0 = time.perf_counter()
+        port.pte(0, descs, wl["eos_idx"], wl["vfrac_tot"], wl["sie_tot"], r["rho"], r["vfrac"],
+                 r["sie"], r["temp"], r["press"], params=port.mix_params(), nthreads=0)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    n = wl["sie_tot"].size
+    return {"value": n / best, "unit": "cells/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"the whole {n}-cell workload, best of 3, OpenMP over all host threads, "
+                      "oracle/port/sgport.cpp PTESolverRhoT"}
 
 
 def bench_helm(args, world, stream, out):
@@ -349,22 +434,46 @@ def bench_helm(args, world, stream, out):
         sie = torch.empty_like(rho)
         lib.fill_eos(eos, rho, Tin, sie, None, None, None, lib.Q_SIE, lam=lam, lam_stride=3,
                      stream=stream)
-        T, P, B, CS = (torch.empty_like(rho) for _ in range(4))
         q = lib.Q_TEMPERATURE | lib.Q_PRESSURE | lib.Q_BULK_MODULUS
+        hbm, hbm_kind = peaks()
+        res, outs = {}, {}
+        for prec, pname in ((lib.PREC_FP64, "fp64"), (lib.PREC_MIXED, "mixed")):
+            T, P, B, CS = (torch.empty_like(rho) for _ in range(4))
 
-        def step():
-            lam.copy_(lam0)
-            lib.fill_eos(eos, rho, T, sie, P, None, B, q, lam=lam, lam_stride=3, cs=CS,
-                         stream=stream)
+            def step():
+                lam.copy_(lam0)
+                lib.fill_eos(eos, rho, T, sie, P, None, B, q, lam=lam, lam_stride=3, cs=CS,
+                             precision=prec, stream=stream)
 
-        steps = max(1, min(args.steps, 5))
-        dt = max_over_ranks(time_steps(step, steps, args.warmup, stream), world)
-        rel = ((T - Tin).abs() / Tin).cpu().numpy()
+            steps = max(1, min(args.steps, 5))
+            dt = max_over_ranks(time_steps(step, steps, args.warmup, stream), world)
+            rel = ((T - Tin).abs() / Tin).cpu().numpy()
+            gbs = HELM_BYTES_PER_CELL * n / (dt / steps) / 1e9
+            res[pname] = {"cells_per_s": world * n * steps / dt, "ms_per_step": dt / steps * 1e3,
+                          "recovered_T_1e-8_frac": float((rel <= 1e-8).mean()),
+                          "roofline": {"bound": "fp64 pipe", "bytes_per_cell": HELM_BYTES_PER_CELL,
+                                       "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                                       "frac": gbs / hbm,
+                                       "peak_kind": hbm_kind + " (burst copy)"}}
+            outs[pname] = (T, P, B, CS)
+        # per-output differences of the mixed inversion to the FP64 one, over
+        # the cells whose FP64 inversion recovers T to 1e-8 (well posed)
+        good = ((outs["fp64"][0] - Tin).abs() / Tin) <= 1e-8
+        err = {}
+        for k, name in enumerate(("T", "P", "bmod", "cs")):
+            a, b = outs["mixed"][k][good], outs["fp64"][k][good]
+            err[name] = rel_stats(a, b)
         out["helmholtz"] = {
             "workload": f"Helmholtz T(rho,sie)+P+bmod+cs, {n} cells, synthetic 271x101 table",
-            "cells_per_s": world * n * steps / dt, "ms_per_step": dt / steps * 1e3,
-            "dtype": "f64", "recovered_T_1e-8_frac": float((rel <= 1e-8).mean()),
-            "kernel": "helm_fill_kernel (sgx_helm.cu)"}
+            "cells_per_s": res["mixed"]["cells_per_s"], "ms_per_step": res["mixed"]["ms_per_step"],
+            "dtype": "f32 Newton phase + f64 Newton steps and evaluations",
+            "fp64": res["fp64"], "mixed": res["mixed"],
+            "mixed_over_fp64": res["mixed"]["cells_per_s"] / res["fp64"]["cells_per_s"],
+            "mixed_error_vs_fp64_well_posed": err,
+            "kernel": "helm_invert_pass1<true>/pass2/pass3 (sgx_helm.cu)",
+            "cpu_baseline": {"value": None, "unavailable": "the oracle restatement "
+                             "(oracle/port) has no Helmholtz model and the compiled reference "
+                             "builds only where its sources are"}}
         lib.load().sgx_eos_finalize(__import__("ctypes").byref(eos))
 
 
@@ -454,6 +563,28 @@ def bench_serve(args, stream, out):
                     "p99_ms": float(np.quantile(lat, 0.99) * 1e3),
                     "cells_per_s": cells / wall}
 
+        # the bound folding aims at: the same payloads as ONE device-resident
+        # mixed solve (no host copies, no arrivals)
+        cat = {k: np.concatenate([pp[k + "_in"] for pp in pays], axis=1)
+               for k in ("rho", "vfrac", "sie", "temp", "press")}
+        cidx = torch.as_tensor(np.concatenate([pp["eos_idx"] for pp in pays], axis=1),
+                               device="cuda")
+        cvt = torch.as_tensor(np.concatenate([pp["vfrac_tot"] for pp in pays]), device="cuda")
+        cst = torch.as_tensor(np.concatenate([pp["sie_tot"] for pp in pays]), device="cuda")
+        cbase = {k: torch.as_tensor(v, device="cuda") for k, v in cat.items()}
+        cwork = {k: v.clone() for k, v in cbase.items()}
+
+        def one_solve():
+            for k in cwork:
+                cwork[k].copy_(cbase[k])
+            lib.pte_solve(lib.PTE_RHOT, eos, cidx, cvt, cst, cwork["rho"], cwork["vfrac"],
+                          cwork["sie"], cwork["temp"], cwork["press"], precision=lib.PREC_MIXED,
+                          stream=stream)
+
+        ncat = int(cvt.numel())
+        dt_cat = time_steps(one_solve, 3, 3, stream)
+        batched_rate = ncat * 3 / dt_cat
+        del cbase, cwork
         nreq = args.serve_requests
         run_server(0, 4, 1)  # warm-up: module loads, pool growth
         lat, wall, cells = run_server(0, nreq, 11)
@@ -473,8 +604,11 @@ def bench_serve(args, stream, out):
         out["serve"] = {
             "workload": f"Poisson closure requests, {npay} payloads of log-uniform 1e3-1e6 cells, "
                         "2-4 of 9 EOS (8 analytic + tabulated), 64 GB budget",
-            "slots": args.serve_slots, "precision": "mixed (FP32 + FP64 refinement)",
+            "batch_slots": args.serve_slots, "precision": "mixed (FP32 + FP64 refinement)",
+            "folding": "requests waiting at each admission are merged into one binned solve",
             "saturation_cells_per_s": sat, "saturation_req_per_s": sat_rate,
+            "one_batched_solve_cells_per_s": batched_rate,
+            "one_batched_solve_cells": ncat,
             "points": points,
             "baseline_percall_fp64": {"saturation_cells_per_s": base_sat, "points": base_pts}}
         lib.load().sgx_eos_finalize(ctypes.byref(tab))
@@ -500,7 +634,7 @@ def run_ours(args):
     return out, world, rank
 
 
-def cpu_baseline(sample=1 << 21, min_seconds=3.0):
+def cpu_baseline(sample=1 << 21, min_seconds=10.0):
     """The oracle restatement timed on the host cores over a bounded sample
     of the lookup workload."""
     import refbind as rb
@@ -528,6 +662,46 @@ def cpu_baseline(sample=1 << 21, min_seconds=3.0):
                       f"host threads, oracle/port/sgport.cpp FillEos(T|P|bmod)"}
 
 
+def reference_arm(args, config):
+    """The CPU implementation of the headline workload on the host cores:
+    the oracle restatement (oracle/port), OpenMP over all host threads,
+    --warmup untimed and exactly --steps timed steps, each the whole
+    --queries-query FillEos(T|P|bmod) plus the sound speed sqrt(bmod/rho)."""
+    import refbind as rb
+    from sgx import sp5lite
+    port = rb.port()
+    n = args.queries
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "stiffgas.sp5")
+        sp5lite.stiffgas_table(path)
+        rho, sie = sp5lite.stiffgas_queries(n, seed=2024)
+        d = rb.eos_desc(rb.SPINER_RHOT, [], path=path, matid=1)
+        T, P, cv, B, cs = (np.zeros(n) for _ in range(5))
+
+        def step():
+            port.fill_eos(d, rho, T, sie, P, cv, B, Q_OUT)
+            np.sqrt(B / rho, out=cs)
+
+        for _ in range(args.warmup):
+            step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step()
+        dt = time.perf_counter() - t0
+    value = n * args.steps / dt
+    cb = {"value": value, "unit": "lookups/s", "cores": os.cpu_count(), "kind": "port",
+          "sample": f"the whole {n}-query workload per step, {args.steps} steps after "
+                    f"{args.warmup} warm-up, OpenMP over all host threads, "
+                    "oracle/port/sgport.cpp FillEos(T|P|bmod) + numpy sqrt(bmod/rho)"}
+    return {"metric": METRIC, "value": value, "unit": "lookups/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded; StiffGas-sampled table)", "config": config,
+            "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": "lookups/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -540,9 +714,9 @@ def main():
     ap.add_argument("--pte-cells", type=int, default=N_PTE_BATCH)
     ap.add_argument("--pte2-cells", type=int, default=N_PTE2)
     ap.add_argument("--helm-cells", type=int, default=N_HELM)
-    ap.add_argument("--serve-requests", type=int, default=32)
+    ap.add_argument("--serve-requests", type=int, default=500)
     ap.add_argument("--serve-payloads", type=int, default=16)
-    ap.add_argument("--serve-slots", type=int, default=8)
+    ap.add_argument("--serve-slots", type=int, default=2)
     ap.add_argument("--only", default="all",
                     choices=["all", "lookup", "pte", "pte2", "ptebatch", "helm", "serve"])
     ap.add_argument("--pte-prec", default="both", choices=["both", "fp64", "mixed"])
@@ -557,16 +731,7 @@ def main():
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:
             return
-        steps = args.steps
-        cb = cpu_baseline(min_seconds=2.0)
-        line = {"metric": METRIC, "value": cb["value"], "unit": "lookups/s", "n_gpus": args.gpus,
-                "steps": steps, "warmup": args.warmup, "ms_per_step": N_LOOKUP / cb["value"] * 1e3,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f64", "data": "synthetic", "config": config, "impl": "reference",
-                "cpu_baseline": cb,
-                "e2e": {"value": cb["value"], "unit": "lookups/s", "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        print(json.dumps(reference_arm(args, config)))
         return
     out, world, rank = run_ours(args)
     if rank != 0:
@@ -581,6 +746,7 @@ def main():
             "data": "synthetic (seeded; StiffGas-sampled table)", "config": config,
             "e2e": out.get("e2e"), "roofline": out["roofline"], "clocks": out["clocks"],
             "gpu_launches": out["gpu_launches"], "plain_fp64": out["plain_fp64"],
+            "mixed_error": out.get("mixed_error"),
             "pte": out.get("pte"), "helmholtz": out.get("helmholtz"),
             "serve": out.get("serve"), "fp_peaks": out.get("fp_peaks"),
             "autotuned": out.get("autotuned")}

@@ -466,6 +466,23 @@ int sgx_tune_autotune_fill(const sgx_eos *eos, int64_t n, double *rho, double *t
                            uint32_t output, double *lambda, int lambda_stride, int reps,
                            int *blocks_per_sm, int *stage, sgx_stream_t stream);
 
+/* The autotuner of the mixed-precision PTE launch: times every combination
+ * of SGX_TUNE_PTE_MIXED_BLOCK (32, 64, 128) and SGX_TUNE_PTE_COUNT_ORDER (0,
+ * 1) -- and, with tune_group non-zero, SGX_TUNE_PTE_GROUP_MIN_N (the current
+ * value, 2, 4, 7) -- on the caller's own RhoT batch (the arguments of
+ * sgx_pte_solve), 1 + reps solves per setting with CUDA events on `stream`,
+ * and keeps the fastest set; chosen (nullable, 3 ints) receives (block,
+ * order, group_min_n). The starting state is copied aside and restored
+ * before every trial (stream-ordered pool memory, five arrays' worth); on
+ * return the arrays hold the solve of the winning setting. The first two
+ * knobs never change a result; the lane-group threshold changes results
+ * within the mixed path's stated tolerance only. No reference counterpart. */
+int sgx_tune_autotune_pte(int nmat, int64_t ncell, const sgx_eos *eos_list, int neos,
+                          const int32_t *eos_idx, const double *vfrac_tot, const double *sie_tot,
+                          double *rho, double *vfrac, double *sie, double *temp, double *press,
+                          double *lambda, const sgx_mix_params *params, sgx_pte_status *status,
+                          int reps, int tune_group, int *chosen, sgx_stream_t stream);
+
 /* Largest ncell sgx_pte_solve_noalloc accepts. */
 #define SGX_PTE_NOALLOC_MAX_CELLS 1048576
 
@@ -593,18 +610,22 @@ int sgx_finalize_sg_eos(int nmat, sgx_eos **eos);
 /* ---- Serving: a device-resident request loop for PTE closure batches ----
  * No reference counterpart: the reference is a library called once per
  * batch (get_sg_eos, singularity_eos.hpp:114-132). The server keeps the EOS
- * tables and a device arena of hbm_budget_bytes resident, admits submitted
- * requests in arrival order whenever an in-flight slot (a CUDA stream) and
- * arena space for the request's arrays and solver scratch are free, and runs
- * each admitted request (host->device copy, PTE solve, device->host copy) on
- * its slot, so requests that arrive while others are on the GPU overlap
- * with them. A request's result is the one sgx_pte_solve gives for the same
- * inputs. Requests larger than the whole arena are rejected at submission. */
+ * tables and a device arena of hbm_budget_bytes resident. Whenever one of
+ * its max_inflight batch slots (each a CUDA stream) is free, it folds the
+ * requests waiting at that moment, in arrival order and as many as fit the
+ * arena (up to 2^22 cells), into ONE merged batch: their cells laid end to
+ * end, one binned PTE solve over all of them, each request's rows copied
+ * back to its own arrays. Requests that arrive while batches are on the GPU
+ * form the next batch, which overlaps with them. A request's result is the
+ * one sgx_pte_solve gives for the same inputs alone, bit for bit (every cell
+ * is solved independently). Requests larger than the whole arena are
+ * rejected at submission; a request that does not fit waits at the head of
+ * the queue until memory frees up (no overtaking). */
 typedef struct sgx_server sgx_server;
 
 typedef struct sgx_server_config {
   size_t hbm_budget_bytes; /* device arena for request arrays and scratch */
-  int max_inflight;        /* concurrent requests on the device (1..64) */
+  int max_inflight;        /* merged batches on the device at once (1..64) */
   int solver;              /* SGX_PTE_RHOT (SGX_PTE_PT with SGX_PREC_FP64 only) */
   int precision;           /* SGX_PREC_FP64 or SGX_PREC_MIXED */
   const sgx_eos *eos_list; /* host array, copied; tables must stay resident */
@@ -632,8 +653,9 @@ typedef struct sgx_pte_request {
 typedef struct sgx_server_stats {
   uint64_t submitted, completed, failed;
   uint64_t cells_completed;
-  int inflight, queued;
+  int inflight, queued; /* requests on the device, requests waiting */
   size_t arena_used, arena_peak;
+  uint64_t batches;     /* merged solves issued */
 } sgx_server_stats;
 
 int sgx_server_create(const sgx_server_config *cfg, sgx_server **out);

@@ -368,8 +368,6 @@ int sgx_eos_fill_ex(const sgx_eos *eos, int64_t n, double *rho, double *temp, do
                                    "temperature must be provided.");
     if ((output & SGX_Q_TEMPERATURE) ? !sie : !temp)
       return fail(SGX_ERR_INVALID, "sgx_eos_fill: the input (sie or temp) array is null");
-    if (precision != SGX_PREC_FP64)
-      return fail(SGX_ERR_UNSUPPORTED, "sgx_eos_fill: Helmholtz runs in FP64 only");
   }
   sgx::FillArgs a;
   a.eos = *eos;
@@ -386,7 +384,12 @@ int sgx_eos_fill_ex(const sgx_eos *eos, int64_t n, double *rho, double *temp, do
   a.output = output;
   a.err = nullptr;
   cudaError_t e;
-  if (precision == SGX_PREC_MIXED) {
+  if (eos->type == SGX_HELMHOLTZ) {
+    // mixed: the T(rho, sie) inversion's Newton iteration starts with an
+    // FP32 phase; evaluations and outputs stay FP64
+    e = sgx::launch_helm_fill(a, reinterpret_cast<cudaStream_t>(stream),
+                              precision == SGX_PREC_MIXED);
+  } else if (precision == SGX_PREC_MIXED) {
     // The mixed path covers the hot call: a tabulated rho-T model with
     // (rho, sie) in and any of T, P, cv, bmod out.
     const uint32_t allowed = SGX_Q_TEMPERATURE | SGX_Q_PRESSURE | SGX_Q_SPECIFIC_HEAT |
@@ -397,8 +400,6 @@ int sgx_eos_fill_ex(const sgx_eos *eos, int64_t n, double *rho, double *temp, do
                   "sgx_eos_fill: mixed precision needs a tabulated rho-T EOS, (rho, sie) "
                   "inputs and T among the outputs");
     e = sgx::launch_fill_mixed(a, reinterpret_cast<cudaStream_t>(stream));
-  } else if (eos->type == SGX_HELMHOLTZ) {
-    e = sgx::launch_helm_fill(a, reinterpret_cast<cudaStream_t>(stream));
   } else {
     e = sgx::launch_fill_fp64(a, reinterpret_cast<cudaStream_t>(stream));
   }

@@ -141,6 +141,10 @@ __device__ __forceinline__ void store_fill(const FillArgs &a, const long long i,
   if ((a.output & Q_BMOD) && a.bmod) a.bmod[i] = bmod;
 }
 
+// MIXED: the Newton iteration starts from the FP32 phase's root (newton_e32,
+// FP32 e(T) to 1e-6) instead of the reference's guess, so the FP64 steps
+// that follow are the reference's last one or two.
+template <bool MIXED>
 __global__ void __launch_bounds__(HELM_BLOCK) helm_invert_pass1(const FillArgs a, HelmQueue q) {
   using namespace helm;
   __shared__ HelmTable st;
@@ -156,6 +160,10 @@ __global__ void __launch_bounds__(HELM_BLOCK) helm_invert_pass1(const FillArgs a
     double *lam = a.lambda + i * a.lambda_stride;
     const Cell c = cell(rho, lam[0], lam[1]);
     Inversion v = inversion_begin(st, opt, c, sie, lam);
+    if (MIXED) {
+      double x32 = v.x;
+      if (newton_e32(st, opt, cell32(c), sie, v.Ta, v.Tb, x32)) v.x = x32;
+    }
     const bool done =
         newton_e_steps(st, opt, c, sie, v.Ta, v.Tb, HELM_EOS_EPS, v.x, v.iter, HELM_PASS1_ITERS);
     if (!done) {
@@ -246,7 +254,7 @@ cudaError_t launch_helm_eval(const EvalArgs &a, cudaStream_t stream) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_helm_fill(const FillArgs &a, cudaStream_t stream) {
+cudaError_t launch_helm_fill(const FillArgs &a, cudaStream_t stream, const bool mixed) {
   if (a.n <= 0) return cudaSuccess;
   const int opt = a.eos.flags;
   const bool iterate = (opt & HELM_RAD) || (opt & HELM_ELE) || (opt & HELM_COUL);
@@ -273,7 +281,10 @@ cudaError_t launch_helm_fill(const FillArgs &a, cudaStream_t stream) {
   q.id_rf = reinterpret_cast<int *>(p + 256 + xs + 2 * ids);
   e = cudaMemsetAsync(p, 0, 256, stream);
   if (e == cudaSuccess) {
-    helm_invert_pass1<<<helm_grid(a.n), HELM_BLOCK, 0, stream>>>(a, q);
+    if (mixed)
+      helm_invert_pass1<true><<<helm_grid(a.n), HELM_BLOCK, 0, stream>>>(a, q);
+    else
+      helm_invert_pass1<false><<<helm_grid(a.n), HELM_BLOCK, 0, stream>>>(a, q);
     int dev = 0, sms = 152;
     if (cudaGetDevice(&dev) == cudaSuccess)
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

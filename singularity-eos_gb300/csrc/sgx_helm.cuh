@@ -38,6 +38,12 @@ enum : int {
 
 struct HelmTable {
   const double *cells; // [HELM_NT - 1][HELM_NRHO - 1][HELM_REC]
+  // FP32 copy of each cell's biquintic free-energy coefficients in the
+  // cell's normalised coordinates ([HELM_NT - 1][HELM_NRHO - 1][36], the
+  // 6 x 6 products of T and density Hermite weights, T-major), for the
+  // FP32 Newton phase of the mixed-precision inversion; null when a
+  // coefficient lies outside the float range
+  const float *cells32;
   const double *rho;   // [HELM_NRHO] node densities 10^lRho
   const double *T;     // [HELM_NT] node temperatures 10^lT
   // RegularGrid1D of lRho (range(0)) and lT (range(1))
@@ -105,6 +111,16 @@ SGX_HDI double xpsi0(double z) { return z * z * (2.0 * z - 3.0) + 1.0; }
 SGX_HDI double xdpsi0(double z) { return z * (6.0 * z - 6.0); }
 SGX_HDI double xpsi1(double z) { return z * (z * (z - 2.0) + 1.0); }
 SGX_HDI double xdpsi1(double z) { return z * (3.0 * z - 4.0) + 1.0; }
+
+// The density and T weight of each of the 36 biquintic terms, in the
+// reference's order (hermite.hpp h5): (d0,t0) (d0m,t0) (d0,t0m) (d0m,t0m)
+// then t1, t2 with d0; then d1, d2 with t0; d1, d2 with t1; d1, d2 with t2.
+// Weight index: 0 psi0(x), 1 psi0(1-x), 2 psi1(x) dx, 3 -psi1(1-x) dx,
+// 4 psi2(x) dx^2, 5 psi2(1-x) dx^2.
+constexpr int H5_DI[36] = {0, 1, 0, 1, 0, 1, 0, 1, 0, 1, 0, 1, 2, 3, 2, 3, 4, 5,
+                           4, 5, 2, 3, 2, 3, 4, 5, 4, 5, 2, 3, 2, 3, 4, 5, 4, 5};
+constexpr int H5_TI[36] = {0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 0, 0, 1, 1, 0, 0,
+                           1, 1, 2, 2, 3, 3, 2, 2, 3, 3, 4, 4, 5, 5, 4, 4, 5, 5};
 
 // Biquintic sum over the 36 coefficients (hermite.hpp h5), left to right.
 SGX_HDI double h5(const double *fi, double w0t, double w1t, double w2t, double w0mt,
@@ -667,6 +683,185 @@ SGX_HDN double lT_from_rho_sie(const HelmTable &t, const int opt, const Cell &c,
   if (v.iterate && v.newton)
     done = newton_e_steps(t, opt, c, e, v.Ta, v.Tb, HELM_EOS_EPS, v.x, v.iter, NEWTON_MAX_ITER);
   return inversion_end(t, opt, c, v, done, lam);
+}
+
+// ---------------------------------------------------------------------------
+// FP32 e(T) for the Newton phase of the mixed-precision inversion: the same
+// components as evaluate(..., only_e) -- radiation, ions, the tabulated
+// electrons and the Coulomb correction with its filter -- in float, with
+// the electron free energy from the normalised FP32 coefficients. Only the
+// root's neighbourhood matters here: the FP64 Newton iteration of the
+// reference finishes from this phase's T. Returns false when a value left
+// the float range (the FP64 iteration then starts from the reference's own
+// guess).
+// ---------------------------------------------------------------------------
+SGX_HDI float fpsi0(float z) { return z * z * z * (z * (-6.0f * z + 15.0f) - 10.0f) + 1.0f; }
+SGX_HDI float fdpsi0(float z) { return z * z * (z * (-30.0f * z + 60.0f) - 30.0f); }
+SGX_HDI float fddpsi0(float z) { return z * (z * (-120.0f * z + 180.0f) - 60.0f); }
+SGX_HDI float fpsi1(float z) { return z * (z * z * (z * (-3.0f * z + 8.0f) - 6.0f) + 1.0f); }
+SGX_HDI float fdpsi1(float z) { return z * z * (z * (-15.0f * z + 32.0f) - 18.0f) + 1.0f; }
+SGX_HDI float fddpsi1(float z) { return z * (z * (-60.0f * z + 96.0f) - 36.0f); }
+SGX_HDI float fpsi2(float z) { return 0.5f * z * z * (z * (z * (-z + 3.0f) - 3.0f) + 1.0f); }
+SGX_HDI float fdpsi2(float z) { return 0.5f * z * (z * (z * (-5.0f * z + 12.0f) - 9.0f) + 2.0f); }
+SGX_HDI float fddpsi2(float z) { return 0.5f * (z * (z * (-20.0f * z + 36.0f) - 18.0f) + 2.0f); }
+
+// Per-cell constants of the FP32 phase.
+struct Cell32 {
+  float rho, De, lDe, ye, ytot, ytot_ion, abar, zbar, lrho;
+};
+SGX_HDI Cell32 cell32(const Cell &c) {
+  Cell32 f;
+  f.rho = static_cast<float>(c.rho);
+  f.De = static_cast<float>(c.De);
+  f.lDe = static_cast<float>(c.lDe);
+  f.ye = static_cast<float>(c.ye);
+  f.ytot = static_cast<float>(c.ytot);
+  f.ytot_ion = static_cast<float>(ratio(c.zbar + 1.0, c.abar));
+  f.abar = static_cast<float>(c.abar);
+  f.zbar = static_cast<float>(c.zbar);
+  f.lrho = log10f(f.rho);
+  return f;
+}
+
+__device__ __forceinline__ bool e_of_T32(const HelmTable &t, const int opt, const Cell32 &c,
+                                         const float T, float &e, float &dedT) {
+  e = 0.0f;
+  dedT = 0.0f;
+  const float lT = log10f(T);
+  if (opt & HELM_RAD) {
+    // 3 a/3 T^4 / rho, with T scaled by 1e-4 to stay inside the float range
+    constexpr float c3 = static_cast<float>(3.0 * RAD_PREFACTOR * 1e16);
+    const float s = T * 1e-4f, s3 = s * s * s;
+    e += c3 * s3 * s / c.rho;
+    dedT += 4.0f * c3 * s3 * 1e-4f / c.rho;
+  }
+  if (opt & HELM_GAS) {
+    const bool ionized = (opt & HELM_ION) != 0, degenerate = (opt & HELM_ELE) != 0;
+    const float y = ((ionized && degenerate) || !ionized) ? c.ytot : c.ytot_ion;
+    constexpr float k15 = static_cast<float>(1.5 * KBNA);
+    e += k15 * y * T;
+    dedT += k15 * y;
+    if (degenerate) {
+      if (!t.cells32) return false;
+      const float De = fminf(static_cast<float>(t.rhoMax), fmaxf(static_cast<float>(t.rhoMin), c.De));
+      const float lDe = fminf(static_cast<float>(t.lRhoMax),
+                              fmaxf(static_cast<float>(t.lRhoMin), c.lDe));
+      float u = (lDe - static_cast<float>(t.lRhoMin)) * static_cast<float>(t.inv_dlRho);
+      const int iat = !(u >= 0.0f) ? 0 : (u > HELM_NRHO - 2 ? HELM_NRHO - 2 : static_cast<int>(u));
+      u = (lT - static_cast<float>(t.lTMin)) * static_cast<float>(t.inv_dlT);
+      const int jat = !(u >= 0.0f) ? 0 : (u > HELM_NT - 2 ? HELM_NT - 2 : static_cast<int>(u));
+      const float Tj = static_cast<float>(t.T[jat]);
+      const float dth = static_cast<float>(t.T[jat + 1]) - Tj;
+      const float ri = static_cast<float>(t.rho[iat]);
+      const float dd = static_cast<float>(t.rho[iat + 1]) - ri;
+      const float xt = fmaxf(0.0f, (T - Tj) / dth), xd = fmaxf(0.0f, (De - ri) / dd);
+      const float mxt = 1.0f - xt, mxd = 1.0f - xd;
+      const float wd[6] = {fpsi0(xd), fpsi0(mxd), fpsi1(xd), fpsi1(mxd), fpsi2(xd), fpsi2(mxd)};
+      const float wt[6] = {fpsi0(xt), fpsi0(mxt), fpsi1(xt), fpsi1(mxt), fpsi2(xt), fpsi2(mxt)};
+      const float w1[6] = {fdpsi0(xt), -fdpsi0(mxt), fdpsi1(xt), -fdpsi1(mxt), fdpsi2(xt),
+                           -fdpsi2(mxt)};
+      const float w2[6] = {fddpsi0(xt), fddpsi0(mxt), fddpsi1(xt), fddpsi1(mxt), fddpsi2(xt),
+                           fddpsi2(mxt)};
+      // the cell's 6 x 6 coefficients (T weight major), 9 aligned 16-byte loads
+      const float4 *c4 = reinterpret_cast<const float4 *>(
+          t.cells32 + (static_cast<long long>(jat) * (HELM_NRHO - 1) + iat) * 36);
+      float C[36];
+#pragma unroll
+      for (int q = 0; q < 9; ++q) {
+        const float4 v = __ldg(c4 + q);
+        C[4 * q] = v.x;
+        C[4 * q + 1] = v.y;
+        C[4 * q + 2] = v.z;
+        C[4 * q + 3] = v.w;
+      }
+      // F and its first two xt derivatives: each T row summed over the
+      // density weights first
+      float F = 0.0f, Fx = 0.0f, Fxx = 0.0f;
+#pragma unroll
+      for (int ti = 0; ti < 6; ++ti) {
+        float ut = 0.0f;
+#pragma unroll
+        for (int di = 0; di < 6; ++di)
+          ut = fmaf(C[ti * 6 + di], wd[di], ut);
+        F = fmaf(ut, wt[ti], F);
+        Fx = fmaf(ut, w1[ti], Fx);
+        Fxx = fmaf(ut, w2[ti], Fxx);
+      }
+      const float dti = 1.0f / dth;
+      e += c.ye * (F - T * Fx * dti);
+      dedT += -c.ye * T * Fxx * dti * dti;
+    }
+    if (degenerate && (opt & HELM_COUL)) {
+      // HelmCoulomb (:1369-1504), energy and its T derivative
+      constexpr float a1 = -0.898004f, b1 = 0.96786f, c1 = 0.220703f, d1 = -0.86097f;
+      constexpr float a2 = 0.29561f, b2 = 1.9885f, c2 = 0.288675f;
+      const float xni = static_cast<float>(NA) * c.ytot * c.rho;
+      const float kbT = static_cast<float>(KB) * T;
+      const float s = static_cast<float>(4.0 / 3.0 * PI) * xni;
+      const float lami = 1.0f / cbrtf(s);
+      const float ez = static_cast<float>(ELECTRON_CHARGE_ESU) * c.zbar;
+      const float plasg = ez * ez / (kbT * lami);
+      const float plasgdt = -plasg / T;
+      float ec, ecdt;
+      if (plasg >= 0.0f) {
+        const float x = sqrtf(sqrtf(plasg));
+        const float y = static_cast<float>(KBNA) * c.ytot;
+        const float c1x = c1 / x;
+        ec = y * T * (a1 * plasg + b1 * x + c1x + d1);
+        const float y2 = static_cast<float>(KBNA) * T * c.ytot * (a1 + 0.25f / plasg * (b1 * x - c1x));
+        ecdt = y2 * plasgdt + ec / T;
+      } else {
+        const float x = plasg * sqrtf(fabsf(plasg));
+        const float y = powf(plasg, b2);
+        const float z = c2 * x - a2 * y / 3.0f;
+        const float pion = xni * kbT;
+        const float ss = 1.5f * c2 * x / plasg - a2 * b2 * y / (3.0f * plasg);
+        ec = 3.0f * (-pion * z) / c.rho;
+        ecdt = 3.0f * (-xni * static_cast<float>(KB) * z - pion * ss * plasgdt) / c.rho;
+      }
+      // the Butterworth filters (the reference takes the T derivative of the
+      // gain from the density filter's derivative; kept)
+      const float fr = (lT - 4.5f) / 3.0f, ft = (c.lrho + 1.0f) / 6.0f;
+      const float fr2 = fr * fr, ft2 = ft * ft;
+      const float fr8 = fr2 * fr2 * fr2 * fr2, ft8 = ft2 * ft2 * ft2 * ft2;
+      const float fr24 = fr8 * fr8 * fr8, ft24 = ft8 * ft8 * ft8;
+      const float g_r = 1.0f / (1.0f + fr24), g_t = 1.0f / (1.0f + ft24);
+      // dg/df = -24 g^2 f^23 / c^24 for the density filter (c = 6)
+      const float ft23 = ft24 / ft;
+      const float dgdf_t = (ft != 0.0f) ? -g_t * g_t * 24.0f * ft23 / 6.0f : 0.0f;
+      const float gain = 1.0f - g_t * g_r;
+      const float dgaindt = -(g_r * dgdf_t) / (T * static_cast<float>(LN10));
+      const float ecg = ec * gain;
+      e += ecg;
+      dedT += gain * ecdt + ecg * dgaindt / gain;
+    }
+  }
+  return isfinite(e) && isfinite(dedT) && dedT != 0.0f;
+}
+
+// The FP32 Newton phase: newton_e_steps in float from the reference's guess
+// to |e - target| < 1e-6 |target| (at most 40 steps, the same bound handling).
+// true with x set when it got there.
+__device__ __forceinline__ bool newton_e32(const HelmTable &t, const int opt, const Cell32 &c,
+                                           const double target, const double a, const double b,
+                                           double &x) {
+  const float tg = static_cast<float>(target), fa = static_cast<float>(a),
+              fb = static_cast<float>(b);
+  float xf = static_cast<float>(x);
+  for (int it = 0; it < 40; ++it) {
+    float ev, de;
+    if (!e_of_T32(t, opt, c, xf, ev, de)) return false;
+    if (fabsf(ev - tg) < 1e-6f * fabsf(tg)) {
+      x = static_cast<double>(xf);
+      return true;
+    }
+    const float xold = xf;
+    xf = xf - (ev - tg) / de;
+    if ((xf <= fa && xold <= fa) || (xf >= fb && xold >= fb)) return false;
+    xf = fmaxf(fminf(xf, fb), fa);
+    if (!isfinite(xf)) return false;
+  }
+  return false;
 }
 
 } // namespace helm

@@ -132,6 +132,8 @@ cudaError_t launch_fill_mixed(const FillArgs &a, cudaStream_t stream);
 cudaError_t launch_fill_ref(const FillArgs &a, const unsigned *left, cudaStream_t stream);
 // Helmholtz vector lookups and FillEos (lambda rows [Abar, Zbar, lT]).
 cudaError_t launch_helm_eval(const EvalArgs &a, cudaStream_t stream);
-cudaError_t launch_helm_fill(const FillArgs &a, cudaStream_t stream);
+// mixed: the inversion's Newton iteration starts from an FP32 Newton phase
+// (T(rho, sie) outputs only; everything else is the FP64 path).
+cudaError_t launch_helm_fill(const FillArgs &a, cudaStream_t stream, bool mixed = false);
 
 } // namespace sgx

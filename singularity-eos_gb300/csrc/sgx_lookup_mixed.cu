@@ -360,11 +360,23 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
         }
       }
       if (fast) {
-        // 3. bracketing cell in FP32: first among every coarse_stride-th
-        //    node (shared memory), then within that stretch
+        // 3. bracketing cell in FP32: with the thermal bin index, between the
+        //    two density rows' cells for the blended thermal target sie -
+        //    sieCold (one or two cells apart); otherwise first among every
+        //    coarse_stride-th node (shared memory), then within that stretch
         const fq4 *row32 = t.sie4f + static_cast<long long>(j) * nc;
         int lo = 0, hi = nc - 1;
-        if (staged) {
+        if (t.therm_idx) {
+          const float ep = ef - sc0;
+          int k = ep > 0.0f ? static_cast<int>(__float_as_uint(ep) >> t.therm_shift) - t.therm_base
+                            : 0;
+          k = k < 0 ? 0 : (k >= t.therm_bins ? t.therm_bins - 1 : k);
+          const uint16_t *ti = t.therm_idx + static_cast<long long>(j) * t.therm_bins + k;
+          const int c0 = __ldg(ti), c1 = __ldg(ti + t.therm_bins);
+          lo = c0 < c1 ? c0 : c1;
+          hi = (c0 < c1 ? c1 : c0) + 1;
+          hi = hi < nc - 1 ? hi : nc - 1;
+        } else if (staged) {
           const float2 *cr = s_coarse + j * CS;
           int kl = 0, kh = SP_COARSE - 1;
           while (kl < kh) {
@@ -516,8 +528,11 @@ cudaError_t launch_fill_mixed(const FillArgs &a, cudaStream_t stream) {
   const int nrho = table_nrho(a.eos.table);
   const size_t coarse =
       nrho > 1 ? static_cast<size_t>(nrho - 1) * SP_COARSE_ROW * sizeof(float2) : 0;
-  const int stage =
-      (coarse > 0 && coarse <= 40 * 1024) ? tune_get(SGX_TUNE_LOOKUP_STAGE) : 0;
+  // (the thermal bin index, where the table has one, replaces the staged
+  // coarse index)
+  const int stage = (coarse > 0 && coarse <= 40 * 1024 && !table_has_thermal_index(a.eos.table))
+                        ? tune_get(SGX_TUNE_LOOKUP_STAGE)
+                        : 0;
   // the left-over mask, one bit per element
   const size_t words = static_cast<size_t>((a.n + 31) >> 5);
   void *left = nullptr;

@@ -161,3 +161,107 @@ extern "C" int sgx_tune_autotune_fill(const sgx_eos *eos, int64_t n, double *rho
   if (stage) *stage = best_s;
   return SGX_OK;
 }
+
+// The autotuner of the mixed PTE launch: every combination of the pass-1
+// block size (32, 64, 128 threads), the order of the material counts and,
+// when allowed, the material count from which pass 1 runs a lane group per
+// cell, timed on the caller's own batch through sgx_pte_solve. The caller's
+// starting state is kept in a device copy and restored before every trial,
+// so each trial solves the same problem and the arrays end holding the
+// solve of the winning setting.
+extern "C" int sgx_tune_autotune_pte(int nmat, int64_t ncell, const sgx_eos *eos_list, int neos,
+                                     const int32_t *eos_idx, const double *vfrac_tot,
+                                     const double *sie_tot, double *rho, double *vfrac,
+                                     double *sie, double *temp, double *press, double *lambda,
+                                     const sgx_mix_params *params, sgx_pte_status *status,
+                                     int reps, int tune_group, int *chosen,
+                                     sgx_stream_t stream) {
+  using namespace sgx;
+  static const char *who = "sgx_tune_autotune_pte";
+  if (nmat < 1 || ncell <= 0 || reps < 1 || reps > 100 || !rho || !vfrac || !sie || !temp ||
+      !press)
+    return set_error(SGX_ERR_INVALID, std::string(who) + ": bad arguments");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const size_t arr = static_cast<size_t>(nmat) * static_cast<size_t>(ncell) * sizeof(double);
+  const size_t lam_bytes = lambda ? 3 * arr : 0;
+  double *io[5] = {rho, vfrac, sie, temp, press};
+  void *keep = nullptr;
+  cudaError_t ce = scratch_alloc(&keep, 5 * arr + lam_bytes, s);
+  if (ce != cudaSuccess) return set_error(SGX_ERR_CUDA, std::string(who) + ": scratch");
+  char *kp = static_cast<char *>(keep);
+  for (int k = 0; k < 5 && ce == cudaSuccess; ++k)
+    ce = cudaMemcpyAsync(kp + k * arr, io[k], arr, cudaMemcpyDeviceToDevice, s);
+  if (ce == cudaSuccess && lambda)
+    ce = cudaMemcpyAsync(kp + 5 * arr, lambda, lam_bytes, cudaMemcpyDeviceToDevice, s);
+  auto restore = [&]() {
+    cudaError_t r = cudaSuccess;
+    for (int k = 0; k < 5 && r == cudaSuccess; ++k)
+      r = cudaMemcpyAsync(io[k], kp + k * arr, arr, cudaMemcpyDeviceToDevice, s);
+    if (r == cudaSuccess && lambda)
+      r = cudaMemcpyAsync(lambda, kp + 5 * arr, lam_bytes, cudaMemcpyDeviceToDevice, s);
+    return r;
+  };
+  const int keep_b = g_knobs[SGX_TUNE_PTE_MIXED_BLOCK].value.load();
+  const int keep_o = g_knobs[SGX_TUNE_PTE_COUNT_ORDER].value.load();
+  const int keep_g = g_knobs[SGX_TUNE_PTE_GROUP_MIN_N].value.load();
+  const int blocks[3] = {32, 64, 128};
+  const int groups[4] = {keep_g, 2, 4, 7};
+  const int ng = tune_group ? 4 : 1;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+  float best = 0.0f;
+  int best_b = keep_b, best_o = keep_o, best_g = keep_g, rc = SGX_OK;
+  for (int gi = 0; gi < ng; ++gi)
+    for (int bi = 0; bi < 3; ++bi)
+      for (int o = 0; o < 2 && ce == cudaSuccess && rc == SGX_OK; ++o) {
+        g_knobs[SGX_TUNE_PTE_MIXED_BLOCK].value.store(blocks[bi]);
+        g_knobs[SGX_TUNE_PTE_COUNT_ORDER].value.store(o);
+        g_knobs[SGX_TUNE_PTE_GROUP_MIN_N].value.store(groups[gi]);
+        float total = 0.0f;
+        for (int r = 0; r <= reps && ce == cudaSuccess && rc == SGX_OK; ++r) {
+          ce = restore();
+          if (ce == cudaSuccess) ce = cudaEventRecord(e0, s);
+          if (ce == cudaSuccess)
+            rc = sgx_pte_solve(SGX_PTE_RHOT, nmat, ncell, eos_list, neos, eos_idx, vfrac_tot,
+                               sie_tot, rho, vfrac, sie, temp, press, lambda, params, status,
+                               SGX_PREC_MIXED, stream);
+          if (rc == SGX_OK && ce == cudaSuccess) ce = cudaEventRecord(e1, s);
+          if (rc == SGX_OK && ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+          float ms = 0.0f;
+          if (rc == SGX_OK && ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
+          if (r > 0) total += ms; // the first run of a setting is untimed
+        }
+        if (rc == SGX_OK && ce == cudaSuccess && (best == 0.0f || total < best)) {
+          best = total;
+          best_b = blocks[bi];
+          best_o = o;
+          best_g = groups[gi];
+        }
+      }
+  const bool ok = rc == SGX_OK && ce == cudaSuccess;
+  g_knobs[SGX_TUNE_PTE_MIXED_BLOCK].value.store(ok ? best_b : keep_b);
+  g_knobs[SGX_TUNE_PTE_COUNT_ORDER].value.store(ok ? best_o : keep_o);
+  g_knobs[SGX_TUNE_PTE_GROUP_MIN_N].value.store(ok ? best_g : keep_g);
+  // leave the arrays holding the winner's solve
+  if (ok) {
+    ce = restore();
+    if (ce == cudaSuccess)
+      rc = sgx_pte_solve(SGX_PTE_RHOT, nmat, ncell, eos_list, neos, eos_idx, vfrac_tot, sie_tot,
+                         rho, vfrac, sie, temp, press, lambda, params, status, SGX_PREC_MIXED,
+                         stream);
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  const cudaError_t f = scratch_free(keep, s);
+  if (ce == cudaSuccess) ce = f;
+  if (rc != SGX_OK) return rc;
+  if (ce != cudaSuccess)
+    return set_error(SGX_ERR_CUDA, std::string(who) + ": " + cudaGetErrorString(ce));
+  if (chosen) {
+    chosen[0] = best_b;
+    chosen[1] = best_o;
+    chosen[2] = best_g;
+  }
+  return SGX_OK;
+}

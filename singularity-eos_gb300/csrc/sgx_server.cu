@@ -1,20 +1,26 @@
-// The serving loop (include/sgx.h, "Serving"): a worker thread that admits
-// PTE closure requests into CUDA-stream slots under a device-memory budget
-// and overlaps their copies and solves on the device.
+// The serving loop (include/sgx.h, "Serving"): a worker thread that folds
+// the PTE closure requests waiting at each admission tick into one merged
+// solve on the device, under a device-memory budget, with several merged
+// batches in flight.
 //
-// Memory: one cudaMalloc of hbm_budget_bytes at creation, carved per request
+// Memory: one cudaMalloc of hbm_budget_bytes at creation, carved per batch
 // by a first-fit free list (256-byte granules, neighbours coalesced on
-// free). A request's block holds its arrays and, for the mixed solver, the
-// scratch that sgx_pte_solve would otherwise take from the stream-ordered
-// pool (launch_pte_mixed_with), so nothing is allocated per request.
+// free). A batch's block holds the merged arrays of its requests and the
+// solver's scratch (what sgx_pte_solve would take from the stream-ordered
+// pool), so nothing is allocated per request or per batch.
 //
-// Scheduling: strict arrival order. The head of the queue is admitted when a
-// slot is idle and its block fits; a request that does not fit waits for
-// blocks to be freed (no overtaking, so no starvation of large requests).
-// An admitted request's host->device copies, solve and device->host copies
-// are issued on its slot's stream, followed by an event; the worker polls
-// the events, releases the block and the slot of each finished request and
-// wakes its waiters. The GPU runs the slots' work concurrently.
+// Folding: when a batch slot is free, the worker takes queued requests in
+// arrival order while their merged layout still fits the largest free block
+// (and stays under SERVE_BATCH_CELLS cells), lays them out one after the
+// other along the cell axis ([nmax][sum of cells], each request's cells
+// contiguous; material slots a request does not use are marked absent),
+// copies every request's inputs into place, runs ONE binned solve over the
+// whole batch, and copies each request's rows back to its own output arrays.
+// Every cell is solved independently of the others, so each result is the
+// one a solve of that request alone gives, bit for bit. A request that does
+// not fit waits at the head of the queue (no overtaking, so no starvation of
+// large requests). Batches in flight overlap: the next batch's copies and
+// solve run while the previous one is still on the device.
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -87,6 +93,13 @@ class Arena {
       }
     }
   }
+  // The largest block alloc() can return now.
+  size_t largest() const {
+    size_t m = 0;
+    for (const auto &f : free_)
+      m = f.second > m ? f.second : m;
+    return m;
+  }
   char *base() const { return base_; }
   size_t cap() const { return cap_; }
   size_t used() const { return used_; }
@@ -98,14 +111,15 @@ class Arena {
   std::map<size_t, size_t> free_;
 };
 
-// Offsets of one request's arrays inside its arena block.
+// Offsets of a batch's merged arrays inside its arena block: nmat material
+// slots by ncell cells (the cells of every request of the batch).
 struct Layout {
   size_t idx, vt, st, mat[5], status, bins, retry, perm, total;
-  Layout(const sgx_pte_request &r, const bool mixed) {
-    const size_t n = static_cast<size_t>(r.ncell), m = static_cast<size_t>(r.nmat);
+  Layout(const int nmat, const int64_t ncell, const bool mixed) {
+    const size_t n = static_cast<size_t>(ncell), m = static_cast<size_t>(nmat);
     size_t o = 0;
     idx = o;
-    o += r.eos_idx ? up(4 * n * m) : 0;
+    o += up(4 * n * m);
     vt = o;
     o += up(8 * n);
     st = o;
@@ -116,33 +130,52 @@ struct Layout {
     }
     status = o;
     o += up(sizeof(sgx_pte_status) * n);
-    bins = retry = perm = o;
-    if (mixed || r.eos_idx) {
-      o += up(PTE_BINS_BYTES); // counters and the signature histogram
-      retry = o;
-      o += mixed ? up(4 * n) : 0;
-      perm = o;
-      o += r.eos_idx ? up(4 * n) : 0;
-    }
+    bins = o;
+    o += up(PTE_BINS_BYTES); // counters and the signature histogram
+    retry = o;
+    o += mixed ? up(4 * n) : 0;
+    perm = o;
+    o += up(4 * n);
     total = o;
   }
 };
 
+// Cells per merged batch at most (bounds the time a request waits behind the
+// batch it lands in).
+constexpr int64_t SERVE_BATCH_CELLS = int64_t(1) << 22;
+
+// The material-slot rows of one request inside a merged batch: eos_idx
+// rows [0, nmat_r) take the request's own indices (or, with none, the slot
+// number), rows [nmat_r, nmat) are absent (-1).
+__global__ void serve_fill_idx(int32_t *idx, const int64_t N, const int64_t off,
+                               const int64_t n, const int nmat_r, const int nmat,
+                               const bool own) {
+  const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  for (int m = own ? nmat_r : 0; m < nmat; ++m)
+    idx[m * N + off + i] = m < nmat_r ? m : -1;
+}
+
 struct Request {
   uint64_t ticket = 0;
   sgx_pte_request r{};
-  size_t bytes = 0, off = 0;
-  int slot = -1;
+  size_t bytes = 0; // the request's layout alone (admission check at submit)
+  int64_t cell_off = 0; // first cell inside its batch
   int state = 0; // 0 queued, 3 being issued, 1 running, 2 finished
   int err = SGX_OK;
   std::string msg;
   Clock::time_point t_submit, t_done;
 };
 
+// One merged batch in flight.
 struct Slot {
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
-  Request *req = nullptr;
+  std::vector<Request *> reqs; // empty: the slot is free
+  int nmat = 0;
+  int64_t ncell = 0;
+  size_t off = 0, bytes = 0;
+  int state = 0; // 3 being issued, 1 running
 };
 
 } // namespace
@@ -161,106 +194,168 @@ struct Server {
   std::unordered_map<uint64_t, std::unique_ptr<Request>> requests;
   uint64_t next_ticket = 1;
   bool stop = false;
-  uint64_t submitted = 0, completed = 0, failed = 0, cells_completed = 0;
+  uint64_t submitted = 0, completed = 0, failed = 0, cells_completed = 0, batches = 0;
   std::thread worker;
 
   bool mixed() const { return precision == SGX_PREC_MIXED; }
 
-  // Issues the copies, the solve and the copies back of q on slot k, then
-  // records the slot's event. Called by the worker without the lock (with
-  // pageable host arrays the device-to-host copies block); returns the first
-  // CUDA error, after which nothing reliable is in flight on the stream.
-  cudaError_t issue(Request *q, const int k) {
+  // Issues the batch of slot k: the requests' inputs copied into their
+  // places in the merged arrays, one solve of the whole batch, each
+  // request's results copied back, then the slot's event. Called by the
+  // worker without the lock (with pageable host arrays the device-to-host
+  // copies block); returns the first CUDA error, after which nothing
+  // reliable is in flight on the stream.
+  cudaError_t issue(const int k) {
     Slot &sl = slots[k];
-    const sgx_pte_request &r = q->r;
-    const Layout L(r, mixed());
-    char *b = arena.base() + q->off;
-    const size_t n = static_cast<size_t>(r.ncell), nm = n * static_cast<size_t>(r.nmat);
+    const Layout L(sl.nmat, sl.ncell, mixed());
+    char *b = arena.base() + sl.off;
+    const size_t N = static_cast<size_t>(sl.ncell);
     cudaStream_t s = sl.stream;
     cudaError_t e = cudaSuccess;
-    auto h2d = [&](size_t off, const void *src, size_t bytes) {
-      if (e == cudaSuccess) e = cudaMemcpyAsync(b + off, src, bytes, cudaMemcpyHostToDevice, s);
-    };
-    auto d2h = [&](void *dst, size_t off, size_t bytes) {
-      if (e == cudaSuccess && dst)
-        e = cudaMemcpyAsync(dst, b + off, bytes, cudaMemcpyDeviceToHost, s);
-    };
-    if (r.eos_idx) h2d(L.idx, r.eos_idx, 4 * nm);
-    h2d(L.vt, r.vfrac_tot, 8 * n);
-    h2d(L.st, r.sie_tot, 8 * n);
-    const double *in[5] = {r.rho_in, r.vfrac_in, r.sie_in, r.temp_in, r.press_in};
-    for (int m = 0; m < 5; ++m)
-      h2d(L.mat[m], in[m], 8 * nm);
-    PteArgs a;
-    std::memset(&a, 0, sizeof(a));
-    a.solver = solver;
-    a.nmat = r.nmat;
-    a.ncell = r.ncell;
-    a.neos = neos;
-    for (int i = 0; i < neos; ++i)
-      a.eos[i] = eos[i];
-    a.eos_idx = r.eos_idx ? reinterpret_cast<const int32_t *>(b + L.idx) : nullptr;
-    a.vfrac_tot = reinterpret_cast<const double *>(b + L.vt);
-    a.sie_tot = reinterpret_cast<const double *>(b + L.st);
+    int32_t *idx = reinterpret_cast<int32_t *>(b + L.idx);
     double *mat[5];
     for (int m = 0; m < 5; ++m)
       mat[m] = reinterpret_cast<double *>(b + L.mat[m]);
+    sgx_pte_status *status = reinterpret_cast<sgx_pte_status *>(b + L.status);
+    for (Request *q : sl.reqs) {
+      const sgx_pte_request &r = q->r;
+      const size_t n = static_cast<size_t>(r.ncell), o = static_cast<size_t>(q->cell_off);
+      auto h2d = [&](void *dst, const void *src, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+      };
+      for (int m = 0; m < r.nmat; ++m) {
+        if (r.eos_idx) h2d(idx + m * N + o, r.eos_idx + m * n, 4 * n);
+        const double *in[5] = {r.rho_in, r.vfrac_in, r.sie_in, r.temp_in, r.press_in};
+        for (int a = 0; a < 5; ++a)
+          h2d(mat[a] + m * N + o, in[a] + m * n, 8 * n);
+      }
+      h2d(reinterpret_cast<double *>(b + L.vt) + o, r.vfrac_tot, 8 * n);
+      h2d(reinterpret_cast<double *>(b + L.st) + o, r.sie_tot, 8 * n);
+      if (e == cudaSuccess && (!r.eos_idx || r.nmat < sl.nmat)) {
+        serve_fill_idx<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(
+            idx, sl.ncell, q->cell_off, r.ncell, r.nmat, sl.nmat, r.eos_idx != nullptr);
+        e = cudaGetLastError();
+      }
+    }
+    PteArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.solver = solver;
+    a.nmat = sl.nmat;
+    a.ncell = sl.ncell;
+    a.neos = neos;
+    for (int i = 0; i < neos; ++i)
+      a.eos[i] = eos[i];
+    a.eos_idx = idx;
+    a.vfrac_tot = reinterpret_cast<const double *>(b + L.vt);
+    a.sie_tot = reinterpret_cast<const double *>(b + L.st);
     a.rho = mat[0];
     a.vfrac = mat[1];
     a.sie = mat[2];
     a.temp = mat[3];
     a.press = mat[4];
     a.lambda = nullptr;
-    a.status = reinterpret_cast<sgx_pte_status *>(b + L.status);
+    a.status = status;
     a.params = params;
+    int *perm = reinterpret_cast<int *>(b + L.perm);
     if (e == cudaSuccess) {
       if (mixed()) {
         a.bins = reinterpret_cast<unsigned *>(b + L.bins);
         a.retry_idx = reinterpret_cast<int *>(b + L.retry);
-        e = launch_pte_mixed_with(a, r.eos_idx ? reinterpret_cast<int *>(b + L.perm) : nullptr,
-                                  s);
+        e = launch_pte_mixed_with(a, perm, s);
       } else {
-        e = launch_pte_fp64_with(a, reinterpret_cast<unsigned *>(b + L.bins),
-                                 r.eos_idx ? reinterpret_cast<int *>(b + L.perm) : nullptr, s);
+        e = launch_pte_fp64_with(a, reinterpret_cast<unsigned *>(b + L.bins), perm, s);
       }
     }
-    double *out[5] = {r.rho_out, r.vfrac_out, r.sie_out, r.temp_out, r.press_out};
-    for (int m = 0; m < 5; ++m)
-      d2h(out[m], L.mat[m], 8 * nm);
-    d2h(r.status, L.status, sizeof(sgx_pte_status) * n);
+    for (Request *q : sl.reqs) {
+      const sgx_pte_request &r = q->r;
+      const size_t n = static_cast<size_t>(r.ncell), o = static_cast<size_t>(q->cell_off);
+      auto d2h = [&](void *dst, const void *src, size_t bytes) {
+        if (e == cudaSuccess && dst)
+          e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s);
+      };
+      double *out[5] = {r.rho_out, r.vfrac_out, r.sie_out, r.temp_out, r.press_out};
+      for (int m = 0; m < r.nmat; ++m)
+        for (int a2 = 0; a2 < 5; ++a2)
+          d2h(out[a2] + m * n, mat[a2] + m * N + o, 8 * n);
+      d2h(r.status, status + o, sizeof(sgx_pte_status) * n);
+    }
     if (e == cudaSuccess) e = cudaEventRecord(sl.done, s);
     if (e != cudaSuccess) cudaStreamSynchronize(s);
     return e;
   }
 
+  // Releases slot k's block and completes its requests.
   void finish(const int k, const int err, const std::string &msg) {
     Slot &sl = slots[k];
-    Request *q = sl.req;
-    sl.req = nullptr;
-    arena.free(q->off, q->bytes);
-    q->err = err;
-    q->msg = msg;
-    q->state = 2;
-    q->t_done = Clock::now();
-    if (err == SGX_OK) {
-      ++completed;
-      cells_completed += static_cast<uint64_t>(q->r.ncell);
-    } else {
-      ++failed;
+    arena.free(sl.off, sl.bytes);
+    const auto now = Clock::now();
+    for (Request *q : sl.reqs) {
+      q->err = err;
+      q->msg = msg;
+      q->state = 2;
+      q->t_done = now;
+      if (err == SGX_OK) {
+        ++completed;
+        cells_completed += static_cast<uint64_t>(q->r.ncell);
+      } else {
+        ++failed;
+      }
     }
+    sl.reqs.clear();
+    sl.state = 0;
     cv_done.notify_all();
+  }
+
+  // Folds the head of the queue into a batch for slot k (with the lock
+  // held): requests in arrival order while the merged layout fits the
+  // largest free block and the cell cap. False when not even the head fits.
+  bool form_batch(const int k) {
+    Slot &sl = slots[k];
+    const size_t room = arena.largest();
+    int nmat = 0;
+    int64_t ncell = 0;
+    size_t bytes = 0;
+    size_t take = 0;
+    for (Request *q : queue) {
+      const int nm = nmat > q->r.nmat ? nmat : q->r.nmat;
+      const int64_t nc = ncell + q->r.ncell;
+      const size_t by = Layout(nm, nc, mixed()).total;
+      if (by > room || (take > 0 && nc > SERVE_BATCH_CELLS)) break;
+      nmat = nm;
+      ncell = nc;
+      bytes = by;
+      ++take;
+    }
+    if (take == 0) return false;
+    sl.off = arena.alloc(bytes);
+    if (sl.off == SIZE_MAX) return false;
+    sl.bytes = bytes;
+    sl.nmat = nmat;
+    sl.ncell = ncell;
+    int64_t off = 0;
+    for (size_t i = 0; i < take; ++i) {
+      Request *q = queue.front();
+      queue.pop_front();
+      q->cell_off = off;
+      off += q->r.ncell;
+      q->state = 3;
+      sl.reqs.push_back(q);
+    }
+    sl.state = 3; // being issued
+    ++batches;
+    return true;
   }
 
   void run() {
     cudaSetDevice(device);
     for (;;) {
-      std::vector<std::pair<Request *, int>> admitted;
+      std::vector<int> admitted;
       bool progress = false;
       {
         std::unique_lock<std::mutex> lk(mu);
         int inflight = 0;
         for (int k = 0; k < static_cast<int>(slots.size()); ++k) {
-          if (!slots[k].req || slots[k].req->state != 1) continue;
+          if (slots[k].reqs.empty() || slots[k].state != 1) continue;
           const cudaError_t e = cudaEventQuery(slots[k].done);
           if (e == cudaSuccess) {
             finish(k, SGX_OK, "");
@@ -273,29 +368,22 @@ struct Server {
           }
         }
         for (int k = 0; k < static_cast<int>(slots.size()) && !queue.empty(); ++k) {
-          if (slots[k].req) continue;
-          Request *q = queue.front();
-          const size_t off = arena.alloc(q->bytes);
-          if (off == SIZE_MAX) break; // the head waits for memory
-          queue.pop_front();
-          q->off = off;
-          q->slot = k;
-          q->state = 3; // being issued
-          slots[k].req = q;
-          admitted.emplace_back(q, k);
+          if (!slots[k].reqs.empty()) continue;
+          if (!form_batch(k)) break; // the head waits for memory
+          admitted.push_back(k);
           ++inflight;
         }
         if (stop && queue.empty() && inflight == 0) break;
         if (admitted.empty() && !progress)
           cv_work.wait_for(lk, std::chrono::microseconds(inflight ? 20 : 2000));
       }
-      for (auto &qk : admitted) {
-        const cudaError_t e = issue(qk.first, qk.second);
+      for (const int k : admitted) {
+        const cudaError_t e = issue(k);
         std::lock_guard<std::mutex> lk(mu);
         if (e == cudaSuccess)
-          qk.first->state = 1;
+          slots[k].state = 1;
         else
-          finish(qk.second, SGX_ERR_CUDA, std::string("sgx_server: ") + cudaGetErrorString(e));
+          finish(k, SGX_ERR_CUDA, std::string("sgx_server: ") + cudaGetErrorString(e));
       }
     }
   }
@@ -386,7 +474,7 @@ int sgx_server_submit(sgx_server *h, const sgx_pte_request *req, uint64_t *ticke
     return set_error(SGX_ERR_INVALID, "sgx_server_submit: eos_idx NULL needs neos >= nmat");
   auto q = std::make_unique<sgx::Request>();
   q->r = r;
-  q->bytes = sgx::Layout(r, s.mixed()).total;
+  q->bytes = sgx::Layout(r.nmat, r.ncell, s.mixed()).total;
   if (q->bytes > s.arena.cap())
     return set_error(SGX_ERR_INVALID, "sgx_server_submit: request needs " +
                                           std::to_string(q->bytes) +
@@ -436,8 +524,9 @@ int sgx_server_stats_get(sgx_server *h, sgx_server_stats *out) {
   out->cells_completed = s.cells_completed;
   int inflight = 0;
   for (auto &sl : s.slots)
-    inflight += sl.req ? 1 : 0;
+    inflight += static_cast<int>(sl.reqs.size());
   out->inflight = inflight;
+  out->batches = s.batches;
   out->queued = static_cast<int>(s.queue.size());
   out->arena_used = s.arena.used();
   out->arena_peak = s.arena.peak();

@@ -98,6 +98,15 @@ struct SpinerTable {
   const float2 *sieCoarse;
   int coarse_stride;
   int ff_ok;
+  // Thermal-energy bin index of each density row (null when the table does
+  // not allow one): for the thermal part t_r(i) = sie(r, i) - sieCold(r),
+  // bins log-spaced by the float bit pattern (bin = (bits(t) >> therm_shift)
+  // - therm_base, therm_bins of them, finer than the T cells), therm_idx[r *
+  // therm_bins + k] is the last T cell whose lower node lies at or below the
+  // bin's lower edge. The root of a density blend of rows r and r + 1 lies
+  // between the two rows' cells for the blended thermal target.
+  const uint16_t *therm_idx;
+  int therm_bins, therm_shift, therm_base;
 };
 constexpr int SP_COARSE = 16;
 // Row length of the coarse index in memory: 16 entries and 2 of padding,

@@ -153,6 +153,60 @@ std::map<uint64_t, Resident> g_tables;
 
 constexpr double VAPOR_DPDR_THRESH = 1e-8;
 
+// The thermal-energy bin index of the float-float lookup (SpinerTable::
+// therm_idx). Bins are slices of the float bit pattern of the thermal energy
+// t = sie - sieCold, 2^s per octave with s chosen so that a bin is at most
+// half the narrowest T cell; the index is left out (idx empty) where the
+// thermal energy does not rise strictly along every row, where the table
+// is coarser than the bins can hold, or where it would exceed 4 Mi entries.
+void build_thermal_index(const std::vector<double> &sie, const std::vector<double> &cold,
+                         const int nR, const int nT, SpinerTable &t, std::vector<uint16_t> &idx) {
+  idx.clear();
+  t.therm_bins = t.therm_shift = t.therm_base = 0;
+  if (nR < 2 || nT < 2 || nT - 1 > 65535 || static_cast<int>(cold.size()) < nR) return;
+  double tlo = INFINITY, thi = 0.0, min_step = INFINITY;
+  for (int r = 0; r < nR; ++r) {
+    double prev = sie[static_cast<size_t>(r) * nT] - cold[r];
+    for (int i = 1; i < nT; ++i) {
+      const double ti = sie[static_cast<size_t>(r) * nT + i] - cold[r];
+      if (!(ti > prev)) return; // thermal energy must rise along T
+      if (i == 1) tlo = std::min(tlo, ti);
+      if (prev > 0.0) min_step = std::min(min_step, std::log2(ti / prev));
+      thi = std::max(thi, ti);
+      prev = ti;
+    }
+  }
+  if (!(tlo > 0.0) || !(thi < 1e37) || !(min_step > 0.0)) return;
+  int sub = 0; // log2 of the bins per octave
+  while (sub < 7 && std::ldexp(1.0, -sub) > 0.5 * min_step)
+    ++sub;
+  if (std::ldexp(1.0, -sub) > 0.5 * min_step) return;
+  const int shift = 23 - sub;
+  auto bin_of = [shift](const float x) {
+    uint32_t u;
+    std::memcpy(&u, &x, sizeof(u));
+    return static_cast<int>(u >> shift);
+  };
+  const int base = bin_of(static_cast<float>(0.5 * tlo));
+  const int nbins = bin_of(static_cast<float>(thi)) - base + 2;
+  if (nbins < 1 || static_cast<size_t>(nbins) * nR > (size_t(1) << 22)) return;
+  idx.assign(static_cast<size_t>(nbins) * nR, 0);
+  for (int r = 0; r < nR; ++r) {
+    int i = 0;
+    for (int k = 0; k < nbins; ++k) {
+      const uint32_t u = static_cast<uint32_t>(base + k) << shift;
+      float edge;
+      std::memcpy(&edge, &u, sizeof(edge));
+      while (i + 1 < nT - 1 && sie[static_cast<size_t>(r) * nT + i + 1] - cold[r] <= edge)
+        ++i;
+      idx[static_cast<size_t>(r) * nbins + k] = static_cast<uint16_t>(i);
+    }
+  }
+  t.therm_bins = nbins;
+  t.therm_shift = shift;
+  t.therm_base = base;
+}
+
 // setlTColdCrit_ (eos_spiner_rho_temp.hpp:716-775) for one density node.
 double cold_crit(const HostTable &h, int j, const Grid1D &gCold) {
   const SpinerTable &t = h.t;
@@ -443,6 +497,11 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
   off = align(off + static_cast<size_t>(nR) * sizeof(float));
   const size_t offm32 = off;
   off = align(off + static_cast<size_t>(nR) * sizeof(float));
+  // the thermal-energy bin index (see SpinerTable::therm_idx)
+  std::vector<uint16_t> therm;
+  build_thermal_index(h.f2[F_SIE], h.f1[F_SIECOLD], nR, nT, t, therm);
+  const size_t offth = off;
+  off = align(off + therm.size() * sizeof(uint16_t));
   const size_t bytes = off;
   std::vector<unsigned char> img(bytes, 0);
   for (int k = 0; k < NF2D; ++k)
@@ -534,6 +593,8 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
     std::memcpy(img.data() + offc32 + j * sizeof(float), &c, sizeof(float));
     std::memcpy(img.data() + offm32 + j * sizeof(float), &m, sizeof(float));
   }
+  if (!therm.empty())
+    std::memcpy(img.data() + offth, therm.data(), therm.size() * sizeof(uint16_t));
   void *dev = nullptr;
   cudaError_t e = cudaMalloc(&dev, bytes);
   if (e != cudaSuccess) {
@@ -557,6 +618,7 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
   td.bmodR = reinterpret_cast<const FfRec *>(d + offbr);
   td.rhoNodes = reinterpret_cast<const double *>(d + offxl);
   td.sieCoarse = reinterpret_cast<const float2 *>(d + offco);
+  td.therm_idx = therm.empty() ? nullptr : reinterpret_cast<const uint16_t *>(d + offth);
   std::memcpy(img.data(), &td, sizeof(td));
   e = cudaMemcpy(dev, img.data(), bytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
@@ -654,10 +716,29 @@ int table_load_helm(const char *path, uint64_t *handle, std::string &msg) {
           for (int q = 0; q < 4; ++q)
             r[o++] = fields[b][cub[f]][c[q]];
     }
+  // FP32 normalised biquintic coefficients (HelmTable::cells32): term k's
+  // coefficient times the powers of the cell widths its weights carry, laid
+  // out [T weight][density weight]
+  std::vector<float> cells32(ncell * 36);
+  bool f32_ok = true;
+  for (int j = 0; j < NT - 1 && f32_ok; ++j)
+    for (int i = 0; i < NR - 1; ++i) {
+      const double *r = cells.data() + (static_cast<size_t>(j) * (NR - 1) + i) * HELM_REC;
+      float *o = cells32.data() + (static_cast<size_t>(j) * (NR - 1) + i) * 36;
+      const double dth = T[j + 1] - T[j], dd = rho[i + 1] - rho[i];
+      const double ts[6] = {1.0, 1.0, dth, -dth, dth * dth, dth * dth};
+      const double ds[6] = {1.0, 1.0, dd, -dd, dd * dd, dd * dd};
+      for (int k = 0; k < 36; ++k) {
+        const double v = r[k] * ts[helm::H5_TI[k]] * ds[helm::H5_DI[k]];
+        if (!(std::fabs(v) < 1e37)) f32_ok = false;
+        o[helm::H5_TI[k] * 6 + helm::H5_DI[k]] = static_cast<float>(v);
+      }
+    }
   const size_t off_cells = 256;
   const size_t off_rho = off_cells + cells.size() * 8;
   const size_t off_T = off_rho + NR * 8;
-  const size_t bytes = off_T + NT * 8;
+  const size_t off_c32 = (off_T + NT * 8 + 255) / 256 * 256;
+  const size_t bytes = off_c32 + (f32_ok ? cells32.size() * sizeof(float) : 0);
   void *dev = nullptr;
   cudaError_t e = cudaMalloc(&dev, bytes);
   if (e != cudaSuccess) {
@@ -668,11 +749,14 @@ int table_load_helm(const char *path, uint64_t *handle, std::string &msg) {
   t.cells = reinterpret_cast<const double *>(d + off_cells);
   t.rho = reinterpret_cast<const double *>(d + off_rho);
   t.T = reinterpret_cast<const double *>(d + off_T);
+  t.cells32 = f32_ok ? reinterpret_cast<const float *>(d + off_c32) : nullptr;
   std::vector<unsigned char> img(bytes, 0);
   std::memcpy(img.data(), &t, sizeof(t));
   std::memcpy(img.data() + off_cells, cells.data(), cells.size() * 8);
   std::memcpy(img.data() + off_rho, rho.data(), NR * 8);
   std::memcpy(img.data() + off_T, T.data(), NT * 8);
+  if (f32_ok)
+    std::memcpy(img.data() + off_c32, cells32.data(), cells32.size() * sizeof(float));
   e = cudaMemcpy(dev, img.data(), bytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     cudaFree(dev);
@@ -715,6 +799,12 @@ int table_nrho(uint64_t handle) {
   std::lock_guard<std::mutex> lk(g_mu);
   auto it = g_tables.find(handle);
   return (it == g_tables.end() || !it->second.dump.empty()) ? 0 : it->second.host.t.nRho;
+}
+
+bool table_has_thermal_index(uint64_t handle) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_tables.find(handle);
+  return it != g_tables.end() && it->second.dump.empty() && it->second.host.t.therm_bins > 0;
 }
 
 size_t table_bytes(uint64_t handle) {

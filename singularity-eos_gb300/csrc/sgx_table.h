@@ -19,6 +19,8 @@ int table_free(uint64_t handle, std::string &msg);
 size_t table_bytes(uint64_t handle);
 // Density nodes of a resident Spiner table (0 if unknown).
 int table_nrho(uint64_t handle);
+// Whether a resident Spiner table carries the thermal-energy bin index.
+bool table_has_thermal_index(uint64_t handle);
 // Spiner: derived tables in the reference's DBLIST order; Helmholtz: node
 // values and fields in its DBLIST order. Returns the count or -1.
 long table_dump(uint64_t handle, double *out, long cap);

@@ -34,7 +34,7 @@ EXPORTED = [
     "sgx_pte_solve", "sgx_pte_solve_noalloc", "sgx_eos_helmholtz", "sgx_eos_helmholtz_dump",
     "sgx_server_create", "sgx_server_submit", "sgx_server_wait", "sgx_server_stats_get",
     "sgx_server_destroy", "sgx_host_alloc", "sgx_host_free", "sgx_eos_fill_host",
-    "sgx_get_sg_eos", "sgx_get_sg_eos_device", "sgx_eos_modify_shifted", "sgx_eos_modify_scaled",
+    "sgx_get_sg_eos", "sgx_get_sg_eos_device", "sgx_tune_autotune_pte", "sgx_eos_modify_shifted", "sgx_eos_modify_scaled",
     "sgx_eos_modify_bilinear_ramp", "sgx_eos_p_alpha_ramp_params", "sgx_eos_apply_modifiers",
     "sgx_eos_pt_derivatives", "sgx_eos_ideal_gas_entropy", "sgx_eos_stiff_gas_ref",
     "sgx_eos_noble_abel_ref", "sgx_init_sg_eos", "sgx_init_sg_IdealGas", "sgx_init_sg_StiffGas",
@@ -103,7 +103,8 @@ class PteRequest(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
                 ("cells_completed", C.c_uint64), ("inflight", C.c_int), ("queued", C.c_int),
-                ("arena_used", C.c_size_t), ("arena_peak", C.c_size_t)]
+                ("arena_used", C.c_size_t), ("arena_peak", C.c_size_t),
+                ("batches", C.c_uint64)]
 
 
 _lib = None
@@ -194,6 +195,8 @@ def load():
     lib.sgx_pte_required_scratch_bytes.restype = C.c_size_t
     lib.sgx_tune_autotune_fill.argtypes = [C.POINTER(SgxEos), C.c_int64] + [P] * 7 + [
         C.c_uint32, P, I, I, C.POINTER(C.c_int), C.POINTER(C.c_int), P]
+    lib.sgx_tune_autotune_pte.argtypes = [I, C.c_int64, P, I] + [P] * 9 + [
+        C.POINTER(MixParams), P, I, I, P, P]
     _lib = lib
     return lib
 
@@ -358,6 +361,21 @@ def autotune_fill(eos, rho, temp, sie, press, cv, bmod, output, cs=None, lam=Non
         ptr(cs), output, ptr(lam), lam_stride, reps, C.byref(b), C.byref(st),
         stream_ptr(stream)))
     return b.value, st.value
+
+
+def autotune_pte(eos_list, eos_idx, vfrac_tot, sie_tot, rho, vfrac, sie, temp, press,
+                 lam=None, params=None, status=None, reps=2, tune_group=True, stream=None):
+    """sgx_tune_autotune_pte on device tensors: returns the (block, count
+    order, group_min_n) it kept; the arrays end holding that setting's solve."""
+    nmat, ncell = rho.shape
+    arr = (SgxEos * len(eos_list))(*eos_list)
+    chosen = (C.c_int * 3)()
+    check(load().sgx_tune_autotune_pte(
+        nmat, ncell, C.cast(arr, C.c_void_p), len(eos_list), ptr(eos_idx), ptr(vfrac_tot),
+        ptr(sie_tot), ptr(rho), ptr(vfrac), ptr(sie), ptr(temp), ptr(press), ptr(lam),
+        C.byref(params) if params is not None else None, ptr(status), reps,
+        1 if tune_group else 0, chosen, stream_ptr(stream)))
+    return tuple(chosen)
 
 
 class PtePlan:

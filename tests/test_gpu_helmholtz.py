@@ -254,3 +254,58 @@ def test_two_pass_inversion_is_bitwise_single_pass(sgx, table, options):
                                       lam1.cpu().numpy().view(np.uint64))
     finally:
         sgx.load().sgx_eos_finalize(C.byref(eos))
+
+
+def test_mixed_inversion_meets_the_reference_criterion(sgx, table):
+    """SGX_PREC_MIXED runs the T(rho, sie) inversion's Newton iteration from
+    an FP32 phase (FP32 e(T) to 1e-6 from normalised FP32 biquintic
+    coefficients), then the reference's FP64 steps; every evaluation behind
+    an output stays FP64. Checked on 2^16 cells of the benchmark's
+    distribution: the outputs are exactly the FP64 forward evaluation at the
+    temperature found; that temperature meets the reference's own stopping
+    criterion, |e(T) - sie| < 1e-10 |sie|, on every cell where the FP64
+    inversion's does (the two may pick different points of that band where
+    e(T) is flat: degenerate cells); and the per-output differences to the
+    FP64 inversion are printed."""
+    from sgx import helmtable
+    n = 1 << 16
+    rho_h, T_h, abar, zbar = helmtable.helm_queries(n, seed=123)
+    eos = sgx.helmholtz_eos(table[0])
+    try:
+        lam_h = np.zeros(3 * n)
+        lam_h[0::3], lam_h[1::3], lam_h[2::3] = abar, zbar, np.nan
+        rho, Tin = dev(rho_h), dev(T_h)
+        sie = torch.empty_like(rho)
+        sgx.fill_eos(eos, rho, Tin, sie, None, None, None, sgx.Q_SIE, lam=dev(lam_h),
+                     lam_stride=3)
+        q = sgx.Q_TEMPERATURE | sgx.Q_PRESSURE | sgx.Q_BULK_MODULUS
+        out = {}
+        for prec in (sgx.PREC_FP64, sgx.PREC_MIXED):
+            T, P, bm, cs = (torch.empty_like(rho) for _ in range(4))
+            sgx.fill_eos(eos, rho, T, sie, P, None, bm, q, lam=dev(lam_h), lam_stride=3, cs=cs,
+                         precision=prec)
+            out[prec] = (T, P, bm, cs)
+        Tm, Pm, bmm, csm = out[sgx.PREC_MIXED]
+        # the forward FP64 evaluation at the mixed temperature
+        e_f, P_f, bm_f = (torch.empty_like(rho) for _ in range(3))
+        sgx.fill_eos(eos, rho, Tm.clone(), e_f, P_f, None, bm_f,
+                     sgx.Q_SIE | sgx.Q_PRESSURE | sgx.Q_BULK_MODULUS, lam=dev(lam_h),
+                     lam_stride=3)
+        e_64 = torch.empty_like(rho)
+        sgx.fill_eos(eos, rho, out[sgx.PREC_FP64][0].clone(), e_64, None, None, None, sgx.Q_SIE,
+                     lam=dev(lam_h), lam_stride=3)
+        torch.cuda.synchronize()
+        for a, b in ((Pm, P_f), (bmm, bm_f)):
+            assert np.array_equal(a.cpu().numpy().view(np.uint64), b.cpu().numpy().view(np.uint64))
+        s = sie.cpu().numpy()
+        ok_m = np.abs(e_f.cpu().numpy() - s) < 1e-10 * np.abs(s)
+        ok_64 = np.abs(e_64.cpu().numpy() - s) < 1e-10 * np.abs(s)
+        print(f"meets |e(T) - sie| < 1e-10 |sie|: mixed {ok_m.mean():.4f}, FP64 {ok_64.mean():.4f}")
+        assert np.all(ok_m[ok_64]), int((ok_64 & ~ok_m).sum())
+        for name, k in (("T", 0), ("P", 1), ("bmod", 2), ("cs", 3)):
+            e = rel_err(out[sgx.PREC_MIXED][k].cpu().numpy(), out[sgx.PREC_FP64][k].cpu().numpy())
+            e = e[ok_64]
+            print(f"  {name} vs FP64 inversion (well-posed cells): max {e.max():.2e} "
+                  f"p99.9 {np.quantile(e, 0.999):.2e} median {np.median(e):.2e}")
+    finally:
+        sgx.load().sgx_eos_finalize(C.byref(eos))

@@ -412,3 +412,53 @@ def test_autotune_fill_keeps_a_valid_shape_and_the_results(sgx):
         for k, v in zip((sgx.TUNE_LOOKUP_BLOCKS_PER_SM, sgx.TUNE_LOOKUP_STAGE), saved):
             L.sgx_tune_set(k, v)
         L.sgx_eos_finalize(C.byref(tab))
+
+
+def test_autotune_pte_keeps_results_within_the_contract(sgx):
+    """sgx_tune_autotune_pte times block size, count order and the lane-group
+    threshold on the batch and keeps the fastest: the knobs it sets are in
+    range, the block size and the count order leave the result bit for bit
+    as it was, and the arrays end holding a solve that meets the bar."""
+    import ctypes as C
+    from sgx import workloads as W
+    L = sgx.load()
+    knobs = (sgx.TUNE_PTE_MIXED_BLOCK, sgx.TUNE_PTE_COUNT_ORDER, sgx.TUNE_PTE_GROUP_MIN_N)
+    saved = []
+    for k in knobs:
+        v = C.c_int()
+        assert L.sgx_tune_get(k, C.byref(v)) == 0
+        saved.append(v.value)
+    try:
+        wl = W.pte_batched(1 << 16, seed=8)
+        base, _ = run_pte(sgx, wl, sgx.PREC_MIXED)
+        for blk, order in ((32, 1), (64, 0)):
+            assert L.sgx_tune_set(sgx.TUNE_PTE_MIXED_BLOCK, blk) == 0
+            assert L.sgx_tune_set(sgx.TUNE_PTE_COUNT_ORDER, order) == 0
+            got, _ = run_pte(sgx, wl, sgx.PREC_MIXED)
+            for k in base:
+                assert np.array_equal(got[k], base[k], equal_nan=True), (blk, order, k)
+        for k, v in zip(knobs, saved):
+            L.sgx_tune_set(k, v)
+        eos = [sgx.make_eos(k, p) for k, p in wl["materials"]]
+        t = {k: torch.as_tensor(wl[k], device="cuda") for k in ("rho", "vfrac", "sie", "temp",
+                                                                 "press")}
+        status = torch.zeros(wl["sie_tot"].size * 16, dtype=torch.uint8, device="cuda")
+        chosen = sgx.autotune_pte(eos, torch.as_tensor(wl["eos_idx"], device="cuda"),
+                                  torch.as_tensor(wl["vfrac_tot"], device="cuda"),
+                                  torch.as_tensor(wl["sie_tot"], device="cuda"), t["rho"],
+                                  t["vfrac"], t["sie"], t["temp"], t["press"], status=status,
+                                  reps=1)
+        assert chosen[0] in (32, 64, 128) and chosen[1] in (0, 1) and 2 <= chosen[2] <= 7
+        got = []
+        for k in knobs:
+            v = C.c_int()
+            L.sgx_tune_get(k, C.byref(v))
+            got.append(v.value)
+        assert tuple(got) == tuple(chosen)
+        # the arrays hold the chosen setting's solve: the same as a fresh call
+        again, _ = run_pte(sgx, wl, sgx.PREC_MIXED)
+        for k in again:
+            assert np.array_equal(t[k].cpu().numpy(), again[k], equal_nan=True), k
+    finally:
+        for k, v in zip(knobs, saved):
+            L.sgx_tune_set(k, v)

@@ -1,8 +1,9 @@
 """The serving loop (sgx_server_*): requests of different sizes submitted at
-once overlap on the device, and each result must be exactly the one
-sgx_pte_solve gives for that request alone (same kernels, every cell
-independent of the others); admission keeps the arena within its budget;
-oversized requests are refused at submission."""
+once are folded into merged solves (their cells end to end in one binned
+batch), and each result must be exactly the one sgx_pte_solve gives for
+that request alone (same kernels, every cell independent of the others);
+admission keeps the arena within its budget; oversized requests are refused
+at submission."""
 import os
 
 import numpy as np
@@ -93,6 +94,8 @@ def test_each_result_is_the_same_alone_and_in_the_mix(sgx, eos_list, precision):
     assert st["completed"] == len(reqs) and st["failed"] == 0
     assert st["cells_completed"] == int(sizes.sum())
     assert 0 < st["arena_peak"] <= budget
+    # requests waiting together were folded into shared solves
+    assert 1 <= st["batches"] < len(reqs), st["batches"]
     for r in reqs:
         same(r, solve_alone(sgx, eos_list, r, precision))
 
