@@ -1491,3 +1491,7 @@ void sgport_nqt(int which, int n, const double *x, double *y) {
 }
 
 } // extern "C"
+
+// The Helmholtz model (same translation unit: it uses the port's ratio and
+// root finders).
+#include "sgport_helm.cpp"

@@ -220,6 +220,18 @@ class Oracle:
         f(path.encode(), _dp(out), C.c_long(n))
         return out
 
+    def helm_fill(self, path, options, rho, temp, sie, press, cv, bmod, output, lam):
+        """Helmholtz FillEos over n elements (port only: sgport_helm_fill),
+        OpenMP over the host threads; lam rows [Abar, Zbar, lT] (n x 3),
+        updated with log10 T as the library's default mode stores it."""
+        n = rho.shape[0]
+        fn = self._fn("helm_fill")
+        fn.restype = C.c_int
+        rc = fn(C.c_char_p(path.encode()), C.c_int(options), C.c_int(n), _dp(rho), _dp(temp),
+                _dp(sie), _dp(press), _dp(cv), _dp(bmod), C.c_uint(output), _dp(lam))
+        if rc != 0:
+            raise RuntimeError(f"{self.prefix}_helm_fill failed")
+
     def helm_T_from_rho_sie(self, path, rho, sie, abar, zbar):
         """T(rho, sie) of the default-option Helmholtz EOS without the lT
         cache read-back (reference library only)."""

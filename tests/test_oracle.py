@@ -281,3 +281,42 @@ def test_entropy_known_answers():
     S = ref.eos_vec(d, 12, np.array([1.0218087167564040e-01]),
                     np.array([3.7350567520918861e+10]))
     np.testing.assert_allclose(S, [-2.0044437857420778e+08], rtol=1e-12)
+
+
+def test_port_helmholtz_matches_golden(tmp_path):
+    """The port's Helmholtz restatement (sgport_helm_fill) against the
+    fixture the compiled reference made on the synthetic table: the forward
+    FillEos (rho, T -> sie, P, cv, bmod) within 1e-12, and the inversion as
+    it is meant (the root kept, as sgref_helm_T_from_rho_sie finds it) within
+    the reference's own stopping band where the reference recovers T."""
+    import refbind as rb
+    from common import golden, rel_err
+    from sgx import helmtable
+    fx = golden("helmholtz")
+    path = str(tmp_path / "helm_table.dat")
+    assert helmtable.helm_table(path) == str(fx["table_sha256"])
+    port = rb.port()
+    n = fx["rho"].size
+
+    def lam_rows():
+        lam = np.zeros(3 * n)
+        lam[0::3], lam[1::3], lam[2::3] = fx["abar"], fx["zbar"], np.nan
+        return lam
+
+    sie, P, cv, bm = (np.zeros(n) for _ in range(4))
+    port.helm_fill(path, 31, fx["rho"].copy(), fx["T"].copy(), sie, P, cv, bm,
+                   rb.Q_SIE | rb.Q_PRESSURE | rb.Q_SPECIFIC_HEAT | rb.Q_BULK_MODULUS,
+                   lam_rows())
+    for k, got in (("sie", sie), ("P", P), ("cv", cv), ("bmod", bm)):
+        e = rel_err(got, fx["fwd_" + k])
+        assert e.max() <= 1e-12, (k, e.max())
+    T = np.zeros(n)
+    port.helm_fill(path, 31, fx["rho"].copy(), T, fx["fwd_sie"].copy(), np.zeros(n),
+                   np.zeros(n), np.zeros(n), rb.Q_TEMPERATURE | rb.Q_PRESSURE, lam_rows())
+    # where the reference recovers T, both stop within 1e-10 |e| of the
+    # target: |dT| <= 2e-10 |e| / cv
+    fix, Tin = fx["fix_T"], fx["T"]
+    good = np.abs(fix - Tin) <= 1e-8 * Tin
+    assert good.mean() > 0.75
+    bound = 2e-10 * np.abs(fx["fwd_sie"][good]) / np.abs(fx["fwd_cv"][good]) + 1e-12 * fix[good]
+    assert (np.abs(T[good] - fix[good]) <= bound).all()
