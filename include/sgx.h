@@ -63,7 +63,8 @@ enum {
   SGX_NOBLE_ABEL = 3,
   SGX_GRUNEISEN = 4,
   SGX_SPINER_RHOT = 5,
-  SGX_HELMHOLTZ = 6
+  SGX_HELMHOLTZ = 6,
+  SGX_SPINER_RHOSIE = 7
 };
 
 /* thermalqs bits (singularity-eos/base/constants.hpp:22-34). */
@@ -219,6 +220,15 @@ int sgx_eos_gruneisen(sgx_eos *out, double C0, double s1, double s2, double s3,
  * tables (SpinerEOSDependsRhoT::loadDataboxes_, eos_spiner_rho_temp.hpp:545-687)
  * and makes the table resident on the current device. */
 int sgx_eos_spiner_rhot(sgx_eos *out, const char *path, int matid, int reproducible);
+/* Loads a tabulated EOS on rho-T and rho-sie grids (SpinerEOSDependsRhoSie
+ * with the default NullTransform, eos_spiner_rho_sie.hpp:80-1052) from an
+ * sp5-lite image: /<matid>/dependsLogRhoLogT, /<matid>/dependsLogRhoLogSie
+ * and /<matid>/coldCurve, with the bulk moduli recomputed and the
+ * minimum-pressure tables derived as loadDataboxes_ (:433-552) does, and
+ * makes the table resident on the current device. Functions of (rho, sie)
+ * interpolate the rho-sie grid directly (no root find); lambda rows carry
+ * one entry, log10(rho). TableSplit::Total only; no mass fractions. */
+int sgx_eos_spiner_rhosie(sgx_eos *out, const char *path, int matid, int reproducible);
 /* Option bits of sgx_eos_helmholtz (Helmholtz::Options, eos_helmholtz.hpp:420-441). */
 enum {
   SGX_HELM_RAD = 1,            /* ENABLE_RAD */
@@ -291,6 +301,22 @@ long sgx_eos_spiner_dump(const sgx_eos *eos, double *out, long cap);
 int sgx_eos_eval(const sgx_eos *eos, int fn, int64_t n, const double *in1,
                  const double *in2, double *out, double *lambda, int lambda_stride,
                  sgx_stream_t stream);
+/* The bounds a model reports (eos_base.hpp:533-560 and the overrides of
+ * each model, through the modifiers as eos_base.hpp:134-153 and
+ * scaled_eos.hpp:254-275 forward them), one per element: out[i] =
+ * MinimumDensity(), MinimumTemperature(), MaximumDensity(),
+ * MinimumPressure(), MaximumPressureAtTemperature(temp[i]) or
+ * RhoPmin(temp[i]). temp may be NULL for the first four. Device arrays. */
+enum {
+  SGX_BOUND_MIN_DENSITY = 0,
+  SGX_BOUND_MIN_TEMPERATURE = 1,
+  SGX_BOUND_MAX_DENSITY = 2,
+  SGX_BOUND_MIN_PRESSURE = 3,
+  SGX_BOUND_MAX_PRESSURE_AT_T = 4,
+  SGX_BOUND_RHO_PMIN = 5
+};
+int sgx_eos_bounds(const sgx_eos *eos, int what, int64_t n, const double *temp, double *out,
+                   sgx_stream_t stream);
 /* PTDerivativesFromPreferred (eos/eos_base.hpp:410-419, eos_variant.hpp:
  * 386-398) at n states (rho, sie, press, temp): dedP_T = (dsie/dP)_T,
  * drdP_T = (drho/dP)_T, dedT_P = (dsie/dT)_P, drdT_P = (drho/dT)_P.
@@ -587,6 +613,8 @@ int sgx_init_sg_Gruneisen(int matindex, sgx_eos *eos, double C0, double s1, doub
 /* split: TableSplit::Total (0) only. */
 int sgx_init_sg_SpinerDependsRhoT(int matindex, sgx_eos *eos, const char *filename, int id,
                                   int split, const int *enabled, double *vals);
+int sgx_init_sg_SpinerDependsRhoSie(int matindex, sgx_eos *eos, const char *filename, int id,
+                                    int split, const int *enabled, double *vals);
 int sgx_init_sg_Helmholtz(int matindex, sgx_eos *eos, const char *filename, int rad, int gas,
                           int coul, int ion, int ele, int verbose, const int *enabled,
                           double *vals);

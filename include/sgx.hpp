@@ -169,7 +169,8 @@ struct NullIndexer {
 // ---------------------------------------------------------------------------
 
 // The lambda slots each model numbers (its Lambda enum): the tabulated
-// model caches log10 rho and log10 T (eos_spiner_rho_temp.hpp:79-81).
+// models cache log10 rho and log10 T (eos_spiner_rho_temp.hpp:79-81;
+// SpinerEOSDependsRhoSie log10 rho only, eos_spiner_rho_sie.hpp:85-87).
 namespace detail {
 struct LambdaRow {
   Real v[3];
@@ -218,6 +219,11 @@ class EOS {
   static EOS SpinerEOSDependsRhoT(const char *path, int matid, bool reproducible = false) {
     EOS x;
     check(sgx_eos_spiner_rhot(&x.e, path, matid, reproducible ? 1 : 0));
+    return x;
+  }
+  static EOS SpinerEOSDependsRhoSie(const char *path, int matid, bool reproducible = false) {
+    EOS x;
+    check(sgx_eos_spiner_rhosie(&x.e, path, matid, reproducible ? 1 : 0));
     return x;
   }
   // Frees a tabulated model's device table (Finalize, eos_variant.hpp:865-867).

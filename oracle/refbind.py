@@ -25,7 +25,7 @@ REF_SO = os.path.join(HERE, "_ref", "libsgref.so")
 PORT_SO = os.path.join(HERE, "_build", "libsgport.so")
 
 # EOS type codes shared by the oracle and the product (include/sgx.h).
-IDEAL, STIFF, NOBLE_ABEL, GRUNEISEN, SPINER_RHOT, HELMHOLTZ = 1, 2, 3, 4, 5, 6
+IDEAL, STIFF, NOBLE_ABEL, GRUNEISEN, SPINER_RHOT, HELMHOLTZ, SPINER_RHOSIE = 1, 2, 3, 4, 5, 6, 7
 
 # thermalqs bits (singularity-eos/base/constants.hpp:22-34)
 Q_DENSITY, Q_SIE, Q_PRESSURE, Q_TEMPERATURE = 1, 2, 4, 8
@@ -339,6 +339,19 @@ class Oracle:
         out = np.zeros(n)
         self._fn("spiner_dump")(path.encode(), C.c_int(matid), _dp(out), C.c_long(n),
                                 _dp(scal))
+        return out, scal
+
+    def spiner_sie_dump(self, path, matid):
+        """SpinerEOSDependsRhoSie's tables in DBLIST order, and its scalars
+        (the compiled reference only)."""
+        f = self._fn("spiner_sie_dump")
+        f.restype = C.c_long
+        scal = np.zeros(18)
+        n = f(path.encode(), C.c_int(matid), None, C.c_long(0), _dp(scal))
+        if n < 0:
+            raise RuntimeError("spiner_sie_dump failed")
+        out = np.zeros(n)
+        f(path.encode(), C.c_int(matid), _dp(out), C.c_long(n), _dp(scal))
         return out, scal
 
     def nqt(self, which, x):

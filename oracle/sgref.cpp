@@ -39,7 +39,8 @@ extern "C" {
 // EOS description passed across the oracle's C boundary.
 struct sgref_eos {
   int32_t type; // 1 IdealGas, 2 StiffGas, 3 NobleAbel, 4 Gruneisen,
-                // 5 SpinerEOSDependsRhoT, 6 Helmholtz
+                // 5 SpinerEOSDependsRhoT, 6 Helmholtz,
+                // 7 SpinerEOSDependsRhoSie
   int32_t flags;
   int32_t matid;
   int32_t pad;
@@ -104,6 +105,8 @@ EOS make_model(const sgref_eos &d) {
     return Helmholtz(std::string(d.path), (d.flags & 1) != 0, (d.flags & 2) != 0,
                      (d.flags & 4) != 0, (d.flags & 8) != 0, (d.flags & 16) != 0, false,
                      (d.flags & 32) == 0);
+  case 7:
+    return SpinerEOSDependsRhoSie(std::string(d.path), d.matid, (d.flags & 1) != 0);
   }
   PORTABLE_ALWAYS_THROW_OR_ABORT("sgref: unknown EOS type");
   return IdealGas(0.4, 1.0);
@@ -611,6 +614,40 @@ long sgref_spiner_dump(const char *path, int matid, double *out, long cap, doubl
     return n;
   } catch (const std::exception &ex) {
     std::fprintf(stderr, "sgref_spiner_dump: %s\n", ex.what());
+    return -1;
+  }
+}
+
+// The same for SpinerEOSDependsRhoSie (DBLIST at eos_spiner_rho_sie.hpp:
+// 329-336: sie_, T_, rho_at_pmin_, the seven rho-T then the seven rho-sie
+// tables, mF_, PlRhoMax_, dPdRhoMax_, PCold_, sieCold_, bModCold_,
+// dPdRhoCold_). scal receives rhoMin, rhoMax, TMin, TMax, sieMin, sieMax,
+// MinimumPressure, the three offsets, then ValuesAtReferenceState's eight
+// values (rho, T, sie, P, cv, bmod, dpde, dvdt).
+long sgref_spiner_sie_dump(const char *path, int matid, double *out, long cap, double *scal) {
+  try {
+    SpinerEOSDependsRhoSie eos(std::string(path), matid);
+    const long n = static_cast<long>(eos.DynamicMemorySizeInBytes() / sizeof(double));
+    if (out && cap >= n) eos.DumpDynamicMemory(reinterpret_cast<char *>(out));
+    if (scal) {
+      scal[0] = eos.rhoMin();
+      scal[1] = eos.rhoMax();
+      scal[2] = eos.TMin();
+      scal[3] = eos.TMax();
+      scal[4] = eos.sieMin();
+      scal[5] = eos.sieMax();
+      scal[6] = eos.MinimumPressure();
+      scal[7] = eos.lRhoOffset();
+      scal[8] = eos.lTOffset();
+      scal[9] = eos.lEOffset();
+      Real *lam = nullptr;
+      eos.ValuesAtReferenceState(scal[10], scal[11], scal[12], scal[13], scal[14], scal[15],
+                                 scal[16], scal[17], lam);
+    }
+    eos.Finalize();
+    return n;
+  } catch (const std::exception &ex) {
+    std::fprintf(stderr, "sgref_spiner_sie_dump: %s\n", ex.what());
     return -1;
   }
 }

@@ -165,6 +165,22 @@ class DataBox {
     return b0 * (a0 * at(k, j) + a1 * at(k, j + 1)) +
            b1 * (a0 * at(k + 1, j) + a1 * at(k + 1, j + 1));
   }
+  // Index ix of the slowest dimension as a box of one rank lower that shares
+  // this box's memory and keeps its remaining grids (spiner's
+  // DataBox::slice, used by eos_spiner_rho_sie.hpp:520-521).
+  DataBox slice(const int ix) const {
+    DataBox out;
+    out.rank_ = rank_ - 1;
+    std::size_t stride = 1;
+    for (int d = 0; d < out.rank_; ++d) {
+      out.dims_[d] = dims_[d];
+      out.grids_[d] = grids_[d];
+      stride *= static_cast<std::size_t>(dims_[d]);
+    }
+    out.data_ = data_ + static_cast<std::size_t>(ix) * stride;
+    out.owns_ = false;
+    return out;
+  }
   void interpFromDB(const DataBox &db, const T x3, const T x2) {
     for (int n = 0; n < dims_[0]; ++n)
       data_[n] = db.interpToReal(x3, x2, n);

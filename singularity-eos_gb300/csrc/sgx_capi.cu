@@ -28,9 +28,13 @@ int cuda_fail(cudaError_t e, const char *what) {
   return fail(SGX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-bool valid_type(int t) { return t >= SGX_IDEAL_GAS && t <= SGX_HELMHOLTZ; }
+bool valid_type(int t) { return t >= SGX_IDEAL_GAS && t <= SGX_SPINER_RHOSIE; }
 // Models the PTE kernels dispatch on (Helmholtz is a lookup-only model here).
-bool pte_type(int t) { return t >= SGX_IDEAL_GAS && t <= SGX_SPINER_RHOT; }
+bool pte_type(int t) { return sgx::pte_model(t); }
+// Entries a lambda row must hold: SpinerEOSDependsRhoSie caches log10(rho)
+// only (nlambda() == 1); the other tabulated models read and write two
+// (Helmholtz checks its three itself).
+int min_lambda_stride(int t) { return t == SGX_SPINER_RHOSIE ? 1 : 2; }
 // Modifier bits must be known ones; Helmholtz carries none; the
 // mixed-precision paths take bare models only.
 int check_mods(const sgx_eos &e, const bool mixed, const char *who) {
@@ -223,6 +227,22 @@ int sgx_eos_spiner_rhot(sgx_eos *out, const char *path, int matid, int reproduci
   return SGX_OK;
 }
 
+int sgx_eos_spiner_rhosie(sgx_eos *out, const char *path, int matid, int reproducible) {
+  if (!out || !path) return fail(SGX_ERR_INVALID, "sgx_eos_spiner_rhosie: null");
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+    return fail(SGX_ERR_NO_DEVICE, "sgx_eos_spiner_rhosie: no CUDA device");
+  std::string msg;
+  uint64_t handle = 0;
+  const int rc = sgx::table_load_spiner_sie(path, matid, reproducible != 0, &handle, msg);
+  if (rc != SGX_OK) return fail(rc, msg);
+  std::memset(out, 0, sizeof(*out));
+  out->type = SGX_SPINER_RHOSIE;
+  out->flags = reproducible ? 1 : 0;
+  out->table = handle;
+  return SGX_OK;
+}
+
 int sgx_eos_helmholtz(sgx_eos *out, const char *path, int options) {
   if (!out || !path) return fail(SGX_ERR_INVALID, "sgx_eos_helmholtz: null");
   if (options & ~127) return fail(SGX_ERR_INVALID, "sgx_eos_helmholtz: unknown option bits");
@@ -263,8 +283,26 @@ size_t sgx_eos_table_bytes(const sgx_eos *eos) {
   return (eos && eos->table) ? sgx::table_bytes(eos->table) : 0;
 }
 
+int sgx_eos_bounds(const sgx_eos *eos, int what, int64_t n, const double *temp, double *out,
+                   sgx_stream_t stream) {
+  if (!eos || !valid_type(eos->type)) return fail(SGX_ERR_INVALID, "sgx_eos_bounds: bad eos");
+  if (eos->type == SGX_HELMHOLTZ)
+    return fail(SGX_ERR_UNSUPPORTED, "sgx_eos_bounds: not available for Helmholtz");
+  if (what < SGX_BOUND_MIN_DENSITY || what > SGX_BOUND_RHO_PMIN)
+    return fail(SGX_ERR_INVALID, "sgx_eos_bounds: bad bound");
+  if (n < 0) return fail(SGX_ERR_INVALID, "sgx_eos_bounds: n < 0");
+  if (n == 0) return SGX_OK;
+  if (!out || (!temp && what >= SGX_BOUND_MAX_PRESSURE_AT_T))
+    return fail(SGX_ERR_INVALID, "sgx_eos_bounds: null array");
+  if (const int rc = check_mods(*eos, false, "sgx_eos_bounds")) return rc;
+  const cudaError_t e =
+      sgx::launch_bounds_fp64(*eos, what, n, temp, out, reinterpret_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "sgx_eos_bounds");
+  return SGX_OK;
+}
+
 long sgx_eos_spiner_dump(const sgx_eos *eos, double *out, long cap) {
-  if (!eos || eos->type != SGX_SPINER_RHOT || !eos->table) {
+  if (!eos || (eos->type != SGX_SPINER_RHOT && eos->type != SGX_SPINER_RHOSIE) || !eos->table) {
     fail(SGX_ERR_INVALID, "sgx_eos_spiner_dump: not a tabulated EOS");
     return -1;
   }
@@ -285,7 +323,8 @@ int sgx_eos_eval(const sgx_eos *eos, int fn, int64_t n, const double *in1, const
   if (n == 0) return SGX_OK;
   if (!in1 || !out || (!in2 && fn != SGX_FN_MIN_SIE_FROM_RHO))
     return fail(SGX_ERR_INVALID, "sgx_eos_eval: null array");
-  if (lambda && lambda_stride < 2) return fail(SGX_ERR_INVALID, "sgx_eos_eval: lambda_stride < 2");
+  if (lambda && lambda_stride < min_lambda_stride(eos->type))
+    return fail(SGX_ERR_INVALID, "sgx_eos_eval: lambda_stride below the model's lambda length");
   if (const int rc = check_mods(*eos, false, "sgx_eos_eval")) return rc;
   if (eos->type == SGX_HELMHOLTZ) {
     // Abar and Zbar come in through lambda (SafeMustGet in the reference)
@@ -326,8 +365,8 @@ int sgx_eos_pt_derivatives(const sgx_eos *eos, int64_t n, const double *rho, con
   if (n == 0) return SGX_OK;
   if (!rho || !sie || !press || !temp || !dedP_T || !drdP_T || !dedT_P || !drdT_P)
     return fail(SGX_ERR_INVALID, std::string(who) + ": null array");
-  if (lambda && lambda_stride < 2)
-    return fail(SGX_ERR_INVALID, std::string(who) + ": lambda_stride < 2");
+  if (lambda && lambda_stride < min_lambda_stride(eos->type))
+    return fail(SGX_ERR_INVALID, std::string(who) + ": lambda_stride below the model's lambda length");
   sgx::PtDerivArgs a;
   a.eos = *eos;
   a.n = n;
@@ -353,7 +392,8 @@ int sgx_eos_fill_ex(const sgx_eos *eos, int64_t n, double *rho, double *temp, do
   if (n < 0) return fail(SGX_ERR_INVALID, "sgx_eos_fill: n < 0");
   if (n == 0) return SGX_OK;
   if (!rho) return fail(SGX_ERR_INVALID, "sgx_eos_fill: rho is required");
-  if (lambda && lambda_stride < 2) return fail(SGX_ERR_INVALID, "sgx_eos_fill: lambda_stride < 2");
+  if (lambda && lambda_stride < min_lambda_stride(eos->type))
+    return fail(SGX_ERR_INVALID, "sgx_eos_fill: lambda_stride below the model's lambda length");
   if (precision != SGX_PREC_FP64 && precision != SGX_PREC_MIXED)
     return fail(SGX_ERR_INVALID, "sgx_eos_fill: bad precision");
   if (const int rc = check_mods(*eos, precision == SGX_PREC_MIXED, "sgx_eos_fill")) return rc;
@@ -420,8 +460,8 @@ int sgx_eos_fill_host(const sgx_eos *eos, int64_t n, double *rho, double *temp, 
   if (n < 0) return fail(SGX_ERR_INVALID, "sgx_eos_fill_host: n < 0");
   if (n == 0) return SGX_OK;
   if (!rho) return fail(SGX_ERR_INVALID, "sgx_eos_fill_host: rho is required");
-  if (lambda && lambda_stride < 2)
-    return fail(SGX_ERR_INVALID, "sgx_eos_fill_host: lambda_stride < 2");
+  if (lambda && lambda_stride < min_lambda_stride(eos->type))
+    return fail(SGX_ERR_INVALID, "sgx_eos_fill_host: lambda_stride below the model's lambda length");
   struct Arr {
     double *h;
     int width;

@@ -1,8 +1,9 @@
 // Model dispatch: one switch over the packed sgx_eos code, standing in for
 // the reference Variant's visit (eos/eos_variant.hpp:152-868). Analytic
 // models come from sgx_eos.cuh, the tabulated rho-T model from
-// sgx_spiner.cuh. `lam` is the per-element lambda row (nullable); only the
-// tabulated model reads or writes it.
+// sgx_spiner.cuh, the tabulated model on rho-T and rho-sie grids from
+// sgx_spiner_sie.cuh. `lam` is the per-element lambda row (nullable); only
+// the tabulated models read or write it.
 //
 // Two levels: md_* evaluates the bare model; ev_* (what every kernel calls)
 // adds the modifiers of sgx_eos.mods around it, nested as the reference's
@@ -12,6 +13,7 @@
 
 #include "sgx_eos.cuh"
 #include "sgx_spiner.cuh"
+#include "sgx_spiner_sie.cuh"
 
 // The translation units of the mixed-precision paths, which take bare models
 // only (the C API rejects a modified EOS there), define SGX_BARE_MODELS
@@ -33,73 +35,91 @@ SGX_HD const SpinerTable &sp_table(const sgx_eos &e) {
   return *reinterpret_cast<const SpinerTable *>(static_cast<uintptr_t>(e.table));
 }
 SGX_HD bool is_spiner(const sgx_eos &e) { return e.type == SGX_SPINER_RHOT; }
+SGX_HD const SieTable &ss_table(const sgx_eos &e) {
+  return *reinterpret_cast<const SieTable *>(static_cast<uintptr_t>(e.table));
+}
+SGX_HD bool is_spiner_sie(const sgx_eos &e) { return e.type == SGX_SPINER_RHOSIE; }
 
 template <typename T>
 SGX_HD T md_T_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
   if (is_spiner(e)) return T(sp_T_from_rho_sie(sp_table(e), double(rho), double(sie), lam));
+  if (is_spiner_sie(e)) return T(ss_T_from_rho_sie(ss_table(e), double(rho), double(sie), lam));
   return eos_T_from_rho_sie<T>(e, rho, sie);
 }
 template <typename T>
 SGX_HD T md_sie_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
   if (is_spiner(e)) return T(sp_sie_from_rho_T(sp_table(e), double(rho), double(temp), lam));
+  if (is_spiner_sie(e)) return T(ss_sie_from_rho_T(ss_table(e), double(rho), double(temp), lam));
   return eos_sie_from_rho_T<T>(e, rho, temp);
 }
 template <typename T>
 SGX_HD T md_P_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
   if (is_spiner(e)) return T(sp_P_from_rho_T(sp_table(e), double(rho), double(temp), lam));
+  if (is_spiner_sie(e)) return T(ss_P_from_rho_T(ss_table(e), double(rho), double(temp), lam));
   return eos_P_from_rho_T<T>(e, rho, temp);
 }
 template <typename T>
 SGX_HD T md_P_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
   if (is_spiner(e)) return T(sp_P_from_rho_sie(sp_table(e), double(rho), double(sie), lam));
+  if (is_spiner_sie(e)) return T(ss_P_from_rho_sie(ss_table(e), double(rho), double(sie), lam));
   return eos_P_from_rho_sie<T>(e, rho, sie);
 }
 template <typename T>
 SGX_HD T md_cv_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
   if (is_spiner(e)) return T(sp_cv_from_rho_T(sp_table(e), double(rho), double(temp), lam));
+  if (is_spiner_sie(e)) return T(ss_cv_from_rho_T(ss_table(e), double(rho), double(temp), lam));
   return eos_cv<T>(e);
 }
 template <typename T>
 SGX_HD T md_cv_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
   if (is_spiner(e)) return T(sp_cv_from_rho_sie(sp_table(e), double(rho), double(sie), lam));
+  if (is_spiner_sie(e)) return T(ss_cv_from_rho_sie(ss_table(e), double(rho), double(sie), lam));
   return eos_cv<T>(e);
 }
 template <typename T>
 SGX_HD T md_B_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
   if (is_spiner(e)) return T(sp_bmod_from_rho_T(sp_table(e), double(rho), double(temp), lam));
+  if (is_spiner_sie(e)) return T(ss_bmod_from_rho_T(ss_table(e), double(rho), double(temp), lam));
   return eos_B_from_rho_T<T>(e, rho, temp);
 }
 template <typename T>
 SGX_HD T md_B_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
   if (is_spiner(e)) return T(sp_bmod_from_rho_sie(sp_table(e), double(rho), double(sie), lam));
+  if (is_spiner_sie(e)) return T(ss_bmod_from_rho_sie(ss_table(e), double(rho), double(sie), lam));
   return eos_B_from_rho_sie<T>(e, rho, sie);
 }
 template <typename T>
 SGX_HD T md_gamma_from_rho_T(const sgx_eos &e, T rho, T temp, double *lam) {
   if (is_spiner(e)) return T(sp_gamma_from_rho_T(sp_table(e), double(rho), double(temp), lam));
+  if (is_spiner_sie(e)) return T(ss_gamma_from_rho_T(ss_table(e), double(rho), double(temp), lam));
   return eos_gamma<T>(e, rho);
 }
 template <typename T>
 SGX_HD T md_gamma_from_rho_sie(const sgx_eos &e, T rho, T sie, double *lam) {
   if (is_spiner(e)) return T(sp_gamma_from_rho_sie(sp_table(e), double(rho), double(sie), lam));
+  if (is_spiner_sie(e)) return T(ss_gamma_from_rho_sie(ss_table(e), double(rho), double(sie), lam));
   return eos_gamma<T>(e, rho);
 }
 template <typename T> SGX_HD T md_min_sie(const sgx_eos &e, T rho) {
   if (is_spiner(e)) return T(sp_min_sie(sp_table(e), double(rho)));
+  if (is_spiner_sie(e)) return T(ss_min_sie(ss_table(e), double(rho)));
   return eos_min_sie<T>(e, rho);
 }
 
 // Bounds (eos_base.hpp:594-613; SpinerEOSDependsRhoT :241-246, :1117-1123)
 SGX_HD double md_min_temperature(const sgx_eos &e) {
   if (is_spiner(e)) return sp_T(sp_table(e), sp_table(e).lTMin);
+  if (is_spiner_sie(e)) return from_log(ss_table(e).gT.min, ss_table(e).lTOffset);
   return eos_min_temperature(e);
 }
 SGX_HD double md_max_density(const sgx_eos &e) {
   if (is_spiner(e)) return sp_table(e).rhoMax;
+  if (is_spiner_sie(e)) return ss_table(e).rhoMax;
   return eos_max_density(e);
 }
 SGX_HD double md_min_density(const sgx_eos &e) {
   if (is_spiner(e)) return sp_rho(sp_table(e), sp_table(e).lRhoMin);
+  if (is_spiner_sie(e)) return from_log(ss_table(e).lRhoMin, ss_table(e).lRhoOffset);
   return 0;
 }
 // The temperature ValuesAtReferenceState reports (eos_ideal.hpp:178-190,
@@ -107,6 +127,7 @@ SGX_HD double md_min_density(const sgx_eos &e) {
 // eos_gruneisen.hpp:554-567: T0; eos_spiner_rho_temp.hpp:1104-1115: TNormal_).
 SGX_HD double md_reference_T(const sgx_eos &e) {
   if (is_spiner(e)) return sp_table(e).TNormal;
+  if (is_spiner_sie(e)) return ss_table(e).TNormal;
   if (e.type == SGX_GRUNEISEN) return e.p[7];
   if (e.type == SGX_STIFF_GAS || e.type == SGX_NOBLE_ABEL) return e.p[pi::rT0];
   return ROOM_TEMPERATURE;
@@ -157,25 +178,39 @@ SGX_HDI void md_reference_state(const sgx_eos &e, double &rho, double &temp, dou
     bmod = t.bModNormal;
     return;
   }
+  case SGX_SPINER_RHOSIE: {
+    const SieTable &t = ss_table(e);
+    rho = t.rhoNormal;
+    temp = t.TNormal;
+    press = t.PNormal;
+    bmod = t.bModNormal;
+    return;
+  }
   }
   rho = temp = press = bmod = 0.0;
 }
 SGX_HD double md_rho_pmin(const sgx_eos &e, const double T) {
   if (is_spiner(e)) return sp_rho_pmin(sp_table(e), T);
+  if (is_spiner_sie(e)) return ss_rho_pmin(ss_table(e), T);
   return eos_rho_pmin(e, T);
 }
 SGX_HD double md_min_pressure(const sgx_eos &e) {
   if (is_spiner(e)) return sp_table(e).PMin;
+  if (is_spiner_sie(e)) return ss_table(e).PMin;
   return eos_min_pressure(e);
 }
 SGX_HDI double md_max_pressure_at_T(const sgx_eos &e, const double T, int *err) {
-  if (is_spiner(e)) return 1e100;
+  if (is_spiner(e) || is_spiner_sie(e)) return 1e100;
   return eos_max_pressure_at_T(e, T, err);
 }
 SGX_HDI void md_rho_sie_from_PT(const sgx_eos &e, const double P, const double T, double &rho,
                                 double &sie, double *lam, int *err) {
   if (is_spiner(e)) {
     sp_rho_sie_from_PT(sp_table(e), P, T, rho, sie, lam);
+    return;
+  }
+  if (is_spiner_sie(e)) {
+    ss_rho_sie_from_PT(ss_table(e), P, T, rho, sie, lam);
     return;
   }
   eos_rho_sie_from_PT(e, P, T, rho, sie, err);
@@ -186,6 +221,7 @@ SGX_HDI void md_rho_sie_from_PT(const sgx_eos &e, const double P, const double T
 //   IdealGas  eos_ideal.hpp:236-262     StiffGas  eos_stiff.hpp:203-229
 //   NobleAbel eos_noble_abel.hpp:216-242  Gruneisen eos_gruneisen.hpp:527-546
 //   SpinerEOSDependsRhoT eos_spiner_rho_temp.hpp:1052-1101
+//   SpinerEOSDependsRhoSie eos_spiner_rho_sie.hpp:844-898
 SGX_HDI void md_fill(const sgx_eos &e, double &rho, double &temp, double &sie, double &press,
                      double &cv, double &bmod, const unsigned output, double *lam, int *err) {
   const double gm1 = e.p[pi::gm1];
@@ -277,6 +313,43 @@ SGX_HDI void md_fill(const sgx_eos &e, double &rho, double &temp, double &sie, d
     if (lam != nullptr) {
       lam[0] = lRho;
       lam[1] = lT;
+    }
+    return;
+  }
+  case SGX_SPINER_RHOSIE: {
+    // SpinerEOSDependsRhoSie::FillEos (eos_spiner_rho_sie.hpp:844-898):
+    // outputs other than rho need T or sie among the outputs, which picks
+    // the grid they come from
+    const SieTable &t = ss_table(e);
+    if (output == 0 || ((output & Q_TEMPERATURE) && (output & Q_SIE))) {
+      *err = 1;
+      return;
+    }
+    double lRho;
+    if (output & Q_DENSITY) {
+      if ((output & Q_PRESSURE) || (output & Q_TEMPERATURE)) {
+        *err = 1;
+        return;
+      }
+      lRho = ss_lRho_from_P_lT(t, press, ss_lT(t, temp), lam);
+      rho = from_log(lRho, t.lRhoOffset);
+    } else {
+      lRho = ss_lRho(t, rho);
+      if (lam != nullptr) lam[0] = lRho;
+    }
+    if (output & Q_TEMPERATURE) {
+      const double lE = ss_lE(t, sie);
+      temp = se_interp(t, SE_T, lRho, lE);
+      if (output & Q_PRESSURE) press = se_interp(t, SE_P, lRho, lE);
+      if (output & Q_CV) cv = 1. / se_interp(t, SE_DTDE, lRho, lE);
+      if (output & Q_BMOD) bmod = se_interp(t, SE_BMOD, lRho, lE);
+    }
+    if (output & Q_SIE) {
+      const double lT = ss_lT(t, temp);
+      sie = st_interp(t, ST_SIE, lRho, lT);
+      if (output & Q_PRESSURE) press = st_interp(t, ST_P, lRho, lT);
+      if (output & Q_CV) cv = 1. / st_interp(t, ST_DTDE, lRho, lT);
+      if (output & Q_BMOD) bmod = st_interp(t, ST_BMOD, lRho, lT);
     }
     return;
   }

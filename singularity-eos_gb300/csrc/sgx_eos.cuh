@@ -152,10 +152,11 @@ SGX_HDN void gru_rho_sie_from_PT(const sgx_eos &e, const double press, const dou
 // Scalar member functions, dispatched on the model code.
 
 SGX_HD unsigned preferred_input(const sgx_eos &e) {
-  // IdealGas prefers pressure too (eos_ideal.hpp:227-229); the tabulated rho-T
-  // model prefers rho, T (eos_spiner_rho_temp.hpp:182-183); the others rho, sie.
+  // IdealGas prefers pressure too (eos_ideal.hpp:227-229); the tabulated
+  // models prefer rho, T (eos_spiner_rho_temp.hpp:182-183,
+  // eos_spiner_rho_sie.hpp:350-351); the others rho, sie.
   if (e.type == SGX_IDEAL_GAS) return Q_DENSITY | Q_SIE | Q_TEMPERATURE | Q_PRESSURE;
-  if (e.type == SGX_SPINER_RHOT) return Q_DENSITY | Q_TEMPERATURE;
+  if (e.type == SGX_SPINER_RHOT || e.type == SGX_SPINER_RHOSIE) return Q_DENSITY | Q_TEMPERATURE;
   return Q_DENSITY | Q_SIE;
 }
 

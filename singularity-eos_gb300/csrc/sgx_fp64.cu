@@ -49,6 +49,28 @@ __global__ void eval_kernel(const EvalArgs a) {
   }
 }
 
+// The bounds introspection members (eos_base.hpp:533-560 and the models'
+// overrides), one value per element; x is the temperature of
+// MaximumPressureAtTemperature and RhoPmin, unused by the others.
+__global__ void bounds_kernel(const sgx_eos e, const int what, const long long n,
+                              const double *x, double *out) {
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += stride) {
+    int err = 0;
+    double v = 0.0;
+    switch (what) {
+    case SGX_BOUND_MIN_DENSITY: v = ev_min_density(e); break;
+    case SGX_BOUND_MIN_TEMPERATURE: v = ev_min_temperature(e); break;
+    case SGX_BOUND_MAX_DENSITY: v = ev_max_density(e); break;
+    case SGX_BOUND_MIN_PRESSURE: v = ev_min_pressure(e); break;
+    case SGX_BOUND_MAX_PRESSURE_AT_T: v = ev_max_pressure_at_T(e, x[i], &err); break;
+    default: v = ev_rho_pmin(e, x[i]); break;
+    }
+    out[i] = v;
+  }
+}
+
 __global__ void fill_kernel(const FillArgs a) {
   const sgx_eos e = a.eos;
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
@@ -215,6 +237,13 @@ cudaError_t launch_pte_fp64(const PteArgs &a, cudaStream_t stream) {
                            reinterpret_cast<int *>(static_cast<char *>(scratch) + nb), stream);
   const cudaError_t f = scratch_free(scratch, stream);
   return e != cudaSuccess ? e : f;
+}
+
+cudaError_t launch_bounds_fp64(const sgx_eos &e, const int what, const long long n,
+                               const double *x, double *out, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  bounds_kernel<<<grid_for(n, 256), 256, 0, stream>>>(e, what, n, x, out);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_eval_fp64(const EvalArgs &a, cudaStream_t stream) {

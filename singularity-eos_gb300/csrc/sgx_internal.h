@@ -11,6 +11,10 @@
 namespace sgx {
 
 constexpr int MAX_EOS = 16;
+// Models the PTE solvers evaluate (Helmholtz is a lookup-only model here).
+inline bool pte_model(const int t) {
+  return (t >= SGX_IDEAL_GAS && t <= SGX_SPINER_RHOT) || t == SGX_SPINER_RHOSIE;
+}
 constexpr int MAX_NMAT = 8;  // material slots per cell
 constexpr int PTE_MAX_N = 6; // materials present per cell (Jacobian up to 6x6)
 
@@ -103,6 +107,8 @@ struct EvalArgs {
   int lambda_stride;
 };
 cudaError_t launch_eval_fp64(const EvalArgs &a, cudaStream_t stream);
+cudaError_t launch_bounds_fp64(const sgx_eos &e, int what, long long n, const double *x,
+                               double *out, cudaStream_t stream);
 
 struct FillArgs {
   sgx_eos eos;

@@ -185,7 +185,7 @@ int check_common(const char *who, int nmat, int64_t ncell, const sgx_eos *eos_li
     if (!eos_idx && neos < nmat)
       return set_error(SGX_ERR_INVALID, std::string(who) + ": eos_idx NULL needs neos >= nmat");
     for (int k = 0; k < neos; ++k)
-      if (eos_list[k].type < SGX_IDEAL_GAS || eos_list[k].type > SGX_SPINER_RHOT)
+      if (!pte_model(eos_list[k].type))
         return set_error(SGX_ERR_UNSUPPORTED, std::string(who) + ": EOS type not available");
   }
   return SGX_OK;

@@ -414,7 +414,7 @@ int sgx_server_create(const sgx_server_config *cfg, sgx_server **out) {
   if (cfg->precision == SGX_PREC_MIXED && cfg->solver != SGX_PTE_RHOT)
     return set_error(SGX_ERR_UNSUPPORTED, "sgx_server_create: mixed precision is RhoT only");
   for (int k = 0; k < cfg->neos; ++k)
-    if (cfg->eos_list[k].type < SGX_IDEAL_GAS || cfg->eos_list[k].type > SGX_SPINER_RHOT)
+    if (!sgx::pte_model(cfg->eos_list[k].type))
       return set_error(SGX_ERR_UNSUPPORTED, "sgx_server_create: EOS not available in PTE");
     else if (const int rc = sgx::check_eos_mods(cfg->eos_list[k],
                                                 cfg->precision == SGX_PREC_MIXED,

@@ -103,6 +103,17 @@ int sgx_init_sg_SpinerDependsRhoT(int matindex, sgx_eos *eos, const char *filena
   return finish_init(sgx_eos_spiner_rhot(&e, filename, id, 0), matindex, eos, e, enabled, vals);
 }
 
+int sgx_init_sg_SpinerDependsRhoSie(int matindex, sgx_eos *eos, const char *filename, int id,
+                                    int split, const int *enabled, double *vals) {
+  static const char *who = "sgx_init_sg_SpinerDependsRhoSie";
+  if (const int rc = check_slot(matindex, eos, who)) return rc;
+  if (split != 0)
+    return sgx::set_error(SGX_ERR_UNSUPPORTED, std::string(who) + ": only TableSplit::Total");
+  sgx_eos e;
+  return finish_init(sgx_eos_spiner_rhosie(&e, filename, id, 0), matindex, eos, e, enabled,
+                     vals);
+}
+
 int sgx_init_sg_Helmholtz(int matindex, sgx_eos *eos, const char *filename, int rad, int gas,
                           int coul, int ion, int ele, int verbose, const int *enabled,
                           double *vals) {

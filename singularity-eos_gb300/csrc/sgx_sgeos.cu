@@ -307,7 +307,7 @@ extern "C" int sgx_get_sg_eos_device(int nmat, int ncell, int cell_dim, int inpu
   a.neos = neos;
   a.mode = input_int;
   for (int k = 0; k < neos; ++k) {
-    if (eos[k].type < SGX_IDEAL_GAS || eos[k].type > SGX_SPINER_RHOT)
+    if (!pte_model(eos[k].type))
       return set_error(SGX_ERR_UNSUPPORTED, "sgx_get_sg_eos_device: EOS not available in PTE");
     if (const int rc = check_eos_mods(eos[k], precision == SGX_PREC_MIXED, "sgx_get_sg_eos_device"))
       return rc;

@@ -35,6 +35,7 @@
 #include "../../include/sgx.h"
 #include "sgx_helm.cuh"
 #include "sgx_spiner.cuh"
+#include "sgx_spiner_sie.cuh"
 #include "sgx_table.h"
 
 namespace sgx {
@@ -637,6 +638,259 @@ int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *
     std::lock_guard<std::mutex> lk(g_mu);
     g_tables[key] = std::move(r);
     g_tables[key].host.bind();
+  }
+  *handle = key;
+  return SGX_OK;
+}
+
+// SpinerEOSDependsRhoSie::loadDataboxes_ (eos/eos_spiner_rho_sie.hpp:433-552)
+// and calcBMod_ (:554-578): both groups' tables, the bulk moduli recomputed
+// from P, dP/drho|e, dP/de|rho and de/drho|T at the nodes, the slices of P
+// and dP/drho at the densest row, SetRhoPMin (eos_spiner_common.hpp:59-109,
+// without vapor-dome exclusion) and the reference state. The reference's
+// DataBox dump order (DBLIST, :329-336) is kept for parity checks.
+int table_load_spiner_sie(const char *path, int matid, bool reproducible, uint64_t *handle,
+                          std::string &msg) {
+  Sp5 s;
+  if (!read_sp5(path, s, msg)) return SGX_ERR_IO;
+  const int lt = s.i32.count("/@log_type") ? s.i32["/@log_type"] : 1;
+  if (lt != 2) {
+    msg = "sp5-lite image was written with a log type other than NQT order 2";
+    return SGX_ERR_IO;
+  }
+  const std::string mat = "/" + std::to_string(matid);
+  // one group's tables, all of one shape; names in the order loadDataboxes_
+  // reads them (the first is sie_ / T_)
+  struct Group {
+    std::vector<std::vector<double>> f;
+    Grid1D gx, gr;
+    int nx = 0, nr = 0;
+  };
+  auto load_group = [&](const std::string &g, const char *const *names, int count, Group &out) {
+    out.f.resize(count);
+    for (int k = 0; k < count; ++k) {
+      auto it = s.ds.find(g + names[k]);
+      if (it == s.ds.end() || it->second.n.size() != 2) {
+        msg = "missing 2-D field " + g + names[k];
+        return false;
+      }
+      const Dataset &d = it->second;
+      if (k == 0) {
+        out.nx = d.n[0];
+        out.nr = d.n[1];
+        out.gx = make_grid(d.mn[0], d.mx[0], out.nx);
+        out.gr = make_grid(d.mn[1], d.mx[1], out.nr);
+      } else if (d.n[0] != out.nx || d.n[1] != out.nr || d.mn[0] != out.gx.min ||
+                 d.mx[0] != out.gx.max || d.mn[1] != out.gr.min || d.mx[1] != out.gr.max) {
+        msg = "inconsistent 2-D field grids in " + g;
+        return false;
+      }
+      out.f[k] = d.data;
+    }
+    return true;
+  };
+  // 0 sie or T, then P, bMod, dPdRho, dPdE, dTdRho, dTdE, dEdRho
+  enum { G_X = 0, G_P, G_BMOD, G_DPDRHO, G_DPDE, G_DTDRHO, G_DTDE, G_DEDRHO, G_N };
+  const char *namesT[G_N] = {"specific internal energy", "pressure", "bulk modulus", "dPdRho",
+                             "dPdE", "dTdRho", "dTdE", "dEdRho"};
+  const char *namesE[G_N] = {"temperature", "pressure", "bulk modulus", "dPdRho",
+                             "dPdE", "dTdRho", "dTdE", "dEdRho"};
+  Group gt, ge;
+  if (!load_group(mat + "/dependsLogRhoLogT/", namesT, G_N, gt) ||
+      !load_group(mat + "/dependsLogRhoLogSie/", namesE, G_N, ge))
+    return SGX_ERR_IO;
+  const std::string cg = mat + "/coldCurve/";
+  const char *namesc[4] = {"pressure", "specific internal energy", "bulk modulus", "dPdRho"};
+  std::vector<double> cold[4];
+  Grid1D gCold{};
+  for (int k = 0; k < 4; ++k) {
+    auto it = s.ds.find(cg + namesc[k]);
+    if (it == s.ds.end() || it->second.n.size() != 1) {
+      msg = "missing cold-curve field " + cg + namesc[k];
+      return SGX_ERR_IO;
+    }
+    if (k == 1) gCold = make_grid(it->second.mn[0], it->second.mx[0], it->second.n[0]);
+    cold[k] = it->second.data;
+  }
+  auto attr = [&](const char *name, double &v) {
+    auto it = s.f64.find(mat + "@" + name);
+    if (it == s.f64.end()) return false;
+    v = it->second;
+    return true;
+  };
+  double rOff = 0, tOff = 0, eOff = 0, rhoNormal = 0, abar = 0, zbar = 0;
+  if (!attr("rhoOffset", rOff) || !attr("TOffset", tOff) || !attr("sieOffset", eOff) ||
+      !attr("normalDensity", rhoNormal) || !attr("meanAtomicMass", abar) ||
+      !attr("meanAtomicNumber", zbar)) {
+    msg = "missing offsets or material attributes on " + mat;
+    return SGX_ERR_IO;
+  }
+  SieTable t;
+  std::memset(&t, 0, sizeof(t));
+  t.lRhoOffset = std::fabs(rOff);
+  t.lTOffset = std::fabs(tOff);
+  t.lEOffset = std::fabs(eOff);
+  t.gT = gt.gx;
+  t.gRhoT = gt.gr;
+  t.gE = ge.gx;
+  t.gRhoE = ge.gr;
+  t.gCold = gCold;
+  t.nT = gt.nx;
+  t.nRhoT = gt.nr;
+  t.nE = ge.nx;
+  t.nRhoE = ge.nr;
+  t.reproducible = reproducible ? 1 : 0;
+  // calcBMod_ on each group
+  for (Group *g : {&gt, &ge}) {
+    for (int j = 0; j < g->nr; j++) {
+      const double lRho = g->gr.x(j);
+      const double rho = from_log(lRho, t.lRhoOffset);
+      for (int i = 0; i < g->nx; i++) {
+        const size_t k = static_cast<size_t>(j) * g->nx + i;
+        const double press = g->f[G_P][k];
+        const double DPDR_E = g->f[G_DPDRHO][k];
+        const double DPDE_R = g->f[G_DPDE][k];
+        const double DEDR_T = g->f[G_DEDRHO][k];
+        const double DPDR_T = DPDR_E + DPDE_R * DEDR_T;
+        double bMod;
+        if (DPDE_R > 0.0 && rho > 0.0)
+          bMod = rho * DPDR_E + DPDE_R * (press / rho);
+        else if (rho > 0.0)
+          bMod = smax(rho * DPDR_T, 0.0);
+        else
+          bMod = 0.0;
+        g->f[G_BMOD][k] = smax(bMod, lim<double>::eps);
+      }
+    }
+  }
+  const int nR = gt.nr, nT = gt.nx;
+  t.lRhoMin = gt.gr.min;
+  t.lRhoMax = gt.gr.max;
+  t.rhoMax = from_log(t.lRhoMax, t.lRhoOffset);
+  // the densest row of P and dP/drho|e on the rho-T grid
+  std::vector<double> PlRhoMax(gt.f[G_P].begin() + static_cast<size_t>(nR - 1) * nT,
+                               gt.f[G_P].begin() + static_cast<size_t>(nR) * nT);
+  std::vector<double> dPdRhoMax(gt.f[G_DPDRHO].begin() + static_cast<size_t>(nR - 1) * nT,
+                                gt.f[G_DPDRHO].begin() + static_cast<size_t>(nR) * nT);
+  // SetRhoPMin without vapor-dome exclusion
+  std::vector<double> rho_at_pmin(nT, 0.0);
+  double PMin = DBL_MAX;
+  for (int i = 0; i < nT; ++i) {
+    double PMin_at_T = DBL_MAX;
+    int jmax = 0;
+    for (int j = 0; j < nR; ++j) {
+      const double p = gt.f[G_P][static_cast<size_t>(j) * nT + i];
+      if (p < PMin_at_T) {
+        PMin_at_T = p;
+        jmax = j;
+      }
+    }
+    if (PMin_at_T > 0) {
+      rho_at_pmin[i] = 0;
+      PMin_at_T = 0;
+    } else {
+      rho_at_pmin[i] = from_log(gt.gr.x(jmax), t.lRhoOffset);
+    }
+    PMin = smin(PMin_at_T, PMin);
+  }
+  t.PMin = PMin;
+  // reference state (:526-548)
+  rhoNormal = std::fabs(rhoNormal);
+  double lRhoNormal = to_log(rhoNormal, t.lRhoOffset);
+  if (!(t.lRhoMin < lRhoNormal && lRhoNormal < t.lRhoMax)) {
+    lRhoNormal = 0.5 * (t.lRhoMin + t.lRhoMax);
+    rhoNormal = from_log(lRhoNormal, t.lRhoOffset);
+  }
+  double TNormal = ROOM_TEMPERATURE;
+  double lTNormal = to_log(TNormal, t.lTOffset);
+  const double lTMin = gt.gx.min, lTMax = gt.gx.max;
+  if (!(lTMin < lTNormal && lTNormal < lTMax)) {
+    lTNormal = 0.5 * (lTMin + lTMax);
+    TNormal = from_log(lTNormal, t.lTOffset);
+  }
+  auto at = [&](const std::vector<double> &f) {
+    return sie_interp2(gt.gx, gt.gr, nT, f.data(), lRhoNormal, lTNormal);
+  };
+  t.rhoNormal = rhoNormal;
+  t.TNormal = TNormal;
+  t.sieNormal = at(gt.f[G_X]);
+  t.PNormal = at(gt.f[G_P]);
+  t.CvNormal = 1. / at(gt.f[G_DTDE]);
+  t.bModNormal = at(gt.f[G_BMOD]);
+  t.dPdENormal = at(gt.f[G_DPDE]);
+  const double dPdR = at(gt.f[G_DPDRHO]);
+  t.dVdTNormal = t.dPdENormal * t.CvNormal / (t.rhoNormal * t.rhoNormal * dPdR);
+
+  // ---- device image ----
+  auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+  const int srcT[NST2D] = {G_X, G_P, G_BMOD, G_DPDE, G_DTDE};
+  const int srcE[NSE2D] = {G_X, G_P, G_BMOD, G_DPDE, G_DTDE};
+  size_t off = align(sizeof(SieTable));
+  size_t offT[NST2D], offE[NSE2D];
+  for (int k = 0; k < NST2D; ++k) {
+    offT[k] = off;
+    off = align(off + gt.f[srcT[k]].size() * 8);
+  }
+  for (int k = 0; k < NSE2D; ++k) {
+    offE[k] = off;
+    off = align(off + ge.f[srcE[k]].size() * 8);
+  }
+  const std::vector<double> *one[4] = {&cold[1], &PlRhoMax, &dPdRhoMax, &rho_at_pmin};
+  size_t off1[4];
+  for (int k = 0; k < 4; ++k) {
+    off1[k] = off;
+    off = align(off + one[k]->size() * 8);
+  }
+  const size_t bytes = off;
+  std::vector<unsigned char> img(bytes, 0);
+  for (int k = 0; k < NST2D; ++k)
+    std::memcpy(img.data() + offT[k], gt.f[srcT[k]].data(), gt.f[srcT[k]].size() * 8);
+  for (int k = 0; k < NSE2D; ++k)
+    std::memcpy(img.data() + offE[k], ge.f[srcE[k]].data(), ge.f[srcE[k]].size() * 8);
+  for (int k = 0; k < 4; ++k)
+    std::memcpy(img.data() + off1[k], one[k]->data(), one[k]->size() * 8);
+  void *dev = nullptr;
+  cudaError_t e = cudaMalloc(&dev, bytes);
+  if (e != cudaSuccess) {
+    msg = std::string("cudaMalloc of table: ") + cudaGetErrorString(e);
+    return SGX_ERR_CUDA;
+  }
+  unsigned char *d = static_cast<unsigned char *>(dev);
+  SieTable td = t;
+  for (int k = 0; k < NST2D; ++k)
+    td.fT[k] = reinterpret_cast<const double *>(d + offT[k]);
+  for (int k = 0; k < NSE2D; ++k)
+    td.fE[k] = reinterpret_cast<const double *>(d + offE[k]);
+  td.sieCold = reinterpret_cast<const double *>(d + off1[0]);
+  td.PlRhoMax = reinterpret_cast<const double *>(d + off1[1]);
+  td.dPdRhoMax = reinterpret_cast<const double *>(d + off1[2]);
+  td.rho_at_pmin = reinterpret_cast<const double *>(d + off1[3]);
+  std::memcpy(img.data(), &td, sizeof(td));
+  e = cudaMemcpy(dev, img.data(), bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(dev);
+    msg = std::string("cudaMemcpy of table: ") + cudaGetErrorString(e);
+    return SGX_ERR_CUDA;
+  }
+  Resident r;
+  r.dev = dev;
+  r.bytes = bytes;
+  cudaGetDevice(&r.device);
+  // DBLIST: sie_, T_, rho_at_pmin_, the rho-T tables, the rho-sie tables,
+  // mF_ (none), PlRhoMax_, dPdRhoMax_, PCold_, sieCold_, bModCold_, dPdRhoCold_
+  std::vector<const std::vector<double> *> order = {&gt.f[G_X], &ge.f[G_X], &rho_at_pmin};
+  for (Group *g : {&gt, &ge})
+    for (int k = G_P; k < G_N; ++k)
+      order.push_back(&g->f[k]);
+  for (const std::vector<double> *v : {&PlRhoMax, &dPdRhoMax, &cold[0], &cold[1], &cold[2],
+                                       &cold[3]})
+    order.push_back(v);
+  for (const std::vector<double> *v : order)
+    r.dump.insert(r.dump.end(), v->begin(), v->end());
+  const uint64_t key = reinterpret_cast<uint64_t>(dev);
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_tables[key] = std::move(r);
   }
   *handle = key;
   return SGX_OK;

@@ -12,6 +12,10 @@ namespace sgx {
 // device. *handle receives the device address of the table header.
 int table_load_spiner(const char *path, int matid, bool reproducible, uint64_t *handle,
                       std::string &msg);
+// Loads /<matid>/dependsLogRhoLogT, /<matid>/dependsLogRhoLogSie and
+// /<matid>/coldCurve for SpinerEOSDependsRhoSie and uploads its image.
+int table_load_spiner_sie(const char *path, int matid, bool reproducible, uint64_t *handle,
+                          std::string &msg);
 // Loads a Helmholtz electron free-energy table (the reference's ASCII
 // helm_table.dat layout) and uploads the per-cell Hermite records.
 int table_load_helm(const char *path, uint64_t *handle, std::string &msg);

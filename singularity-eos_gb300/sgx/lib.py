@@ -10,7 +10,9 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(os.path.dirname(HERE), "lib", "libsgx.so")
 
-IDEAL_GAS, STIFF_GAS, NOBLE_ABEL, GRUNEISEN, SPINER_RHOT, HELMHOLTZ = 1, 2, 3, 4, 5, 6
+IDEAL_GAS, STIFF_GAS, NOBLE_ABEL, GRUNEISEN, SPINER_RHOT, HELMHOLTZ, SPINER_RHOSIE = 1, 2, 3, 4, 5, 6, 7
+(BOUND_MIN_DENSITY, BOUND_MIN_TEMPERATURE, BOUND_MAX_DENSITY, BOUND_MIN_PRESSURE,
+ BOUND_MAX_PRESSURE_AT_T, BOUND_RHO_PMIN) = range(6)
 Q_DENSITY, Q_SIE, Q_PRESSURE, Q_TEMPERATURE, Q_SPECIFIC_HEAT, Q_BULK_MODULUS = 1, 2, 4, 8, 16, 32
 (FN_T_FROM_RHO_SIE, FN_SIE_FROM_RHO_T, FN_P_FROM_RHO_T, FN_P_FROM_RHO_SIE, FN_CV_FROM_RHO_T,
  FN_CV_FROM_RHO_SIE, FN_B_FROM_RHO_T, FN_B_FROM_RHO_SIE, FN_G_FROM_RHO_T, FN_G_FROM_RHO_SIE,
@@ -23,9 +25,10 @@ PREC_FP64, PREC_MIXED = 0, 1
 
 EXPORTED = [
     "sgx_version", "sgx_last_error", "sgx_eos_ideal_gas", "sgx_eos_stiff_gas",
-    "sgx_eos_noble_abel", "sgx_eos_gruneisen", "sgx_eos_spiner_rhot", "sgx_eos_finalize",
+    "sgx_eos_noble_abel", "sgx_eos_gruneisen", "sgx_eos_spiner_rhot", "sgx_eos_spiner_rhosie",
+    "sgx_eos_finalize",
     "sgx_eos_table_bytes", "sgx_eos_spiner_dump", "sgx_eos_eval", "sgx_eos_fill",
-    "sgx_eos_fill_ex",
+    "sgx_eos_fill_ex", "sgx_eos_bounds",
     "sgx_mix_params_default", "sgx_pte_rhot_required_scratch", "sgx_pte_pt_required_scratch",
     "sgx_pte_fixed_t_required_scratch", "sgx_pte_fixed_p_required_scratch",
     "sgx_pte_rhou_required_scratch", "sgx_pte_approx_temperature",
@@ -39,6 +42,7 @@ EXPORTED = [
     "sgx_eos_pt_derivatives", "sgx_eos_ideal_gas_entropy", "sgx_eos_stiff_gas_ref",
     "sgx_eos_noble_abel_ref", "sgx_init_sg_eos", "sgx_init_sg_IdealGas", "sgx_init_sg_StiffGas",
     "sgx_init_sg_NobleAbel", "sgx_init_sg_Gruneisen", "sgx_init_sg_SpinerDependsRhoT",
+    "sgx_init_sg_SpinerDependsRhoSie",
     "sgx_init_sg_Helmholtz", "sgx_get_sg_EntropyFromDensityInternalEnergy",
     "sgx_get_sg_PressureFromDensityInternalEnergy", "sgx_get_sg_MinInternalEnergyFromDensity",
     "sgx_get_sg_BulkModulusFromDensityInternalEnergy", "sgx_finalize_sg_eos",
@@ -129,6 +133,8 @@ def load():
     lib.sgx_eos_noble_abel_ref.argtypes = [C.POINTER(SgxEos)] + [D] * 7
     lib.sgx_eos_gruneisen.argtypes = [C.POINTER(SgxEos)] + [D] * 11
     lib.sgx_eos_spiner_rhot.argtypes = [C.POINTER(SgxEos), C.c_char_p, I, I]
+    lib.sgx_eos_spiner_rhosie.argtypes = [C.POINTER(SgxEos), C.c_char_p, I, I]
+    lib.sgx_eos_bounds.argtypes = [C.POINTER(SgxEos), I, C.c_int64, P, P, P]
     lib.sgx_eos_finalize.argtypes = [C.POINTER(SgxEos)]
     lib.sgx_eos_table_bytes.argtypes = [C.POINTER(SgxEos)]
     lib.sgx_eos_table_bytes.restype = C.c_size_t
@@ -181,6 +187,7 @@ def load():
     lib.sgx_init_sg_NobleAbel.argtypes = [I, PE, D, D, D, D, P, P]
     lib.sgx_init_sg_Gruneisen.argtypes = [I, PE] + [D] * 10 + [P, P]
     lib.sgx_init_sg_SpinerDependsRhoT.argtypes = [I, PE, C.c_char_p, I, I, P, P]
+    lib.sgx_init_sg_SpinerDependsRhoSie.argtypes = [I, PE, C.c_char_p, I, I, P, P]
     lib.sgx_init_sg_Helmholtz.argtypes = [I, PE, C.c_char_p, I, I, I, I, I, I, P, P]
     for name in ("Entropy", "Pressure", "BulkModulus"):
         getattr(lib, f"sgx_get_sg_{name}FromDensityInternalEnergy").argtypes = [
@@ -249,6 +256,15 @@ def spiner_eos(path, matid, reproducible=False):
     return e
 
 
+def spiner_rhosie_eos(path, matid, reproducible=False):
+    """SpinerEOSDependsRhoSie from an sp5-lite image with rho-T and rho-sie
+    groups (sp5lite.rhosie_table writes one)."""
+    lib = load()
+    e = SgxEos()
+    check(lib.sgx_eos_spiner_rhosie(C.byref(e), path.encode(), int(matid), int(reproducible)))
+    return e
+
+
 def helmholtz_eos(path, options=HELM_DEFAULT):
     lib = load()
     e = SgxEos()
@@ -312,6 +328,13 @@ def eval_eos(eos, fn, in1, in2, out, lam=None, lam_stride=0, stream=None):
     n = in1.numel()
     check(load().sgx_eos_eval(C.byref(eos), fn, n, ptr(in1), ptr(in2), ptr(out), ptr(lam),
                               lam_stride, stream_ptr(stream)))
+
+
+def eos_bounds(eos, what, out, temp=None, stream=None):
+    """out[i] = the model's bound `what` (BOUND_*), at temp[i] for the
+    temperature-dependent two."""
+    check(load().sgx_eos_bounds(C.byref(eos), int(what), out.numel(), ptr(temp), ptr(out),
+                                stream_ptr(stream)))
 
 
 def fill_eos(eos, rho, temp, sie, press, cv, bmod, output, lam=None, lam_stride=0, stream=None,

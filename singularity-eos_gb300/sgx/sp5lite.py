@@ -142,6 +142,94 @@ def stiffgas_table(fname, matid=1, nrho=256, nt=256, rho_range=(1e-4, 1e2),
                 rho_range=rho_range, t_range=t_range)
 
 
+def rhosie_table(fname, matid=3, nrho=64, nt=96, ne=80, rho_range=(1e-3, 1e1),
+                 t_range=(1e2, 1e5), gm1=3.4, Cv=1.816e7, Pinf=6e9, qq=0.0,
+                 sie_offset=1e9, rho_offset=0.0):
+    """Writes a SpinerEOSDependsRhoSie-layout table sampled from the StiffGas
+    model: the rho-T group (as stiffgas_table), the rho-sie group on an NQT
+    grid of log10(sie + sie_offset) spanning the energies the rho-T group
+    reaches, and the cold curve. Below a row's cold energy the rho-sie
+    group's temperature is floored at 1 K (the pressure keeps the model's
+    formula). Returns a dict with the grids and model parameters."""
+    lr = grid(to_log(rho_range[0], rho_offset), to_log(rho_range[1], rho_offset), nrho)
+    lt = grid(to_log(t_range[0]), to_log(t_range[1]), nt)
+    rho1 = pow10_nqt(lr) - rho_offset
+    rho = rho1[:, None]
+    T = pow10_nqt(lt)[None, :]
+    e_lo = Cv * t_range[0] + Pinf / rho_range[1] + qq
+    e_hi = Cv * t_range[1] + Pinf / rho_range[0] + qq
+    le = grid(to_log(e_lo, sie_offset), to_log(e_hi, sie_offset), ne)
+    E = (pow10_nqt(le) - sie_offset)[None, :]
+    ones_t = np.ones((nrho, nt))
+    ones_e = np.ones((nrho, ne))
+    sie_t = (rho * Cv * T + Pinf) / rho + qq
+    groups = {
+        "dependsLogRhoLogT": (lt, {
+            "pressure": gm1 * rho * Cv * T - Pinf,
+            "specific internal energy": sie_t,
+            "bulk modulus": gm1 * (gm1 + 1.0) * rho * Cv * T,
+            "dPdRho": gm1 * (sie_t - qq),
+            "dPdE": gm1 * rho * ones_t,
+            "dTdRho": Pinf / (rho * rho * Cv) * ones_t,
+            "dTdE": ones_t / Cv,
+            "dEdRho": -Pinf / (rho * rho) * ones_t,
+            "dEdT": Cv * ones_t}),
+        "dependsLogRhoLogSie": (le, {
+            "temperature": np.maximum((E - qq - Pinf / rho) / Cv, 1.0),
+            "pressure": gm1 * rho * (E - qq) - (gm1 + 1.0) * Pinf,
+            "bulk modulus": gm1 * (gm1 + 1.0) * rho * np.maximum(E - qq - Pinf / rho, 0.0),
+            "dPdRho": gm1 * (E - qq) * ones_e,
+            "dPdE": gm1 * rho * ones_e,
+            "dTdRho": Pinf / (rho * rho * Cv) * ones_e,
+            "dTdE": ones_e / Cv,
+            "dEdRho": -Pinf / (rho * rho) * ones_e}),
+    }
+    w = Writer()
+    w.attr_i32("/", "log_type", 2)
+    g = f"/{matid}"
+    for name, v in (("rhoOffset", rho_offset), ("TOffset", 0.0), ("sieOffset", sie_offset),
+                    ("normalDensity", 1.0), ("meanAtomicMass", 47.9),
+                    ("meanAtomicNumber", 22.0)):
+        w.attr_f64(g, name, v)
+    w.attr_i32(g, "matid", matid)
+    for grp, (fast, fields) in groups.items():
+        r2 = [(fast.size, fast[0], fast[-1]), (nrho, lr[0], lr[-1])]
+        for key, arr in fields.items():
+            w.dataset(f"{g}/{grp}/{key}", arr, r2)
+    r1g = [(nrho, lr[0], lr[-1])]
+    cold = {"pressure": np.full(nrho, -Pinf), "specific internal energy": Pinf / rho1 + qq,
+            "bulk modulus": np.full(nrho, SMALL), "dPdRho": gm1 * Pinf / rho1}
+    for key, arr in cold.items():
+        w.dataset(f"{g}/coldCurve/{key}", arr, r1g)
+    w.write(fname)
+    return dict(lrho=lr, lt=lt, le=le, gm1=gm1, Cv=Cv, Pinf=Pinf, qq=qq, matid=matid,
+                rho_range=rho_range, t_range=t_range, e_range=(e_lo, e_hi),
+                sie_offset=sie_offset, rho_offset=rho_offset)
+
+
+def rhosie_queries(n, seed=0, rho_range=(1e-3, 1e1), t_range=(1e2, 1e5), Cv=1.816e7,
+                   Pinf=6e9, qq=0.0, off_table=0.05):
+    """(rho, sie, T) queries for rhosie_table: rho log-uniform, T log-uniform,
+    sie uniform between the model's energies at the T range's ends; a
+    fraction off_table of the rows is pushed outside the table (density
+    beyond either end, energy below the cold curve or above the top)."""
+    rng = np.random.default_rng(seed)
+    rho = np.exp(rng.uniform(np.log(rho_range[0]), np.log(rho_range[1]), n))
+    T = np.exp(rng.uniform(np.log(t_range[0]), np.log(t_range[1]), n))
+    e_lo = Cv * t_range[0] + Pinf / rho + qq
+    e_hi = Cv * t_range[1] + Pinf / rho + qq
+    sie = e_lo + rng.random(n) * (e_hi - e_lo)
+    k = rng.random(n) < off_table
+    which = rng.integers(0, 4, n)
+    rho = np.where(k & (which == 0), rho * 1e-2, rho)
+    rho = np.where(k & (which == 1), rho * 1e2, rho)
+    sie = np.where(k & (which == 2), 0.5 * (Pinf / rho + qq), sie)
+    T = np.where(k & (which == 2), 0.3 * t_range[0], T)
+    sie = np.where(k & (which == 3), 3.0 * e_hi, sie)
+    T = np.where(k & (which == 3), 3.0 * t_range[1], T)
+    return rho, sie, T
+
+
 def stiffgas_queries(n, seed=0, rho_range=(1e-4, 1e2), t_range=(1e2, 1e6), gm1=3.4,
                      Cv=1.816e7, Pinf=6e9, qq=0.0):
     """Lookup queries: rho log-uniform over the table range, sie uniform

@@ -48,6 +48,18 @@ def bitwise_frac(a, b):
 _TABLE = {}
 
 
+def rhosie_table_path():
+    """The synthetic StiffGas rho-T / rho-sie table of SpinerEOSDependsRhoSie
+    (sp5lite.rhosie_table, matid 3), regenerated and cached for the session."""
+    if "rhosie" not in _TABLE:
+        from sgx import sp5lite
+        d = tempfile.mkdtemp(prefix="sgx_table_")
+        path = os.path.join(d, "rhosie.sp5")
+        sp5lite.rhosie_table(path)
+        _TABLE["rhosie"] = (path, hashlib.sha256(open(path, "rb").read()).hexdigest())
+    return _TABLE["rhosie"]
+
+
 def stiffgas_table_path():
     """The synthetic StiffGas rho-T table, regenerated deterministically and
     cached for the session; checked against the fixture's SHA-256."""

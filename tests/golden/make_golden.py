@@ -97,6 +97,48 @@ def spiner_fixture(ref, path, nq=4096, seed=5):
     return out
 
 
+def spiner_rhosie_fixture(ref, path, n=2048, seed=7):
+    """SpinerEOSDependsRhoSie on the StiffGas-sampled rho-T / rho-sie table:
+    the eleven vector functions and e(rho, P) with lambda rows of one entry,
+    FillEos from (rho, sie), from (rho, T) and from (P, T), the load-time
+    tables (DBLIST order), the scalars and the bounds."""
+    rho, sie, T = sp5lite.rhosie_queries(n, seed=seed)
+    d = rb.eos_desc(rb.SPINER_RHOSIE, [], path=path, matid=3)
+    out = dict(rho=rho, sie=sie, T=T)
+    for fn in ALL_FN + [13]:
+        second = T if fn in (1, 2, 4, 6, 8) else sie
+        if fn == 13:
+            second = ref.eos_vec(d, 3, rho, sie)  # P(rho, sie) as the target pressure
+            out["P_target"] = second
+        lam = np.full(n, np.nan)
+        out[f"fn{fn}"] = ref.eos_vec(d, fn, rho, second, lam=lam, lam_stride=1)
+        out[f"fn{fn}_lambda"] = lam
+    # FillEos: (rho, sie) -> T, P, cv, bmod; (rho, T) -> sie, P, cv, bmod;
+    # (P, T) -> rho, sie
+    fills = {"e": (Q_TPB, rb.Q_SIE), "t": (rb.Q_SIE | rb.Q_PRESSURE | rb.Q_SPECIFIC_HEAT |
+                                             rb.Q_BULK_MODULUS, rb.Q_TEMPERATURE),
+             "pt": (rb.Q_DENSITY | rb.Q_SIE, rb.Q_PRESSURE | rb.Q_TEMPERATURE)}
+    P_in = ref.eos_vec(d, 2, rho, T)
+    for tag, (q, _) in fills.items():
+        r, t, e, p, cv, bm = rho.copy(), T.copy(), sie.copy(), P_in.copy(), np.zeros(n), np.zeros(n)
+        lam = np.full(n, np.nan)
+        ref.fill_eos(d, r, t, e, p, cv, bm, q, lam=lam, lam_stride=1)
+        out.update({f"fill_{tag}_rho": r, f"fill_{tag}_T": t, f"fill_{tag}_sie": e,
+                    f"fill_{tag}_P": p, f"fill_{tag}_cv": cv, f"fill_{tag}_bmod": bm,
+                    f"fill_{tag}_lambda": lam, f"fill_{tag}_output": np.int64(q)})
+    out["P_in"] = P_in
+    dump, scal = ref.spiner_sie_dump(path, 3)
+    out["dump_sha256"] = np.array(hashlib.sha256(dump.tobytes()).hexdigest())
+    out["dump_len"] = np.int64(dump.size)
+    out["dump_sample"] = dump[::97].copy()
+    out["scal"] = scal
+    Tb = np.array([50.0, 300.0, 1e4, 1e6])
+    out["bounds_T"] = Tb
+    for w in range(6):
+        out[f"bound{w}"] = ref.eos_bounds(d, w, Tb)
+    return out
+
+
 def helm_fixture(ref, path, n=2048, seed=31):
     """Helmholtz EOS on the synthetic table, default options (all on): the
     forward FillEos, the vector member functions, the inversion as the
@@ -530,6 +572,29 @@ def main():
         fx["pt_derivs"]["table_sha256"] = np.array(sha)
         fx["eos_vector_ext"] = vector_ext_fixture(ref, path)
         fx["eos_vector_ext"]["table_sha256"] = np.array(sha)
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "rhosie.sp5")
+        sp5lite.rhosie_table(path)
+        sha = hashlib.sha256(open(path, "rb").read()).hexdigest()
+        fx["spiner_rhosie"] = spiner_rhosie_fixture(ref, path)
+        fx["spiner_rhosie"]["table_sha256"] = np.array(sha)
+        # PTE with the rho-sie tabulated material beside an ideal gas, both
+        # solvers that take it (RhoT and PT)
+        for solver, tag, seed in ((0, "rhot", 141), (1, "pt", 143)):
+            wl = W.pte_two_material(512, seed=seed)
+            wl["materials"] = [W.IDEAL_AIR, (rb.SPINER_RHOSIE, ())]
+            descs = [desc(W.IDEAL_AIR), rb.eos_desc(rb.SPINER_RHOSIE, [], path=path, matid=3)]
+            r = {k: wl[k].copy() for k in ("rho", "vfrac", "sie", "temp", "press")}
+            conv, nit, res = ref.pte(solver, descs, None, wl["vfrac_tot"], wl["sie_tot"],
+                                     r["rho"], r["vfrac"], r["sie"], r["temp"], r["press"],
+                                     params=ref.mix_params())
+            o = dict(vfrac_tot=wl["vfrac_tot"], sie_tot=wl["sie_tot"], converged=conv,
+                     niter=nit, residual=res, table_sha256=np.array(sha),
+                     solver=np.int32(solver))
+            for k in ("rho", "vfrac", "sie", "temp", "press"):
+                o["in_" + k] = wl[k]
+                o["out_" + k] = r[k]
+            fx[f"pte_{tag}_rhosie"] = o
     air_ramp = ref.p_alpha(desc(W.IDEAL_AIR), 1.5, 5e6, 1e7)
     sg_rows = [mods_row(ramp=air_ramp), mods_row(1e8, 1.02), mods_row(1e7, None),
                mods_row(None, 1.01)]

@@ -320,3 +320,29 @@ def test_port_helmholtz_matches_golden(tmp_path):
     assert good.mean() > 0.75
     bound = 2e-10 * np.abs(fx["fwd_sie"][good]) / np.abs(fx["fwd_cv"][good]) + 1e-12 * fix[good]
     assert (np.abs(T[good] - fix[good]) <= bound).all()
+
+
+# ---- SpinerEOSDependsRhoSie: fixture provenance --------------------------
+
+def test_rhosie_table_generator_is_stable():
+    # the table the fixture was made on is what sp5lite writes today
+    from common import rhosie_table_path
+    _, sha = rhosie_table_path()
+    assert sha == str(golden("spiner_rhosie")["table_sha256"])
+
+
+@needs_reference
+def test_rhosie_fixture_is_current():
+    # the committed fixture is what the compiled reference gives today
+    from common import rhosie_table_path
+    ref = rb.reference()
+    fx = golden("spiner_rhosie")
+    path, _ = rhosie_table_path()
+    d = rb.eos_desc(rb.SPINER_RHOSIE, [], path=path, matid=3)
+    for fn in (0, 1, 3, 5, 7, 10):
+        second = fx["T"] if fn in (1, 2, 4, 6, 8) else fx["sie"]
+        np.testing.assert_array_equal(ref.eos_vec(d, fn, fx["rho"], second), fx[f"fn{fn}"])
+    dump, scal = ref.spiner_sie_dump(path, 3)
+    import hashlib
+    assert hashlib.sha256(dump.tobytes()).hexdigest() == str(fx["dump_sha256"])
+    np.testing.assert_array_equal(scal, fx["scal"])
