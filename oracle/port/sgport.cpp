@@ -1390,8 +1390,17 @@ int sgport_pte(int solver, int nmat_max, int ncell, const sgref_eos *descs, int 
   return 0;
 }
 
+// SpinerEOSDependsRhoSie (type 7) lives in sgport_sie.cpp.
+int sgport_sie_eos_vec(const sgref_eos *d, int fn, int n, const double *in1, const double *in2,
+                       double *out, double *lambda, int stride);
+int sgport_sie_fill_eos(const sgref_eos *d, int n, double *rho, double *temp, double *sie,
+                        double *press, double *cv, double *bmod, unsigned long output,
+                        double *lambda, int stride);
+int sgport_sie_eos_bounds(const sgref_eos *d, int what, int n, const double *x, double *out);
+
 int sgport_eos_vec(const sgref_eos *desc, int fn, int n, const double *in1, const double *in2,
                    double *out, double *lambda, int stride) {
+  if (desc->type == 7) return sgport_sie_eos_vec(desc, fn, n, in1, in2, out, lambda, stride);
   std::vector<port::Eos> v;
   if (!make_eos(desc, 1, v)) return 1;
   const port::Eos &e = v[0];
@@ -1423,6 +1432,8 @@ int sgport_eos_vec(const sgref_eos *desc, int fn, int n, const double *in1, cons
 int sgport_fill_eos(const sgref_eos *desc, int n, double *rho, double *temp, double *sie,
                     double *press, double *cv, double *bmod, unsigned long output,
                     double *lambda, int stride) {
+  if (desc->type == 7)
+    return sgport_sie_fill_eos(desc, n, rho, temp, sie, press, cv, bmod, output, lambda, stride);
   std::vector<port::Eos> v;
   if (!make_eos(desc, 1, v)) return 1;
   const port::Eos &e = v[0];
@@ -1447,6 +1458,7 @@ int sgport_rho_sie_from_pt(const sgref_eos *desc, int n, const double *P, const 
 }
 
 int sgport_eos_bounds(const sgref_eos *desc, int what, int n, const double *x, double *out) {
+  if (desc->type == 7) return sgport_sie_eos_bounds(desc, what, n, x, out);
   std::vector<port::Eos> v;
   if (!make_eos(desc, 1, v)) return 1;
   const port::Eos &e = v[0];
@@ -1495,3 +1507,5 @@ void sgport_nqt(int which, int n, const double *x, double *y) {
 // The Helmholtz model (same translation unit: it uses the port's ratio and
 // root finders).
 #include "sgport_helm.cpp"
+// SpinerEOSDependsRhoSie.
+#include "sgport_sie.cpp"

@@ -384,7 +384,7 @@ template <int N, int G> struct GroupRefine {
   const Lanes<G> &g;
   bool act;
   double rhobar, alpha, rho, sie, u, press, res, res0;
-  double T, Tnorm, uscale, utotal_scale;
+  double T, Tnorm, uscale, utotal_scale, inv_uscale; // (see Refine)
   int ms;
   __device__ GroupRefine(const Lanes<G> &lanes) : g(lanes) {}
 
@@ -395,10 +395,10 @@ template <int N, int G> struct GroupRefine {
       rho = ratio(rhobar, alpha);
       const double e_m = ev_sie_from_rho_T<double>(*m.eos, rho, Tnorm * T, m.lam);
       sie = e_m;
-      u = ratio(rhobar * e_m, uscale);
+      u = rhobar * e_m * inv_uscale;
       const double P = (m.pref & Q_SIE) ? ev_P_from_rho_sie<double>(*m.eos, rho, e_m, m.lam)
                                         : ev_P_from_rho_T<double>(*m.eos, rho, Tnorm * T, m.lam);
-      press = ratio(P, uscale);
+      press = P * inv_uscale;
       usum_part = u;
     } else {
       press = 0.0;
@@ -410,9 +410,10 @@ template <int N, int G> struct GroupRefine {
   }
   __device__ bool converged() const {
     const double mean_p = g.sum(act ? alpha * press : 0.0);
-    const double ep = ssqrt(g.sum(res * res));
-    return (ep < SGX_REFINE_TOL * sabs(mean_p) || ep < 0.1 * SGX_REFINE_TOL) &&
-           sabs(res0) < SGX_REFINE_TOL;
+    const double ep2 = g.sum(res * res);
+    const double lim_p = SGX_REFINE_TOL * sabs(mean_p);
+    constexpr double lim_abs = 0.1 * SGX_REFINE_TOL;
+    return (ep2 < lim_p * lim_p || ep2 < lim_abs * lim_abs) && sabs(res0) < SGX_REFINE_TOL;
   }
   // Up to SGX_REFINE_STEPS corrections x <- x + J32^-1 r64(x); true when
   // the FP64 residual meets the refinement tolerance.
@@ -505,6 +506,7 @@ __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_group_kernel(const PteArg
   const double utotal = rho_total * a.sie_tot[i];
   R.uscale = smax(sabs(utotal), 1.0e-14);
   R.utotal_scale = ratio(utotal, R.uscale);
+  R.inv_uscale = 1.0 / R.uscale;
   R.res = 0.0;
   bool done = false;
   int steps = 0;

@@ -346,3 +346,35 @@ def test_rhosie_fixture_is_current():
     import hashlib
     assert hashlib.sha256(dump.tobytes()).hexdigest() == str(fx["dump_sha256"])
     np.testing.assert_array_equal(scal, fx["scal"])
+
+
+def test_port_rhosie_matches_golden():
+    # the port's SpinerEOSDependsRhoSie reproduces the compiled reference's
+    # fixture bit for bit: load-time tables, vector functions with their
+    # lambda rows, the three FillEos forms and the bounds
+    import hashlib
+    from common import rhosie_table_path
+    port = rb.port()
+    fx = golden("spiner_rhosie")
+    path, _ = rhosie_table_path()
+    dump, scal = port.spiner_sie_dump(path, 3)
+    assert hashlib.sha256(dump.tobytes()).hexdigest() == str(fx["dump_sha256"])
+    np.testing.assert_array_equal(scal, fx["scal"])
+    d = rb.eos_desc(rb.SPINER_RHOSIE, [], path=path, matid=3)
+    for fn in list(range(11)) + [13]:
+        second = fx["P_target"] if fn == 13 else (fx["T"] if fn in (1, 2, 4, 6, 8) else fx["sie"])
+        lam = np.full(fx["rho"].size, np.nan)
+        np.testing.assert_array_equal(port.eos_vec(d, fn, fx["rho"], second, lam=lam,
+                                                   lam_stride=1), fx[f"fn{fn}"])
+        np.testing.assert_array_equal(lam, fx[f"fn{fn}_lambda"])
+    for tag in ("e", "t", "pt"):
+        a = {k: fx[k].copy() for k in ("rho", "T", "sie", "P_in")}
+        cv, bm, lam = np.zeros(a["rho"].size), np.zeros(a["rho"].size), np.full(a["rho"].size,
+                                                                              np.nan)
+        port.fill_eos(d, a["rho"], a["T"], a["sie"], a["P_in"], cv, bm,
+                      int(fx[f"fill_{tag}_output"]), lam=lam, lam_stride=1)
+        for name, v in (("rho", a["rho"]), ("T", a["T"]), ("sie", a["sie"]), ("P", a["P_in"]),
+                        ("cv", cv), ("bmod", bm), ("lambda", lam)):
+            np.testing.assert_array_equal(v, fx[f"fill_{tag}_{name}"])
+    for w in range(6):
+        np.testing.assert_array_equal(port.eos_bounds(d, w, fx["bounds_T"]), fx[f"bound{w}"])
