@@ -26,6 +26,7 @@ UNITS = [
     ("sgx_fp64", "sgx_fp64.cu", ["--fmad=false"]),
     ("sgx_mixed", "sgx_mixed.cu", ["--fmad=true"]),
     ("sgx_lookup_mixed", "sgx_lookup_mixed.cu", ["--fmad=true"]),
+    ("sgx_lookup_sie", "sgx_lookup_sie.cu", ["--fmad=true"]),
     ("sgx_capi", "sgx_capi.cu", ["--fmad=false"]),
     ("sgx_table", "sgx_table.cu", ["--fmad=false"]),
     ("sgx_noalloc", "sgx_noalloc.cu", ["--fmad=false"]),

@@ -430,16 +430,22 @@ int sgx_eos_fill_ex(const sgx_eos *eos, int64_t n, double *rho, double *temp, do
     e = sgx::launch_helm_fill(a, reinterpret_cast<cudaStream_t>(stream),
                               precision == SGX_PREC_MIXED);
   } else if (precision == SGX_PREC_MIXED) {
-    // The mixed path covers the hot call: a tabulated rho-T model with
-    // (rho, sie) in and any of T, P, cv, bmod out.
+    // The mixed path covers the hot call: a tabulated model with (rho, sie)
+    // in and any of T, P, cv, bmod out.
     const uint32_t allowed = SGX_Q_TEMPERATURE | SGX_Q_PRESSURE | SGX_Q_SPECIFIC_HEAT |
                              SGX_Q_BULK_MODULUS;
-    if (eos->type != SGX_SPINER_RHOT || (output & ~allowed) || !(output & SGX_Q_TEMPERATURE) ||
-        !sie)
+    if ((eos->type != SGX_SPINER_RHOT && eos->type != SGX_SPINER_RHOSIE) ||
+        (output & ~allowed) || !(output & SGX_Q_TEMPERATURE) || !sie)
       return fail(SGX_ERR_UNSUPPORTED,
-                  "sgx_eos_fill: mixed precision needs a tabulated rho-T EOS, (rho, sie) "
+                  "sgx_eos_fill: mixed precision needs a tabulated EOS, (rho, sie) "
                   "inputs and T among the outputs");
-    e = sgx::launch_fill_mixed(a, reinterpret_cast<cudaStream_t>(stream));
+    const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (eos->type == SGX_SPINER_RHOT)
+      e = sgx::launch_fill_mixed(a, s);
+    else if (sgx::table_has_sie_cells(eos->table))
+      e = sgx::launch_fill_sie_mixed(a, s);
+    else // a table with values outside the float range: the FP64 path
+      e = sgx::launch_fill_fp64(a, s);
   } else {
     e = sgx::launch_fill_fp64(a, reinterpret_cast<cudaStream_t>(stream));
   }

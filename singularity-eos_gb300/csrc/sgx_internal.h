@@ -120,6 +120,9 @@ struct FillArgs {
   int *err; // device flag: set to 1 on an undefined input/output combination
 };
 cudaError_t launch_fill_fp64(const FillArgs &a, cudaStream_t stream);
+// SpinerEOSDependsRhoSie FillEos from (rho, sie) in float-float
+// (sgx_lookup_sie.cu); the table must carry its float-float cells.
+cudaError_t launch_fill_sie_mixed(const FillArgs &a, cudaStream_t stream);
 // PTDerivativesFromPreferred per element: d[0..3] = dedP_T, drdP_T, dedT_P,
 // drdT_P.
 struct PtDerivArgs {

@@ -1,0 +1,192 @@
+// FillEos of SpinerEOSDependsRhoSie from (rho, sie) in float-float, for the
+// FP32 pipe.
+//
+// The reference's FillEos (eos/eos_spiner_rho_sie.hpp:844-898) with T among
+// the outputs takes lRho = to_log(rho), lE = to_log(sie) and interpolates
+// T, P, 1 / dT/de and bMod bilinearly on the rho-sie grid: two NQT logs and
+// four interpolations, no root find. In FP64 that is about forty operations
+// on GB300's FP64 pipe (1/64 of the FP32 rate) per query, so the plain path
+// runs at a tenth of the HBM bandwidth. Here no FP64 arithmetic is left:
+//   1. to_log(x, off) = log10_nqt(|max(x, -off) + off| + EPS): the sum in
+//      float-float, rounded to the double whose bit pattern the NQT log
+//      (logs.hpp:188-200) takes apart in integers, the integer result
+//      scaled by scale_down * log2(10)^-1 in float-float;
+//   2. the cell coordinate u = lX / dx - min / dx per axis, its index
+//      clamped to the grid and its weight unclamped (linear extrapolation
+//      off the grid, as DataBox::interpToReal);
+//   3. one 128-byte cell holding the four fields in difference form
+//      (SieCellFF), each f = x + a dE + b dR + a b dRE evaluated in
+//      float-float and converted to double by integer operations.
+// The result differs from the FP64 path by the float-float rounding of the
+// coordinates (~1e-14 of the log) times the interpolant's slope, a few
+// 1e-14 relative wherever the cell's corners share a sign. Elements whose
+// inputs lie outside the float range (or NaN), and tables with values
+// outside it, take the reference's FP64 arithmetic in the same kernel.
+#define SGX_BARE_MODELS
+#include <cuda_runtime.h>
+
+#include "sgx_dispatch.cuh"
+#include "sgx_ff.cuh"
+#include "sgx_ff_table.cuh"
+#include "sgx_internal.h"
+
+namespace sgx {
+
+namespace {
+
+constexpr int SIE_BLOCK = 256;
+
+// robust::EPS() and scale_down * log2_over_log10 as float pairs
+constexpr double K_EPS = lim<double>::eps;
+constexpr float K_EPS_HI = static_cast<float>(K_EPS);
+constexpr float K_EPS_LO = static_cast<float>(K_EPS - static_cast<double>(K_EPS_HI));
+constexpr double K_LG = nqt::scale_down * nqt::log2_over_log10;
+constexpr float K_LG_HI = static_cast<float>(K_LG);
+constexpr float K_LG_LO = static_cast<float>(K_LG - static_cast<double>(K_LG_HI));
+
+// Whether a double converts to float-float without leaving the float range.
+__device__ __forceinline__ bool ff_in_range(const double x) {
+  const long long b = __double_as_longlong(x);
+  const int e = static_cast<int>((b >> 52) & 0x7ff) - 1023;
+  return (b & 0x7fffffffffffffffLL) == 0 || (e >= -74 && e <= 120);
+}
+
+// The integer core of lg_nqt (logs.hpp:188-200) on the bits of y.
+__device__ __forceinline__ long long nqt_lg_int(const double y) {
+  using namespace nqt;
+  const long long x_as_int = __double_as_longlong(y) - one_as_int;
+  const long long frac = x_as_int & mantissa_mask;
+  const long long fh = frac >> 26, fl = frac & low_mask;
+  const long long fsq = fh * fh + ((fh * fl) >> 25);
+  return x_as_int + (frac - fsq) / 3;
+}
+
+// An int64 of magnitude below 2^62 as float-float (about 48 of its bits).
+__device__ __forceinline__ ff ff_from_i64(const long long v) {
+  const float hi = __ll2float_rn(v);
+  return quick_two_sum(hi, __ll2float_rn(v - f2ll_bits(hi)));
+}
+
+// spiner_common::to_log (eos_spiner_common.hpp:52-54) in float-float.
+__device__ __forceinline__ ff to_log_ff(const double x, const float *off, const bool has_off) {
+  ff X = d2ff(x);
+  if (has_off) X = ff_add(X, ff_make(off[0], off[1]));
+  if (!(X.hi > 0.0f)) X = ff_make(0.0f); // std::max(x, -off) + off
+  X = ff_add(X, ff_make(K_EPS_HI, K_EPS_LO));
+  return ff_mul(ff_from_i64(nqt_lg_int(ff2d(X))), ff_make(K_LG_HI, K_LG_LO));
+}
+
+// Cell index and weight on one axis: u = lX inv - off, index clamped to
+// [0, n - 2], weight u - index (unclamped).
+__device__ __forceinline__ int cell_of(const ff lX, const float *inv, const float *off,
+                                       const int n, ff &w) {
+  const ff u = ff_sub(ff_mul(lX, ff_make(inv[0], inv[1])), ff_make(off[0], off[1]));
+  float fj = floorf(u.hi);
+  if (u.hi == fj && u.lo < 0.0f) fj -= 1.0f; // the value lies just below fj
+  fj = fminf(fmaxf(fj, 0.0f), static_cast<float>(n - 2));
+  w = ff_sub(u, ff_make(fj));
+  return static_cast<int>(fj);
+}
+
+// The reference's FP64 arithmetic for one element (inputs outside the float
+// range), with the outputs of the float-float path.
+__device__ __noinline__ void sie_fill_fp64(const SieTable &t, const FillArgs &a, const long long e,
+                                           const double rho, const double sie) {
+  const double lRho = ss_lRho(t, rho), lE = ss_lE(t, sie);
+  const unsigned out = a.output;
+  if ((out & Q_TEMPERATURE) && a.temp) a.temp[e] = se_interp(t, SE_T, lRho, lE);
+  if ((out & Q_PRESSURE) && a.press) a.press[e] = se_interp(t, SE_P, lRho, lE);
+  if ((out & Q_CV) && a.cv) a.cv[e] = 1. / se_interp(t, SE_DTDE, lRho, lE);
+  if ((out & Q_BMOD) || a.cs) {
+    const double bmod = se_interp(t, SE_BMOD, lRho, lE);
+    if ((out & Q_BMOD) && a.bmod) a.bmod[e] = bmod;
+    if (a.cs) a.cs[e] = sqrt(bmod / rho);
+  }
+  if (a.lambda) a.lambda[e * a.lambda_stride] = lRho;
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(SIE_BLOCK, MINB) sie_fill_fast(const FillArgs a) {
+  __shared__ SieTable st;
+  if (threadIdx.x == 0) st = ss_table(a.eos);
+  __syncthreads();
+  const SieTable &t = st;
+  const unsigned out = a.output;
+  const bool rho_off = t.ffRhoOff[0] != 0.0f, e_off = t.ffEOff[0] != 0.0f;
+  const int ncE = t.nE - 1;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; e < a.n;
+       e += stride) {
+    const double rho = __ldg(a.rho + e);
+    const double sie = __ldg(a.sie + e);
+    if (!(ff_in_range(rho) && ff_in_range(sie))) {
+      sie_fill_fp64(t, a, e, rho, sie);
+      continue;
+    }
+    const ff lRho = to_log_ff(rho, t.ffRhoOff, rho_off);
+    const ff lE = to_log_ff(sie, t.ffEOff, e_off);
+    ff B, A;
+    const int j = cell_of(lRho, t.ffR_inv, t.ffR_off, t.nRhoE, B);
+    const int i = cell_of(lE, t.ffE_inv, t.ffE_off, t.nE, A);
+    const SieCellFF *c = t.cellsE + static_cast<long long>(j) * ncE + i;
+    const ff AB = ff_mul(A, B);
+    if ((out & Q_TEMPERATURE) && a.temp) a.temp[e] = ff2d(ff_cell(load_rec(&c->T), A, B, AB));
+    if ((out & Q_PRESSURE) && a.press) a.press[e] = ff2d(ff_cell(load_rec(&c->P), A, B, AB));
+    if ((out & Q_CV) && a.cv) {
+      const ff d = ff_cell(load_rec(&c->dTdE), A, B, AB);
+      const ff dn = quick_two_sum(d.hi, d.lo);
+      // 1 / dT/de: the reciprocal of a zero is the reference's signed infinity
+      const unsigned long long inf =
+          0x7ff0000000000000ULL |
+          (static_cast<unsigned long long>(__float_as_uint(dn.hi) >> 31) << 63);
+      a.cv[e] = dn.hi == 0.0f ? __longlong_as_double(static_cast<long long>(inf))
+                              : ff2d(ff_div(ff_make(1.0f), dn));
+    }
+    if ((out & Q_BMOD) || a.cs) {
+      const ff bm = ff_cell(load_rec(&c->bMod), A, B, AB);
+      const ff BM = quick_two_sum(bm.hi, bm.lo);
+      if ((out & Q_BMOD) && a.bmod) a.bmod[e] = ff2d(BM);
+      if (a.cs) {
+        // sqrt(bmod / rho) by one rsqrt correction while b rho stays well
+        // inside the float range (and positive); the FP64 form otherwise
+        const ff R = d2ff(rho);
+        const float pr = BM.hi * R.hi;
+        a.cs[e] = (BM.hi > 0.0f && R.hi > 0.0f && pr > 1e-30f && pr < 1e30f)
+                      ? ff2d(ff_sqrt_ratio(BM, R))
+                      : sqrt(ff2d(BM) / rho);
+      }
+    }
+    if (a.lambda) a.lambda[e * a.lambda_stride] = ff2d(lRho);
+  }
+}
+
+} // namespace
+
+cudaError_t launch_fill_sie_mixed(const FillArgs &a, cudaStream_t stream) {
+  if (a.n <= 0) return cudaSuccess;
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  // persistent grid: the blocks resident at once for the registers budgeted
+  const int minb = tune_get(SGX_TUNE_LOOKUP_BLOCKS_PER_SM);
+  int resident = 0;
+  if (minb >= 6)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, sie_fill_fast<6>, SIE_BLOCK, 0);
+  else if (minb == 5)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, sie_fill_fast<5>, SIE_BLOCK, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, sie_fill_fast<4>, SIE_BLOCK, 0);
+  const int per_sm = resident > 0 ? resident : 1;
+  const long long want = (a.n + SIE_BLOCK - 1) / SIE_BLOCK;
+  const long long cap = static_cast<long long>(sms) * per_sm;
+  const int grid = static_cast<int>(want < cap ? want : cap);
+  if (minb >= 6)
+    sie_fill_fast<6><<<grid, SIE_BLOCK, 0, stream>>>(a);
+  else if (minb == 5)
+    sie_fill_fast<5><<<grid, SIE_BLOCK, 0, stream>>>(a);
+  else
+    sie_fill_fast<4><<<grid, SIE_BLOCK, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+} // namespace sgx

@@ -26,6 +26,14 @@ namespace sgx {
 enum SieField2D { ST_SIE = 0, ST_P, ST_BMOD, ST_DPDE, ST_DTDE, NST2D };
 enum SieFieldE2D { SE_T = 0, SE_P, SE_BMOD, SE_DPDE, SE_DTDE, NSE2D };
 
+// One (lRho, lE) cell of the rho-sie group for the float-float FillEos: the
+// four fields it outputs in difference form (FfRec: f = x + a dE + b dR +
+// a b dRE over the cell's unit square, a the lE weight, b the density
+// weight), 128 bytes, one cache line per query.
+struct alignas(128) SieCellFF {
+  FfRec T, P, dTdE, bMod;
+};
+
 struct SieTable {
   Grid1D gT, gRhoT;  // rho-T group: T grid (fastest), density grid
   Grid1D gE, gRhoE;  // rho-sie group: lE grid (fastest), density grid
@@ -40,6 +48,13 @@ struct SieTable {
   const double *fT[NST2D]; // rho-T group
   const double *fE[NSE2D]; // rho-sie group
   const double *sieCold, *PlRhoMax, *dPdRhoMax, *rho_at_pmin;
+  // float-float FillEos from (rho, sie): the cells [nRhoE-1][nE-1] (null when
+  // a value lies outside the float range) and, per axis, the cell
+  // coordinate u = lX * inv_dx - min * inv_dx as float pairs (hi, lo); the
+  // offsets of the density and energy coordinates likewise
+  const SieCellFF *cellsE;
+  float ffE_inv[2], ffE_off[2], ffR_inv[2], ffR_off[2];
+  float ffRhoOff[2], ffEOff[2];
 };
 
 // DataBox::interpToReal(x2 = lRho, x1 = fast coordinate) on one group.

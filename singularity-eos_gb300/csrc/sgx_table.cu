@@ -148,6 +148,7 @@ struct Resident {
   int device = 0;
   HostTable host;
   std::vector<double> dump; // non-empty: the dump of a non-Spiner table
+  bool sie_cells = false;   // a SpinerEOSDependsRhoSie table with float-float cells
 };
 std::mutex g_mu;
 std::map<uint64_t, Resident> g_tables;
@@ -841,6 +842,43 @@ int table_load_spiner_sie(const char *path, int matid, bool reproducible, uint64
     off1[k] = off;
     off = align(off + one[k]->size() * 8);
   }
+  // the float-float cells of the rho-sie group (see SieCellFF); values
+  // beyond the float range leave the mixed path off for this table
+  const int nE = ge.nx, nRE = ge.nr;
+  std::vector<SieCellFF> cells(static_cast<size_t>(nRE - 1) * (nE - 1));
+  bool ff_ok = true;
+  {
+    auto split = [&ff_ok](const double v, float out[2]) {
+      if (!(std::fabs(v) <= 1e37)) ff_ok = false;
+      const double w = std::fabs(v) < 1e-30 ? 0.0 : v;
+      out[0] = static_cast<float>(w);
+      out[1] = static_cast<float>(w - static_cast<double>(out[0]));
+    };
+    auto rec = [&](const std::vector<double> &f, const int j, const int i, FfRec &r) {
+      const size_t k00 = static_cast<size_t>(j) * nE + i, k01 = k00 + 1, k10 = k00 + nE,
+                   k11 = k10 + 1;
+      split(f[k00], r.x);
+      split(f[k01] - f[k00], r.dT);
+      split(f[k10] - f[k00], r.dR);
+      split((f[k11] - f[k10]) - (f[k01] - f[k00]), r.dRT);
+    };
+    for (int j = 0; j < nRE - 1; ++j)
+      for (int i = 0; i < nE - 1; ++i) {
+        SieCellFF &c = cells[static_cast<size_t>(j) * (nE - 1) + i];
+        rec(ge.f[G_X], j, i, c.T);
+        rec(ge.f[G_P], j, i, c.P);
+        rec(ge.f[G_DTDE], j, i, c.dTdE);
+        rec(ge.f[G_BMOD], j, i, c.bMod);
+      }
+    split(t.gE.inv_dx, t.ffE_inv);
+    split(t.gE.min * t.gE.inv_dx, t.ffE_off);
+    split(t.gRhoE.inv_dx, t.ffR_inv);
+    split(t.gRhoE.min * t.gRhoE.inv_dx, t.ffR_off);
+    split(t.lRhoOffset, t.ffRhoOff);
+    split(t.lEOffset, t.ffEOff);
+  }
+  const size_t offc = off;
+  if (ff_ok) off = align(off + cells.size() * sizeof(SieCellFF));
   const size_t bytes = off;
   std::vector<unsigned char> img(bytes, 0);
   for (int k = 0; k < NST2D; ++k)
@@ -849,6 +887,7 @@ int table_load_spiner_sie(const char *path, int matid, bool reproducible, uint64
     std::memcpy(img.data() + offE[k], ge.f[srcE[k]].data(), ge.f[srcE[k]].size() * 8);
   for (int k = 0; k < 4; ++k)
     std::memcpy(img.data() + off1[k], one[k]->data(), one[k]->size() * 8);
+  if (ff_ok) std::memcpy(img.data() + offc, cells.data(), cells.size() * sizeof(SieCellFF));
   void *dev = nullptr;
   cudaError_t e = cudaMalloc(&dev, bytes);
   if (e != cudaSuccess) {
@@ -865,6 +904,7 @@ int table_load_spiner_sie(const char *path, int matid, bool reproducible, uint64
   td.PlRhoMax = reinterpret_cast<const double *>(d + off1[1]);
   td.dPdRhoMax = reinterpret_cast<const double *>(d + off1[2]);
   td.rho_at_pmin = reinterpret_cast<const double *>(d + off1[3]);
+  td.cellsE = ff_ok ? reinterpret_cast<const SieCellFF *>(d + offc) : nullptr;
   std::memcpy(img.data(), &td, sizeof(td));
   e = cudaMemcpy(dev, img.data(), bytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
@@ -875,6 +915,7 @@ int table_load_spiner_sie(const char *path, int matid, bool reproducible, uint64
   Resident r;
   r.dev = dev;
   r.bytes = bytes;
+  r.sie_cells = ff_ok;
   cudaGetDevice(&r.device);
   // DBLIST: sie_, T_, rho_at_pmin_, the rho-T tables, the rho-sie tables,
   // mF_ (none), PlRhoMax_, dPdRhoMax_, PCold_, sieCold_, bModCold_, dPdRhoCold_
@@ -1059,6 +1100,12 @@ bool table_has_thermal_index(uint64_t handle) {
   std::lock_guard<std::mutex> lk(g_mu);
   auto it = g_tables.find(handle);
   return it != g_tables.end() && it->second.dump.empty() && it->second.host.t.therm_bins > 0;
+}
+
+bool table_has_sie_cells(uint64_t handle) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_tables.find(handle);
+  return it != g_tables.end() && it->second.sie_cells;
 }
 
 size_t table_bytes(uint64_t handle) {

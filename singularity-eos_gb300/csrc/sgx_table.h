@@ -23,6 +23,9 @@ int table_free(uint64_t handle, std::string &msg);
 size_t table_bytes(uint64_t handle);
 // Density nodes of a resident Spiner table (0 if unknown).
 int table_nrho(uint64_t handle);
+// Whether a resident SpinerEOSDependsRhoSie table carries the float-float
+// cells of its rho-sie grid (every value inside the float range).
+bool table_has_sie_cells(uint64_t handle);
 // Whether a resident Spiner table carries the thermal-energy bin index.
 bool table_has_thermal_index(uint64_t handle);
 // Spiner: derived tables in the reference's DBLIST order; Helmholtz: node

@@ -99,6 +99,49 @@ class Writer:
                         struct.pack("<I", len(n)) + n + payload)
 
 
+def read(fname):
+    """An sp5-lite image as {"attrs": {path@name: value}, "datasets": {path:
+    (array in C order, [(n, min, max)] fastest first)}}."""
+    with open(fname, "rb") as f:
+        buf = f.read()
+    assert buf[:8] == b"SGXSP5L\0"
+    _, nrec = struct.unpack_from("<II", buf, 8)
+    off = 16
+    attrs, datasets = {}, {}
+
+    def string():
+        nonlocal off
+        (n,) = struct.unpack_from("<I", buf, off)
+        off += 4
+        v = buf[off:off + n].decode()
+        off += n
+        return v
+    for _ in range(nrec):
+        (kind,) = struct.unpack_from("<I", buf, off)
+        off += 4
+        path, name = string(), string()
+        if kind == 1:
+            attrs[path + "@" + name] = struct.unpack_from("<d", buf, off)[0]
+            off += 8
+        elif kind == 2:
+            attrs[path + "@" + name] = struct.unpack_from("<i", buf, off)[0]
+            off += 4
+        elif kind == 4:
+            attrs[path + "@" + name] = string()
+        else:
+            (rank,) = struct.unpack_from("<I", buf, off)
+            off += 4
+            ranges = []
+            for _ in range(rank):
+                ranges.append(struct.unpack_from("<idd", buf, off))
+                off += 20
+            count = int(np.prod([r[0] for r in ranges]))
+            data = np.frombuffer(buf, np.float64, count, off).copy()
+            off += 8 * count
+            datasets[path] = (data.reshape([r[0] for r in reversed(ranges)]), ranges)
+    return {"attrs": attrs, "datasets": datasets}
+
+
 def stiffgas_table(fname, matid=1, nrho=256, nt=256, rho_range=(1e-4, 1e2),
                    t_range=(1e2, 1e6), gm1=3.4, Cv=1.816e7, Pinf=6e9, qq=0.0):
     """Writes a SpinerEOSDependsRhoT-layout table sampled from the StiffGas

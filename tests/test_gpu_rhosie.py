@@ -139,3 +139,75 @@ def test_rejects(sgx, table):
         pass
     torch.cuda.synchronize()
     assert float(T.abs().sum()) == 0.0 and float(sie.abs().sum()) == 0.0
+
+
+def interp_scale(path, field, rho, sie):
+    """sum_k |w_k| |f_k| over the four corners of each query's cell on the
+    rho-sie grid: the magnitude the bilinear form's roundings scale with."""
+    from sgx import sp5lite
+    img = sp5lite.read(path)
+    a = img["attrs"]
+    g = "/3/dependsLogRhoLogSie/"
+    data, ranges = img["datasets"][g + field]
+    (ne, emin, emax), (nr, rmin, rmax) = ranges
+    if field == "bulk modulus":
+        # the values calcBMod_ (eos_spiner_rho_sie.hpp:554-578) leaves
+        r = (sp5lite.pow10_nqt(np.linspace(rmin, rmax, nr)) - a["/3@rhoOffset"])[:, None]
+        P, dPdR, dPdE, dEdR = (img["datasets"][g + k][0] for k in
+                               ("pressure", "dPdRho", "dPdE", "dEdRho"))
+        b = np.where(dPdE > 0, r * dPdR + dPdE * (P / r), np.maximum(r * (dPdR + dPdE * dEdR), 0))
+        data = np.maximum(b, 10 * np.finfo(float).eps)
+    lr = sp5lite.to_log(rho, a["/3@rhoOffset"])
+    le = sp5lite.to_log(sie, a["/3@sieOffset"])
+
+    def weights(x, n, mn, mx):
+        dx = (mx - mn) / (n - 1)
+        u = (x - mn) / dx
+        i = np.clip(np.where(u >= 0, np.floor(u), 0), 0, n - 2).astype(int)
+        w1 = u - i
+        return i, 1.0 - w1, w1
+    j, b0, b1 = weights(lr, nr, rmin, rmax)
+    i, a0, a1 = weights(le, ne, emin, emax)
+    f = np.abs(data)
+    return (np.abs(b0) * (np.abs(a0) * f[j, i] + np.abs(a1) * f[j, i + 1]) +
+            np.abs(b1) * (np.abs(a0) * f[j + 1, i] + np.abs(a1) * f[j + 1, i + 1]))
+
+
+def test_mixed_fill_against_fp64(sgx, table):
+    """The float-float FillEos (sgx_lookup_sie.cu) against the FP64 path (bit
+    for bit the reference's, test_fill_eos): every output within 1e-11 of
+    the interpolant's own magnitude scale sum_k |w_k f_k| (that is, within
+    1e-11 relative wherever the cell's corners share a sign), the lambda
+    entry log10(rho) within 1e-13, the sound speed within 1e-10 relative."""
+    tab, fx = table
+    path, _ = rhosie_table_path()
+    # the fixture's queries (5 % off the table) plus a denser on-table set
+    from sgx import sp5lite
+    r2, e2, _ = sp5lite.rhosie_queries(1 << 16, seed=11, off_table=0.0)
+    rho_h = np.concatenate([fx["rho"], r2])
+    sie_h = np.concatenate([fx["sie"], e2])
+    rho, sie = dev(rho_h), dev(sie_h)
+    q = sgx.Q_TEMPERATURE | sgx.Q_PRESSURE | sgx.Q_SPECIFIC_HEAT | sgx.Q_BULK_MODULUS
+    res = {}
+    for prec in (sgx.PREC_FP64, sgx.PREC_MIXED):
+        T, P, cv, bm, cs = (torch.zeros_like(rho) for _ in range(5))
+        lam = torch.full_like(rho, float("nan"))
+        sgx.fill_eos(tab, rho, T, sie, P, cv, bm, q, lam=lam, lam_stride=1, cs=cs,
+                     precision=prec)
+        torch.cuda.synchronize()
+        res[prec] = {k: v.cpu().numpy() for k, v in
+                     (("T", T), ("P", P), ("cv", cv), ("bmod", bm), ("cs", cs), ("lam", lam))}
+    ref, got = res[sgx.PREC_FP64], res[sgx.PREC_MIXED]
+    for name, field in (("T", "temperature"), ("P", "pressure"), ("bmod", "bulk modulus")):
+        S = interp_scale(path, field, rho_h, sie_h)
+        e = np.abs(got[name] - ref[name]) / S
+        print(f"mixed {name}: max |err| / scale {e.max():.2e}, max rel "
+              f"{rel_err(got[name], ref[name]).max():.2e}")
+        assert e.max() <= 1e-11, name
+    # cv = 1 / dT/de: relative error of the reciprocal is that of dT/de
+    S = interp_scale(path, "dTdE", rho_h, sie_h)
+    e = np.abs(1.0 / got["cv"] - 1.0 / ref["cv"]) / S
+    assert e.max() <= 1e-11, "cv"
+    assert np.abs(got["lam"] - ref["lam"]).max() <= 1e-13
+    ok = ref["bmod"] > 0
+    assert rel_err(got["cs"][ok], ref["cs"][ok]).max() <= 1e-10
