@@ -871,7 +871,8 @@ def main():
     if rank != 0:
         return
     if "value" not in out:  # a profiling run of one leg: no headline line
-        print(json.dumps({k: out.get(k) for k in ("pte", "helmholtz", "serve", "fp_peaks")}))
+        print(json.dumps({k: out.get(k) for k in ("pte", "helmholtz", "serve", "rhosie",
+                                                  "fp_peaks", "autotuned")}))
         return
     line = {"metric": METRIC, "value": out["value"], "unit": "lookups/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["ms_per_step"],
@@ -882,8 +883,8 @@ def main():
             "gpu_launches": out["gpu_launches"], "plain_fp64": out["plain_fp64"],
             "mixed_error": out.get("mixed_error"),
             "pte": out.get("pte"), "helmholtz": out.get("helmholtz"),
-            "serve": out.get("serve"), "fp_peaks": out.get("fp_peaks"),
-            "autotuned": out.get("autotuned")}
+            "serve": out.get("serve"), "rhosie": out.get("rhosie"),
+            "fp_peaks": out.get("fp_peaks"), "autotuned": out.get("autotuned")}
     if "e2e" not in out:
         line["e2e"] = None
     if not args.no_cpu_baseline and world == 1:

@@ -291,8 +291,10 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
       const long long fsq = fh * fh + ((fh * fl) >> 25);
       // two roundings, as lg_nqt then log10 (scale_down is the reference's
       // 15-digit literal, not exactly 2^-52)
+      // (the int64-to-double conversion in integers: it leaves the FP64 pipe
+      // to the roundings that must be the reference's)
       lRho = __dmul_rn(log2_over_log10,
-                       __dmul_rn(static_cast<double>(x_as_int + ((frac - fsq) / 3)), scale_down));
+                       __dmul_rn(i64_to_f64_rn(x_as_int + ((frac - fsq) / 3)), scale_down));
       // Grid1D::index and ::weights with the FP64 path's roundings: the
       // interpolant has a kink at every density node, so the cell must be the
       // reference's, and the root multiplies an error in b by dR / dT (up to

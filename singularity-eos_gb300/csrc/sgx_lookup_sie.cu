@@ -6,22 +6,26 @@
 // T, P, 1 / dT/de and bMod bilinearly on the rho-sie grid: two NQT logs and
 // four interpolations, no root find. In FP64 that is about forty operations
 // on GB300's FP64 pipe (1/64 of the FP32 rate) per query, so the plain path
-// runs at a tenth of the HBM bandwidth. Here no FP64 arithmetic is left:
+// runs at a few percent of the HBM bandwidth. Here FP64 keeps one addition
+// per coordinate:
 //   1. to_log(x, off) = log10_nqt(|max(x, -off) + off| + EPS): the sum in
-//      float-float, rounded to the double whose bit pattern the NQT log
-//      (logs.hpp:188-200) takes apart in integers, the integer result
-//      scaled by scale_down * log2(10)^-1 in float-float;
-//   2. the cell coordinate u = lX / dx - min / dx per axis, its index
-//      clamped to the grid and its weight unclamped (linear extrapolation
-//      off the grid, as DataBox::interpToReal);
+//      FP64 as the reference rounds it, then the NQT log's integer core
+//      (logs.hpp:188-200) on its bits -- the same integer v the reference
+//      scales by scale_down log10(2) (lambda gets that value bit for bit);
+//   2. the cell coordinate u = (lX - min) / dx straight from v in fixed
+//      point (one 64 x 64 -> 128-bit product with the table's constant), its
+//      index clamped to the grid and its weight unclamped (linear
+//      extrapolation off the grid, as DataBox::interpToReal) -- about 2^-46
+//      absolute, where a float-float lX would lose two to three digits to
+//      the scaling by 1 / dx;
 //   3. one 128-byte cell holding the four fields in difference form
 //      (SieCellFF), each f = x + a dE + b dR + a b dRE evaluated in
 //      float-float and converted to double by integer operations.
-// The result differs from the FP64 path by the float-float rounding of the
-// coordinates (~1e-14 of the log) times the interpolant's slope, a few
-// 1e-14 relative wherever the cell's corners share a sign. Elements whose
+// The result differs from the FP64 path by the reference's own roundings of
+// the coordinates (~1e-15 of the log) times the interpolant's slope, about
+// 1e-13 relative wherever the cell's corners share a sign. Elements whose
 // inputs lie outside the float range (or NaN), and tables with values
-// outside it, take the reference's FP64 arithmetic in the same kernel.
+// outside it, take the reference's FP64 arithmetic.
 #define SGX_BARE_MODELS
 #include <cuda_runtime.h>
 
@@ -36,13 +40,6 @@ namespace {
 
 constexpr int SIE_BLOCK = 256;
 
-// robust::EPS() and scale_down * log2_over_log10 as float pairs
-constexpr double K_EPS = lim<double>::eps;
-constexpr float K_EPS_HI = static_cast<float>(K_EPS);
-constexpr float K_EPS_LO = static_cast<float>(K_EPS - static_cast<double>(K_EPS_HI));
-constexpr double K_LG = nqt::scale_down * nqt::log2_over_log10;
-constexpr float K_LG_HI = static_cast<float>(K_LG);
-constexpr float K_LG_LO = static_cast<float>(K_LG - static_cast<double>(K_LG_HI));
 
 // Whether a double converts to float-float without leaving the float range.
 __device__ __forceinline__ bool ff_in_range(const double x) {
@@ -61,31 +58,43 @@ __device__ __forceinline__ long long nqt_lg_int(const double y) {
   return x_as_int + (frac - fsq) / 3;
 }
 
+// The NQT log's integer v of spiner_common::to_log (eos_spiner_common.hpp:
+// 52-54): the argument |max(x, -off) + off| + EPS in FP64 as the reference
+// rounds it.
+__device__ __forceinline__ long long to_log_int(const double x, const double off,
+                                                const bool has_off) {
+  double y;
+  if (has_off)
+    y = (x < -off ? -off : x) + off;
+  else // std::max(x, -0.0) + 0.0: zero for every negative x
+    y = __double_as_longlong(x) < 0 ? 0.0 : x;
+  return nqt_lg_int(fabs(y) + lim<double>::eps);
+}
+
 // An int64 of magnitude below 2^62 as float-float (about 48 of its bits).
 __device__ __forceinline__ ff ff_from_i64(const long long v) {
   const float hi = __ll2float_rn(v);
   return quick_two_sum(hi, __ll2float_rn(v - f2ll_bits(hi)));
 }
 
-// spiner_common::to_log (eos_spiner_common.hpp:52-54) in float-float.
-__device__ __forceinline__ ff to_log_ff(const double x, const float *off, const bool has_off) {
-  ff X = d2ff(x);
-  if (has_off) X = ff_add(X, ff_make(off[0], off[1]));
-  if (!(X.hi > 0.0f)) X = ff_make(0.0f); // std::max(x, -off) + off
-  X = ff_add(X, ff_make(K_EPS_HI, K_EPS_LO));
-  return ff_mul(ff_from_i64(nqt_lg_int(ff2d(X))), ff_make(K_LG_HI, K_LG_LO));
-}
-
-// Cell index and weight on one axis: u = lX inv - off, index clamped to
-// [0, n - 2], weight u - index (unclamped).
-__device__ __forceinline__ int cell_of(const ff lX, const float *inv, const float *off,
-                                       const int n, ff &w) {
-  const ff u = ff_sub(ff_mul(lX, ff_make(inv[0], inv[1])), ff_make(off[0], off[1]));
-  float fj = floorf(u.hi);
-  if (u.hi == fj && u.lo < 0.0f) fj -= 1.0f; // the value lies just below fj
-  fj = fminf(fmaxf(fj, 0.0f), static_cast<float>(n - 2));
-  w = ff_sub(u, ff_make(fj));
-  return static_cast<int>(fj);
+// Cell index and weight on one axis from v: u 2^F = mulhi(v, M) - Off, the
+// index floor(u) clamped to [0, n - 2], the weight u - index (unclamped) as
+// float-float, exact for |weight| < 2^(47 - F) (two 24-bit halves).
+__device__ __forceinline__ int cell_of(const long long v, const long long M, const long long off,
+                                       const int F, const int n, ff &w) {
+  const long long U = __mul64hi(v, M) - off;
+  long long j = U >> F;
+  j = j < 0 ? 0 : (j > n - 2 ? n - 2 : j);
+  const long long frac = U - (j << F);
+  const float scale = __int_as_float((127 - F) << 23); // 2^-F
+  if (frac > -(1LL << 47) && frac < (1LL << 47)) {
+    const int hi = static_cast<int>(frac >> 24), lo = static_cast<int>(frac & 0xffffff);
+    w = quick_two_sum(__int2float_rn(hi) * (scale * 16777216.0f), __int2float_rn(lo) * scale);
+  } else { // far off the grid
+    const ff f = ff_from_i64(frac);
+    w = ff_make(f.hi * scale, f.lo * scale);
+  }
+  return static_cast<int>(j);
 }
 
 // The reference's FP64 arithmetic for one element (inputs outside the float
@@ -112,7 +121,7 @@ __global__ void __launch_bounds__(SIE_BLOCK, MINB) sie_fill_fast(const FillArgs 
   __syncthreads();
   const SieTable &t = st;
   const unsigned out = a.output;
-  const bool rho_off = t.ffRhoOff[0] != 0.0f, e_off = t.ffEOff[0] != 0.0f;
+  const bool rho_off = t.lRhoOffset != 0.0, e_off = t.lEOffset != 0.0;
   const int ncE = t.nE - 1;
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
   for (long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; e < a.n;
@@ -123,11 +132,11 @@ __global__ void __launch_bounds__(SIE_BLOCK, MINB) sie_fill_fast(const FillArgs 
       sie_fill_fp64(t, a, e, rho, sie);
       continue;
     }
-    const ff lRho = to_log_ff(rho, t.ffRhoOff, rho_off);
-    const ff lE = to_log_ff(sie, t.ffEOff, e_off);
+    const long long vR = to_log_int(rho, t.lRhoOffset, rho_off);
+    const long long vE = to_log_int(sie, t.lEOffset, e_off);
     ff B, A;
-    const int j = cell_of(lRho, t.ffR_inv, t.ffR_off, t.nRhoE, B);
-    const int i = cell_of(lE, t.ffE_inv, t.ffE_off, t.nE, A);
+    const int j = cell_of(vR, t.fxM[0], t.fxOff[0], t.fxF[0], t.nRhoE, B);
+    const int i = cell_of(vE, t.fxM[1], t.fxOff[1], t.fxF[1], t.nE, A);
     const SieCellFF *c = t.cellsE + static_cast<long long>(j) * ncE + i;
     const ff AB = ff_mul(A, B);
     if ((out & Q_TEMPERATURE) && a.temp) a.temp[e] = ff2d(ff_cell(load_rec(&c->T), A, B, AB));
@@ -140,7 +149,7 @@ __global__ void __launch_bounds__(SIE_BLOCK, MINB) sie_fill_fast(const FillArgs 
           0x7ff0000000000000ULL |
           (static_cast<unsigned long long>(__float_as_uint(dn.hi) >> 31) << 63);
       a.cv[e] = dn.hi == 0.0f ? __longlong_as_double(static_cast<long long>(inf))
-                              : ff2d(ff_div(ff_make(1.0f), dn));
+                              : ff2d(ff_div_fast(ff_make(1.0f), dn));
     }
     if ((out & Q_BMOD) || a.cs) {
       const ff bm = ff_cell(load_rec(&c->bMod), A, B, AB);
@@ -156,7 +165,9 @@ __global__ void __launch_bounds__(SIE_BLOCK, MINB) sie_fill_fast(const FillArgs 
                       : sqrt(ff2d(BM) / rho);
       }
     }
-    if (a.lambda) a.lambda[e * a.lambda_stride] = ff2d(lRho);
+    if (a.lambda) // log10(rho) as the reference rounds it
+      a.lambda[e * a.lambda_stride] =
+          __dmul_rn(nqt::log2_over_log10, __dmul_rn(i64_to_f64_rn(vR), nqt::scale_down));
   }
 }
 

@@ -49,12 +49,13 @@ struct SieTable {
   const double *fE[NSE2D]; // rho-sie group
   const double *sieCold, *PlRhoMax, *dPdRhoMax, *rho_at_pmin;
   // float-float FillEos from (rho, sie): the cells [nRhoE-1][nE-1] (null when
-  // a value lies outside the float range) and, per axis, the cell
-  // coordinate u = lX * inv_dx - min * inv_dx as float pairs (hi, lo); the
-  // offsets of the density and energy coordinates likewise
+  // a value lies outside the float range) and, per axis (0 density, 1
+  // energy), the cell coordinate u = (lX - min) / dx in fixed point from
+  // the NQT log's integer v (lX = v scale_down log10(2)):
+  // u 2^fxF = mulhi64(v, fxM) - fxOff
   const SieCellFF *cellsE;
-  float ffE_inv[2], ffE_off[2], ffR_inv[2], ffR_off[2];
-  float ffRhoOff[2], ffEOff[2];
+  long long fxM[2], fxOff[2];
+  int fxF[2];
 };
 
 // DataBox::interpToReal(x2 = lRho, x1 = fast coordinate) on one group.

@@ -870,12 +870,24 @@ int table_load_spiner_sie(const char *path, int matid, bool reproducible, uint64
         rec(ge.f[G_DTDE], j, i, c.dTdE);
         rec(ge.f[G_BMOD], j, i, c.bMod);
       }
-    split(t.gE.inv_dx, t.ffE_inv);
-    split(t.gE.min * t.gE.inv_dx, t.ffE_off);
-    split(t.gRhoE.inv_dx, t.ffR_inv);
-    split(t.gRhoE.min * t.gRhoE.inv_dx, t.ffR_off);
-    split(t.lRhoOffset, t.ffRhoOff);
-    split(t.lEOffset, t.ffEOff);
+    // per axis: u = lX inv - min inv with lX = v K, K = scale_down
+    // log10(2); in fixed point with F fractional bits, u 2^F =
+    // floor(v M / 2^64) - Off, M = K inv 2^(64+F) in [2^60, 2^61) and
+    // |u 2^F| < 2^60 for |v| < 2^62. The products are formed in double-double
+    // (fma gives each rounding error exactly).
+    const Grid1D *ax[2] = {&t.gRhoE, &t.gE};
+    for (int k = 0; k < 2; ++k) {
+      const double a = nqt::scale_down, b = nqt::log2_over_log10, inv = ax[k]->inv_dx;
+      const double k1 = a * b, k1e = std::fma(a, b, -k1); // K = k1 + k1e
+      const double c1 = k1 * inv;
+      const double c1e = std::fma(k1, inv, -c1) + k1e * inv; // K inv = c1 + c1e
+      const int F = static_cast<int>(std::floor(-std::log2(c1))) - 3;
+      const double mh = std::ldexp(c1, 64 + F), ml = std::ldexp(c1e, 64 + F);
+      t.fxM[k] = std::llround(mh) + std::llround(ml);
+      const double o = ax[k]->min * inv, oe = std::fma(ax[k]->min, inv, -o);
+      t.fxOff[k] = std::llround(std::ldexp(o, F)) + std::llround(std::ldexp(oe, F));
+      t.fxF[k] = F;
+    }
   }
   const size_t offc = off;
   if (ff_ok) off = align(off + cells.size() * sizeof(SieCellFF));
