@@ -210,6 +210,30 @@ __device__ __noinline__ double unbracketed_lT(const SpinerTable &t, const double
   return lT;
 }
 
+// Grid1D::index and ::weights in FP64 (the rare queries whose FP32 cell
+// estimate lies within 1e-4 of a density node): the last cell takes
+// everything above it (the weight check of the caller keeps only the table's
+// own range). Out of line, keeping the rare path's FP64 code out of the hot
+// loop. Returns whether lRho lies at or above the grid's start.
+__device__ __noinline__ bool density_cell_fp64(const SpinerTable &t, const double lRho, int &j,
+                                               double &b1) {
+  const double u = __dmul_rn(__dsub_rn(lRho, t.gRho.min), t.gRho.inv_dx);
+  const bool fast = u >= 0.0;
+  j = !fast ? 0 : (u > static_cast<double>(t.nRho - 2) ? t.nRho - 2 : static_cast<int>(u));
+  b1 = __dmul_rn(__dsub_rn(lRho, __ldg(t.rhoNodes + j)), t.gRho.inv_dx);
+  return fast;
+}
+
+// cv on the table at the cell (j, i) and weights (a1, b1), in FP64 (out of
+// line, off the hot loop of the FillEos forms that do not ask for cv).
+__device__ __noinline__ double cv_fp64(const SpinerTable &t, const int j, const int i,
+                                       const double b1, const double a1) {
+  const double *d = t.f2[F_DEDT] + static_cast<long long>(j) * t.nT + i;
+  const double cv = b1 * (a1 * d[t.nT + 1] + (1.0 - a1) * d[t.nT]) +
+                    (1.0 - b1) * (a1 * d[1] + (1.0 - a1) * d[0]);
+  return cv > lim<double>::eps ? cv : lim<double>::eps;
+}
+
 // MINB: resident blocks per SM the registers are budgeted for (4: 64
 // registers, 5: 48, 6: 40).
 template <int MINB>
@@ -291,10 +315,8 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
       const long long fsq = fh * fh + ((fh * fl) >> 25);
       // two roundings, as lg_nqt then log10 (scale_down is the reference's
       // 15-digit literal, not exactly 2^-52)
-      // (the int64-to-double conversion in integers: it leaves the FP64 pipe
-      // to the roundings that must be the reference's)
       lRho = __dmul_rn(log2_over_log10,
-                       __dmul_rn(i64_to_f64_rn(x_as_int + ((frac - fsq) / 3)), scale_down));
+                       __dmul_rn(static_cast<double>(x_as_int + ((frac - fsq) / 3)), scale_down));
       // Grid1D::index and ::weights with the FP64 path's roundings: the
       // interpolant has a kink at every density node, so the cell must be the
       // reference's, and the root multiplies an error in b by dR / dT (up to
@@ -313,14 +335,7 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
         const long long bb = __double_as_longlong(b1);
         exact = !(bb >= 0 && bb <= 0x3FF0000000000000LL);
       }
-      if (exact) {
-        // Grid1D::index: the last cell takes everything above it (the weight
-        // check below keeps only the table's own range)
-        const double u = __dmul_rn(__dsub_rn(lRho, t.gRho.min), t.gRho.inv_dx);
-        fast = u >= 0.0;
-        j = !fast ? 0 : (u > static_cast<double>(t.nRho - 2) ? t.nRho - 2 : static_cast<int>(u));
-        b1 = __dmul_rn(__dsub_rn(lRho, __ldg(t.rhoNodes + j)), t.gRho.inv_dx);
-      }
+      if (exact) fast = density_cell_fp64(t, lRho, j, b1);
       B = ff_ok_bits(b1) ? d2ff(b1) : ff_make(0.0f);
       fast = fast && B.hi >= 0.0f && B.hi <= 1.0f;
     }
@@ -385,6 +400,8 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
         const SieRec *row = t.sieR + static_cast<long long>(j) * nc;
         bool ok = false;
         int edge = 0; // -1 / +1: sie below / above the whole row pair
+        // (one probe almost always; not unrolled)
+#pragma unroll 1
         for (int k = 0; k < 4; ++k) {
           const SieRec r = load_sie(row + i);
           // sie = x + a (dT + b dRT) + b dR: numerator and denominator in FP64
@@ -455,13 +472,7 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
                                                         : ff_sqrt(ff_div(BM, R)));
           }
         }
-        if ((out & Q_CV) && a.cv) {
-          const double a1 = ff2d(A);
-          const double *d = t.f2[F_DEDT] + static_cast<long long>(j) * t.nT + i;
-          const double cv = b1 * (a1 * d[t.nT + 1] + (1.0 - a1) * d[t.nT]) +
-                            (1.0 - b1) * (a1 * d[1] + (1.0 - a1) * d[0]);
-          a.cv[e] = cv > lim<double>::eps ? cv : lim<double>::eps;
-        }
+        if ((out & Q_CV) && a.cv) a.cv[e] = cv_fp64(t, j, i, b1, ff2d(A));
         if (a.lambda) {
           double *lam = a.lambda + e * a.lambda_stride;
           lam[0] = lRho;

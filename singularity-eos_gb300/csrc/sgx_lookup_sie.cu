@@ -114,6 +114,12 @@ __device__ __noinline__ void sie_fill_fp64(const SieTable &t, const FillArgs &a,
   if (a.lambda) a.lambda[e * a.lambda_stride] = lRho;
 }
 
+// sqrt(bmod / rho) in FP64 for the rare states the float-float form does
+// not take (out of line, off the hot loop).
+__device__ __noinline__ double cs_fp64(const double bmod, const double rho) {
+  return sqrt(bmod / rho);
+}
+
 template <int MINB>
 __global__ void __launch_bounds__(SIE_BLOCK, MINB) sie_fill_fast(const FillArgs a) {
   __shared__ SieTable st;
@@ -160,14 +166,15 @@ __global__ void __launch_bounds__(SIE_BLOCK, MINB) sie_fill_fast(const FillArgs 
         // inside the float range (and positive); the FP64 form otherwise
         const ff R = d2ff(rho);
         const float pr = BM.hi * R.hi;
-        a.cs[e] = (BM.hi > 0.0f && R.hi > 0.0f && pr > 1e-30f && pr < 1e30f)
-                      ? ff2d(ff_sqrt_ratio(BM, R))
-                      : sqrt(ff2d(BM) / rho);
+        if (BM.hi > 0.0f && R.hi > 0.0f && pr > 1e-30f && pr < 1e30f)
+          a.cs[e] = ff2d(ff_sqrt_ratio(BM, R));
+        else
+          a.cs[e] = cs_fp64(ff2d(BM), rho);
       }
     }
     if (a.lambda) // log10(rho) as the reference rounds it
       a.lambda[e * a.lambda_stride] =
-          __dmul_rn(nqt::log2_over_log10, __dmul_rn(i64_to_f64_rn(vR), nqt::scale_down));
+          __dmul_rn(nqt::log2_over_log10, __dmul_rn(static_cast<double>(vR), nqt::scale_down));
   }
 }
 

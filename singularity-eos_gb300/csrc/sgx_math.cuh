@@ -114,32 +114,6 @@ SGX_HD double as_f64(int64_t i) {
 #endif
 }
 
-// static_cast<double>(v) for |v| < 2^63 by integer operations: IEEE 754
-// round to nearest, ties to even, on the bits below the 53-bit significand.
-// Kernels that keep the FP64 pipe for the arithmetic that must round as the
-// reference's use it in place of the int64-to-double conversion.
-SGX_HD double i64_to_f64_rn(const int64_t v) {
-  if (v == 0) return 0.0;
-  const uint64_t sign = v < 0 ? (uint64_t(1) << 63) : 0;
-  const uint64_t a = v < 0 ? uint64_t(0) - uint64_t(v) : uint64_t(v);
-#if defined(__CUDA_ARCH__)
-  const int e = 63 - __clzll(static_cast<long long>(a));
-#else
-  const int e = 63 - __builtin_clzll(a);
-#endif
-  uint64_t m; // the significand with its leading bit, 2^52 <= m <= 2^53
-  if (e <= 52) {
-    m = a << (52 - e);
-  } else {
-    const int sh = e - 52;
-    const uint64_t rem = a & ((uint64_t(1) << sh) - 1), half = uint64_t(1) << (sh - 1);
-    m = a >> sh;
-    if (rem > half || (rem == half && (m & 1))) ++m;
-  }
-  // (e + 1022) << 52 plus m: the leading bit of m carries into the exponent
-  // (twice when rounding reached 2^53)
-  return as_f64(static_cast<int64_t>(sign | ((uint64_t(e + 1022) << 52) + m)));
-}
 namespace nqt {
 constexpr int64_t one = 1;
 constexpr int64_t one_as_int = (one << 62) - (one << 52);

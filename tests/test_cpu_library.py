@@ -225,21 +225,3 @@ def test_plan_and_derivative_argument_checks_without_gpu():
     assert lib.sgx_eos_eval(C.byref(g), 11, 4, C.c_void_p(16), C.c_void_p(16), C.c_void_p(16),
                             None, 0, None) == 5
 
-
-def test_integer_int64_to_double_conversion():
-    # the lookup's integer conversion rounds as the hardware conversion does
-    import shutil
-    import subprocess
-    import tempfile
-    gxx = shutil.which("g++")
-    if gxx is None:
-        pytest.skip("no host C++ compiler")
-    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    exe = os.path.join(tempfile.mkdtemp(prefix="sgx_i64_"), "check")
-    r = subprocess.run([gxx, "-O2", "-std=c++17", "-I",
-                        os.path.join(root, "singularity-eos_gb300", "csrc"),
-                        os.path.join(root, "tests", "cpp", "i64_to_f64_check.cpp"), "-o", exe],
-                       capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr
-    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
-    assert r.returncode == 0 and "bad=0" in r.stdout, r.stdout
