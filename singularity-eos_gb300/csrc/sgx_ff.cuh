@@ -216,34 +216,39 @@ __device__ __forceinline__ double f2d_bits(const float f) {
   return __longlong_as_double(static_cast<long long>(sign | (e64 << 52) | mant));
 }
 
-// hi + lo as a double, by integer operations: lo's significand is aligned
-// to hi's 2^(e-52) grid (bits below that grid are dropped, an error below
-// 2^-52 relative) and added to hi's; one renormalisation step covers the
-// carry or borrow. hi must be a normal float or zero (lo may be anything).
-__device__ __forceinline__ double ff2d(const ff x) {
+// hi + lo as a double, by 32-bit integer operations. The pair is first
+// renormalised (two_sum, exact), so |lo| <= ulp(hi) / 2; hi as a double then
+// has 29 zero bits below its float significand, and lo's significand,
+// aligned to hi's 2^(e-52) grid (bits below it dropped: an error below 2^-52
+// relative), is at most 2^28 units of that grid. It is added to or
+// subtracted from the low word of hi's bit pattern: an addition cannot
+// carry out of it, a subtraction borrows from the high word, and when hi is
+// a power of two that borrow moves the result into the binade below, whose
+// grid is twice as fine (the amount is counted twice). hi must be a normal
+// float or zero after the renormalisation (lo may be anything); zero, inf
+// and NaN come out as f2d_bits of hi.
+__device__ __forceinline__ double ff2d(const ff x0) {
+  const ff x = two_sum(x0.hi, x0.lo);
   const unsigned uh = __float_as_uint(x.hi), ul = __float_as_uint(x.lo);
-  const int eh = static_cast<int>((uh >> 23) & 0xff), el = static_cast<int>((ul >> 23) & 0xff);
-  if (eh == 0 || eh == 0xff) return f2d_bits(x.hi);
-  // hi as a 53-bit integer significand m (units 2^(eh-127-52))
-  long long m = static_cast<long long>((uh & 0x7fffff) | 0x800000) << 29;
-  if (el != 0) {
-    const long long ml = static_cast<long long>((ul & 0x7fffff) | 0x800000);
-    const int shift = eh - el; // lo = ml * 2^(el-127-23): 29 - shift bits above the grid
-    const long long add = shift <= 29 ? (ml << (29 - shift)) : (shift < 53 ? ml >> (shift - 29) : 0);
-    m += ((uh ^ ul) & 0x80000000u) ? -add : add;
+  const unsigned eh = (uh >> 23) & 0xffu, el = (ul >> 23) & 0xffu;
+  if (eh == 0u || eh == 0xffu) return f2d_bits(x.hi);
+  // hi as a double: high word sign | exponent | top 20 significand bits,
+  // low word the other 3 bits
+  int H = static_cast<int>((uh & 0x80000000u) | ((eh + 896u) << 20) | ((uh & 0x7fffffu) >> 3));
+  unsigned L = uh << 29;
+  if (el != 0u) {
+    const unsigned ml = (ul & 0x7fffffu) | 0x800000u;
+    const unsigned sh = eh - el; // >= 24 after the renormalisation
+    const unsigned add = sh <= 29u ? ml << (29u - sh) : (sh < 53u ? ml >> (sh - 29u) : 0u);
+    if ((uh ^ ul) & 0x80000000u) {
+      const unsigned sub = (uh & 0x7fffffu) == 0u ? add << 1 : add;
+      H -= L < sub ? 1 : 0;
+      L -= sub;
+    } else {
+      L += add;
+    }
   }
-  int e = eh;
-  if (m >= (1LL << 53)) {
-    m >>= 1;
-    ++e;
-  } else if (m < (1LL << 52)) {
-    m <<= 1;
-    --e;
-  }
-  const unsigned long long sign = static_cast<unsigned long long>(uh & 0x80000000u) << 32;
-  return __longlong_as_double(static_cast<long long>(
-      sign | (static_cast<unsigned long long>(e + 896) << 52) |
-      (static_cast<unsigned long long>(m) & ((1ULL << 52) - 1))));
+  return __hiloint2double(H, static_cast<int>(L));
 }
 
 // A float that holds an integer of magnitude < 2^62, as int64 (shift of the

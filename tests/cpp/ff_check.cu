@@ -1,0 +1,83 @@
+// Device check of sgx_ff.cuh's conversions between float-float and double:
+// ff2d(hi, lo) against the FP64 sum (double)hi + (double)lo over seeded
+// pairs of every magnitude, unnormalised pairs, exact powers of two with a
+// low part of the opposite sign, zero and subnormal low parts; d2ff round
+// trips. Prints "bad=<count>"; run by tests/test_gpu_ff.py.
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "sgx_ff.cuh"
+
+__global__ void conv(const float *hi, const float *lo, const double *d, double *out, double *rt,
+                     const int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = sgx::ff2d(sgx::ff_make(hi[i], lo[i]));
+  rt[i] = sgx::ff2d(sgx::d2ff(d[i]));
+}
+
+static double ulp(const double x) {
+  return std::nextafter(std::fabs(x), INFINITY) - std::fabs(x);
+}
+
+int main() {
+  const int n = 1 << 20;
+  std::mt19937_64 g(7);
+  std::uniform_real_distribution<double> u(-1.0, 1.0);
+  std::vector<float> hi(n), lo(n);
+  std::vector<double> d(n);
+  for (int i = 0; i < n; ++i) {
+    const int kind = i % 8;
+    const int e = static_cast<int>(g() % 200) - 100;
+    float h = static_cast<float>(std::ldexp(1.0 + std::fabs(u(g)), e)) * (u(g) < 0 ? -1.f : 1.f);
+    float l;
+    if (kind == 0) l = 0.0f;
+    else if (kind == 1) { h = std::ldexp(1.0f, e) * (u(g) < 0 ? -1.f : 1.f); l = -h * static_cast<float>(std::fabs(u(g))) * 5.9604645e-8f; }
+    else if (kind == 2) l = h * static_cast<float>(u(g)) * 1e-3f; // unnormalised
+    else if (kind == 3) l = std::ldexp(1.0f, -140) * static_cast<float>(u(g)); // subnormal low part
+    else l = h * static_cast<float>(u(g)) * 5.9604645e-8f;
+    hi[i] = h;
+    lo[i] = l;
+    d[i] = std::ldexp(u(g), static_cast<int>(g() % 190) - 70); // d2ff's range
+  }
+  float *dh, *dl;
+  double *dd, *dout, *drt;
+  cudaMalloc(&dh, n * 4);
+  cudaMalloc(&dl, n * 4);
+  cudaMalloc(&dd, n * 8);
+  cudaMalloc(&dout, n * 8);
+  cudaMalloc(&drt, n * 8);
+  cudaMemcpy(dh, hi.data(), n * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(dl, lo.data(), n * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(dd, d.data(), n * 8, cudaMemcpyHostToDevice);
+  conv<<<(n + 255) / 256, 256>>>(dh, dl, dd, dout, drt, n);
+  std::vector<double> out(n), rt(n);
+  if (cudaMemcpy(out.data(), dout, n * 8, cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(rt.data(), drt, n * 8, cudaMemcpyDeviceToHost) != cudaSuccess) {
+    std::printf("cuda error\n");
+    return 2;
+  }
+  long bad = 0;
+  for (int i = 0; i < n; ++i) {
+    // a subnormal low part is dropped (at most 2^-126 absolute)
+    const double lo_d = (std::fpclassify(lo[i]) == FP_SUBNORMAL) ? 0.0 : double(lo[i]);
+    const double want = double(hi[i]) + lo_d;
+    if (!(std::fabs(out[i] - want) <= ulp(want))) {
+      if (bad < 5) std::printf("ff2d %a %a -> %a want %a\n", hi[i], lo[i], out[i], want);
+      ++bad;
+    }
+    // d2ff keeps ~48 bits: the round trip within 2^-47 relative
+    if (!(std::fabs(rt[i] - d[i]) <= std::ldexp(std::fabs(d[i]), -47))) {
+      if (bad < 5) std::printf("round trip %a -> %a\n", d[i], rt[i]);
+      ++bad;
+    }
+  }
+  std::printf("bad=%ld\n", bad);
+  return bad != 0;
+}
