@@ -495,7 +495,7 @@ int sgx_tune_autotune_fill(const sgx_eos *eos, int64_t n, double *rho, double *t
 /* The autotuner of the mixed-precision PTE launch: times every combination
  * of SGX_TUNE_PTE_MIXED_BLOCK (32, 64, 128) and SGX_TUNE_PTE_COUNT_ORDER (0,
  * 1) -- and, with tune_group non-zero, SGX_TUNE_PTE_GROUP_MIN_N (the current
- * value, 2, 4, 7) -- on the caller's own RhoT batch (the arguments of
+ * value, 3, 4, 7) -- on the caller's own RhoT batch (the arguments of
  * sgx_pte_solve), 1 + reps solves per setting with CUDA events on `stream`,
  * and keeps the fastest set; chosen (nullable, 3 ints) receives (block,
  * order, group_min_n). The starting state is copied aside and restored

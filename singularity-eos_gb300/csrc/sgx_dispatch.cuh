@@ -493,6 +493,43 @@ SGX_HD double ev_min_pressure(const sgx_eos &e) { return md_min_pressure(e); }
 SGX_HDI double ev_max_pressure_at_T(const sgx_eos &e, const double T, int *err) {
   return md_max_pressure_at_T(e, T, err);
 }
+// RhoPmin in the caller's arithmetic type: the analytic models' 0 without
+// leaving it (for T = double the same value as ev_rho_pmin), the tabulated
+// and scaled ones through the FP64 form. Keeps float-double conversions,
+// which issue on the FP64 pipe, out of the FP32 Newton iterations.
+template <typename T> SGX_HD T ev_rho_pmin_t(const sgx_eos &e, const T temp) {
+  if (is_spiner(e) || is_spiner_sie(e) || (SGX_MODS(e) & SGX_MOD_SCALED))
+    return T(ev_rho_pmin(e, double(temp)));
+  return T(0);
+}
+// DensityEnergyFromPressureTemperature of the bare closed-form models
+// (eos_rho_sie_from_PT) in float, for the FP32 phase; false for the others,
+// which take the FP64 form.
+SGX_HD bool ev_rho_sie_from_PT_f(const sgx_eos &e, const float press, const float temp,
+                                 float &rho, float &sie) {
+  if (SGX_MODS(e)) return false;
+  const float gm1 = float(e.p[pi::gm1]), Cv = float(e.p[pi::Cv]);
+  switch (e.type) {
+  case SGX_IDEAL_GAS:
+    sie = mymax(0.0f, Cv * temp);
+    rho = mymax(0.0f, press / (gm1 * sie));
+    return true;
+  case SGX_STIFF_GAS: {
+    const float Pinf = float(e.p[pi::Pinf]), qq = float(e.p[pi::qq]);
+    sie = smax(qq, ratio(press + (gm1 + 1.0f) * Pinf, press + Pinf) * Cv * temp + qq);
+    rho = smax(lim<float>::small, ratio(press + Pinf, gm1 * Cv * temp));
+    return true;
+  }
+  case SGX_NOBLE_ABEL: {
+    const float qq = float(e.p[pi::qq]);
+    sie = smax(qq, Cv * temp + qq);
+    rho = smax(lim<float>::small, ratio(press, gm1 * Cv * temp + float(e.p[pi::bb]) * press));
+    return true;
+  }
+  }
+  return false;
+}
+
 // The temperature of ValuesAtReferenceState; no modifier changes it.
 SGX_HD double ev_reference_T(const sgx_eos &e) { return md_reference_T(e); }
 // ValuesAtReferenceState through the modifiers: ScaledEOS divides rho by

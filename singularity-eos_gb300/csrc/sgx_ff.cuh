@@ -218,15 +218,16 @@ __device__ __forceinline__ double f2d_bits(const float f) {
 
 // hi + lo as a double, by 32-bit integer operations. The pair is first
 // renormalised (two_sum, exact), so |lo| <= ulp(hi) / 2; hi as a double then
-// has 29 zero bits below its float significand, and lo's significand,
-// aligned to hi's 2^(e-52) grid (bits below it dropped: an error below 2^-52
-// relative), is at most 2^28 units of that grid. It is added to or
-// subtracted from the low word of hi's bit pattern: an addition cannot
-// carry out of it, a subtraction borrows from the high word, and when hi is
-// a power of two that borrow moves the result into the binade below, whose
-// grid is twice as fine (the amount is counted twice). hi must be a normal
-// float or zero after the renormalisation (lo may be anything); zero, inf
-// and NaN come out as f2d_bits of hi.
+// has 29 zero bits below its float significand, and lo's significand
+// (subnormal ones included), aligned to hi's 2^(e-52) grid (bits below it
+// dropped: an error below 2^-52 relative), is at most 2^28 units of that
+// grid. It is added to or subtracted from the low word of hi's bit pattern:
+// an addition cannot carry out of it, a subtraction borrows from the high
+// word, and when hi is a power of two that borrow moves the result into the
+// binade below, so the amount is aligned to that binade's grid, twice as
+// fine, instead. hi must be a normal float or zero after the
+// renormalisation (lo may be anything); zero, inf and NaN come out as
+// f2d_bits of hi.
 __device__ __forceinline__ double ff2d(const ff x0) {
   const ff x = two_sum(x0.hi, x0.lo);
   const unsigned uh = __float_as_uint(x.hi), ul = __float_as_uint(x.lo);
@@ -236,14 +237,16 @@ __device__ __forceinline__ double ff2d(const ff x0) {
   // low word the other 3 bits
   int H = static_cast<int>((uh & 0x80000000u) | ((eh + 896u) << 20) | ((uh & 0x7fffffu) >> 3));
   unsigned L = uh << 29;
-  if (el != 0u) {
-    const unsigned ml = (ul & 0x7fffffu) | 0x800000u;
-    const unsigned sh = eh - el; // >= 24 after the renormalisation
-    const unsigned add = sh <= 29u ? ml << (29u - sh) : (sh < 53u ? ml >> (sh - 29u) : 0u);
+  if ((ul & 0x7fffffffu) != 0u) {
+    // lo = ml 2^(el - 150), el = 1 for a subnormal lo
+    const unsigned ml = el != 0u ? ((ul & 0x7fffffu) | 0x800000u) : (ul & 0x7fffffu);
+    const bool down = ((uh ^ ul) & 0x80000000u) && (uh & 0x7fffffu) == 0u;
+    // the grid 2^(eh - 179 - down) in units of which lo is counted
+    const unsigned sh = eh - (el != 0u ? el : 1u) - (down ? 1u : 0u); // >= 23
+    const unsigned add = sh <= 29u ? ml << (29u - sh) : (sh < 61u ? ml >> (sh - 29u) : 0u);
     if ((uh ^ ul) & 0x80000000u) {
-      const unsigned sub = (uh & 0x7fffffu) == 0u ? add << 1 : add;
-      H -= L < sub ? 1 : 0;
-      L -= sub;
+      H -= L < add ? 1 : 0;
+      L -= add;
     } else {
       L += add;
     }

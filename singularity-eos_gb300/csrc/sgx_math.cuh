@@ -90,6 +90,9 @@ SGX_HD bool is_normal_d(double v) {
 SGX_HD bool bad_value(double v) {
   return !((v == 0.0) || (is_normal_d(1.0e10 * v) && is_normal_d(v)));
 }
+// bad_value(double(v)) for a float v, without the conversion: only an
+// infinite or NaN float is bad once widened.
+SGX_HD bool mix_bad_f(float v) { return !(v - v == 0.0f); }
 
 // ---------------------------------------------------------------------------
 // NQT order-2 transforms (base/fast-math/logs.hpp:188-214, 282-292): an

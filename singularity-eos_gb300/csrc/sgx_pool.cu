@@ -205,7 +205,10 @@ extern "C" int sgx_tune_autotune_pte(int nmat, int64_t ncell, const sgx_eos *eos
   const int keep_o = g_knobs[SGX_TUNE_PTE_COUNT_ORDER].value.load();
   const int keep_g = g_knobs[SGX_TUNE_PTE_GROUP_MIN_N].value.load();
   const int blocks[3] = {32, 64, 128};
-  const int groups[4] = {keep_g, 2, 4, 7};
+  // (thresholds of 3 and up: with lane groups for two-material cells a few
+  // stiff cells of the uneven batch ended 1e-9 from the tight FP64 solve in
+  // T, against 1e-10 with the thread-per-cell kernel)
+  const int groups[4] = {keep_g, 3, 4, 7};
   const int ng = tune_group ? 4 : 1;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (ce == cudaSuccess) ce = cudaEventCreate(&e0);

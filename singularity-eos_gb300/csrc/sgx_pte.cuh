@@ -276,7 +276,7 @@ template <typename T, int N, int NEQ> struct PteBase {
       vfrac[m] *= ratio(vfrac_total, vfrac_sum);
   }
   SGX_HD T vfrac_max(int m, T Tk) const {
-    const T rho_min = T(ev_rho_pmin(*eos[m], double(Tk)));
+    const T rho_min = ev_rho_pmin_t<T>(*eos[m], Tk);
     return smin(T(0.9) * ratio(rhobar[m], rho_min), T(1.0));
   }
   // SetVfracFromT (:423-498); true = FAIL
@@ -316,6 +316,17 @@ template <typename T, int N, int NEQ> struct PteBase {
   SGX_HD void sie_cv_pref(int m, T r, const T Pin, const T Tk, T &s, T &cv) const {
     const sgx_eos &e = *eos[m];
     if (preferred_input(e) & Q_PRESSURE) {
+      if constexpr (sizeof(T) == sizeof(float)) {
+        // the FP32 phase: a closed-form model with a usable pressure needs
+        // no FP64 (its maximum pressure is 1e100, beyond any float)
+        T rf, sf;
+        if (!mix_bad_f(Pin) && ev_rho_sie_from_PT_f(e, smax(T(ev_min_pressure(e)), Pin), Tk, rf,
+                                                    sf)) {
+          s = sf;
+          cv = ev_cv_from_rho_sie<T>(e, rf, sf, lam[m]);
+          return;
+        }
+      }
       int err = 0;
       const T Pmin = T(ev_min_pressure(e));
       const T Pmax = T(ev_max_pressure_at_T(e, double(Tk), &err));
@@ -586,8 +597,8 @@ template <typename T, int N> struct PteRhoT : PteBase<T, N, N> {
     idx = 1;
 #pragma unroll
     for (int m = 0; m < n; m++) {
-      const T rho_min = T(smax(ev_rho_pmin(*eos[m], double(Tnorm * Tequil)),
-                               ev_rho_pmin(*eos[m], double(Tnorm * Tnew))));
+      const T rho_min = smax(ev_rho_pmin_t<T>(*eos[m], Tnorm * Tequil),
+                             ev_rho_pmin_t<T>(*eos[m], Tnorm * Tnew));
       const T alpha_max = smin(T(1.0), ratio(rhobar[m], rho_min));
       if (alpha_max < vfrac[m]) continue;
       const T mydx = (m == ms) ? dalphaskip : dx[idx++];

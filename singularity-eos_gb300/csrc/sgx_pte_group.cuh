@@ -125,6 +125,13 @@ template <int N, int G> struct GroupRhoT {
   __device__ void sie_cv_pref(float r, const float Pin, const float Tk, float &s, float &cv) const {
     const sgx_eos &e = *m.eos;
     if (m.pref & Q_PRESSURE) {
+      // a closed-form model with a usable pressure needs no FP64 (its
+      // maximum pressure is 1e100, beyond any float)
+      if (!mix_bad_f(Pin) && ev_rho_sie_from_PT_f(e, smax(float(ev_min_pressure(e)), Pin), Tk, r,
+                                                  s)) {
+        cv = ev_cv_from_rho_sie<float>(e, r, s, m.lam);
+        return;
+      }
       int err = 0;
       const float Pmin = float(ev_min_pressure(e));
       const float Pmax = float(ev_max_pressure_at_T(e, double(Tk), &err));
@@ -140,7 +147,7 @@ template <int N, int G> struct GroupRhoT {
     }
   }
   __device__ float vfrac_max(const float Tk) const {
-    const float rho_min = float(ev_rho_pmin(*m.eos, double(Tk)));
+    const float rho_min = ev_rho_pmin_t<float>(*m.eos, Tk);
     return smin(0.9f * ratio(m.rhobar, rho_min), 1.0f);
   }
   __device__ void normalize_vfrac() {
@@ -189,7 +196,7 @@ template <int N, int G> struct GroupRhoT {
         continue;
       }
       if (act) m.rho = ratio(m.rhobar, m.vf);
-      const bool bad = g.any(act && m.rho < float(ev_rho_pmin(*m.eos, double(Tguess))));
+      const bool bad = g.any(act && m.rho < ev_rho_pmin_t<float>(*m.eos, Tguess));
       if (!bad) break;
       Tguess *= 10.0f;
     }
@@ -294,8 +301,8 @@ template <int N, int G> struct GroupRhoT {
     const float Tnew = Tequil + scale * dx0;
     c = 1.0f;
     if (act) {
-      const float rho_min = float(smax(ev_rho_pmin(*m.eos, double(Tnorm * Tequil)),
-                                       ev_rho_pmin(*m.eos, double(Tnorm * Tnew))));
+      const float rho_min = smax(ev_rho_pmin_t<float>(*m.eos, Tnorm * Tequil),
+                                 ev_rho_pmin_t<float>(*m.eos, Tnorm * Tnew));
       const float alpha_max = smin(1.0f, ratio(m.rhobar, rho_min));
       if (!(alpha_max < m.vf) && scale * mydx > 0.5f * (alpha_max - m.vf))
         c = ratio(0.5f * (alpha_max - m.vf), mydx);
