@@ -466,6 +466,9 @@ int sgx_mix_enforce_energies_sum(int nmat, int64_t ncell, const int32_t *eos_idx
  *      or 8 lanes per cell (one material per lane), and smaller cells with
  *      one thread each; 7 keeps one thread per cell everywhere. Both forms
  *      meet the same tolerance; their results differ in rounding.
+ *  SGX_TUNE_PTE_FP32_TOL  3..6 (default 4): the FP32 Newton phase of the
+ *      mixed path iterates to relative residuals of 10^-value before the
+ *      FP64 residual correction (which ends at 1e-12 either way).
  */
 enum {
   SGX_TUNE_LOOKUP_BLOCKS_PER_SM = 1,
@@ -476,7 +479,8 @@ enum {
   SGX_TUNE_PTE_RETRY_ITERS = 6,
   SGX_TUNE_PTE_COUNT_ORDER = 7,
   SGX_TUNE_PTE_MIXED_BLOCK = 8,
-  SGX_TUNE_PTE_GROUP_MIN_N = 9
+  SGX_TUNE_PTE_GROUP_MIN_N = 9,
+  SGX_TUNE_PTE_FP32_TOL = 10
 };
 int sgx_tune_set(int knob, int value);
 int sgx_tune_get(int knob, int *value);

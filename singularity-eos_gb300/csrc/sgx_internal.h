@@ -46,6 +46,8 @@ struct PteArgs {
   int *retry_idx;
   // iteration limits per material of pass 1 (FP32) and pass 2 (FP64)
   int fp32_iters, retry_iters;
+  // the FP32 phase's relative residual tolerance, 10^-fp32_tol_exp
+  int fp32_tol_exp;
 };
 constexpr int PTE_BINS = 8;
 // Cells are binned by material count and by the ordered EOS types of their

@@ -203,6 +203,7 @@ cudaError_t launch_pte_mixed_with(const PteArgs &args, int *perm, cudaStream_t s
   PteArgs a = args;
   a.perm = nullptr;
   a.fp32_iters = tune_get(SGX_TUNE_PTE_FP32_ITERS);
+  a.fp32_tol_exp = tune_get(SGX_TUNE_PTE_FP32_TOL);
   a.retry_iters = tune_get(SGX_TUNE_PTE_RETRY_ITERS);
   cudaError_t e = cudaMemsetAsync(a.bins, 0, a.eos_idx ? PTE_BINS_BYTES : 256, stream);
   if (e != cudaSuccess) return e;

@@ -77,6 +77,7 @@ Knob g_knobs[] = {
     {{0}, 0, 1},    // SGX_TUNE_PTE_COUNT_ORDER
     {{128}, 32, 128}, // SGX_TUNE_PTE_MIXED_BLOCK
     {{3}, 2, 7},      // SGX_TUNE_PTE_GROUP_MIN_N
+    {{4}, 3, 6},      // SGX_TUNE_PTE_FP32_TOL
 };
 constexpr int NKNOBS = sizeof(g_knobs) / sizeof(g_knobs[0]);
 } // namespace

@@ -488,7 +488,7 @@ __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_group_kernel(const PteArg
   const float temp_in = act ? static_cast<float>(a.temp[k]) : 0.0f;
   const float press_in = act ? static_cast<float>(a.press[k]) : 0.0f;
   // ---- FP32 phase ----
-  const MixP<float> mp32 = fp32_params(a.params, a.fp32_iters);
+  const MixP<float> mp32 = fp32_params(a.params, a.fp32_iters, a.fp32_tol_exp);
   GroupRhoT<N, G> f(g);
   f.act = act;
   f.P = &mp32;

@@ -36,16 +36,19 @@ constexpr int PTE_MIXED_BLOCK = 128;
 constexpr int SGX_REFINE_STEPS = 6;
 constexpr double SGX_REFINE_TOL = 1e-12;
 
-// FP32-phase controls: the reference's, with tolerances FP32 can reach.
-SGX_HDI MixP<float> fp32_params(const sgx_mix_params &q, const int iters_per_mat = 8) {
+// FP32-phase controls: the reference's, with tolerances FP32 can reach
+// (10^-tol_exp, the "sufficient" ones ten times looser).
+SGX_HDI MixP<float> fp32_params(const sgx_mix_params &q, const int iters_per_mat = 8,
+                                const int tol_exp = 4) {
   MixP<float> m(q);
+  const float tol = tol_exp >= 6 ? 1e-6f : (tol_exp == 5 ? 1e-5f : (tol_exp <= 3 ? 1e-3f : 1e-4f));
   m.derivative_eps = 2.5e-4f;
-  m.tol_p = 1e-4f;
-  m.tol_e = 1e-4f;
-  m.abs_p = 1e-4f;
-  m.tol_p_suff = 1e-3f;
-  m.tol_e_suff = 1e-3f;
-  m.abs_p_suff = 1e-3f;
+  m.tol_p = tol;
+  m.tol_e = tol;
+  m.abs_p = tol;
+  m.tol_p_suff = 10.0f * tol;
+  m.tol_e_suff = 10.0f * tol;
+  m.abs_p_suff = 10.0f * tol;
   m.max_iter_per_mat = iters_per_mat;
   m.small_step_thresh = 1e-7f;
   return m;
@@ -201,7 +204,7 @@ __global__ void __launch_bounds__(PTE_MIXED_BLOCK) pte_mixed_kernel(const PteArg
   const long long nc = a.ncell;
   double cache[N][3];
   // ---- FP32 phase ----
-  const MixP<float> mp32 = fp32_params(a.params, a.fp32_iters);
+  const MixP<float> mp32 = fp32_params(a.params, a.fp32_iters, a.fp32_tol_exp);
   PteRhoT<float, N> f;
   f.P = &mp32;
   f.vfrac_total = static_cast<float>(a.vfrac_tot[i]);
