@@ -177,12 +177,33 @@ __device__ __forceinline__ bool ff_lt(const ff a, const ff b) {
 
 // ---- conversions through the bit patterns ----
 
+// The two 32-bit words of a double's bit pattern, through a move the
+// compiler cannot see into: tests of the pattern then stay integer
+// instructions. (A test of the 64-bit pattern with the sign masked off
+// against zero is otherwise folded into a floating-point compare with 0.0,
+// which issues on the FP64 pipe.)
+__device__ __forceinline__ void d_words(const double x, unsigned &lo, unsigned &hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "d"(x));
+}
+// x == +-0, as an integer test
+__device__ __forceinline__ bool d_zero_bits(const double x) {
+  unsigned lo, hi;
+  d_words(x, lo, hi);
+  return ((hi & 0x7fffffffu) | lo) == 0u;
+}
+// x == +-0, or its unbiased binary exponent in [emin, emax]
+__device__ __forceinline__ bool d_zero_or_exp_in(const double x, const int emin, const int emax) {
+  unsigned lo, hi;
+  d_words(x, lo, hi);
+  const int e = static_cast<int>((hi >> 20) & 0x7ffu) - 1023;
+  return ((hi & 0x7fffffffu) | lo) == 0u || (e >= emin && e <= emax);
+}
+
 // Whether d2ff below represents x to ~48 bits: x == 0, or its binary
 // exponent in [-74, 127] (then hi is a normal float and lo does not
 // underflow).
 __device__ __forceinline__ bool ff_from_double_ok(const double x) {
-  const int e = static_cast<int>((__double_as_longlong(x) >> 52) & 0x7ff) - 1023;
-  return x == 0.0 || (e >= -74 && e <= 127);
+  return d_zero_or_exp_in(x, -74, 127);
 }
 
 // hi: x truncated to 24 significant bits; lo: the remaining 29 bits,

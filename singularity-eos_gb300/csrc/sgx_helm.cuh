@@ -50,6 +50,11 @@ struct HelmTable {
   double lRhoMin, lRhoMax, dlRho, inv_dlRho;
   double lTMin, lTMax, dlT, inv_dlT;
   double rhoMin, rhoMax;
+  // The FP32 phase's copies, rounded to float at load (a double-to-float
+  // conversion issues on the FP64 pipe): the nodes (with cells32) and the
+  // grid constants
+  const float *rho32, *T32;
+  float f_lRhoMin, f_lRhoMax, f_inv_dlRho, f_lTMin, f_inv_dlT, f_rhoMin, f_rhoMax;
 };
 
 namespace helm {
@@ -743,17 +748,16 @@ __device__ __forceinline__ bool e_of_T32(const HelmTable &t, const int opt, cons
     dedT += k15 * y;
     if (degenerate) {
       if (!t.cells32) return false;
-      const float De = fminf(static_cast<float>(t.rhoMax), fmaxf(static_cast<float>(t.rhoMin), c.De));
-      const float lDe = fminf(static_cast<float>(t.lRhoMax),
-                              fmaxf(static_cast<float>(t.lRhoMin), c.lDe));
-      float u = (lDe - static_cast<float>(t.lRhoMin)) * static_cast<float>(t.inv_dlRho);
+      const float De = fminf(t.f_rhoMax, fmaxf(t.f_rhoMin, c.De));
+      const float lDe = fminf(t.f_lRhoMax, fmaxf(t.f_lRhoMin, c.lDe));
+      float u = (lDe - t.f_lRhoMin) * t.f_inv_dlRho;
       const int iat = !(u >= 0.0f) ? 0 : (u > HELM_NRHO - 2 ? HELM_NRHO - 2 : static_cast<int>(u));
-      u = (lT - static_cast<float>(t.lTMin)) * static_cast<float>(t.inv_dlT);
+      u = (lT - t.f_lTMin) * t.f_inv_dlT;
       const int jat = !(u >= 0.0f) ? 0 : (u > HELM_NT - 2 ? HELM_NT - 2 : static_cast<int>(u));
-      const float Tj = static_cast<float>(t.T[jat]);
-      const float dth = static_cast<float>(t.T[jat + 1]) - Tj;
-      const float ri = static_cast<float>(t.rho[iat]);
-      const float dd = static_cast<float>(t.rho[iat + 1]) - ri;
+      const float Tj = __ldg(t.T32 + jat);
+      const float dth = __ldg(t.T32 + jat + 1) - Tj;
+      const float ri = __ldg(t.rho32 + iat);
+      const float dd = __ldg(t.rho32 + iat + 1) - ri;
       const float xt = fmaxf(0.0f, (T - Tj) / dth), xd = fmaxf(0.0f, (De - ri) / dd);
       const float mxt = 1.0f - xt, mxd = 1.0f - xd;
       const float wd[6] = {fpsi0(xd), fpsi0(mxd), fpsi1(xd), fpsi1(mxd), fpsi2(xd), fpsi2(mxd)};

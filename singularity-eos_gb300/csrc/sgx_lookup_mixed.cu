@@ -19,17 +19,20 @@
 //      the reference's roundings). Off-top states, non-monotone tables and
 //      tables with values outside the float range take the reference's FP64
 //      iteration unchanged;
-//   3. binary search for the bracketing T cell over the FP32 corner-packed
-//      copy of sie (8 probes for 256 nodes, one 16-byte load each);
+//   3. the bracketing T cell from the per-row thermal-energy bin index (one
+//      16-bit load per density row, then 0-2 probes of the FP32
+//      corner-packed copy of sie), or by binary search over that copy for
+//      tables without the index;
 //   4. the cell's bilinear form in difference form, sie = s00 + a dT + b dR
 //      + a b dRT (differences formed in FP64 at load), solved for a: the
 //      numerator sie - s00 - b dR, which cancels where the cold energy
 //      dominates, and the denominator by FP64 fma, the quotient in ff. A
 //      target under (over) the whole row pair is one the reference's regula
 //      falsi cannot bracket: its answer is then its guess, reproduced here;
-//   5. T = 10^lT by the NQT pow (logs.hpp:202-214) in integers, with its
-//      square root in float-float; P, bmod and cs from their difference-form
-//      cells at (a, b), each rounded to double once.
+//   5. T = 10^lT by the NQT pow (logs.hpp:202-214) in integers: its
+//      argument lT log10(2)^-1 2^52 in fixed point from the cell position
+//      (nqt_arg), its square root in float-float; P, bmod and cs from their
+//      difference-form cells at (a, b), each rounded to double once.
 // Accuracy against the FP64 path: T within ~1e-13 relative plus the
 // conditioning of the root itself (about eps * sie / (dsie/dlT) where the
 // cold energy dominates), P, bmod and cs within 1e-10 of the larger of the
@@ -61,16 +64,77 @@ namespace {
 
 constexpr int LOOKUP_BLOCK = 256;
 
-// Constants of one table, in float-float, shared by a block.
+// Constants of one table, shared by a block.
 struct FfConsts {
   float rho_min_f, rho_inv_f; // density grid in FP32, for the cell estimate
   ff t_min, t_dx;      // temperature grid: lT min and dlT (lambda cache)
-  ff p_min, p_dx;      // the same scaled by log10(2)^-1 * 2^52 (NQT pow integer)
-  ff p_lo, p_hi;       // on-table lT bounds (getLocDependsRhoT_), scaled alike
+  // The NQT pow's integer argument X = lT log10(2)^-1 2^52 at the cell
+  // position i + a of the T grid (nqt_arg): the nodes in fixed point,
+  // (pm + i pd) 2^-fx, and the cell width pd as float-float with the split
+  // 2^sh of a pd into integers (|a pd| < 2^(sh + 22), sh >= 22)
+  long long pm, pd;
+  int fx, sh;
+  float pdh, pdl;
+  float split, split_inv, m2; // 2^sh, 2^-sh, 1.5 2^(sh + 1)
+  long long x_lo, x_hi; // on-table X (getLocDependsRhoT_), a guard band inside
+  bool x_ok;            // the grid's X fits these forms
   ff eps;
 };
 
 __device__ __forceinline__ ff ff_of_int(const int i) { return ff_make(static_cast<float>(i)); }
+
+// X = lT log10(2)^-1 2^52 at the T-cell position i + a (a in [0, 1]): the
+// node's value from the fixed-point constants, plus a pd as a float-float
+// product rounded to an integer by two magic-number additions (the high
+// part to multiples of 2^sh, the rest to multiples of 2^(sh - 22)). About
+// 30 units of an integer of magnitude ~2^55 (a's own ~2^-45 included),
+// where the float-float sum of the scaled lT it replaces carried ~100.
+__device__ __forceinline__ long long nqt_arg(const FfConsts &c, const int i, const ff A) {
+  constexpr float M1 = 12582912.0f; // 1.5 2^23: y + M1 rounds |y| < 2^22 to an integer
+  const long long xb = (c.pm + static_cast<long long>(i) * c.pd) >> c.fx;
+  const float ph = __fmul_rn(A.hi, c.pdh);
+  const float pl = fmaf(A.lo, c.pdh, fmaf(A.hi, c.pdl, fmaf(A.hi, c.pdh, -ph)));
+  const float y1 = fmaf(ph, c.split_inv, M1);
+  const int xh = __float_as_int(y1) - __float_as_int(M1);
+  // ph - xh 2^sh, exact (|.| <= 2^(sh - 1), on ph's grid)
+  const float r = fmaf(-__fsub_rn(y1, M1), c.split, ph);
+  // m2's binade has the grid 2^(sh - 22) and holds m2 + y for |y| < 2^sh
+  const float y2 = __fadd_rn(__fadd_rn(r, pl), c.m2);
+  const int xl = __float_as_int(y2) - __float_as_int(c.m2);
+  return xb + (static_cast<long long>(xh) << c.sh) + (static_cast<long long>(xl) << (c.sh - 22));
+}
+
+// pow2_nqt's result (logs.hpp:202-214) from its integer argument X: the
+// square root 2^26 sqrt(c - 3 frac) in float-float (one Newton step on the
+// correctly rounded float root), its two parts truncated to integers by
+// their bit fields (2^26 hi has 53 bits; |2^26 lo| < 2^29).
+__device__ __forceinline__ double nqt_pow_int(const long long X) {
+  using namespace nqt;
+  constexpr long long ca = 1LL << 53, cc = 1LL << 54;
+  const long long frac = X & mantissa_mask;
+  const long long N = cc - 3 * frac; // in (2^52, 2^54]
+  const ff NF = quick_two_sum(static_cast<float>(static_cast<int>(N >> 30)) * 1073741824.0f,
+                              static_cast<float>(static_cast<int>(N & ((1LL << 30) - 1))));
+  const ff SQ = ff_sqrt_fast(NF);
+  const unsigned uh = __float_as_uint(SQ.hi), ul = __float_as_uint(SQ.lo);
+  // 2^26 x = m 2^(e - 124) for a float x of biased exponent e, significand m
+  const long long fhi = static_cast<long long>((uh & 0x7fffffu) | 0x800000u)
+                        << (static_cast<int>(uh >> 23) - 124);
+  const int sl = static_cast<int>((ul >> 23) & 0xffu) - 124;
+  const unsigned ml = (ul & 0x7fffffu) | 0x800000u;
+  int flo = sl >= 0 ? static_cast<int>(ml << sl) : static_cast<int>(ml >> (-sl < 31 ? -sl : 31));
+  flo = (ul & 0x7fffffffu) == 0u ? 0 : flo;
+  flo = (ul & 0x80000000u) ? -flo : flo;
+  return __longlong_as_double(X + ca - (fhi + flo) - frac + one_as_int);
+}
+
+// T and the on-table test for the reference's guess lT (roots its regula
+// falsi cannot bracket), in FP64 as the reference computes both.
+__device__ __noinline__ bool guess_T(const SpinerTable &t, const double lT, double &temp) {
+  if (sp_loc_rho_T(t, 0.0, lT) != TableStatus::OnTable) return false;
+  temp = sp_T(t, lT);
+  return true;
+}
 
 __device__ __forceinline__ SieRec load_sie(const SieRec *p) {
   SieRec r;
@@ -81,21 +145,25 @@ __device__ __forceinline__ SieRec load_sie(const SieRec *p) {
 }
 
 // Integer tests of a double's bit pattern (no FP64 pipe).
-__device__ __forceinline__ bool d_is_zero(const double x) {
-  return (__double_as_longlong(x) & 0x7fffffffffffffffLL) == 0;
-}
+__device__ __forceinline__ bool d_is_zero(const double x) { return d_zero_bits(x); }
 // The unbiased binary exponent of x (normal x).
 __device__ __forceinline__ int d_exp(const double x) {
   return static_cast<int>((__double_as_longlong(x) >> 52) & 0x7ff) - 1023;
 }
 // x > 0 and not NaN (for the callers' range checks that follow)
-__device__ __forceinline__ bool d_positive(const double x) { return __double_as_longlong(x) > 0; }
-// ff_from_double_ok without a floating-point compare
-__device__ __forceinline__ bool ff_ok_bits(const double x) {
-  const long long b = __double_as_longlong(x);
-  const int e = static_cast<int>((b >> 52) & 0x7ff) - 1023;
-  return (b & 0x7fffffffffffffffLL) == 0 || (e >= -74 && e <= 127);
+__device__ __forceinline__ bool d_positive(const double x) {
+  unsigned lo, hi;
+  d_words(x, lo, hi);
+  return (hi >> 31) == 0u && (hi | lo) != 0u;
 }
+// x in [+0, 1] (non-negative doubles order as their bit patterns)
+__device__ __forceinline__ bool d_in_unit(const double x) {
+  unsigned lo, hi;
+  d_words(x, lo, hi);
+  return hi < 0x3FF00000u || (hi == 0x3FF00000u && lo == 0u);
+}
+// ff_from_double_ok
+__device__ __forceinline__ bool ff_ok_bits(const double x) { return d_zero_or_exp_in(x, -74, 127); }
 
 // One bulk copy (cp.async.bulk, the TMA engine) of `bytes` (a multiple of
 // 16, both addresses 16-byte aligned) from global to shared memory, issued
@@ -248,11 +316,31 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
     sc.rho_inv_f = d2ff(st.gRho.inv_dx).hi;
     sc.t_min = d2ff(st.gT.min);
     sc.t_dx = d2ff(st.gT.dx);
-    const ff p2 = d2ff(nqt::log10_over_log2 * nqt::scale_up);
-    sc.p_min = ff_mul(sc.t_min, p2);
-    sc.p_dx = ff_mul(sc.t_dx, p2);
-    sc.p_lo = ff_mul(d2ff((1 + SP_SOFT_THRESH) * st.lTMin), p2);
-    sc.p_hi = ff_mul(d2ff((1 - SP_SOFT_THRESH) * st.lTMax), p2);
+    // X = lT K; the nodes' X in fixed point with 2^fx their largest |X|
+    // below 2^62, the cell width as float-float
+    const double K = nqt::log10_over_log2 * nqt::scale_up;
+    const double pmin = st.gT.min * K, pdx = st.gT.dx * K;
+    const double mx = fabs(pmin) + (st.gT.n - 1) * fabs(pdx) + 1.0;
+    sc.fx = 61 - ilogb(mx);
+    sc.sh = ilogb(pdx) - 21;
+    sc.sh = sc.sh < 22 ? 22 : sc.sh;
+    sc.x_ok = sc.fx >= 0 && pdx > 0.0 && sc.sh <= 40 && ff_ok_bits(pdx);
+    if (sc.x_ok) {
+      sc.pm = llrint(ldexp(pmin, sc.fx));
+      sc.pd = llrint(ldexp(pdx, sc.fx));
+      const ff pd = d2ff(pdx);
+      sc.pdh = pd.hi;
+      sc.pdl = pd.lo;
+      sc.split = ldexpf(1.0f, sc.sh);
+      sc.split_inv = ldexpf(1.0f, -sc.sh);
+      sc.m2 = ldexpf(1.5f, sc.sh + 1);
+      // the reference's bounds, a band of 2^20 units (~3e-11 of lT) inside
+      // them, far wider than X's error against the FP64 root, so that a
+      // state the fast path answers is one the reference finds on the table
+      constexpr long long band = 1LL << 20;
+      sc.x_lo = llrint(floor((1 + SP_SOFT_THRESH) * st.lTMin * K)) + band;
+      sc.x_hi = llrint(ceil((1 - SP_SOFT_THRESH) * st.lTMax * K)) - band;
+    }
     sc.eps = d2ff(lim<double>::eps);
   }
   __syncthreads();
@@ -275,7 +363,7 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
   const SpinerTable &t = st;
   const unsigned out = a.output;
   const int nc = t.nT - 1;
-  const bool table_fast = t.ff_ok && t.sie_monotone_T && d_is_zero(t.lRhoOffset) &&
+  const bool table_fast = t.ff_ok && sc.x_ok && t.sie_monotone_T && d_is_zero(t.lRhoOffset) &&
                           (t.gCold.min == t.gRho.min) && (t.gCold.dx == t.gRho.dx) &&
                           (t.gCold.n == t.gRho.n) && ff_ok_bits(t.gRho.min) &&
                           ff_ok_bits(t.gT.min);
@@ -309,14 +397,10 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
       //    density weight in FP64 (its error is multiplied by the cell's
       //    density difference in the root below)
       using namespace nqt;
-      const long long x_as_int = __double_as_longlong(rho + lim<double>::eps) - one_as_int;
-      const long long frac = x_as_int & mantissa_mask;
-      const long long fh = frac >> 26, fl = frac & low_mask;
-      const long long fsq = fh * fh + ((fh * fl) >> 25);
       // two roundings, as lg_nqt then log10 (scale_down is the reference's
       // 15-digit literal, not exactly 2^-52)
       lRho = __dmul_rn(log2_over_log10,
-                       __dmul_rn(static_cast<double>(x_as_int + ((frac - fsq) / 3)), scale_down));
+                       __dmul_rn(static_cast<double>(lg_nqt_int(rho + lim<double>::eps)), scale_down));
       // Grid1D::index and ::weights with the FP64 path's roundings: the
       // interpolant has a kink at every density node, so the cell must be the
       // reference's, and the root multiplies an error in b by dR / dT (up to
@@ -330,10 +414,8 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
       if (!exact) {
         j = static_cast<int>(jf);
         b1 = __dmul_rn(__dsub_rn(lRho, __ldg(t.rhoNodes + j)), t.gRho.inv_dx);
-        // a wrong estimate shows as a weight outside [0, 1] (tested on the
-        // bit pattern: non-negative doubles order as their integers)
-        const long long bb = __double_as_longlong(b1);
-        exact = !(bb >= 0 && bb <= 0x3FF0000000000000LL);
+        // a wrong estimate shows as a weight outside [0, 1]
+        exact = !d_in_unit(b1);
       }
       if (exact) fast = density_cell_fp64(t, lRho, j, b1);
       B = ff_ok_bits(b1) ? d2ff(b1) : ff_make(0.0f);
@@ -433,27 +515,22 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
       }
     }
     if (fast) {
-      // 5. lT, then T = 10^lT by the NQT pow in integers
-      using namespace nqt;
-      // the NQT pow's integer argument lT log10(2)^-1 2^52, from the cell
-      // position i + a on the scaled grid
+      // 5. T = 10^lT by the NQT pow in integers, its argument X = lT
+      //    log10(2)^-1 2^52 from the cell position i + a; on the table in T
+      //    too (getLocDependsRhoT_): a root within 1e-8 of either end takes
+      //    the FP64 pass, whose off-table forms then apply
       const bool rooted = d_is_zero(lt_guess);
-      const ff IA = rooted ? ff_add(ff_of_int(i), A) : ff_make(0.0f);
-      const ff P52 = rooted ? ff_add(ff_mul(IA, sc.p_dx), sc.p_min)
-                            : ff_mul(d2ff(lt_guess), d2ff(nqt::log10_over_log2 * nqt::scale_up));
-      // on the table in T too (getLocDependsRhoT_); a root within 1e-8 of
-      // either end takes the FP64 pass, whose off-table forms then apply
-      if (fabsf(P52.hi) >= 1.1e12f && ff_gt(P52, sc.p_lo) && ff_lt(P52, sc.p_hi)) {
-        constexpr long long ca = 9007199254740992LL, cc = 18014398509481984LL;
-        const long long x_as_int = f2ll_bits(P52.hi) + f2ll_bits(P52.lo);
-        const long long frac = x_as_int & mantissa_mask;
-        const long long N = cc - 3 * frac; // in [2^52, 2^54]
-        const ff NF = quick_two_sum(static_cast<float>(static_cast<int>(N >> 30)) * 1073741824.0f,
-                                    static_cast<float>(static_cast<int>(N & ((1LL << 30) - 1))));
-        const ff SQ = ff_sqrt_fast(NF);
-        const long long fsqrt = f2ll_bits(SQ.hi * 67108864.0f) + f2ll_bits(SQ.lo * 67108864.0f);
-        double temp = __longlong_as_double(x_as_int + ca - fsqrt - frac + one_as_int);
+      double temp = 0.0;
+      bool on;
+      if (rooted) {
+        const long long X = nqt_arg(sc, i, A);
+        on = X > sc.x_lo && X < sc.x_hi;
+        temp = nqt_pow_int(X);
         if (t_offset) temp -= t.lTOffset;
+      } else {
+        on = guess_T(t, lt_guess, temp);
+      }
+      if (on) {
         const long long ci = static_cast<long long>(j) * nc + i;
         const ff AB = ff_mul(A, B);
         if ((out & Q_TEMPERATURE) && a.temp) a.temp[e] = temp;
@@ -476,7 +553,8 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
         if (a.lambda) {
           double *lam = a.lambda + e * a.lambda_stride;
           lam[0] = lRho;
-          lam[1] = rooted ? ff2d(ff_add(ff_mul(IA, sc.t_dx), sc.t_min)) : lt_guess;
+          lam[1] = rooted ? ff2d(ff_add(ff_mul(ff_add(ff_of_int(i), A), sc.t_dx), sc.t_min))
+                          : lt_guess;
         }
         done = true;
       }

@@ -42,21 +42,7 @@ constexpr int SIE_BLOCK = 256;
 
 
 // Whether a double converts to float-float without leaving the float range.
-__device__ __forceinline__ bool ff_in_range(const double x) {
-  const long long b = __double_as_longlong(x);
-  const int e = static_cast<int>((b >> 52) & 0x7ff) - 1023;
-  return (b & 0x7fffffffffffffffLL) == 0 || (e >= -74 && e <= 120);
-}
-
-// The integer core of lg_nqt (logs.hpp:188-200) on the bits of y.
-__device__ __forceinline__ long long nqt_lg_int(const double y) {
-  using namespace nqt;
-  const long long x_as_int = __double_as_longlong(y) - one_as_int;
-  const long long frac = x_as_int & mantissa_mask;
-  const long long fh = frac >> 26, fl = frac & low_mask;
-  const long long fsq = fh * fh + ((fh * fl) >> 25);
-  return x_as_int + (frac - fsq) / 3;
-}
+__device__ __forceinline__ bool ff_in_range(const double x) { return d_zero_or_exp_in(x, -74, 120); }
 
 // The NQT log's integer v of spiner_common::to_log (eos_spiner_common.hpp:
 // 52-54): the argument |max(x, -off) + off| + EPS in FP64 as the reference
@@ -64,11 +50,14 @@ __device__ __forceinline__ long long nqt_lg_int(const double y) {
 __device__ __forceinline__ long long to_log_int(const double x, const double off,
                                                 const bool has_off) {
   double y;
-  if (has_off)
+  if (has_off) {
     y = (x < -off ? -off : x) + off;
-  else // std::max(x, -0.0) + 0.0: zero for every negative x
-    y = __double_as_longlong(x) < 0 ? 0.0 : x;
-  return nqt_lg_int(fabs(y) + lim<double>::eps);
+  } else { // std::max(x, -0.0) + 0.0: zero for every negative x
+    unsigned lo, hi;
+    d_words(x, lo, hi);
+    y = (hi >> 31) != 0u ? 0.0 : x;
+  }
+  return lg_nqt_int(fabs(y) + lim<double>::eps);
 }
 
 // An int64 of magnitude below 2^62 as float-float (about 48 of its bits).

@@ -152,6 +152,26 @@ SGX_HD double pow2_nqt(double x) {
   const int64_t frac_sqrt = static_cast<int64_t>(b * sq);
   return as_f64(x_as_int + a - frac_sqrt - frac_as_int + one_as_int);
 }
+// lg_nqt's integer x_as_int + (frac - frac_squared) / 3 on the bits of x,
+// bit for bit, in 32-bit pieces: frac_high and frac_low are below 2^26,
+// and frac - frac_squared lies in [0, 2^52) (frac_squared <= frac^2 2^-52
+// <= frac), so the signed division is a floor, taken on the two 26-bit
+// halves by floor(n / 3) = (n * 0xAAAAAAAB) >> 33 (exact for every 32-bit
+// n). lg_nqt(x) is this value times scale_down.
+SGX_HD int64_t lg_nqt_int(const double x) {
+  using namespace nqt;
+  const int64_t x_as_int = as_i64(x) - one_as_int;
+  const uint64_t frac = static_cast<uint64_t>(x_as_int & mantissa_mask);
+  const uint32_t fh = static_cast<uint32_t>(frac >> 26);
+  const uint32_t fl = static_cast<uint32_t>(frac) & 0x3ffffffu;
+  const uint64_t fsq = static_cast<uint64_t>(fh) * fh + ((static_cast<uint64_t>(fh) * fl) >> 25);
+  const uint64_t d = frac - fsq;
+  const uint32_t dh = static_cast<uint32_t>(d >> 26);
+  const uint32_t qh = static_cast<uint32_t>((static_cast<uint64_t>(dh) * 0xAAAAAAABu) >> 33);
+  const uint32_t rl = ((dh - 3u * qh) << 26) | (static_cast<uint32_t>(d) & 0x3ffffffu);
+  const uint32_t ql = static_cast<uint32_t>((static_cast<uint64_t>(rl) * 0xAAAAAAABu) >> 33);
+  return x_as_int + static_cast<int64_t>((static_cast<uint64_t>(qh) << 26) + ql);
+}
 SGX_HD double log10_nqt(double x) { return nqt::log2_over_log10 * lg_nqt(x); }
 SGX_HD double pow10_nqt(double x) { return pow2_nqt(nqt::log10_over_log2 * x); }
 

@@ -1045,7 +1045,22 @@ int table_load_helm(const char *path, uint64_t *handle, std::string &msg) {
   const size_t off_rho = off_cells + cells.size() * 8;
   const size_t off_T = off_rho + NR * 8;
   const size_t off_c32 = (off_T + NT * 8 + 255) / 256 * 256;
-  const size_t bytes = off_c32 + (f32_ok ? cells32.size() * sizeof(float) : 0);
+  const size_t off_rho32 = off_c32 + cells32.size() * sizeof(float);
+  const size_t off_T32 = off_rho32 + NR * sizeof(float);
+  const size_t bytes = f32_ok ? off_T32 + NT * sizeof(float) : off_c32;
+  // the FP32 phase's float copies of the nodes and grid constants
+  std::vector<float> rho32(NR), T32(NT);
+  for (int i = 0; i < NR; ++i)
+    rho32[i] = static_cast<float>(rho[i]);
+  for (int j = 0; j < NT; ++j)
+    T32[j] = static_cast<float>(T[j]);
+  t.f_lRhoMin = static_cast<float>(t.lRhoMin);
+  t.f_lRhoMax = static_cast<float>(t.lRhoMax);
+  t.f_inv_dlRho = static_cast<float>(t.inv_dlRho);
+  t.f_lTMin = static_cast<float>(t.lTMin);
+  t.f_inv_dlT = static_cast<float>(t.inv_dlT);
+  t.f_rhoMin = static_cast<float>(t.rhoMin);
+  t.f_rhoMax = static_cast<float>(t.rhoMax);
   void *dev = nullptr;
   cudaError_t e = cudaMalloc(&dev, bytes);
   if (e != cudaSuccess) {
@@ -1057,13 +1072,18 @@ int table_load_helm(const char *path, uint64_t *handle, std::string &msg) {
   t.rho = reinterpret_cast<const double *>(d + off_rho);
   t.T = reinterpret_cast<const double *>(d + off_T);
   t.cells32 = f32_ok ? reinterpret_cast<const float *>(d + off_c32) : nullptr;
+  t.rho32 = f32_ok ? reinterpret_cast<const float *>(d + off_rho32) : nullptr;
+  t.T32 = f32_ok ? reinterpret_cast<const float *>(d + off_T32) : nullptr;
   std::vector<unsigned char> img(bytes, 0);
   std::memcpy(img.data(), &t, sizeof(t));
   std::memcpy(img.data() + off_cells, cells.data(), cells.size() * 8);
   std::memcpy(img.data() + off_rho, rho.data(), NR * 8);
   std::memcpy(img.data() + off_T, T.data(), NT * 8);
-  if (f32_ok)
+  if (f32_ok) {
     std::memcpy(img.data() + off_c32, cells32.data(), cells32.size() * sizeof(float));
+    std::memcpy(img.data() + off_rho32, rho32.data(), NR * sizeof(float));
+    std::memcpy(img.data() + off_T32, T32.data(), NT * sizeof(float));
+  }
   e = cudaMemcpy(dev, img.data(), bytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     cudaFree(dev);

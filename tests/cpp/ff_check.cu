@@ -2,7 +2,9 @@
 // ff2d(hi, lo) against the FP64 sum (double)hi + (double)lo over seeded
 // pairs of every magnitude, unnormalised pairs, exact powers of two with a
 // low part of the opposite sign, zero and subnormal low parts; d2ff round
-// trips. Prints "bad=<count>"; run by tests/test_gpu_ff.py.
+// trips; the NQT log's integer core in 32-bit pieces (lg_nqt_int) against
+// the reference's 64-bit formula (logs.hpp:188-200), bit for bit. Prints
+// "bad=<count>"; run by tests/test_gpu_ff.py.
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -13,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include "sgx_ff.cuh"
+#include "sgx_math.cuh"
 
 __global__ void conv(const float *hi, const float *lo, const double *d, double *out, double *rt,
                      const int n) {
@@ -20,6 +23,11 @@ __global__ void conv(const float *hi, const float *lo, const double *d, double *
   if (i >= n) return;
   out[i] = sgx::ff2d(sgx::ff_make(hi[i], lo[i]));
   rt[i] = sgx::ff2d(sgx::d2ff(d[i]));
+}
+
+__global__ void lgint(const double *x, long long *out, const int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = sgx::lg_nqt_int(x[i]);
 }
 
 static double ulp(const double x) {
@@ -75,6 +83,33 @@ int main() {
     // d2ff keeps ~48 bits: the round trip within 2^-47 relative
     if (!(std::fabs(rt[i] - d[i]) <= std::ldexp(std::fabs(d[i]), -47))) {
       if (bad < 5) std::printf("round trip %a -> %a\n", d[i], rt[i]);
+      ++bad;
+    }
+  }
+  // lg_nqt_int over positive normal doubles of every exponent
+  for (int i = 0; i < n; ++i) {
+    uint64_t b = g() & 0x7fefffffffffffffULL;
+    if ((b >> 52) == 0) b |= 1ULL << 52;
+    std::memcpy(&d[i], &b, 8);
+  }
+  long long *dl_out;
+  cudaMalloc(&dl_out, n * 8);
+  cudaMemcpy(dd, d.data(), n * 8, cudaMemcpyHostToDevice);
+  lgint<<<(n + 255) / 256, 256>>>(dd, dl_out, n);
+  std::vector<long long> li(n);
+  if (cudaMemcpy(li.data(), dl_out, n * 8, cudaMemcpyDeviceToHost) != cudaSuccess) {
+    std::printf("cuda error\n");
+    return 2;
+  }
+  for (int i = 0; i < n; ++i) {
+    int64_t xb;
+    std::memcpy(&xb, &d[i], 8);
+    const int64_t x_as_int = xb - sgx::nqt::one_as_int;
+    const int64_t frac = x_as_int & sgx::nqt::mantissa_mask;
+    const int64_t fh = frac >> 26, fl = frac & sgx::nqt::low_mask;
+    const int64_t want = x_as_int + (frac - (fh * fh + ((fh * fl) >> 25))) / 3;
+    if (li[i] != want) {
+      if (bad < 5) std::printf("lg_nqt_int %a -> %lld want %lld\n", d[i], li[i], (long long)want);
       ++bad;
     }
   }
