@@ -44,8 +44,11 @@ N_PTE_BATCH = 1 << 22
 N_HELM = 1 << 22
 LOOKUP_BYTES_PER_QUERY = 16 + 32  # rho, sie in; T, P, bmod, cs out (float64)
 HELM_BYTES_PER_CELL = 32 + 32     # rho, sie, Abar, Zbar in; T, P, bmod, cs out
-# FP64-pipe share of active cycles of the inversion kernels (one ncu capture)
-HELM_FP64_PIPE_NCU = {"helm_invert_pass1": 0.838, "helm_invert_pass2": 0.781}
+# FP64-pipe share of active cycles of the inversion kernels of the FP64 step
+# (one ncu capture at 2^18 cells; pass 2 runs once per step-cap stage)
+HELM_FP64_PIPE_NCU = {"helm_invert_pass1": 0.839, "helm_invert_pass2 (steps 10-20)": 0.846,
+                      "helm_invert_pass2 (steps 20-40)": 0.850,
+                      "helm_invert_pass2 (steps 40-100)": 0.772, "helm_invert_pass3": 0.669}
 LOOKUP_TRAFFIC_2_24 = (283.67 + 489.62 + 2.19) * 1e6  # measured DRAM bytes per 2^24-query step
 Q_OUT = 8 | 4 | 32                # temperature | pressure | bulk modulus
 METRIC = "PTE mixed cells/s & EOS lookups/s, 1 GB300, batched+FP32-refined vs plain FP64"
@@ -558,8 +561,8 @@ def bench_helm(args, world, stream, out):
                                        "peak_kind": hbm_kind + " (burst copy)",
                                        "fp64_pipe_active": HELM_FP64_PIPE_NCU,
                                        "fp64_pipe_source": "ncu capture of the FP64 step's "
-                                       "pass 1 and pass 2 at 2^18 cells; constants, not "
-                                       "measured by this run"}}
+                                       "passes at 2^18 cells; constants, not measured by "
+                                       "this run"}}
             outs[pname] = (T, P, B, CS)
         # per-output differences of the mixed inversion to the FP64 one, over
         # the cells whose FP64 inversion recovers T to 1e-8 (well posed)
@@ -575,7 +578,7 @@ def bench_helm(args, world, stream, out):
             "fp64": res["fp64"], "mixed": res["mixed"],
             "mixed_over_fp64": res["mixed"]["cells_per_s"] / res["fp64"]["cells_per_s"],
             "mixed_error_vs_fp64_well_posed": err,
-            "kernel": "helm_invert_pass1<true>/pass2/pass3 (sgx_helm.cu)",
+            "kernel": "helm_invert_pass1<true>, pass2 per step-cap stage, pass3 (sgx_helm.cu)",
             "cpu_baseline": helm_cpu_baseline(path, rho_h, sie.cpu().numpy(), abar, zbar)
             if (world == 1 and not args.no_cpu_baseline) else None}
         lib.load().sgx_eos_finalize(__import__("ctypes").byref(eos))

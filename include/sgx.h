@@ -469,6 +469,16 @@ int sgx_mix_enforce_energies_sum(int nmat, int64_t ncell, const int32_t *eos_idx
  *  SGX_TUNE_PTE_FP32_TOL  3..6 (default 4): the FP32 Newton phase of the
  *      mixed path iterates to relative residuals of 10^-value before the
  *      FP64 residual correction (which ends at 1e-12 either way).
+ *  SGX_TUNE_HELM_PASS1_STEPS  0..100: Newton steps of the Helmholtz
+ *      T(rho, sie) inversion in its first pass (FP64 steps after the FP32
+ *      phase on the mixed path); the elements still iterating are resumed
+ *      from their saved state over a compacted queue.
+ *  SGX_TUNE_HELM_MID_STEPS, SGX_TUNE_HELM_MID2_STEPS  0..100: each one
+ *      above the cap before it adds a middle pass that resumes the elements
+ *      still iterating up to that many steps, before the last pass takes the
+ *      rest to the reference's 100 (100: no such pass).
+ *      Left at 0, the three take their precision's defaults: 10, 20, 40 for
+ *      FP64 and 3, 12, 40 for the mixed path. Results do not change.
  */
 enum {
   SGX_TUNE_LOOKUP_BLOCKS_PER_SM = 1,
@@ -480,7 +490,10 @@ enum {
   SGX_TUNE_PTE_COUNT_ORDER = 7,
   SGX_TUNE_PTE_MIXED_BLOCK = 8,
   SGX_TUNE_PTE_GROUP_MIN_N = 9,
-  SGX_TUNE_PTE_FP32_TOL = 10
+  SGX_TUNE_PTE_FP32_TOL = 10,
+  SGX_TUNE_HELM_PASS1_STEPS = 11,
+  SGX_TUNE_HELM_MID_STEPS = 12,
+  SGX_TUNE_HELM_MID2_STEPS = 13
 };
 int sgx_tune_set(int knob, int value);
 int sgx_tune_get(int knob, int *value);

@@ -110,23 +110,24 @@ __global__ void __launch_bounds__(HELM_BLOCK) helm_fill_kernel(const FillArgs a)
   if (bad && a.err) atomicOr(a.err, 1);
 }
 
-// Two-pass inversion FillEos (outputs include T, inputs rho and sie): pass 1
-// runs every element's Newton iteration for at most HELM_PASS1_ITERS steps
-// and finishes the ones that stop; the others are queued with their exact
-// iteration state (x, iteration count) and pass 2 resumes them over the
-// compacted queue, up to the reference's 100 iterations and its fallbacks.
-// Each element's result is the one a single pass gives; the hard elements
-// (hundreds of evaluations where e(T) is not monotone) no longer hold up
-// the warps of the easy ones.
-constexpr int HELM_PASS1_ITERS = 12;
+// Staged inversion FillEos (outputs include T, inputs rho and sie): pass 1
+// runs every element's Newton iteration for at most a few steps and
+// finishes the ones that stop; the others are queued with their exact
+// iteration state (x, iteration count) and resumed over the compacted queue
+// by up to three more passes (the last up to the reference's 100
+// iterations), then its fallbacks. Each element's result is the one a single
+// pass gives; the hard elements (hundreds of evaluations where e(T) is not
+// monotone) no longer hold up the warps of the easy ones, nor the ones that
+// wander to the iteration limit those that converge on the way. The step
+// caps are launch knobs (SGX_TUNE_HELM_PASS1_STEPS, SGX_TUNE_HELM_MID_STEPS,
+// SGX_TUNE_HELM_MID2_STEPS).
 
+// An iteration-state queue between two passes.
 struct HelmQueue {
   int *id;
   double *x;
   int *iter;
   unsigned *count;
-  int *id_rf;         // pass 2 -> 3: Newton ran out of iterations
-  unsigned *count_rf;
 };
 
 __device__ __forceinline__ void store_fill(const FillArgs &a, const long long i, const double rho,
@@ -141,11 +142,28 @@ __device__ __forceinline__ void store_fill(const FillArgs &a, const long long i,
   if ((a.output & Q_BMOD) && a.bmod) a.bmod[i] = bmod;
 }
 
+// An element whose iteration stopped at `cap` steps: queued for the next
+// pass with its state, or, at the reference's 100, for the regula falsi of
+// pass 3 (id only).
+__device__ __forceinline__ void queue_unfinished(const HelmQueue &next, const HelmQueue &rf,
+                                                 const long long i, const double x,
+                                                 const int iter) {
+  if (iter < helm::NEWTON_MAX_ITER) {
+    const unsigned pos = atomicAdd(next.count, 1u);
+    next.id[pos] = static_cast<int>(i);
+    next.x[pos] = x;
+    next.iter[pos] = iter;
+  } else {
+    rf.id[atomicAdd(rf.count, 1u)] = static_cast<int>(i);
+  }
+}
+
 // MIXED: the Newton iteration starts from the FP32 phase's root (newton_e32,
 // FP32 e(T) to 1e-6) instead of the reference's guess, so the FP64 steps
 // that follow are the reference's last one or two.
 template <bool MIXED>
-__global__ void __launch_bounds__(HELM_BLOCK) helm_invert_pass1(const FillArgs a, HelmQueue q) {
+__global__ void __launch_bounds__(HELM_BLOCK)
+    helm_invert_pass1(const FillArgs a, HelmQueue next, HelmQueue rf, const int cap) {
   using namespace helm;
   __shared__ HelmTable st;
   if (threadIdx.x == 0) st = *reinterpret_cast<const HelmTable *>(a.eos.table);
@@ -164,13 +182,9 @@ __global__ void __launch_bounds__(HELM_BLOCK) helm_invert_pass1(const FillArgs a
       double x32 = v.x;
       if (newton_e32(st, opt, cell32(c), sie, v.Ta, v.Tb, x32)) v.x = x32;
     }
-    const bool done =
-        newton_e_steps(st, opt, c, sie, v.Ta, v.Tb, HELM_EOS_EPS, v.x, v.iter, HELM_PASS1_ITERS);
+    const bool done = newton_e_steps(st, opt, c, sie, v.Ta, v.Tb, HELM_EOS_EPS, v.x, v.iter, cap);
     if (!done) {
-      const unsigned pos = atomicAdd(q.count, 1u);
-      q.id[pos] = static_cast<int>(i);
-      q.x[pos] = v.x;
-      q.iter[pos] = v.iter;
+      queue_unfinished(next, rf, i, v.x, v.iter);
       continue;
     }
     const double temp = pow10e(inversion_end(st, opt, c, v, true, lam));
@@ -180,28 +194,31 @@ __global__ void __launch_bounds__(HELM_BLOCK) helm_invert_pass1(const FillArgs a
   }
 }
 
-__global__ void __launch_bounds__(HELM_BLOCK) helm_invert_pass2(const FillArgs a, HelmQueue q) {
+// The elements of `in` resumed from their saved state, up to `cap` steps
+// in all; those still running are queued on (next, or rf at 100 steps).
+__global__ void __launch_bounds__(HELM_BLOCK)
+    helm_invert_pass2(const FillArgs a, const HelmQueue in, HelmQueue next, HelmQueue rf,
+                      const int cap) {
   using namespace helm;
   __shared__ HelmTable st;
   if (threadIdx.x == 0) st = *reinterpret_cast<const HelmTable *>(a.eos.table);
   __syncthreads();
   const int opt = a.eos.flags;
   const unsigned output = a.output | (a.cs ? Q_BMOD : 0u);
-  const unsigned count = *q.count;
+  const unsigned count = *in.count;
   for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < count;
        k += gridDim.x * blockDim.x) {
-    const long long i = q.id[k];
+    const long long i = in.id[k];
     const double rho = a.rho[i];
     const double sie = a.sie[i];
     double *lam = a.lambda + i * a.lambda_stride;
     const Cell c = cell(rho, lam[0], lam[1]);
     Inversion v = inversion_begin(st, opt, c, sie, lam);
-    v.x = q.x[k];
-    v.iter = q.iter[k];
-    const bool done =
-        newton_e_steps(st, opt, c, sie, v.Ta, v.Tb, HELM_EOS_EPS, v.x, v.iter, NEWTON_MAX_ITER);
+    v.x = in.x[k];
+    v.iter = in.iter[k];
+    const bool done = newton_e_steps(st, opt, c, sie, v.Ta, v.Tb, HELM_EOS_EPS, v.x, v.iter, cap);
     if (!done) {
-      q.id_rf[atomicAdd(q.count_rf, 1u)] = static_cast<int>(i);
+      queue_unfinished(next, rf, i, v.x, v.iter);
       continue;
     }
     const double temp = pow10e(inversion_end(st, opt, c, v, true, lam));
@@ -214,17 +231,17 @@ __global__ void __launch_bounds__(HELM_BLOCK) helm_invert_pass2(const FillArgs a
 // Pass 3: the elements whose Newton iteration used all 100 steps go on to
 // the reference's regula falsi (up to 1000 more evaluations) and, failing
 // that, the analytic estimate.
-__global__ void __launch_bounds__(HELM_BLOCK) helm_invert_pass3(const FillArgs a, HelmQueue q) {
+__global__ void __launch_bounds__(HELM_BLOCK) helm_invert_pass3(const FillArgs a, const HelmQueue rf) {
   using namespace helm;
   __shared__ HelmTable st;
   if (threadIdx.x == 0) st = *reinterpret_cast<const HelmTable *>(a.eos.table);
   __syncthreads();
   const int opt = a.eos.flags;
   const unsigned output = a.output | (a.cs ? Q_BMOD : 0u);
-  const unsigned count = *q.count_rf;
+  const unsigned count = *rf.count;
   for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < count;
        k += gridDim.x * blockDim.x) {
-    const long long i = q.id_rf[k];
+    const long long i = rf.id[k];
     const double rho = a.rho[i];
     const double sie = a.sie[i];
     double *lam = a.lambda + i * a.lambda_stride;
@@ -264,34 +281,67 @@ cudaError_t launch_helm_fill(const FillArgs &a, cudaStream_t stream, const bool 
     helm_fill_kernel<<<helm_grid(a.n), HELM_BLOCK, 0, stream>>>(a);
     return cudaGetLastError();
   }
-  // queues: 256 B counter block, then x[n], id[n], iter[n], id_rf[n]
+  // queues: a 256 B counter block, then two state queues (x, id, iter) that
+  // the passes hand on alternately, and the ids for pass 3
   const size_t n = static_cast<size_t>(a.n);
   const size_t ids = (n * sizeof(int) + 255) / 256 * 256;
   const size_t xs = (n * sizeof(double) + 255) / 256 * 256;
   void *scratch = nullptr;
-  cudaError_t e = scratch_alloc(&scratch, 256 + 3 * ids + xs, stream);
+  cudaError_t e = scratch_alloc(&scratch, 256 + 2 * (xs + 2 * ids) + ids, stream);
   if (e != cudaSuccess) return e;
   char *p = static_cast<char *>(scratch);
-  HelmQueue q;
-  q.count = reinterpret_cast<unsigned *>(p);
-  q.count_rf = reinterpret_cast<unsigned *>(p + 64);
-  q.x = reinterpret_cast<double *>(p + 256);
-  q.id = reinterpret_cast<int *>(p + 256 + xs);
-  q.iter = reinterpret_cast<int *>(p + 256 + xs + ids);
-  q.id_rf = reinterpret_cast<int *>(p + 256 + xs + 2 * ids);
+  HelmQueue qa, qb, rf;
+  qa.count = reinterpret_cast<unsigned *>(p);
+  qb.count = reinterpret_cast<unsigned *>(p + 64);
+  rf.count = reinterpret_cast<unsigned *>(p + 128);
+  char *o = p + 256;
+  for (HelmQueue *q : {&qa, &qb}) {
+    q->x = reinterpret_cast<double *>(o);
+    q->id = reinterpret_cast<int *>(o + xs);
+    q->iter = reinterpret_cast<int *>(o + xs + ids);
+    o += xs + 2 * ids;
+  }
+  rf.id = reinterpret_cast<int *>(o);
+  rf.x = nullptr;
+  rf.iter = nullptr;
+  // the step caps: a knob left at 0 takes its precision's default schedule,
+  // measured on 2^20 cells of the benchmark's distribution (FP64 10, 20,
+  // 40: 59 ms against 91 ms for 12 and 100; mixed 3, 12, 40: 47 ms against
+  // 72 ms -- after the FP32 phase most elements need one to three FP64 steps)
+  int cap1 = tune_get(SGX_TUNE_HELM_PASS1_STEPS);
+  int mid = tune_get(SGX_TUNE_HELM_MID_STEPS);
+  int mid2 = tune_get(SGX_TUNE_HELM_MID2_STEPS);
+  if (cap1 == 0) cap1 = mixed ? 3 : 10;
+  if (mid == 0) mid = mixed ? 12 : 20;
+  if (mid2 == 0) mid2 = 40;
   e = cudaMemsetAsync(p, 0, 256, stream);
   if (e == cudaSuccess) {
     if (mixed)
-      helm_invert_pass1<true><<<helm_grid(a.n), HELM_BLOCK, 0, stream>>>(a, q);
+      helm_invert_pass1<true><<<helm_grid(a.n), HELM_BLOCK, 0, stream>>>(a, qa, rf, cap1);
     else
-      helm_invert_pass1<false><<<helm_grid(a.n), HELM_BLOCK, 0, stream>>>(a, q);
+      helm_invert_pass1<false><<<helm_grid(a.n), HELM_BLOCK, 0, stream>>>(a, qa, rf, cap1);
     int dev = 0, sms = 152;
     if (cudaGetDevice(&dev) == cudaSuccess)
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long want = (a.n + HELM_BLOCK - 1) / HELM_BLOCK;
     const int grid2 = static_cast<int>(want < 4LL * sms ? want : 4LL * sms);
-    helm_invert_pass2<<<grid2, HELM_BLOCK, 0, stream>>>(a, q);
-    helm_invert_pass3<<<grid2, HELM_BLOCK, 0, stream>>>(a, q);
+    // the resumed passes, each to a higher cap, the last to the reference's
+    // 100; the state queues alternate (a pass reads one, fills the other,
+    // whose counter it has cleared)
+    int caps[3], nst = 0, prev = cap1;
+    for (const int c : {mid, mid2})
+      if (c > prev && c < helm::NEWTON_MAX_ITER) caps[nst++] = prev = c;
+    caps[nst++] = helm::NEWTON_MAX_ITER;
+    HelmQueue *in = &qa, *nx = &qb;
+    for (int k = 0; k < nst && e == cudaSuccess; ++k) {
+      if (k > 0) e = cudaMemsetAsync(nx->count, 0, sizeof(unsigned), stream);
+      if (e != cudaSuccess) break;
+      helm_invert_pass2<<<grid2, HELM_BLOCK, 0, stream>>>(a, *in, *nx, rf, caps[k]);
+      HelmQueue *t = in;
+      in = nx;
+      nx = t;
+    }
+    helm_invert_pass3<<<grid2, HELM_BLOCK, 0, stream>>>(a, rf);
     e = cudaGetLastError();
   }
   const cudaError_t f = scratch_free(scratch, stream);

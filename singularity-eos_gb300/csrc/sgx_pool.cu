@@ -78,6 +78,9 @@ Knob g_knobs[] = {
     {{128}, 32, 128}, // SGX_TUNE_PTE_MIXED_BLOCK
     {{3}, 2, 7},      // SGX_TUNE_PTE_GROUP_MIN_N
     {{4}, 3, 6},      // SGX_TUNE_PTE_FP32_TOL
+    {{0}, 0, 100},    // SGX_TUNE_HELM_PASS1_STEPS (0: the precision's default)
+    {{0}, 0, 100},    // SGX_TUNE_HELM_MID_STEPS
+    {{0}, 0, 100},    // SGX_TUNE_HELM_MID2_STEPS
 };
 constexpr int NKNOBS = sizeof(g_knobs) / sizeof(g_knobs[0]);
 } // namespace

@@ -21,6 +21,7 @@ PTE_RHOT, PTE_PT, PTE_RHOU, PTE_FIXED_T, PTE_FIXED_P = 0, 1, 2, 3, 4
 TUNE_LOOKUP_BLOCKS_PER_SM, TUNE_LOOKUP_STAGE, TUNE_L2_PERSIST, TUNE_HOST_FILL_STAGED = 1, 2, 3, 4
 TUNE_PTE_FP32_ITERS, TUNE_PTE_RETRY_ITERS, TUNE_PTE_COUNT_ORDER = 5, 6, 7
 TUNE_PTE_MIXED_BLOCK, TUNE_PTE_GROUP_MIN_N, TUNE_PTE_FP32_TOL = 8, 9, 10
+TUNE_HELM_PASS1_STEPS, TUNE_HELM_MID_STEPS, TUNE_HELM_MID2_STEPS = 11, 12, 13
 PREC_FP64, PREC_MIXED = 0, 1
 
 EXPORTED = [

@@ -223,16 +223,44 @@ def test_helmholtz_argument_checks(sgx, table):
         lib.sgx_eos_finalize(C.byref(eos))
 
 
-@pytest.mark.parametrize("options", [31, 31 | 64])
-def test_two_pass_inversion_is_bitwise_single_pass(sgx, table, options):
-    """FillEos with T among the outputs runs the inversion in two passes
-    (bounded Newton steps, then the queued cells resumed); each element must
-    come out exactly as the one-pass member functions give it."""
+@pytest.mark.parametrize("options,caps", [(31, (0, 0, 0)), (31 | 64, (0, 0, 0)),
+                                          (31, (12, 100, 100)), (31, (2, 100, 100)),
+                                          (31, (3, 24, 100)), (31, (8, 20, 50))])
+def test_two_pass_inversion_is_bitwise_single_pass(sgx, table, options, caps):
+    """FillEos with T among the outputs runs the inversion in stages
+    (bounded Newton steps, then the queued cells resumed, with up to two
+    middle stages: SGX_TUNE_HELM_PASS1_STEPS, SGX_TUNE_HELM_MID_STEPS,
+    SGX_TUNE_HELM_MID2_STEPS); each
+    element must come out exactly as the one-pass member functions give it,
+    whatever the caps; the mixed path's results do not depend on them
+    either."""
     from sgx import helmtable
     n = 1 << 16
     rho_h, T_h, abar, zbar = helmtable.helm_queries(n, seed=99)
     eos = sgx.helmholtz_eos(table[0], options)
+    L = sgx.load()
+    saved = []
+    knobs = (sgx.TUNE_HELM_PASS1_STEPS, sgx.TUNE_HELM_MID_STEPS, sgx.TUNE_HELM_MID2_STEPS)
+    for k in knobs:
+        v = C.c_int()
+        assert L.sgx_tune_get(k, C.byref(v)) == 0
+        saved.append(v.value)
     try:
+        lam_h = np.zeros(3 * n)
+        lam_h[0::3], lam_h[1::3], lam_h[2::3] = abar, zbar, np.nan
+        rho0, Tin0 = dev(rho_h), dev(T_h)
+        sie0 = torch.empty_like(rho0)
+        sgx.fill_eos(eos, rho0, Tin0, sie0, None, None, None, sgx.Q_SIE, lam=dev(lam_h),
+                     lam_stride=3)
+        mixed = []
+        for c in ((12, 100, 100), caps):
+            for k, v in zip(knobs, c):
+                assert L.sgx_tune_set(k, v) == 0
+            Tm = torch.empty_like(rho0)
+            sgx.fill_eos(eos, rho0, Tm, sie0, None, None, None, sgx.Q_TEMPERATURE,
+                         lam=dev(lam_h), lam_stride=3, precision=sgx.PREC_MIXED)
+            mixed.append(Tm.cpu().numpy())
+        assert np.array_equal(mixed[0].view(np.uint64), mixed[1].view(np.uint64))
         lam_h = np.zeros(3 * n)
         lam_h[0::3], lam_h[1::3], lam_h[2::3] = abar, zbar, np.nan
         rho, Tin = dev(rho_h), dev(T_h)
@@ -253,6 +281,8 @@ def test_two_pass_inversion_is_bitwise_single_pass(sgx, table, options):
                 assert np.array_equal(lam2.cpu().numpy().view(np.uint64),
                                       lam1.cpu().numpy().view(np.uint64))
     finally:
+        for k, v in zip(knobs, saved):
+            L.sgx_tune_set(k, v)
         sgx.load().sgx_eos_finalize(C.byref(eos))
 
 
