@@ -281,6 +281,22 @@ def bench_lookup(args, world, local, stream, out):
                           "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 32 * n,
                           "host_link_copy_ms": link_s * 1e3,
                           "frac_of_host_link": link_s / (dte / e2e_steps)}
+        if args.lookup_parts:
+            # the marginal cost of each output: the mixed FillEos over the
+            # same queries for subsets of the outputs
+            qt, qp, qb = lib.Q_TEMPERATURE, lib.Q_PRESSURE, lib.Q_BULK_MODULUS
+            parts = {}
+            for pname, q, cs in (("T", qt, None), ("T+P", qt | qp, None),
+                                 ("T+P+bmod", qt | qp | qb, None),
+                                 ("T+P+bmod+cs", qt | qp | qb, CS), ("T+cs", qt, CS)):
+                def part_step(q=q, cs=cs):
+                    lib.fill_eos(tab, rho, T, sie, P if q & qp else None, None,
+                                 B if q & qb else None, q, cs=cs, precision=lib.PREC_MIXED,
+                                 stream=stream)
+                dtp = time_steps(part_step, args.steps, args.warmup, stream)
+                parts[pname] = {"ms_per_step": dtp / args.steps * 1e3,
+                                "lookups_per_s": n * args.steps / dtp}
+            out["lookup_parts"] = parts
         lib.load().sgx_eos_finalize(__import__("ctypes").byref(tab))
         out["value"], out["ms_per_step"] = m["value"], m["ms"]
         # two kernels per FillEos: the float-float pass and the FP64 pass
@@ -541,6 +557,10 @@ def bench_helm(args, world, stream, out):
         q = lib.Q_TEMPERATURE | lib.Q_PRESSURE | lib.Q_BULK_MODULUS
         hbm, hbm_kind = peaks()
         res, outs = {}, {}
+        if args.helm_caps:
+            for knob, v in zip((lib.TUNE_HELM_PASS1_STEPS, lib.TUNE_HELM_MID_STEPS,
+                                lib.TUNE_HELM_MID2_STEPS), args.helm_caps.split(",")):
+                lib.check(lib.load().sgx_tune_set(knob, int(v)))
         for prec, pname in ((lib.PREC_FP64, "fp64"), (lib.PREC_MIXED, "mixed")):
             T, P, B, CS = (torch.empty_like(rho) for _ in range(4))
 
@@ -579,6 +599,7 @@ def bench_helm(args, world, stream, out):
             "mixed_over_fp64": res["mixed"]["cells_per_s"] / res["fp64"]["cells_per_s"],
             "mixed_error_vs_fp64_well_posed": err,
             "kernel": "helm_invert_pass1<true>, pass2 per step-cap stage, pass3 (sgx_helm.cu)",
+            "step_caps": args.helm_caps or "library defaults (FP64 10,20,40; mixed 3,12,40)",
             "cpu_baseline": helm_cpu_baseline(path, rho_h, sie.cpu().numpy(), abar, zbar)
             if (world == 1 and not args.no_cpu_baseline) else None}
         lib.load().sgx_eos_finalize(__import__("ctypes").byref(eos))
@@ -858,6 +879,12 @@ def main():
                              "rhosie"])
     ap.add_argument("--pte-prec", default="both", choices=["both", "fp64", "mixed"])
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--lookup-parts", action="store_true",
+                    help="also time the mixed lookup for output subsets (T; T+P; T+P+bmod; "
+                         "all + cs; T+cs), reported under lookup_parts")
+    ap.add_argument("--helm-caps", default=None,
+                    help="pass-1, middle and second middle Newton step caps of the Helmholtz "
+                         "inversion, e.g. 12,100,100 (sgx_tune_set; default: the library's)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -880,7 +907,7 @@ def main():
     line = {"metric": METRIC, "value": out["value"], "unit": "lookups/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64 (f32 bracket search)",
+            "dtype": "f64 (float-float interpolation and root; FP64 density weight)",
             "data": "synthetic (seeded; StiffGas-sampled table)", "config": config,
             "e2e": out.get("e2e"), "roofline": out["roofline"], "clocks": out["clocks"],
             "gpu_launches": out["gpu_launches"], "plain_fp64": out["plain_fp64"],
@@ -888,6 +915,8 @@ def main():
             "pte": out.get("pte"), "helmholtz": out.get("helmholtz"),
             "serve": out.get("serve"), "rhosie": out.get("rhosie"),
             "fp_peaks": out.get("fp_peaks"), "autotuned": out.get("autotuned")}
+    if "lookup_parts" in out:
+        line["lookup_parts"] = out["lookup_parts"]
     if "e2e" not in out:
         line["e2e"] = None
     if not args.no_cpu_baseline and world == 1:
