@@ -275,6 +275,15 @@ __device__ __forceinline__ double ff2d(const ff x0) {
   return __hiloint2double(H, static_cast<int>(L));
 }
 
+// hi + lo as a double, correctly rounded, by one FP64 addition of the two
+// parts widened exactly by moving their fields (subnormal parts count as
+// zero). Fewer instructions than ff2d for one FP64-pipe instruction, which
+// pays where the FP64 pipe has room and instruction issue binds; lo need
+// not be normalised.
+__device__ __forceinline__ double ff2d_add(const ff x) {
+  return __dadd_rn(f2d_bits(x.hi), f2d_bits(x.lo));
+}
+
 // A float that holds an integer of magnitude < 2^62, as int64 (shift of the
 // significand by the exponent); values below 1 give 0.
 __device__ __forceinline__ long long f2ll_bits(const float f) {

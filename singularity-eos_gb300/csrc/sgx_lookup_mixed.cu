@@ -534,19 +534,20 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
         const long long ci = static_cast<long long>(j) * nc + i;
         const ff AB = ff_mul(A, B);
         if ((out & Q_TEMPERATURE) && a.temp) a.temp[e] = temp;
-        if ((out & Q_PRESSURE) && a.press) a.press[e] = ff2d(ff_cell(load_rec(t.PR + ci), A, B, AB));
+        if ((out & Q_PRESSURE) && a.press)
+          a.press[e] = ff2d_add(ff_cell(load_rec(t.PR + ci), A, B, AB));
         if ((out & Q_BMOD) || a.cs) {
           const ff bm = ff_cell(load_rec(t.bmodR + ci), A, B, AB);
           ff BM = quick_two_sum(bm.hi, bm.lo);
           if (ff_lt(BM, sc.eps)) BM = sc.eps;
-          if ((out & Q_BMOD) && a.bmod) a.bmod[e] = ff2d(BM);
+          if ((out & Q_BMOD) && a.bmod) a.bmod[e] = ff2d_add(BM);
           if (a.cs) {
             // sqrt(bmod / rho) by one rsqrt correction while b rho stays well
             // inside the float range, by the exact ff quotient otherwise
             const ff R = d2ff(rho);
             const float pr = BM.hi * R.hi;
-            a.cs[e] = ff2d((pr > 1e-30f && pr < 1e30f) ? ff_sqrt_ratio(BM, R)
-                                                        : ff_sqrt(ff_div(BM, R)));
+            a.cs[e] = ff2d_add((pr > 1e-30f && pr < 1e30f) ? ff_sqrt_ratio(BM, R)
+                                                            : ff_sqrt(ff_div(BM, R)));
           }
         }
         if ((out & Q_CV) && a.cv) a.cv[e] = cv_fp64(t, j, i, b1, ff2d(A));

@@ -134,8 +134,8 @@ __global__ void __launch_bounds__(SIE_BLOCK, MINB) sie_fill_fast(const FillArgs 
     const int i = cell_of(vE, t.fxM[1], t.fxOff[1], t.fxF[1], t.nE, A);
     const SieCellFF *c = t.cellsE + static_cast<long long>(j) * ncE + i;
     const ff AB = ff_mul(A, B);
-    if ((out & Q_TEMPERATURE) && a.temp) a.temp[e] = ff2d(ff_cell(load_rec(&c->T), A, B, AB));
-    if ((out & Q_PRESSURE) && a.press) a.press[e] = ff2d(ff_cell(load_rec(&c->P), A, B, AB));
+    if ((out & Q_TEMPERATURE) && a.temp) a.temp[e] = ff2d_add(ff_cell(load_rec(&c->T), A, B, AB));
+    if ((out & Q_PRESSURE) && a.press) a.press[e] = ff2d_add(ff_cell(load_rec(&c->P), A, B, AB));
     if ((out & Q_CV) && a.cv) {
       const ff d = ff_cell(load_rec(&c->dTdE), A, B, AB);
       const ff dn = quick_two_sum(d.hi, d.lo);
@@ -144,19 +144,19 @@ __global__ void __launch_bounds__(SIE_BLOCK, MINB) sie_fill_fast(const FillArgs 
           0x7ff0000000000000ULL |
           (static_cast<unsigned long long>(__float_as_uint(dn.hi) >> 31) << 63);
       a.cv[e] = dn.hi == 0.0f ? __longlong_as_double(static_cast<long long>(inf))
-                              : ff2d(ff_div_fast(ff_make(1.0f), dn));
+                              : ff2d_add(ff_div_fast(ff_make(1.0f), dn));
     }
     if ((out & Q_BMOD) || a.cs) {
       const ff bm = ff_cell(load_rec(&c->bMod), A, B, AB);
       const ff BM = quick_two_sum(bm.hi, bm.lo);
-      if ((out & Q_BMOD) && a.bmod) a.bmod[e] = ff2d(BM);
+      if ((out & Q_BMOD) && a.bmod) a.bmod[e] = ff2d_add(BM);
       if (a.cs) {
         // sqrt(bmod / rho) by one rsqrt correction while b rho stays well
         // inside the float range (and positive); the FP64 form otherwise
         const ff R = d2ff(rho);
         const float pr = BM.hi * R.hi;
         if (BM.hi > 0.0f && R.hi > 0.0f && pr > 1e-30f && pr < 1e30f)
-          a.cs[e] = ff2d(ff_sqrt_ratio(BM, R));
+          a.cs[e] = ff2d_add(ff_sqrt_ratio(BM, R));
         else
           a.cs[e] = cs_fp64(ff2d(BM), rho);
       }

@@ -1,8 +1,9 @@
 // Device check of sgx_ff.cuh's conversions between float-float and double:
 // ff2d(hi, lo) against the FP64 sum (double)hi + (double)lo over seeded
 // pairs of every magnitude, unnormalised pairs, exact powers of two with a
-// low part of the opposite sign, zero and subnormal low parts; d2ff round
-// trips; the NQT log's integer core in 32-bit pieces (lg_nqt_int) against
+// low part of the opposite sign, zero and subnormal low parts; ff2d_add
+// bit for bit against the correctly rounded FP64 sum; d2ff round trips; the
+// NQT log's integer core in 32-bit pieces (lg_nqt_int) against
 // the reference's 64-bit formula (logs.hpp:188-200), bit for bit. Prints
 // "bad=<count>"; run by tests/test_gpu_ff.py.
 #include <cmath>
@@ -18,11 +19,12 @@
 #include "sgx_math.cuh"
 
 __global__ void conv(const float *hi, const float *lo, const double *d, double *out, double *rt,
-                     const int n) {
+                     double *add, const int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   out[i] = sgx::ff2d(sgx::ff_make(hi[i], lo[i]));
   rt[i] = sgx::ff2d(sgx::d2ff(d[i]));
+  add[i] = sgx::ff2d_add(sgx::ff_make(hi[i], lo[i]));
 }
 
 __global__ void lgint(const double *x, long long *out, const int n) {
@@ -57,25 +59,34 @@ int main() {
            (u(g) < 0 ? -1.0 : 1.0);
   }
   float *dh, *dl;
-  double *dd, *dout, *drt;
+  double *dd, *dout, *drt, *dadd;
   cudaMalloc(&dh, n * 4);
   cudaMalloc(&dl, n * 4);
   cudaMalloc(&dd, n * 8);
   cudaMalloc(&dout, n * 8);
   cudaMalloc(&drt, n * 8);
+  cudaMalloc(&dadd, n * 8);
   cudaMemcpy(dh, hi.data(), n * 4, cudaMemcpyHostToDevice);
   cudaMemcpy(dl, lo.data(), n * 4, cudaMemcpyHostToDevice);
   cudaMemcpy(dd, d.data(), n * 8, cudaMemcpyHostToDevice);
-  conv<<<(n + 255) / 256, 256>>>(dh, dl, dd, dout, drt, n);
-  std::vector<double> out(n), rt(n);
+  conv<<<(n + 255) / 256, 256>>>(dh, dl, dd, dout, drt, dadd, n);
+  std::vector<double> out(n), rt(n), add(n);
   if (cudaMemcpy(out.data(), dout, n * 8, cudaMemcpyDeviceToHost) != cudaSuccess ||
-      cudaMemcpy(rt.data(), drt, n * 8, cudaMemcpyDeviceToHost) != cudaSuccess) {
+      cudaMemcpy(rt.data(), drt, n * 8, cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(add.data(), dadd, n * 8, cudaMemcpyDeviceToHost) != cudaSuccess) {
     std::printf("cuda error\n");
     return 2;
   }
   long bad = 0;
   for (int i = 0; i < n; ++i) {
     const double want = double(hi[i]) + double(lo[i]);
+    // ff2d_add: the correctly rounded sum, a subnormal part counting as 0
+    const double want_add = (std::fpclassify(lo[i]) == FP_SUBNORMAL ? 0.0 : double(lo[i])) +
+                            (std::fpclassify(hi[i]) == FP_SUBNORMAL ? 0.0 : double(hi[i]));
+    if (std::memcmp(&want_add, &add[i], 8) != 0) {
+      if (bad < 5) std::printf("ff2d_add %a %a -> %a want %a\n", hi[i], lo[i], add[i], want_add);
+      ++bad;
+    }
     if (!(std::fabs(out[i] - want) <= ulp(want))) {
       if (bad < 5) std::printf("ff2d %a %a -> %a want %a\n", hi[i], lo[i], out[i], want);
       ++bad;

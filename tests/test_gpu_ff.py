@@ -2,7 +2,8 @@
 FP64 sums computed on the host (tests/cpp/ff_check.cu): ff2d within one ulp
 of (double)hi + (double)lo for pairs of every magnitude, unnormalised pairs,
 powers of two with a low part of the opposite sign, zero and subnormal low
-parts; d2ff -> ff2d round trips within 2^-47; and the NQT log's integer
+parts; ff2d_add bit for bit against the correctly rounded FP64 sum; d2ff ->
+ff2d round trips within 2^-47; and the NQT log's integer
 core in 32-bit pieces (lg_nqt_int, sgx_math.cuh) bit for bit against the
 reference's 64-bit formula."""
 import os
