@@ -245,6 +245,43 @@ def test_mixed_lookup_between_coarse_density_nodes(sgx):
         sgx.load().sgx_eos_finalize(C.byref(tab))
 
 
+def test_mixed_lookup_top_band(sgx):
+    """Roots in the band within 1e-8 of lTMax, below the table's top in sie:
+    the reference's regula falsi finds lT there, and its outputs take the
+    off-top forms (e0 + Cv (T - TMax) from the lTMax curves). The mixed path
+    leaves these to its FP64 pass; T, P, bmod and cs within the same bounds
+    as everywhere else."""
+    import ctypes as C
+    path, _ = stiffgas_table_path()
+    tab = sgx.spiner_eos(path, 1)
+    try:
+        rng = np.random.default_rng(21)
+        n = 1 << 14
+        rho_h = 10.0 ** rng.uniform(-3.0, 2.0, n)
+        # T within 1.1e-7 of TMax = 1e6: lT inside (1 - 1e-8) lTMax .. lTMax
+        T_in = 1e6 * (1.0 - rng.uniform(0.5, 0.9, n) * 1.2e-7)
+        rho = torch.as_tensor(rho_h, device="cuda")
+        sie = torch.zeros_like(rho)
+        sgx.fill_eos(tab, rho, torch.as_tensor(T_in, device="cuda"), sie, None, None, None,
+                     sgx.Q_SIE)
+        q = sgx.Q_TEMPERATURE | sgx.Q_PRESSURE | sgx.Q_BULK_MODULUS
+        out = {}
+        for prec in (sgx.PREC_FP64, sgx.PREC_MIXED):
+            Tt, P, bm, cs = (torch.zeros_like(rho) for _ in range(4))
+            sgx.fill_eos(tab, rho, Tt, sie, P, None, bm, q, cs=cs, precision=prec)
+            torch.cuda.synchronize()
+            out[prec] = [x.cpu().numpy() for x in (Tt, P, bm, cs)]
+        a, b = out[sgx.PREC_MIXED], out[sgx.PREC_FP64]
+        # the reference's roots lie in the band (T within 1.4e-7 of TMax)
+        assert (b[0] >= 1e6 * (1 - 1.4e-7)).all() and (b[0] <= 1e6 * (1 + 1e-12)).all()
+        check_T(a[0], b[0], bulk=False)
+        moved = fp64_moved(sgx, tab, rho, sie, q)
+        for k in (1, 2, 3):
+            assert within(a[k], b[k], moved[k]) <= 1.0, k
+    finally:
+        sgx.load().sgx_eos_finalize(C.byref(tab))
+
+
 def test_mixed_rejects_unsupported_calls(sgx):
     e = sgx.make_eos(1, (0.4, 0.718e7))
     x = torch.ones(4, dtype=torch.float64, device="cuda")
