@@ -492,15 +492,20 @@ __global__ void __launch_bounds__(LOOKUP_BLOCK, MINB)
           // (ff_div_fast's reciprocal needs |den| < 2^126)
           if (!ff_ok_bits(num) || !ff_ok_bits(den) || d_is_zero(den) || d_exp(den) > 120) break;
           A = ff_div_fast(d2ff(num), d2ff(den));
+          // a past the cell's upper node: a weight of 1 + 1e-9 has a float
+          // leading part of exactly 1, so the test takes the low part too
+          // (the lower cell's form extended past the node misses the root
+          // in the next cell by up to ~1e-9 of a cell)
+          const bool above = A.hi > 1.0f || (A.hi == 1.0f && A.lo > 0.0f);
           if (A.hi < 0.0f && i > 0) {
             --i;
             continue;
           }
-          if (A.hi > 1.0f && i < nc - 1) {
+          if (above && i < nc - 1) {
             ++i;
             continue;
           }
-          ok = A.hi >= 0.0f && A.hi <= 1.0f;
+          ok = A.hi >= 0.0f && !above;
           if (!ok) edge = (i == 0 && A.hi < -1e-6f) ? -1 : (i == nc - 1 && A.hi > 1.000001f) ? 1 : 0;
           break;
         }

@@ -245,6 +245,47 @@ def test_mixed_lookup_between_coarse_density_nodes(sgx):
         sgx.load().sgx_eos_finalize(C.byref(tab))
 
 
+def test_mixed_lookup_roots_just_above_T_nodes(sgx):
+    """Roots a hair above a T node: the lower cell's weight 1 + 1e-10 ..
+    5e-8 has a float leading part of exactly 1, yet the root is the next
+    cell's (the lower cell's form extended past the node misses it by up to
+    ~1e-10 relative in T on this table). T within the same bounds as
+    everywhere else."""
+    import ctypes as C
+    import refbind as rb
+    from sgx import sp5lite
+    path, _ = stiffgas_table_path()
+    grid = sp5lite.read(path)["datasets"]["/1/dependsLogRhoLogT/specific internal energy"][1]
+    nT, lTmin, lTmax = grid[0]
+    dlT = (lTmax - lTmin) / (nT - 1)
+    tab = sgx.spiner_eos(path, 1)
+    try:
+        rng = np.random.default_rng(33)
+        n = 1 << 14
+        k = rng.integers(1, nT - 2, n)
+        lT = lTmin + k * dlT + dlT * 10.0 ** rng.uniform(-10.0, np.log10(5e-8), n)
+        T_in = rb.port().nqt(1, lT)  # the reference's 10^lT (NQT)
+        rho_h = 10.0 ** rng.uniform(-3.5, 2.0, n)
+        rho = torch.as_tensor(rho_h, device="cuda")
+        sie = torch.zeros_like(rho)
+        sgx.fill_eos(tab, rho, torch.as_tensor(T_in, device="cuda"), sie, None, None, None,
+                     sgx.Q_SIE)
+        q = sgx.Q_TEMPERATURE | sgx.Q_PRESSURE | sgx.Q_BULK_MODULUS
+        out = {}
+        for prec in (sgx.PREC_FP64, sgx.PREC_MIXED):
+            Tt, P, bm, cs = (torch.zeros_like(rho) for _ in range(4))
+            sgx.fill_eos(tab, rho, Tt, sie, P, None, bm, q, cs=cs, precision=prec)
+            torch.cuda.synchronize()
+            out[prec] = [x.cpu().numpy() for x in (Tt, P, bm, cs)]
+        a, b = out[sgx.PREC_MIXED], out[sgx.PREC_FP64]
+        check_T(a[0], b[0], bulk=False)
+        moved = fp64_moved(sgx, tab, rho, sie, q)
+        for j in (1, 2, 3):
+            assert within(a[j], b[j], moved[j]) <= 1.0, j
+    finally:
+        sgx.load().sgx_eos_finalize(C.byref(tab))
+
+
 def test_mixed_lookup_top_band(sgx):
     """Roots in the band within 1e-8 of lTMax, below the table's top in sie:
     the reference's regula falsi finds lT there, and its outputs take the
