@@ -8,7 +8,7 @@
 // increases along T (checked per table at load) its root is unique and lies
 // in the one grid cell whose density-blended end values bracket the target.
 // On GB300 the FP64 pipe issues 1/64 of the FP32 pipe's operations, so the
-// fast path below keeps FP64 to about fifteen operations per query and does
+// fast path below keeps FP64 to about a dozen operations per query and does
 // the rest in float-float (sgx_ff.cuh, ~48 bits) and integer arithmetic:
 //   1. lRho: the NQT log (logs.hpp:188-200) in integers and two FP64
 //      scalings, the density cell and its weight b in FP64, all rounded as
@@ -32,20 +32,24 @@
 //   5. T = 10^lT by the NQT pow (logs.hpp:202-214) in integers: its
 //      argument lT log10(2)^-1 2^52 in fixed point from the cell position
 //      (nqt_arg), its square root in float-float; P, bmod and cs from their
-//      difference-form cells at (a, b), each rounded to double once.
+//      difference-form cells at (a, b), each rounded to double once by one
+//      FP64 addition of its exactly widened parts (ff2d_add).
 // Accuracy against the FP64 path: T within ~1e-13 relative plus the
 // conditioning of the root itself (about eps * sie / (dsie/dlT) where the
-// cold energy dominates), P, bmod and cs within 1e-10 of the larger of the
-// value and 1e-6 of the batch's largest magnitude.
+// cold energy dominates); P, bmod and cs within 1e-10 relative, or, where P
+// is a small difference of large table entries, within how far the FP64
+// value itself moves when sie changes by 1e-14 relative.
 //
 // Two kernels: spiner_fill_fast runs the steps above and marks, one bit per
 // element, what it leaves to spiner_fill_ref (sgx_fp64.cu, compiled without
 // FMA contraction, so those elements are bit-identical to the plain path),
-// which runs the reference's FP64 iteration on the marked elements only. Keeping that iteration out of
-// the fast kernel keeps its registers within the 4-blocks-per-SM budget
-// without spilling. Predicates on doubles are integer tests of the bit
-// patterns, so the FP64 pipe sees only the nine roundings that must be the
-// reference's.
+// which runs the reference's FP64 iteration on the marked elements only.
+// Keeping that iteration out of the fast kernel keeps its registers within
+// the 5-blocks-per-SM budget without spilling. Predicates on doubles are
+// integer tests of the bit patterns (read through an opaque move, so that
+// they are not turned into double compares), so the FP64 pipe sees the
+// eight roundings that must be the reference's, one int64 conversion and
+// the outputs' additions.
 // a mixed-precision path: bare models only (see sgx_dispatch.cuh)
 #define SGX_BARE_MODELS
 #include <mutex>
