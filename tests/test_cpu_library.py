@@ -225,3 +225,32 @@ def test_plan_and_derivative_argument_checks_without_gpu():
     assert lib.sgx_eos_eval(C.byref(g), 11, 4, C.c_void_p(16), C.c_void_p(16), C.c_void_p(16),
                             None, 0, None) == 5
 
+
+
+def test_tuning_knobs_hold_their_documented_ranges(lib):
+    """sgx_tune_set / sgx_tune_get (host only): every knob of sgx.h takes
+    the values of its documented range and refuses the ones outside it,
+    leaving the value unchanged; unknown knobs are refused."""
+    ranges = {L.TUNE_LOOKUP_BLOCKS_PER_SM: (4, 6), L.TUNE_LOOKUP_STAGE: (0, 2),
+              L.TUNE_L2_PERSIST: (0, 1), L.TUNE_HOST_FILL_STAGED: (0, 1),
+              L.TUNE_PTE_FP32_ITERS: (2, 64), L.TUNE_PTE_RETRY_ITERS: (4, 128),
+              L.TUNE_PTE_COUNT_ORDER: (0, 1), L.TUNE_PTE_MIXED_BLOCK: (32, 128),
+              L.TUNE_PTE_GROUP_MIN_N: (2, 7), L.TUNE_PTE_FP32_TOL: (3, 6),
+              L.TUNE_HELM_PASS1_STEPS: (0, 100), L.TUNE_HELM_MID_STEPS: (0, 100),
+              L.TUNE_HELM_MID2_STEPS: (0, 100)}
+    for knob, (lo, hi) in ranges.items():
+        v = C.c_int()
+        assert lib.sgx_tune_get(knob, C.byref(v)) == 0
+        keep = v.value
+        try:
+            for x in (lo, hi):
+                assert lib.sgx_tune_set(knob, x) == 0, (knob, x)
+                assert lib.sgx_tune_get(knob, C.byref(v)) == 0 and v.value == x
+            for x in (lo - 1, hi + 1):
+                assert lib.sgx_tune_set(knob, x) != 0, (knob, x)
+                assert lib.sgx_tune_get(knob, C.byref(v)) == 0 and v.value == hi
+        finally:
+            lib.sgx_tune_set(knob, keep)
+    for knob in (0, max(ranges) + 1, -1):
+        assert lib.sgx_tune_set(knob, 1) != 0
+        assert lib.sgx_tune_get(knob, C.byref(C.c_int())) != 0
