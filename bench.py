@@ -281,7 +281,7 @@ def bench_lookup(args, world, local, stream, out):
                           "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 32 * n,
                           "host_link_copy_ms": link_s * 1e3,
                           "frac_of_host_link": link_s / (dte / e2e_steps)}
-        if args.lookup_parts:
+        if args.lookup_parts or args.only == "all":
             # the marginal cost of each output: the mixed FillEos over the
             # same queries for subsets of the outputs
             qt, qp, qb = lib.Q_TEMPERATURE, lib.Q_PRESSURE, lib.Q_BULK_MODULUS
@@ -881,7 +881,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--lookup-parts", action="store_true",
                     help="also time the mixed lookup for output subsets (T; T+P; T+P+bmod; "
-                         "all + cs; T+cs), reported under lookup_parts")
+                         "all + cs; T+cs), reported under lookup_parts (always on in the "
+                         "full run)")
     ap.add_argument("--helm-caps", default=None,
                     help="pass-1, middle and second middle Newton step caps of the Helmholtz "
                          "inversion, e.g. 12,100,100 (sgx_tune_set; default: the library's)")
