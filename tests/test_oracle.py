@@ -378,3 +378,28 @@ def test_port_rhosie_matches_golden():
             np.testing.assert_array_equal(v, fx[f"fill_{tag}_{name}"])
     for w in range(6):
         np.testing.assert_array_equal(port.eos_bounds(d, w, fx["bounds_T"]), fx[f"bound{w}"])
+
+
+def test_bench_reference_arm_line():
+    """bench.py --impl reference (the CPU arm the benchmark's ratio is
+    taken against) on a small workload: exactly the requested steps, one
+    JSON line with the headline metric's keys, impl = reference, no host
+    copies."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference",
+                        "--queries", "65536", "--steps", "2", "--warmup", "3"],
+                       capture_output=True, text=True, timeout=600, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["steps"] == 2 and line["warmup"] == 3
+    for k in ("metric", "value", "unit", "n_gpus", "ms_per_step", "higher_is_better",
+              "scaling", "config", "cpu_baseline", "e2e"):
+        assert k in line, k
+    assert line["value"] > 0 and line["unit"] == "lookups/s"
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+    assert abs(line["ms_per_step"] * 1e-3 * line["value"] - 65536) <= 1e-6 * 65536
