@@ -336,12 +336,24 @@ int sgx_eos_fill(const sgx_eos *eos, int64_t n, double *rho, double *temp, doubl
                  double *press, double *cv, double *bmod, uint32_t output, double *lambda,
                  int lambda_stride, sgx_stream_t stream);
 /* FillEos with two extensions: cs (nullable) receives the sound speed
- * sqrt(bmod / rho), and precision selects the arithmetic. SGX_PREC_MIXED is
- * available for a tabulated rho-T EOS with (rho, sie) inputs and T among the
- * outputs: the bracketing table cell is found in FP32 and the root and every
- * output are computed in FP64 (results agree with SGX_PREC_FP64 to the
- * reference's root tolerance, 1e-14 in log10 T). No reference counterpart
- * beyond FillEos (eos/eos_base.hpp:503-531). */
+ * sqrt(bmod / rho), and precision selects the arithmetic. SGX_PREC_MIXED
+ * takes (rho, sie) inputs with T among the outputs, for three models:
+ *  - SpinerEOSDependsRhoT: the root and the outputs in float-float on the
+ *    FP32 pipe, the roundings the root is sensitive to (log10 rho, the
+ *    density weight) in FP64 as the reference takes them. Against
+ *    SGX_PREC_FP64: T within 1e-11 relative; P, bmod, cs within 1e-10, or,
+ *    where P is a small difference of large table entries, within how far
+ *    the FP64 value moves under a 1e-14 relative change of sie. Elements it
+ *    cannot answer (off the table's top, roots within 1e-8 of either end of
+ *    the T range) take the reference's FP64 iteration in the same call.
+ *  - SpinerEOSDependsRhoSie: the interpolations in float-float, within
+ *    about 1e-11 of the interpolant's magnitude.
+ *  - Helmholtz: the inversion's Newton iteration starts from an FP32 phase;
+ *    every output is the FP64 evaluation at the temperature found.
+ * The analytic models, and the tabulated ones with other inputs or outputs,
+ * return SGX_ERR_UNSUPPORTED; Helmholtz without T among the outputs runs its
+ * FP64 path. No reference counterpart beyond FillEos
+ * (eos/eos_base.hpp:503-531). */
 int sgx_eos_fill_ex(const sgx_eos *eos, int64_t n, double *rho, double *temp, double *sie,
                     double *press, double *cv, double *bmod, double *cs, uint32_t output,
                     double *lambda, int lambda_stride, int precision, sgx_stream_t stream);
