@@ -189,7 +189,10 @@ enum {
 
 /* Precision of the PTE / lookup arithmetic.
  * SGX_PREC_FP64: the plain path; follows the reference's iteration exactly.
- * SGX_PREC_MIXED: FP32 iterations followed by FP64 refinement. */
+ * SGX_PREC_MIXED: the PTE's Newton iteration in FP32 followed by FP64
+ *   residual correction to 1e-12 (cells it cannot finish take the FP64
+ *   iteration); the tabulated lookups in float-float; the Helmholtz
+ *   inversion from an FP32 phase (sgx_eos_fill_ex). */
 enum { SGX_PREC_FP64 = 0, SGX_PREC_MIXED = 1 };
 
 const char *sgx_version(void);
@@ -452,7 +455,8 @@ int sgx_mix_enforce_energies_sum(int nmat, int64_t ncell, const int32_t *eos_idx
  *      of the mixed-precision tabulated lookup (register budget 64/48/40).
  *  SGX_TUNE_LOOKUP_STAGE  0..2 (default 2): how that lookup stages the
  *      table's coarse search index in shared memory: 0 not at all, 1 by
- *      vector loads, 2 by one bulk copy (TMA).
+ *      vector loads, 2 by one bulk copy (TMA). Tables with the thermal bin
+ *      index (monotone thermal energy) do not use the coarse index.
  *  SGX_TUNE_L2_PERSIST  0/1 (default 0): mark the table's lines persisting
  *      in L2 (an access-policy window on the lookup's launch; sets aside
  *      L2 for persisting lines in this process's context).
