@@ -560,7 +560,7 @@ def bench_helm(args, world, stream, out):
         if args.helm_caps:
             for knob, v in zip((lib.TUNE_HELM_PASS1_STEPS, lib.TUNE_HELM_MID_STEPS,
                                 lib.TUNE_HELM_MID2_STEPS), args.helm_caps.split(",")):
-                lib.check(lib.load().sgx_tune_set(knob, int(v)))
+                lib.tune_set(knob, int(v))
         for prec, pname in ((lib.PREC_FP64, "fp64"), (lib.PREC_MIXED, "mixed")):
             T, P, B, CS = (torch.empty_like(rho) for _ in range(4))
 

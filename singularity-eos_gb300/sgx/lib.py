@@ -375,6 +375,19 @@ def pte_solve(solver, eos_list, eos_idx, vfrac_tot, sie_tot, rho, vfrac, sie, te
         stream_ptr(stream)))
 
 
+def tune_set(knob, value):
+    """sgx_tune_set: a process-wide launch or iteration knob (TUNE_*);
+    raises on a value outside the knob's range."""
+    check(load().sgx_tune_set(int(knob), int(value)))
+
+
+def tune_get(knob):
+    """sgx_tune_get: the knob's current value."""
+    v = C.c_int()
+    check(load().sgx_tune_get(int(knob), C.byref(v)))
+    return v.value
+
+
 def autotune_fill(eos, rho, temp, sie, press, cv, bmod, output, cs=None, lam=None,
                   lam_stride=0, reps=3, stream=None):
     """sgx_tune_autotune_fill on device tensors: returns the (blocks per SM,

@@ -254,3 +254,17 @@ def test_tuning_knobs_hold_their_documented_ranges(lib):
     for knob in (0, max(ranges) + 1, -1):
         assert lib.sgx_tune_set(knob, 1) != 0
         assert lib.sgx_tune_get(knob, C.byref(C.c_int())) != 0
+
+
+def test_python_tune_wrappers(lib):
+    """sgx.lib.tune_set / tune_get over the C calls: a value in range is
+    kept, one outside raises and leaves it."""
+    keep = L.tune_get(L.TUNE_HELM_MID_STEPS)
+    try:
+        L.tune_set(L.TUNE_HELM_MID_STEPS, 30)
+        assert L.tune_get(L.TUNE_HELM_MID_STEPS) == 30
+        with pytest.raises(RuntimeError):
+            L.tune_set(L.TUNE_HELM_MID_STEPS, 101)
+        assert L.tune_get(L.TUNE_HELM_MID_STEPS) == 30
+    finally:
+        L.tune_set(L.TUNE_HELM_MID_STEPS, keep)
